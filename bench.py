@@ -1,0 +1,387 @@
+"""Benchmark of the GB300 finite-volume hot path.
+
+Workload (the configuration the headline metric is quoted on): implicit heat
+transfer  ddt(T) - laplacian(k, T) = 0  on a 128^3 hex box (2,097,152 cells,
+6,242,304 internal faces) with interior vertices jittered by +-10% of the
+spacing (seed 12345), per-cell lognormal conductivity k (mu 0, sigma 0.5,
+same seed stream; face conductivity by linear interpolation), T0 = 300, a
+fixed 400 wall at x = 0, zero-gradient elsewhere, implicit Euler dt = 0.01.
+One step = CSR assembly of the system + FP64 Jacobi-PCG to a 1e-8 relative
+residual + boundary update, i.e. the reference's heatTransfer time step.
+
+metric: face-updates/s = (internal faces + active boundary faces) * steps / s.
+Inputs are synthetic (seeded), resident in HBM for `value`; `e2e` adds the
+host->device copy of T and the device->host copy of the result every step.
+Multi-GPU: independent replicas (the path has no data-parallel exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+HEAT = dict(n=128, jitter=0.1, seed=12345, dt=0.01, sigma=0.5, T0=300.0, Twall=400.0, rel_tol=1e-8)
+
+
+def heat_inputs(n):
+    from foamadapter_gb300 import mesh
+
+    hm = mesh.box(n, n, n, jitter=HEAT["jitter"], seed=HEAT["seed"])
+    rng = np.random.default_rng(HEAT["seed"])
+    k = np.exp(HEAT["sigma"] * rng.standard_normal(hm.n))
+    return hm, k
+
+
+def active_bfaces(hm):
+    s = hm.patch_slice("xmin")
+    return s.stop - s.start
+
+
+def alg_bytes(hm):
+    n, nnz, nif = hm.n, hm.nnz, hm.nif
+    nbfa = active_bfaces(hm)
+    return {
+        "pcg_spmv": 12 * nnz + 4 * (n + 1) + 16 * n,
+        "pcg_update": 56 * n,
+        "pcg_dir": 32 * n,
+        "pcg_iteration": 12 * nnz + 4 * (n + 1) + 104 * n,
+        "assembly": 8 * nnz + 24 * nif + 28 * n + 28 * nbfa,
+    }
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = [r.split(",") for r in (self.out or "").strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows]
+        mx = float(rows[0][2])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_gpu(args, rank, world):
+    import torch
+
+    from foamadapter_gb300 import abi, neon
+    from foamadapter_gb300.mesh import DeviceMesh
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    n = args.n
+    hm, k = heat_inputs(n)
+    dm = DeviceMesh(hm)
+    nbfa = active_bfaces(hm)
+    face_updates = hm.nif + nbfa
+    bcs = [("fixedValue", HEAT["Twall"])] + [("zeroGradient", 0.0)] * (hm.npatch - 1)
+    T = neon.VolumeField(dm, np.full(hm.n, HEAT["T0"]), bcs)
+    kf = neon.VolumeField(dm, k, [("zeroGradient", 0.0)] * hm.npatch)
+    gamma = neon.SurfaceInterpolation(dm, "linear").interpolate(kf)
+    T_old = T.internal.clone()
+    ls = neon.LinearSystem(dm)
+    terms = [neon.ddt(T_old), neon.laplacian(gamma, -1.0)]
+    tarr = (abi.Term * 2)(*[t.struct() for t in terms])
+    bc = T.bc_struct()
+    L = abi.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    cfg = abi.SolverCfg(HEAT["rel_tol"], 0.0, 1000, abi.PREC_FP64, 0.0, 0, 0)
+    stats_dev = torch.zeros((max(args.steps, args.warmup) + 8) * 8, dtype=torch.int32, device="cuda")
+    SZ = C.sizeof(abi.SolverStats)
+
+    def step(i, cfg=cfg):
+        T_old.copy_(T.internal)
+        abi.check(L.fvgb_assemble(ls.handle, tarr, 2, HEAT["dt"], C.byref(bc), abi.ptr(T.boundary), stream))
+        abi.check(L.fvgb_solve_async(ls.handle, abi.ptr(T.internal), C.byref(cfg),
+                                     stats_dev.data_ptr() + i * SZ, stream))
+        abi.check(L.fvgb_bc_correct(dm.handle, 1, C.byref(bc), abi.ptr(T.internal), abi.ptr(T.boundary),
+                                    stream))
+
+    def read_stats(count):
+        raw = stats_dev[: count * SZ // 4].cpu().numpy().tobytes()
+        return [abi.SolverStats.from_buffer_copy(raw[i * SZ:(i + 1) * SZ]) for i in range(count)]
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    warm_stats = read_stats(args.warmup)
+    # ---- device-resident timed region
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ev0.record()
+        for i in range(args.steps):
+            step(i)
+        ev1.record()
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    stats = read_stats(args.steps)
+    assert all(s.status == abi.OK for s in stats), [s.status for s in stats]
+    iters = [s.num_iter for s in stats]
+    # ---- end to end through the ABI with host buffers (pinned), copies inside the region
+    h_in = torch.empty(hm.n, dtype=torch.float64, pin_memory=True)
+    h_out = torch.empty(hm.n, dtype=torch.float64, pin_memory=True)
+    h_in.copy_(T.internal.cpu())
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.steps):
+        T.internal.copy_(h_in, non_blocking=True)
+        step(i)
+        h_out.copy_(T.internal, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    e2e_iters = [s.num_iter for s in read_stats(args.steps)]
+    # ---- per-kernel times for the roofline (outside the graph, same system)
+    kt = (C.c_double * 4)()
+    abi.check(L.fvgb_solve_kernel_times(ls.handle, abi.ptr(T.internal), 30, kt, stream))
+    # ---- FP64 vs mixed-precision solve of one step's system
+    mixed = compare_precisions(torch, abi, L, ls, T, T_old, tarr, bc, dm, hm, stream)
+    result = dict(ms=ms, iters=iters, e2e_ms=e2e_ms, e2e_iters=e2e_iters, kt=list(kt), clocks=clk.summary(),
+                  mixed=mixed, face_updates=face_updates, warm_iters=[s.num_iter for s in warm_stats],
+                  mesh_bytes=dm.device_bytes())
+    return hm, result
+
+
+def compare_precisions(torch, abi, L, ls, T, T_old, tarr, bc, dm, hm, stream):
+    """Solve one step's system both ways from the same start; time, iterations, error."""
+    T_old.copy_(T.internal)
+    abi.check(L.fvgb_assemble(ls.handle, tarr, 2, HEAT["dt"], C.byref(bc), abi.ptr(T.boundary), stream))
+    out = {}
+    sols = {}
+    for name, prec, inner in (("fp64", abi.PREC_FP64, 0.0), ("mixed", abi.PREC_MIXED_IR, 1e-3)):
+        cfg = abi.SolverCfg(HEAT["rel_tol"], 0.0, 4000, prec, inner, 1000, 50)
+        best = None
+        for rep in range(3):
+            x = T_old.clone()
+            st = abi.SolverStats()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            abi.check(L.fvgb_solve(ls.handle, abi.ptr(x), C.byref(cfg), C.byref(st), stream))
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1)
+            best = t if best is None else min(best, t)
+        sols[name] = x
+        # true FP64 residual of the returned solution
+        r = torch.empty_like(x)
+        abi.check(L.fvgb_apply_operator(ls.handle, abi.ptr(x), abi.ptr(r), stream))
+        out[name] = {"ms": best, "iters": st.num_iter, "outer": st.num_outer,
+                     "rel_residual": float(torch.linalg.vector_norm(r).item() / st.init_res_norm)}
+    d = (sols["mixed"] - sols["fp64"]).abs()
+    out["speedup"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    out["max_abs_err_vs_fp64"] = float(d.max().item())
+    out["l2_rel_err_vs_fp64"] = float((torch.linalg.vector_norm(sols["mixed"] - sols["fp64"]) /
+                                       torch.linalg.vector_norm(sols["fp64"])).item())
+    return out
+
+
+# ----------------------------------------------------------------------------- CPU (oracle)
+def cpu_steps(hm, k, nsteps, threads):
+    """The same heat-transfer steps on the host cores with the CPU oracle."""
+    from oracle import build_oracle
+    from oracle.pyoracle import Oracle, get_threads, set_threads
+
+    build_oracle.build()
+    if threads:
+        set_threads(threads)
+    o = Oracle(hm)
+    o.csr()
+    nbf = hm.nbf
+    kb = np.ascontiguousarray(k[hm.bcells])
+    gamma = o.interp_linear(1, k, kb)
+    types = np.asarray([1] + [2] * (hm.npatch - 1), np.int32)
+    ref = np.zeros(nbf)
+    ref[hm.patch_slice("xmin")] = HEAT["Twall"]
+    T = np.full(hm.n, HEAT["T0"])
+    Tb = np.zeros(nbf)
+    o.bc_correct(1, types, ref, T, Tb)
+    times, iters = [], []
+    for _ in range(nsteps):
+        t0 = time.perf_counter()
+        told = T.copy()
+        terms = [(0, 0, 1.0, told, None), (1, 0, -1.0, None, gamma)]
+        v, r, _, _ = o.assemble(1, terms, HEAT["dt"], types, ref, Tb)
+        st = o.solve(v, r, T, rel_tol=HEAT["rel_tol"], max_iter=1000)
+        o.bc_correct(1, types, ref, T, Tb)
+        times.append(time.perf_counter() - t0)
+        iters.append(st.num_iter)
+    return times, iters, get_threads()
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle port of the reference's CPU path, all host threads."""
+    if rank != 0:
+        return
+    hm, k = heat_inputs(args.n)
+    nbfa = active_bfaces(hm)
+    w = min(args.warmup, 1)
+    ksteps = max(1, min(args.steps, args.ref_max_steps))
+    times, iters, threads = cpu_steps(hm, k, w + ksteps, os.cpu_count())
+    t = sum(times[w:])
+    val = (hm.nif + nbfa) * ksteps / t
+    line = {
+        "impl": "reference", "metric": "face-updates/s", "value": val, "unit": "face-updates/s",
+        "n_gpus": world, "steps": ksteps, "warmup": w, "ms_per_step": 1e3 * t / ksteps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(args),
+        "cpu_baseline": {"value": val, "unit": "face-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{ksteps} implicit steps of the 128^3 case (assembly + FP64 Jacobi-PCG "
+                                   f"to 1e-8, iterations {iters[w:]}), OpenMP x{threads}"},
+        "e2e": {"value": val, "unit": "face-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def workload_config(args):
+    return {"workload": f"implicit heat transfer {args.n}^3 jittered hex box, FP64 Jacobi-PCG to 1e-8",
+            "cells": args.n ** 3, "dt": HEAT["dt"], "parallelism": "replicas",
+            "l2": "working set > 129 MB L2 (matrix 175 MB + vectors), no flush needed"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=HEAT["n"])
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--ref-max-steps", type=int, default=8)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    from foamadapter_gb300 import _build
+
+    if rank == 0:
+        _build.build()
+    if world > 1:
+        torch.distributed.barrier()
+    hm, r = run_gpu(args, rank, world)
+    ms = r["ms"]
+    if world > 1:
+        t = torch.tensor([ms, r["e2e_ms"]], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, e2e_ms = t.tolist()
+    else:
+        e2e_ms = r["e2e_ms"]
+    if rank != 0:
+        return
+    fu = r["face_updates"]
+    value = fu * args.steps * world / (ms / 1e3)
+    e2e_value = fu * args.steps * world / (e2e_ms / 1e3)
+    peak, peak_kind = load_peaks()
+    ab = alg_bytes(hm)
+    t_spmv = r["kt"][0] * 1e-3
+    achieved = ab["pcg_spmv"] / t_spmv / 1e9
+    traffic = read_traffic("pcg_spmv")
+    launches = sum(5 + 3 * it for it in r["iters"])
+    line = {
+        "metric": "face-updates/s", "value": value, "unit": "face-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(args),
+        "roofline": {"bound": "hbm", "kernel": "k_pcg_spmv (SpMV + p.Ap)", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": traffic, "alg_bytes_per_launch": ab["pcg_spmv"],
+                     "kernel_ms": {"spmv": r["kt"][0], "update": r["kt"][1], "dir": r["kt"][2]},
+                     "iteration_GBps": ab["pcg_iteration"] / (sum(r["kt"][:3]) * 1e-3) / 1e9},
+        "e2e": {"value": e2e_value, "unit": "face-updates/s", "h2d_bytes_per_step": 8 * hm.n,
+                "d2h_bytes_per_step": 8 * hm.n},
+        "gpu_launches": launches,
+        "clocks": r["clocks"],
+        "pcg_iterations_per_step": r["iters"],
+        "mixed_precision": r["mixed"],
+    }
+    if not args.no_cpu and world == 1:
+        from oracle.pyoracle import set_threads  # noqa: F401
+
+        hm2, k = heat_inputs(args.n)
+        times, iters, threads = cpu_steps(hm2, k, args.cpu_steps, os.cpu_count())
+        t = sum(times)
+        line["cpu_baseline"] = {"value": fu * len(times) / t, "unit": "face-updates/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"{len(times)} implicit step(s) of the same {args.n}^3 case "
+                                          f"(assembly + FP64 Jacobi-PCG to 1e-8, {iters} iterations) on the "
+                                          f"CPU oracle, OpenMP x{threads}"}
+    print(json.dumps(line))
+
+
+def read_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "ncu_summary.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get(kernel, {}).get("dram_bytes_per_launch")
+        except (ValueError, AttributeError):
+            return None
+    return None
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,360 @@
+// Explicit finite-volume operators: surface interpolation (linear, upwind),
+// Gauss-Green div / grad / laplacian, uncorrected snGrad and the fused
+// upwind-advection forward-Euler step.
+//
+// The reference's Serial executor scatters face contributions into owner (+)
+// and neighbour (-) cells in ascending face order.  Here one thread owns one
+// cell and walks that cell's faces in the same ascending order through the
+// gather list, so every cell sees the same sequence of IEEE operations and the
+// result is bit-identical to the Serial face loop, with no atomics.  This file
+// is compiled with -fmad=false so no multiply-add is contracted.
+#include "internal.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int gwidth(const MeshView& m, int slice) {
+    return (__ldg(&m.g_ptr[slice + 1]) - __ldg(&m.g_ptr[slice])) >> 5;
+}
+
+// ---------------------------------------------------------------- interpolation
+template <int NC>
+__global__ void k_interp_linear(MeshView m, const double* __restrict__ src,
+                                const double* __restrict__ src_b, double* __restrict__ dst) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < m.nif) {
+        int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
+        double w = __ldg(&m.w[f]);
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            double sN = __ldg(&src[N * NC + k]);
+            dst[f * NC + k] = w * (__ldg(&src[P * NC + k]) - sN) + sN;
+        }
+    } else if (f < m.nif + m.nbf) {
+        int b = f - m.nif;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) dst[f * NC + k] = __ldg(&src_b[b * NC + k]);
+    }
+}
+
+template <int NC>
+__global__ void k_interp_upwind(MeshView m, const double* __restrict__ flux,
+                                const double* __restrict__ src, const double* __restrict__ src_b,
+                                double* __restrict__ dst) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < m.nif) {
+        int c = __ldg(&flux[f]) >= 0.0 ? __ldg(&m.own[f]) : __ldg(&m.nei[f]);
+#pragma unroll
+        for (int k = 0; k < NC; ++k) dst[f * NC + k] = __ldg(&src[c * NC + k]);
+    } else if (f < m.nif + m.nbf) {
+        int b = f - m.nif;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) dst[f * NC + k] = __ldg(&src_b[b * NC + k]);
+    }
+}
+
+// ------------------------------------------------------------------------ div
+// face value seen from cell c across internal face f: owner-side formulas of
+// the reference with (P, N) = (owner, neighbour).
+template <int NC, int SCHEME>
+__device__ __forceinline__ void div_cell(const MeshView& m, int c, const double* __restrict__ flux,
+                                         const double* __restrict__ phi,
+                                         const double* __restrict__ phi_b, double* s) {
+    const int slice = c >> 5, lane = c & 31;
+    const int base = __ldg(&m.g_ptr[slice]);
+    const int width = gwidth(m, slice);
+    double Tc[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        Tc[k] = __ldg(&phi[c * NC + k]);
+        s[k] = 0.0;
+    }
+    for (int j = 0; j < width; ++j) {
+        const int pos = base + j * 32 + lane;
+        const int code = __ldg(&m.g_code[pos]);
+        if (code == FVGB_PAD) break;
+        if (code >= m.nif) {  // boundary face: value from the boundary field
+            const int b = code - m.nif;
+            const double F = __ldg(&flux[code]);
+#pragma unroll
+            for (int k = 0; k < NC; ++k) s[k] = s[k] + F * __ldg(&phi_b[b * NC + k]);
+            continue;
+        }
+        const bool isOwner = code >= 0;
+        const int f = isOwner ? code : -code - 1;
+        const int o = __ldg(&m.g_other[pos]);
+        const double F = __ldg(&flux[f]);
+        double wf = 0.0;
+        if (SCHEME == FVGB_SCHEME_LINEAR) wf = __ldg(&m.w[f]);
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const double To = __ldg(&phi[o * NC + k]);
+            const double Town = isOwner ? Tc[k] : To;
+            const double Tnei = isOwner ? To : Tc[k];
+            double tf;
+            if (SCHEME == FVGB_SCHEME_UPWIND) tf = F >= 0.0 ? Town : Tnei;
+            else tf = wf * (Town - Tnei) + Tnei;
+            const double fl = F * tf;
+            s[k] = isOwner ? s[k] + fl : s[k] - fl;
+        }
+    }
+}
+
+template <int NC, int SCHEME>
+__global__ void __launch_bounds__(kThreads)
+    k_div(MeshView m, const double* __restrict__ flux, const double* __restrict__ phi,
+          const double* __restrict__ phi_b, double coeff, int unit, double* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n) return;
+    double s[NC];
+    div_cell<NC, SCHEME>(m, c, flux, phi, phi_b, s);
+    const double sc = unit ? __ldg(&m.invV[c]) : coeff / __ldg(&m.V[c]);
+#pragma unroll
+    for (int k = 0; k < NC; ++k) out[c * NC + k] = out[c * NC + k] + s[k] * sc;
+}
+
+// Fused forward-Euler upwind advection step + boundary correction.
+__global__ void __launch_bounds__(kThreads)
+    k_advect_euler(MeshView m, PatchTable pt, const double* __restrict__ flux,
+                   const double* __restrict__ Told, const double* __restrict__ Told_b, double dt,
+                   const double* __restrict__ ref, double* __restrict__ Tnew,
+                   double* __restrict__ Tnew_b) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n) return;
+    double s[1];
+    div_cell<1, FVGB_SCHEME_UPWIND>(m, c, flux, Told, Told_b, s);
+    const double dv = 0.0 + s[0] * __ldg(&m.invV[c]);
+    const double tn = __ldg(&Told[c]) - dt * dv;
+    Tnew[c] = tn;
+    // boundary faces of this cell (they follow its internal faces in the list)
+    const int slice = c >> 5, lane = c & 31;
+    const int base = __ldg(&m.g_ptr[slice]);
+    const int width = gwidth(m, slice);
+    for (int j = width - 1; j >= 0; --j) {
+        const int code = __ldg(&m.g_code[base + j * 32 + lane]);
+        if (code == FVGB_PAD) continue;
+        if (code < m.nif) break;
+        const int b = code - m.nif;
+        const int t = pt.type[__ldg(&m.bpatch[b])];
+        double v = __ldg(&Told_b[b]);
+        if (t == FVGB_BC_FIXED_VALUE) v = __ldg(&ref[b]);
+        else if (t == FVGB_BC_FIXED_GRADIENT) v = tn + __ldg(&ref[b]) / __ldg(&m.bdelta[b]);
+        Tnew_b[b] = v;
+    }
+}
+
+// ----------------------------------------------------------------------- grad
+__global__ void __launch_bounds__(kThreads)
+    k_grad(MeshView m, const double* __restrict__ phi, const double* __restrict__ phi_b,
+           double coeff, int unit, double* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n) return;
+    const int slice = c >> 5, lane = c & 31;
+    const int base = __ldg(&m.g_ptr[slice]);
+    const int width = gwidth(m, slice);
+    const double Tc = __ldg(&phi[c]);
+    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+    for (int j = 0; j < width; ++j) {
+        const int pos = base + j * 32 + lane;
+        const int code = __ldg(&m.g_code[pos]);
+        if (code == FVGB_PAD) break;
+        if (code >= m.nif) {
+            const int b = code - m.nif;
+            const double tb = __ldg(&phi_b[b]);
+            g0 = g0 + __ldg(&m.bSf[3 * b]) * tb;
+            g1 = g1 + __ldg(&m.bSf[3 * b + 1]) * tb;
+            g2 = g2 + __ldg(&m.bSf[3 * b + 2]) * tb;
+            continue;
+        }
+        const bool isOwner = code >= 0;
+        const int f = isOwner ? code : -code - 1;
+        const double To = __ldg(&phi[__ldg(&m.g_other[pos])]);
+        const double Town = isOwner ? Tc : To;
+        const double Tnei = isOwner ? To : Tc;
+        const double tf = __ldg(&m.w[f]) * (Town - Tnei) + Tnei;
+        const double v0 = __ldg(&m.Sf[3 * f]) * tf;
+        const double v1 = __ldg(&m.Sf[3 * f + 1]) * tf;
+        const double v2 = __ldg(&m.Sf[3 * f + 2]) * tf;
+        if (isOwner) {
+            g0 = g0 + v0;
+            g1 = g1 + v1;
+            g2 = g2 + v2;
+        } else {
+            g0 = g0 - v0;
+            g1 = g1 - v1;
+            g2 = g2 - v2;
+        }
+    }
+    const double sc = unit ? __ldg(&m.invV[c]) : coeff / __ldg(&m.V[c]);
+    out[3 * c] = out[3 * c] + g0 * sc;
+    out[3 * c + 1] = out[3 * c + 1] + g1 * sc;
+    out[3 * c + 2] = out[3 * c + 2] + g2 * sc;
+}
+
+// ------------------------------------------------------------------ laplacian
+template <int NC>
+__global__ void __launch_bounds__(kThreads)
+    k_lap(MeshView m, const double* __restrict__ gamma, const double* __restrict__ phi,
+          const double* __restrict__ phi_b, double coeff, int unit, double* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n) return;
+    const int slice = c >> 5, lane = c & 31;
+    const int base = __ldg(&m.g_ptr[slice]);
+    const int width = gwidth(m, slice);
+    double Tc[NC], s[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        Tc[k] = __ldg(&phi[c * NC + k]);
+        s[k] = 0.0;
+    }
+    for (int j = 0; j < width; ++j) {
+        const int pos = base + j * 32 + lane;
+        const int code = __ldg(&m.g_code[pos]);
+        if (code == FVGB_PAD) break;
+        if (code >= m.nif) {
+            const int b = code - m.nif;
+            const double g = __ldg(&gamma[code]) * __ldg(&m.bgeo[b]);
+#pragma unroll
+            for (int k = 0; k < NC; ++k) s[k] = s[k] + g * (__ldg(&phi_b[b * NC + k]) - Tc[k]);
+            continue;
+        }
+        const bool isOwner = code >= 0;
+        const int f = isOwner ? code : -code - 1;
+        const int o = __ldg(&m.g_other[pos]);
+        const double g = __ldg(&gamma[f]) * __ldg(&m.geo[f]);
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const double To = __ldg(&phi[o * NC + k]);
+            // face flux is g*(T_nei - T_own); the owner adds it, the neighbour subtracts it
+            if (isOwner) s[k] = s[k] + g * (To - Tc[k]);
+            else s[k] = s[k] - g * (Tc[k] - To);
+        }
+    }
+    const double sc = unit ? __ldg(&m.invV[c]) : coeff / __ldg(&m.V[c]);
+#pragma unroll
+    for (int k = 0; k < NC; ++k) out[c * NC + k] = out[c * NC + k] + s[k] * sc;
+}
+
+// --------------------------------------------------------------------- snGrad
+__global__ void k_sngrad(MeshView m, const double* __restrict__ phi,
+                         const double* __restrict__ phi_b, double* __restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < m.nif) {
+        out[f] = __ldg(&m.delta[f]) * (__ldg(&phi[__ldg(&m.nei[f])]) - __ldg(&phi[__ldg(&m.own[f])]));
+    } else if (f < m.nif + m.nbf) {
+        const int b = f - m.nif;
+        out[f] = __ldg(&m.bdelta[b]) * (__ldg(&phi_b[b]) - __ldg(&phi[__ldg(&m.bcells[b])]));
+    }
+}
+
+}  // namespace
+
+// ==================================================================== C ABI
+#define CHECK_MESH_NC(m, nc, name)                                                         \
+    FVGB_CHECK_ARG(m, name ": null mesh");                                                 \
+    FVGB_CHECK_ARG((nc) == 1 || (nc) == 3, name ": ncomp must be 1 or 3")
+
+extern "C" fvgb_status fvgb_interp_linear(const fvgb_mesh* m, int32_t nc, const double* src,
+                                          const double* src_b, double* dst, fvgb_stream stream) {
+    CHECK_MESH_NC(m, nc, "fvgb_interp_linear");
+    FVGB_CHECK_ARG(src && dst && (src_b || m->v.nbf == 0), "fvgb_interp_linear: null field");
+    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+    if (nf == 0) return FVGB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (nc == 1) k_interp_linear<1><<<grid_for(nf, kThreads), kThreads, 0, s>>>(m->v, src, src_b, dst);
+    else k_interp_linear<3><<<grid_for(nf, kThreads), kThreads, 0, s>>>(m->v, src, src_b, dst);
+    FVGB_LAUNCH_CHECK("fvgb_interp_linear");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_interp_upwind(const fvgb_mesh* m, int32_t nc, const double* flux,
+                                          const double* src, const double* src_b, double* dst,
+                                          fvgb_stream stream) {
+    CHECK_MESH_NC(m, nc, "fvgb_interp_upwind");
+    FVGB_CHECK_ARG(flux && src && dst && (src_b || m->v.nbf == 0), "fvgb_interp_upwind: null field");
+    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+    if (nf == 0) return FVGB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (nc == 1)
+        k_interp_upwind<1><<<grid_for(nf, kThreads), kThreads, 0, s>>>(m->v, flux, src, src_b, dst);
+    else
+        k_interp_upwind<3><<<grid_for(nf, kThreads), kThreads, 0, s>>>(m->v, flux, src, src_b, dst);
+    FVGB_LAUNCH_CHECK("fvgb_interp_upwind");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_div_explicit(const fvgb_mesh* m, int32_t scheme, int32_t nc,
+                                         const double* flux, const double* phi,
+                                         const double* phi_b, double coeff, double* out,
+                                         fvgb_stream stream) {
+    CHECK_MESH_NC(m, nc, "fvgb_div_explicit");
+    FVGB_CHECK_ARG(scheme == FVGB_SCHEME_LINEAR || scheme == FVGB_SCHEME_UPWIND,
+                   "fvgb_div_explicit: unknown scheme");
+    FVGB_CHECK_ARG(flux && phi && out && (phi_b || m->v.nbf == 0), "fvgb_div_explicit: null field");
+    const int unit = coeff == 1.0;
+    cudaStream_t s = (cudaStream_t)stream;
+    const unsigned g = grid_for(m->v.n, kThreads);
+    if (nc == 1 && scheme == FVGB_SCHEME_UPWIND)
+        k_div<1, FVGB_SCHEME_UPWIND><<<g, kThreads, 0, s>>>(m->v, flux, phi, phi_b, coeff, unit, out);
+    else if (nc == 1)
+        k_div<1, FVGB_SCHEME_LINEAR><<<g, kThreads, 0, s>>>(m->v, flux, phi, phi_b, coeff, unit, out);
+    else if (scheme == FVGB_SCHEME_UPWIND)
+        k_div<3, FVGB_SCHEME_UPWIND><<<g, kThreads, 0, s>>>(m->v, flux, phi, phi_b, coeff, unit, out);
+    else
+        k_div<3, FVGB_SCHEME_LINEAR><<<g, kThreads, 0, s>>>(m->v, flux, phi, phi_b, coeff, unit, out);
+    FVGB_LAUNCH_CHECK("fvgb_div_explicit");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_grad(const fvgb_mesh* m, const double* phi, const double* phi_b,
+                                 double coeff, double* out, fvgb_stream stream) {
+    FVGB_CHECK_ARG(m, "fvgb_grad: null mesh");
+    FVGB_CHECK_ARG(phi && out && (phi_b || m->v.nbf == 0), "fvgb_grad: null field");
+    k_grad<<<grid_for(m->v.n, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
+        m->v, phi, phi_b, coeff, coeff == 1.0, out);
+    FVGB_LAUNCH_CHECK("fvgb_grad");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_laplacian_explicit(const fvgb_mesh* m, int32_t nc, const double* gamma,
+                                               const double* phi, const double* phi_b,
+                                               double coeff, double* out, fvgb_stream stream) {
+    CHECK_MESH_NC(m, nc, "fvgb_laplacian_explicit");
+    FVGB_CHECK_ARG(gamma && phi && out && (phi_b || m->v.nbf == 0),
+                   "fvgb_laplacian_explicit: null field");
+    cudaStream_t s = (cudaStream_t)stream;
+    const unsigned g = grid_for(m->v.n, kThreads);
+    if (nc == 1) k_lap<1><<<g, kThreads, 0, s>>>(m->v, gamma, phi, phi_b, coeff, coeff == 1.0, out);
+    else k_lap<3><<<g, kThreads, 0, s>>>(m->v, gamma, phi, phi_b, coeff, coeff == 1.0, out);
+    FVGB_LAUNCH_CHECK("fvgb_laplacian_explicit");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_sngrad(const fvgb_mesh* m, const double* phi, const double* phi_b,
+                                   double* out, fvgb_stream stream) {
+    FVGB_CHECK_ARG(m, "fvgb_sngrad: null mesh");
+    FVGB_CHECK_ARG(phi && out && (phi_b || m->v.nbf == 0), "fvgb_sngrad: null field");
+    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+    if (nf == 0) return FVGB_OK;
+    k_sngrad<<<grid_for(nf, kThreads), kThreads, 0, (cudaStream_t)stream>>>(m->v, phi, phi_b, out);
+    FVGB_LAUNCH_CHECK("fvgb_sngrad");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_advect_euler_step(const fvgb_mesh* m, const double* flux,
+                                              const double* T_old, const double* T_old_b,
+                                              double dt, const fvgb_bc* bc, double* T_new,
+                                              double* T_new_b, fvgb_stream stream) {
+    FVGB_CHECK_ARG(m && bc, "fvgb_advect_euler_step: null argument");
+    FVGB_CHECK_ARG(flux && T_old && T_new && ((T_old_b && T_new_b) || m->v.nbf == 0),
+                   "fvgb_advect_euler_step: null field");
+    FVGB_CHECK_ARG(T_new != T_old, "fvgb_advect_euler_step: T_new must not alias T_old");
+    PatchTable pt;
+    FVGB_CHECK_ARG(make_patch_table(m, bc->patch_type, &pt), "fvgb_advect_euler_step: bad patch types");
+    FVGB_CHECK_ARG(bc->ref || !patch_table_needs_ref(pt), "fvgb_advect_euler_step: ref is null");
+    k_advect_euler<<<grid_for(m->v.n, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
+        m->v, pt, flux, T_old, T_old_b, dt, bc->ref, T_new, T_new_b);
+    FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
+    return FVGB_OK;
+}

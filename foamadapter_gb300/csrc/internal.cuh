@@ -1,0 +1,145 @@
+// Internal definitions of libfvgb: the device-resident mesh and linear-system
+// handles and the index layouts the kernels read.
+//
+// Layouts (all device arrays):
+//  * Gather lists: for every cell the faces it touches, in ascending face
+//    index (internal faces, then its boundary faces), stored sliced-ELL with
+//    32-cell slices, column-major inside a slice: entry k of cell c sits at
+//    g_ptr[c/32] + 32*k + c%32.  g_code: 0 <= code < nif: c owns internal face
+//    `code`; code < 0: c is the neighbour of face -code-1; code >= nif: boundary
+//    face code-nif; FVGB_PAD: padding (only at the end of a row).  g_other: the
+//    cell across an internal face.
+//  * Matrix: the CSR pattern of NeoN (row = [lower, diagonal, upper] in column
+//    order) stored sliced-ELL the same way: m_ptr, m_col, values.  m_code per
+//    slot: code >= 0: a_PN with P the owner of face code; code <= -2: a_NP with
+//    P the neighbour of face -code-2; -1: diagonal; FVGB_PAD: padding (value 0,
+//    column = row).  diag_pos / own_pos / nei_pos give the slot of a_PP, a_PN
+//    (row owner) and a_NP (row neighbour).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "fvgb.h"
+#include "fvgb_host_common.h"
+
+#define FVGB_PAD INT32_MIN
+#define FVGB_MAX_PATCHES 256
+#define FVGB_MAX_TERMS 8
+
+constexpr int kSlice = 32;
+
+struct MeshView {
+    int32_t n, nif, nbf, npatch;
+    const double* V;
+    const double* invV;
+    const int32_t* own;
+    const int32_t* nei;
+    const double* Sf;
+    const double* magSf;
+    const double* w;
+    const double* delta;
+    const double* geo;       // |Sf| * delta
+    const int32_t* bcells;
+    const double* bSf;
+    const double* bmagSf;
+    const double* bdelta;
+    const double* bgeo;      // |Sf_b| * delta_b
+    const int32_t* bpatch;   // patch index of every boundary face
+    const int32_t* g_ptr;
+    const int32_t* g_code;
+    const int32_t* g_other;
+    const int32_t* m_ptr;
+    const int32_t* m_col;
+    const int32_t* m_code;
+    const int32_t* diag_pos;
+    const int32_t* own_pos;
+    const int32_t* nei_pos;
+};
+
+struct fvgb_mesh {
+    MeshView v{};
+    int32_t nnz = 0;
+    int32_t nslices = 0;
+    int64_t m_len = 0, g_len = 0;
+    int32_t* csr_pos = nullptr;  // [nnz] slot of CSR entry j
+    std::vector<int32_t> h_patch_offs;
+    std::vector<int32_t> h_row_offs, h_col, h_diag_off, h_own_off, h_nei_off;
+    std::vector<void*> allocs;
+    int64_t bytes = 0;
+};
+
+struct SolverCache;  // solver.cu
+
+struct fvgb_ls {
+    const fvgb_mesh* mesh = nullptr;
+    int32_t ncomp = 1;
+    double* values = nullptr;  // [m_len]
+    double* rhs = nullptr;     // [n*ncomp]
+    double* bmat = nullptr;    // [nbf]
+    double* brhs = nullptr;    // [nbf*ncomp]
+    SolverCache* solver = nullptr;
+};
+
+// Per-call patch table passed to kernels by value.
+struct PatchTable {
+    int32_t n;
+    int8_t type[FVGB_MAX_PATCHES];
+};
+
+inline fvgb_status cuda_fail(cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return fvgb_fail(e == cudaErrorMemoryAllocation ? FVGB_ERR_OOM : FVGB_ERR_CUDA, m.c_str());
+}
+
+#define FVGB_CUDA_TRY(call)                                   \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+#define FVGB_LAUNCH_CHECK(where)                              \
+    do {                                                      \
+        cudaError_t e_ = cudaGetLastError();                  \
+        if (e_ != cudaSuccess) return cuda_fail(e_, where);   \
+    } while (0)
+
+inline unsigned grid_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// Builds a PatchTable from a host array of per-patch types; false if invalid.
+inline bool make_patch_table(const fvgb_mesh* m, const int32_t* types, PatchTable* t) {
+    t->n = m->v.npatch;
+    if (t->n > FVGB_MAX_PATCHES) return false;
+    for (int i = 0; i < t->n; ++i) {
+        int32_t ty = types ? types[i] : FVGB_BC_CALCULATED;
+        if (ty < FVGB_BC_CALCULATED || ty > FVGB_BC_FIXED_GRADIENT) return false;
+        t->type[i] = (int8_t)ty;
+    }
+    return true;
+}
+
+inline bool patch_table_needs_ref(const PatchTable& t) {
+    for (int i = 0; i < t.n; ++i)
+        if (t.type[i] != FVGB_BC_CALCULATED) return true;
+    return false;
+}
+
+// Device-side allocation helper that records the allocation on the mesh.
+template <class T>
+inline cudaError_t mesh_alloc(fvgb_mesh* m, T** p, int64_t count) {
+    size_t bytes = sizeof(T) * (size_t)(count > 0 ? count : 1);
+    cudaError_t e = cudaMalloc((void**)p, bytes);
+    if (e == cudaSuccess) {
+        m->allocs.push_back(*p);
+        m->bytes += (int64_t)bytes;
+    }
+    return e;
+}
+
+#define FVGB_CHECK_ARG(cond, msg) \
+    do {                          \
+        if (!(cond)) return fvgb_fail(FVGB_ERR_INVALID_ARG, msg); \
+    } while (0)

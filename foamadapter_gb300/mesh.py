@@ -1,0 +1,187 @@
+"""Host-side mesh arrays and their upload through the C ABI.
+
+``HostMesh`` is the array set of NeoN::UnstructuredMesh + BoundaryMesh that
+FoamAdapter's MeshAdapter builds from a Foam::fvMesh
+(src/datastructures/meshAdapter.cpp:59-136): int32 labels, FP64 geometry,
+Vec3 as 3 interleaved doubles, boundary arrays flat over the non-empty patches.
+It is produced by the library's hex-box builder or from a polyMesh (points,
+faces, owner, neighbour, patches) through the library's OpenFOAM geometry.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+
+
+@dataclass
+class HostMesh:
+    n: int
+    nif: int
+    nbf: int
+    npatch: int
+    V: np.ndarray
+    C: np.ndarray
+    own: np.ndarray
+    nei: np.ndarray
+    Sf: np.ndarray
+    Cf: np.ndarray
+    magSf: np.ndarray
+    w: np.ndarray
+    delta: np.ndarray
+    bcells: np.ndarray
+    bSf: np.ndarray
+    bCf: np.ndarray
+    bmagSf: np.ndarray
+    bw: np.ndarray
+    bdelta: np.ndarray
+    patch_offsets: np.ndarray
+    patch_names: list = field(default_factory=list)
+    points: np.ndarray | None = None
+
+    @property
+    def nnz(self) -> int:
+        return self.n + 2 * self.nif
+
+    def patch_slice(self, name: str) -> slice:
+        p = self.patch_names.index(name)
+        return slice(int(self.patch_offsets[p]), int(self.patch_offsets[p + 1]))
+
+    def desc(self) -> abi.MeshDesc:
+        d = abi.MeshDesc()
+        d.n_cells, d.n_ifaces, d.n_bfaces, d.n_patches = self.n, self.nif, self.nbf, self.npatch
+        for name, arr in (("cell_volumes", self.V), ("cell_centres", self.C), ("owner", self.own),
+                          ("neighbour", self.nei), ("face_areas", self.Sf), ("mag_face_areas", self.magSf),
+                          ("weights", self.w), ("delta_coeffs", self.delta), ("bface_cells", self.bcells),
+                          ("bface_areas", self.bSf), ("bmag_face_areas", self.bmagSf),
+                          ("bweights", self.bw), ("bdelta_coeffs", self.bdelta),
+                          ("patch_offsets", self.patch_offsets)):
+            setattr(d, name, abi.ptr(arr))
+        return d
+
+
+def _alloc_arrays(n, nif, nbf, npatch, npoints=0):
+    a = dict(
+        points=np.zeros(3 * npoints) if npoints else None,
+        cell_volumes=np.zeros(n), cell_centres=np.zeros(3 * n), owner=np.zeros(nif, np.int32),
+        neighbour=np.zeros(nif, np.int32), face_areas=np.zeros(3 * nif), face_centres=np.zeros(3 * nif),
+        mag_face_areas=np.zeros(nif), weights=np.zeros(nif), delta_coeffs=np.zeros(nif),
+        bface_cells=np.zeros(nbf, np.int32), bface_areas=np.zeros(3 * nbf), bface_centres=np.zeros(3 * nbf),
+        bmag_face_areas=np.zeros(nbf), bweights=np.zeros(nbf), bdelta_coeffs=np.zeros(nbf),
+        patch_offsets=np.zeros(npatch + 1, np.int32))
+    ma = abi.MeshArrays()
+    for k, v in a.items():
+        setattr(ma, k, abi.ptr(v) if v is not None else None)
+    return a, ma
+
+
+def _to_host(a, n, nif, nbf, npatch, names) -> HostMesh:
+    return HostMesh(
+        n=n, nif=nif, nbf=nbf, npatch=npatch, V=a["cell_volumes"], C=a["cell_centres"].reshape(-1, 3),
+        own=a["owner"], nei=a["neighbour"], Sf=a["face_areas"].reshape(-1, 3),
+        Cf=a["face_centres"].reshape(-1, 3), magSf=a["mag_face_areas"], w=a["weights"],
+        delta=a["delta_coeffs"], bcells=a["bface_cells"], bSf=a["bface_areas"].reshape(-1, 3),
+        bCf=a["bface_centres"].reshape(-1, 3), bmagSf=a["bmag_face_areas"], bw=a["bweights"],
+        bdelta=a["bdelta_coeffs"], patch_offsets=a["patch_offsets"], patch_names=list(names),
+        points=None if a["points"] is None else a["points"].reshape(-1, 3))
+
+
+def box(nx: int, ny: int, nz: int, lx: float = 1.0, ly: float = 1.0, lz: float = 1.0,
+        jitter: float = 0.0, seed: int = 0, two_d: bool = False) -> HostMesh:
+    """OpenFOAM-ordered hex box; patches xmin xmax ymin ymax [zmin zmax]."""
+    spec = abi.BoxSpec(nx, ny, nz, lx, ly, lz, jitter, seed, 1 if two_d else 0)
+    sizes = (C.c_int64 * 7)()
+    abi.check(abi.lib().fvgb_box_sizes(C.byref(spec), sizes))
+    npoints, _, n, nif, nbf, npatch, _ = list(sizes)
+    a, ma = _alloc_arrays(n, nif, nbf, npatch, npoints)
+    abi.check(abi.lib().fvgb_box_build(C.byref(spec), C.byref(ma)))
+    names = ["xmin", "xmax", "ymin", "ymax"] + ([] if two_d else ["zmin", "zmax"])
+    return _to_host(a, n, nif, nbf, npatch, names)
+
+
+def from_polymesh(points: np.ndarray, faces: list, owner: np.ndarray, neighbour: np.ndarray,
+                  patches: list) -> tuple[HostMesh, np.ndarray]:
+    """Geometry of an OpenFOAM polyMesh.
+
+    ``patches`` is a list of (name, type, nFaces, startFace).  Empty patches are
+    left out of the flat boundary, as fvPatch sizes them 0.  Returns the mesh
+    and the polyMesh face index of every internal and flat boundary face.
+    """
+    n_cells = int(max(owner.max(), neighbour.max() if len(neighbour) else -1)) + 1
+    nif = len(neighbour)
+    order = list(range(nif))
+    names, offs, empties = [], [0], []
+    for name, typ, nfaces, start in patches:
+        rng = list(range(start, start + nfaces))
+        if typ == "empty":
+            empties += rng
+        else:
+            names.append(name)
+            order += rng
+            offs.append(offs[-1] + nfaces)
+    nbf = len(order) - nif
+    perm = order + empties
+    face_offs = np.zeros(len(perm) + 1, np.int32)
+    pts = []
+    for i, f in enumerate(perm):
+        pts += list(faces[f])
+        face_offs[i + 1] = len(pts)
+    face_pts = np.asarray(pts, np.int32)
+    owner_all = np.asarray(owner, np.int32)[perm].copy()
+    nei = np.ascontiguousarray(neighbour, dtype=np.int32)
+    points = np.ascontiguousarray(points, dtype=np.float64)
+    a, ma = _alloc_arrays(n_cells, nif, nbf, len(names))
+    abi.check(abi.lib().fvgb_geometry_compute(
+        len(points), abi.ptr(points), n_cells, len(perm), abi.ptr(face_offs), abi.ptr(face_pts),
+        abi.ptr(owner_all), nif, abi.ptr(nei), nbf, C.byref(ma)))
+    a["patch_offsets"][:] = np.asarray(offs, np.int32)
+    return _to_host(a, n_cells, nif, nbf, len(names), names), np.asarray(order, np.int64)
+
+
+class DeviceMesh:
+    """A mesh uploaded and indexed on the GPU (fvgb_mesh handle)."""
+
+    def __init__(self, host: HostMesh):
+        self.host = host
+        h = C.c_void_p()
+        d = host.desc()
+        abi.check(abi.lib().fvgb_mesh_create(C.byref(d), C.byref(h)))
+        self.handle = h
+
+    @property
+    def n(self):
+        return self.host.n
+
+    @property
+    def nif(self):
+        return self.host.nif
+
+    @property
+    def nbf(self):
+        return self.host.nbf
+
+    def device_bytes(self) -> int:
+        return int(abi.lib().fvgb_mesh_device_bytes(self.handle))
+
+    def sparsity(self):
+        n, nif = self.host.n, self.host.nif
+        nnz = n + 2 * nif
+        ro, col = np.zeros(n + 1, np.int32), np.zeros(nnz, np.int32)
+        do, oo, no = np.zeros(n, np.int32), np.zeros(nif, np.int32), np.zeros(nif, np.int32)
+        abi.check(abi.lib().fvgb_mesh_sparsity(self.handle, abi.ptr(ro), abi.ptr(col), abi.ptr(do),
+                                               abi.ptr(oo), abi.ptr(no)))
+        return ro, col, do, oo, no
+
+    def close(self):
+        if self.handle:
+            abi.lib().fvgb_mesh_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

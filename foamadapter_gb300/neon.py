@@ -1,0 +1,283 @@
+"""NeoN-shaped Python mirror of the drop-in, on top of the C ABI.
+
+Class and method names follow the NeoN operators FoamAdapter calls
+(GaussGreenDiv(exec, mesh, scheme).div(out, phi, T, coeff),
+GaussGreenGrad(exec, mesh).grad(T, coeff, out), SurfaceInterpolation,
+GaussGreenLaplacian, FaceNormalGradient, la::createSparsity,
+LinearSystem, PDESolver::{assemble, setReference, solve}, applyOperator, diag)
+so that the tests read like the reference's own tests
+(test/test_operators.cpp, test/test_implicitOperators.cpp).  Device storage
+is torch CUDA tensors: torch is only the allocator here; every operation is a
+call into libfvgb.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import abi
+from .mesh import DeviceMesh, HostMesh
+
+_SCHEMES = {"linear": abi.SCHEME_LINEAR, "upwind": abi.SCHEME_UPWIND}
+_BC = {"calculated": abi.BC_CALCULATED, "fixedValue": abi.BC_FIXED_VALUE,
+       "fixedGradient": abi.BC_FIXED_GRADIENT, "zeroGradient": abi.BC_FIXED_GRADIENT,
+       "noSlip": abi.BC_FIXED_VALUE}
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _scheme(s) -> int:
+    if isinstance(s, (list, tuple)):
+        s = [t for t in s if t not in ("Gauss", "uncorrected")][0]
+    return _SCHEMES[s] if isinstance(s, str) else int(s)
+
+
+def dev(a, dtype=torch.float64) -> torch.Tensor:
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).cuda()
+
+
+class VolumeField:
+    """Cell values [n*ncomp] plus flat boundary values [nbf*ncomp] and a BC per patch.
+
+    bcs: list of (type, value) per non-empty patch; value is a scalar/Vec3 or a
+    per-face array (fixed value or fixed gradient); zeroGradient = fixedGradient 0
+    and noSlip = fixedValue 0, as FoamAdapter's readers map them (readers.hpp:43-95).
+    """
+
+    def __init__(self, mesh: DeviceMesh, internal, bcs=None, ncomp: int = 1, name: str = ""):
+        self.mesh, self.ncomp, self.name = mesh, ncomp, name
+        hm = mesh.host
+        self.internal = dev(np.asarray(internal, np.float64).reshape(-1))
+        assert self.internal.numel() == hm.n * ncomp
+        bcs = bcs or [("calculated", 0.0)] * hm.npatch
+        assert len(bcs) == hm.npatch
+        self.types = np.asarray([_BC[t] for t, _ in bcs], np.int32)
+        ref = np.zeros((hm.nbf, ncomp))
+        for p, (t, v) in enumerate(bcs):
+            sl = slice(int(hm.patch_offsets[p]), int(hm.patch_offsets[p + 1]))
+            if t in ("zeroGradient", "noSlip"):
+                v = 0.0
+            v = np.asarray(v, np.float64).reshape(-1)
+            nfp = sl.stop - sl.start
+            if v.size == 1 or (v.size == ncomp and nfp != 1):
+                ref[sl] = np.broadcast_to(v if v.size == ncomp else np.repeat(v, ncomp), (nfp, ncomp))
+            else:
+                ref[sl] = v.reshape(nfp, ncomp)
+        self.ref = dev(ref.reshape(-1))
+        self.boundary = torch.zeros(max(1, hm.nbf * ncomp), dtype=torch.float64, device="cuda")
+        self.correctBoundaryConditions()
+
+    def bc_struct(self) -> abi.BC:
+        return abi.BC(abi.ptr(self.types), abi.ptr(self.ref))
+
+    def correctBoundaryConditions(self):
+        bc = self.bc_struct()
+        abi.check(abi.lib().fvgb_bc_correct(self.mesh.handle, self.ncomp, C.byref(bc),
+                                            abi.ptr(self.internal), abi.ptr(self.boundary), _stream()))
+
+    def host(self):
+        return self.internal.cpu().numpy()
+
+
+class SurfaceField:
+    """Face values: internal faces then boundary faces [(nif+nbf)*ncomp]."""
+
+    def __init__(self, mesh: DeviceMesh, values=None, ncomp: int = 1):
+        self.mesh, self.ncomp = mesh, ncomp
+        nf = mesh.nif + mesh.nbf
+        if values is None:
+            self.values = torch.zeros(max(1, nf * ncomp), dtype=torch.float64, device="cuda")
+        else:
+            self.values = dev(np.asarray(values, np.float64).reshape(-1))
+
+    def host(self):
+        return self.values.cpu().numpy()
+
+
+class SurfaceInterpolation:
+    def __init__(self, mesh: DeviceMesh, scheme="linear"):
+        self.mesh, self.scheme = mesh, _scheme(scheme)
+
+    def interpolate(self, src: VolumeField, dst: SurfaceField | None = None, flux: SurfaceField | None = None):
+        dst = dst or SurfaceField(self.mesh, ncomp=src.ncomp)
+        L = abi.lib()
+        if self.scheme == abi.SCHEME_LINEAR:
+            abi.check(L.fvgb_interp_linear(self.mesh.handle, src.ncomp, abi.ptr(src.internal),
+                                           abi.ptr(src.boundary), abi.ptr(dst.values), _stream()))
+        else:
+            assert flux is not None, "upwind interpolation needs the face flux"
+            abi.check(L.fvgb_interp_upwind(self.mesh.handle, src.ncomp, abi.ptr(flux.values),
+                                           abi.ptr(src.internal), abi.ptr(src.boundary),
+                                           abi.ptr(dst.values), _stream()))
+        return dst
+
+
+class GaussGreenDiv:
+    def __init__(self, mesh: DeviceMesh, scheme="linear"):
+        self.mesh, self.scheme = mesh, _scheme(scheme)
+
+    def div(self, out: torch.Tensor, faceFlux: SurfaceField, phi: VolumeField, coeff: float = 1.0):
+        abi.check(abi.lib().fvgb_div_explicit(self.mesh.handle, self.scheme, phi.ncomp,
+                                              abi.ptr(faceFlux.values), abi.ptr(phi.internal),
+                                              abi.ptr(phi.boundary), float(coeff), abi.ptr(out),
+                                              _stream()))
+        return out
+
+
+class GaussGreenGrad:
+    def __init__(self, mesh: DeviceMesh):
+        self.mesh = mesh
+
+    def grad(self, phi: VolumeField, coeff: float = 1.0, out: torch.Tensor | None = None):
+        if out is None:
+            out = torch.zeros(3 * self.mesh.n, dtype=torch.float64, device="cuda")
+        abi.check(abi.lib().fvgb_grad(self.mesh.handle, abi.ptr(phi.internal), abi.ptr(phi.boundary),
+                                      float(coeff), abi.ptr(out), _stream()))
+        return out
+
+
+class GaussGreenLaplacian:
+    def __init__(self, mesh: DeviceMesh, scheme=("Gauss", "linear", "uncorrected")):
+        self.mesh = mesh
+
+    def laplacian(self, out: torch.Tensor, gamma: SurfaceField, phi: VolumeField, coeff: float = 1.0):
+        abi.check(abi.lib().fvgb_laplacian_explicit(self.mesh.handle, phi.ncomp, abi.ptr(gamma.values),
+                                                    abi.ptr(phi.internal), abi.ptr(phi.boundary),
+                                                    float(coeff), abi.ptr(out), _stream()))
+        return out
+
+
+class FaceNormalGradient:
+    def __init__(self, mesh: DeviceMesh, scheme="uncorrected"):
+        self.mesh = mesh
+
+    def faceNormalGrad(self, phi: VolumeField, out: SurfaceField | None = None):
+        out = out or SurfaceField(self.mesh)
+        abi.check(abi.lib().fvgb_sngrad(self.mesh.handle, abi.ptr(phi.internal), abi.ptr(phi.boundary),
+                                        abi.ptr(out.values), _stream()))
+        return out
+
+
+def createSparsity(mesh: DeviceMesh):
+    """la::createSparsity: (rowOffs, colIdxs, diagOffset, ownerOffset, neighbourOffset) on the host."""
+    return mesh.sparsity()
+
+
+@dataclass
+class Term:
+    """One operator of a dsl::Expression (see fvgb_term in include/fvgb.h)."""
+    kind: int
+    coeff: float = 1.0
+    scheme: int = abi.SCHEME_LINEAR
+    cell: torch.Tensor | None = None
+    face: torch.Tensor | None = None
+
+    def struct(self) -> abi.Term:
+        return abi.Term(self.kind, self.scheme, self.coeff, abi.ptr(self.cell), abi.ptr(self.face))
+
+
+def ddt(old: torch.Tensor, coeff: float = 1.0) -> Term:
+    return Term(abi.TERM_DDT, coeff, cell=old)
+
+
+def laplacian(gamma: SurfaceField, coeff: float = 1.0) -> Term:
+    return Term(abi.TERM_LAPLACIAN, coeff, face=gamma.values)
+
+
+def div(flux: SurfaceField, scheme="linear", coeff: float = 1.0) -> Term:
+    return Term(abi.TERM_DIV, coeff, scheme=_scheme(scheme), face=flux.values)
+
+
+def source(coeff: float = 1.0, s: torch.Tensor | None = None) -> Term:
+    return Term(abi.TERM_SOURCE, coeff, cell=s)
+
+
+def explicit(values: torch.Tensor, coeff: float = 1.0) -> Term:
+    return Term(abi.TERM_EXPLICIT, coeff, cell=values)
+
+
+class LinearSystem:
+    """la::LinearSystem on the mesh pattern (device resident)."""
+
+    def __init__(self, mesh: DeviceMesh, ncomp: int = 1):
+        self.mesh, self.ncomp = mesh, ncomp
+        h = C.c_void_p()
+        abi.check(abi.lib().fvgb_ls_create(mesh.handle, ncomp, C.byref(h)))
+        self.handle = h
+
+    def assemble(self, terms, dt: float, psi: VolumeField):
+        arr = (abi.Term * max(1, len(terms)))(*[t.struct() for t in terms])
+        bc = psi.bc_struct()
+        abi.check(abi.lib().fvgb_assemble(self.handle, arr, len(terms), float(dt), C.byref(bc),
+                                          abi.ptr(psi.boundary), _stream()))
+
+    def setReference(self, cell: int, value: float):
+        abi.check(abi.lib().fvgb_set_reference(self.handle, int(cell), float(value), _stream()))
+
+    def apply(self, x: torch.Tensor) -> torch.Tensor:
+        out = torch.empty(self.mesh.n * self.ncomp, dtype=torch.float64, device="cuda")
+        abi.check(abi.lib().fvgb_apply_operator(self.handle, abi.ptr(x), abi.ptr(out), _stream()))
+        return out
+
+    def diag(self) -> torch.Tensor:
+        out = torch.empty(self.mesh.n, dtype=torch.float64, device="cuda")
+        abi.check(abi.lib().fvgb_ls_diag(self.handle, abi.ptr(out), _stream()))
+        return out
+
+    def export(self):
+        hm = self.mesh.host
+        v = torch.empty(hm.nnz, dtype=torch.float64, device="cuda")
+        r = torch.empty(hm.n * self.ncomp, dtype=torch.float64, device="cuda")
+        bm = torch.empty(max(1, hm.nbf), dtype=torch.float64, device="cuda")
+        br = torch.empty(max(1, hm.nbf * self.ncomp), dtype=torch.float64, device="cuda")
+        abi.check(abi.lib().fvgb_ls_export(self.handle, abi.ptr(v), abi.ptr(r), abi.ptr(bm), abi.ptr(br),
+                                           _stream()))
+        return v, r, bm[:hm.nbf], br[:hm.nbf * self.ncomp]
+
+    def solve(self, x: torch.Tensor, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=abi.PREC_FP64,
+              inner_rel_tol=1e-3, inner_max_iter=200, max_outer=30, allow=(abi.ERR_NOT_CONVERGED,)):
+        cfg = abi.SolverCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer)
+        st = abi.SolverStats()
+        abi.check(abi.lib().fvgb_solve(self.handle, abi.ptr(x), C.byref(cfg), C.byref(st), _stream()),
+                  allow=allow)
+        return st
+
+    def close(self):
+        if self.handle:
+            abi.lib().fvgb_ls_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PDESolver:
+    """FoamAdapter::PDESolver (expression.hpp:23-179): owns the system of one PDE."""
+
+    def __init__(self, terms, psi: VolumeField, dt: float):
+        self.terms, self.psi, self.dt = terms, psi, dt
+        self.ls = LinearSystem(psi.mesh, psi.ncomp)
+        self.ref = None
+
+    def assemble(self):
+        self.ls.assemble(self.terms, self.dt, self.psi)
+        return self.ls
+
+    def setReference(self, cell: int, value: float):
+        self.ref = (cell, value)
+
+    def solve(self, **cfg):
+        self.assemble()
+        if self.ref is not None:
+            self.ls.setReference(*self.ref)
+        st = self.ls.solve(self.psi.internal, **cfg)
+        self.psi.correctBoundaryConditions()
+        return st

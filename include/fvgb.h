@@ -1,0 +1,347 @@
+/*
+ * fvgb.h -- C ABI of the GB300 (sm_103a) finite-volume hot path.
+ *
+ * This is the drop-in boundary for the NeoN / FoamAdapter operator and DSL
+ * calls that FoamAdapter makes on its finite-volume hot path.  Every entry
+ * point takes plain pointers and sizes; field and matrix data live in device
+ * memory owned by the caller unless the entry point says otherwise, and every
+ * asynchronous call takes the CUDA stream it is ordered on (a cudaStream_t
+ * passed as fvgb_stream; NULL is the legacy default stream).
+ *
+ * Conventions shared by every entry point
+ *   - Labels are int32, values are IEEE binary64 (double) unless a name says
+ *     otherwise.  Vector (Vec3) fields are stored as 3 doubles per cell,
+ *     interleaved (x,y,z), the in-memory layout of NeoN::Vec3.
+ *   - A volume field is two device arrays: `internal` [n_cells*ncomp] and
+ *     `boundary` [n_bfaces*ncomp] (the flat boundary values of every
+ *     non-empty patch, in patch order).  Empty patches hold zero faces.
+ *   - A surface field is one device array of n_ifaces + n_bfaces entries:
+ *     internal faces first, then the boundary faces patch by patch.
+ *   - Explicit operators ACCUMULATE into the caller's output: out += result.
+ *     With `coeff` the operator scaling (NeoN dsl::Coeff, a scalar here),
+ *     the per-cell scaling is exactly  sum * (coeff / V[c]).
+ *   - All calls return an fvgb_status; fvgb_last_error() gives the message of
+ *     the most recent failure on the calling thread.
+ *   - Handles are not thread safe; distinct handles on distinct streams are.
+ */
+#ifndef FVGB_H
+#define FVGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum fvgb_status {
+    FVGB_OK = 0,
+    FVGB_ERR_INVALID_ARG = 1,   /* bad size, null pointer, malformed mesh     */
+    FVGB_ERR_OOM = 2,           /* device allocation failed                    */
+    FVGB_ERR_NOT_CONVERGED = 3, /* iteration cap reached before the criteria   */
+    FVGB_ERR_BREAKDOWN = 4,     /* p.Ap == 0 or a non-finite scalar in a solve */
+    FVGB_ERR_CUDA = 5,          /* any other CUDA runtime error                */
+    FVGB_ERR_UNSUPPORTED = 6,   /* valid request this build does not implement */
+    FVGB_ERR_BUDGET = 7,        /* serving: request exceeds the HBM budget     */
+    FVGB_ERR_CANCELLED = 8      /* serving: request cancelled before it ran    */
+} fvgb_status;
+
+typedef void* fvgb_stream; /* cudaStream_t */
+
+/* Human readable name of a status code (static storage). */
+const char* fvgb_status_string(int status);
+/* Message of the last failing call on this thread ("" if none). */
+const char* fvgb_last_error(void);
+/* ABI version, (major << 16) | minor. */
+int32_t fvgb_abi_version(void);
+
+/* -------------------------------------------------------------------- mesh */
+/*
+ * Host-side description of an unstructured finite-volume mesh, the array set
+ * of NeoN::UnstructuredMesh + NeoN::BoundaryMesh as FoamAdapter builds it from
+ * a Foam::fvMesh (reference: src/datastructures/meshAdapter.cpp:59-136).
+ * All pointers are HOST pointers; fvgb_mesh_create copies what it needs.
+ *   weights / nonorth_delta_coeffs: internal faces; boundary faces use
+ *   bweights / bdelta_coeffs.  The laplacian and snGrad use
+ *   nonorth_delta_coeffs (1 / max(n.d, 0.05|d|), OpenFOAM's uncorrected
+ *   scheme coefficient).
+ */
+typedef struct fvgb_mesh_desc {
+    int32_t n_cells;
+    int32_t n_ifaces;          /* internal faces                          */
+    int32_t n_bfaces;          /* faces of all non-empty patches          */
+    int32_t n_patches;         /* non-empty patches                       */
+    const double* cell_volumes;     /* [n_cells]                          */
+    const double* cell_centres;     /* [n_cells*3]   (optional, may be NULL) */
+    const int32_t* owner;           /* [n_ifaces]                         */
+    const int32_t* neighbour;       /* [n_ifaces]                         */
+    const double* face_areas;       /* Sf  [n_ifaces*3]                   */
+    const double* mag_face_areas;   /* |Sf| [n_ifaces]                    */
+    const double* weights;          /* [n_ifaces]                         */
+    const double* delta_coeffs;     /* [n_ifaces]                         */
+    const int32_t* bface_cells;     /* [n_bfaces]                         */
+    const double* bface_areas;      /* [n_bfaces*3]                       */
+    const double* bmag_face_areas;  /* [n_bfaces]                         */
+    const double* bweights;         /* [n_bfaces]                         */
+    const double* bdelta_coeffs;    /* [n_bfaces]                         */
+    const int32_t* patch_offsets;   /* [n_patches+1], patch p = [off[p], off[p+1]) */
+} fvgb_mesh_desc;
+
+typedef struct fvgb_mesh fvgb_mesh;
+
+/* Validate, upload and index a mesh: builds the cell->face gather lists
+ * (ascending face order per cell), the CSR/sliced-ELL matrix pattern with
+ * owner/neighbour/diagonal slot maps (NeoN la::SparsityPattern,
+ * test/test_sparsityPattern.cpp:36-62) on the device. Synchronous. */
+fvgb_status fvgb_mesh_create(const fvgb_mesh_desc* desc, fvgb_mesh** out);
+fvgb_status fvgb_mesh_destroy(fvgb_mesh* mesh);
+/* Sizes: n_cells, n_ifaces, n_bfaces, n_patches, nnz (= n_cells + 2*n_ifaces). */
+fvgb_status fvgb_mesh_sizes(const fvgb_mesh* mesh, int64_t out[5]);
+/* Device bytes held by the mesh handle (geometry + index structures). */
+int64_t fvgb_mesh_device_bytes(const fvgb_mesh* mesh);
+
+/* CSR sparsity pattern in NeoN's layout, copied to HOST arrays:
+ * row_offs[n+1], col_idxs[nnz], diag_offset[n], owner_offset[n_ifaces],
+ * neighbour_offset[n_ifaces] (offsets relative to the row start).
+ * Reference: la::SparsityPattern (expression.hpp:35, test_sparsityPattern.cpp:36-62). */
+fvgb_status fvgb_mesh_sparsity(const fvgb_mesh* mesh, int32_t* row_offs, int32_t* col_idxs,
+                               int32_t* diag_offset, int32_t* owner_offset,
+                               int32_t* neighbour_offset);
+
+/* ------------------------------------------------------- boundary conditions */
+typedef enum fvgb_bc_type {
+    FVGB_BC_CALCULATED = 0,     /* boundary values are whatever was written      */
+    FVGB_BC_FIXED_VALUE = 1,    /* value = ref (noSlip is fixedValue 0)          */
+    FVGB_BC_FIXED_GRADIENT = 2  /* value = internal + ref/deltaCoeff; zeroGradient = ref 0 */
+} fvgb_bc_type;
+
+/* Boundary condition of a volume field: a type per patch (host array) and a
+ * per-boundary-face reference (device array [n_bfaces*ncomp]: the fixed value
+ * or the fixed gradient).  Reference semantics: readers.hpp:43-95. */
+typedef struct fvgb_bc {
+    const int32_t* patch_type; /* HOST [n_patches]                        */
+    const double* ref;         /* DEVICE [n_bfaces*ncomp] (may be NULL when every patch is CALCULATED) */
+} fvgb_bc;
+
+/* VolumeField::correctBoundaryConditions: recompute boundary values. */
+fvgb_status fvgb_bc_correct(const fvgb_mesh* mesh, int32_t ncomp, const fvgb_bc* bc,
+                            const double* internal, double* boundary, fvgb_stream stream);
+
+/* ------------------------------------------------------- explicit operators */
+typedef enum fvgb_scheme { FVGB_SCHEME_LINEAR = 0, FVGB_SCHEME_UPWIND = 1 } fvgb_scheme;
+
+/* SurfaceInterpolation linear (NeoN; reference call sites neoIcoFoam.cpp:118-124,
+ * test_operators.cpp:52-58):  dst_f = w_f*(src_P - src_N) + src_N on internal
+ * faces, dst_b = boundary value.  dst [(n_ifaces+n_bfaces)*ncomp] is overwritten. */
+fvgb_status fvgb_interp_linear(const fvgb_mesh* mesh, int32_t ncomp, const double* src,
+                               const double* src_b, double* dst, fvgb_stream stream);
+/* SurfaceInterpolation upwind: dst_f = flux_f >= 0 ? src_P : src_N; dst_b = boundary value. */
+fvgb_status fvgb_interp_upwind(const fvgb_mesh* mesh, int32_t ncomp, const double* flux,
+                               const double* src, const double* src_b, double* dst,
+                               fvgb_stream stream);
+/* GaussGreenDiv::div(out, faceFlux, phi, coeff) (bench_explicitOperators.cpp:114-115):
+ * out_P += (sum over faces of P in ascending face order of +-flux_f*phi_f) * (coeff/V_P),
+ * + for owner and boundary faces, - for neighbour faces. */
+fvgb_status fvgb_div_explicit(const fvgb_mesh* mesh, int32_t scheme, int32_t ncomp,
+                              const double* flux, const double* phi, const double* phi_b,
+                              double coeff, double* out, fvgb_stream stream);
+/* GaussGreenGrad::grad(T, coeff, out) (test_operators.cpp:72): linear face values,
+ * out_P[3] += (sum +-Sf*T_f) * (coeff/V_P). */
+fvgb_status fvgb_grad(const fvgb_mesh* mesh, const double* phi, const double* phi_b,
+                      double coeff, double* out, fvgb_stream stream);
+/* GaussGreenLaplacian::laplacian(out, gamma, T, coeff), uncorrected
+ * (bench_explicitOperators.cpp:212-213): flux_f = gamma_f*(|Sf|*delta_f)*(T_N - T_P),
+ * boundary flux_b = gamma_b*(|Sf|*delta_b)*(T_b - T_P); out_P += (sum +-flux)*(coeff/V_P). */
+fvgb_status fvgb_laplacian_explicit(const fvgb_mesh* mesh, int32_t ncomp, const double* gamma,
+                                    const double* phi, const double* phi_b, double coeff,
+                                    double* out, fvgb_stream stream);
+/* FaceNormalGradient uncorrected (bench_explicitOperators.cpp:455-479):
+ * out_f = delta_f*(T_N - T_P), out_b = delta_b*(T_b - T_P); overwritten. */
+fvgb_status fvgb_sngrad(const fvgb_mesh* mesh, const double* phi, const double* phi_b,
+                        double* out, fvgb_stream stream);
+/* Fused explicit step of  ddt(T) + div(phi, T) = 0, Gauss upwind, forward Euler
+ * (test_advection.cpp:116-170): T_new_P = T_old_P - dt*(div_P) with div_P the
+ * fvgb_div_explicit value for coeff 1; then the boundary values of T_new are
+ * corrected with `bc` (bit-identical to the three unfused calls). */
+fvgb_status fvgb_advect_euler_step(const fvgb_mesh* mesh, const double* flux,
+                                   const double* T_old, const double* T_old_b, double dt,
+                                   const fvgb_bc* bc, double* T_new, double* T_new_b,
+                                   fvgb_stream stream);
+
+/* ----------------------------------------------- linear system and assembly */
+typedef struct fvgb_ls fvgb_ls;
+
+typedef enum fvgb_term_kind {
+    FVGB_TERM_DDT = 0,             /* implicit Euler ddt  (DdtOperator)                */
+    FVGB_TERM_LAPLACIAN = 1,       /* implicit laplacian(gamma, psi) uncorrected       */
+    FVGB_TERM_DIV = 2,             /* implicit div(flux, psi), linear or upwind        */
+    FVGB_TERM_SOURCE = 3,          /* implicit source: diag += coeff*s_P*V_P           */
+    FVGB_TERM_EXPLICIT = 4         /* rhs -= coeff*E_P (E already volume integrated)   */
+} fvgb_term_kind;
+
+/* One operator of a dsl::Expression. The expression is
+ *   sum_t coeff_t * op_t(psi) = 0,
+ * each implicit op_t(psi) = A_t psi - b_t, so A = sum coeff_t A_t and
+ * b = sum coeff_t b_t (EXPLICIT: b -= coeff*E).  Terms are applied in array order. */
+typedef struct fvgb_term {
+    int32_t kind;
+    int32_t scheme;        /* DIV: FVGB_SCHEME_LINEAR or FVGB_SCHEME_UPWIND           */
+    double coeff;          /* operator scaling                                        */
+    const double* cell;    /* DDT: old-time psi [n*ncomp]; SOURCE: s [n] or NULL (=1);
+                              EXPLICIT: E [n*ncomp]                                   */
+    const double* face;    /* LAPLACIAN: gamma [nIF+nBF]; DIV: face flux [nIF+nBF]    */
+} fvgb_term;
+
+/* LinearSystem on the mesh pattern: values[nnz], rhs[n*ncomp],
+ * boundaryCoefficients {matrixValues[nBF], rhsValues[nBF*ncomp]}
+ * (reference: expression.hpp:36-39, pressureVelocityCoupling.cpp:180-185).
+ * Vector systems (ncomp 3) share one scalar coefficient per entry. */
+fvgb_status fvgb_ls_create(const fvgb_mesh* mesh, int32_t ncomp, fvgb_ls** out);
+fvgb_status fvgb_ls_destroy(fvgb_ls* ls);
+/* Assemble all terms from zero (PDESolver::assemble, expression.hpp:69-73).
+ * psi_bc / psi_b: boundary condition and current boundary values of psi. */
+fvgb_status fvgb_assemble(fvgb_ls* ls, const fvgb_term* terms, int32_t nterms, double dt,
+                          const fvgb_bc* psi_bc, const double* psi_b, fvgb_stream stream);
+/* PDESolver::SetReference (expression.hpp:102-111): rhs[r] += a_rr*value; a_rr += a_rr. */
+fvgb_status fvgb_set_reference(fvgb_ls* ls, int32_t ref_cell, double ref_value,
+                               fvgb_stream stream);
+/* applyOperator / la::computeResidual (expression.hpp:204-220): out = A x - b. */
+fvgb_status fvgb_apply_operator(const fvgb_ls* ls, const double* x, double* out,
+                                fvgb_stream stream);
+/* diag (expression.hpp:181-201): out[n] = a_PP. */
+fvgb_status fvgb_ls_diag(const fvgb_ls* ls, double* out, fvgb_stream stream);
+/* Copy the system out in NeoN's CSR order: values[nnz], rhs[n*ncomp],
+ * bmatrix[nBF], brhs[nBF*ncomp] (DEVICE destination pointers, any may be NULL). */
+fvgb_status fvgb_ls_export(const fvgb_ls* ls, double* values, double* rhs, double* bmatrix,
+                           double* brhs, fvgb_stream stream);
+
+/* ------------------------------------------------------------------- solve */
+typedef enum fvgb_precision {
+    FVGB_PREC_FP64 = 0,      /* Jacobi-PCG in FP64 (Ginkgo solver::Cg + Jacobi, block 1)        */
+    FVGB_PREC_MIXED_IR = 1   /* FP32 inner CG on the Jacobi-scaled system inside FP64
+                                iterative refinement: FP64 b-Ax, update and convergence test  */
+} fvgb_precision;
+
+/* Stopping criteria of fvSolution.cpp:106-142: relative (to the initial residual
+ * norm) and absolute residual norm, iteration cap (default 1000). 0 disables a
+ * tolerance.  The residual is the unpreconditioned r = b - A x, 2-norm. */
+typedef struct fvgb_solver_cfg {
+    double rel_tol;
+    double abs_tol;
+    int32_t max_iter;          /* FP64: CG iterations; MIXED_IR: total inner iterations */
+    int32_t precision;
+    double inner_rel_tol;      /* MIXED_IR: residual reduction asked of each inner solve */
+    int32_t inner_max_iter;    /* MIXED_IR: inner iteration cap per refinement step    */
+    int32_t max_outer;         /* MIXED_IR: refinement step cap                        */
+} fvgb_solver_cfg;
+
+/* SolverStats {initResNorm, finalResNorm, numIter} (expression.hpp:155-158). */
+typedef struct fvgb_solver_stats {
+    double init_res_norm;
+    double final_res_norm;
+    int32_t num_iter;          /* FP64: CG iterations; MIXED_IR: total inner iterations */
+    int32_t num_outer;         /* MIXED_IR refinement steps (0 for FP64)               */
+    int32_t status;            /* FVGB_OK, FVGB_ERR_NOT_CONVERGED or FVGB_ERR_BREAKDOWN */
+    int32_t reserved;
+} fvgb_solver_stats;
+
+/* dsl::solve / PDESolver::solve: solve A x = b in place (x holds the initial
+ * guess).  Enqueues one CUDA graph (device-side while loop, no host round
+ * trips per iteration) and waits for it; *stats is filled on return.
+ * Returns FVGB_OK, FVGB_ERR_NOT_CONVERGED or FVGB_ERR_BREAKDOWN. */
+fvgb_status fvgb_solve(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg,
+                       fvgb_solver_stats* stats, fvgb_stream stream);
+/* Asynchronous form: stats are written to DEVICE memory stats_dev when the
+ * stream reaches the end of the solve; nothing is waited for. */
+fvgb_status fvgb_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg,
+                             fvgb_solver_stats* stats_dev, fvgb_stream stream);
+
+/* Measurement aid (no reference counterpart): runs the FP64 CG init and
+ * `iters` iterations outside the graph on a private copy of x0, with CUDA
+ * events around each kernel; ms_out[4] = mean milliseconds of
+ * [spmv + p.Ap, x/r update + r.z, direction update, init].  Synchronous. */
+fvgb_status fvgb_solve_kernel_times(fvgb_ls* ls, const double* x0, int32_t iters, double* ms_out,
+                                    fvgb_stream stream);
+
+/* ------------------------------------------------- pressure-velocity (PISO) */
+/* computeRAUandHByA (pressureVelocityCoupling.cpp:65-128) on an assembled vector
+ * system: rAU_P = V_P / a_PP; HbyA_P = (b_P - sum_{faces asc} a_Pj U_j) * (rAU_P / V_P).
+ * A deterministic cell gather in ascending face order replaces the atomics. */
+fvgb_status fvgb_piso_rau_hbya(const fvgb_ls* ueqn, const double* U, double* rAU,
+                               double* HbyA, fvgb_stream stream);
+/* constrainHbyA (pressureVelocityCoupling.cpp:14-36): HbyA_b = U_b on every patch
+ * whose U condition is not assignable (patch_assignable[p] == 0, HOST array). */
+fvgb_status fvgb_piso_constrain_hbya(const fvgb_mesh* mesh, const int32_t* patch_assignable,
+                                     const double* U_b, double* HbyA_b, fvgb_stream stream);
+/* flux(volVectorField) (pressureVelocityCoupling.cpp:215-267):
+ * F_f = Sf . (w (U_P - U_N) + U_N); F_b = Sf_b . U_b.  out [nIF+nBF] overwritten. */
+fvgb_status fvgb_flux_vec(const fvgb_mesh* mesh, const double* U, const double* U_b,
+                          double* out, fvgb_stream stream);
+/* updateFaceVelocity (pressureVelocityCoupling.cpp:131-197):
+ * phi_f = phiHbyA_f - (a_NP p_N - a_PN p_P); phi_b = phiHbyA_b - (brhs_b - bmat_b p_P). */
+fvgb_status fvgb_piso_face_update(const fvgb_ls* peqn, const double* phiHbyA, const double* p,
+                                  double* phi, fvgb_stream stream);
+/* updateVelocity (pressureVelocityCoupling.cpp:199-213): U = HbyA - rAU * grad(p). */
+fvgb_status fvgb_piso_velocity_update(const fvgb_mesh* mesh, const double* HbyA,
+                                      const double* rAU, const double* p, const double* p_b,
+                                      double* U, fvgb_stream stream);
+
+/* ------------------------------------------------------------ mesh builder */
+/* Host helpers (no GPU): an OpenFOAM-ordered hex box and OpenFOAM geometry.
+ * They stand in for Foam::fvMesh, which provides these arrays in the reference. */
+typedef struct fvgb_box_spec {
+    int32_t nx, ny, nz;
+    double lx, ly, lz;         /* box edge lengths, origin at 0                   */
+    double jitter;             /* interior vertex jitter, fraction of the spacing */
+    uint64_t seed;
+    int32_t two_d;             /* 1: nz must be 1, front/back are empty patches   */
+} fvgb_box_spec;
+
+/* Array sizes of a box: [n_points, n_faces_total, n_cells, n_ifaces, n_bfaces,
+ * n_patches, face_point_entries]. */
+fvgb_status fvgb_box_sizes(const fvgb_box_spec* spec, int64_t out[7]);
+/* Topology + geometry of a box into caller-allocated HOST arrays sized by
+ * fvgb_box_sizes.  Patches (non-empty only): xmin, xmax, ymin, ymax[, zmin, zmax].
+ * cell_centres [n*3], face_centres [nIF*3], bface_centres [nBF*3], points [np*3]
+ * may be NULL.  Geometry as fvgb_geometry_compute. */
+typedef struct fvgb_mesh_arrays {
+    double* points;            /* [n_points*3]                 */
+    double* cell_volumes;      /* [n_cells]                    */
+    double* cell_centres;      /* [n_cells*3]                  */
+    int32_t* owner;            /* [n_ifaces]                   */
+    int32_t* neighbour;        /* [n_ifaces]                   */
+    double* face_areas;        /* [n_ifaces*3]                 */
+    double* face_centres;      /* [n_ifaces*3]                 */
+    double* mag_face_areas;    /* [n_ifaces]                   */
+    double* weights;           /* [n_ifaces]                   */
+    double* delta_coeffs;      /* [n_ifaces]                   */
+    int32_t* bface_cells;      /* [n_bfaces]                   */
+    double* bface_areas;       /* [n_bfaces*3]                 */
+    double* bface_centres;     /* [n_bfaces*3]                 */
+    double* bmag_face_areas;   /* [n_bfaces]                   */
+    double* bweights;          /* [n_bfaces]                   */
+    double* bdelta_coeffs;     /* [n_bfaces]                   */
+    int32_t* patch_offsets;    /* [n_patches+1]                */
+} fvgb_mesh_arrays;
+fvgb_status fvgb_box_build(const fvgb_box_spec* spec, fvgb_mesh_arrays* out);
+
+/* OpenFOAM geometry of a general polyMesh (HOST): face centres/areas by triangle
+ * decomposition about the point average, cell volumes/centres by pyramid
+ * decomposition about the face-centre average, linear weights
+ * |Sf.(C_N-Cf)| / (|Sf.(Cf-C_P)| + |Sf.(C_N-Cf)|) and non-orthogonal delta
+ * coefficients 1/max(nf.d, 0.05|d|).  Faces: face_offs[n_faces_total+1] into
+ * face_points; faces [0,n_ifaces) internal, then the boundary faces of the
+ * `out` patches in order (faces of empty patches must be given after all of
+ * them and are skipped: n_faces_total may exceed n_ifaces+n_bfaces).
+ * `owner_all` has n_faces_total entries. */
+fvgb_status fvgb_geometry_compute(int32_t n_points, const double* points, int32_t n_cells,
+                                  int32_t n_faces_total, const int32_t* face_offs,
+                                  const int32_t* face_points, const int32_t* owner_all,
+                                  int32_t n_ifaces, const int32_t* neighbour,
+                                  int32_t n_bfaces, fvgb_mesh_arrays* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FVGB_H */

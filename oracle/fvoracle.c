@@ -1,0 +1,743 @@
+/*
+ * fvoracle.c -- CPU restatement of the FoamAdapter / NeoN finite-volume hot
+ * path.  TEST INFRASTRUCTURE ONLY (the checker for the GPU path and the timed
+ * CPU baseline); see fvoracle.h for scope and pinning.
+ *
+ * Floating point: compiled with -ffp-contract=off.  Where the algorithm uses a
+ * fused multiply-add (the CG kernels), it calls fma()/fmaf() explicitly, and the
+ * dot products follow the fixed two-stage reduction tree that the GPU kernels
+ * use (blocks of 256 threads x 4 rows, warp sums, block sum, sum of block
+ * partials), so the CG iterates are reproducible bit for bit.
+ */
+#include "fvoracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+enum { BC_CALCULATED = 0, BC_FIXED_VALUE = 1, BC_FIXED_GRADIENT = 2 };
+enum { SCHEME_LINEAR = 0, SCHEME_UPWIND = 1 };
+enum { TERM_DDT = 0, TERM_LAPLACIAN = 1, TERM_DIV = 2, TERM_SOURCE = 3, TERM_EXPLICIT = 4 };
+enum { ST_OK = 0, ST_NOT_CONVERGED = 3, ST_BREAKDOWN = 4, ST_UNSUPPORTED = 6 };
+
+#define RED_THREADS 256
+#define RED_ROWS_PER_THREAD 4
+#define RED_ROWS_PER_BLOCK (RED_THREADS * RED_ROWS_PER_THREAD)
+
+void or_set_threads(int32_t nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+}
+
+int32_t or_get_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* patch type of every boundary face */
+static int32_t face_bc(const or_mesh* m, const int32_t* patch_type, int32_t b) {
+    for (int32_t p = 0; p < m->npatch; ++p)
+        if (b >= m->patch_offs[p] && b < m->patch_offs[p + 1]) return patch_type[p];
+    return BC_CALCULATED;
+}
+
+/* VolumeField::correctBoundaryConditions for fixedValue / fixedGradient / calculated
+ * (readers.hpp:43-95: zeroGradient = fixedGradient 0, noSlip = fixedValue 0).
+ * fixedGradient: b = P + g / deltaCoeff (OpenFOAM fixedGradientFvPatchField). */
+void or_bc_correct(const or_mesh* m, int32_t nc, const int32_t* patch_type, const double* ref,
+                   const double* internal, double* boundary) {
+    for (int32_t b = 0; b < m->nbf; ++b) {
+        int32_t t = face_bc(m, patch_type, b);
+        int32_t P = m->bcells[b];
+        for (int32_t k = 0; k < nc; ++k) {
+            if (t == BC_FIXED_VALUE) boundary[b * nc + k] = ref[b * nc + k];
+            else if (t == BC_FIXED_GRADIENT)
+                boundary[b * nc + k] = internal[P * nc + k] + ref[b * nc + k] / m->bdelta[b];
+        }
+    }
+}
+
+/* linear: w*(P - N) + N (pressureVelocityCoupling.cpp:249-251 form); boundary = value */
+void or_interp_linear(const or_mesh* m, int32_t nc, const double* src, const double* src_b,
+                      double* dst) {
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t P = m->own[f], N = m->nei[f];
+        for (int32_t k = 0; k < nc; ++k)
+            dst[f * nc + k] = m->w[f] * (src[P * nc + k] - src[N * nc + k]) + src[N * nc + k];
+    }
+    for (int32_t b = 0; b < m->nbf; ++b)
+        for (int32_t k = 0; k < nc; ++k) dst[(m->nif + b) * nc + k] = src_b[b * nc + k];
+}
+
+void or_interp_upwind(const or_mesh* m, int32_t nc, const double* flux, const double* src,
+                      const double* src_b, double* dst) {
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t c = flux[f] >= 0.0 ? m->own[f] : m->nei[f];
+        for (int32_t k = 0; k < nc; ++k) dst[f * nc + k] = src[c * nc + k];
+    }
+    for (int32_t b = 0; b < m->nbf; ++b)
+        for (int32_t k = 0; k < nc; ++k) dst[(m->nif + b) * nc + k] = src_b[b * nc + k];
+}
+
+static double* zalloc(size_t n) { return (double*)calloc(n ? n : 1, sizeof(double)); }
+
+/* GaussGreenDiv, Serial executor: res[own] += F*phi_f, res[nei] -= F*phi_f over
+ * internal faces in order, res[faceCell] += F_b*phi_b over boundary faces, then
+ * out += res * (coeff / V). */
+void or_div(const or_mesh* m, int32_t scheme, int32_t nc, const double* flux, const double* phi,
+            const double* phi_b, double coeff, double* out) {
+    const int32_t nf = m->nif + m->nbf;
+    double* phif = zalloc((size_t)nf * nc);
+    if (scheme == SCHEME_UPWIND) or_interp_upwind(m, nc, flux, phi, phi_b, phif);
+    else or_interp_linear(m, nc, phi, phi_b, phif);
+    double* res = zalloc((size_t)m->n * nc);
+    for (int32_t f = 0; f < m->nif; ++f)
+        for (int32_t k = 0; k < nc; ++k) {
+            double fl = flux[f] * phif[f * nc + k];
+            res[m->own[f] * nc + k] += fl;
+            res[m->nei[f] * nc + k] -= fl;
+        }
+    for (int32_t b = 0; b < m->nbf; ++b)
+        for (int32_t k = 0; k < nc; ++k)
+            res[m->bcells[b] * nc + k] += flux[m->nif + b] * phif[(m->nif + b) * nc + k];
+    for (int32_t c = 0; c < m->n; ++c) {
+        double s = coeff / m->V[c];
+        for (int32_t k = 0; k < nc; ++k) out[c * nc + k] += res[c * nc + k] * s;
+    }
+    free(res);
+    free(phif);
+}
+
+/* GaussGreenGrad: res[own] += Sf*T_f, res[nei] -= Sf*T_f, boundary += Sf_b*T_b */
+void or_grad(const or_mesh* m, const double* phi, const double* phi_b, double coeff, double* out) {
+    double* res = zalloc((size_t)m->n * 3);
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t P = m->own[f], N = m->nei[f];
+        double tf = m->w[f] * (phi[P] - phi[N]) + phi[N];
+        for (int32_t k = 0; k < 3; ++k) {
+            double v = m->Sf[3 * f + k] * tf;
+            res[3 * P + k] += v;
+            res[3 * N + k] -= v;
+        }
+    }
+    for (int32_t b = 0; b < m->nbf; ++b)
+        for (int32_t k = 0; k < 3; ++k) res[3 * m->bcells[b] + k] += m->bSf[3 * b + k] * phi_b[b];
+    for (int32_t c = 0; c < m->n; ++c) {
+        double s = coeff / m->V[c];
+        for (int32_t k = 0; k < 3; ++k) out[3 * c + k] += res[3 * c + k] * s;
+    }
+    free(res);
+}
+
+/* GaussGreenLaplacian uncorrected: flux = gamma*(|Sf|*delta)*(T_N - T_P) */
+void or_laplacian(const or_mesh* m, int32_t nc, const double* gamma, const double* phi,
+                  const double* phi_b, double coeff, double* out) {
+    double* res = zalloc((size_t)m->n * nc);
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t P = m->own[f], N = m->nei[f];
+        double g = gamma[f] * (m->magSf[f] * m->delta[f]);
+        for (int32_t k = 0; k < nc; ++k) {
+            double fl = g * (phi[N * nc + k] - phi[P * nc + k]);
+            res[P * nc + k] += fl;
+            res[N * nc + k] -= fl;
+        }
+    }
+    for (int32_t b = 0; b < m->nbf; ++b) {
+        int32_t P = m->bcells[b];
+        double g = gamma[m->nif + b] * (m->bmagSf[b] * m->bdelta[b]);
+        for (int32_t k = 0; k < nc; ++k) res[P * nc + k] += g * (phi_b[b * nc + k] - phi[P * nc + k]);
+    }
+    for (int32_t c = 0; c < m->n; ++c) {
+        double s = coeff / m->V[c];
+        for (int32_t k = 0; k < nc; ++k) out[c * nc + k] += res[c * nc + k] * s;
+    }
+    free(res);
+}
+
+void or_sngrad(const or_mesh* m, const double* phi, const double* phi_b, double* out) {
+    for (int32_t f = 0; f < m->nif; ++f) out[f] = m->delta[f] * (phi[m->nei[f]] - phi[m->own[f]]);
+    for (int32_t b = 0; b < m->nbf; ++b)
+        out[m->nif + b] = m->bdelta[b] * (phi_b[b] - phi[m->bcells[b]]);
+}
+
+/* ddt(T) + div(phi,T) = 0, upwind, forward Euler: T_new = T_old - dt*div(T_old) */
+void or_advect_euler(const or_mesh* m, const double* flux, const double* T_old,
+                     const double* T_old_b, double dt, const int32_t* patch_type,
+                     const double* ref, double* T_new, double* T_new_b) {
+    double* dv = zalloc((size_t)m->n);
+    or_div(m, SCHEME_UPWIND, 1, flux, T_old, T_old_b, 1.0, dv);
+    for (int32_t c = 0; c < m->n; ++c) T_new[c] = T_old[c] - dt * dv[c];
+    for (int32_t b = 0; b < m->nbf; ++b) T_new_b[b] = T_old_b[b];
+    or_bc_correct(m, 1, patch_type, ref, T_new, T_new_b);
+    free(dv);
+}
+
+/* la::createSparsity: row P = [lower neighbours ascending, P, upper neighbours
+ * ascending]; owner_offset[f] = slot of a_PN in row P, neighbour_offset[f] =
+ * slot of a_NP in row N (relative to the row start). Returns nnz or -1. */
+int32_t or_sparsity(const or_mesh* m, int32_t* row_offs, int32_t* col, int32_t* diag_off,
+                    int32_t* own_off, int32_t* nei_off) {
+    const int32_t n = m->n;
+    int32_t* cnt = (int32_t*)calloc((size_t)n + 1, sizeof(int32_t));
+    for (int32_t f = 0; f < m->nif; ++f) {
+        cnt[m->own[f]]++;
+        cnt[m->nei[f]]++;
+    }
+    row_offs[0] = 0;
+    for (int32_t c = 0; c < n; ++c) row_offs[c + 1] = row_offs[c] + cnt[c] + 1;
+    /* gather neighbour columns per row, then sort (rows are short) */
+    int32_t* fill = (int32_t*)calloc((size_t)n, sizeof(int32_t));
+    int32_t* slotface = (int32_t*)malloc(sizeof(int32_t) * (size_t)row_offs[n]);
+    for (int32_t c = 0; c < n; ++c) {
+        col[row_offs[c]] = c;
+        slotface[row_offs[c]] = -1;
+        fill[c] = 1;
+    }
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t P = m->own[f], N = m->nei[f];
+        col[row_offs[P] + fill[P]] = N;
+        slotface[row_offs[P] + fill[P]++] = 2 * f;
+        col[row_offs[N] + fill[N]] = P;
+        slotface[row_offs[N] + fill[N]++] = 2 * f + 1;
+    }
+    for (int32_t c = 0; c < n; ++c) {
+        int32_t b = row_offs[c], e = row_offs[c + 1];
+        for (int32_t i = b + 1; i < e; ++i) { /* insertion sort by column */
+            int32_t cc = col[i], sf = slotface[i], j = i - 1;
+            while (j >= b && col[j] > cc) {
+                col[j + 1] = col[j];
+                slotface[j + 1] = slotface[j];
+                --j;
+            }
+            col[j + 1] = cc;
+            slotface[j + 1] = sf;
+        }
+        for (int32_t i = b; i < e; ++i) {
+            if (i > b && col[i] == col[i - 1]) { /* two faces between one cell pair */
+                free(cnt); free(fill); free(slotface);
+                return -1;
+            }
+            int32_t sf = slotface[i];
+            if (sf < 0) diag_off[c] = i - b;
+            else if ((sf & 1) == 0) own_off[sf >> 1] = i - b;
+            else nei_off[sf >> 1] = i - b;
+        }
+    }
+    int32_t nnz = row_offs[n];
+    free(cnt);
+    free(fill);
+    free(slotface);
+    return nnz;
+}
+
+/* Implicit assembly.  Terms are applied in order; inside a term the face loop is
+ * in ascending face order, scattering like the reference's Serial executor.
+ *   DDT:       a_PP += c*V*(1/dt);  b_P += (c*V*(1/dt))*psi_old
+ *   SOURCE:    a_PP += (c*s)*V   (s = 1 if absent)
+ *   EXPLICIT:  b_P  -= c*E
+ *   LAPLACIAN: g = c*(gamma*(|Sf|*delta)); a_PN += g, a_PP -= g, a_NP += g, a_NN -= g;
+ *              boundary value faces: m = c*(gamma_b*(|Sf_b|*delta_b)), r = m*v_b;
+ *              fixedGradient faces:  m = 0, r = (c*(gamma_b*|Sf_b|))*g_b
+ *   DIV:       cF = c*F; upwind: owner (F>=0 ? a_PP : a_PN) += cF,
+ *              neighbour (F>=0 ? a_NP : a_NN) -= cF; linear: owner a_PP += cF*w,
+ *              a_PN += cF*(1-w), neighbour a_NP -= cF*w, a_NN -= cF*(1-w);
+ *              boundary value faces: m = 0, r = cF*v_b; fixedGradient: m = -cF,
+ *              r = cF*(g/delta_b)
+ *   boundary faces: a_PP -= m; b_P -= r; bmat += m; brhs += r. */
+void or_assemble(const or_mesh* m, const or_csr* A, int32_t nc, const or_term* terms,
+                 int32_t nterms, double dt, const int32_t* patch_type, const double* ref,
+                 const double* psi_b, double* values, double* rhs, double* bmat, double* brhs) {
+    const int32_t n = m->n;
+    memset(values, 0, sizeof(double) * (size_t)A->nnz);
+    memset(rhs, 0, sizeof(double) * (size_t)n * nc);
+    memset(bmat, 0, sizeof(double) * (size_t)m->nbf);
+    memset(brhs, 0, sizeof(double) * (size_t)m->nbf * nc);
+    const double dtInv = 1.0 / dt;
+#define DIAG(c) values[A->row_offs[c] + A->diag_off[c]]
+    for (int32_t t = 0; t < nterms; ++t) {
+        const or_term* T = &terms[t];
+        const double c = T->coeff;
+        if (T->kind == TERM_DDT) {
+            for (int32_t i = 0; i < n; ++i) {
+                double cc = c * m->V[i] * dtInv;
+                DIAG(i) += cc;
+                for (int32_t k = 0; k < nc; ++k) rhs[i * nc + k] += cc * T->cell[i * nc + k];
+            }
+        } else if (T->kind == TERM_SOURCE) {
+            for (int32_t i = 0; i < n; ++i) DIAG(i) += (T->cell ? c * T->cell[i] : c) * m->V[i];
+        } else if (T->kind == TERM_EXPLICIT) {
+            for (int32_t i = 0; i < n * nc; ++i) rhs[i] -= c * T->cell[i];
+        } else if (T->kind == TERM_LAPLACIAN) {
+            for (int32_t f = 0; f < m->nif; ++f) {
+                int32_t P = m->own[f], N = m->nei[f];
+                double g = c * (T->face[f] * (m->magSf[f] * m->delta[f]));
+                values[A->row_offs[P] + A->own_off[f]] += g;
+                DIAG(P) -= g;
+                values[A->row_offs[N] + A->nei_off[f]] += g;
+                DIAG(N) -= g;
+            }
+            for (int32_t b = 0; b < m->nbf; ++b) {
+                int32_t P = m->bcells[b], bt = face_bc(m, patch_type, b);
+                double gb = T->face[m->nif + b];
+                double mm;
+                if (bt == BC_FIXED_GRADIENT) {
+                    mm = 0.0;
+                    double q = c * (gb * m->bmagSf[b]);
+                    for (int32_t k = 0; k < nc; ++k) {
+                        double r = q * ref[b * nc + k];
+                        rhs[P * nc + k] -= r;
+                        brhs[b * nc + k] += r;
+                    }
+                } else {
+                    mm = c * (gb * (m->bmagSf[b] * m->bdelta[b]));
+                    for (int32_t k = 0; k < nc; ++k) {
+                        double r = mm * psi_b[b * nc + k];
+                        rhs[P * nc + k] -= r;
+                        brhs[b * nc + k] += r;
+                    }
+                }
+                DIAG(P) -= mm;
+                bmat[b] += mm;
+            }
+        } else if (T->kind == TERM_DIV) {
+            for (int32_t f = 0; f < m->nif; ++f) {
+                int32_t P = m->own[f], N = m->nei[f];
+                double F = T->face[f], cF = c * F;
+                if (T->scheme == SCHEME_UPWIND) {
+                    if (F >= 0.0) {
+                        DIAG(P) += cF;
+                        values[A->row_offs[N] + A->nei_off[f]] -= cF;
+                    } else {
+                        values[A->row_offs[P] + A->own_off[f]] += cF;
+                        DIAG(N) -= cF;
+                    }
+                } else {
+                    double w = m->w[f], wm = 1.0 - w;
+                    DIAG(P) += cF * w;
+                    values[A->row_offs[P] + A->own_off[f]] += cF * wm;
+                    values[A->row_offs[N] + A->nei_off[f]] -= cF * w;
+                    DIAG(N) -= cF * wm;
+                }
+            }
+            for (int32_t b = 0; b < m->nbf; ++b) {
+                int32_t P = m->bcells[b], bt = face_bc(m, patch_type, b);
+                double cF = c * T->face[m->nif + b];
+                double mm;
+                if (bt == BC_FIXED_GRADIENT) {
+                    mm = -cF;
+                    for (int32_t k = 0; k < nc; ++k) {
+                        double r = cF * (ref[b * nc + k] / m->bdelta[b]);
+                        rhs[P * nc + k] -= r;
+                        brhs[b * nc + k] += r;
+                    }
+                } else {
+                    mm = 0.0;
+                    for (int32_t k = 0; k < nc; ++k) {
+                        double r = cF * psi_b[b * nc + k];
+                        rhs[P * nc + k] -= r;
+                        brhs[b * nc + k] += r;
+                    }
+                }
+                DIAG(P) -= mm;
+                bmat[b] += mm;
+            }
+        }
+    }
+#undef DIAG
+}
+
+/* PDESolver::SetReference (expression.hpp:102-111) */
+void or_set_reference(const or_csr* A, double* values, double* rhs, int32_t r, double v) {
+    int32_t d = A->row_offs[r] + A->diag_off[r];
+    double dv = values[d];
+    rhs[r] += dv * v;
+    values[d] += dv;
+}
+
+/* out = A x - b, row sums as fma chains in column order */
+void or_apply_operator(const or_csr* A, const double* values, const double* rhs, int32_t nc,
+                       const double* x, double* out) {
+    for (int32_t i = 0; i < A->n; ++i)
+        for (int32_t k = 0; k < nc; ++k) {
+            double s = 0.0;
+            for (int32_t j = A->row_offs[i]; j < A->row_offs[i + 1]; ++j)
+                s = fma(values[j], x[A->col[j] * nc + k], s);
+            out[i * nc + k] = s - rhs[i * nc + k];
+        }
+}
+
+/* ---------------------------------------------------------------- reductions */
+/* The GPU reduction tree: thread t of a 256-thread block owns rows
+ * base + (t/32)*128 + j*32 + t%32, j = 0..3; its partial is a sequential sum;
+ * then lane l of warp 0 sums partials l, l+32, ..., l+224 in order and a
+ * butterfly (xor 16, 8, 4, 2, 1) finishes.  Stage two: thread t sums block
+ * partials t, t+256, ... and the same block tree follows. */
+static double block_tree(const double* tp) {
+    double v[32], nv[32];
+    for (int l = 0; l < 32; ++l) {
+        double s = tp[l];
+        for (int k = 1; k < RED_THREADS / 32; ++k) s = s + tp[l + 32 * k];
+        v[l] = s;
+    }
+    for (int off = 16; off >= 1; off >>= 1) {
+        for (int l = 0; l < 32; ++l) nv[l] = v[l] + v[l ^ off];
+        memcpy(v, nv, sizeof v);
+    }
+    return v[0];
+}
+
+static double final_tree(int32_t nb, const double* partials) {
+    double tp[RED_THREADS];
+    for (int t = 0; t < RED_THREADS; ++t) {
+        double a = 0.0;
+        for (int32_t i = t; i < nb; i += RED_THREADS) a = a + partials[i];
+        tp[t] = a;
+    }
+    return block_tree(tp);
+}
+
+static inline int32_t red_row(int32_t blk, int t, int j) {
+    return blk * RED_ROWS_PER_BLOCK + (t >> 5) * 128 + j * 32 + (t & 31);
+}
+
+static int32_t nblocks_of(int32_t n) { return (n + RED_ROWS_PER_BLOCK - 1) / RED_ROWS_PER_BLOCK; }
+
+double or_dot_tree(int32_t n, const double* a, const double* b) {
+    int32_t nb = nblocks_of(n);
+    double* part = zalloc((size_t)nb);
+#pragma omp parallel for schedule(static)
+    for (int32_t blk = 0; blk < nb; ++blk) {
+        double tp[RED_THREADS];
+        for (int t = 0; t < RED_THREADS; ++t) {
+            double acc = 0.0;
+            for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
+                int32_t i = red_row(blk, t, j);
+                if (i < n) acc = fma(a[i], b[i], acc);
+            }
+            tp[t] = acc;
+        }
+        part[blk] = block_tree(tp);
+    }
+    double r = final_tree(nb, part);
+    free(part);
+    return r;
+}
+
+/* ------------------------------------------------------------ FP64 Jacobi CG */
+static void spmv_row_fma(const or_csr* A, const double* val, const double* x, int32_t i, double* s) {
+    double acc = 0.0;
+    for (int32_t j = A->row_offs[i]; j < A->row_offs[i + 1]; ++j) acc = fma(val[j], x[A->col[j]], acc);
+    *s = acc;
+}
+
+static int32_t solve_fp64(const or_csr* A, const double* val, const double* b, double* x,
+                          const or_solver_cfg* cfg, or_solver_stats* st) {
+    const int32_t n = A->n, nb = nblocks_of(n);
+    double *dinv = zalloc(n), *r = zalloc(n), *p = zalloc(n), *q = zalloc(n);
+    double *pa = zalloc(nb), *pb = zalloc(nb);
+    for (int32_t i = 0; i < n; ++i) dinv[i] = 1.0 / val[A->row_offs[i] + A->diag_off[i]];
+    /* init: r = b - A x; z = dinv*r; p = z; rz, rr */
+#pragma omp parallel for schedule(static)
+    for (int32_t blk = 0; blk < nb; ++blk) {
+        double ta[RED_THREADS], tb[RED_THREADS];
+        for (int t = 0; t < RED_THREADS; ++t) {
+            double arz = 0.0, arr = 0.0;
+            for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
+                int32_t i = red_row(blk, t, j);
+                if (i >= n) continue;
+                double s;
+                spmv_row_fma(A, val, x, i, &s);
+                double ri = b[i] - s, zi = dinv[i] * ri;
+                r[i] = ri;
+                p[i] = zi;
+                arz = fma(ri, zi, arz);
+                arr = fma(ri, ri, arr);
+            }
+            ta[t] = arz;
+            tb[t] = arr;
+        }
+        pa[blk] = block_tree(ta);
+        pb[blk] = block_tree(tb);
+    }
+    double rz = final_tree(nb, pa), rr = final_tree(nb, pb);
+    double res0 = sqrt(rr), res = res0;
+    double tol = cfg->rel_tol * res0;
+    if (cfg->abs_tol > tol) tol = cfg->abs_tol;
+    int32_t it = 0, status = ST_OK;
+    int done = !(res > tol) || res == 0.0;
+    if (!done && cfg->max_iter <= 0) { done = 1; status = ST_NOT_CONVERGED; }
+    while (!done) {
+        /* q = A p ; pq */
+#pragma omp parallel for schedule(static)
+        for (int32_t blk = 0; blk < nb; ++blk) {
+            double ta[RED_THREADS];
+            for (int t = 0; t < RED_THREADS; ++t) {
+                double acc = 0.0;
+                for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
+                    int32_t i = red_row(blk, t, j);
+                    if (i >= n) continue;
+                    double s;
+                    spmv_row_fma(A, val, p, i, &s);
+                    q[i] = s;
+                    acc = fma(p[i], s, acc);
+                }
+                ta[t] = acc;
+            }
+            pa[blk] = block_tree(ta);
+        }
+        double pq = final_tree(nb, pa);
+        double alpha = rz / pq;
+        if (pq == 0.0 || !isfinite(alpha)) { status = ST_BREAKDOWN; break; }
+        /* x += alpha p ; r -= alpha q ; z = dinv r ; rz, rr */
+#pragma omp parallel for schedule(static)
+        for (int32_t blk = 0; blk < nb; ++blk) {
+            double ta[RED_THREADS], tb[RED_THREADS];
+            for (int t = 0; t < RED_THREADS; ++t) {
+                double arz = 0.0, arr = 0.0;
+                for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
+                    int32_t i = red_row(blk, t, j);
+                    if (i >= n) continue;
+                    x[i] = fma(alpha, p[i], x[i]);
+                    double ri = fma(-alpha, q[i], r[i]);
+                    r[i] = ri;
+                    double zi = dinv[i] * ri;
+                    arz = fma(ri, zi, arz);
+                    arr = fma(ri, ri, arr);
+                }
+                ta[t] = arz;
+                tb[t] = arr;
+            }
+            pa[blk] = block_tree(ta);
+            pb[blk] = block_tree(tb);
+        }
+        double rzn = final_tree(nb, pa);
+        rr = final_tree(nb, pb);
+        res = sqrt(rr);
+        ++it;
+        double beta = rzn / rz;
+        rz = rzn;
+        if (!isfinite(res)) { status = ST_BREAKDOWN; break; }
+        if (!(res > tol)) break;
+        if (it >= cfg->max_iter) { status = ST_NOT_CONVERGED; break; }
+        /* p = z + beta p */
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < n; ++i) p[i] = fma(beta, p[i], dinv[i] * r[i]);
+    }
+    st->init_res_norm = res0;
+    st->final_res_norm = res;
+    st->num_iter = it;
+    st->num_outer = 0;
+    st->status = status;
+    free(dinv); free(r); free(p); free(q); free(pa); free(pb);
+    return status;
+}
+
+/* ----------------------------------------- mixed precision iterative refinement
+ * Outer (FP64): r = b - A x (fma row chains), ||r||, test; inner (FP32): CG on the
+ * Jacobi-scaled system  S A S y = S r,  S = diag(1/sqrt|a_ii|), from y = 0; the
+ * scaled diagonal is sign(a_ii) (all diagonals must share one sign); update
+ * x += S y in FP64.  Scaled off-diagonals are rounded once to float:
+ * ahat_ij = (float)((a_ij * s_i) * s_j).  Row sums: q = sign*p_i, then fmaf over
+ * the off-diagonals in column order.  Dots: per-thread fmaf in float, converted
+ * to double for the block and final trees. */
+static double dot_tree_f(int32_t n, const float* a, const float* b, double* part) {
+    int32_t nb = nblocks_of(n);
+#pragma omp parallel for schedule(static)
+    for (int32_t blk = 0; blk < nb; ++blk) {
+        double tp[RED_THREADS];
+        for (int t = 0; t < RED_THREADS; ++t) {
+            float acc = 0.0f;
+            for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
+                int32_t i = red_row(blk, t, j);
+                if (i < n) acc = fmaf(a[i], b[i], acc);
+            }
+            tp[t] = (double)acc;
+        }
+        part[blk] = block_tree(tp);
+    }
+    return final_tree(nb, part);
+}
+
+static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, double* x,
+                           const or_solver_cfg* cfg, or_solver_stats* st) {
+    const int32_t n = A->n, nb = nblocks_of(n), nnz = A->nnz;
+    double* s = zalloc(n);
+    float* ah = (float*)calloc((size_t)nnz, sizeof(float));
+    double dsign = 0.0;
+    for (int32_t i = 0; i < n; ++i) {
+        double d = val[A->row_offs[i] + A->diag_off[i]];
+        double sg = d > 0 ? 1.0 : (d < 0 ? -1.0 : 0.0);
+        if (i == 0) dsign = sg;
+        if (sg == 0.0 || sg != dsign) {
+            free(s); free(ah);
+            st->status = ST_UNSUPPORTED;
+            return ST_UNSUPPORTED;
+        }
+        s[i] = 1.0 / sqrt(fabs(d));
+    }
+    for (int32_t i = 0; i < n; ++i)
+        for (int32_t j = A->row_offs[i]; j < A->row_offs[i + 1]; ++j)
+            ah[j] = (float)((val[j] * s[i]) * s[A->col[j]]);
+    const float fs = (float)dsign;
+    double *r = zalloc(n), *part = zalloc(nb);
+    float *rh = (float*)calloc(n, sizeof(float)), *y = (float*)calloc(n, sizeof(float));
+    float *p = (float*)calloc(n, sizeof(float)), *q = (float*)calloc(n, sizeof(float));
+    int32_t total = 0, outer = 0, status = ST_OK;
+    double res0 = 0.0, res = 0.0, tol = 0.0;
+    for (;;) {
+        /* FP64 residual and the scaled FP32 right-hand side */
+#pragma omp parallel for schedule(static)
+        for (int32_t blk = 0; blk < nb; ++blk) {
+            double tp[RED_THREADS];
+            for (int t = 0; t < RED_THREADS; ++t) {
+                double arr = 0.0;
+                for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
+                    int32_t i = red_row(blk, t, j);
+                    if (i >= n) continue;
+                    double sm;
+                    spmv_row_fma(A, val, x, i, &sm);
+                    double ri = b[i] - sm;
+                    r[i] = ri;
+                    arr = fma(ri, ri, arr);
+                    rh[i] = (float)(s[i] * ri);
+                }
+                tp[t] = arr;
+            }
+            part[blk] = block_tree(tp);
+        }
+        res = sqrt(final_tree(nb, part));
+        if (outer == 0) {
+            res0 = res;
+            tol = cfg->rel_tol * res0;
+            if (cfg->abs_tol > tol) tol = cfg->abs_tol;
+        }
+        if (!isfinite(res)) { status = ST_BREAKDOWN; break; }
+        if (!(res > tol) || res == 0.0) break;
+        if (outer >= cfg->max_outer || total >= cfg->max_iter) { status = ST_NOT_CONVERGED; break; }
+        /* inner CG from y = 0 */
+        for (int32_t i = 0; i < n; ++i) { y[i] = 0.0f; p[i] = rh[i]; }
+        double rho = dot_tree_f(n, rh, rh, part);
+        double rho0 = rho, itol = cfg->inner_rel_tol * cfg->inner_rel_tol * rho0;
+        int32_t it = 0;
+        int brk = 0;
+        while (rho > itol && it < cfg->inner_max_iter && total < cfg->max_iter) {
+#pragma omp parallel for schedule(static)
+            for (int32_t i = 0; i < n; ++i) {
+                float acc = fs * p[i];
+                for (int32_t j = A->row_offs[i]; j < A->row_offs[i + 1]; ++j)
+                    if (A->col[j] != i) acc = fmaf(ah[j], p[A->col[j]], acc);
+                q[i] = acc;
+            }
+            double pq = dot_tree_f(n, p, q, part);
+            double alpha = rho / pq;
+            if (pq == 0.0 || !isfinite(alpha)) { brk = 1; break; }
+            float fa = (float)alpha;
+            for (int32_t i = 0; i < n; ++i) {
+                y[i] = fmaf(fa, p[i], y[i]);
+                rh[i] = fmaf(-fa, q[i], rh[i]);
+            }
+            double rhon = dot_tree_f(n, rh, rh, part);
+            float fb = (float)(rhon / rho);
+            rho = rhon;
+            ++it;
+            ++total;
+            for (int32_t i = 0; i < n; ++i) p[i] = fmaf(fb, p[i], rh[i]);
+        }
+        if (brk && it == 0) { status = ST_BREAKDOWN; break; }
+        for (int32_t i = 0; i < n; ++i) x[i] = fma(s[i], (double)y[i], x[i]);
+        ++outer;
+    }
+    st->init_res_norm = res0;
+    st->final_res_norm = res;
+    st->num_iter = total;
+    st->num_outer = outer;
+    st->status = status;
+    free(s); free(ah); free(r); free(part); free(rh); free(y); free(p); free(q);
+    return status;
+}
+
+int32_t or_solve(const or_csr* A, const double* values, const double* rhs, double* x,
+                 const or_solver_cfg* cfg, or_solver_stats* stats) {
+    if (cfg->precision == 1) return solve_mixed(A, values, rhs, x, cfg, stats);
+    return solve_fp64(A, values, rhs, x, cfg, stats);
+}
+
+/* ------------------------------------------------------------------ PISO */
+/* computeRAUandHByA (pressureVelocityCoupling.cpp:65-128), Serial order */
+void or_rau_hbya(const or_mesh* m, const or_csr* A, const double* val, const double* rhs,
+                 const double* U, double* rAU, double* H) {
+    for (int32_t c = 0; c < m->n; ++c) rAU[c] = m->V[c] / val[A->row_offs[c] + A->diag_off[c]];
+    memset(H, 0, sizeof(double) * 3 * (size_t)m->n);
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t P = m->own[f], N = m->nei[f];
+        double lower = val[A->row_offs[N] + A->nei_off[f]];
+        double upper = val[A->row_offs[P] + A->own_off[f]];
+        for (int32_t k = 0; k < 3; ++k) {
+            H[3 * N + k] -= lower * U[3 * P + k];
+            H[3 * P + k] -= upper * U[3 * N + k];
+        }
+    }
+    for (int32_t c = 0; c < m->n; ++c) {
+        double sc = rAU[c] / m->V[c];
+        for (int32_t k = 0; k < 3; ++k) {
+            H[3 * c + k] += rhs[3 * c + k];
+            H[3 * c + k] *= sc;
+        }
+    }
+}
+
+void or_constrain_hbya(const or_mesh* m, const int32_t* assignable, const double* U_b,
+                       double* H_b) {
+    for (int32_t p = 0; p < m->npatch; ++p)
+        if (!assignable[p])
+            for (int32_t b = m->patch_offs[p]; b < m->patch_offs[p + 1]; ++b)
+                for (int32_t k = 0; k < 3; ++k) H_b[3 * b + k] = U_b[3 * b + k];
+}
+
+/* flux (pressureVelocityCoupling.cpp:215-267) */
+void or_flux_vec(const or_mesh* m, const double* U, const double* U_b, double* out) {
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t P = m->own[f], N = m->nei[f];
+        double t[3];
+        for (int32_t k = 0; k < 3; ++k) t[k] = m->w[f] * (U[3 * P + k] - U[3 * N + k]) + U[3 * N + k];
+        out[f] = m->Sf[3 * f] * t[0] + m->Sf[3 * f + 1] * t[1] + m->Sf[3 * f + 2] * t[2];
+    }
+    for (int32_t b = 0; b < m->nbf; ++b)
+        out[m->nif + b] = m->bSf[3 * b] * U_b[3 * b] + m->bSf[3 * b + 1] * U_b[3 * b + 1] +
+                          m->bSf[3 * b + 2] * U_b[3 * b + 2];
+}
+
+/* updateFaceVelocity (pressureVelocityCoupling.cpp:131-197) */
+void or_face_update(const or_mesh* m, const or_csr* A, const double* val, const double* bmat,
+                    const double* brhs, const double* phiHbyA, const double* p, double* phi) {
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t P = m->own[f], N = m->nei[f];
+        double upper = val[A->row_offs[N] + A->nei_off[f]];
+        double lower = val[A->row_offs[P] + A->own_off[f]];
+        phi[f] = phiHbyA[f] - (upper * p[N] - lower * p[P]);
+    }
+    for (int32_t b = 0; b < m->nbf; ++b) {
+        double bflux = brhs[b] - bmat[b] * p[m->bcells[b]];
+        phi[m->nif + b] = phiHbyA[m->nif + b] - bflux;
+    }
+}
+
+/* updateVelocity (pressureVelocityCoupling.cpp:199-213) */
+void or_velocity_update(const or_mesh* m, const double* H, const double* rAU, const double* p,
+                        const double* p_b, double* U) {
+    double* g = zalloc((size_t)3 * m->n);
+    or_grad(m, p, p_b, 1.0, g);
+    for (int32_t c = 0; c < m->n; ++c)
+        for (int32_t k = 0; k < 3; ++k) U[3 * c + k] = H[3 * c + k] - rAU[c] * g[3 * c + k];
+    free(g);
+}

@@ -1,0 +1,195 @@
+"""GPU implicit assembly, LinearSystem utilities and Krylov solves against the
+CPU oracle.
+
+Assembly, SetReference, applyOperator and diag are bit-exact.  The FP64
+Jacobi-CG follows the same reduction tree as the oracle, so its iterates,
+iteration count and residual norms are bit-exact too.  The mixed-precision
+solve must reach the same 1e-8 relative FP64 residual (checked by an FP64
+residual computed on the CPU) and its error against the FP64 solution is
+bounded by the conditioning of the system.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_polymesh
+from foamadapter_gb300 import abi, mesh, neon
+from foamadapter_gb300.mesh import DeviceMesh
+from oracle.pyoracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def heat_case(nx=12, ny=10, nz=8, jitter=0.1, seed=12345, dt=0.01):
+    hm = mesh.box(nx, ny, nz, jitter=jitter, seed=seed)
+    rng = np.random.default_rng(seed)
+    k = np.exp(0.5 * rng.standard_normal(hm.n))
+    bcs = [("fixedValue", 400.0)] + [("zeroGradient", 0.0)] * (hm.npatch - 1)
+    return hm, k, bcs, dt
+
+
+def csr_of(o, values_csr):
+    return values_csr
+
+
+def assemble_both(hm, dm, terms_fn, bcs, ncomp=1, dt=0.01, seed=0):
+    rng = np.random.default_rng(seed)
+    o = Oracle(hm)
+    T = neon.VolumeField(dm, 300.0 + rng.standard_normal(hm.n * ncomp), bcs, ncomp)
+    gpu_terms, host_terms = terms_fn(dm, T, rng)
+    ls = neon.LinearSystem(dm, ncomp)
+    ls.assemble(gpu_terms, dt, T)
+    v, r, bm, br = [t.cpu().numpy() for t in ls.export()]
+    ov, orr, obm, obr = o.assemble(ncomp, host_terms, dt, T.types, T.ref.cpu().numpy(),
+                                   T.boundary.cpu().numpy())
+    return ls, T, o, (v, r, bm, br), (ov, orr, obm, obr)
+
+
+def test_sparsity_matches_oracle(cuda):
+    hm, _ = load_polymesh("setup_stencil3D")
+    dm = DeviceMesh(hm)
+    gpu = dm.sparsity()
+    host = Oracle(hm).csr_arrays()
+    for a, b in zip(gpu, host):
+        np.testing.assert_array_equal(a, b)
+    assert gpu[0][-1] == 135
+
+
+@pytest.mark.parametrize("ncomp", [1, 3])
+def test_assembly_all_terms_bit_exact(cuda, ncomp):
+    hm = mesh.box(7, 6, 5, jitter=0.12, seed=9)
+    dm = DeviceMesh(hm)
+    nf = hm.nif + hm.nbf
+    bcs = [("fixedValue", 400.0), ("zeroGradient", 0.0), ("fixedGradient", 2.0),
+           ("fixedValue", 1.5), ("calculated", 0.0), ("zeroGradient", 0.0)]
+
+    def terms(dm, T, rng):
+        old = rng.standard_normal(hm.n * ncomp)
+        gamma = np.exp(rng.standard_normal(nf))
+        F = rng.standard_normal(nf)
+        s = rng.random(hm.n)
+        E = rng.standard_normal(hm.n * ncomp)
+        g = [neon.ddt(neon.dev(old)), neon.laplacian(neon.SurfaceField(dm, gamma), -0.8),
+             neon.div(neon.SurfaceField(dm, F), "upwind", 1.3), neon.div(neon.SurfaceField(dm, F), "linear", 0.6),
+             neon.source(0.4, neon.dev(s)), neon.explicit(neon.dev(E), -1.0)]
+        h = [(abi.TERM_DDT, 0, 1.0, old, None), (abi.TERM_LAPLACIAN, 0, -0.8, None, gamma),
+             (abi.TERM_DIV, abi.SCHEME_UPWIND, 1.3, None, F), (abi.TERM_DIV, abi.SCHEME_LINEAR, 0.6, None, F),
+             (abi.TERM_SOURCE, 0, 0.4, s, None), (abi.TERM_EXPLICIT, 0, -1.0, E, None)]
+        g[0].keep = old
+        return g, h
+
+    ls, T, o, gpu, ref = assemble_both(hm, dm, terms, bcs, ncomp)
+    for a, b in zip(gpu, ref):
+        np.testing.assert_array_equal(a, b)
+    # diag and applyOperator (A x - b)
+    v = gpu[0]
+    ro, col, do, oo, no = o.csr_arrays()
+    np.testing.assert_array_equal(ls.diag().cpu().numpy(), v[ro[:-1] + do])
+    x = np.random.default_rng(1).standard_normal(hm.n * ncomp)
+    np.testing.assert_array_equal(ls.apply(neon.dev(x)).cpu().numpy(), o.apply_operator(v, gpu[1], ncomp, x))
+
+
+def test_ddt_and_source_semantics(cuda):
+    """Implicit ddt: diag V/dt, rhs V/dt*T_old, A T - b = V (T - T_old)/dt
+    (test/test_implicitOperators.cpp:170-234); implicit source diag = c*V (:236-286)."""
+    hm = mesh.box(5, 4, 3, jitter=0.1, seed=2)
+    dm = DeviceMesh(hm)
+    T = neon.VolumeField(dm, np.arange(hm.n, dtype=float))
+    old = T.host() - 1.0
+    ls = neon.LinearSystem(dm)
+    ls.assemble([neon.ddt(neon.dev(old))], 1.0, T)
+    np.testing.assert_allclose(ls.apply(T.internal).cpu().numpy(), hm.V, rtol=1e-14, atol=0)
+    ls.assemble([neon.source(2.0)], 1.0, T)
+    np.testing.assert_array_equal(ls.diag().cpu().numpy(), 2.0 * hm.V)
+
+
+def test_laplacian_matches_explicit_operator(cuda):
+    """A T - b of the implicit laplacian equals the explicit laplacian times V
+    (the check of test/test_implicitOperators.cpp:344-396, 1e-14)."""
+    hm = mesh.box(8, 6, 5, jitter=0.1, seed=4)
+    dm = DeviceMesh(hm)
+    rng = np.random.default_rng(0)
+    T = neon.VolumeField(dm, rng.standard_normal(hm.n), [("fixedValue", 1.0)] + [("zeroGradient", 0)] * 5)
+    gamma = neon.SurfaceField(dm, np.full(hm.nif + hm.nbf, 0.1))
+    ls = neon.LinearSystem(dm)
+    ls.assemble([neon.laplacian(gamma)], 1.0, T)
+    imp = ls.apply(T.internal).cpu().numpy()
+    exp = neon.GaussGreenLaplacian(dm).laplacian(torch.zeros(hm.n, dtype=torch.float64, device="cuda"),
+                                                 gamma, T).cpu().numpy() * hm.V
+    np.testing.assert_allclose(imp, exp, rtol=0, atol=1e-14 * max(1.0, np.abs(exp).max()))
+
+
+def test_set_reference(cuda):
+    hm = mesh.box(6, 6, 1, two_d=True)
+    dm = DeviceMesh(hm)
+    p = neon.VolumeField(dm, np.zeros(hm.n), [("zeroGradient", 0)] * 4)
+    gamma = neon.SurfaceField(dm, np.ones(hm.nif + hm.nbf))
+    ls = neon.LinearSystem(dm)
+    ls.assemble([neon.laplacian(gamma)], 1.0, p)
+    v0 = ls.export()
+    ls.setReference(3, 0.25)
+    v1 = ls.export()
+    o = Oracle(hm)
+    ov, orr = v0[0].cpu().numpy().copy(), v0[1].cpu().numpy().copy()
+    o.set_reference(ov, orr, 3, 0.25)
+    np.testing.assert_array_equal(v1[0].cpu().numpy(), ov)
+    np.testing.assert_array_equal(v1[1].cpu().numpy(), orr)
+
+
+def solve_case(nx=14, ny=12, nz=10):
+    hm, k, bcs, dt = heat_case(nx, ny, nz)
+    dm = DeviceMesh(hm)
+    T = neon.VolumeField(dm, np.full(hm.n, 300.0), bcs)
+    o = Oracle(hm)
+    kf = o.interp_linear(1, k, k[hm.bcells].copy())
+    gamma = neon.SurfaceField(dm, kf)
+    ls = neon.LinearSystem(dm)
+    ls.assemble([neon.ddt(T.internal.clone()), neon.laplacian(gamma, -1.0)], dt, T)
+    v, r, bm, br = [t.cpu().numpy() for t in ls.export()]
+    return hm, dm, T, o, ls, v, r
+
+
+def test_pcg_fp64_bit_exact(cuda):
+    hm, dm, T, o, ls, v, r = solve_case()
+    x = T.internal.clone()
+    st = ls.solve(x, rel_tol=1e-8, max_iter=1000)
+    xo = np.full(hm.n, 300.0)
+    so = o.solve(v, r, xo, rel_tol=1e-8, max_iter=1000)
+    assert st.status == abi.OK and so.status == 0
+    assert st.num_iter == so.num_iter > 5
+    assert st.init_res_norm == so.init_res_norm and st.final_res_norm == so.final_res_norm
+    np.testing.assert_array_equal(x.cpu().numpy(), xo)
+    true = np.linalg.norm(o.apply_operator(v, r, 1, xo))
+    assert true <= 1.01e-8 * so.init_res_norm
+
+
+def test_pcg_iteration_cap_and_abs_tol(cuda):
+    hm, dm, T, o, ls, v, r = solve_case(8, 8, 8)
+    x = T.internal.clone()
+    st = ls.solve(x, rel_tol=1e-12, max_iter=3)
+    assert st.status == abi.ERR_NOT_CONVERGED and st.num_iter == 3
+    x = T.internal.clone()
+    st = ls.solve(x, rel_tol=0.0, abs_tol=1e300, max_iter=50)
+    assert st.status == abi.OK and st.num_iter == 0
+
+
+@pytest.mark.parametrize("inner", [1e-2, 1e-4])
+def test_mixed_ir_reaches_fp64_residual(cuda, inner):
+    hm, dm, T, o, ls, v, r = solve_case()
+    x64 = T.internal.clone()
+    ls.solve(x64, rel_tol=1e-8)
+    x = T.internal.clone()
+    st = ls.solve(x, rel_tol=1e-8, precision=abi.PREC_MIXED_IR, inner_rel_tol=inner, inner_max_iter=500,
+                  max_outer=40)
+    assert st.status == abi.OK, st.status
+    xh = x.cpu().numpy()
+    true = np.linalg.norm(o.apply_operator(v, r, 1, xh))
+    assert true <= 1.01e-8 * st.init_res_norm
+    # the same algorithm on the CPU (FP32 inner CG emulated with fmaf) gives the same bits
+    xo = np.full(hm.n, 300.0)
+    so = o.solve(v, r, xo, rel_tol=1e-8, precision=1, inner_rel_tol=inner, inner_max_iter=500, max_outer=40)
+    assert (st.num_iter, st.num_outer) == (so.num_iter, so.num_outer)
+    np.testing.assert_array_equal(xh, xo)
+    # error against the FP64 solve
+    err = np.abs(xh - x64.cpu().numpy()).max()
+    assert err < 1e-6 * 400.0
