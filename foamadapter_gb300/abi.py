@@ -19,7 +19,7 @@ OK, ERR_INVALID_ARG, ERR_OOM, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_CUDA, ERR_UN
     ERR_BUDGET, ERR_CANCELLED = range(9)
 BC_CALCULATED, BC_FIXED_VALUE, BC_FIXED_GRADIENT = 0, 1, 2
 SCHEME_LINEAR, SCHEME_UPWIND = 0, 1
-TERM_DDT, TERM_LAPLACIAN, TERM_DIV, TERM_SOURCE, TERM_EXPLICIT = range(5)
+TERM_DDT, TERM_LAPLACIAN, TERM_DIV, TERM_SOURCE, TERM_EXPLICIT, TERM_DIV_FLUX = range(6)
 PREC_FP64, PREC_MIXED_IR = 0, 1
 
 vp = C.c_void_p

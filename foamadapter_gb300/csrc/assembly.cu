@@ -66,6 +66,16 @@ __global__ void __launch_bounds__(kThreads)
         } else if (T.kind == FVGB_TERM_EXPLICIT) {
 #pragma unroll
             for (int k = 0; k < NC; ++k) r[k] = r[k] - cf * __ldg(&T.cell[c * NC + k]);
+        } else if (T.kind == FVGB_TERM_DIV_FLUX) {
+            double dv = 0.0;  // sum of +-F over the row's faces, ascending face order
+            for (int j = 0; j < gw; ++j) {
+                const int code = __ldg(&m.g_code[gbase + j * 32 + lane]);
+                if (code == FVGB_PAD) break;
+                if (code >= m.nif || code >= 0) dv = dv + __ldg(&T.face[code]);
+                else dv = dv - __ldg(&T.face[-code - 1]);
+            }
+#pragma unroll
+            for (int k = 0; k < NC; ++k) r[k] = r[k] - cf * dv;
         } else if (T.kind == FVGB_TERM_LAPLACIAN || T.kind == FVGB_TERM_DIV) {
             const bool lap = T.kind == FVGB_TERM_LAPLACIAN;
             for (int j = 0; j < gw; ++j) {
@@ -277,12 +287,13 @@ extern "C" fvgb_status fvgb_assemble(fvgb_ls* ls, const fvgb_term* terms, int32_
     bool needs_b = false, needs_dt = false;
     for (int i = 0; i < nterms; ++i) {
         const fvgb_term& t = terms[i];
-        FVGB_CHECK_ARG(t.kind >= FVGB_TERM_DDT && t.kind <= FVGB_TERM_EXPLICIT, "fvgb_assemble: unknown term kind");
+        FVGB_CHECK_ARG(t.kind >= FVGB_TERM_DDT && t.kind <= FVGB_TERM_DIV_FLUX, "fvgb_assemble: unknown term kind");
         if (t.kind == FVGB_TERM_DDT) {
             FVGB_CHECK_ARG(t.cell, "fvgb_assemble: ddt needs the old-time field");
             needs_dt = true;
         }
         if (t.kind == FVGB_TERM_EXPLICIT) FVGB_CHECK_ARG(t.cell, "fvgb_assemble: explicit term needs its values");
+        if (t.kind == FVGB_TERM_DIV_FLUX) FVGB_CHECK_ARG(t.face, "fvgb_assemble: flux divergence needs the flux");
         if (t.kind == FVGB_TERM_LAPLACIAN || t.kind == FVGB_TERM_DIV) {
             FVGB_CHECK_ARG(t.face, "fvgb_assemble: laplacian/div need a surface field");
             needs_b = true;

@@ -262,7 +262,7 @@ __global__ void k_finish(SolverState* st) {
     fvgb_solver_stats s;
     s.init_res_norm = st->res0;
     s.final_res_norm = st->res;
-    s.num_iter = st->iter;
+    s.num_iter = st->iter + st->total;  // FP64 counts iter, mixed counts total (the other is 0)
     s.num_outer = st->outer;
     s.status = st->status;
     s.reserved = 0;

@@ -201,6 +201,11 @@ def explicit(values: torch.Tensor, coeff: float = 1.0) -> Term:
     return Term(abi.TERM_EXPLICIT, coeff, cell=values)
 
 
+def div_flux(flux: SurfaceField, coeff: float = 1.0) -> Term:
+    """dsl::exp::div(phi) of a face flux, volume integrated, into the rhs."""
+    return Term(abi.TERM_DIV_FLUX, coeff, face=flux.values)
+
+
 class LinearSystem:
     """la::LinearSystem on the mesh pattern (device resident)."""
 

@@ -177,7 +177,9 @@ typedef enum fvgb_term_kind {
     FVGB_TERM_LAPLACIAN = 1,       /* implicit laplacian(gamma, psi) uncorrected       */
     FVGB_TERM_DIV = 2,             /* implicit div(flux, psi), linear or upwind        */
     FVGB_TERM_SOURCE = 3,          /* implicit source: diag += coeff*s_P*V_P           */
-    FVGB_TERM_EXPLICIT = 4         /* rhs -= coeff*E_P (E already volume integrated)   */
+    FVGB_TERM_EXPLICIT = 4,        /* rhs -= coeff*E_P (E already volume integrated)   */
+    FVGB_TERM_DIV_FLUX = 5         /* rhs -= coeff*sum_f(+-F_f): explicit div of a face
+                                      flux, volume integrated (dsl::exp::div(phi))     */
 } fvgb_term_kind;
 
 /* One operator of a dsl::Expression. The expression is
@@ -190,7 +192,7 @@ typedef struct fvgb_term {
     double coeff;          /* operator scaling                                        */
     const double* cell;    /* DDT: old-time psi [n*ncomp]; SOURCE: s [n] or NULL (=1);
                               EXPLICIT: E [n*ncomp]                                   */
-    const double* face;    /* LAPLACIAN: gamma [nIF+nBF]; DIV: face flux [nIF+nBF]    */
+    const double* face;    /* LAPLACIAN: gamma [nIF+nBF]; DIV, DIV_FLUX: face flux [nIF+nBF] */
 } fvgb_term;
 
 /* LinearSystem on the mesh pattern: values[nnz], rhs[n*ncomp],

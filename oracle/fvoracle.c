@@ -21,7 +21,7 @@
 
 enum { BC_CALCULATED = 0, BC_FIXED_VALUE = 1, BC_FIXED_GRADIENT = 2 };
 enum { SCHEME_LINEAR = 0, SCHEME_UPWIND = 1 };
-enum { TERM_DDT = 0, TERM_LAPLACIAN = 1, TERM_DIV = 2, TERM_SOURCE = 3, TERM_EXPLICIT = 4 };
+enum { TERM_DDT = 0, TERM_LAPLACIAN = 1, TERM_DIV = 2, TERM_SOURCE = 3, TERM_EXPLICIT = 4, TERM_DIV_FLUX = 5 };
 enum { ST_OK = 0, ST_NOT_CONVERGED = 3, ST_BREAKDOWN = 4, ST_UNSUPPORTED = 6 };
 
 #define RED_THREADS 256
@@ -245,6 +245,7 @@ int32_t or_sparsity(const or_mesh* m, int32_t* row_offs, int32_t* col, int32_t* 
  *   DDT:       a_PP += c*V*(1/dt);  b_P += (c*V*(1/dt))*psi_old
  *   SOURCE:    a_PP += (c*s)*V   (s = 1 if absent)
  *   EXPLICIT:  b_P  -= c*E
+ *   DIV_FLUX:  E_P = sum of +-F_f (owner +, neighbour -, boundary +, face order); b_P -= c*E_P
  *   LAPLACIAN: g = c*(gamma*(|Sf|*delta)); a_PN += g, a_PP -= g, a_NP += g, a_NN -= g;
  *              boundary value faces: m = c*(gamma_b*(|Sf_b|*delta_b)), r = m*v_b;
  *              fixedGradient faces:  m = 0, r = (c*(gamma_b*|Sf_b|))*g_b
@@ -277,6 +278,16 @@ void or_assemble(const or_mesh* m, const or_csr* A, int32_t nc, const or_term* t
             for (int32_t i = 0; i < n; ++i) DIAG(i) += (T->cell ? c * T->cell[i] : c) * m->V[i];
         } else if (T->kind == TERM_EXPLICIT) {
             for (int32_t i = 0; i < n * nc; ++i) rhs[i] -= c * T->cell[i];
+        } else if (T->kind == TERM_DIV_FLUX) {
+            double* e = zalloc((size_t)n);
+            for (int32_t f = 0; f < m->nif; ++f) {
+                e[m->own[f]] += T->face[f];
+                e[m->nei[f]] -= T->face[f];
+            }
+            for (int32_t b = 0; b < m->nbf; ++b) e[m->bcells[b]] += T->face[m->nif + b];
+            for (int32_t i = 0; i < n; ++i)
+                for (int32_t k = 0; k < nc; ++k) rhs[i * nc + k] -= c * e[i];
+            free(e);
         } else if (T->kind == TERM_LAPLACIAN) {
             for (int32_t f = 0; f < m->nif; ++f) {
                 int32_t P = m->own[f], N = m->nei[f];
