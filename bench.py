@@ -171,6 +171,8 @@ def run_gpu(args, rank, world):
     stats = read_stats(args.steps)
     assert all(s.status == abi.OK for s in stats), [s.status for s in stats]
     iters = [s.num_iter for s in stats]
+    if args.profile:
+        return hm, dict(ms=ms, iters=iters)
     # ---- end to end through the ABI with host buffers (pinned), copies inside the region
     h_in = torch.empty(hm.n, dtype=torch.float64, pin_memory=True)
     h_out = torch.empty(hm.n, dtype=torch.float64, pin_memory=True)
@@ -306,6 +308,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--ref-max-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one warm-up and one timed FP64 step only (the command the ncu captures run)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -322,7 +326,12 @@ def main():
         _build.build()
     if world > 1:
         torch.distributed.barrier()
+    if args.profile:
+        args.steps, args.warmup = 1, 1
     hm, r = run_gpu(args, rank, world)
+    if args.profile:
+        print(json.dumps({"profile_run": True, "ms": r["ms"], "iters": r["iters"]}))
+        return
     ms = r["ms"]
     if world > 1:
         t = torch.tensor([ms, r["e2e_ms"]], dtype=torch.float64, device="cuda")
