@@ -33,6 +33,7 @@ CU_UNITS = {
     "assembly.cu": ["-fmad=false"],
     "solver.cu": ["-fmad=false"],
     "piso.cu": ["-fmad=false"],
+    "noalloc.cu": ["-fmad=false"],
 }
 CPP_UNITS = ["common.cpp", "meshgen.cpp"]
 HEADERS = [INCLUDE / "fvgb.h", CSRC / "internal.cuh", CSRC / "fvgb_host_common.h"]

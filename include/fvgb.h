@@ -266,6 +266,24 @@ fvgb_status fvgb_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg,
 fvgb_status fvgb_solve_kernel_times(fvgb_ls* ls, const double* x0, int32_t iters, double* ms_out,
                                     fvgb_stream stream);
 
+/* FP64 Jacobi-CG that allocates nothing.  No counterpart in the reference: it
+ * exists for callers that cannot call cudaMalloc (a solver embedded in a host
+ * application that owns the device memory under a fixed budget, or code that
+ * must not let an allocation synchronize the device).  The system is given in
+ * NeoN's CSR layout in caller-owned device memory (row_offs[n+1],
+ * col_idxs[nnz], diag_offset[n] relative to the row start, values[nnz],
+ * rhs[n]); x[n] is the initial guess and the solution.  Work vectors live in a
+ * fixed device array inside the library (about 8.2 MiB, held by every GPU that
+ * loads the library until the process exits), so n is limited to 262,144 rows
+ * (larger n: FVGB_ERR_INVALID_ARG).  All calls on a device share that array:
+ * calls that overlap on the GPU race.  The first call on a device looks up the
+ * array's address; make that first call before any stream capture.
+ * Synchronous; same criteria and the same iterates as fvgb_solve (FP64). */
+fvgb_status fvgb_pcg_csr_noalloc(int32_t n, const int32_t* row_offs, const int32_t* col_idxs,
+                                 const int32_t* diag_offset, const double* values,
+                                 const double* rhs, double* x, const fvgb_solver_cfg* cfg,
+                                 fvgb_solver_stats* stats, fvgb_stream stream);
+
 /* ------------------------------------------------- pressure-velocity (PISO) */
 /* computeRAUandHByA (pressureVelocityCoupling.cpp:65-128) on an assembled vector
  * system: rAU_P = V_P / a_PP; HbyA_P = (b_P - sum_{faces asc} a_Pj U_j) * (rAU_P / V_P).
