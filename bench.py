@@ -172,6 +172,9 @@ def run_gpu(args, rank, world):
     assert all(s.status == abi.OK for s in stats), [s.status for s in stats]
     iters = [s.num_iter for s in stats]
     if args.profile:
+        # the same kernels outside the graph, where ncu can capture them one by one
+        kt = (C.c_double * 4)()
+        abi.check(L.fvgb_solve_kernel_times(ls.handle, abi.ptr(T.internal), 3, kt, stream))
         return hm, dict(ms=ms, iters=iters)
     # ---- end to end through the ABI with host buffers (pinned), copies inside the region
     h_in = torch.empty(hm.n, dtype=torch.float64, pin_memory=True)

@@ -22,7 +22,7 @@
 //    (cudaGetSymbolAddress, with that device current) and caches it; that
 //    first call should come before any stream capture.
 // The arithmetic and the reduction tree are those of the graph-based FP64 solve
-// in solver.cu (same fma order per row, same 256-thread x 4-row blocks), so the
+// in solver.cu (same fma order per row, same 256-thread blocks and rows per thread), so the
 // iterates are the same bits.
 #include <cmath>
 #include <mutex>
@@ -32,7 +32,7 @@
 namespace {
 
 constexpr int kT = 256;
-constexpr int kRowsPerThread = 4;
+constexpr int kRowsPerThread = 1;
 constexpr int kRowsPerBlock = kT * kRowsPerThread;
 constexpr int kMaxRows = 262144;
 constexpr int kMaxBlocks = kMaxRows / kRowsPerBlock;
@@ -72,7 +72,7 @@ std::mutex g_mu;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 __device__ __forceinline__ int red_row(int j) {
-    return blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5) * 128 + j * 32 + (threadIdx.x & 31);
+    return blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5) * (32 * kRowsPerThread) + j * 32 + (threadIdx.x & 31);
 }
 
 __device__ __forceinline__ double block_tree(double v, double* sm) {

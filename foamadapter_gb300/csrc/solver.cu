@@ -14,9 +14,9 @@
 // condition, so there is no host round trip per iteration.  Every loop is
 // bounded by an iteration cap.
 //
-// Reductions are deterministic: each 256-thread block owns 1024 rows
-// (thread t: rows blk*1024 + (t/32)*128 + j*32 + t%32, j = 0..3), sums its rows
-// sequentially, then warp 0 sums the 256 partials (lane l: l, l+32, ..., l+224)
+// Reductions are deterministic: each 256-thread block owns 256*R rows
+// (thread t: rows blk*256R + (t/32)*32R + j*32 + t%32, j < R; R = kRowsPerThread),
+// sums its rows sequentially, then warp 0 sums the 256 partials (lane l: l, l+32, ..., l+224)
 // and a xor butterfly finishes; the last block to arrive sums the block
 // partials in index order with the same tree.  The CPU oracle reproduces this
 // tree, so the FP64 iterates match it bit for bit.
@@ -27,7 +27,7 @@
 namespace {
 
 constexpr int kT = 256;
-constexpr int kRowsPerThread = 4;
+constexpr int kRowsPerThread = 1;
 constexpr int kRowsPerBlock = kT * kRowsPerThread;
 
 struct SolverParams {
@@ -49,7 +49,7 @@ struct SolverState {
 };
 
 __device__ __forceinline__ int red_row(int j) {
-    return blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5) * 128 + j * 32 + (threadIdx.x & 31);
+    return blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5) * (32 * kRowsPerThread) + j * 32 + (threadIdx.x & 31);
 }
 
 // Block sum of one value per thread; result valid in warp 0 (every lane).
@@ -86,29 +86,51 @@ __device__ __forceinline__ bool arrive_last(unsigned int* counter) {
     return am_last;
 }
 
+// Row sum of a sliced-ELL row, fma chain in slot (= column) order.  The slot
+// loads of the first 8 slots are issued before the dependent gathers.
 __device__ __forceinline__ double spmv_row(const MeshView& m, const double* __restrict__ val,
                                            const double* __restrict__ x, int i) {
     const int slice = i >> 5, lane = i & 31;
-    const int base = __ldg(&m.m_ptr[slice]);
-    const int w = (__ldg(&m.m_ptr[slice + 1]) - base) >> 5;
-    double s = 0.0;
-    for (int k = 0; k < w; ++k) {
-        const int pos = base + k * 32 + lane;
-        s = fma(__ldg(&val[pos]), __ldg(&x[__ldg(&m.m_col[pos])]), s);
+    const int base = __ldg(&m.m_ptr[slice]) + lane;
+    const int w = (__ldg(&m.m_ptr[slice + 1]) - __ldg(&m.m_ptr[slice])) >> 5;
+    double v[8], xv[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = 0.0;
+        xv[k] = 0.0;
+        if (k < w) {
+            v[k] = __ldg(&val[base + k * 32]);
+            xv[k] = __ldg(&x[__ldg(&m.m_col[base + k * 32])]);
+        }
     }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (k < w) s = fma(v[k], xv[k], s);
+    for (int k = 8; k < w; ++k) s = fma(__ldg(&val[base + k * 32]), __ldg(&x[__ldg(&m.m_col[base + k * 32])]), s);
     return s;
 }
 
 __device__ __forceinline__ float spmv_row_f(const MeshView& m, const float* __restrict__ val,
                                             const float* __restrict__ x, int i, float diag) {
     const int slice = i >> 5, lane = i & 31;
-    const int base = __ldg(&m.m_ptr[slice]);
-    const int w = (__ldg(&m.m_ptr[slice + 1]) - base) >> 5;
-    float s = diag;
-    for (int k = 0; k < w; ++k) {
-        const int pos = base + k * 32 + lane;
-        s = fmaf(__ldg(&val[pos]), __ldg(&x[__ldg(&m.m_col[pos])]), s);
+    const int base = __ldg(&m.m_ptr[slice]) + lane;
+    const int w = (__ldg(&m.m_ptr[slice + 1]) - __ldg(&m.m_ptr[slice])) >> 5;
+    float v[8], xv[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = 0.0f;
+        xv[k] = 0.0f;
+        if (k < w) {
+            v[k] = __ldg(&val[base + k * 32]);
+            xv[k] = __ldg(&x[__ldg(&m.m_col[base + k * 32])]);
+        }
     }
+    float s = diag;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (k < w) s = fmaf(v[k], xv[k], s);
+    for (int k = 8; k < w; ++k) s = fmaf(__ldg(&val[base + k * 32]), __ldg(&x[__ldg(&m.m_col[base + k * 32])]), s);
     return s;
 }
 

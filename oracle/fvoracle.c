@@ -6,7 +6,7 @@
  * Floating point: compiled with -ffp-contract=off.  Where the algorithm uses a
  * fused multiply-add (the CG kernels), it calls fma()/fmaf() explicitly, and the
  * dot products follow the fixed two-stage reduction tree that the GPU kernels
- * use (blocks of 256 threads x 4 rows, warp sums, block sum, sum of block
+ * use (blocks of 256 threads x R rows, warp sums, block sum, sum of block
  * partials), so the CG iterates are reproducible bit for bit.
  */
 #include "fvoracle.h"
@@ -25,7 +25,7 @@ enum { TERM_DDT = 0, TERM_LAPLACIAN = 1, TERM_DIV = 2, TERM_SOURCE = 3, TERM_EXP
 enum { ST_OK = 0, ST_NOT_CONVERGED = 3, ST_BREAKDOWN = 4, ST_UNSUPPORTED = 6 };
 
 #define RED_THREADS 256
-#define RED_ROWS_PER_THREAD 4
+#define RED_ROWS_PER_THREAD 1
 #define RED_ROWS_PER_BLOCK (RED_THREADS * RED_ROWS_PER_THREAD)
 
 void or_set_threads(int32_t nthreads) {
@@ -389,7 +389,7 @@ void or_apply_operator(const or_csr* A, const double* values, const double* rhs,
 
 /* ---------------------------------------------------------------- reductions */
 /* The GPU reduction tree: thread t of a 256-thread block owns rows
- * base + (t/32)*128 + j*32 + t%32, j = 0..3; its partial is a sequential sum;
+ * base + (t/32)*32R + j*32 + t%32, j < R (R = RED_ROWS_PER_THREAD); its partial is a sequential sum;
  * then lane l of warp 0 sums partials l, l+32, ..., l+224 in order and a
  * butterfly (xor 16, 8, 4, 2, 1) finishes.  Stage two: thread t sums block
  * partials t, t+256, ... and the same block tree follows. */
@@ -418,7 +418,7 @@ static double final_tree(int32_t nb, const double* partials) {
 }
 
 static inline int32_t red_row(int32_t blk, int t, int j) {
-    return blk * RED_ROWS_PER_BLOCK + (t >> 5) * 128 + j * 32 + (t & 31);
+    return blk * RED_ROWS_PER_BLOCK + (t >> 5) * (32 * RED_ROWS_PER_THREAD) + j * 32 + (t & 31);
 }
 
 static int32_t nblocks_of(int32_t n) { return (n + RED_ROWS_PER_BLOCK - 1) / RED_ROWS_PER_BLOCK; }
