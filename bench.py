@@ -295,6 +295,80 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+# ----------------------------------------------------------------------------- other workloads
+def run_advection(args):
+    """Explicit upwind advection, 64x64x1, 100 forward-Euler steps, vs the oracle bit for bit."""
+    import torch
+
+    from foamadapter_gb300 import apps
+    from oracle.pyoracle import Oracle
+
+    case = apps.Advection(n=64)
+    hm = case.hm
+    T0 = case.T.host().copy()
+    Tb0 = case.T.boundary.cpu().numpy()[:hm.nbf].copy()
+    nsteps = 100
+    for _ in range(5):                      # warm-up on a copy of the state
+        case.step()
+    case.T.internal.copy_(torch.as_tensor(T0).cuda())
+    case.T.boundary[:hm.nbf].copy_(torch.as_tensor(Tb0).cuda())
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(nsteps):
+        case.step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    o = Oracle(hm)
+    types = np.full(hm.npatch, 2, np.int32)
+    T, Tb = T0.copy(), Tb0.copy()
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        T, Tb = o.advect_euler(case.flux.host(), T, Tb, case.dt, types, np.zeros(hm.nbf))
+    cpu_s = time.perf_counter() - t0
+    fu = (hm.nif + hm.nbf) * nsteps
+    return {"workload": "advection 64x64x1 upwind forward Euler, 100 steps", "metric": "face-updates/s",
+            "value": fu / (ms / 1e3), "us_per_step": 1e3 * ms / nsteps,
+            "bit_exact_vs_oracle": bool(np.array_equal(case.T.host(), T)),
+            "cpu_baseline": {"value": fu / cpu_s, "cores": 1, "kind": "port", "sample": "100 steps, serial"}}
+
+
+def run_cavity(args):
+    """Lid-driven cavity PISO on 512x512x1: FP64 vs mixed-precision pressure solve."""
+    import torch
+
+    from foamadapter_gb300 import abi, apps
+
+    nsteps = args.cavity_steps
+    out = {}
+    fields = {}
+    for name, prec in (("fp64", abi.PREC_FP64), ("mixed", abi.PREC_MIXED_IR)):
+        case = apps.CavityPiso(n=512, precision=prec)
+        case.step()                                     # warm-up (builds the solver graphs)
+        torch.cuda.synchronize()
+        case = apps.CavityPiso(n=512, precision=prec)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(nsteps):
+            case.step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        its = [s[0] for s in case.stats]
+        out[name] = {"ms_per_step": ms / nsteps, "pressure_iters_mean": float(np.mean(its)),
+                     "all_solves_ok": all(s[4] == abi.OK for s in case.stats),
+                     "max_final_rel_residual": max(s[3] / s[2] if s[2] > 0 else 0.0 for s in case.stats)}
+        fields[name] = (case.p.host(), case.U.host())
+    (p64, U64), (pm, Um) = fields["fp64"], fields["mixed"]
+    out["speedup_step"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    out["err_vs_fp64"] = {"p_max": float(np.abs(pm - p64).max()), "p_l2_rel": float(np.linalg.norm(pm - p64) / max(
+        np.linalg.norm(p64), 1e-300)), "U_max": float(np.abs(Um - U64).max()),
+        "U_l2_rel": float(np.linalg.norm(Um - U64) / max(np.linalg.norm(U64), 1e-300))}
+    return {"workload": f"lid-driven cavity PISO 512x512x1, +-5% jitter, dt 5e-4, 2 correctors, {nsteps} steps",
+            "pressure_solve_to": "1e-8 relative FP64 residual", **out}
+
+
 def workload_config(args):
     return {"workload": f"implicit heat transfer {args.n}^3 jittered hex box, FP64 Jacobi-PCG to 1e-8",
             "cells": args.n ** 3, "dt": HEAT["dt"], "parallelism": "replicas",
@@ -311,6 +385,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--ref-max-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity"])
+    ap.add_argument("--cavity-steps", type=int, default=200)
     ap.add_argument("--profile", action="store_true",
                     help="one warm-up and one timed FP64 step only (the command the ncu captures run)")
     args = ap.parse_args()
@@ -329,6 +405,11 @@ def main():
         _build.build()
     if world > 1:
         torch.distributed.barrier()
+    if args.workload != "heat":
+        fn = {"advection": run_advection, "cavity": run_cavity}[args.workload]
+        if rank == 0:
+            print(json.dumps(fn(args)))
+        return
     if args.profile:
         args.steps, args.warmup = 1, 1
     hm, r = run_gpu(args, rank, world)

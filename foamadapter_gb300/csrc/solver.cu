@@ -27,7 +27,7 @@
 namespace {
 
 constexpr int kT = 256;
-constexpr int kRowsPerThread = 1;
+constexpr int kRowsPerThread = 4;
 constexpr int kRowsPerBlock = kT * kRowsPerThread;
 
 struct SolverParams {
@@ -57,6 +57,23 @@ __device__ __forceinline__ double block_tree(double v, double* sm) {
     sm[threadIdx.x] = v;
     __syncthreads();
     double s = 0.0;
+    if (threadIdx.x < 32) {
+        s = sm[threadIdx.x];
+#pragma unroll
+        for (int k = 1; k < kT / 32; ++k) s = s + sm[threadIdx.x + 32 * k];
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off);
+    }
+    __syncthreads();
+    return s;
+}
+
+// FP32 block sum (inner solve of the mixed scheme: keeps the FP64 pipe free);
+// same tree shape as block_tree.
+__device__ __forceinline__ float block_tree_f(float v, float* sm) {
+    sm[threadIdx.x] = v;
+    __syncthreads();
+    float s = 0.0f;
     if (threadIdx.x < 32) {
         s = sm[threadIdx.x];
 #pragma unroll
@@ -224,8 +241,8 @@ __global__ void __launch_bounds__(kT)
 __global__ void __launch_bounds__(kT)
     k_pcg_update(SolverState* st, MeshView m, const double* __restrict__ dinv,
                  const double* __restrict__ p, const double* __restrict__ q,
-                 double* __restrict__ r, double* __restrict__ pa, double* __restrict__ pb,
-                 cudaGraphConditionalHandle h, int setc) {
+                 double* __restrict__ r, double* __restrict__ z, double* __restrict__ pa,
+                 double* __restrict__ pb, cudaGraphConditionalHandle h, int setc) {
     if (st->status == FVGB_ERR_BREAKDOWN) return;
     __shared__ double sma[kT], smb[kT];
     const int n = m.n;
@@ -241,6 +258,7 @@ __global__ void __launch_bounds__(kT)
         const double ri = fma(-alpha, __ldg(&q[i]), r[i]);
         r[i] = ri;
         const double zi = __ldg(&dinv[i]) * ri;
+        z[i] = zi;
         arz = fma(ri, zi, arz);
         arr = fma(ri, ri, arr);
     }
@@ -267,15 +285,14 @@ __global__ void __launch_bounds__(kT)
 }
 
 __global__ void __launch_bounds__(kT)
-    k_pcg_dir(const SolverState* st, int n, const double* __restrict__ dinv,
-              const double* __restrict__ r, double* __restrict__ p) {
+    k_pcg_dir(const SolverState* st, int n, const double* __restrict__ z, double* __restrict__ p) {
     if (st->status == FVGB_ERR_BREAKDOWN) return;
     const double beta = st->beta;
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int i = red_row(j);
         if (i >= n) continue;
-        p[i] = fma(beta, p[i], __ldg(&dinv[i]) * __ldg(&r[i]));
+        p[i] = fma(beta, p[i], __ldg(&z[i]));  // z = dinv*r, stored by the update
     }
 }
 
@@ -366,10 +383,12 @@ __global__ void __launch_bounds__(kT)
         p[i] = rhi;
         arho = fmaf(rhi, rhi, arho);
     }
-    const double ba = block_tree(arr, sma), bb = block_tree((double)arho, smb);
+    __shared__ float smf[kT];
+    const double ba = block_tree(arr, sma);
+    const float bb = block_tree_f(arho, smf);
     if (threadIdx.x == 0) {
         pa[blockIdx.x] = ba;
-        pb[blockIdx.x] = bb;
+        pb[blockIdx.x] = (double)bb;
     }
     if (!arrive_last(&st->counter)) return;
     const double rr = final_tree(pa, gridDim.x, sma), rho = final_tree(pb, gridDim.x, smb);
@@ -426,8 +445,9 @@ __global__ void __launch_bounds__(kT)
         q[i] = qi;
         acc = fmaf(pi, qi, acc);
     }
-    const double ba = block_tree((double)acc, sma);
-    if (threadIdx.x == 0) pa[blockIdx.x] = ba;
+    __shared__ float smf[kT];
+    const float ba = block_tree_f(acc, smf);
+    if (threadIdx.x == 0) pa[blockIdx.x] = (double)ba;
     if (!arrive_last(&st->counter)) return;
     const double pq = final_tree(pa, gridDim.x, sma);
     if (threadIdx.x == 0) {
@@ -463,8 +483,9 @@ __global__ void __launch_bounds__(kT)
         rh[i] = ri;
         acc = fmaf(ri, ri, acc);
     }
-    const double ba = block_tree((double)acc, sma);
-    if (threadIdx.x == 0) pa[blockIdx.x] = ba;
+    __shared__ float smf[kT];
+    const float ba = block_tree_f(acc, smf);
+    if (threadIdx.x == 0) pa[blockIdx.x] = (double)ba;
     if (!arrive_last(&st->counter)) return;
     const double rhon = final_tree(pa, gridDim.x, sma);
     if (threadIdx.x == 0) {
@@ -530,7 +551,8 @@ struct SolverCache {
     const fvgb_ls* ls = nullptr;
     int n = 0, nb = 0;
     SolverState* st = nullptr;
-    double *dinv = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *pa = nullptr, *pb = nullptr;
+    double *dinv = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *pa = nullptr,
+           *pb = nullptr;
     double* s = nullptr;
     float *ah = nullptr, *rh = nullptr, *y = nullptr, *pf = nullptr, *qf = nullptr;
     cudaGraphExec_t g64 = nullptr, gmix = nullptr;
@@ -541,7 +563,7 @@ void fvgb_solver_cache_free(SolverCache* c) {
     if (!c) return;
     if (c->g64) cudaGraphExecDestroy(c->g64);
     if (c->gmix) cudaGraphExecDestroy(c->gmix);
-    void* ptrs[] = {c->st, c->dinv, c->r, c->p, c->q, c->pa, c->pb, c->s, c->ah, c->rh, c->y, c->pf, c->qf};
+    void* ptrs[] = {c->st, c->dinv, c->r, c->p, c->q, c->z, c->pa, c->pb, c->s, c->ah, c->rh, c->y, c->pf, c->qf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->h_stats) cudaFreeHost(c->h_stats);
@@ -581,6 +603,7 @@ fvgb_status build_fp64(SolverCache* c) {
     if (e == cudaSuccess) e = cudaMalloc(&c->r, sizeof(double) * n);
     if (e == cudaSuccess) e = cudaMalloc(&c->p, sizeof(double) * n);
     if (e == cudaSuccess) e = cudaMalloc(&c->q, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&c->z, sizeof(double) * n);
     if (e != cudaSuccess) return cuda_fail(e, "FP64 CG workspace");
     const fvgb_ls* ls = c->ls;
     MeshView m = ls->mesh->v;
@@ -600,8 +623,8 @@ fvgb_status build_fp64(SolverCache* c) {
     if (e == cudaSuccess) e = add_kernel(g, &n0, nullptr, (void*)k_pcg_init, nb, a_init);
     if (e == cudaSuccess) e = add_while(g, &n1, &n0, h, &body);
     void* a_spmv[] = {&st, &m, &val, &c->p, &c->q, &c->pa, &h, &setc};
-    void* a_upd[] = {&st, &m, &c->dinv, &c->p, &c->q, &c->r, &c->pa, &c->pb, &h, &setc};
-    void* a_dir[] = {&st, &nn, &c->dinv, &c->r, &c->p};
+    void* a_upd[] = {&st, &m, &c->dinv, &c->p, &c->q, &c->r, &c->z, &c->pa, &c->pb, &h, &setc};
+    void* a_dir[] = {&st, &nn, &c->z, &c->p};
     if (e == cudaSuccess) e = add_kernel(body, &b0, nullptr, (void*)k_pcg_spmv, nb, a_spmv);
     if (e == cudaSuccess) e = add_kernel(body, &b1, &b0, (void*)k_pcg_update, nb, a_upd);
     if (e == cudaSuccess) e = add_kernel(body, &b2, &b1, (void*)k_pcg_dir, nb, a_dir);
@@ -786,9 +809,9 @@ extern "C" fvgb_status fvgb_solve_kernel_times(fvgb_ls* ls, const double* x0, in
         cudaEventRecord(ev[2], s);
         k_pcg_spmv<<<nb, kT, 0, s>>>(c->st, m, ls->values, c->p, c->q, c->pa, h, 0);
         cudaEventRecord(ev[3], s);
-        k_pcg_update<<<nb, kT, 0, s>>>(c->st, m, c->dinv, c->p, c->q, c->r, c->pa, c->pb, h, 0);
+        k_pcg_update<<<nb, kT, 0, s>>>(c->st, m, c->dinv, c->p, c->q, c->r, c->z, c->pa, c->pb, h, 0);
         cudaEventRecord(ev[4], s);
-        k_pcg_dir<<<nb, kT, 0, s>>>(c->st, c->n, c->dinv, c->r, c->p);
+        k_pcg_dir<<<nb, kT, 0, s>>>(c->st, c->n, c->z, c->p);
         cudaEventRecord(ev[5], s);
         e = cudaEventSynchronize(ev[5]);
         if (e != cudaSuccess) break;

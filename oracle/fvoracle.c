@@ -25,7 +25,7 @@ enum { TERM_DDT = 0, TERM_LAPLACIAN = 1, TERM_DIV = 2, TERM_SOURCE = 3, TERM_EXP
 enum { ST_OK = 0, ST_NOT_CONVERGED = 3, ST_BREAKDOWN = 4, ST_UNSUPPORTED = 6 };
 
 #define RED_THREADS 256
-#define RED_ROWS_PER_THREAD 1
+#define RED_ROWS_PER_THREAD 4
 #define RED_ROWS_PER_BLOCK (RED_THREADS * RED_ROWS_PER_THREAD)
 
 void or_set_threads(int32_t nthreads) {
@@ -407,6 +407,21 @@ static double block_tree(const double* tp) {
     return v[0];
 }
 
+/* the same tree in float (block level of the FP32 inner solve) */
+static float block_tree_f(const float* tp) {
+    float v[32], nv[32];
+    for (int l = 0; l < 32; ++l) {
+        float s = tp[l];
+        for (int k = 1; k < RED_THREADS / 32; ++k) s = s + tp[l + 32 * k];
+        v[l] = s;
+    }
+    for (int off = 16; off >= 1; off >>= 1) {
+        for (int l = 0; l < 32; ++l) nv[l] = v[l] + v[l ^ off];
+        memcpy(v, nv, sizeof v);
+    }
+    return v[0];
+}
+
 static double final_tree(int32_t nb, const double* partials) {
     double tp[RED_THREADS];
     for (int t = 0; t < RED_THREADS; ++t) {
@@ -559,22 +574,22 @@ static int32_t solve_fp64(const or_csr* A, const double* val, const double* b, d
  * scaled diagonal is sign(a_ii) (all diagonals must share one sign); update
  * x += S y in FP64.  Scaled off-diagonals are rounded once to float:
  * ahat_ij = (float)((a_ij * s_i) * s_j).  Row sums: q = sign*p_i, then fmaf over
- * the off-diagonals in column order.  Dots: per-thread fmaf in float, converted
- * to double for the block and final trees. */
+ * the off-diagonals in column order.  Dots: per-thread fmaf and the block tree
+ * in float, the sum of block partials in double. */
 static double dot_tree_f(int32_t n, const float* a, const float* b, double* part) {
     int32_t nb = nblocks_of(n);
 #pragma omp parallel for schedule(static)
     for (int32_t blk = 0; blk < nb; ++blk) {
-        double tp[RED_THREADS];
+        float tp[RED_THREADS];
         for (int t = 0; t < RED_THREADS; ++t) {
             float acc = 0.0f;
             for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
                 int32_t i = red_row(blk, t, j);
                 if (i < n) acc = fmaf(a[i], b[i], acc);
             }
-            tp[t] = (double)acc;
+            tp[t] = acc;
         }
-        part[blk] = block_tree(tp);
+        part[blk] = (double)block_tree_f(tp);
     }
     return final_tree(nb, part);
 }
