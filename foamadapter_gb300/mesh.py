@@ -141,6 +141,59 @@ def from_polymesh(points: np.ndarray, faces: list, owner: np.ndarray, neighbour:
     return _to_host(a, n_cells, nif, nbf, len(names), names), np.asarray(order, np.int64)
 
 
+def concat(meshes: list, align: int = 32) -> tuple[HostMesh, np.ndarray, list]:
+    """Pack independent meshes into one block-diagonal mesh.
+
+    Case k's cells start at a multiple of ``align`` (so 32-row slices never mix
+    cases); the cells between cases are isolated placeholders (volume 1, no
+    faces).  Internal faces are concatenated case by case; boundary faces are
+    grouped by patch, then by case, so every cell keeps the ascending order of
+    its own faces and each case computes exactly what it computes alone.
+    All meshes must share the patch list.  Returns the mesh, the row ranges
+    [2*ncases] (case k = rows [ranges[2k], ranges[2k+1])) and, per case, the
+    slice of its faces inside each merged patch.
+    """
+    names = meshes[0].patch_names
+    assert all(m.patch_names == names for m in meshes), "cases must share the patch list"
+    starts, pos = [], 0
+    for m in meshes:
+        pos = -(-pos // align) * align
+        starts.append(pos)
+        pos += m.n
+    N = -(-pos // align) * align
+    V = np.ones(N)
+    Cc = np.zeros((N, 3))
+    for m, s0 in zip(meshes, starts):
+        V[s0:s0 + m.n] = m.V
+        Cc[s0:s0 + m.n] = m.C
+    cat = lambda key: np.concatenate([getattr(m, key) for m in meshes])
+    own = np.concatenate([m.own + s0 for m, s0 in zip(meshes, starts)]).astype(np.int32)
+    nei = np.concatenate([m.nei + s0 for m, s0 in zip(meshes, starts)]).astype(np.int32)
+    bcells, poffs = [], [0]
+    # per-case slices inside the merged flat boundary
+    case_slices = [[None] * len(names) for _ in meshes]
+    cursor = 0
+    parts = {key: [] for key in ("bSf", "bCf", "bmagSf", "bw", "bdelta")}
+    for p in range(len(names)):
+        for k, (m, s0) in enumerate(zip(meshes, starts)):
+            lo, hi = int(m.patch_offsets[p]), int(m.patch_offsets[p + 1])
+            case_slices[k][p] = slice(cursor, cursor + hi - lo)
+            cursor += hi - lo
+            bcells.append(m.bcells[lo:hi] + s0)
+            for key in parts:
+                parts[key].append(getattr(m, key)[lo:hi])
+        poffs.append(cursor)
+    hm = HostMesh(
+        n=N, nif=len(own), nbf=cursor, npatch=len(names), V=V, C=Cc, own=own, nei=nei,
+        Sf=np.ascontiguousarray(cat("Sf")), Cf=np.ascontiguousarray(cat("Cf")), magSf=cat("magSf"), w=cat("w"),
+        delta=cat("delta"), bcells=np.concatenate(bcells).astype(np.int32),
+        bSf=np.ascontiguousarray(np.concatenate(parts["bSf"])), bCf=np.ascontiguousarray(np.concatenate(parts["bCf"])),
+        bmagSf=np.concatenate(parts["bmagSf"]), bw=np.concatenate(parts["bw"]), bdelta=np.concatenate(parts["bdelta"]),
+        patch_offsets=np.asarray(poffs, np.int32), patch_names=list(names))
+    ranges = np.asarray([v for m, s0 in zip(meshes, starts) for v in (s0, s0 + m.n)], np.int32)
+    return hm, ranges, case_slices
+
+
 class DeviceMesh:
     """A mesh uploaded and indexed on the GPU (fvgb_mesh handle)."""
 

@@ -264,6 +264,37 @@ class LinearSystem:
             pass
 
 
+class Batch:
+    """Independent cases packed into one LinearSystem, solved together
+    (fvgb_batch_*): one launch per kernel for all cases, per-case criteria."""
+
+    def __init__(self, ls: LinearSystem, row_ranges):
+        self.ls = ls
+        self.ranges = np.ascontiguousarray(row_ranges, dtype=np.int32)
+        self.ncases = len(self.ranges) // 2
+        h = C.c_void_p()
+        abi.check(abi.lib().fvgb_batch_create(ls.handle, self.ncases, abi.ptr(self.ranges), C.byref(h)))
+        self.handle = h
+
+    def solve(self, x: torch.Tensor, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=abi.PREC_FP64,
+              inner_rel_tol=1e-3, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,)):
+        cfg = abi.SolverCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer)
+        stats = (abi.SolverStats * self.ncases)()
+        abi.check(abi.lib().fvgb_batch_solve(self.handle, abi.ptr(x), C.byref(cfg), stats, _stream()), allow=allow)
+        return list(stats)
+
+    def close(self):
+        if self.handle:
+            abi.lib().fvgb_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class PDESolver:
     """FoamAdapter::PDESolver (expression.hpp:23-179): owns the system of one PDE."""
 

@@ -259,6 +259,23 @@ fvgb_status fvgb_solve(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg,
 fvgb_status fvgb_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg,
                              fvgb_solver_stats* stats_dev, fvgb_stream stream);
 
+/* Batched solve of independent cases packed into one linear system (a
+ * block-diagonal matrix, e.g. the concatenated meshes of many cases): case c
+ * owns rows [row_ranges[2c], row_ranges[2c+1]) (HOST array; cases in row order,
+ * not overlapping); rows outside every case are left untouched.  One launch per kernel serves
+ * every case, each case keeps its own CG scalars and stops on its own
+ * criteria, and a case's iterates are bit-identical to solving it alone.
+ * No counterpart in the reference, which solves one case per call. */
+typedef struct fvgb_batch fvgb_batch;
+fvgb_status fvgb_batch_create(fvgb_ls* ls, int32_t ncases, const int32_t* row_ranges, fvgb_batch** out);
+fvgb_status fvgb_batch_destroy(fvgb_batch* batch);
+/* stats: HOST array [ncases]; returns the worst case status. */
+fvgb_status fvgb_batch_solve(fvgb_batch* batch, double* x, const fvgb_solver_cfg* cfg,
+                             fvgb_solver_stats* stats, fvgb_stream stream);
+/* stats_dev: DEVICE array [ncases] (may be NULL); nothing is waited for. */
+fvgb_status fvgb_batch_solve_async(fvgb_batch* batch, double* x, const fvgb_solver_cfg* cfg,
+                                   fvgb_solver_stats* stats_dev, fvgb_stream stream);
+
 /* Measurement aid (no reference counterpart): runs the FP64 CG init and
  * `iters` iterations outside the graph on a private copy of x0, with CUDA
  * events around each kernel; ms_out[4] = mean milliseconds of
