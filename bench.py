@@ -210,7 +210,7 @@ def compare_precisions(torch, abi, L, ls, T, T_old, tarr, bc, dm, hm, stream):
     abi.check(L.fvgb_assemble(ls.handle, tarr, 2, HEAT["dt"], C.byref(bc), abi.ptr(T.boundary), stream))
     out = {}
     sols = {}
-    for name, prec, inner in (("fp64", abi.PREC_FP64, 0.0), ("mixed", abi.PREC_MIXED_IR, 1e-3)):
+    for name, prec, inner in (("fp64", abi.PREC_FP64, 0.0), ("mixed", abi.PREC_MIXED_IR, 1e-2)):
         cfg = abi.SolverCfg(HEAT["rel_tol"], 0.0, 4000, prec, inner, 1000, 50)
         best = None
         for rep in range(3):
@@ -369,6 +369,115 @@ def run_cavity(args):
             "pressure_solve_to": "1e-8 relative FP64 residual", **out}
 
 
+def batch_cases(ncases, seed=4):
+    """512 hex boxes, nx,ny,nz = round(exp(U(ln 16, ln 64))), +-10% jitter, lognormal k (sigma 0.5),
+    wall temperature U[350, 450]."""
+    from foamadapter_gb300 import mesh
+
+    rng = np.random.default_rng(seed)
+    dims = np.rint(np.exp(rng.uniform(np.log(16), np.log(64), size=(ncases, 3)))).astype(int)
+    cases = []
+    for k, d in enumerate(dims):
+        hm = mesh.box(int(d[0]), int(d[1]), int(d[2]), jitter=0.1, seed=seed * 100000 + k)
+        cases.append((hm, np.exp(0.5 * rng.standard_normal(hm.n)), float(rng.uniform(350.0, 450.0))))
+    return cases
+
+
+def run_batch(args):
+    """One launch per operator for all cases (packed), mixed-precision inner solve,
+    against one-at-a-time plain FP64 launches of the same cases."""
+    import torch
+
+    from foamadapter_gb300 import abi, mesh, neon
+    from foamadapter_gb300.mesh import DeviceMesh
+
+    t0 = time.perf_counter()
+    cases = batch_cases(args.cases)
+    big, ranges, slices = mesh.concat([c[0] for c in cases])
+    setup_s = time.perf_counter() - t0
+    dm = DeviceMesh(big)
+    ref = np.zeros(big.nbf)
+    kap = np.ones(big.n)
+    for k, (hm, kk, tw) in enumerate(cases):
+        ref[slices[k][0]] = tw
+        kap[ranges[2 * k]:ranges[2 * k + 1]] = kk
+    xmin = slice(slices[0][0].start, slices[-1][0].stop)
+    T = neon.VolumeField(dm, np.full(big.n, 300.0), [("fixedValue", ref[xmin])] + [("zeroGradient", 0.0)] * 5)
+    kf = neon.VolumeField(dm, kap, [("zeroGradient", 0.0)] * 6)
+    gamma = neon.SurfaceInterpolation(dm, "linear").interpolate(kf)
+    T_old = T.internal.clone()
+    ls = neon.LinearSystem(dm)
+    batch = neon.Batch(ls, ranges)
+    L, s = abi.lib(), torch.cuda.current_stream().cuda_stream
+    terms = (abi.Term * 2)(*[t.struct() for t in (neon.ddt(T_old), neon.laplacian(gamma, -1.0))])
+    bc = T.bc_struct()
+    stats_dev = torch.zeros(len(cases) * 8, dtype=torch.int32, device="cuda")
+
+    def packed_step(cfg):
+        T_old.copy_(T.internal)
+        abi.check(L.fvgb_assemble(ls.handle, terms, 2, 0.01, C.byref(bc), abi.ptr(T.boundary), s))
+        abi.check(L.fvgb_batch_solve_async(batch.handle, abi.ptr(T.internal), C.byref(cfg), stats_dev.data_ptr(), s))
+        abi.check(L.fvgb_bc_correct(dm.handle, 1, C.byref(bc), abi.ptr(T.internal), abi.ptr(T.boundary), s))
+
+    def timed(fn, nsteps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(nsteps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    out = {"cases": len(cases), "cells_total": int(sum(c[0].n for c in cases)),
+           "cells_min_max": [int(min(c[0].n for c in cases)), int(max(c[0].n for c in cases))],
+           "host_mesh_build_s": setup_s}
+    cfg_mixed = abi.SolverCfg(1e-8, 0.0, 4000, abi.PREC_MIXED_IR, args.inner_tol, 2000, 50)
+    cfg_fp64 = abi.SolverCfg(1e-8, 0.0, 4000, abi.PREC_FP64, 0.0, 0, 0)
+    for name, cfg in (("packed_mixed", cfg_mixed), ("packed_fp64", cfg_fp64)):
+        T.internal.fill_(300.0)
+        packed_step(cfg)                                      # warm-up (graph build)
+        T.internal.fill_(300.0)
+        sec = timed(lambda: packed_step(cfg), args.batch_steps)
+        st = stats_dev.cpu().numpy().tobytes()
+        stl = [abi.SolverStats.from_buffer_copy(st[i * 32:(i + 1) * 32]) for i in range(len(cases))]
+        out[name] = {"case_steps_per_s": len(cases) * args.batch_steps / sec, "s": sec,
+                     "all_ok": all(x.status == 0 for x in stl),
+                     "iters_last_step_mean": float(np.mean([x.num_iter for x in stl]))}
+    # one case at a time, plain FP64 (a sample of cases, every case its own mesh/system/launches)
+    sample = cases[:: max(1, len(cases) // args.alone_cases)][: args.alone_cases]
+    solo = []
+    for hm, kk, tw in sample:
+        d1 = DeviceMesh(hm)
+        T1 = neon.VolumeField(d1, np.full(hm.n, 300.0), [("fixedValue", tw)] + [("zeroGradient", 0.0)] * 5)
+        g1 = neon.SurfaceInterpolation(d1, "linear").interpolate(
+            neon.VolumeField(d1, kk, [("zeroGradient", 0.0)] * 6))
+        o1 = T1.internal.clone()
+        l1 = neon.LinearSystem(d1)
+        t1 = (abi.Term * 2)(*[t.struct() for t in (neon.ddt(o1), neon.laplacian(g1, -1.0))])
+        b1 = T1.bc_struct()
+        solo.append((d1, T1, g1, o1, l1, t1, b1))
+
+    def solo_step(cfg):
+        for d1, T1, g1, o1, l1, t1, b1 in solo:
+            o1.copy_(T1.internal)
+            abi.check(L.fvgb_assemble(l1.handle, t1, 2, 0.01, C.byref(b1), abi.ptr(T1.boundary), s))
+            abi.check(L.fvgb_solve_async(l1.handle, abi.ptr(T1.internal), C.byref(cfg), None, s))
+            abi.check(L.fvgb_bc_correct(d1.handle, 1, C.byref(b1), abi.ptr(T1.internal), abi.ptr(T1.boundary), s))
+
+    for name, cfg in (("one_at_a_time_fp64", cfg_fp64), ("one_at_a_time_mixed", cfg_mixed)):
+        solo_step(cfg)
+        for _, T1, *_ in solo:
+            T1.internal.fill_(300.0)
+        steps = max(1, args.batch_steps // 5)
+        sec = timed(lambda: solo_step(cfg), steps)
+        out[name] = {"case_steps_per_s": len(solo) * steps / sec, "cases_sampled": len(solo)}
+    out["speedup_packed_mixed_vs_one_at_a_time_fp64"] = (out["packed_mixed"]["case_steps_per_s"] /
+                                                         out["one_at_a_time_fp64"]["case_steps_per_s"])
+    return {"workload": f"{len(cases)} implicit heat-transfer cases, dims logU[16,64], {args.batch_steps} steps",
+            **out}
+
+
 def workload_config(args):
     return {"workload": f"implicit heat transfer {args.n}^3 jittered hex box, FP64 Jacobi-PCG to 1e-8",
             "cells": args.n ** 3, "dt": HEAT["dt"], "parallelism": "replicas",
@@ -385,7 +494,11 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--ref-max-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity"])
+    ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity", "batch"])
+    ap.add_argument("--cases", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--alone-cases", type=int, default=64)
+    ap.add_argument("--inner-tol", type=float, default=1e-2)
     ap.add_argument("--cavity-steps", type=int, default=200)
     ap.add_argument("--profile", action="store_true",
                     help="one warm-up and one timed FP64 step only (the command the ncu captures run)")
@@ -406,7 +519,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     if args.workload != "heat":
-        fn = {"advection": run_advection, "cavity": run_cavity}[args.workload]
+        fn = {"advection": run_advection, "cavity": run_cavity, "batch": run_batch}[args.workload]
         if rank == 0:
             print(json.dumps(fn(args)))
         return

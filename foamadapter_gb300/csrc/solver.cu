@@ -5,8 +5,11 @@
 // preconditioner::Jacobi (max_block_size 1) that FoamAdapter maps OpenFOAM's
 // PCG/DIC to (src/compatibility/fvSolution.cpp:19-104), with its stopping
 // criteria (fvSolution.cpp:106-142).  MIXED_IR: CG on the Jacobi-scaled system
-// in FP32 inside FP64 iterative refinement; the true residual b - A x, the
-// update of x and the convergence test stay in FP64.
+// in FP32 with reliable updates: whenever the FP32 residual has dropped by
+// inner_rel_tol (or should be below the tolerance), x is updated in FP64, the
+// true residual b - A x is recomputed in FP64 and tested for convergence, and
+// it replaces the FP32 residual while the search direction is kept (not
+// restarted), so the iteration count stays close to the FP64 solver's.
 //
 // Batches.  A system may hold several independent cases (a block-diagonal
 // matrix); case c owns rows [begin_c, end_c).  Every kernel is ONE launch
@@ -48,8 +51,8 @@ struct SolverParams {
 
 struct CaseState {
     double rz, alpha, beta, res0, res, tol;
-    double rho, itol;
-    float falpha, fbeta;
+    double rho, rho_prev, itol;
+    float falpha, fbeta, frel;  // frel: direction factor after a reliable update (-1: restart)
     int32_t iter, status, total, outer, inner_it;
     int32_t active;        // FP64: iterating; mixed: refinement loop running
     int32_t inner_active;  // mixed: inner CG running
@@ -434,7 +437,8 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
-// refinement step: r = b - A x (FP64), rr; rhat = (float)(s r); y = 0; p = rhat; rho = rhat.rhat
+// refinement step: r = b - A x (FP64), rr; rhat = (float)(s r); y = 0; rho = rhat.rhat;
+// FIRST: p = rhat.  Later steps keep p; k_ir_reliable_dir folds rhat into it.
 template <bool FIRST>
 __global__ void __launch_bounds__(kT)
     k_ir_residual(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
@@ -458,7 +462,7 @@ __global__ void __launch_bounds__(kT)
             const float rhi = (float)(__ldg(&s[i]) * ri);
             rh[i] = rhi;
             y[i] = 0.0f;
-            p[i] = rhi;
+            if (FIRST) p[i] = rhi;
             arho = fmaf(rhi, rhi, arho);
         }
         const double ba = block_tree(arr, sma);
@@ -497,8 +501,15 @@ __global__ void __launch_bounds__(kT)
                         done = true;
                     }
                 }
+                // direction after this update: keep p (beta = rho/rho_prev) unless no
+                // inner iteration ran since the last update, then restart from rhat
+                cs->frel = (FIRST || cs->inner_it == 0) ? -1.0f : (float)(rho / cs->rho_prev);
                 cs->rho = rho;
-                cs->itol = prm.inner_rel_tol * prm.inner_rel_tol * rho;
+                // leave the inner loop when the FP32 residual dropped by inner_rel_tol or
+                // should be below the FP64 tolerance (estimated through this update's ratio)
+                const double dr = prm.inner_rel_tol * prm.inner_rel_tol;
+                const double dt = (cs->tol / res) * (cs->tol / res);
+                cs->itol = rho * (dr > dt ? dr : dt);
                 cs->inner_it = 0;
                 const bool inner = !done && rho > cs->itol && prm.inner_max_iter > 0 && cs->total < prm.max_iter;
                 cs->inner_active = inner ? 1 : 0;
@@ -510,6 +521,21 @@ __global__ void __launch_bounds__(kT)
     if (arrive_last(&L.bs->gcounter, gridDim.x) && threadIdx.x == 0) {
         cudaGraphSetConditional(h_inner, ld_volatile(&L.bs->n_inner) > 0 ? 1u : 0u);
         cudaGraphSetConditional(h_outer, ld_volatile(&L.bs->n_active) > 0 ? 1u : 0u);
+    }
+}
+
+// p = rhat + frel * p after a reliable update (p = rhat when frel < 0)
+__global__ void __launch_bounds__(kT)
+    k_ir_reliable_dir(Layout L, const float* __restrict__ rh, float* __restrict__ p) {
+    const Blk k = blk_info(L);
+    const CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->inner_active)) return;
+    const float fb = cs->frel;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        p[i] = fb < 0.0f ? __ldg(&rh[i]) : fmaf(fb, p[i], __ldg(&rh[i]));
     }
 }
 
@@ -583,6 +609,7 @@ __global__ void __launch_bounds__(kT)
             if (threadIdx.x == 0) {
                 const SolverParams& prm = L.bs->prm;
                 cs->fbeta = (float)(rhon / cs->rho);
+                cs->rho_prev = cs->rho;
                 cs->rho = rhon;
                 cs->inner_it += 1;
                 cs->total += 1;
@@ -793,7 +820,7 @@ fvgb_status build_mixed(SolverCache* c) {
     const unsigned nb = (unsigned)c->nb;
     e = cudaGraphConditionalHandleCreate(&ho, g, 0, cudaGraphCondAssignDefault);
     if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
-    cudaGraphNode_t n_scale, n_vals, n_res0, n_outer, n_fin, o_inner, o_x, o_res, i_spmv, i_upd, i_dir;
+    cudaGraphNode_t n_scale, n_vals, n_res0, n_outer, n_fin, o_inner, o_x, o_res, o_dir, i_spmv, i_upd, i_dir;
     cudaGraph_t obody = nullptr, ibody = nullptr;
     void* a_scale[] = {&L, &m, &val, &c->s};
     void* a_vals[] = {&L, &m, &val, &c->s, &c->ah};
@@ -802,6 +829,7 @@ fvgb_status build_mixed(SolverCache* c) {
     void* a_upd[] = {&L, &c->pf, &c->qf, &c->y, &c->rh, &c->pa, &hi};
     void* a_dir[] = {&L, &c->rh, &c->pf};
     void* a_x[] = {&L, &c->s, &c->y};
+    void* a_rdir[] = {&L, &c->rh, &c->pf};
     void* a_fin[] = {&L};
     if (e == cudaSuccess) e = add_kernel(g, &n_scale, nullptr, (void*)k_ir_scale, nb, kT, a_scale);
     if (e == cudaSuccess) e = add_kernel(g, &n_vals, &n_scale, (void*)k_ir_scaled_values, nb, kT, a_vals);
@@ -813,6 +841,7 @@ fvgb_status build_mixed(SolverCache* c) {
     if (e == cudaSuccess) e = add_kernel(ibody, &i_dir, &i_upd, (void*)k_ir_dir, nb, kT, a_dir);
     if (e == cudaSuccess) e = add_kernel(obody, &o_x, &o_inner, (void*)k_ir_xupdate, nb, kT, a_x);
     if (e == cudaSuccess) e = add_kernel(obody, &o_res, &o_x, (void*)k_ir_residual<false>, nb, kT, a_res);
+    if (e == cudaSuccess) e = add_kernel(obody, &o_dir, &o_res, (void*)k_ir_reliable_dir, nb, kT, a_rdir);
     if (e == cudaSuccess) e = add_kernel(g, &n_fin, &n_outer, (void*)k_finish, grid_for(c->ncases, 128), 128, a_fin);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->gmix, g, 0);
     cudaGraphDestroy(g);

@@ -568,14 +568,16 @@ static int32_t solve_fp64(const or_csr* A, const double* val, const double* b, d
     return status;
 }
 
-/* ----------------------------------------- mixed precision iterative refinement
- * Outer (FP64): r = b - A x (fma row chains), ||r||, test; inner (FP32): CG on the
- * Jacobi-scaled system  S A S y = S r,  S = diag(1/sqrt|a_ii|), from y = 0; the
- * scaled diagonal is sign(a_ii) (all diagonals must share one sign); update
- * x += S y in FP64.  Scaled off-diagonals are rounded once to float:
- * ahat_ij = (float)((a_ij * s_i) * s_j).  Row sums: q = sign*p_i, then fmaf over
- * the off-diagonals in column order.  Dots: per-thread fmaf and the block tree
- * in float, the sum of block partials in double. */
+/* ---------------------------------- mixed precision CG with reliable updates
+ * CG on the Jacobi-scaled system  S A S y = S r,  S = diag(1/sqrt|a_ii|), in
+ * FP32 (the scaled diagonal is sign(a_ii); all diagonals must share one sign).
+ * Scaled off-diagonals are rounded once to float: ahat_ij = (float)((a_ij*s_i)*s_j);
+ * row sums q = sign*p_i, then fmaf over the off-diagonals in column order.
+ * Dots: per-thread fmaf and block tree in float, block partials summed in double.
+ * Reliable update (FP64): when rho has dropped below rho_ref*max(d^2, (tol/res)^2)
+ * (d = inner_rel_tol) or after inner_max_iter steps, x += S y, r = b - A x is
+ * recomputed, tested, and replaces the FP32 residual; the direction continues
+ * with beta = rho_true/rho_prev (restarted from rhat when no step ran). */
 static double dot_tree_f(int32_t n, const float* a, const float* b, double* part) {
     int32_t nb = nblocks_of(n);
 #pragma omp parallel for schedule(static)
@@ -592,6 +594,30 @@ static double dot_tree_f(int32_t n, const float* a, const float* b, double* part
         part[blk] = (double)block_tree_f(tp);
     }
     return final_tree(nb, part);
+}
+
+static double residual_step(const or_csr* A, const double* val, const double* b, const double* x,
+                            const double* s, float* rh, double* r, double* part, int32_t n, int32_t nb) {
+#pragma omp parallel for schedule(static)
+    for (int32_t blk = 0; blk < nb; ++blk) {
+        double tp[RED_THREADS];
+        for (int t = 0; t < RED_THREADS; ++t) {
+            double arr = 0.0;
+            for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
+                int32_t i = red_row(blk, t, j);
+                if (i >= n) continue;
+                double sm;
+                spmv_row_fma(A, val, x, i, &sm);
+                double ri = b[i] - sm;
+                r[i] = ri;
+                arr = fma(ri, ri, arr);
+                rh[i] = (float)(s[i] * ri);
+            }
+            tp[t] = arr;
+        }
+        part[blk] = block_tree(tp);
+    }
+    return sqrt(final_tree(nb, part));
 }
 
 static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, double* x,
@@ -615,48 +641,27 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
         for (int32_t j = A->row_offs[i]; j < A->row_offs[i + 1]; ++j)
             ah[j] = (float)((val[j] * s[i]) * s[A->col[j]]);
     const float fs = (float)dsign;
+    const double dr = cfg->inner_rel_tol * cfg->inner_rel_tol;
     double *r = zalloc(n), *part = zalloc(nb);
     float *rh = (float*)calloc(n, sizeof(float)), *y = (float*)calloc(n, sizeof(float));
     float *p = (float*)calloc(n, sizeof(float)), *q = (float*)calloc(n, sizeof(float));
-    int32_t total = 0, outer = 0, status = ST_OK;
-    double res0 = 0.0, res = 0.0, tol = 0.0;
-    for (;;) {
-        /* FP64 residual and the scaled FP32 right-hand side */
-#pragma omp parallel for schedule(static)
-        for (int32_t blk = 0; blk < nb; ++blk) {
-            double tp[RED_THREADS];
-            for (int t = 0; t < RED_THREADS; ++t) {
-                double arr = 0.0;
-                for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
-                    int32_t i = red_row(blk, t, j);
-                    if (i >= n) continue;
-                    double sm;
-                    spmv_row_fma(A, val, x, i, &sm);
-                    double ri = b[i] - sm;
-                    r[i] = ri;
-                    arr = fma(ri, ri, arr);
-                    rh[i] = (float)(s[i] * ri);
-                }
-                tp[t] = arr;
-            }
-            part[blk] = block_tree(tp);
-        }
-        res = sqrt(final_tree(nb, part));
-        if (outer == 0) {
-            res0 = res;
-            tol = cfg->rel_tol * res0;
-            if (cfg->abs_tol > tol) tol = cfg->abs_tol;
-        }
-        if (!isfinite(res)) { status = ST_BREAKDOWN; break; }
-        if (!(res > tol) || res == 0.0) break;
-        if (outer >= cfg->max_outer || total >= cfg->max_iter) { status = ST_NOT_CONVERGED; break; }
-        /* inner CG from y = 0 */
-        for (int32_t i = 0; i < n; ++i) { y[i] = 0.0f; p[i] = rh[i]; }
-        double rho = dot_tree_f(n, rh, rh, part);
-        double rho0 = rho, itol = cfg->inner_rel_tol * cfg->inner_rel_tol * rho0;
-        int32_t it = 0;
-        int brk = 0;
-        while (rho > itol && it < cfg->inner_max_iter && total < cfg->max_iter) {
+    int32_t total = 0, outer = 0, status = ST_OK, inner_it = 0;
+    double rho, rho_prev = 0.0, itol, res, res0, tol;
+    /* first residual */
+    res = residual_step(A, val, b, x, s, rh, r, part, n, nb);
+    for (int32_t i = 0; i < n; ++i) { y[i] = 0.0f; p[i] = rh[i]; }
+    rho = dot_tree_f(n, rh, rh, part);
+    res0 = res;
+    tol = cfg->rel_tol * res0;
+    if (cfg->abs_tol > tol) tol = cfg->abs_tol;
+    int done = 0;
+    if (!isfinite(res)) { status = ST_BREAKDOWN; done = 1; }
+    else if (!(res > tol) || res == 0.0) done = 1;
+    else if (cfg->max_outer <= 0 || cfg->max_iter <= 0) { status = ST_NOT_CONVERGED; done = 1; }
+    { double dt = (tol / res) * (tol / res); itol = rho * (dr > dt ? dr : dt); }
+    int inner = !done && rho > itol && cfg->inner_max_iter > 0 && total < cfg->max_iter;
+    while (!done) {
+        while (inner) {
 #pragma omp parallel for schedule(static)
             for (int32_t i = 0; i < n; ++i) {
                 float acc = fs * p[i];
@@ -666,7 +671,11 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
             }
             double pq = dot_tree_f(n, p, q, part);
             double alpha = rho / pq;
-            if (pq == 0.0 || !isfinite(alpha)) { brk = 1; break; }
+            if (pq == 0.0 || !isfinite(alpha)) {
+                inner = 0;
+                if (inner_it == 0) { status = ST_BREAKDOWN; done = 1; }
+                break;
+            }
             float fa = (float)alpha;
             for (int32_t i = 0; i < n; ++i) {
                 y[i] = fmaf(fa, p[i], y[i]);
@@ -674,14 +683,31 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
             }
             double rhon = dot_tree_f(n, rh, rh, part);
             float fb = (float)(rhon / rho);
+            rho_prev = rho;
             rho = rhon;
-            ++it;
+            ++inner_it;
             ++total;
+            int more = rhon > itol && inner_it < cfg->inner_max_iter && total < cfg->max_iter;
+            if (!more) { inner = 0; break; }
             for (int32_t i = 0; i < n; ++i) p[i] = fmaf(fb, p[i], rh[i]);
         }
-        if (brk && it == 0) { status = ST_BREAKDOWN; break; }
+        if (done) break;
+        /* reliable update */
         for (int32_t i = 0; i < n; ++i) x[i] = fma(s[i], (double)y[i], x[i]);
+        res = residual_step(A, val, b, x, s, rh, r, part, n, nb);
+        for (int32_t i = 0; i < n; ++i) y[i] = 0.0f;
+        double rho_true = dot_tree_f(n, rh, rh, part);
         ++outer;
+        if (!isfinite(res)) { status = ST_BREAKDOWN; done = 1; }
+        else if (!(res > tol) || res == 0.0) done = 1;
+        else if (outer >= cfg->max_outer || total >= cfg->max_iter) { status = ST_NOT_CONVERGED; done = 1; }
+        float frel = inner_it == 0 ? -1.0f : (float)(rho_true / rho_prev);
+        rho = rho_true;
+        { double dt = (tol / res) * (tol / res); itol = rho * (dr > dt ? dr : dt); }
+        inner_it = 0;
+        inner = !done && rho > itol && cfg->inner_max_iter > 0 && total < cfg->max_iter;
+        if (inner)
+            for (int32_t i = 0; i < n; ++i) p[i] = frel < 0.0f ? rh[i] : fmaf(frel, p[i], rh[i]);
     }
     st->init_res_norm = res0;
     st->final_res_norm = res;
