@@ -478,6 +478,76 @@ def run_batch(args):
             **out}
 
 
+def serve_requests(count, seed=5):
+    """Poisson arrivals (200/s), edges logU[16,160] per axis, |U| in [0.1,2] with a random
+    direction, D logU[1e-4,1e-2], 10..200 steps."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / 200.0, size=count))
+    reqs = []
+    for k in range(count):
+        e = np.rint(np.exp(rng.uniform(np.log(16), np.log(160), size=3))).astype(int)
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        U = d * rng.uniform(0.1, 2.0)
+        D = float(np.exp(rng.uniform(np.log(1e-4), np.log(1e-2))))
+        reqs.append((float(t[k]), int(e[0]), int(e[1]), int(e[2]), int(rng.integers(10, 201)), U, D))
+    return reqs
+
+
+def run_serve(args):
+    """Continuous batching server vs sequential plain (FP64, one request at a time) runs."""
+    from foamadapter_gb300 import abi
+
+    L = abi.lib()
+    reqs = serve_requests(args.requests)
+
+    def serve(sample, precision, paced, streams, budget):
+        cfg = abi.ServerCfg(int(budget), streams, 100000)
+        sv = C.c_void_p()
+        abi.check(L.fvgb_server_create(C.byref(cfg), C.byref(sv)))
+        buf = (abi.ServeResult * 1024)()
+        results, t0 = {}, time.perf_counter()
+        keep = []
+        for (ta, nx, ny, nz, steps, U, D) in sample:
+            if paced:
+                while time.perf_counter() - t0 < ta:
+                    time.sleep(0.0005)
+            req = abi.ServeRequest(nx, ny, nz, steps, (C.c_double * 3)(*U), D, 0.0, precision, 0, None)
+            rid = C.c_int64()
+            abi.check(L.fvgb_server_submit(sv, C.byref(req), C.byref(rid)))
+            keep.append(req)
+            if not paced:  # sequential: wait for this one before the next
+                while rid.value not in results:
+                    cnt = C.c_int32()
+                    L.fvgb_server_poll(sv, buf, 1024, C.byref(cnt))
+                    for i in range(cnt.value):
+                        results[buf[i].id] = abi.ServeResult.from_buffer_copy(buf[i])
+                    time.sleep(0.0002)
+        while len(results) < len(sample):
+            cnt = C.c_int32()
+            L.fvgb_server_poll(sv, buf, 1024, C.byref(cnt))
+            for i in range(cnt.value):
+                results[buf[i].id] = abi.ServeResult.from_buffer_copy(buf[i])
+            time.sleep(0.001)
+        wall = time.perf_counter() - t0
+        info = (C.c_int64 * 6)()
+        L.fvgb_server_info(sv, info)
+        abi.check(L.fvgb_server_destroy(sv))
+        r = list(results.values())
+        lat = np.array([x.finish_s - x.submit_s for x in r])
+        ok = all(x.status == 0 for x in r)
+        return {"requests": len(r), "wall_s": wall, "solves_per_s": len(r) / wall,
+                "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+                "all_ok": ok, "peak_device_GB": info[4] / 1e9, "ticks": int(info[5]),
+                "cell_steps": int(sum(x[1] * x[2] * x[3] * x[4] for x in sample))}
+
+    served = serve(reqs, abi.PREC_MIXED_IR, True, args.serve_streams, 150e9)
+    seq = serve(reqs[: args.seq_requests], abi.PREC_FP64, False, 1, 150e9)
+    return {"workload": f"serving: {len(reqs)} Poisson arrivals at 200/s, edges logU[16,160], 10-200 IMEX steps",
+            "served_mixed": served, "sequential_plain_fp64": seq,
+            "solves_per_s_ratio": served["solves_per_s"] / seq["solves_per_s"]}
+
+
 def workload_config(args):
     return {"workload": f"implicit heat transfer {args.n}^3 jittered hex box, FP64 Jacobi-PCG to 1e-8",
             "cells": args.n ** 3, "dt": HEAT["dt"], "parallelism": "replicas",
@@ -494,7 +564,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--ref-max-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity", "batch"])
+    ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity", "batch", "serve"])
+    ap.add_argument("--requests", type=int, default=400)
+    ap.add_argument("--seq-requests", type=int, default=40)
+    ap.add_argument("--serve-streams", type=int, default=16)
     ap.add_argument("--cases", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--alone-cases", type=int, default=64)
@@ -519,7 +592,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     if args.workload != "heat":
-        fn = {"advection": run_advection, "cavity": run_cavity, "batch": run_batch}[args.workload]
+        fn = {"advection": run_advection, "cavity": run_cavity, "batch": run_batch, "serve": run_serve}[args.workload]
         if rank == 0:
             print(json.dumps(fn(args)))
         return

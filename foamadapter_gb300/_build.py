@@ -34,6 +34,8 @@ CU_UNITS = {
     "solver.cu": ["-fmad=false"],
     "piso.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
+    "boxmesh.cu": ["-fmad=false"],
+    "serve.cu": [],
 }
 CPP_UNITS = ["common.cpp", "meshgen.cpp"]
 HEADERS = [INCLUDE / "fvgb.h", CSRC / "internal.cuh", CSRC / "fvgb_host_common.h"]

@@ -19,7 +19,7 @@ OK, ERR_INVALID_ARG, ERR_OOM, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_CUDA, ERR_UN
     ERR_BUDGET, ERR_CANCELLED = range(9)
 BC_CALCULATED, BC_FIXED_VALUE, BC_FIXED_GRADIENT = 0, 1, 2
 SCHEME_LINEAR, SCHEME_UPWIND = 0, 1
-TERM_DDT, TERM_LAPLACIAN, TERM_DIV, TERM_SOURCE, TERM_EXPLICIT, TERM_DIV_FLUX = range(6)
+TERM_DDT, TERM_LAPLACIAN, TERM_DIV, TERM_SOURCE, TERM_EXPLICIT, TERM_DIV_FLUX, TERM_DIV_EXPLICIT = range(7)
 PREC_FP64, PREC_MIXED_IR = 0, 1
 
 vp = C.c_void_p
@@ -62,6 +62,20 @@ class BoxSpec(C.Structure):
                 ("jitter", dbl), ("seed", C.c_uint64), ("two_d", i32)]
 
 
+class ServerCfg(C.Structure):
+    _fields_ = [("budget_bytes", i64), ("n_streams", i32), ("max_active", i32)]
+
+
+class ServeRequest(C.Structure):
+    _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("steps", i32), ("U", dbl * 3), ("D", dbl), ("dt", dbl),
+                ("precision", i32), ("reserved", i32), ("T_out", vp)]
+
+
+class ServeResult(C.Structure):
+    _fields_ = [("id", i64), ("status", i32), ("steps_done", i32), ("total_iters", i32), ("reserved", i32),
+                ("submit_s", dbl), ("start_s", dbl), ("finish_s", dbl), ("device_bytes", i64)]
+
+
 class MeshArrays(C.Structure):
     _fields_ = [(name, vp) for name in (
         "points", "cell_volumes", "cell_centres", "owner", "neighbour", "face_areas", "face_centres",
@@ -78,6 +92,7 @@ _SIGS = {
     "fvgb_mesh_sizes": (C.c_int, [vp, P_i64]),
     "fvgb_mesh_device_bytes": (i64, [vp]),
     "fvgb_mesh_sparsity": (C.c_int, [vp, vp, vp, vp, vp, vp]),
+    "fvgb_mesh_create_boxes": (C.c_int, [vp, i32, C.POINTER(vp), vp, vp]),
     "fvgb_bc_correct": (C.c_int, [vp, i32, C.POINTER(BC), vp, vp, vp]),
     "fvgb_interp_linear": (C.c_int, [vp, i32, vp, vp, vp, vp]),
     "fvgb_interp_upwind": (C.c_int, [vp, i32, vp, vp, vp, vp, vp]),
@@ -107,6 +122,12 @@ _SIGS = {
     "fvgb_flux_vec": (C.c_int, [vp, vp, vp, vp, vp]),
     "fvgb_piso_face_update": (C.c_int, [vp, vp, vp, vp, vp]),
     "fvgb_piso_velocity_update": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
+    "fvgb_server_create": (C.c_int, [C.POINTER(ServerCfg), C.POINTER(vp)]),
+    "fvgb_server_submit": (C.c_int, [vp, C.POINTER(ServeRequest), P_i64]),
+    "fvgb_server_cancel": (C.c_int, [vp, i64]),
+    "fvgb_server_poll": (C.c_int, [vp, vp, i32, C.POINTER(i32)]),
+    "fvgb_server_info": (C.c_int, [vp, P_i64]),
+    "fvgb_server_destroy": (C.c_int, [vp]),
     "fvgb_box_sizes": (C.c_int, [C.POINTER(BoxSpec), P_i64]),
     "fvgb_box_build": (C.c_int, [C.POINTER(BoxSpec), C.POINTER(MeshArrays)]),
     "fvgb_geometry_compute": (C.c_int, [i32, vp, i32, i32, vp, vp, vp, i32, vp, i32,

@@ -66,6 +66,37 @@ __global__ void __launch_bounds__(kThreads)
         } else if (T.kind == FVGB_TERM_EXPLICIT) {
 #pragma unroll
             for (int k = 0; k < NC; ++k) r[k] = r[k] - cf * __ldg(&T.cell[c * NC + k]);
+        } else if (T.kind == FVGB_TERM_DIV_EXPLICIT) {
+            // sum of +-F*psi_f, psi_f interpolated from the term's field, faces ascending
+            double e[NC];
+#pragma unroll
+            for (int k = 0; k < NC; ++k) e[k] = 0.0;
+            for (int j = 0; j < gw; ++j) {
+                const int pos = gbase + j * 32 + lane;
+                const int code = __ldg(&m.g_code[pos]);
+                if (code == FVGB_PAD) break;
+                const double F = __ldg(&T.face[code >= 0 ? code : -code - 1]);
+                if (code >= m.nif) {
+                    const int b = code - m.nif;
+#pragma unroll
+                    for (int k = 0; k < NC; ++k) e[k] = e[k] + F * __ldg(&psi_b[b * NC + k]);
+                    continue;
+                }
+                const bool isOwner = code >= 0;
+                const int o = __ldg(&m.g_other[pos]);
+                const double wf = T.scheme == FVGB_SCHEME_LINEAR ? __ldg(&m.w[isOwner ? code : -code - 1]) : 0.0;
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    const double Tc = __ldg(&T.cell[c * NC + k]), To = __ldg(&T.cell[o * NC + k]);
+                    const double Town = isOwner ? Tc : To, Tnei = isOwner ? To : Tc;
+                    const double tf = T.scheme == FVGB_SCHEME_UPWIND ? (F >= 0.0 ? Town : Tnei)
+                                                                      : wf * (Town - Tnei) + Tnei;
+                    const double fl = F * tf;
+                    e[k] = isOwner ? e[k] + fl : e[k] - fl;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NC; ++k) r[k] = r[k] - cf * e[k];
         } else if (T.kind == FVGB_TERM_DIV_FLUX) {
             double dv = 0.0;  // sum of +-F over the row's faces, ascending face order
             for (int j = 0; j < gw; ++j) {
@@ -287,7 +318,13 @@ extern "C" fvgb_status fvgb_assemble(fvgb_ls* ls, const fvgb_term* terms, int32_
     bool needs_b = false, needs_dt = false;
     for (int i = 0; i < nterms; ++i) {
         const fvgb_term& t = terms[i];
-        FVGB_CHECK_ARG(t.kind >= FVGB_TERM_DDT && t.kind <= FVGB_TERM_DIV_FLUX, "fvgb_assemble: unknown term kind");
+        FVGB_CHECK_ARG(t.kind >= FVGB_TERM_DDT && t.kind <= FVGB_TERM_DIV_EXPLICIT, "fvgb_assemble: unknown term kind");
+        if (t.kind == FVGB_TERM_DIV_EXPLICIT) {
+            FVGB_CHECK_ARG(t.cell && t.face, "fvgb_assemble: explicit convection needs the field and the flux");
+            FVGB_CHECK_ARG(t.scheme == FVGB_SCHEME_LINEAR || t.scheme == FVGB_SCHEME_UPWIND,
+                           "fvgb_assemble: unknown div scheme");
+            needs_b = true;
+        }
         if (t.kind == FVGB_TERM_DDT) {
             FVGB_CHECK_ARG(t.cell, "fvgb_assemble: ddt needs the old-time field");
             needs_dt = true;
@@ -365,6 +402,8 @@ extern "C" fvgb_status fvgb_ls_export(const fvgb_ls* ls, double* values, double*
     FVGB_CHECK_ARG(ls, "fvgb_ls_export: null system");
     const fvgb_mesh* m = ls->mesh;
     cudaStream_t s = (cudaStream_t)stream;
+    if (values && !m->csr_pos)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_ls_export: this mesh keeps no CSR map (built on the device)");
     if (values) {
         k_gather_csr<<<grid_for(m->nnz, kThreads), kThreads, 0, s>>>(m->nnz, m->csr_pos, ls->values, values);
         FVGB_LAUNCH_CHECK("fvgb_ls_export");

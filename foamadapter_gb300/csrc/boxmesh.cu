@@ -1,0 +1,357 @@
+// Device-side builder of packed uniform hex boxes.
+//
+// Serving admits many box-shaped cases per second; building their mesh
+// arrays on the host (OpenFOAM geometry + sparsity + gather lists) costs about
+// a microsecond per cell plus the upload.  For an unjittered box every array
+// is a closed-form function of the cell index, so one kernel writes the whole
+// device mesh (geometry, gather lists, matrix pattern, slot maps) in place.
+//
+// Numbering follows the host box builder (and blockMesh): cells i fastest,
+// internal faces by owner then +x, +y, +z, boundary faces patch by patch
+// (xmin, xmax, ymin, ymax, zmin, zmax), each patch grouped by box.  Boxes start
+// at multiples of 32 cells; cells in the gaps are isolated placeholders
+// (volume 1, no faces).  Geometry is analytic (weights 0.5, delta 1/h, boundary
+// delta 2/h), so values can differ in the last bits from the triangle-
+// decomposition geometry of the host builder; every result computed on such a
+// mesh is reproducible on the same mesh.
+#include <cmath>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace {
+
+struct BoxDev {
+    int32_t nx, ny, nz, n;
+    int32_t cell0, face0;
+    int32_t bface0[6];
+    double hx, hy, hz;
+};
+
+// internal faces owned by cells before local cell (i,j,k) of the box
+__device__ __forceinline__ int32_t faces_before(const BoxDev& b, int i, int j, int k) {
+    const int nx = b.nx, ny = b.ny, nz = b.nz;
+    const int32_t rows = j + ny * k;
+    const int32_t X = rows * (nx - 1) + min(i, nx - 1);
+    const int32_t Y = k * nx * (ny - 1) + nx * min(j, ny - 1) + (j < ny - 1 ? i : 0);
+    const int32_t Z = nx * ny * min(k, nz - 1) + (k < nz - 1 ? j * nx + i : 0);
+    return X + Y + Z;
+}
+
+__device__ __forceinline__ int32_t face_of(const BoxDev& b, int i, int j, int k, int dir) {
+    // global index of the +dir face owned by local cell (i,j,k) (that face must exist)
+    int32_t f = b.face0 + faces_before(b, i, j, k);
+    if (dir >= 1 && i < b.nx - 1) ++f;
+    if (dir >= 2 && j < b.ny - 1) ++f;
+    return f;
+}
+
+struct MeshOut {
+    double *V, *invV, *Sf, *magSf, *w, *delta, *geo;
+    int32_t *own, *nei;
+    int32_t* bcells;
+    double *bSf, *bmagSf, *bdelta, *bgeo;
+    int32_t* bpatch;
+    int32_t *g_code, *g_other, *m_col, *m_code, *diag_pos, *own_pos, *nei_pos;
+};
+
+constexpr int kGW = 6;  // gather-list width (every box cell has 6 faces)
+constexpr int kMW = 7;  // matrix row width
+
+__global__ void k_box_cells(const BoxDev* __restrict__ boxes, const int32_t* __restrict__ slice_box, int N,
+                            int nif, MeshOut o) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const int slice = c >> 5, lane = c & 31;
+    const int gbase = slice * 32 * kGW + lane, mbase = slice * 32 * kMW + lane;
+    const int bi = slice_box[slice];
+    int loc = -1;
+    BoxDev b;
+    if (bi >= 0) {
+        b = boxes[bi];
+        loc = c - b.cell0;
+        if (loc >= b.n) loc = -1;
+    }
+    if (loc < 0) {  // placeholder: unit volume, no faces, diagonal-only row
+        o.V[c] = 1.0;
+        o.invV[c] = 1.0;
+        for (int k = 0; k < kGW; ++k) {
+            o.g_code[gbase + k * 32] = FVGB_PAD;
+            o.g_other[gbase + k * 32] = 0;
+        }
+        for (int k = 0; k < kMW; ++k) {
+            o.m_col[mbase + k * 32] = c;
+            o.m_code[mbase + k * 32] = k == 0 ? -1 : FVGB_PAD;
+        }
+        o.diag_pos[c] = mbase;
+        return;
+    }
+    const int nx = b.nx, ny = b.ny, nz = b.nz;
+    const int i = loc % nx, j = (loc / nx) % ny, k = loc / (nx * ny);
+    const int sy = nx, sz = nx * ny;
+    const double ax = b.hy * b.hz, ay = b.hx * b.hz, az = b.hx * b.hy;
+    const double vol = (b.hx * b.hy) * b.hz;
+    o.V[c] = vol;
+    o.invV[c] = 1.0 / vol;
+    // upper faces owned by this cell
+    int32_t f = b.face0 + faces_before(b, i, j, k);
+    const int32_t fx = i < nx - 1 ? f++ : -1;
+    const int32_t fy = j < ny - 1 ? f++ : -1;
+    const int32_t fz = k < nz - 1 ? f++ : -1;
+    const int32_t up_f[3] = {fx, fy, fz};
+    const int32_t up_n[3] = {c + 1, c + sy, c + sz};
+    const double up_a[3] = {ax, ay, az};
+    const double up_h[3] = {b.hx, b.hy, b.hz};
+    for (int d = 0; d < 3; ++d) {
+        const int32_t ff = up_f[d];
+        if (ff < 0) continue;
+        o.own[ff] = c;
+        o.nei[ff] = up_n[d];
+        o.Sf[3 * ff] = d == 0 ? ax : 0.0;
+        o.Sf[3 * ff + 1] = d == 1 ? ay : 0.0;
+        o.Sf[3 * ff + 2] = d == 2 ? az : 0.0;
+        o.magSf[ff] = up_a[d];
+        o.w[ff] = 0.5;
+        const double dc = 1.0 / up_h[d];
+        o.delta[ff] = dc;
+        o.geo[ff] = up_a[d] * dc;
+    }
+    // lower faces (this cell is the neighbour), ascending face index: -z, -y, -x
+    int32_t lo_f[3], lo_o[3];
+    int nlo = 0;
+    if (k > 0) {
+        lo_f[nlo] = face_of(b, i, j, k - 1, 2);
+        lo_o[nlo++] = c - sz;
+    }
+    if (j > 0) {
+        lo_f[nlo] = face_of(b, i, j - 1, k, 1);
+        lo_o[nlo++] = c - sy;
+    }
+    if (i > 0) {
+        lo_f[nlo] = face_of(b, i - 1, j, k, 0);
+        lo_o[nlo++] = c - 1;
+    }
+    // boundary faces of this cell, patch order
+    int32_t bf[6];
+    int nb = 0;
+    const double bdc[3] = {2.0 / b.hx, 2.0 / b.hy, 2.0 / b.hz};
+    auto bface = [&](int patch, int32_t idx, int d, double sign) {
+        const int32_t bb = b.bface0[patch] + idx;
+        o.bcells[bb] = c;
+        o.bSf[3 * bb] = d == 0 ? sign * ax : 0.0;
+        o.bSf[3 * bb + 1] = d == 1 ? sign * ay : 0.0;
+        o.bSf[3 * bb + 2] = d == 2 ? sign * az : 0.0;
+        o.bmagSf[bb] = up_a[d];
+        o.bdelta[bb] = bdc[d];
+        o.bgeo[bb] = up_a[d] * bdc[d];
+        o.bpatch[bb] = patch;
+        bf[nb++] = bb;
+    };
+    if (i == 0) bface(0, j + ny * k, 0, -1.0);
+    if (i == nx - 1) bface(1, j + ny * k, 0, 1.0);
+    if (j == 0) bface(2, i + nx * k, 1, -1.0);
+    if (j == ny - 1) bface(3, i + nx * k, 1, 1.0);
+    if (k == 0) bface(4, i + nx * j, 2, -1.0);
+    if (k == nz - 1) bface(5, i + nx * j, 2, 1.0);
+    // gather list
+    int g = 0;
+    for (int q = 0; q < nlo; ++q, ++g) {
+        o.g_code[gbase + g * 32] = -lo_f[q] - 1;
+        o.g_other[gbase + g * 32] = lo_o[q];
+    }
+    for (int d = 0; d < 3; ++d) {
+        if (up_f[d] < 0) continue;
+        o.g_code[gbase + g * 32] = up_f[d];
+        o.g_other[gbase + g * 32] = up_n[d];
+        ++g;
+    }
+    for (int q = 0; q < nb; ++q, ++g) {
+        o.g_code[gbase + g * 32] = nif + bf[q];
+        o.g_other[gbase + g * 32] = bf[q];
+    }
+    for (; g < kGW; ++g) {
+        o.g_code[gbase + g * 32] = FVGB_PAD;
+        o.g_other[gbase + g * 32] = 0;
+    }
+    // matrix row in column order: lower neighbours (ascending), diagonal, upper
+    int s = 0;
+    for (int q = 0; q < nlo; ++q, ++s) {  // lo_o is ascending: c-sz < c-sy < c-1
+        const int pos = mbase + s * 32;
+        o.m_col[pos] = lo_o[q];
+        o.m_code[pos] = -lo_f[q] - 2;
+        o.nei_pos[lo_f[q]] = pos;
+    }
+    o.m_col[mbase + s * 32] = c;
+    o.m_code[mbase + s * 32] = -1;
+    o.diag_pos[c] = mbase + s * 32;
+    ++s;
+    for (int d = 0; d < 3; ++d) {
+        if (up_f[d] < 0) continue;
+        const int pos = mbase + s * 32;
+        o.m_col[pos] = up_n[d];
+        o.m_code[pos] = up_f[d];
+        o.own_pos[up_f[d]] = pos;
+        ++s;
+    }
+    for (; s < kMW; ++s) {
+        o.m_col[mbase + s * 32] = c;
+        o.m_code[mbase + s * 32] = FVGB_PAD;
+    }
+}
+
+__global__ void k_fill_ptr(int32_t* p, int count, int width) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s <= count) p[s] = s * 32 * width;
+}
+
+void free_mesh_partial(fvgb_mesh* m) {
+    for (void* p : m->allocs) cudaFree(p);
+    delete m;
+}
+
+}  // namespace
+
+extern "C" fvgb_status fvgb_mesh_create_boxes(const fvgb_box_spec* specs, int32_t nboxes, fvgb_mesh** out,
+                                              int32_t* row_ranges, fvgb_stream stream) {
+    fvgb_clear_error();
+    FVGB_CHECK_ARG(specs && out && row_ranges && nboxes > 0, "fvgb_mesh_create_boxes: bad argument");
+    *out = nullptr;
+    std::vector<BoxDev> boxes(nboxes);
+    int64_t N = 0, NIF = 0;
+    int64_t nb_patch[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = 0; q < nboxes; ++q) {
+        const fvgb_box_spec& s = specs[q];
+        FVGB_CHECK_ARG(s.nx >= 1 && s.ny >= 1 && s.nz >= 1 && s.lx > 0 && s.ly > 0 && s.lz > 0,
+                       "fvgb_mesh_create_boxes: bad box size");
+        FVGB_CHECK_ARG(s.jitter == 0.0 && !s.two_d, "fvgb_mesh_create_boxes: unjittered 3-D boxes only");
+        BoxDev& b = boxes[q];
+        b.nx = s.nx;
+        b.ny = s.ny;
+        b.nz = s.nz;
+        const int64_t n = (int64_t)s.nx * s.ny * s.nz;
+        FVGB_CHECK_ARG(n < INT32_MAX / 8, "fvgb_mesh_create_boxes: box too large");
+        b.n = (int32_t)n;
+        N = (N + 31) / 32 * 32;
+        b.cell0 = (int32_t)N;
+        row_ranges[2 * q] = (int32_t)N;
+        row_ranges[2 * q + 1] = (int32_t)(N + n);
+        N += n;
+        b.face0 = (int32_t)NIF;
+        NIF += (int64_t)(s.nx - 1) * s.ny * s.nz + (int64_t)s.nx * (s.ny - 1) * s.nz + (int64_t)s.nx * s.ny * (s.nz - 1);
+        b.hx = s.lx / s.nx;
+        b.hy = s.ly / s.ny;
+        b.hz = s.lz / s.nz;
+        const int64_t pf[6] = {(int64_t)s.ny * s.nz, (int64_t)s.ny * s.nz, (int64_t)s.nx * s.nz,
+                               (int64_t)s.nx * s.nz, (int64_t)s.nx * s.ny, (int64_t)s.nx * s.ny};
+        for (int p = 0; p < 6; ++p) nb_patch[p] += pf[p];
+    }
+    N = (N + 31) / 32 * 32;
+    FVGB_CHECK_ARG(N + 2 * NIF < INT32_MAX / 2 && N * kMW < INT32_MAX, "fvgb_mesh_create_boxes: too large");
+    // boundary face offsets: patch-major, box-minor
+    int64_t NBF = 0;
+    std::vector<int32_t> poffs(7, 0);
+    for (int p = 0; p < 6; ++p) {
+        poffs[p] = (int32_t)NBF;
+        for (int q = 0; q < nboxes; ++q) {
+            const fvgb_box_spec& s = specs[q];
+            const int64_t pf = p < 2 ? (int64_t)s.ny * s.nz : (p < 4 ? (int64_t)s.nx * s.nz : (int64_t)s.nx * s.ny);
+            boxes[q].bface0[p] = (int32_t)NBF;
+            NBF += pf;
+        }
+    }
+    poffs[6] = (int32_t)NBF;
+    const int32_t nslices = (int32_t)(N / 32);
+    std::vector<int32_t> slice_box(nslices, -1);
+    for (int q = 0; q < nboxes; ++q)
+        for (int32_t sl = boxes[q].cell0 / 32; sl < (boxes[q].cell0 + boxes[q].n + 31) / 32; ++sl) slice_box[sl] = q;
+
+    fvgb_mesh* m = new fvgb_mesh();
+    m->h_patch_offs = poffs;
+    m->nnz = (int32_t)(N + 2 * NIF);
+    m->nslices = nslices;
+    m->m_len = (int64_t)N * kMW;
+    m->g_len = (int64_t)N * kGW;
+    MeshView& v = m->v;
+    v.n = (int32_t)N;
+    v.nif = (int32_t)NIF;
+    v.nbf = (int32_t)NBF;
+    v.npatch = 6;
+    MeshOut o{};
+    cudaError_t e = cudaSuccess;
+    auto A = [&](auto** p, int64_t count) {
+        if (e == cudaSuccess) e = mesh_alloc(m, p, count);
+    };
+    A(&o.V, N);
+    A(&o.invV, N);
+    A(&o.own, NIF);
+    A(&o.nei, NIF);
+    A(&o.Sf, 3 * NIF);
+    A(&o.magSf, NIF);
+    A(&o.w, NIF);
+    A(&o.delta, NIF);
+    A(&o.geo, NIF);
+    A(&o.bcells, NBF);
+    A(&o.bSf, 3 * NBF);
+    A(&o.bmagSf, NBF);
+    A(&o.bdelta, NBF);
+    A(&o.bgeo, NBF);
+    A(&o.bpatch, NBF);
+    int32_t *g_ptr = nullptr, *m_ptr = nullptr, *d_slice_box = nullptr;
+    BoxDev* d_boxes = nullptr;
+    A(&g_ptr, nslices + 1);
+    A(&m_ptr, nslices + 1);
+    A(&o.g_code, N * kGW);
+    A(&o.g_other, N * kGW);
+    A(&o.m_col, N * kMW);
+    A(&o.m_code, N * kMW);
+    A(&o.diag_pos, N);
+    A(&o.own_pos, NIF);
+    A(&o.nei_pos, NIF);
+    A(&d_slice_box, nslices);
+    A(&d_boxes, nboxes);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_slice_box, slice_box.data(), 4 * (size_t)nslices, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_boxes, boxes.data(), sizeof(BoxDev) * (size_t)nboxes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        free_mesh_partial(m);
+        return cuda_fail(e, "fvgb_mesh_create_boxes: allocation");
+    }
+    k_fill_ptr<<<grid_for(nslices + 1, 256), 256, 0, st>>>(g_ptr, nslices, kGW);
+    k_fill_ptr<<<grid_for(nslices + 1, 256), 256, 0, st>>>(m_ptr, nslices, kMW);
+    k_box_cells<<<grid_for(N, 256), 256, 0, st>>>(d_boxes, d_slice_box, (int)N, (int)NIF, o);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors above go out of scope
+    if (e != cudaSuccess) {
+        free_mesh_partial(m);
+        return cuda_fail(e, "fvgb_mesh_create_boxes: build");
+    }
+    v.V = o.V;
+    v.invV = o.invV;
+    v.own = o.own;
+    v.nei = o.nei;
+    v.Sf = o.Sf;
+    v.magSf = o.magSf;
+    v.w = o.w;
+    v.delta = o.delta;
+    v.geo = o.geo;
+    v.bcells = o.bcells;
+    v.bSf = o.bSf;
+    v.bmagSf = o.bmagSf;
+    v.bdelta = o.bdelta;
+    v.bgeo = o.bgeo;
+    v.bpatch = o.bpatch;
+    v.g_ptr = g_ptr;
+    v.g_code = o.g_code;
+    v.g_other = o.g_other;
+    v.m_ptr = m_ptr;
+    v.m_col = o.m_col;
+    v.m_code = o.m_code;
+    v.diag_pos = o.diag_pos;
+    v.own_pos = o.own_pos;
+    v.nei_pos = o.nei_pos;
+    m->csr_pos = nullptr;  // no host CSR copy: fvgb_mesh_sparsity / values export are not available
+    *out = m;
+    return FVGB_OK;
+}

@@ -302,6 +302,8 @@ extern "C" fvgb_status fvgb_mesh_sparsity(const fvgb_mesh* m, int32_t* row_offs,
                                           int32_t* diag_offset, int32_t* owner_offset,
                                           int32_t* neighbour_offset) {
     FVGB_CHECK_ARG(m, "fvgb_mesh_sparsity: null mesh");
+    if (m->h_row_offs.empty())
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_mesh_sparsity: this mesh keeps no CSR copy (built on the device)");
     auto cp = [](int32_t* dst, const std::vector<int32_t>& src) {
         if (dst && !src.empty()) std::memcpy(dst, src.data(), sizeof(int32_t) * src.size());
     };

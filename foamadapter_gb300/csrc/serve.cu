@@ -1,0 +1,404 @@
+// Serving loop: continuous batching of scalar advection-diffusion solves.
+//
+// Requests (a box mesh, a uniform velocity, a diffusivity and a number of
+// implicit steps) arrive at any time through fvgb_server_submit.  A host thread
+// admits waiting requests in arrival order whenever their estimated device
+// footprint fits the HBM budget, builds their mesh on the device
+// (fvgb_mesh_create_boxes) and keeps fields, matrix and solver state resident
+// until the request finishes.  Every tick advances EVERY active request by one
+// time step: the steps are enqueued on a pool of CUDA streams so that the
+// work of different requests overlaps on the GPU, then the tick waits for all
+// of them, retires finished requests (copying the result to the caller's host
+// buffer), frees their memory and admits more.  Each request runs exactly the
+// computation it would run alone, so its result does not depend on the mix.
+//
+// Time step (IMEX, as `imp::ddt(T) + exp::div(phi, T) - imp::laplacian(D, T)`):
+// explicit upwind convection of the previous field, implicit ddt + diffusion,
+// Jacobi-CG (FP64 or mixed precision) to a relative residual of 1e-8.
+// Boundaries: zero gradient; initial field: a Gaussian blob at the box centre.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "fvgb.h"
+#include "fvgb_host_common.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Slot {
+    int64_t id = 0;
+    fvgb_serve_request req{};
+    double submit_s = 0, start_s = 0;
+    int32_t steps_done = 0, iters = 0, status = FVGB_OK;
+    int64_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    fvgb_mesh* mesh = nullptr;
+    fvgb_ls* ls = nullptr;
+    int32_t n = 0, nif = 0, nbf = 0;
+    double *T = nullptr, *Told = nullptr, *Tb = nullptr, *F = nullptr, *gamma = nullptr, *ref = nullptr;
+    double *U = nullptr, *Ub = nullptr;
+    fvgb_solver_stats* stats_dev = nullptr;
+    int32_t types[6] = {FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT,
+                        FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT};
+    double dt = 0;
+};
+
+__attribute__((unused)) int64_t nbf_of(const fvgb_serve_request& r) {
+    return 2LL * ((int64_t)r.ny * r.nz + (int64_t)r.nx * r.nz + (int64_t)r.nx * r.ny);
+}
+
+}  // namespace
+
+struct fvgb_server {
+    fvgb_server_cfg cfg{};
+    std::vector<cudaStream_t> streams;
+    std::thread loop;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Slot*> waiting;
+    std::vector<Slot*> active;
+    std::vector<fvgb_serve_result> done;
+    std::vector<int64_t> cancel_ids;
+    int64_t next_id = 1, used = 0, peak_used = 0;
+    int64_t ticks = 0;
+    bool stop = false;
+    int device = 0;
+    Clock::time_point t0;
+    fvgb_solver_stats* h_stats = nullptr;  // pinned staging for per-step stats
+    size_t h_stats_cap = 0;
+
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+namespace {
+
+// Device bytes a request holds while resident (mesh, system, solver, fields).
+int64_t estimate_bytes(const fvgb_serve_request& r) {
+    const int64_t n = ((int64_t)r.nx * r.ny * r.nz + 31) / 32 * 32;
+    const int64_t nif = (int64_t)(r.nx - 1) * r.ny * r.nz + (int64_t)r.nx * (r.ny - 1) * r.nz +
+                        (int64_t)r.nx * r.ny * (r.nz - 1);
+    const int64_t nbf = nbf_of(r);
+    const int64_t mesh = 16 * n + 72 * nif + 64 * nbf + 4 * 6 * 2 * n + 4 * 7 * 2 * n + 4 * n;
+    const int64_t system = 8 * 7 * n + 8 * n + 16 * nbf;
+    const int64_t solver = r.precision == FVGB_PREC_MIXED_IR ? (8 + 28 + 16) * n : 40 * n;
+    const int64_t fields = 16 * n + 8 * nbf + 16 * (nif + nbf) + 24 * (n + nbf) + 8 * nbf;
+    return mesh + system + solver + fields + (1 << 20);
+}
+
+void release(Slot* s) {
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    double* bufs[] = {s->T, s->Told, s->Tb, s->F, s->gamma, s->ref, s->U, s->Ub};
+    for (double* b : bufs)
+        if (b) cudaFree(b);
+    if (s->stats_dev) cudaFree(s->stats_dev);
+    if (s->ls) fvgb_ls_destroy(s->ls);
+    if (s->mesh) fvgb_mesh_destroy(s->mesh);
+    s->T = s->Told = s->Tb = s->F = s->gamma = s->ref = s->U = s->Ub = nullptr;
+    s->stats_dev = nullptr;
+    s->ls = nullptr;
+    s->mesh = nullptr;
+}
+
+__global__ void k_blob(double* T, int nx, int ny, int nz, int cell0) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nx * ny * nz) return;
+    const int i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+    const double x = (i + 0.5) / nx - 0.5, y = (j + 0.5) / ny - 0.5, z = (k + 0.5) / nz - 0.5;
+    T[cell0 + c] = exp(-(x * x + y * y + z * z) / (2.0 * 0.1 * 0.1));
+}
+
+__global__ void k_fill3(double* a, int count, double x, double y, double z) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= count) return;
+    a[3 * c] = x;
+    a[3 * c + 1] = y;
+    a[3 * c + 2] = z;
+}
+
+__global__ void k_fill(double* a, int count, double v) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < count) a[c] = v;
+}
+
+fvgb_status setup(fvgb_server* sv, Slot* s) {
+    const fvgb_serve_request& r = s->req;
+    fvgb_box_spec spec{r.nx, r.ny, r.nz, 1.0, 1.0, 1.0, 0.0, 0, 0};
+    int32_t range[2];
+    fvgb_status st = fvgb_mesh_create_boxes(&spec, 1, &s->mesh, range, s->stream);
+    if (st != FVGB_OK) return st;
+    int64_t sz[5];
+    fvgb_mesh_sizes(s->mesh, sz);
+    s->n = (int32_t)sz[0];
+    s->nif = (int32_t)sz[1];
+    s->nbf = (int32_t)sz[2];
+    st = fvgb_ls_create(s->mesh, 1, &s->ls);
+    if (st != FVGB_OK) return st;
+    const size_t n = (size_t)s->n, nbf = (size_t)s->nbf, nf = (size_t)(s->nif + s->nbf);
+    cudaError_t e = cudaSuccess;
+    auto A = [&](double** p, size_t count) {
+        if (e == cudaSuccess) e = cudaMalloc(p, sizeof(double) * (count ? count : 1));
+    };
+    A(&s->T, n);
+    A(&s->Told, n);
+    A(&s->Tb, nbf);
+    A(&s->F, nf);
+    A(&s->gamma, nf);
+    A(&s->ref, nbf);
+    A(&s->U, 3 * n);
+    A(&s->Ub, 3 * nbf);
+    if (e == cudaSuccess) e = cudaMalloc(&s->stats_dev, sizeof(fvgb_solver_stats));
+    if (e != cudaSuccess) return fvgb_fail(FVGB_ERR_OOM, "server: request allocation");
+    const int nn = s->n, rn = r.nx * r.ny * r.nz;
+    k_fill<<<(nn + 255) / 256, 256, 0, s->stream>>>(s->T, nn, 0.0);
+    k_blob<<<(rn + 255) / 256, 256, 0, s->stream>>>(s->T, r.nx, r.ny, r.nz, range[0]);
+    k_fill<<<(int)((nbf + 255) / 256 + 1), 256, 0, s->stream>>>(s->ref, (int)nbf, 0.0);
+    k_fill<<<(int)((nf + 255) / 256), 256, 0, s->stream>>>(s->gamma, (int)nf, r.D);
+    k_fill3<<<(nn + 255) / 256, 256, 0, s->stream>>>(s->U, nn, r.U[0], r.U[1], r.U[2]);
+    k_fill3<<<(int)((nbf + 255) / 256 + 1), 256, 0, s->stream>>>(s->Ub, (int)nbf, r.U[0], r.U[1], r.U[2]);
+    fvgb_bc bc{s->types, s->ref};
+    st = fvgb_bc_correct(s->mesh, 1, &bc, s->T, s->Tb, s->stream);
+    if (st == FVGB_OK) st = fvgb_flux_vec(s->mesh, s->U, s->Ub, s->F, s->stream);
+    if (st != FVGB_OK) return st;
+    const double umag = std::sqrt(r.U[0] * r.U[0] + r.U[1] * r.U[1] + r.U[2] * r.U[2]);
+    const double h = 1.0 / std::max(r.nx, std::max(r.ny, r.nz));
+    s->dt = r.dt > 0 ? r.dt : 0.5 * h / std::max(umag, 1e-12);
+    (void)sv;
+    return FVGB_OK;
+}
+
+fvgb_status enqueue_step(Slot* s) {
+    const fvgb_serve_request& r = s->req;
+    cudaError_t e = cudaMemcpyAsync(s->Told, s->T, sizeof(double) * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream);
+    if (e != cudaSuccess) return fvgb_fail(FVGB_ERR_CUDA, "server: copy");
+    fvgb_term terms[3] = {
+        {FVGB_TERM_DDT, 0, 1.0, s->Told, nullptr},
+        {FVGB_TERM_DIV_EXPLICIT, FVGB_SCHEME_UPWIND, 1.0, s->Told, s->F},
+        {FVGB_TERM_LAPLACIAN, 0, -1.0, nullptr, s->gamma},
+    };
+    fvgb_bc bc{s->types, s->ref};
+    fvgb_status st = fvgb_assemble(s->ls, terms, 3, s->dt, &bc, s->Tb, s->stream);
+    if (st != FVGB_OK) return st;
+    fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, 1e-2, 1000, 50};
+    st = fvgb_solve_async(s->ls, s->T, &cfg, s->stats_dev, s->stream);
+    if (st != FVGB_OK) return st;
+    return fvgb_bc_correct(s->mesh, 1, &bc, s->T, s->Tb, s->stream);
+}
+
+void finish(fvgb_server* sv, Slot* s, int32_t status) {
+    if (status == FVGB_OK && s->req.T_out && s->mesh) {
+        // the box occupies rows [0, nx*ny*nz) of its own mesh
+        const size_t rn = (size_t)s->req.nx * s->req.ny * s->req.nz;
+        cudaMemcpyAsync(s->req.T_out, s->T, sizeof(double) * rn, cudaMemcpyDeviceToHost, s->stream);
+    }
+    release(s);
+    fvgb_serve_result res{};
+    res.id = s->id;
+    res.status = status;
+    res.steps_done = s->steps_done;
+    res.total_iters = s->iters;
+    res.submit_s = s->submit_s;
+    res.start_s = s->start_s;
+    res.finish_s = sv->now();
+    res.device_bytes = s->bytes;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->used -= s->bytes;
+    sv->done.push_back(res);
+    delete s;
+}
+
+void run(fvgb_server* sv) {
+    cudaSetDevice(sv->device);
+    size_t next_stream = 0;
+    for (;;) {
+        std::vector<Slot*> admit;
+        std::vector<int64_t> cancels;
+        {
+            std::unique_lock<std::mutex> lk(sv->mu);
+            sv->cv.wait(lk, [&] { return sv->stop || !sv->waiting.empty() || !sv->active.empty(); });
+            if (sv->stop && sv->waiting.empty() && sv->active.empty()) break;
+            cancels.swap(sv->cancel_ids);
+            // cancel waiting requests
+            for (auto it = sv->waiting.begin(); it != sv->waiting.end();) {
+                if (std::find(cancels.begin(), cancels.end(), (*it)->id) != cancels.end()) {
+                    fvgb_serve_result res{};
+                    res.id = (*it)->id;
+                    res.status = FVGB_ERR_CANCELLED;
+                    res.submit_s = (*it)->submit_s;
+                    res.finish_s = sv->now();
+                    sv->done.push_back(res);
+                    delete *it;
+                    it = sv->waiting.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+            // admit in arrival order while the head fits the budget
+            while (!sv->waiting.empty() && (int32_t)(sv->active.size() + admit.size()) < sv->cfg.max_active) {
+                Slot* s = sv->waiting.front();
+                if (sv->used + s->bytes > sv->cfg.budget_bytes) break;
+                sv->used += s->bytes;
+                sv->peak_used = std::max(sv->peak_used, sv->used);
+                sv->waiting.pop_front();
+                admit.push_back(s);
+            }
+        }
+        for (Slot* s : admit) {
+            s->stream = sv->streams[next_stream++ % sv->streams.size()];
+            s->start_s = sv->now();
+            fvgb_status st = setup(sv, s);
+            if (st != FVGB_OK) {
+                finish(sv, s, st);
+                continue;
+            }
+            sv->active.push_back(s);
+        }
+        // cancel active requests between steps
+        if (!cancels.empty()) {
+            std::vector<Slot*> keep;
+            for (Slot* s : sv->active) {
+                if (std::find(cancels.begin(), cancels.end(), s->id) != cancels.end()) finish(sv, s, FVGB_ERR_CANCELLED);
+                else keep.push_back(s);
+            }
+            sv->active.swap(keep);
+        }
+        if (sv->active.empty()) continue;
+        // one step of every active request, overlapping across streams
+        if (sv->h_stats_cap < sv->active.size()) {
+            if (sv->h_stats) cudaFreeHost(sv->h_stats);
+            sv->h_stats_cap = sv->active.size() * 2;
+            cudaMallocHost(&sv->h_stats, sizeof(fvgb_solver_stats) * sv->h_stats_cap);
+        }
+        std::vector<int32_t> failed(sv->active.size(), FVGB_OK);
+        for (size_t q = 0; q < sv->active.size(); ++q) {
+            Slot* s = sv->active[q];
+            failed[q] = enqueue_step(s);
+            if (failed[q] == FVGB_OK)
+                cudaMemcpyAsync(&sv->h_stats[q], s->stats_dev, sizeof(fvgb_solver_stats), cudaMemcpyDeviceToHost,
+                                s->stream);
+        }
+        for (cudaStream_t st : sv->streams) cudaStreamSynchronize(st);
+        ++sv->ticks;
+        std::vector<Slot*> keep;
+        for (size_t q = 0; q < sv->active.size(); ++q) {
+            Slot* s = sv->active[q];
+            int32_t status = failed[q];
+            if (status == FVGB_OK) {
+                const fvgb_solver_stats& stt = sv->h_stats[q];
+                s->iters += stt.num_iter;
+                s->steps_done += 1;
+                if (stt.status != FVGB_OK) status = stt.status;
+            }
+            if (status != FVGB_OK || s->steps_done >= s->req.steps) finish(sv, s, status);
+            else keep.push_back(s);
+        }
+        sv->active.swap(keep);
+        for (cudaStream_t st : sv->streams) cudaStreamSynchronize(st);  // result copies of retired requests
+    }
+}
+
+}  // namespace
+
+extern "C" fvgb_status fvgb_server_create(const fvgb_server_cfg* cfg, fvgb_server** out) {
+    fvgb_clear_error();
+    if (!cfg || !out || cfg->budget_bytes <= 0 || cfg->n_streams <= 0 || cfg->n_streams > 64 || cfg->max_active <= 0)
+        return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_server_create: bad configuration");
+    fvgb_server* sv = new fvgb_server();
+    sv->cfg = *cfg;
+    sv->t0 = Clock::now();
+    cudaGetDevice(&sv->device);
+    for (int i = 0; i < cfg->n_streams; ++i) {
+        cudaStream_t s;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+            for (cudaStream_t t : sv->streams) cudaStreamDestroy(t);
+            delete sv;
+            return fvgb_fail(FVGB_ERR_CUDA, "fvgb_server_create: stream creation");
+        }
+        sv->streams.push_back(s);
+    }
+    sv->loop = std::thread(run, sv);
+    *out = sv;
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_server_submit(fvgb_server* sv, const fvgb_serve_request* req, int64_t* id) {
+    if (!sv || !req || !id) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_server_submit: null argument");
+    if (req->nx < 2 || req->ny < 2 || req->nz < 2 || req->steps < 1 || !(req->D >= 0) ||
+        (req->precision != FVGB_PREC_FP64 && req->precision != FVGB_PREC_MIXED_IR))
+        return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_server_submit: bad request");
+    Slot* s = new Slot();
+    s->req = *req;
+    s->bytes = estimate_bytes(*req);
+    if (s->bytes > sv->cfg.budget_bytes) {
+        delete s;
+        return fvgb_fail(FVGB_ERR_BUDGET, "fvgb_server_submit: request alone exceeds the HBM budget");
+    }
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (sv->stop) {
+            delete s;
+            return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_server_submit: server is shutting down");
+        }
+        s->id = sv->next_id++;
+        s->submit_s = sv->now();
+        sv->waiting.push_back(s);
+        *id = s->id;
+    }
+    sv->cv.notify_one();
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_server_cancel(fvgb_server* sv, int64_t id) {
+    if (!sv) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_server_cancel: null server");
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->cancel_ids.push_back(id);
+    }
+    sv->cv.notify_one();
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_server_poll(fvgb_server* sv, fvgb_serve_result* out, int32_t max, int32_t* count) {
+    if (!sv || !count || (max > 0 && !out)) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_server_poll: bad argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    const int32_t k = std::min<int32_t>(max, (int32_t)sv->done.size());
+    for (int32_t i = 0; i < k; ++i) out[i] = sv->done[i];
+    sv->done.erase(sv->done.begin(), sv->done.begin() + k);
+    *count = k;
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_server_info(fvgb_server* sv, int64_t out[6]) {
+    if (!sv || !out) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_server_info: bad argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    out[0] = (int64_t)sv->waiting.size();
+    out[1] = (int64_t)sv->active.size();
+    out[2] = (int64_t)sv->done.size();
+    out[3] = sv->used;
+    out[4] = sv->peak_used;
+    out[5] = sv->ticks;
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_server_destroy(fvgb_server* sv) {
+    if (!sv) return FVGB_OK;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv.notify_one();
+    if (sv->loop.joinable()) sv->loop.join();
+    for (cudaStream_t s : sv->streams) cudaStreamDestroy(s);
+    if (sv->h_stats) cudaFreeHost(sv->h_stats);
+    delete sv;
+    return FVGB_OK;
+}

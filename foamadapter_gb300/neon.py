@@ -201,6 +201,12 @@ def explicit(values: torch.Tensor, coeff: float = 1.0) -> Term:
     return Term(abi.TERM_EXPLICIT, coeff, cell=values)
 
 
+def div_explicit(flux: SurfaceField, field: torch.Tensor, scheme="upwind", coeff: float = 1.0) -> Term:
+    """dsl::exp::div(phi, psi) of `field` (psi's boundary values are taken from
+    the assembled field), volume integrated into the rhs."""
+    return Term(abi.TERM_DIV_EXPLICIT, coeff, scheme=_scheme(scheme), cell=field, face=flux.values)
+
+
 def div_flux(flux: SurfaceField, coeff: float = 1.0) -> Term:
     """dsl::exp::div(phi) of a face flux, volume integrated, into the rhs."""
     return Term(abi.TERM_DIV_FLUX, coeff, face=flux.values)

@@ -101,6 +101,20 @@ fvgb_status fvgb_mesh_sizes(const fvgb_mesh* mesh, int64_t out[5]);
 /* Device bytes held by the mesh handle (geometry + index structures). */
 int64_t fvgb_mesh_device_bytes(const fvgb_mesh* mesh);
 
+/* Build ONE device mesh holding `nboxes` unjittered 3-D hex boxes packed
+ * block-diagonally, entirely on the device (no host geometry, no upload of
+ * mesh arrays).  Box q's cells are rows [row_ranges[2q], row_ranges[2q+1])
+ * (HOST output array [2*nboxes]); boxes start at multiples of 32 cells and the
+ * cells between them are isolated placeholders.  Patches: xmin, xmax, ymin,
+ * ymax, zmin, zmax, each grouped by box.  Geometry is analytic (weights 0.5,
+ * delta 1/h, boundary delta 2/h).  Such a mesh keeps no host CSR copy:
+ * fvgb_mesh_sparsity and the values part of fvgb_ls_export return
+ * FVGB_ERR_UNSUPPORTED.  No counterpart in the reference (its meshes come
+ * from OpenFOAM); used by the serving loop, which admits many boxes per second. */
+struct fvgb_box_spec;
+fvgb_status fvgb_mesh_create_boxes(const struct fvgb_box_spec* specs, int32_t nboxes, fvgb_mesh** out,
+                                   int32_t* row_ranges, fvgb_stream stream);
+
 /* CSR sparsity pattern in NeoN's layout, copied to HOST arrays:
  * row_offs[n+1], col_idxs[nnz], diag_offset[n], owner_offset[n_ifaces],
  * neighbour_offset[n_ifaces] (offsets relative to the row start).
@@ -178,8 +192,12 @@ typedef enum fvgb_term_kind {
     FVGB_TERM_DIV = 2,             /* implicit div(flux, psi), linear or upwind        */
     FVGB_TERM_SOURCE = 3,          /* implicit source: diag += coeff*s_P*V_P           */
     FVGB_TERM_EXPLICIT = 4,        /* rhs -= coeff*E_P (E already volume integrated)   */
-    FVGB_TERM_DIV_FLUX = 5         /* rhs -= coeff*sum_f(+-F_f): explicit div of a face
+    FVGB_TERM_DIV_FLUX = 5,        /* rhs -= coeff*sum_f(+-F_f): explicit div of a face
                                       flux, volume integrated (dsl::exp::div(phi))     */
+    FVGB_TERM_DIV_EXPLICIT = 6     /* rhs -= coeff*sum_f(+-F_f*psi_f) with psi_f from the
+                                      term's cell field (`cell`, boundary values psi_b),
+                                      linear or upwind: dsl::exp::div(phi, psi), volume
+                                      integrated (IMEX convection)                     */
 } fvgb_term_kind;
 
 /* One operator of a dsl::Expression. The expression is
@@ -191,8 +209,9 @@ typedef struct fvgb_term {
     int32_t scheme;        /* DIV: FVGB_SCHEME_LINEAR or FVGB_SCHEME_UPWIND           */
     double coeff;          /* operator scaling                                        */
     const double* cell;    /* DDT: old-time psi [n*ncomp]; SOURCE: s [n] or NULL (=1);
-                              EXPLICIT: E [n*ncomp]                                   */
-    const double* face;    /* LAPLACIAN: gamma [nIF+nBF]; DIV, DIV_FLUX: face flux [nIF+nBF] */
+                              EXPLICIT: E [n*ncomp]; DIV_EXPLICIT: the convected field  */
+    const double* face;    /* LAPLACIAN: gamma [nIF+nBF]; DIV, DIV_FLUX, DIV_EXPLICIT:
+                              face flux [nIF+nBF]                                       */
 } fvgb_term;
 
 /* LinearSystem on the mesh pattern: values[nnz], rhs[n*ncomp],
@@ -323,6 +342,55 @@ fvgb_status fvgb_piso_face_update(const fvgb_ls* peqn, const double* phiHbyA, co
 fvgb_status fvgb_piso_velocity_update(const fvgb_mesh* mesh, const double* HbyA,
                                       const double* rAU, const double* p, const double* p_b,
                                       double* U, fvgb_stream stream);
+
+/* ----------------------------------------------------------------- serving */
+/* A serving loop for scalar advection-diffusion solves (no counterpart in the
+ * reference): requests arrive at any time, are admitted in arrival order as
+ * the HBM budget allows, keep their mesh, fields, matrix and solver state on
+ * the device while they run, and every tick advances all active requests by
+ * one implicit step, overlapping their work on a pool of CUDA streams.
+ * A request's result does not depend on what else runs (each request executes
+ * exactly its own computation).  The loop runs on its own host thread. */
+typedef struct fvgb_server fvgb_server;
+typedef struct fvgb_server_cfg {
+    int64_t budget_bytes;      /* device bytes requests may hold at once              */
+    int32_t n_streams;         /* CUDA streams the active requests are spread over    */
+    int32_t max_active;        /* cap on concurrently active requests                 */
+} fvgb_server_cfg;
+/* One request: the unit box [0,1]^3 with nx*ny*nz cells, a uniform velocity U,
+ * diffusivity D, `steps` implicit steps of  ddt(T) + div(phi,T) - laplacian(D,T) = 0
+ * (explicit upwind convection, implicit diffusion, zero-gradient walls, initial
+ * Gaussian blob at the centre); dt <= 0 picks 0.5*h/|U|.  T_out: optional HOST
+ * buffer [nx*ny*nz] that receives the final field. */
+typedef struct fvgb_serve_request {
+    int32_t nx, ny, nz, steps;
+    double U[3];
+    double D;
+    double dt;
+    int32_t precision;         /* FVGB_PREC_FP64 or FVGB_PREC_MIXED_IR                */
+    int32_t reserved;
+    double* T_out;
+} fvgb_serve_request;
+typedef struct fvgb_serve_result {
+    int64_t id;
+    int32_t status;            /* FVGB_OK, a solver status, FVGB_ERR_CANCELLED        */
+    int32_t steps_done;
+    int32_t total_iters;
+    int32_t reserved;
+    double submit_s, start_s, finish_s;   /* seconds since the server started        */
+    int64_t device_bytes;      /* the budget the request held                         */
+} fvgb_serve_result;
+fvgb_status fvgb_server_create(const fvgb_server_cfg* cfg, fvgb_server** out);
+/* Thread safe; FVGB_ERR_BUDGET if the request alone exceeds the budget. */
+fvgb_status fvgb_server_submit(fvgb_server* server, const fvgb_serve_request* req, int64_t* id);
+/* Cancel a waiting or running request (takes effect between steps). */
+fvgb_status fvgb_server_cancel(fvgb_server* server, int64_t id);
+/* Move up to `max` finished results out; *count = how many. */
+fvgb_status fvgb_server_poll(fvgb_server* server, fvgb_serve_result* out, int32_t max, int32_t* count);
+/* [waiting, active, finished-unpolled, bytes in use, peak bytes, ticks] */
+fvgb_status fvgb_server_info(fvgb_server* server, int64_t out[6]);
+/* Finishes every submitted request, then stops the loop. */
+fvgb_status fvgb_server_destroy(fvgb_server* server);
 
 /* ------------------------------------------------------------ mesh builder */
 /* Host helpers (no GPU): an OpenFOAM-ordered hex box and OpenFOAM geometry.

@@ -21,7 +21,8 @@
 
 enum { BC_CALCULATED = 0, BC_FIXED_VALUE = 1, BC_FIXED_GRADIENT = 2 };
 enum { SCHEME_LINEAR = 0, SCHEME_UPWIND = 1 };
-enum { TERM_DDT = 0, TERM_LAPLACIAN = 1, TERM_DIV = 2, TERM_SOURCE = 3, TERM_EXPLICIT = 4, TERM_DIV_FLUX = 5 };
+enum { TERM_DDT = 0, TERM_LAPLACIAN = 1, TERM_DIV = 2, TERM_SOURCE = 3, TERM_EXPLICIT = 4, TERM_DIV_FLUX = 5,
+       TERM_DIV_EXPLICIT = 6 };
 enum { ST_OK = 0, ST_NOT_CONVERGED = 3, ST_BREAKDOWN = 4, ST_UNSUPPORTED = 6 };
 
 #define RED_THREADS 256
@@ -246,6 +247,8 @@ int32_t or_sparsity(const or_mesh* m, int32_t* row_offs, int32_t* col, int32_t* 
  *   SOURCE:    a_PP += (c*s)*V   (s = 1 if absent)
  *   EXPLICIT:  b_P  -= c*E
  *   DIV_FLUX:  E_P = sum of +-F_f (owner +, neighbour -, boundary +, face order); b_P -= c*E_P
+ *   DIV_EXPLICIT: E_P = sum of +-F_f*psi_f (psi_f of the term's field, linear or upwind,
+ *              boundary psi_b), the Serial face loop of GaussGreenDiv without 1/V; b_P -= c*E_P
  *   LAPLACIAN: g = c*(gamma*(|Sf|*delta)); a_PN += g, a_PP -= g, a_NP += g, a_NN -= g;
  *              boundary value faces: m = c*(gamma_b*(|Sf_b|*delta_b)), r = m*v_b;
  *              fixedGradient faces:  m = 0, r = (c*(gamma_b*|Sf_b|))*g_b
@@ -278,6 +281,24 @@ void or_assemble(const or_mesh* m, const or_csr* A, int32_t nc, const or_term* t
             for (int32_t i = 0; i < n; ++i) DIAG(i) += (T->cell ? c * T->cell[i] : c) * m->V[i];
         } else if (T->kind == TERM_EXPLICIT) {
             for (int32_t i = 0; i < n * nc; ++i) rhs[i] -= c * T->cell[i];
+        } else if (T->kind == TERM_DIV_EXPLICIT) {
+            const int32_t nf = m->nif + m->nbf;
+            double* phif = zalloc((size_t)nf * nc);
+            if (T->scheme == SCHEME_UPWIND) or_interp_upwind(m, nc, T->face, T->cell, psi_b, phif);
+            else or_interp_linear(m, nc, T->cell, psi_b, phif);
+            double* e = zalloc((size_t)n * nc);
+            for (int32_t f = 0; f < m->nif; ++f)
+                for (int32_t k = 0; k < nc; ++k) {
+                    double fl = T->face[f] * phif[f * nc + k];
+                    e[m->own[f] * nc + k] += fl;
+                    e[m->nei[f] * nc + k] -= fl;
+                }
+            for (int32_t b = 0; b < m->nbf; ++b)
+                for (int32_t k = 0; k < nc; ++k)
+                    e[m->bcells[b] * nc + k] += T->face[m->nif + b] * phif[(m->nif + b) * nc + k];
+            for (int32_t i = 0; i < n * nc; ++i) rhs[i] -= c * e[i];
+            free(e);
+            free(phif);
         } else if (T->kind == TERM_DIV_FLUX) {
             double* e = zalloc((size_t)n);
             for (int32_t f = 0; f < m->nif; ++f) {

@@ -71,11 +71,12 @@ def test_assembly_all_terms_bit_exact(cuda, ncomp):
         E = rng.standard_normal(hm.n * ncomp)
         g = [neon.ddt(neon.dev(old)), neon.laplacian(neon.SurfaceField(dm, gamma), -0.8),
              neon.div(neon.SurfaceField(dm, F), "upwind", 1.3), neon.div(neon.SurfaceField(dm, F), "linear", 0.6),
-             neon.source(0.4, neon.dev(s)), neon.explicit(neon.dev(E), -1.0)]
+             neon.source(0.4, neon.dev(s)), neon.explicit(neon.dev(E), -1.0),
+             neon.div_explicit(neon.SurfaceField(dm, F), neon.dev(old), "upwind", 0.9)]
         h = [(abi.TERM_DDT, 0, 1.0, old, None), (abi.TERM_LAPLACIAN, 0, -0.8, None, gamma),
              (abi.TERM_DIV, abi.SCHEME_UPWIND, 1.3, None, F), (abi.TERM_DIV, abi.SCHEME_LINEAR, 0.6, None, F),
-             (abi.TERM_SOURCE, 0, 0.4, s, None), (abi.TERM_EXPLICIT, 0, -1.0, E, None)]
-        g[0].keep = old
+             (abi.TERM_SOURCE, 0, 0.4, s, None), (abi.TERM_EXPLICIT, 0, -1.0, E, None),
+             (abi.TERM_DIV_EXPLICIT, abi.SCHEME_UPWIND, 0.9, old, F)]
         return g, h
 
     ls, T, o, gpu, ref = assemble_both(hm, dm, terms, bcs, ncomp)
