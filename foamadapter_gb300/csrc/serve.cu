@@ -5,12 +5,16 @@
 // admits waiting requests in arrival order whenever their estimated device
 // footprint fits the HBM budget, builds their mesh on the device
 // (fvgb_mesh_create_boxes) and keeps fields, matrix and solver state resident
-// until the request finishes.  Every tick advances EVERY active request by one
-// time step: the steps are enqueued on a pool of CUDA streams so that the
-// work of different requests overlaps on the GPU, then the tick waits for all
-// of them, retires finished requests (copying the result to the caller's host
-// buffer), frees their memory and admits more.  Each request runs exactly the
-// computation it would run alone, so its result does not depend on the mix.
+// until the request finishes.  Each active request advances on its own CUDA
+// stream (from a pool) in chunks of a few time steps; the loop polls the
+// chunk-completion events, enqueues the next chunk of every request whose
+// previous chunk finished, retires finished requests (copying the result to the
+// caller's host buffer) and admits waiting ones as budget frees up, so requests
+// of very different sizes progress at their own pace and their work overlaps
+// on the GPU.  Device memory of retired requests is released in batches (one
+// device synchronisation per batch, not per request).  Each request runs
+// exactly the computation it would run alone, so its result does not depend
+// on the mix.
 //
 // Time step (IMEX, as `imp::ddt(T) + exp::div(phi, T) - imp::laplacian(D, T)`):
 // explicit upwind convection of the previous field, implicit ddt + diffusion,
@@ -34,6 +38,7 @@
 namespace {
 
 using Clock = std::chrono::steady_clock;
+constexpr int kChunk = 4;  // steps enqueued per request before the loop looks at it again
 
 struct Slot {
     int64_t id = 0;
@@ -47,7 +52,10 @@ struct Slot {
     int32_t n = 0, nif = 0, nbf = 0;
     double *T = nullptr, *Told = nullptr, *Tb = nullptr, *F = nullptr, *gamma = nullptr, *ref = nullptr;
     double *U = nullptr, *Ub = nullptr;
-    fvgb_solver_stats* stats_dev = nullptr;
+    fvgb_solver_stats* stats_dev = nullptr;  // [kChunk]
+    fvgb_solver_stats* stats_host = nullptr; // pinned [kChunk]
+    cudaEvent_t done_ev = nullptr;
+    int32_t inflight = 0;                    // steps of the chunk in flight
     int32_t types[6] = {FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT,
                         FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT};
     double dt = 0;
@@ -74,8 +82,7 @@ struct fvgb_server {
     bool stop = false;
     int device = 0;
     Clock::time_point t0;
-    fvgb_solver_stats* h_stats = nullptr;  // pinned staging for per-step stats
-    size_t h_stats_cap = 0;
+    std::vector<Slot*> graveyard;           // retired, memory not yet released
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
@@ -96,11 +103,14 @@ int64_t estimate_bytes(const fvgb_serve_request& r) {
 }
 
 void release(Slot* s) {
-    if (s->stream) cudaStreamSynchronize(s->stream);
     double* bufs[] = {s->T, s->Told, s->Tb, s->F, s->gamma, s->ref, s->U, s->Ub};
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (s->stats_dev) cudaFree(s->stats_dev);
+    if (s->stats_host) cudaFreeHost(s->stats_host);
+    if (s->done_ev) cudaEventDestroy(s->done_ev);
+    s->stats_host = nullptr;
+    s->done_ev = nullptr;
     if (s->ls) fvgb_ls_destroy(s->ls);
     if (s->mesh) fvgb_mesh_destroy(s->mesh);
     s->T = s->Told = s->Tb = s->F = s->gamma = s->ref = s->U = s->Ub = nullptr;
@@ -156,7 +166,9 @@ fvgb_status setup(fvgb_server* sv, Slot* s) {
     A(&s->ref, nbf);
     A(&s->U, 3 * n);
     A(&s->Ub, 3 * nbf);
-    if (e == cudaSuccess) e = cudaMalloc(&s->stats_dev, sizeof(fvgb_solver_stats));
+    if (e == cudaSuccess) e = cudaMalloc(&s->stats_dev, sizeof(fvgb_solver_stats) * kChunk);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->stats_host, sizeof(fvgb_solver_stats) * kChunk);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->done_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return fvgb_fail(FVGB_ERR_OOM, "server: request allocation");
     const int nn = s->n, rn = r.nx * r.ny * r.nz;
     k_fill<<<(nn + 255) / 256, 256, 0, s->stream>>>(s->T, nn, 0.0);
@@ -176,7 +188,7 @@ fvgb_status setup(fvgb_server* sv, Slot* s) {
     return FVGB_OK;
 }
 
-fvgb_status enqueue_step(Slot* s) {
+fvgb_status enqueue_step(Slot* s, int k) {
     const fvgb_serve_request& r = s->req;
     cudaError_t e = cudaMemcpyAsync(s->Told, s->T, sizeof(double) * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream);
     if (e != cudaSuccess) return fvgb_fail(FVGB_ERR_CUDA, "server: copy");
@@ -189,7 +201,7 @@ fvgb_status enqueue_step(Slot* s) {
     fvgb_status st = fvgb_assemble(s->ls, terms, 3, s->dt, &bc, s->Tb, s->stream);
     if (st != FVGB_OK) return st;
     fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, 1e-2, 1000, 50};
-    st = fvgb_solve_async(s->ls, s->T, &cfg, s->stats_dev, s->stream);
+    st = fvgb_solve_async(s->ls, s->T, &cfg, s->stats_dev + k, s->stream);
     if (st != FVGB_OK) return st;
     return fvgb_bc_correct(s->mesh, 1, &bc, s->T, s->Tb, s->stream);
 }
@@ -200,7 +212,7 @@ void finish(fvgb_server* sv, Slot* s, int32_t status) {
         const size_t rn = (size_t)s->req.nx * s->req.ny * s->req.nz;
         cudaMemcpyAsync(s->req.T_out, s->T, sizeof(double) * rn, cudaMemcpyDeviceToHost, s->stream);
     }
-    release(s);
+    if (s->stream) cudaStreamSynchronize(s->stream);  // result copy done before the caller sees it
     fvgb_serve_result res{};
     res.id = s->id;
     res.status = status;
@@ -210,10 +222,26 @@ void finish(fvgb_server* sv, Slot* s, int32_t status) {
     res.start_s = s->start_s;
     res.finish_s = sv->now();
     res.device_bytes = s->bytes;
+    sv->graveyard.push_back(s);  // device memory released in a batch (release_graveyard)
     std::lock_guard<std::mutex> lk(sv->mu);
-    sv->used -= s->bytes;
     sv->done.push_back(res);
-    delete s;
+}
+
+// One device synchronisation for many retired requests; then their memory and
+// budget are returned.
+void release_graveyard(fvgb_server* sv, bool force) {
+    if (sv->graveyard.empty()) return;
+    if (!force && sv->graveyard.size() < 16) return;
+    cudaDeviceSynchronize();
+    int64_t freed = 0;
+    for (Slot* s : sv->graveyard) {
+        release(s);
+        freed += s->bytes;
+        delete s;
+    }
+    sv->graveyard.clear();
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->used -= freed;
 }
 
 void run(fvgb_server* sv) {
@@ -271,39 +299,59 @@ void run(fvgb_server* sv) {
             }
             sv->active.swap(keep);
         }
-        if (sv->active.empty()) continue;
-        // one step of every active request, overlapping across streams
-        if (sv->h_stats_cap < sv->active.size()) {
-            if (sv->h_stats) cudaFreeHost(sv->h_stats);
-            sv->h_stats_cap = sv->active.size() * 2;
-            cudaMallocHost(&sv->h_stats, sizeof(fvgb_solver_stats) * sv->h_stats_cap);
-        }
-        std::vector<int32_t> failed(sv->active.size(), FVGB_OK);
-        for (size_t q = 0; q < sv->active.size(); ++q) {
-            Slot* s = sv->active[q];
-            failed[q] = enqueue_step(s);
-            if (failed[q] == FVGB_OK)
-                cudaMemcpyAsync(&sv->h_stats[q], s->stats_dev, sizeof(fvgb_solver_stats), cudaMemcpyDeviceToHost,
-                                s->stream);
-        }
-        for (cudaStream_t st : sv->streams) cudaStreamSynchronize(st);
-        ++sv->ticks;
+        // advance every request whose previous chunk finished
+        bool progressed = !admit.empty();
         std::vector<Slot*> keep;
-        for (size_t q = 0; q < sv->active.size(); ++q) {
-            Slot* s = sv->active[q];
-            int32_t status = failed[q];
-            if (status == FVGB_OK) {
-                const fvgb_solver_stats& stt = sv->h_stats[q];
-                s->iters += stt.num_iter;
-                s->steps_done += 1;
-                if (stt.status != FVGB_OK) status = stt.status;
+        for (Slot* s : sv->active) {
+            if (s->inflight > 0) {
+                const cudaError_t q = cudaEventQuery(s->done_ev);
+                if (q == cudaErrorNotReady) {
+                    keep.push_back(s);
+                    continue;
+                }
+                progressed = true;
+                int32_t status = q == cudaSuccess ? FVGB_OK : FVGB_ERR_CUDA;
+                for (int k = 0; k < s->inflight && status == FVGB_OK; ++k) {
+                    s->iters += s->stats_host[k].num_iter;
+                    s->steps_done += 1;
+                    if (s->stats_host[k].status != FVGB_OK) status = s->stats_host[k].status;
+                }
+                s->inflight = 0;
+                if (status != FVGB_OK || s->steps_done >= s->req.steps) {
+                    finish(sv, s, status);
+                    continue;
+                }
             }
-            if (status != FVGB_OK || s->steps_done >= s->req.steps) finish(sv, s, status);
-            else keep.push_back(s);
+            const int todo = std::min(kChunk, s->req.steps - s->steps_done);
+            int32_t status = FVGB_OK;
+            for (int k = 0; k < todo && status == FVGB_OK; ++k) status = enqueue_step(s, k);
+            if (status == FVGB_OK &&
+                cudaMemcpyAsync(s->stats_host, s->stats_dev, sizeof(fvgb_solver_stats) * todo,
+                                cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
+                status = FVGB_ERR_CUDA;
+            if (status == FVGB_OK && cudaEventRecord(s->done_ev, s->stream) != cudaSuccess) status = FVGB_ERR_CUDA;
+            if (status != FVGB_OK) {
+                finish(sv, s, status);
+                continue;
+            }
+            s->inflight = todo;
+            progressed = true;
+            keep.push_back(s);
         }
         sv->active.swap(keep);
-        for (cudaStream_t st : sv->streams) cudaStreamSynchronize(st);  // result copies of retired requests
+        ++sv->ticks;
+        bool flush;
+        {
+            // release now if nothing runs, or if the next waiting request is held back
+            // by budget that retired requests still hold
+            std::lock_guard<std::mutex> lk(sv->mu);
+            flush = sv->active.empty() ||
+                    (!sv->waiting.empty() && sv->used + sv->waiting.front()->bytes > sv->cfg.budget_bytes);
+        }
+        release_graveyard(sv, flush);
+        if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
+    release_graveyard(sv, true);
 }
 
 }  // namespace
@@ -398,7 +446,6 @@ extern "C" fvgb_status fvgb_server_destroy(fvgb_server* sv) {
     sv->cv.notify_one();
     if (sv->loop.joinable()) sv->loop.join();
     for (cudaStream_t s : sv->streams) cudaStreamDestroy(s);
-    if (sv->h_stats) cudaFreeHost(sv->h_stats);
     delete sv;
     return FVGB_OK;
 }
