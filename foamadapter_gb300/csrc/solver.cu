@@ -649,6 +649,232 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
+// ------------------------------------------------- persistent FP64 CG (one case)
+// For systems small enough that launch latency dominates an iteration: ONE
+// cooperative launch runs the whole solve.  Each resident block walks the
+// 1024-row virtual blocks vb = blockIdx.x, blockIdx.x + gridDim.x, ... exactly
+// as the graph kernels' blocks do, writes the same per-virtual-block partials,
+// and after a grid barrier EVERY block sums all partials with the same tree,
+// so all blocks take identical decisions and the iterates are the bits of the
+// graph path.  Data written during the kernel is read through L2 (__ldcg).
+// Grid barriers spin a bounded number of times; on time-out a block raises the
+// abort flag, every block leaves at its next barrier and the solve reports
+// FVGB_ERR_CUDA.
+struct GridBar {
+    unsigned int count, gen;
+    int abort, pad;
+};
+
+__device__ __forceinline__ bool grid_sync(GridBar* g, unsigned int nblocks) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = &g->gen;
+        const unsigned int my = *vgen;
+        __threadfence();
+        int good = 1;
+        if (atomicAdd(&g->count, 1u) == nblocks - 1) {
+            atomicExch(&g->count, 0u);
+            __threadfence();
+            atomicAdd(&g->gen, 1u);
+        } else {
+            unsigned long long spins = 0;
+            while (*vgen == my) {
+                if (*(volatile int*)&g->abort) {
+                    good = 0;
+                    break;
+                }
+                if (++spins > (1ull << 24)) {  // about 2 s
+                    atomicExch(&g->abort, 1);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+__device__ __forceinline__ double spmv_row_cg(const MeshView& m, const double* __restrict__ val, const double* x,
+                                              int i) {
+    const int slice = i >> 5, lane = i & 31;
+    const int b0 = __ldg(&m.m_ptr[slice]);
+    const int base = b0 + lane;
+    const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+    double v[8], xv[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = 0.0;
+        xv[k] = 0.0;
+        if (k < w) {
+            v[k] = __ldg(&val[base + k * 32]);
+            xv[k] = __ldcg(&x[__ldg(&m.m_col[base + k * 32])]);
+        }
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (k < w) s = fma(v[k], xv[k], s);
+    for (int k = 8; k < w; ++k) s = fma(__ldg(&val[base + k * 32]), __ldcg(&x[__ldg(&m.m_col[base + k * 32])]), s);
+    return s;
+}
+
+__device__ __forceinline__ int vrow(int vb, int j) {
+    return vb * kRowsPerBlock + (threadIdx.x >> 5) * (32 * kRowsPerThread) + j * 32 + (threadIdx.x & 31);
+}
+
+__global__ void __launch_bounds__(kT)
+    k_pcg_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
+                     double* dinv, double* r, double* p, double* q, double* z, double* pa, double* pb, GridBar* gb,
+                     int nvb) {
+    __shared__ double sma[kT], smb[kT];
+    const int n = m.n;
+    const SolverParams prm = L.bs->prm;
+    double* x = prm.x;
+    const unsigned int G = gridDim.x;
+    // init: r = b - A x, z = p = dinv r, r.z, r.r
+    for (int vb = blockIdx.x; vb < nvb; vb += G) {
+        double arz = 0.0, arr = 0.0;
+#pragma unroll
+        for (int j = 0; j < kRowsPerThread; ++j) {
+            const int i = vrow(vb, j);
+            if (i >= n) continue;
+            const double di = 1.0 / __ldg(&val[__ldg(&m.diag_pos[i])]);
+            dinv[i] = di;
+            const double ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
+            const double zi = di * ri;
+            r[i] = ri;
+            p[i] = zi;
+            arz = fma(ri, zi, arz);
+            arr = fma(ri, ri, arr);
+        }
+        const double ba = block_tree(arz, sma), bb = block_tree(arr, smb);
+        if (threadIdx.x == 0) {
+            pa[vb] = ba;
+            pb[vb] = bb;
+        }
+    }
+    bool aborted = !grid_sync(gb, G);
+    __shared__ double s_rz, s_rr, s_a, s_b2;
+    double rz = 0.0, rr = 0.0;
+    if (!aborted) {
+        const double rzb = final_tree(pa, nvb, sma), rrb = final_tree(pb, nvb, smb);
+        if (threadIdx.x == 0) {
+            s_rz = rzb;
+            s_rr = rrb;
+        }
+        __syncthreads();
+        rz = s_rz;
+        rr = s_rr;
+    }
+    const double res0 = sqrt(rr);
+    double tol = prm.rel_tol * res0;
+    if (prm.abs_tol > tol) tol = prm.abs_tol;
+    double res = res0;
+    int iter = 0, status = FVGB_OK;
+    bool done = aborted || !(res0 > tol) || res0 == 0.0;
+    if (!done && prm.max_iter <= 0) {
+        done = true;
+        status = FVGB_ERR_NOT_CONVERGED;
+    }
+    while (!done) {
+        for (int vb = blockIdx.x; vb < nvb; vb += G) {
+            double acc = 0.0;
+#pragma unroll
+            for (int j = 0; j < kRowsPerThread; ++j) {
+                const int i = vrow(vb, j);
+                if (i >= n) continue;
+                const double qi = spmv_row_cg(m, val, p, i);
+                q[i] = qi;
+                acc = fma(__ldcg(&p[i]), qi, acc);
+            }
+            const double ba = block_tree(acc, sma);
+            if (threadIdx.x == 0) pa[vb] = ba;
+        }
+        if (!grid_sync(gb, G)) {
+            aborted = true;
+            break;
+        }
+        const double pqb = final_tree(pa, nvb, sma);
+        if (threadIdx.x == 0) s_a = pqb;
+        __syncthreads();
+        const double pq = s_a;
+        const double alpha = rz / pq;
+        if (pq == 0.0 || !isfinite(alpha)) {
+            status = FVGB_ERR_BREAKDOWN;
+            break;
+        }
+        for (int vb = blockIdx.x; vb < nvb; vb += G) {
+            double arz = 0.0, arr = 0.0;
+#pragma unroll
+            for (int j = 0; j < kRowsPerThread; ++j) {
+                const int i = vrow(vb, j);
+                if (i >= n) continue;
+                x[i] = fma(alpha, __ldcg(&p[i]), __ldcg(&x[i]));
+                const double ri = fma(-alpha, __ldcg(&q[i]), __ldcg(&r[i]));
+                r[i] = ri;
+                const double zi = __ldcg(&dinv[i]) * ri;
+                z[i] = zi;
+                arz = fma(ri, zi, arz);
+                arr = fma(ri, ri, arr);
+            }
+            const double ba = block_tree(arz, sma), bb = block_tree(arr, smb);
+            if (threadIdx.x == 0) {
+                pa[vb] = ba;
+                pb[vb] = bb;
+            }
+        }
+        if (!grid_sync(gb, G)) {
+            aborted = true;
+            break;
+        }
+        const double rznb = final_tree(pa, nvb, sma), rrb = final_tree(pb, nvb, smb);
+        if (threadIdx.x == 0) {
+            s_a = rznb;
+            s_b2 = rrb;
+        }
+        __syncthreads();
+        const double rzn = s_a;
+        rr = s_b2;
+        res = sqrt(rr);
+        ++iter;
+        const double beta = rzn / rz;
+        rz = rzn;
+        if (!isfinite(res)) {
+            status = FVGB_ERR_BREAKDOWN;
+            break;
+        }
+        if (!(res > tol)) break;
+        if (iter >= prm.max_iter) {
+            status = FVGB_ERR_NOT_CONVERGED;
+            break;
+        }
+        for (int vb = blockIdx.x; vb < nvb; vb += G) {
+#pragma unroll
+            for (int j = 0; j < kRowsPerThread; ++j) {
+                const int i = vrow(vb, j);
+                if (i >= n) continue;
+                p[i] = fma(beta, __ldcg(&p[i]), __ldcg(&z[i]));
+            }
+        }
+        if (!grid_sync(gb, G)) {
+            aborted = true;
+            break;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        CaseState* cs = &L.cases[0];
+        cs->res0 = res0;
+        cs->res = res;
+        cs->iter = iter;
+        cs->status = aborted ? FVGB_ERR_CUDA : status;
+    }
+}
+
 // ---------------------------------------------------------------- graph glue
 cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* dep, void* func, unsigned grid,
                        unsigned block, void** args) {
@@ -688,6 +914,8 @@ struct SolverCache {
     float *ah = nullptr, *rh = nullptr, *y = nullptr, *pf = nullptr, *qf = nullptr;
     cudaGraphExec_t g64 = nullptr, gmix = nullptr;
     fvgb_solver_stats* h_stats = nullptr;  // pinned [ncases]
+    GridBar* bar = nullptr;
+    int persistent_grid = 0;               // co-resident blocks of k_pcg_persistent (0: not set up)
 };
 
 struct fvgb_batch {
@@ -854,11 +1082,34 @@ fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
                    "fvgb_solve: unknown precision");
     FVGB_CHECK_ARG(cfg->rel_tol >= 0 && cfg->abs_tol >= 0, "fvgb_solve: negative tolerance");
     FVGB_CHECK_ARG(cfg->max_iter >= 0 && cfg->max_iter <= 100000000, "fvgb_solve: bad max_iter");
+    FVGB_CHECK_ARG(cfg->kernel_mode >= 0 && cfg->kernel_mode <= 2, "fvgb_solve: bad kernel_mode");
     if (cfg->precision == FVGB_PREC_MIXED_IR)
         FVGB_CHECK_ARG(cfg->inner_rel_tol > 0 && cfg->inner_rel_tol < 1 && cfg->inner_max_iter > 0 &&
                            cfg->max_outer > 0,
                        "fvgb_solve: mixed precision needs inner_rel_tol in (0,1), inner_max_iter > 0, max_outer > 0");
     return FVGB_OK;
+}
+
+// FP64 single-case solves of small systems run as one persistent cooperative
+// kernel (launch latency dominates their iterations); everything else runs the
+// graph.  cfg->kernel_mode: 0 automatic, 1 graph, 2 persistent when possible.
+bool use_persistent(SolverCache* c, const fvgb_solver_cfg* cfg) {
+    if (cfg->precision != FVGB_PREC_FP64 || c->ncases != 1 || cfg->kernel_mode == 1) return false;
+    if (cfg->kernel_mode != 2 && c->n > (1 << 20)) return false;
+    if (c->persistent_grid == 0) {
+        int dev = 0, sms = 0, per_sm = 0, coop = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent, kT, 0);
+        if (!coop || per_sm <= 0 || cudaMalloc(&c->bar, sizeof(GridBar)) != cudaSuccess) {
+            c->persistent_grid = -1;
+        } else {
+            c->allocs.push_back(c->bar);
+            c->persistent_grid = sms * per_sm;
+        }
+    }
+    return c->persistent_grid > 0;
 }
 
 fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev,
@@ -884,6 +1135,20 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
     prm.max_outer = cfg->max_outer;
     k_set_params<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L, c->ncases, prm);
     FVGB_LAUNCH_CHECK("fvgb_solve: parameters");
+    if (use_persistent(c, cfg)) {
+        MeshView m = c->ls->mesh->v;
+        Layout L = c->L;
+        const double* val = c->ls->values;
+        const double* b = c->ls->rhs;
+        int nvb = c->nb;
+        FVGB_CUDA_TRY(cudaMemsetAsync(c->bar, 0, sizeof(GridBar), s));
+        void* args[] = {&L, &m, &val, &b, &c->dinv, &c->r, &c->p, &c->q, &c->z, &c->pa, &c->pb, &c->bar, &nvb};
+        const int grid = c->nb < c->persistent_grid ? c->nb : c->persistent_grid;
+        FVGB_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_pcg_persistent, dim3(grid), dim3(kT), args, 0, s));
+        k_finish<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L);
+        FVGB_LAUNCH_CHECK("fvgb_solve: finish");
+        return FVGB_OK;
+    }
     FVGB_CUDA_TRY(cudaGraphLaunch(cfg->precision == FVGB_PREC_FP64 ? c->g64 : c->gmix, s));
     return FVGB_OK;
 }

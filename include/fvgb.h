@@ -255,6 +255,8 @@ typedef struct fvgb_solver_cfg {
     double inner_rel_tol;      /* MIXED_IR: residual reduction asked of each inner solve */
     int32_t inner_max_iter;    /* MIXED_IR: inner iteration cap per refinement step    */
     int32_t max_outer;         /* MIXED_IR: refinement step cap                        */
+    int32_t kernel_mode;       /* 0 automatic, 1 graph of kernels, 2 one persistent
+                                  cooperative kernel (FP64 single case); same results   */
 } fvgb_solver_cfg;
 
 /* SolverStats {initResNorm, finalResNorm, numIter} (expression.hpp:155-158). */

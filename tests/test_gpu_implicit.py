@@ -194,3 +194,15 @@ def test_mixed_ir_reaches_fp64_residual(cuda, inner):
     # error against the FP64 solve
     err = np.abs(xh - x64.cpu().numpy()).max()
     assert err < 1e-6 * 400.0
+
+
+def test_persistent_and_graph_paths_agree(cuda):
+    """The one-kernel cooperative solve and the graph of kernels give the same bits."""
+    hm, dm, T, o, ls, v, r = solve_case(40, 32, 24)
+    out = []
+    for mode in (1, 2):
+        x = T.internal.clone()
+        st = ls.solve(x, rel_tol=1e-9, max_iter=2000, kernel_mode=mode)
+        out.append((x.cpu().numpy(), st.num_iter, st.final_res_norm))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert out[0][1:] == out[1][1:]
