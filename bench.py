@@ -60,6 +60,21 @@ def alg_bytes(hm):
     }
 
 
+def aggregate_replicas(local_ms: float, local_e2e_ms: float, local_units: float, device=None):
+    """Replicas-only scaling: every rank runs its own copy of the workload; the
+    job time is the maximum over ranks, the units are summed.  Returns
+    (ms, e2e_ms, units) on every rank (plain values when not distributed)."""
+    import torch
+
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return local_ms, local_e2e_ms, local_units
+    t = torch.tensor([local_ms, local_e2e_ms], dtype=torch.float64, device=device)
+    u = torch.tensor([local_units], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.all_reduce(u, op=torch.distributed.ReduceOp.SUM)
+    return float(t[0]), float(t[1]), float(u[0])
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -334,6 +349,75 @@ def run_advection(args):
             "cpu_baseline": {"value": fu / cpu_s, "cores": 1, "kind": "port", "sample": "100 steps, serial"}}
 
 
+def run_explicit(args):
+    """Every explicit operator once per launch on the 128^3 jittered box, each launch
+    timed alone with CUDA events after an L2 flush, against the HBM roofline.
+    Algorithmic bytes: int32 labels, every listed array once at its width."""
+    import torch
+
+    from foamadapter_gb300 import abi, neon
+    from foamadapter_gb300.mesh import DeviceMesh
+
+    hm, k = heat_inputs(args.explicit_n)
+    dm = DeviceMesh(hm)
+    n, nif, nbf = hm.n, hm.nif, hm.nbf
+    nbfa = active_bfaces(hm)
+    rng = np.random.default_rng(7)
+    bcs = [("fixedValue", 400.0)] + [("zeroGradient", 0.0)] * (hm.npatch - 1)
+    T = neon.VolumeField(dm, 300.0 + rng.standard_normal(n), bcs)
+    F = neon.dev(rng.standard_normal(nif + nbf))
+    gamma = neon.dev(np.exp(rng.standard_normal(nif + nbf)))
+    out = torch.zeros(n, dtype=torch.float64, device="cuda")
+    out3 = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    fout = torch.zeros(nif + nbf, dtype=torch.float64, device="cuda")
+    T2 = torch.empty_like(T.internal)
+    Tb2 = torch.empty_like(T.boundary)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    L, h, s = abi.lib(), dm.handle, torch.cuda.current_stream().cuda_stream
+    P = abi.ptr
+    bc = T.bc_struct()
+    ops = {
+        "interp_linear": (lambda: L.fvgb_interp_linear(h, 1, P(T.internal), P(T.boundary), P(fout), s),
+                          24 * nif + 8 * n + 16 * nbf),
+        "interp_upwind": (lambda: L.fvgb_interp_upwind(h, 1, P(F), P(T.internal), P(T.boundary), P(fout), s),
+                          24 * nif + 8 * n + 24 * nbf),
+        "div_upwind": (lambda: L.fvgb_div_explicit(h, 1, 1, P(F), P(T.internal), P(T.boundary), 1.0, P(out), s),
+                       16 * nif + 20 * nbf + 32 * n),
+        "div_linear": (lambda: L.fvgb_div_explicit(h, 0, 1, P(F), P(T.internal), P(T.boundary), 1.0, P(out), s),
+                       24 * nif + 20 * nbf + 32 * n),
+        "grad": (lambda: L.fvgb_grad(h, P(T.internal), P(T.boundary), 1.0, P(out3), s),
+                 40 * nif + 36 * nbf + 40 * n),
+        "laplacian": (lambda: L.fvgb_laplacian_explicit(h, 1, P(gamma), P(T.internal), P(T.boundary), 1.0, P(out), s),
+                      24 * nif + 28 * nbfa + 24 * n),
+        "sngrad": (lambda: L.fvgb_sngrad(h, P(T.internal), P(T.boundary), P(fout), s),
+                   24 * nif + 8 * n + 28 * nbf),
+        "advect_euler": (lambda: L.fvgb_advect_euler_step(h, P(F), P(T.internal), P(T.boundary), 1e-3, C.byref(bc),
+                                                          P(T2), P(Tb2), s),
+                         16 * nif + 12 * nbfa + 24 * n),
+    }
+    peak, peak_kind = load_peaks()
+    res = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, (fn, nbytes) in ops.items():
+        for _ in range(3):
+            abi.check(fn())
+        times = []
+        for _ in range(args.explicit_reps):
+            flush.fill_(1.0)
+            e0.record()
+            abi.check(fn())
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        us = 1e3 * float(np.median(times))
+        gbs = nbytes / (us * 1e-6) / 1e9
+        res[name] = {"us": us, "alg_bytes": nbytes, "GBps": gbs, "frac_of_peak": gbs / peak}
+    return {"workload": f"explicit operators, {args.explicit_n}^3 jittered box, one launch each, L2 flushed",
+            "n": n, "n_ifaces": nif, "n_bfaces": nbf, "peak_GBps": peak, "peak_source": peak_kind,
+            "timing": "median of CUDA-event times of single launches, 512 MB written between launches",
+            "ops": res}
+
+
 def run_cavity(args):
     """Lid-driven cavity PISO on 512x512x1: FP64 vs mixed-precision pressure solve."""
     import torch
@@ -495,27 +579,30 @@ def serve_requests(count, seed=5):
 
 
 def run_serve(args):
-    """Continuous batching server vs sequential plain (FP64, one request at a time) runs."""
+    """Continuous-batching server (mixed precision) against one-at-a-time FP64 runs of
+    the same requests: plain launches (host-driven CG loop, the reference's launch
+    pattern) and this library's single-request path (graph / persistent kernel)."""
     from foamadapter_gb300 import abi
 
     L = abi.lib()
     reqs = serve_requests(args.requests)
 
-    def serve(sample, precision, paced, streams, budget):
+    def serve(sample, precision, paced, streams, budget, kernel_mode=0):
         cfg = abi.ServerCfg(int(budget), streams, 100000)
         sv = C.c_void_p()
         abi.check(L.fvgb_server_create(C.byref(cfg), C.byref(sv)))
         buf = (abi.ServeResult * 1024)()
         results, t0 = {}, time.perf_counter()
-        keep = []
+        keep, ids = [], []
         for (ta, nx, ny, nz, steps, U, D) in sample:
             if paced:
                 while time.perf_counter() - t0 < ta:
                     time.sleep(0.0005)
-            req = abi.ServeRequest(nx, ny, nz, steps, (C.c_double * 3)(*U), D, 0.0, precision, 0, None)
+            req = abi.ServeRequest(nx, ny, nz, steps, (C.c_double * 3)(*U), D, 0.0, precision, kernel_mode, None)
             rid = C.c_int64()
             abi.check(L.fvgb_server_submit(sv, C.byref(req), C.byref(rid)))
             keep.append(req)
+            ids.append(rid.value)
             if not paced:  # sequential: wait for this one before the next
                 while rid.value not in results:
                     cnt = C.c_int32()
@@ -533,19 +620,30 @@ def run_serve(args):
         info = (C.c_int64 * 6)()
         L.fvgb_server_info(sv, info)
         abi.check(L.fvgb_server_destroy(sv))
-        r = list(results.values())
+        r = [results[i] for i in ids]
         lat = np.array([x.finish_s - x.submit_s for x in r])
-        ok = all(x.status == 0 for x in r)
+        failed = [{"request": k, "status": x.status, "steps_done": x.steps_done, "cells": sample[k][1:4],
+                   "steps": sample[k][4], "D": sample[k][6], "U": float(np.linalg.norm(sample[k][5]))}
+                  for k, x in enumerate(r) if x.status != 0]
         return {"requests": len(r), "wall_s": wall, "solves_per_s": len(r) / wall,
                 "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
-                "all_ok": ok, "peak_device_GB": info[4] / 1e9, "ticks": int(info[5]),
+                "all_ok": not failed, "failed": failed[:8], "n_failed": len(failed),
+                "peak_device_GB": info[4] / 1e9, "ticks": int(info[5]),
+                "total_cg_iters": int(sum(x.total_iters for x in r)),
                 "cell_steps": int(sum(x[1] * x[2] * x[3] * x[4] for x in sample))}
 
     served = serve(reqs, abi.PREC_MIXED_IR, True, args.serve_streams, 150e9)
-    seq = serve(reqs[: args.seq_requests], abi.PREC_FP64, False, 1, 150e9)
-    return {"workload": f"serving: {len(reqs)} Poisson arrivals at 200/s, edges logU[16,160], 10-200 IMEX steps",
-            "served_mixed": served, "sequential_plain_fp64": seq,
-            "solves_per_s_ratio": served["solves_per_s"] / seq["solves_per_s"]}
+    seq_n = min(args.seq_requests, len(reqs))
+    plain = serve(reqs[:seq_n], abi.PREC_FP64, False, 1, 150e9, kernel_mode=3)
+    best = serve(reqs[:seq_n], abi.PREC_FP64, False, 1, 150e9, kernel_mode=0)
+    out = {"workload": f"serving: {len(reqs)} Poisson arrivals at 200/s, edges logU[16,160], 10-200 IMEX steps",
+           "served_mixed": served, "sequential_plain_launches_fp64": plain, "sequential_graph_fp64": best}
+    if seq_n == len(reqs):
+        out["solves_per_s_ratio_vs_plain"] = served["solves_per_s"] / plain["solves_per_s"]
+        out["solves_per_s_ratio_vs_graph"] = served["solves_per_s"] / best["solves_per_s"]
+    else:
+        out["note"] = f"sequential runs cover the first {seq_n} requests only; compare solves/s with care"
+    return out
 
 
 def workload_config(args):
@@ -564,10 +662,12 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--ref-max-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity", "batch", "serve"])
+    ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity", "batch", "serve", "explicit"])
     ap.add_argument("--requests", type=int, default=400)
-    ap.add_argument("--seq-requests", type=int, default=40)
+    ap.add_argument("--seq-requests", type=int, default=400)
     ap.add_argument("--serve-streams", type=int, default=16)
+    ap.add_argument("--explicit-n", type=int, default=128)
+    ap.add_argument("--explicit-reps", type=int, default=20)
     ap.add_argument("--cases", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--alone-cases", type=int, default=64)
@@ -592,7 +692,8 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     if args.workload != "heat":
-        fn = {"advection": run_advection, "cavity": run_cavity, "batch": run_batch, "serve": run_serve}[args.workload]
+        fn = {"advection": run_advection, "cavity": run_cavity, "batch": run_batch, "serve": run_serve,
+              "explicit": run_explicit}[args.workload]
         if rank == 0:
             print(json.dumps(fn(args)))
         return
@@ -602,23 +703,17 @@ def main():
     if args.profile:
         print(json.dumps({"profile_run": True, "ms": r["ms"], "iters": r["iters"]}))
         return
-    ms = r["ms"]
-    if world > 1:
-        t = torch.tensor([ms, r["e2e_ms"]], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, e2e_ms = t.tolist()
-    else:
-        e2e_ms = r["e2e_ms"]
+    fu = r["face_updates"]
+    ms, e2e_ms, units = aggregate_replicas(r["ms"], r["e2e_ms"], float(fu * args.steps), device="cuda")
     if rank != 0:
         return
-    fu = r["face_updates"]
-    value = fu * args.steps * world / (ms / 1e3)
-    e2e_value = fu * args.steps * world / (e2e_ms / 1e3)
+    value = units / (ms / 1e3)
+    e2e_value = units / (e2e_ms / 1e3)
     peak, peak_kind = load_peaks()
     ab = alg_bytes(hm)
     t_spmv = r["kt"][0] * 1e-3
     achieved = ab["pcg_spmv"] / t_spmv / 1e9
-    traffic = read_traffic("pcg_spmv")
+    traffic = read_traffic("k_pcg_spmv")
     launches = sum(5 + 3 * it for it in r["iters"])
     line = {
         "metric": "face-updates/s", "value": value, "unit": "face-updates/s", "n_gpus": world,
@@ -651,14 +746,23 @@ def main():
     print(json.dumps(line))
 
 
-def read_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "ncu_summary.json"
-    if p.exists():
-        try:
-            return json.loads(p.read_text()).get(kernel, {}).get("dram_bytes_per_launch")
-        except (ValueError, AttributeError):
-            return None
+def read_traffic(kernel, summary="pcg_fp64_kernels_128cube.md"):
+    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum + dram__bytes_write.sum)
+    from the table of the committed ncu summary, whose header names the columns
+    'DRAM read (bytes)' and 'DRAM write (bytes)'; None when absent."""
+    p = ROOT / "profiles" / summary
+    if not p.exists():
+        return None
+    cols = None
+    for line in p.read_text().splitlines():
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if cols is None and "DRAM read (bytes)" in cells and "DRAM write (bytes)" in cells:
+            cols = (cells.index("DRAM read (bytes)"), cells.index("DRAM write (bytes)"))
+        elif cols is not None and cells and cells[0].split(" ")[0] == kernel:
+            try:
+                return int(cells[cols[0]].replace(",", "")) + int(cells[cols[1]].replace(",", ""))
+            except (ValueError, IndexError):
+                return None
     return None
 
 

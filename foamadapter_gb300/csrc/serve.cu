@@ -200,7 +200,7 @@ fvgb_status enqueue_step(Slot* s, int k) {
     fvgb_bc bc{s->types, s->ref};
     fvgb_status st = fvgb_assemble(s->ls, terms, 3, s->dt, &bc, s->Tb, s->stream);
     if (st != FVGB_OK) return st;
-    fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, 1e-2, 1000, 50};
+    fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, 1e-2, 1000, 50, r.kernel_mode};
     st = fvgb_solve_async(s->ls, s->T, &cfg, s->stats_dev + k, s->stream);
     if (st != FVGB_OK) return st;
     return fvgb_bc_correct(s->mesh, 1, &bc, s->T, s->Tb, s->stream);
@@ -381,7 +381,8 @@ extern "C" fvgb_status fvgb_server_create(const fvgb_server_cfg* cfg, fvgb_serve
 extern "C" fvgb_status fvgb_server_submit(fvgb_server* sv, const fvgb_serve_request* req, int64_t* id) {
     if (!sv || !req || !id) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_server_submit: null argument");
     if (req->nx < 2 || req->ny < 2 || req->nz < 2 || req->steps < 1 || !(req->D >= 0) ||
-        (req->precision != FVGB_PREC_FP64 && req->precision != FVGB_PREC_MIXED_IR))
+        (req->precision != FVGB_PREC_FP64 && req->precision != FVGB_PREC_MIXED_IR) || req->kernel_mode < 0 ||
+        req->kernel_mode > 3 || (req->kernel_mode == 3 && req->precision != FVGB_PREC_FP64))
         return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_server_submit: bad request");
     Slot* s = new Slot();
     s->req = *req;

@@ -52,6 +52,7 @@ struct SolverParams {
 struct CaseState {
     double rz, alpha, beta, res0, res, tol;
     double rho, rho_prev, itol;
+    double sres, sig, isig;     // mixed: |s r| of the latest residual; power-of-two scale of rhat and 1/scale
     float falpha, fbeta, frel;  // frel: direction factor after a reliable update (-1: restart)
     int32_t iter, status, total, outer, inner_it;
     int32_t active;        // FP64: iterating; mixed: refinement loop running
@@ -397,21 +398,53 @@ __global__ void k_set_params(Layout L, int ncases, SolverParams prm) {
 }
 
 // --------------------------------------------------- mixed precision (FP32 inner)
-// s_i = 1/sqrt|a_ii|; signflags bit0: a positive diagonal, bit1: negative, bit2: zero/NaN
+// Power-of-two scale that brings |s r| to [1, 2): the FP32 inner solve works on
+// (float)(sig * s r).  Scaling by a power of two is exact, so the inner iterates
+// are the unscaled ones times sig, except that FP32 products of a tiny residual
+// (a field that has almost stopped changing) no longer underflow.
+__device__ __host__ __forceinline__ void residual_scale(double sres, double* sig, double* isig) {
+    int e = 0;
+    if (sres > 0.0 && isfinite(sres)) {
+        e = ilogb(sres);
+        e = e > 900 ? 900 : (e < -900 ? -900 : e);
+    }
+    *sig = ldexp(1.0, -e);
+    *isig = ldexp(1.0, e);
+}
+
+// s_i = 1/sqrt|a_ii|; signflags bit0: a positive diagonal, bit1: negative, bit2: zero/NaN;
+// |s (b - A x0)| of every case -> sres, the magnitude the first residual is scaled by
 __global__ void __launch_bounds__(kT)
-    k_ir_scale(Layout L, MeshView m, const double* __restrict__ val, double* __restrict__ s) {
+    k_ir_scale(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
+               double* __restrict__ s, double* __restrict__ pa) {
+    __shared__ double sma[kT];
     const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    const double* __restrict__ x = L.bs->prm.x;
     unsigned int f = 0;
+    double asr = 0.0;
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int i = blk_row(k, j);
         if (i >= k.end) continue;
         const double d = __ldg(&val[__ldg(&m.diag_pos[i])]);
         f |= d > 0.0 ? 1u : (d < 0.0 ? 2u : 4u);
-        s[i] = 1.0 / sqrt(fabs(d));
+        const double si = 1.0 / sqrt(fabs(d));
+        s[i] = si;
+        const double sr = si * (__ldg(&b[i]) - spmv_row(m, val, x, i));
+        asr = fma(sr, sr, asr);
     }
     f = __reduce_or_sync(0xffffffffu, f);
-    if ((threadIdx.x & 31) == 0 && f) atomicOr(&L.cases[k.c].signflags, f);
+    if ((threadIdx.x & 31) == 0 && f) atomicOr(&cs->signflags, f);
+    const double ba = block_tree(asr, sma);
+    if (threadIdx.x == 0) pa[blockIdx.x] = ba;
+    if (!arrive_last(&cs->counter, k.nbc)) return;
+    const double sr2 = final_tree(pa + k.blk0, k.nbc, sma);
+    if (threadIdx.x == 0) {
+        cs->sres = sqrt(sr2);
+        cs->sig = 1.0;
+        cs->isig = 1.0;
+    }
 }
 
 // ahat at every slot of the case's rows: (float)((a * s_row) * s_col); diagonal and padding 0
@@ -443,15 +476,17 @@ template <bool FIRST>
 __global__ void __launch_bounds__(kT)
     k_ir_residual(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
                   const double* __restrict__ s, float* __restrict__ rh, float* __restrict__ y,
-                  float* __restrict__ p, double* __restrict__ pa, double* __restrict__ pb,
+                  float* __restrict__ p, double* __restrict__ pa, double* __restrict__ pb, double* __restrict__ pc,
                   cudaGraphConditionalHandle h_outer, cudaGraphConditionalHandle h_inner) {
-    __shared__ double sma[kT], smb[kT];
+    __shared__ double sma[kT], smb[kT], smc[kT];
     __shared__ float smf[kT];
     const Blk k = blk_info(L);
     CaseState* cs = &L.cases[k.c];
     if (FIRST || ld_volatile(&cs->active)) {
         const double* __restrict__ x = L.bs->prm.x;
-        double arr = 0.0;
+        double sig, isig;
+        residual_scale(cs->sres, &sig, &isig);  // from the previous residual (k_ir_scale's for the first)
+        double arr = 0.0, asr = 0.0;
         float arho = 0.0f;
 #pragma unroll
         for (int j = 0; j < kRowsPerThread; ++j) {
@@ -459,20 +494,25 @@ __global__ void __launch_bounds__(kT)
             if (i >= k.end) continue;
             const double ri = __ldg(&b[i]) - spmv_row(m, val, x, i);
             arr = fma(ri, ri, arr);
-            const float rhi = (float)(__ldg(&s[i]) * ri);
+            const double sr = __ldg(&s[i]) * ri;
+            asr = fma(sr, sr, asr);
+            const float rhi = (float)(sr * sig);
             rh[i] = rhi;
             y[i] = 0.0f;
             if (FIRST) p[i] = rhi;
             arho = fmaf(rhi, rhi, arho);
         }
         const double ba = block_tree(arr, sma);
+        const double bc = block_tree(asr, smc);
         const float bb = block_tree_f(arho, smf);
         if (threadIdx.x == 0) {
             pa[blockIdx.x] = ba;
             pb[blockIdx.x] = (double)bb;
+            pc[blockIdx.x] = bc;
         }
         if (arrive_last(&cs->counter, k.nbc)) {
             const double rr = final_tree(pa + k.blk0, k.nbc, sma), rho = final_tree(pb + k.blk0, k.nbc, smb);
+            const double sr2 = final_tree(pc + k.blk0, k.nbc, smc);
             if (threadIdx.x == 0) {
                 const SolverParams& prm = L.bs->prm;
                 const double res = sqrt(rr);
@@ -501,9 +541,13 @@ __global__ void __launch_bounds__(kT)
                         done = true;
                     }
                 }
-                // direction after this update: keep p (beta = rho/rho_prev) unless no
-                // inner iteration ran since the last update, then restart from rhat
-                cs->frel = (FIRST || cs->inner_it == 0) ? -1.0f : (float)(rho / cs->rho_prev);
+                // direction after this update: keep p (beta = rho/rho_prev, with p brought
+                // from the previous scale to this one) unless no inner iteration ran since
+                // the last update, then restart from rhat
+                cs->frel = (FIRST || cs->inner_it == 0) ? -1.0f : (float)((rho / cs->rho_prev) * (cs->sig * isig));
+                cs->sig = sig;
+                cs->isig = isig;
+                cs->sres = sqrt(sr2);
                 cs->rho = rho;
                 // leave the inner loop when the FP32 residual dropped by inner_rel_tol or
                 // should be below the FP64 tolerance (estimated through this update's ratio)
@@ -639,13 +683,15 @@ __global__ void __launch_bounds__(kT)
 __global__ void __launch_bounds__(kT)
     k_ir_xupdate(Layout L, const double* __restrict__ s, const float* __restrict__ y) {
     const Blk k = blk_info(L);
-    if (!ld_volatile(&L.cases[k.c].active)) return;
+    const CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->active)) return;
     double* __restrict__ x = L.bs->prm.x;
+    const double isig = cs->isig;  // y carries the scale of its residual
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int i = blk_row(k, j);
         if (i >= k.end) continue;
-        x[i] = fma(__ldg(&s[i]), (double)__ldg(&y[i]), x[i]);
+        x[i] = fma(__ldg(&s[i]) * isig, (double)__ldg(&y[i]), x[i]);
     }
 }
 
@@ -910,12 +956,14 @@ struct SolverCache {
     Layout L{};
     std::vector<void*> allocs;
     double *dinv = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *pa = nullptr, *pb = nullptr;
+    double* pc = nullptr;
     double* s = nullptr;
     float *ah = nullptr, *rh = nullptr, *y = nullptr, *pf = nullptr, *qf = nullptr;
     cudaGraphExec_t g64 = nullptr, gmix = nullptr;
     fvgb_solver_stats* h_stats = nullptr;  // pinned [ncases]
     GridBar* bar = nullptr;
     int persistent_grid = 0;               // co-resident blocks of k_pcg_persistent (0: not set up)
+    int32_t* h_active = nullptr;           // pinned copy of n_active for the host-driven loop
 };
 
 struct fvgb_batch {
@@ -928,6 +976,7 @@ void fvgb_solver_cache_free(SolverCache* c) {
     if (c->gmix) cudaGraphExecDestroy(c->gmix);
     for (void* p : c->allocs) cudaFree(p);
     if (c->h_stats) cudaFreeHost(c->h_stats);
+    if (c->h_active) cudaFreeHost(c->h_active);
     delete c;
 }
 
@@ -979,6 +1028,7 @@ fvgb_status cache_create(const fvgb_ls* ls, int ncases, const int32_t* ranges, S
     if (e == cudaSuccess) e = calloc_dev(c, &st, (size_t)ncases);
     if (e == cudaSuccess) e = calloc_dev(c, &c->pa, (size_t)c->nb);
     if (e == cudaSuccess) e = calloc_dev(c, &c->pb, (size_t)c->nb);
+    if (e == cudaSuccess) e = calloc_dev(c, &c->pc, (size_t)c->nb);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_stats, sizeof(fvgb_solver_stats) * (size_t)ncases);
     if (e != cudaSuccess) {
         fvgb_solver_cache_free(c);
@@ -1050,9 +1100,9 @@ fvgb_status build_mixed(SolverCache* c) {
     if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
     cudaGraphNode_t n_scale, n_vals, n_res0, n_outer, n_fin, o_inner, o_x, o_res, o_dir, i_spmv, i_upd, i_dir;
     cudaGraph_t obody = nullptr, ibody = nullptr;
-    void* a_scale[] = {&L, &m, &val, &c->s};
+    void* a_scale[] = {&L, &m, &val, &b, &c->s, &c->pa};
     void* a_vals[] = {&L, &m, &val, &c->s, &c->ah};
-    void* a_res[] = {&L, &m, &val, &b, &c->s, &c->rh, &c->y, &c->pf, &c->pa, &c->pb, &ho, &hi};
+    void* a_res[] = {&L, &m, &val, &b, &c->s, &c->rh, &c->y, &c->pf, &c->pa, &c->pb, &c->pc, &ho, &hi};
     void* a_spmv[] = {&L, &m, &c->ah, &c->pf, &c->qf, &c->pa};
     void* a_upd[] = {&L, &c->pf, &c->qf, &c->y, &c->rh, &c->pa, &hi};
     void* a_dir[] = {&L, &c->rh, &c->pf};
@@ -1082,7 +1132,9 @@ fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
                    "fvgb_solve: unknown precision");
     FVGB_CHECK_ARG(cfg->rel_tol >= 0 && cfg->abs_tol >= 0, "fvgb_solve: negative tolerance");
     FVGB_CHECK_ARG(cfg->max_iter >= 0 && cfg->max_iter <= 100000000, "fvgb_solve: bad max_iter");
-    FVGB_CHECK_ARG(cfg->kernel_mode >= 0 && cfg->kernel_mode <= 2, "fvgb_solve: bad kernel_mode");
+    FVGB_CHECK_ARG(cfg->kernel_mode >= 0 && cfg->kernel_mode <= 3, "fvgb_solve: bad kernel_mode");
+    FVGB_CHECK_ARG(cfg->kernel_mode != 3 || cfg->precision == FVGB_PREC_FP64,
+                   "fvgb_solve: the host-driven loop (kernel_mode 3) is FP64 only");
     if (cfg->precision == FVGB_PREC_MIXED_IR)
         FVGB_CHECK_ARG(cfg->inner_rel_tol > 0 && cfg->inner_rel_tol < 1 && cfg->inner_max_iter > 0 &&
                            cfg->max_outer > 0,
@@ -1092,7 +1144,8 @@ fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
 
 // FP64 single-case solves of small systems run as one persistent cooperative
 // kernel (launch latency dominates their iterations); everything else runs the
-// graph.  cfg->kernel_mode: 0 automatic, 1 graph, 2 persistent when possible.
+// graph.  cfg->kernel_mode: 0 automatic, 1 graph, 2 persistent when possible,
+// 3 host-driven loop (see host_loop).
 bool use_persistent(SolverCache* c, const fvgb_solver_cfg* cfg) {
     if (cfg->precision != FVGB_PREC_FP64 || c->ncases != 1 || cfg->kernel_mode == 1) return false;
     if (cfg->kernel_mode != 2 && c->n > (1 << 20)) return false;
@@ -1110,6 +1163,35 @@ bool use_persistent(SolverCache* c, const fvgb_solver_cfg* cfg) {
         }
     }
     return c->persistent_grid > 0;
+}
+
+// FP64 CG driven from the host: three launches per iteration and a read of the
+// number of unconverged cases after each, the way a solver that evaluates its
+// stopping criterion on the host runs (Ginkgo's CG checks its criteria between
+// iterations).  Same kernels in the same order as the graph, so the same bits;
+// it blocks the calling thread until the solve ends.  Kept as the plain-launch
+// baseline the graph and the persistent kernel are measured against.
+fvgb_status host_loop(SolverCache* c, cudaStream_t s) {
+    if (!c->h_active) FVGB_CUDA_TRY(cudaMallocHost(&c->h_active, sizeof(int32_t)));
+    const MeshView m = c->ls->mesh->v;
+    const double* val = c->ls->values;
+    const double* b = c->ls->rhs;
+    const unsigned nb = (unsigned)c->nb;
+    const cudaGraphConditionalHandle h{};  // not used: setc = 0 outside a graph
+    k_pcg_init<<<nb, kT, 0, s>>>(c->L, m, val, b, c->dinv, c->r, c->p, c->pa, c->pb, h, 0);
+    FVGB_LAUNCH_CHECK("fvgb_solve: init");
+    for (;;) {
+        FVGB_CUDA_TRY(cudaMemcpyAsync(c->h_active, &c->L.bs->n_active, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        FVGB_CUDA_TRY(cudaStreamSynchronize(s));
+        if (*c->h_active <= 0) break;  // the update kernel retires every case by max_iter at the latest
+        k_pcg_spmv<<<nb, kT, 0, s>>>(c->L, m, val, c->p, c->q, c->pa);
+        k_pcg_update<<<nb, kT, 0, s>>>(c->L, c->dinv, c->p, c->q, c->r, c->z, c->pa, c->pb, h, 0);
+        k_pcg_dir<<<nb, kT, 0, s>>>(c->L, c->z, c->p);
+        FVGB_LAUNCH_CHECK("fvgb_solve: iteration");
+    }
+    k_finish<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L);
+    FVGB_LAUNCH_CHECK("fvgb_solve: finish");
+    return FVGB_OK;
 }
 
 fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev,
@@ -1135,6 +1217,7 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
     prm.max_outer = cfg->max_outer;
     k_set_params<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L, c->ncases, prm);
     FVGB_LAUNCH_CHECK("fvgb_solve: parameters");
+    if (cfg->kernel_mode == 3) return host_loop(c, s);
     if (use_persistent(c, cfg)) {
         MeshView m = c->ls->mesh->v;
         Layout L = c->L;

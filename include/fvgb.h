@@ -256,7 +256,8 @@ typedef struct fvgb_solver_cfg {
     int32_t inner_max_iter;    /* MIXED_IR: inner iteration cap per refinement step    */
     int32_t max_outer;         /* MIXED_IR: refinement step cap                        */
     int32_t kernel_mode;       /* 0 automatic, 1 graph of kernels, 2 one persistent
-                                  cooperative kernel (FP64 single case); same results   */
+                                  cooperative kernel (FP64 single case), 3 host-driven
+                                  loop (FP64; blocks the caller); same results          */
 } fvgb_solver_cfg;
 
 /* SolverStats {initResNorm, finalResNorm, numIter} (expression.hpp:155-158). */
@@ -370,7 +371,7 @@ typedef struct fvgb_serve_request {
     double D;
     double dt;
     int32_t precision;         /* FVGB_PREC_FP64 or FVGB_PREC_MIXED_IR                */
-    int32_t reserved;
+    int32_t kernel_mode;       /* fvgb_solver_cfg.kernel_mode of every solve          */
     double* T_out;
 } fvgb_serve_request;
 typedef struct fvgb_serve_result {

@@ -617,13 +617,27 @@ static double dot_tree_f(int32_t n, const float* a, const float* b, double* part
     return final_tree(nb, part);
 }
 
+/* Power-of-two scale bringing |s r| to [1, 2) (solver.cu residual_scale): exact,
+ * it only keeps the FP32 products of a tiny residual out of the subnormal range. */
+static void residual_scale(double sres, double* sig, double* isig) {
+    int e = 0;
+    if (sres > 0.0 && isfinite(sres)) {
+        e = ilogb(sres);
+        e = e > 900 ? 900 : (e < -900 ? -900 : e);
+    }
+    *sig = ldexp(1.0, -e);
+    *isig = ldexp(1.0, e);
+}
+
+/* r = b - A x; rh = (float)((s r) sig); returns |r|, *sres = |s r| (both by the GPU's tree) */
 static double residual_step(const or_csr* A, const double* val, const double* b, const double* x,
-                            const double* s, float* rh, double* r, double* part, int32_t n, int32_t nb) {
+                            const double* s, double sig, float* rh, double* r, double* part, double* part2,
+                            int32_t n, int32_t nb, double* sres) {
 #pragma omp parallel for schedule(static)
     for (int32_t blk = 0; blk < nb; ++blk) {
-        double tp[RED_THREADS];
+        double tp[RED_THREADS], tq[RED_THREADS];
         for (int t = 0; t < RED_THREADS; ++t) {
-            double arr = 0.0;
+            double arr = 0.0, asr = 0.0;
             for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
                 int32_t i = red_row(blk, t, j);
                 if (i >= n) continue;
@@ -632,12 +646,17 @@ static double residual_step(const or_csr* A, const double* val, const double* b,
                 double ri = b[i] - sm;
                 r[i] = ri;
                 arr = fma(ri, ri, arr);
-                rh[i] = (float)(s[i] * ri);
+                double sr = s[i] * ri;
+                asr = fma(sr, sr, asr);
+                rh[i] = (float)(sr * sig);
             }
             tp[t] = arr;
+            tq[t] = asr;
         }
         part[blk] = block_tree(tp);
+        part2[blk] = block_tree(tq);
     }
+    *sres = sqrt(final_tree(nb, part2));
     return sqrt(final_tree(nb, part));
 }
 
@@ -663,13 +682,15 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
             ah[j] = (float)((val[j] * s[i]) * s[A->col[j]]);
     const float fs = (float)dsign;
     const double dr = cfg->inner_rel_tol * cfg->inner_rel_tol;
-    double *r = zalloc(n), *part = zalloc(nb);
+    double *r = zalloc(n), *part = zalloc(nb), *part2 = zalloc(nb);
     float *rh = (float*)calloc(n, sizeof(float)), *y = (float*)calloc(n, sizeof(float));
     float *p = (float*)calloc(n, sizeof(float)), *q = (float*)calloc(n, sizeof(float));
     int32_t total = 0, outer = 0, status = ST_OK, inner_it = 0;
-    double rho, rho_prev = 0.0, itol, res, res0, tol;
-    /* first residual */
-    res = residual_step(A, val, b, x, s, rh, r, part, n, nb);
+    double rho, rho_prev = 0.0, itol, res, res0, tol, sres, sig, isig;
+    /* |s r0| sets the scale of the first residual (k_ir_scale), then the first residual */
+    residual_step(A, val, b, x, s, 1.0, rh, r, part, part2, n, nb, &sres);
+    residual_scale(sres, &sig, &isig);
+    res = residual_step(A, val, b, x, s, sig, rh, r, part, part2, n, nb, &sres);
     for (int32_t i = 0; i < n; ++i) { y[i] = 0.0f; p[i] = rh[i]; }
     rho = dot_tree_f(n, rh, rh, part);
     res0 = res;
@@ -713,16 +734,18 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
             for (int32_t i = 0; i < n; ++i) p[i] = fmaf(fb, p[i], rh[i]);
         }
         if (done) break;
-        /* reliable update */
-        for (int32_t i = 0; i < n; ++i) x[i] = fma(s[i], (double)y[i], x[i]);
-        res = residual_step(A, val, b, x, s, rh, r, part, n, nb);
+        /* reliable update; the new residual takes the scale of the previous |s r| */
+        for (int32_t i = 0; i < n; ++i) x[i] = fma(s[i] * isig, (double)y[i], x[i]);
+        const double sig_old = sig;
+        residual_scale(sres, &sig, &isig);
+        res = residual_step(A, val, b, x, s, sig, rh, r, part, part2, n, nb, &sres);
         for (int32_t i = 0; i < n; ++i) y[i] = 0.0f;
         double rho_true = dot_tree_f(n, rh, rh, part);
         ++outer;
         if (!isfinite(res)) { status = ST_BREAKDOWN; done = 1; }
         else if (!(res > tol) || res == 0.0) done = 1;
         else if (outer >= cfg->max_outer || total >= cfg->max_iter) { status = ST_NOT_CONVERGED; done = 1; }
-        float frel = inner_it == 0 ? -1.0f : (float)(rho_true / rho_prev);
+        float frel = inner_it == 0 ? -1.0f : (float)((rho_true / rho_prev) * (sig_old * isig));
         rho = rho_true;
         { double dt = (tol / res) * (tol / res); itol = rho * (dr > dt ? dr : dt); }
         inner_it = 0;
@@ -735,7 +758,7 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
     st->num_iter = total;
     st->num_outer = outer;
     st->status = status;
-    free(s); free(ah); free(r); free(part); free(rh); free(y); free(p); free(q);
+    free(s); free(ah); free(r); free(part); free(part2); free(rh); free(y); free(p); free(q);
     return status;
 }
 

@@ -137,10 +137,11 @@ def test_set_reference(cuda):
     np.testing.assert_array_equal(v1[1].cpu().numpy(), orr)
 
 
-def solve_case(nx=14, ny=12, nz=10):
+def solve_case(nx=14, ny=12, nz=10, scale=1.0):
     hm, k, bcs, dt = heat_case(nx, ny, nz)
+    bcs = [(kind, val * scale) for kind, val in bcs]
     dm = DeviceMesh(hm)
-    T = neon.VolumeField(dm, np.full(hm.n, 300.0), bcs)
+    T = neon.VolumeField(dm, np.full(hm.n, 300.0 * scale), bcs)
     o = Oracle(hm)
     kf = o.interp_linear(1, k, k[hm.bcells].copy())
     gamma = neon.SurfaceField(dm, kf)
@@ -196,13 +197,44 @@ def test_mixed_ir_reaches_fp64_residual(cuda, inner):
     assert err < 1e-6 * 400.0
 
 
-def test_persistent_and_graph_paths_agree(cuda):
-    """The one-kernel cooperative solve and the graph of kernels give the same bits."""
+def test_persistent_graph_and_host_loop_agree(cuda):
+    """The one-kernel cooperative solve, the graph of kernels and the host-driven
+    loop (plain launches) give the same bits."""
     hm, dm, T, o, ls, v, r = solve_case(40, 32, 24)
     out = []
-    for mode in (1, 2):
+    for mode in (1, 2, 3):
         x = T.internal.clone()
         st = ls.solve(x, rel_tol=1e-9, max_iter=2000, kernel_mode=mode)
         out.append((x.cpu().numpy(), st.num_iter, st.final_res_norm))
-    np.testing.assert_array_equal(out[0][0], out[1][0])
-    assert out[0][1:] == out[1][1:]
+    for other in out[1:]:
+        np.testing.assert_array_equal(out[0][0], other[0])
+        assert out[0][1:] == other[1:]
+
+
+def test_host_loop_is_fp64_only(cuda):
+    hm, dm, T, o, ls, v, r = solve_case(6, 6, 6)
+    with pytest.raises(RuntimeError):
+        ls.solve(T.internal.clone(), precision=abi.PREC_MIXED_IR, kernel_mode=3)
+
+
+def test_mixed_tiny_residual_is_scale_invariant(cuda):
+    """Initial field and wall value scaled by 2^-100 (so b and x0 are, exactly):
+    the power-of-two scaling of the FP32 residual keeps the inner solve identical,
+    so x is the unscaled solution times 2^-100 (the FP32 dot products would
+    otherwise underflow), and the oracle agrees bit for bit."""
+    sc = 2.0 ** -100
+    hm, dm, T1, o, ls1, v1, r1 = solve_case()
+    _, _, T2, _, ls2, v2, r2 = solve_case(scale=sc)
+    np.testing.assert_array_equal(v2, v1)
+    np.testing.assert_array_equal(r2, r1 * sc)
+    x1, x2 = T1.internal.clone(), T2.internal.clone()
+    s1 = ls1.solve(x1, rel_tol=1e-8, precision=abi.PREC_MIXED_IR)
+    s2 = ls2.solve(x2, rel_tol=1e-8, precision=abi.PREC_MIXED_IR)
+    assert s1.status == abi.OK and s2.status == abi.OK
+    assert (s1.num_iter, s1.num_outer) == (s2.num_iter, s2.num_outer)
+    assert s2.final_res_norm == s1.final_res_norm * sc
+    np.testing.assert_array_equal(x2.cpu().numpy(), x1.cpu().numpy() * sc)
+    xo = np.full(hm.n, 300.0 * sc)
+    so = o.solve(v2, r2, xo, rel_tol=1e-8, precision=1)
+    assert so.status == 0 and so.num_iter == s2.num_iter
+    np.testing.assert_array_equal(x2.cpu().numpy(), xo)

@@ -1,0 +1,56 @@
+"""The oracle's Jacobi-CG and mixed-precision refinement on the CPU (no GPU).
+
+The mixed solve scales the FP32 residual of every refinement step by a power
+of two, so a system whose right-hand side and initial guess are scaled by 2^-100
+is solved with exactly the same FP32 inner iterates: the solution is the
+unscaled one times 2^-100, bit for bit, with the same iteration counts.
+Without the scaling the FP32 dot products of that residual (about 1e-60)
+underflow and the refinement stalls.
+"""
+import numpy as np
+import pytest
+
+from foamadapter_gb300 import mesh
+from oracle.pyoracle import Oracle
+
+DDT, LAP = 0, 1
+FIXED_VALUE, FIXED_GRADIENT = 1, 2
+
+
+def heat_system(nx=10, ny=9, nz=7, seed=3):
+    hm = mesh.box(nx, ny, nz, jitter=0.1, seed=seed)
+    o = Oracle(hm)
+    rng = np.random.default_rng(seed)
+    k = np.exp(0.5 * rng.standard_normal(hm.n))
+    gamma = o.interp_linear(1, k, np.ascontiguousarray(k[hm.bcells]))
+    types = np.asarray([FIXED_VALUE] + [FIXED_GRADIENT] * (hm.npatch - 1), np.int32)
+    ref = np.zeros(hm.nbf)
+    ref[hm.patch_slice("xmin")] = 400.0
+    T = np.full(hm.n, 300.0)
+    Tb = np.zeros(hm.nbf)
+    o.bc_correct(1, types, ref, T, Tb)
+    v, r, _, _ = o.assemble(1, [(DDT, 0, 1.0, T.copy(), None), (LAP, 0, -1.0, None, gamma)], 0.01, types, ref, Tb)
+    return o, v, r, T
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_solve_reaches_tolerance(precision):
+    o, v, r, T = heat_system()
+    x = T.copy()
+    st = o.solve(v, r, x, rel_tol=1e-8, precision=precision)
+    assert st.status == 0 and st.num_iter > 5
+    true = np.linalg.norm(o.apply_operator(v, r, 1, x))
+    assert true <= 1.01e-8 * st.init_res_norm
+
+
+def test_mixed_is_exactly_scale_invariant():
+    o, v, r, T = heat_system()
+    x1 = T.copy()
+    s1 = o.solve(v, r, x1, rel_tol=1e-8, precision=1)
+    sc = 2.0 ** -100
+    x2 = T * sc
+    s2 = o.solve(v, r * sc, x2, rel_tol=1e-8, precision=1)
+    assert s1.status == 0 and s2.status == 0
+    assert (s1.num_iter, s1.num_outer) == (s2.num_iter, s2.num_outer)
+    assert s2.init_res_norm == s1.init_res_norm * sc and s2.final_res_norm == s1.final_res_norm * sc
+    np.testing.assert_array_equal(x2, x1 * sc)
