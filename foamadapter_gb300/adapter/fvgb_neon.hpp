@@ -334,7 +334,7 @@ struct SolverConfig {
     double tolerance = 0.0;
     int maxIter = 1000;
     bool mixedPrecision = false;
-    double innerRelTol = 1e-3;
+    double innerRelTol = 0.1;
     int innerMaxIter = 1000;
     int maxOuter = 50;
 };

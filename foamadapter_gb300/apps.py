@@ -56,7 +56,7 @@ class CavityPiso:
     non-orthogonal correctors), pressure reference cell 0 = 0."""
 
     def __init__(self, n=512, jitter=0.05, seed=12345, nu=0.01, dt=5e-4, n_corr=2, lid=(1.0, 0.0, 0.0),
-                 precision=abi.PREC_FP64, p_rel_tol=1e-8, p_max_iter=20000, inner_rel_tol=1e-2):
+                 precision=abi.PREC_FP64, p_rel_tol=1e-8, p_max_iter=20000, inner_rel_tol=0.1):
         self.hm = hm = mesh.box(n, n, 1, 1.0, 1.0, 1.0 / n, jitter=jitter, seed=seed, two_d=True)
         self.dm = dm = DeviceMesh(hm)
         self.dt, self.n_corr = dt, n_corr

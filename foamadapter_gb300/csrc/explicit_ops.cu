@@ -54,50 +54,107 @@ __global__ void k_interp_upwind(MeshView m, const double* __restrict__ flux,
     }
 }
 
+// ------------------------------------------------------------ gather entries
+// A cell's first kG gather entries are fetched together: the entry codes and
+// the cells (or boundary faces) across, then every face and cell value they
+// point to, so a thread has all its loads in flight at once instead of one
+// dependent pair per face.  The arithmetic then runs in ascending face order
+// exactly as the one-entry-at-a-time loop did; entries beyond kG (cells with
+// more than kG faces) take the per-entry path.
+constexpr int kG = 8;
+
+struct Entries {
+    int base, width;
+    int code[kG], other[kG];  // code FVGB_PAD beyond the cell's row
+};
+
+__device__ __forceinline__ void load_entries(const MeshView& m, int c, Entries& e) {
+    const int slice = c >> 5;
+    e.base = __ldg(&m.g_ptr[slice]) + (c & 31);
+    e.width = gwidth(m, slice);
+#pragma unroll
+    for (int j = 0; j < kG; ++j) {
+        e.code[j] = FVGB_PAD;
+        e.other[j] = 0;
+        if (j < e.width) {
+            e.code[j] = __ldg(&m.g_code[e.base + j * 32]);
+            e.other[j] = __ldg(&m.g_other[e.base + j * 32]);
+        }
+    }
+}
+
+// face index of an entry (a boundary entry's code is its index in face fields)
+__device__ __forceinline__ int entry_face(int code) { return code >= 0 ? code : -code - 1; }
+
 // ------------------------------------------------------------------------ div
 // face value seen from cell c across internal face f: owner-side formulas of
 // the reference with (P, N) = (owner, neighbour).
 template <int NC, int SCHEME>
+__device__ __forceinline__ void div_entry(const MeshView& m, int code, double F, const double* To, double wf,
+                                          const double* Tc, double* s) {
+    if (code >= m.nif) {  // boundary face: value from the boundary field
+#pragma unroll
+        for (int k = 0; k < NC; ++k) s[k] = s[k] + F * To[k];
+        return;
+    }
+    const bool isOwner = code >= 0;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        const double Town = isOwner ? Tc[k] : To[k];
+        const double Tnei = isOwner ? To[k] : Tc[k];
+        double tf;
+        if (SCHEME == FVGB_SCHEME_UPWIND) tf = F >= 0.0 ? Town : Tnei;
+        else tf = wf * (Town - Tnei) + Tnei;
+        const double fl = F * tf;
+        s[k] = isOwner ? s[k] + fl : s[k] - fl;
+    }
+}
+
+template <int NC, int SCHEME>
 __device__ __forceinline__ void div_cell(const MeshView& m, int c, const double* __restrict__ flux,
                                          const double* __restrict__ phi,
                                          const double* __restrict__ phi_b, double* s) {
-    const int slice = c >> 5, lane = c & 31;
-    const int base = __ldg(&m.g_ptr[slice]);
-    const int width = gwidth(m, slice);
+    Entries e;
+    load_entries(m, c, e);
     double Tc[NC];
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
         Tc[k] = __ldg(&phi[c * NC + k]);
         s[k] = 0.0;
     }
-    for (int j = 0; j < width; ++j) {
-        const int pos = base + j * 32 + lane;
-        const int code = __ldg(&m.g_code[pos]);
-        if (code == FVGB_PAD) break;
-        if (code >= m.nif) {  // boundary face: value from the boundary field
-            const int b = code - m.nif;
-            const double F = __ldg(&flux[code]);
+    double F[kG], W[kG], T[kG][NC];
 #pragma unroll
-            for (int k = 0; k < NC; ++k) s[k] = s[k] + F * __ldg(&phi_b[b * NC + k]);
-            continue;
-        }
-        const bool isOwner = code >= 0;
-        const int f = isOwner ? code : -code - 1;
-        const int o = __ldg(&m.g_other[pos]);
-        const double F = __ldg(&flux[f]);
-        double wf = 0.0;
-        if (SCHEME == FVGB_SCHEME_LINEAR) wf = __ldg(&m.w[f]);
+    for (int j = 0; j < kG; ++j) {
+        const int cd = e.code[j];
+        F[j] = 0.0;
+        W[j] = 0.0;
 #pragma unroll
-        for (int k = 0; k < NC; ++k) {
-            const double To = __ldg(&phi[o * NC + k]);
-            const double Town = isOwner ? Tc[k] : To;
-            const double Tnei = isOwner ? To : Tc[k];
-            double tf;
-            if (SCHEME == FVGB_SCHEME_UPWIND) tf = F >= 0.0 ? Town : Tnei;
-            else tf = wf * (Town - Tnei) + Tnei;
-            const double fl = F * tf;
-            s[k] = isOwner ? s[k] + fl : s[k] - fl;
-        }
+        for (int k = 0; k < NC; ++k) T[j][k] = 0.0;
+        if (cd == FVGB_PAD) continue;
+        const bool bnd = cd >= m.nif;
+        const int f = entry_face(cd);
+        F[j] = __ldg(&flux[f]);
+        const double* src = bnd ? phi_b : phi;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) T[j][k] = __ldg(&src[e.other[j] * NC + k]);
+        if (SCHEME == FVGB_SCHEME_LINEAR && !bnd) W[j] = __ldg(&m.w[f]);
+    }
+#pragma unroll
+    for (int j = 0; j < kG; ++j) {
+        if (e.code[j] == FVGB_PAD) break;
+        div_entry<NC, SCHEME>(m, e.code[j], F[j], T[j], W[j], Tc, s);
+    }
+    for (int j = kG; j < e.width; ++j) {
+        const int cd = __ldg(&m.g_code[e.base + j * 32]);
+        if (cd == FVGB_PAD) break;
+        const int o = __ldg(&m.g_other[e.base + j * 32]);
+        const int f = entry_face(cd);
+        const double* src = cd >= m.nif ? phi_b : phi;
+        double To[NC];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) To[k] = __ldg(&src[o * NC + k]);
+        const double wf = (SCHEME == FVGB_SCHEME_LINEAR && cd < m.nif) ? __ldg(&m.w[f]) : 0.0;
+        div_entry<NC, SCHEME>(m, cd, __ldg(&flux[f]), To, wf, Tc, s);
     }
 }
 
@@ -145,46 +202,71 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ----------------------------------------------------------------------- grad
+__device__ __forceinline__ void grad_entry(const MeshView& m, int code, double To, double wf, const double* S,
+                                           double Tc, double& g0, double& g1, double& g2) {
+    if (code >= m.nif) {
+        g0 = g0 + S[0] * To;
+        g1 = g1 + S[1] * To;
+        g2 = g2 + S[2] * To;
+        return;
+    }
+    const bool isOwner = code >= 0;
+    const double Town = isOwner ? Tc : To;
+    const double Tnei = isOwner ? To : Tc;
+    const double tf = wf * (Town - Tnei) + Tnei;
+    const double v0 = S[0] * tf;
+    const double v1 = S[1] * tf;
+    const double v2 = S[2] * tf;
+    if (isOwner) {
+        g0 = g0 + v0;
+        g1 = g1 + v1;
+        g2 = g2 + v2;
+    } else {
+        g0 = g0 - v0;
+        g1 = g1 - v1;
+        g2 = g2 - v2;
+    }
+}
+
 __global__ void __launch_bounds__(kThreads)
     k_grad(MeshView m, const double* __restrict__ phi, const double* __restrict__ phi_b,
            double coeff, int unit, double* __restrict__ out) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.n) return;
-    const int slice = c >> 5, lane = c & 31;
-    const int base = __ldg(&m.g_ptr[slice]);
-    const int width = gwidth(m, slice);
+    Entries e;
+    load_entries(m, c, e);
     const double Tc = __ldg(&phi[c]);
+    double T[kG], W[kG], S[kG][3];
+#pragma unroll
+    for (int j = 0; j < kG; ++j) {
+        const int cd = e.code[j];
+        T[j] = W[j] = S[j][0] = S[j][1] = S[j][2] = 0.0;
+        if (cd == FVGB_PAD) continue;
+        const bool bnd = cd >= m.nif;
+        const int f = entry_face(cd);
+        const double* src = bnd ? phi_b : phi;
+        T[j] = __ldg(&src[e.other[j]]);
+        const double* sf = bnd ? m.bSf + 3 * (cd - m.nif) : m.Sf + 3 * f;
+        S[j][0] = __ldg(&sf[0]);
+        S[j][1] = __ldg(&sf[1]);
+        S[j][2] = __ldg(&sf[2]);
+        if (!bnd) W[j] = __ldg(&m.w[f]);
+    }
     double g0 = 0.0, g1 = 0.0, g2 = 0.0;
-    for (int j = 0; j < width; ++j) {
-        const int pos = base + j * 32 + lane;
-        const int code = __ldg(&m.g_code[pos]);
-        if (code == FVGB_PAD) break;
-        if (code >= m.nif) {
-            const int b = code - m.nif;
-            const double tb = __ldg(&phi_b[b]);
-            g0 = g0 + __ldg(&m.bSf[3 * b]) * tb;
-            g1 = g1 + __ldg(&m.bSf[3 * b + 1]) * tb;
-            g2 = g2 + __ldg(&m.bSf[3 * b + 2]) * tb;
-            continue;
-        }
-        const bool isOwner = code >= 0;
-        const int f = isOwner ? code : -code - 1;
-        const double To = __ldg(&phi[__ldg(&m.g_other[pos])]);
-        const double Town = isOwner ? Tc : To;
-        const double Tnei = isOwner ? To : Tc;
-        const double tf = __ldg(&m.w[f]) * (Town - Tnei) + Tnei;
-        const double v0 = __ldg(&m.Sf[3 * f]) * tf;
-        const double v1 = __ldg(&m.Sf[3 * f + 1]) * tf;
-        const double v2 = __ldg(&m.Sf[3 * f + 2]) * tf;
-        if (isOwner) {
-            g0 = g0 + v0;
-            g1 = g1 + v1;
-            g2 = g2 + v2;
-        } else {
-            g0 = g0 - v0;
-            g1 = g1 - v1;
-            g2 = g2 - v2;
-        }
+#pragma unroll
+    for (int j = 0; j < kG; ++j) {
+        if (e.code[j] == FVGB_PAD) break;
+        grad_entry(m, e.code[j], T[j], W[j], S[j], Tc, g0, g1, g2);
+    }
+    for (int j = kG; j < e.width; ++j) {
+        const int cd = __ldg(&m.g_code[e.base + j * 32]);
+        if (cd == FVGB_PAD) break;
+        const int o = __ldg(&m.g_other[e.base + j * 32]);
+        const bool bnd = cd >= m.nif;
+        const int f = entry_face(cd);
+        const double* sf = bnd ? m.bSf + 3 * (cd - m.nif) : m.Sf + 3 * f;
+        const double Sv[3] = {__ldg(&sf[0]), __ldg(&sf[1]), __ldg(&sf[2])};
+        grad_entry(m, cd, __ldg(&(bnd ? phi_b : phi)[o]), bnd ? 0.0 : __ldg(&m.w[f]), Sv, Tc, g0, g1, g2);
     }
     const double sc = unit ? __ldg(&m.invV[c]) : coeff / __ldg(&m.V[c]);
     out[3 * c] = out[3 * c] + g0 * sc;
@@ -193,43 +275,69 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------------ laplacian
+// face flux g*(T_nei - T_own); the owner adds it, the neighbour subtracts it;
+// a boundary face adds g_b*(T_b - T_c)
+template <int NC>
+__device__ __forceinline__ void lap_entry(const MeshView& m, int code, double g, const double* To, const double* Tc,
+                                          double* s) {
+    if (code >= m.nif) {
+#pragma unroll
+        for (int k = 0; k < NC; ++k) s[k] = s[k] + g * (To[k] - Tc[k]);
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        if (code >= 0) s[k] = s[k] + g * (To[k] - Tc[k]);
+        else s[k] = s[k] - g * (Tc[k] - To[k]);
+    }
+}
+
 template <int NC>
 __global__ void __launch_bounds__(kThreads)
     k_lap(MeshView m, const double* __restrict__ gamma, const double* __restrict__ phi,
           const double* __restrict__ phi_b, double coeff, int unit, double* __restrict__ out) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.n) return;
-    const int slice = c >> 5, lane = c & 31;
-    const int base = __ldg(&m.g_ptr[slice]);
-    const int width = gwidth(m, slice);
+    Entries e;
+    load_entries(m, c, e);
     double Tc[NC], s[NC];
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
         Tc[k] = __ldg(&phi[c * NC + k]);
         s[k] = 0.0;
     }
-    for (int j = 0; j < width; ++j) {
-        const int pos = base + j * 32 + lane;
-        const int code = __ldg(&m.g_code[pos]);
-        if (code == FVGB_PAD) break;
-        if (code >= m.nif) {
-            const int b = code - m.nif;
-            const double g = __ldg(&gamma[code]) * __ldg(&m.bgeo[b]);
+    double Gm[kG], Ge[kG], T[kG][NC];
 #pragma unroll
-            for (int k = 0; k < NC; ++k) s[k] = s[k] + g * (__ldg(&phi_b[b * NC + k]) - Tc[k]);
-            continue;
-        }
-        const bool isOwner = code >= 0;
-        const int f = isOwner ? code : -code - 1;
-        const int o = __ldg(&m.g_other[pos]);
-        const double g = __ldg(&gamma[f]) * __ldg(&m.geo[f]);
+    for (int j = 0; j < kG; ++j) {
+        const int cd = e.code[j];
+        Gm[j] = Ge[j] = 0.0;
 #pragma unroll
-        for (int k = 0; k < NC; ++k) {
-            const double To = __ldg(&phi[o * NC + k]);
-            // face flux is g*(T_nei - T_own); the owner adds it, the neighbour subtracts it
-            if (isOwner) s[k] = s[k] + g * (To - Tc[k]);
-            else s[k] = s[k] - g * (Tc[k] - To);
-        }
+        for (int k = 0; k < NC; ++k) T[j][k] = 0.0;
+        if (cd == FVGB_PAD) continue;
+        const bool bnd = cd >= m.nif;
+        const int f = entry_face(cd);
+        Gm[j] = __ldg(&gamma[f]);
+        Ge[j] = bnd ? __ldg(&m.bgeo[cd - m.nif]) : __ldg(&m.geo[f]);
+        const double* src = bnd ? phi_b : phi;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) T[j][k] = __ldg(&src[e.other[j] * NC + k]);
+    }
+#pragma unroll
+    for (int j = 0; j < kG; ++j) {
+        if (e.code[j] == FVGB_PAD) break;
+        lap_entry<NC>(m, e.code[j], Gm[j] * Ge[j], T[j], Tc, s);
+    }
+    for (int j = kG; j < e.width; ++j) {
+        const int cd = __ldg(&m.g_code[e.base + j * 32]);
+        if (cd == FVGB_PAD) break;
+        const int o = __ldg(&m.g_other[e.base + j * 32]);
+        const bool bnd = cd >= m.nif;
+        const int f = entry_face(cd);
+        const double g = __ldg(&gamma[f]) * (bnd ? __ldg(&m.bgeo[cd - m.nif]) : __ldg(&m.geo[f]));
+        double To[NC];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) To[k] = __ldg(&(bnd ? phi_b : phi)[o * NC + k]);
+        lap_entry<NC>(m, cd, g, To, Tc, s);
     }
     const double sc = unit ? __ldg(&m.invV[c]) : coeff / __ldg(&m.V[c]);
 #pragma unroll

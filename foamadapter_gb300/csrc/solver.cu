@@ -179,8 +179,10 @@ __device__ __forceinline__ double spmv_row(const MeshView& m, const double* __re
     return s;
 }
 
-__device__ __forceinline__ float spmv_row_f(const MeshView& m, const float* __restrict__ val,
-                                            const float* __restrict__ x, int i, float diag) {
+// FP32 row of the difference-form SpMV: e_i x_i + sum_k a_k (x_{col_k} - x_i),
+// fmaf chain in slot order (the diagonal and padding slots hold 0 and add 0).
+__device__ __forceinline__ float spmv_row_diff(const MeshView& m, const float* __restrict__ a,
+                                               const float* __restrict__ x, int i, float xi, float ei) {
     const int slice = i >> 5, lane = i & 31;
     const int b0 = __ldg(&m.m_ptr[slice]);
     const int base = b0 + lane;
@@ -191,16 +193,16 @@ __device__ __forceinline__ float spmv_row_f(const MeshView& m, const float* __re
         v[k] = 0.0f;
         xv[k] = 0.0f;
         if (k < w) {
-            v[k] = __ldg(&val[base + k * 32]);
+            v[k] = __ldg(&a[base + k * 32]);
             xv[k] = __ldg(&x[__ldg(&m.m_col[base + k * 32])]);
         }
     }
-    float s = diag;
+    float s = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-        if (k < w) s = fmaf(v[k], xv[k], s);
-    for (int k = 8; k < w; ++k) s = fmaf(__ldg(&val[base + k * 32]), __ldg(&x[__ldg(&m.m_col[base + k * 32])]), s);
-    return s;
+        if (k < w) s = fmaf(v[k], xv[k] - xi, s);
+    for (int k = 8; k < w; ++k) s = fmaf(__ldg(&a[base + k * 32]), __ldg(&x[__ldg(&m.m_col[base + k * 32])]) - xi, s);
+    return fmaf(ei, xi, s);
 }
 
 __device__ __forceinline__ void case_done(BatchState* bs, CaseState* cs) {
@@ -398,10 +400,21 @@ __global__ void k_set_params(Layout L, int ncases, SolverParams prm) {
 }
 
 // --------------------------------------------------- mixed precision (FP32 inner)
-// Power-of-two scale that brings |s r| to [1, 2): the FP32 inner solve works on
-// (float)(sig * s r).  Scaling by a power of two is exact, so the inner iterates
-// are the unscaled ones times sig, except that FP32 products of a tiny residual
-// (a field that has almost stopped changing) no longer underflow.
+// The inner CG runs in FP32 on the row-sign-normalised system  D_s A y = D_s r
+// (D_s = the sign of each row's diagonal: the solution is unchanged, and for a
+// case whose diagonals share one sign every dot product is positive), Jacobi
+// preconditioned with |1/a_ii|.  The FP32 SpMV uses the difference form
+//     (A p)_i = e_i p_i + sum_{j != i} a_ij (p_j - p_i),   e_i = sum_j a_ij,
+// which keeps the near-null space of a Laplacian (smooth fields) exact in FP32:
+// in a pressure equation every e_i but the reference cell's is zero up to
+// round-off, so rounding a_ij to FP32 no longer perturbs the smallest
+// eigenvalues (the plain form needs about 20% more inner iterations there).
+// Dots: per-thread fmaf and block trees in FP32, block partials summed in FP64.
+
+// Power-of-two scale bringing |D^-1/2 r| to [1, 2): the FP32 residual is
+// (float)(sig * r).  Scaling by a power of two is exact, so the inner iterates
+// are the unscaled ones times sig, except that the FP32 products of a tiny
+// residual (a field that has almost stopped changing) no longer underflow.
 __device__ __host__ __forceinline__ void residual_scale(double sres, double* sig, double* isig) {
     int e = 0;
     if (sres > 0.0 && isfinite(sres)) {
@@ -412,11 +425,14 @@ __device__ __host__ __forceinline__ void residual_scale(double sres, double* sig
     *isig = ldexp(1.0, e);
 }
 
-// s_i = 1/sqrt|a_ii|; signflags bit0: a positive diagonal, bit1: negative, bit2: zero/NaN;
-// |s (b - A x0)| of every case -> sres, the magnitude the first residual is scaled by
+// Per row: dinv = (float)(1/a_ii) (signed), a32 = (float)(sign * a_ij) at the
+// off-diagonal slots (0 at the diagonal and the padding), ev = (float)(sign * e_i)
+// with e_i summed in FP64 in slot order; signflags bit0: a positive diagonal,
+// bit1: negative, bit2: zero/NaN; sres = sqrt(sum r_i^2 |1/a_ii|) of r = b - A x0,
+// the magnitude the first residual is scaled by.
 __global__ void __launch_bounds__(kT)
-    k_ir_scale(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
-               double* __restrict__ s, double* __restrict__ pa) {
+    k_ir_prepare(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
+                 float* __restrict__ a32, float* __restrict__ ev, float* __restrict__ dinv, double* __restrict__ pa) {
     __shared__ double sma[kT];
     const Blk k = blk_info(L);
     CaseState* cs = &L.cases[k.c];
@@ -429,10 +445,27 @@ __global__ void __launch_bounds__(kT)
         if (i >= k.end) continue;
         const double d = __ldg(&val[__ldg(&m.diag_pos[i])]);
         f |= d > 0.0 ? 1u : (d < 0.0 ? 2u : 4u);
-        const double si = 1.0 / sqrt(fabs(d));
-        s[i] = si;
-        const double sr = si * (__ldg(&b[i]) - spmv_row(m, val, x, i));
-        asr = fma(sr, sr, asr);
+        const float di = (float)(1.0 / d);
+        dinv[i] = di;
+        const double sg = d < 0.0 ? -1.0 : 1.0;
+        const int slice = i >> 5, lane = i & 31;
+        const int b0 = __ldg(&m.m_ptr[slice]);
+        const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+        double e = 0.0;
+        for (int kk = 0; kk < w; ++kk) {
+            const int pos = b0 + kk * 32 + lane;
+            const int code = __ldg(&m.m_code[pos]);
+            if (code == FVGB_PAD) {
+                a32[pos] = 0.0f;
+                continue;
+            }
+            const double a = __ldg(&val[pos]);
+            e = e + a;
+            a32[pos] = code == -1 ? 0.0f : (float)(sg * a);
+        }
+        ev[i] = (float)(sg * e);
+        const double ri = __ldg(&b[i]) - spmv_row(m, val, x, i);
+        asr = fma(ri * (double)fabsf(di), ri, asr);
     }
     f = __reduce_or_sync(0xffffffffu, f);
     if ((threadIdx.x & 31) == 0 && f) atomicOr(&cs->signflags, f);
@@ -447,35 +480,13 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
-// ahat at every slot of the case's rows: (float)((a * s_row) * s_col); diagonal and padding 0
-__global__ void __launch_bounds__(kT)
-    k_ir_scaled_values(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ s,
-                       float* __restrict__ ah) {
-    const Blk k = blk_info(L);
-#pragma unroll
-    for (int j = 0; j < kRowsPerThread; ++j) {
-        const int i = blk_row(k, j);
-        if (i >= k.end) continue;
-        const int slice = i >> 5, lane = i & 31;
-        const int b0 = __ldg(&m.m_ptr[slice]);
-        const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
-        const double si = s[i];
-        for (int kk = 0; kk < w; ++kk) {
-            const int pos = b0 + kk * 32 + lane;
-            const int code = __ldg(&m.m_code[pos]);
-            float v = 0.0f;
-            if (code != FVGB_PAD && code != -1) v = (float)((__ldg(&val[pos]) * si) * s[__ldg(&m.m_col[pos])]);
-            ah[pos] = v;
-        }
-    }
-}
-
-// refinement step: r = b - A x (FP64), rr; rhat = (float)(s r); y = 0; rho = rhat.rhat;
-// FIRST: p = rhat.  Later steps keep p; k_ir_reliable_dir folds rhat into it.
+// refinement step: r = b - A x (FP64), |r|; rh = sign * (float)(sig r); y = 0;
+// rho = rh . (|dinv| rh).  FIRST: p = |dinv| rh.  Later steps keep p;
+// k_ir_reliable_dir folds the new residual into it.
 template <bool FIRST>
 __global__ void __launch_bounds__(kT)
     k_ir_residual(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
-                  const double* __restrict__ s, float* __restrict__ rh, float* __restrict__ y,
+                  const float* __restrict__ dinv, float* __restrict__ rh, float* __restrict__ y,
                   float* __restrict__ p, double* __restrict__ pa, double* __restrict__ pb, double* __restrict__ pc,
                   cudaGraphConditionalHandle h_outer, cudaGraphConditionalHandle h_inner) {
     __shared__ double sma[kT], smb[kT], smc[kT];
@@ -485,7 +496,7 @@ __global__ void __launch_bounds__(kT)
     if (FIRST || ld_volatile(&cs->active)) {
         const double* __restrict__ x = L.bs->prm.x;
         double sig, isig;
-        residual_scale(cs->sres, &sig, &isig);  // from the previous residual (k_ir_scale's for the first)
+        residual_scale(cs->sres, &sig, &isig);  // from the previous residual (k_ir_prepare's for the first)
         double arr = 0.0, asr = 0.0;
         float arho = 0.0f;
 #pragma unroll
@@ -494,13 +505,15 @@ __global__ void __launch_bounds__(kT)
             if (i >= k.end) continue;
             const double ri = __ldg(&b[i]) - spmv_row(m, val, x, i);
             arr = fma(ri, ri, arr);
-            const double sr = __ldg(&s[i]) * ri;
-            asr = fma(sr, sr, asr);
-            const float rhi = (float)(sr * sig);
+            const float di = __ldg(&dinv[i]);
+            asr = fma(ri * (double)fabsf(di), ri, asr);
+            float rhi = (float)(ri * sig);
+            if (di < 0.0f) rhi = -rhi;
             rh[i] = rhi;
             y[i] = 0.0f;
-            if (FIRST) p[i] = rhi;
-            arho = fmaf(rhi, rhi, arho);
+            const float zi = fabsf(di) * rhi;
+            if (FIRST) p[i] = zi;
+            arho = fmaf(rhi, zi, arho);
         }
         const double ba = block_tree(arr, sma);
         const double bc = block_tree(asr, smc);
@@ -542,9 +555,14 @@ __global__ void __launch_bounds__(kT)
                     }
                 }
                 // direction after this update: keep p (beta = rho/rho_prev, with p brought
-                // from the previous scale to this one) unless no inner iteration ran since
-                // the last update, then restart from rhat
-                cs->frel = (FIRST || cs->inner_it == 0) ? -1.0f : (float)((rho / cs->rho_prev) * (cs->sig * isig));
+                // from the previous scale to this one), or restart from the new
+                // preconditioned residual when no inner iteration ran since the last update
+                // or the FP32 recursion has drifted (true rho above 4x the recursive one:
+                // the old direction would then swamp the new residual)
+                const double g = sig * cs->isig;  // new scale / old scale, a power of two
+                const double rho_rec = cs->rho * g * g;
+                const bool restart = FIRST || cs->inner_it == 0 || rho > 4.0 * rho_rec;
+                cs->frel = restart ? -1.0f : (float)((rho / cs->rho_prev) * (cs->sig * isig));
                 cs->sig = sig;
                 cs->isig = isig;
                 cs->sres = sqrt(sr2);
@@ -568,9 +586,9 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
-// p = rhat + frel * p after a reliable update (p = rhat when frel < 0)
+// p = z + frel * p after a reliable update (p = z when frel < 0), z = |dinv| rh
 __global__ void __launch_bounds__(kT)
-    k_ir_reliable_dir(Layout L, const float* __restrict__ rh, float* __restrict__ p) {
+    k_ir_reliable_dir(Layout L, const float* __restrict__ dinv, const float* __restrict__ rh, float* __restrict__ p) {
     const Blk k = blk_info(L);
     const CaseState* cs = &L.cases[k.c];
     if (!ld_volatile(&cs->inner_active)) return;
@@ -579,7 +597,8 @@ __global__ void __launch_bounds__(kT)
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int i = blk_row(k, j);
         if (i >= k.end) continue;
-        p[i] = fb < 0.0f ? __ldg(&rh[i]) : fmaf(fb, p[i], __ldg(&rh[i]));
+        const float zi = fabsf(__ldg(&dinv[i])) * __ldg(&rh[i]);
+        p[i] = fb < 0.0f ? zi : fmaf(fb, p[i], zi);
     }
 }
 
@@ -588,23 +607,22 @@ __device__ __forceinline__ void inner_stop(const Layout& L, CaseState* cs) {
     atomicSub(&L.bs->n_inner, 1);
 }
 
-// q = (S A S) p with the diagonal sign; pq -> alpha
+// q = (D_s A) p in the difference form; p.q -> alpha
 __global__ void __launch_bounds__(kT)
-    k_ir_spmv(Layout L, MeshView m, const float* __restrict__ ah, const float* __restrict__ p,
-              float* __restrict__ q, double* __restrict__ pa) {
+    k_ir_spmv(Layout L, MeshView m, const float* __restrict__ a32, const float* __restrict__ ev,
+              const float* __restrict__ p, float* __restrict__ q, double* __restrict__ pa) {
     const Blk k = blk_info(L);
     CaseState* cs = &L.cases[k.c];
     if (!ld_volatile(&cs->inner_active)) return;
     __shared__ double sma[kT];
     __shared__ float smf[kT];
-    const float dsign = cs->signflags == 2u ? -1.0f : 1.0f;  // sign of every diagonal of the case
     float acc = 0.0f;
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int i = blk_row(k, j);
         if (i >= k.end) continue;
         const float pi = __ldg(&p[i]);
-        const float qi = spmv_row_f(m, ah, p, i, dsign * pi);
+        const float qi = spmv_row_diff(m, a32, p, i, pi, __ldg(&ev[i]));
         q[i] = qi;
         acc = fmaf(pi, qi, acc);
     }
@@ -626,9 +644,11 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
+// y += alpha p, rh -= alpha q, rho = rh . (|dinv| rh)
 __global__ void __launch_bounds__(kT)
-    k_ir_update(Layout L, const float* __restrict__ p, const float* __restrict__ q, float* __restrict__ y,
-                float* __restrict__ rh, double* __restrict__ pa, cudaGraphConditionalHandle h_inner) {
+    k_ir_update(Layout L, const float* __restrict__ dinv, const float* __restrict__ p, const float* __restrict__ q,
+                float* __restrict__ y, float* __restrict__ rh, double* __restrict__ pa,
+                cudaGraphConditionalHandle h_inner) {
     __shared__ double sma[kT];
     __shared__ float smf[kT];
     const Blk k = blk_info(L);
@@ -644,7 +664,7 @@ __global__ void __launch_bounds__(kT)
             y[i] = fmaf(fa, pi, y[i]);
             const float ri = fmaf(-fa, __ldg(&q[i]), rh[i]);
             rh[i] = ri;
-            acc = fmaf(ri, ri, acc);
+            acc = fmaf(ri, fabsf(__ldg(&dinv[i])) * ri, acc);
         }
         const float ba = block_tree_f(acc, smf);
         if (threadIdx.x == 0) pa[blockIdx.x] = (double)ba;
@@ -666,8 +686,9 @@ __global__ void __launch_bounds__(kT)
         cudaGraphSetConditional(h_inner, ld_volatile(&L.bs->n_inner) > 0 ? 1u : 0u);
 }
 
+// p = z + beta p, z = |dinv| rh
 __global__ void __launch_bounds__(kT)
-    k_ir_dir(Layout L, const float* __restrict__ rh, float* __restrict__ p) {
+    k_ir_dir(Layout L, const float* __restrict__ dinv, const float* __restrict__ rh, float* __restrict__ p) {
     const Blk k = blk_info(L);
     const CaseState* cs = &L.cases[k.c];
     if (!ld_volatile(&cs->inner_active)) return;
@@ -676,22 +697,22 @@ __global__ void __launch_bounds__(kT)
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int i = blk_row(k, j);
         if (i >= k.end) continue;
-        p[i] = fmaf(fb, p[i], __ldg(&rh[i]));
+        p[i] = fmaf(fb, p[i], fabsf(__ldg(&dinv[i])) * __ldg(&rh[i]));
     }
 }
 
-__global__ void __launch_bounds__(kT)
-    k_ir_xupdate(Layout L, const double* __restrict__ s, const float* __restrict__ y) {
+// x += y / sig (y carries the power-of-two scale of its residual)
+__global__ void __launch_bounds__(kT) k_ir_xupdate(Layout L, const float* __restrict__ y) {
     const Blk k = blk_info(L);
     const CaseState* cs = &L.cases[k.c];
     if (!ld_volatile(&cs->active)) return;
     double* __restrict__ x = L.bs->prm.x;
-    const double isig = cs->isig;  // y carries the scale of its residual
+    const double isig = cs->isig;
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int i = blk_row(k, j);
         if (i >= k.end) continue;
-        x[i] = fma(__ldg(&s[i]) * isig, (double)__ldg(&y[i]), x[i]);
+        x[i] = fma((double)__ldg(&y[i]), isig, x[i]);
     }
 }
 
@@ -957,8 +978,8 @@ struct SolverCache {
     std::vector<void*> allocs;
     double *dinv = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *pa = nullptr, *pb = nullptr;
     double* pc = nullptr;
-    double* s = nullptr;
-    float *ah = nullptr, *rh = nullptr, *y = nullptr, *pf = nullptr, *qf = nullptr;
+    float *ah = nullptr, *dinvf = nullptr, *ev = nullptr, *rh = nullptr, *y = nullptr, *pf = nullptr,
+          *qf = nullptr;
     cudaGraphExec_t g64 = nullptr, gmix = nullptr;
     fvgb_solver_stats* h_stats = nullptr;  // pinned [ncases]
     GridBar* bar = nullptr;
@@ -1081,8 +1102,9 @@ fvgb_status build_mixed(SolverCache* c) {
     const size_t n = (size_t)c->n;
     const fvgb_ls* ls = c->ls;
     const fvgb_mesh* mesh = ls->mesh;
-    cudaError_t e = calloc_dev(c, &c->s, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->ah, (size_t)mesh->m_len);
+    cudaError_t e = calloc_dev(c, &c->ah, (size_t)mesh->m_len);
+    if (e == cudaSuccess) e = calloc_dev(c, &c->dinvf, n);
+    if (e == cudaSuccess) e = calloc_dev(c, &c->ev, n);
     if (e == cudaSuccess) e = calloc_dev(c, &c->rh, n);
     if (e == cudaSuccess) e = calloc_dev(c, &c->y, n);
     if (e == cudaSuccess) e = calloc_dev(c, &c->pf, n);
@@ -1098,20 +1120,18 @@ fvgb_status build_mixed(SolverCache* c) {
     const unsigned nb = (unsigned)c->nb;
     e = cudaGraphConditionalHandleCreate(&ho, g, 0, cudaGraphCondAssignDefault);
     if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
-    cudaGraphNode_t n_scale, n_vals, n_res0, n_outer, n_fin, o_inner, o_x, o_res, o_dir, i_spmv, i_upd, i_dir;
+    cudaGraphNode_t n_prep, n_res0, n_outer, n_fin, o_inner, o_x, o_res, o_dir, i_spmv, i_upd, i_dir;
     cudaGraph_t obody = nullptr, ibody = nullptr;
-    void* a_scale[] = {&L, &m, &val, &b, &c->s, &c->pa};
-    void* a_vals[] = {&L, &m, &val, &c->s, &c->ah};
-    void* a_res[] = {&L, &m, &val, &b, &c->s, &c->rh, &c->y, &c->pf, &c->pa, &c->pb, &c->pc, &ho, &hi};
-    void* a_spmv[] = {&L, &m, &c->ah, &c->pf, &c->qf, &c->pa};
-    void* a_upd[] = {&L, &c->pf, &c->qf, &c->y, &c->rh, &c->pa, &hi};
-    void* a_dir[] = {&L, &c->rh, &c->pf};
-    void* a_x[] = {&L, &c->s, &c->y};
-    void* a_rdir[] = {&L, &c->rh, &c->pf};
+    void* a_prep[] = {&L, &m, &val, &b, &c->ah, &c->ev, &c->dinvf, &c->pa};
+    void* a_res[] = {&L, &m, &val, &b, &c->dinvf, &c->rh, &c->y, &c->pf, &c->pa, &c->pb, &c->pc, &ho, &hi};
+    void* a_spmv[] = {&L, &m, &c->ah, &c->ev, &c->pf, &c->qf, &c->pa};
+    void* a_upd[] = {&L, &c->dinvf, &c->pf, &c->qf, &c->y, &c->rh, &c->pa, &hi};
+    void* a_dir[] = {&L, &c->dinvf, &c->rh, &c->pf};
+    void* a_x[] = {&L, &c->y};
+    void* a_rdir[] = {&L, &c->dinvf, &c->rh, &c->pf};
     void* a_fin[] = {&L};
-    if (e == cudaSuccess) e = add_kernel(g, &n_scale, nullptr, (void*)k_ir_scale, nb, kT, a_scale);
-    if (e == cudaSuccess) e = add_kernel(g, &n_vals, &n_scale, (void*)k_ir_scaled_values, nb, kT, a_vals);
-    if (e == cudaSuccess) e = add_kernel(g, &n_res0, &n_vals, (void*)k_ir_residual<true>, nb, kT, a_res);
+    if (e == cudaSuccess) e = add_kernel(g, &n_prep, nullptr, (void*)k_ir_prepare, nb, kT, a_prep);
+    if (e == cudaSuccess) e = add_kernel(g, &n_res0, &n_prep, (void*)k_ir_residual<true>, nb, kT, a_res);
     if (e == cudaSuccess) e = add_while(g, &n_outer, &n_res0, ho, &obody);
     if (e == cudaSuccess) e = add_while(obody, &o_inner, nullptr, hi, &ibody);
     if (e == cudaSuccess) e = add_kernel(ibody, &i_spmv, nullptr, (void*)k_ir_spmv, nb, kT, a_spmv);

@@ -251,7 +251,7 @@ class LinearSystem:
         return v, r, bm[:hm.nbf], br[:hm.nbf * self.ncomp]
 
     def solve(self, x: torch.Tensor, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=abi.PREC_FP64,
-              inner_rel_tol=1e-2, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,), kernel_mode=0):
+              inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,), kernel_mode=0):
         cfg = abi.SolverCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer,
                             kernel_mode)
         st = abi.SolverStats()

@@ -16,7 +16,7 @@ CALC, FIXED_VALUE, FIXED_GRADIENT = 0, 1, 2
 
 class CavityPisoCPU:
     def __init__(self, hm, nu=0.01, dt=5e-4, n_corr=2, lid=(1.0, 0.0, 0.0), precision=0, p_rel_tol=1e-8,
-                 p_max_iter=20000, inner_rel_tol=1e-2):
+                 p_max_iter=20000, inner_rel_tol=0.1):
         self.hm, self.o = hm, Oracle(hm)
         self.dt, self.n_corr = dt, n_corr
         self.solve_kw = dict(rel_tol=p_rel_tol, max_iter=p_max_iter, precision=precision,

@@ -590,15 +590,21 @@ static int32_t solve_fp64(const or_csr* A, const double* val, const double* b, d
 }
 
 /* ---------------------------------- mixed precision CG with reliable updates
- * CG on the Jacobi-scaled system  S A S y = S r,  S = diag(1/sqrt|a_ii|), in
- * FP32 (the scaled diagonal is sign(a_ii); all diagonals must share one sign).
- * Scaled off-diagonals are rounded once to float: ahat_ij = (float)((a_ij*s_i)*s_j);
- * row sums q = sign*p_i, then fmaf over the off-diagonals in column order.
+ * (solver.cu, mixed-precision section)
+ * FP32 CG on the row-sign-normalised system D_s A y = D_s r (D_s = sign of each
+ * row's diagonal; all diagonals must share one sign), Jacobi-preconditioned with
+ * |1/a_ii| held as the FP32 dinv = (float)(1/a_ii).  The FP32 SpMV is the
+ * difference form: a32_ij = (float)(sign*a_ij) off the diagonal, ev_i =
+ * (float)(sign*e_i) with e_i the FP64 row sum in column order, and
+ * q_i = fmaf(ev_i, p_i, sum fmaf(a32_ij, p_j - p_i, .)) over the row in column
+ * order (the diagonal entry holds 0).
  * Dots: per-thread fmaf and block tree in float, block partials summed in double.
+ * Residuals are scaled by sig = 2^-ilogb(|D^-1/2 r_prev|), exactly.
  * Reliable update (FP64): when rho has dropped below rho_ref*max(d^2, (tol/res)^2)
- * (d = inner_rel_tol) or after inner_max_iter steps, x += S y, r = b - A x is
+ * (d = inner_rel_tol) or after inner_max_iter steps, x += y/sig, r = b - A x is
  * recomputed, tested, and replaces the FP32 residual; the direction continues
- * with beta = rho_true/rho_prev (restarted from rhat when no step ran). */
+ * with beta = rho_true/rho_prev, restarted from z when no step ran or when
+ * rho_true > 4 rho_recursive (drift of the FP32 recursion). */
 static double dot_tree_f(int32_t n, const float* a, const float* b, double* part) {
     int32_t nb = nblocks_of(n);
 #pragma omp parallel for schedule(static)
@@ -617,7 +623,7 @@ static double dot_tree_f(int32_t n, const float* a, const float* b, double* part
     return final_tree(nb, part);
 }
 
-/* Power-of-two scale bringing |s r| to [1, 2) (solver.cu residual_scale): exact,
+/* Power-of-two scale bringing |D^-1/2 r| to [1, 2) (solver.cu residual_scale): exact,
  * it only keeps the FP32 products of a tiny residual out of the subnormal range. */
 static void residual_scale(double sres, double* sig, double* isig) {
     int e = 0;
@@ -629,9 +635,10 @@ static void residual_scale(double sres, double* sig, double* isig) {
     *isig = ldexp(1.0, e);
 }
 
-/* r = b - A x; rh = (float)((s r) sig); returns |r|, *sres = |s r| (both by the GPU's tree) */
+/* r = b - A x; rh = sign*(float)(r*sig), z = |dinv|*rh; returns |r|,
+ * *sres = sqrt(sum r^2 |dinv|) (both by the GPU's tree) */
 static double residual_step(const or_csr* A, const double* val, const double* b, const double* x,
-                            const double* s, double sig, float* rh, double* r, double* part, double* part2,
+                            const float* dinv, double sig, float* rh, float* z, double* part, double* part2,
                             int32_t n, int32_t nb, double* sres) {
 #pragma omp parallel for schedule(static)
     for (int32_t blk = 0; blk < nb; ++blk) {
@@ -644,11 +651,12 @@ static double residual_step(const or_csr* A, const double* val, const double* b,
                 double sm;
                 spmv_row_fma(A, val, x, i, &sm);
                 double ri = b[i] - sm;
-                r[i] = ri;
                 arr = fma(ri, ri, arr);
-                double sr = s[i] * ri;
-                asr = fma(sr, sr, asr);
-                rh[i] = (float)(sr * sig);
+                asr = fma(ri * (double)fabsf(dinv[i]), ri, asr);
+                float rhi = (float)(ri * sig);
+                if (dinv[i] < 0.0f) rhi = -rhi;
+                rh[i] = rhi;
+                z[i] = fabsf(dinv[i]) * rhi;
             }
             tp[t] = arr;
             tq[t] = asr;
@@ -663,36 +671,39 @@ static double residual_step(const or_csr* A, const double* val, const double* b,
 static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, double* x,
                            const or_solver_cfg* cfg, or_solver_stats* st) {
     const int32_t n = A->n, nb = nblocks_of(n), nnz = A->nnz;
-    double* s = zalloc(n);
-    float* ah = (float*)calloc((size_t)nnz, sizeof(float));
-    double dsign = 0.0;
+    float* dinv = (float*)calloc(n ? n : 1, sizeof(float));
+    float* ev = (float*)calloc(n ? n : 1, sizeof(float));
+    float* a32 = (float*)calloc((size_t)(nnz ? nnz : 1), sizeof(float));
+    unsigned flags = 0;
     for (int32_t i = 0; i < n; ++i) {
         double d = val[A->row_offs[i] + A->diag_off[i]];
-        double sg = d > 0 ? 1.0 : (d < 0 ? -1.0 : 0.0);
-        if (i == 0) dsign = sg;
-        if (sg == 0.0 || sg != dsign) {
-            free(s); free(ah);
-            st->status = ST_UNSUPPORTED;
-            return ST_UNSUPPORTED;
+        flags |= d > 0.0 ? 1u : (d < 0.0 ? 2u : 4u);
+        dinv[i] = (float)(1.0 / d);
+        double sg = d < 0.0 ? -1.0 : 1.0, e = 0.0;
+        for (int32_t j = A->row_offs[i]; j < A->row_offs[i + 1]; ++j) {
+            e = e + val[j];
+            a32[j] = A->col[j] == i ? 0.0f : (float)(sg * val[j]);
         }
-        s[i] = 1.0 / sqrt(fabs(d));
+        ev[i] = (float)(sg * e);
     }
-    for (int32_t i = 0; i < n; ++i)
-        for (int32_t j = A->row_offs[i]; j < A->row_offs[i + 1]; ++j)
-            ah[j] = (float)((val[j] * s[i]) * s[A->col[j]]);
-    const float fs = (float)dsign;
+    if ((flags & 4u) || flags == 3u) {
+        free(dinv); free(ev); free(a32);
+        st->status = ST_UNSUPPORTED;
+        return ST_UNSUPPORTED;
+    }
     const double dr = cfg->inner_rel_tol * cfg->inner_rel_tol;
-    double *r = zalloc(n), *part = zalloc(nb), *part2 = zalloc(nb);
+    double *part = zalloc(nb), *part2 = zalloc(nb);
     float *rh = (float*)calloc(n, sizeof(float)), *y = (float*)calloc(n, sizeof(float));
     float *p = (float*)calloc(n, sizeof(float)), *q = (float*)calloc(n, sizeof(float));
+    float *z = (float*)calloc(n, sizeof(float));
     int32_t total = 0, outer = 0, status = ST_OK, inner_it = 0;
     double rho, rho_prev = 0.0, itol, res, res0, tol, sres, sig, isig;
-    /* |s r0| sets the scale of the first residual (k_ir_scale), then the first residual */
-    residual_step(A, val, b, x, s, 1.0, rh, r, part, part2, n, nb, &sres);
+    /* |D^-1/2 r0| sets the scale of the first residual (k_ir_prepare), then the first residual */
+    residual_step(A, val, b, x, dinv, 1.0, rh, z, part, part2, n, nb, &sres);
     residual_scale(sres, &sig, &isig);
-    res = residual_step(A, val, b, x, s, sig, rh, r, part, part2, n, nb, &sres);
-    for (int32_t i = 0; i < n; ++i) { y[i] = 0.0f; p[i] = rh[i]; }
-    rho = dot_tree_f(n, rh, rh, part);
+    res = residual_step(A, val, b, x, dinv, sig, rh, z, part, part2, n, nb, &sres);
+    for (int32_t i = 0; i < n; ++i) { y[i] = 0.0f; p[i] = z[i]; }
+    rho = dot_tree_f(n, rh, z, part);
     res0 = res;
     tol = cfg->rel_tol * res0;
     if (cfg->abs_tol > tol) tol = cfg->abs_tol;
@@ -706,10 +717,11 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
         while (inner) {
 #pragma omp parallel for schedule(static)
             for (int32_t i = 0; i < n; ++i) {
-                float acc = fs * p[i];
+                const float pi = p[i];
+                float acc = 0.0f;
                 for (int32_t j = A->row_offs[i]; j < A->row_offs[i + 1]; ++j)
-                    if (A->col[j] != i) acc = fmaf(ah[j], p[A->col[j]], acc);
-                q[i] = acc;
+                    acc = fmaf(a32[j], p[A->col[j]] - pi, acc);
+                q[i] = fmaf(ev[i], pi, acc);
             }
             double pq = dot_tree_f(n, p, q, part);
             double alpha = rho / pq;
@@ -722,8 +734,9 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
             for (int32_t i = 0; i < n; ++i) {
                 y[i] = fmaf(fa, p[i], y[i]);
                 rh[i] = fmaf(-fa, q[i], rh[i]);
+                z[i] = fabsf(dinv[i]) * rh[i];
             }
-            double rhon = dot_tree_f(n, rh, rh, part);
+            double rhon = dot_tree_f(n, rh, z, part);
             float fb = (float)(rhon / rho);
             rho_prev = rho;
             rho = rhon;
@@ -731,34 +744,37 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
             ++total;
             int more = rhon > itol && inner_it < cfg->inner_max_iter && total < cfg->max_iter;
             if (!more) { inner = 0; break; }
-            for (int32_t i = 0; i < n; ++i) p[i] = fmaf(fb, p[i], rh[i]);
+            for (int32_t i = 0; i < n; ++i) p[i] = fmaf(fb, p[i], z[i]);
         }
         if (done) break;
-        /* reliable update; the new residual takes the scale of the previous |s r| */
-        for (int32_t i = 0; i < n; ++i) x[i] = fma(s[i] * isig, (double)y[i], x[i]);
-        const double sig_old = sig;
+        /* reliable update; the new residual takes the scale of the previous |D^-1/2 r| */
+        for (int32_t i = 0; i < n; ++i) x[i] = fma((double)y[i], isig, x[i]);
+        const double sig_old = sig, isig_old = isig;
         residual_scale(sres, &sig, &isig);
-        res = residual_step(A, val, b, x, s, sig, rh, r, part, part2, n, nb, &sres);
+        res = residual_step(A, val, b, x, dinv, sig, rh, z, part, part2, n, nb, &sres);
         for (int32_t i = 0; i < n; ++i) y[i] = 0.0f;
-        double rho_true = dot_tree_f(n, rh, rh, part);
+        double rho_true = dot_tree_f(n, rh, z, part);
         ++outer;
         if (!isfinite(res)) { status = ST_BREAKDOWN; done = 1; }
         else if (!(res > tol) || res == 0.0) done = 1;
         else if (outer >= cfg->max_outer || total >= cfg->max_iter) { status = ST_NOT_CONVERGED; done = 1; }
-        float frel = inner_it == 0 ? -1.0f : (float)((rho_true / rho_prev) * (sig_old * isig));
+        /* restart when no step ran or the FP32 recursion drifted (true rho > 4x recursive) */
+        const double g = sig * isig_old, rho_rec = rho * g * g;
+        const int restart = inner_it == 0 || rho_true > 4.0 * rho_rec;
+        float frel = restart ? -1.0f : (float)((rho_true / rho_prev) * (sig_old * isig));
         rho = rho_true;
         { double dt = (tol / res) * (tol / res); itol = rho * (dr > dt ? dr : dt); }
         inner_it = 0;
         inner = !done && rho > itol && cfg->inner_max_iter > 0 && total < cfg->max_iter;
         if (inner)
-            for (int32_t i = 0; i < n; ++i) p[i] = frel < 0.0f ? rh[i] : fmaf(frel, p[i], rh[i]);
+            for (int32_t i = 0; i < n; ++i) p[i] = frel < 0.0f ? z[i] : fmaf(frel, p[i], z[i]);
     }
     st->init_res_norm = res0;
     st->final_res_norm = res;
     st->num_iter = total;
     st->num_outer = outer;
     st->status = status;
-    free(s); free(ah); free(r); free(part); free(part2); free(rh); free(y); free(p); free(q);
+    free(dinv); free(ev); free(a32); free(part); free(part2); free(rh); free(y); free(p); free(q); free(z);
     return status;
 }
 

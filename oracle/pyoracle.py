@@ -158,7 +158,7 @@ class Oracle:
         return out
 
     def solve(self, values, rhs, x, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=0,
-              inner_rel_tol=1e-3, inner_max_iter=200, max_outer=30):
+              inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50):
         cfg = OrCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer)
         st = OrStats()
         self.L.or_solve(C.byref(self.csr()), p(values), p(rhs), p(x), C.byref(cfg), C.byref(st))

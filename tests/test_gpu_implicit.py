@@ -228,13 +228,14 @@ def test_mixed_tiny_residual_is_scale_invariant(cuda):
     np.testing.assert_array_equal(v2, v1)
     np.testing.assert_array_equal(r2, r1 * sc)
     x1, x2 = T1.internal.clone(), T2.internal.clone()
-    s1 = ls1.solve(x1, rel_tol=1e-8, precision=abi.PREC_MIXED_IR)
-    s2 = ls2.solve(x2, rel_tol=1e-8, precision=abi.PREC_MIXED_IR)
+    kw = dict(rel_tol=1e-8, inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50)
+    s1 = ls1.solve(x1, precision=abi.PREC_MIXED_IR, **kw)
+    s2 = ls2.solve(x2, precision=abi.PREC_MIXED_IR, **kw)
     assert s1.status == abi.OK and s2.status == abi.OK
     assert (s1.num_iter, s1.num_outer) == (s2.num_iter, s2.num_outer)
     assert s2.final_res_norm == s1.final_res_norm * sc
     np.testing.assert_array_equal(x2.cpu().numpy(), x1.cpu().numpy() * sc)
     xo = np.full(hm.n, 300.0 * sc)
-    so = o.solve(v2, r2, xo, rel_tol=1e-8, precision=1)
+    so = o.solve(v2, r2, xo, precision=1, **kw)
     assert so.status == 0 and so.num_iter == s2.num_iter
     np.testing.assert_array_equal(x2.cpu().numpy(), xo)
