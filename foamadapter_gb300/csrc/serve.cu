@@ -200,7 +200,9 @@ fvgb_status enqueue_step(Slot* s, int k) {
     fvgb_bc bc{s->types, s->ref};
     fvgb_status st = fvgb_assemble(s->ls, terms, 3, s->dt, &bc, s->Tb, s->stream);
     if (st != FVGB_OK) return st;
-    fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, 0.1, 1000, 50, r.kernel_mode};
+    // the graph path by default: requests overlap on the device, which one
+    // cooperative (persistent) kernel per request would serialise
+    fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, 0.1, 1000, 50, r.kernel_mode == 0 ? 1 : r.kernel_mode};
     st = fvgb_solve_async(s->ls, s->T, &cfg, s->stats_dev + k, s->stream);
     if (st != FVGB_OK) return st;
     return fvgb_bc_correct(s->mesh, 1, &bc, s->T, s->Tb, s->stream);

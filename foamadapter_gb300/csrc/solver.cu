@@ -716,54 +716,102 @@ __global__ void __launch_bounds__(kT) k_ir_xupdate(Layout L, const float* __rest
     }
 }
 
-// ------------------------------------------------- persistent FP64 CG (one case)
-// For systems small enough that launch latency dominates an iteration: ONE
-// cooperative launch runs the whole solve.  Each resident block walks the
-// 1024-row virtual blocks vb = blockIdx.x, blockIdx.x + gridDim.x, ... exactly
-// as the graph kernels' blocks do, writes the same per-virtual-block partials,
-// and after a grid barrier EVERY block sums all partials with the same tree,
-// so all blocks take identical decisions and the iterates are the bits of the
-// graph path.  Data written during the kernel is read through L2 (__ldcg).
-// Grid barriers spin a bounded number of times; on time-out a block raises the
-// abort flag, every block leaves at its next barrier and the solve reports
-// FVGB_ERR_CUDA.
+// ------------------------------------------------------ persistent solves (one case)
+// For systems small enough that launch latency dominates an iteration, ONE
+// cooperative launch runs the whole solve.  A persistent block has 1024 threads
+// and walks the 1024-row virtual blocks vb = blockIdx.x, blockIdx.x + gridDim.x,
+// ...; thread t computes row vb*1024 + t.  Dot products are staged in shared
+// memory and summed by 256 "tree threads" with exactly the row assignment and
+// order of the graph kernels (4 rows per thread, then the block tree), so the
+// per-virtual-block partials, and after a grid barrier the final trees that
+// EVERY block computes over all partials, are the bits of the graph path; all
+// blocks then take identical decisions.  Data written during the kernel is
+// read through L2 (__ldcg).  Grid barriers spin a bounded number of times; on
+// time-out a block raises the abort flag, every block leaves at its next
+// barrier and the solve reports FVGB_ERR_CUDA.
+constexpr int kPT = 1024;
+
 struct GridBar {
-    unsigned int count, gen;
+    unsigned long long count;  // arrivals since the launch (never reset inside it)
     int abort, pad;
 };
 
-__device__ __forceinline__ bool grid_sync(GridBar* g, unsigned int nblocks) {
+// Barrier number `epoch` (1, 2, ...) of a grid of `nblocks` blocks.
+__device__ __forceinline__ bool grid_sync(GridBar* g, unsigned long long target) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned int* vgen = &g->gen;
-        const unsigned int my = *vgen;
-        __threadfence();
         int good = 1;
-        if (atomicAdd(&g->count, 1u) == nblocks - 1) {
-            atomicExch(&g->count, 0u);
-            __threadfence();
-            atomicAdd(&g->gen, 1u);
-        } else {
-            unsigned long long spins = 0;
-            while (*vgen == my) {
-                if (*(volatile int*)&g->abort) {
-                    good = 0;
-                    break;
-                }
-                if (++spins > (1ull << 24)) {  // about 2 s
-                    atomicExch(&g->abort, 1);
-                    good = 0;
-                    break;
-                }
-                __nanosleep(100);
+        unsigned long long v;
+        asm volatile("atom.add.release.gpu.u64 %0, [%1], 1;" : "=l"(v) : "l"(&g->count) : "memory");
+        v += 1;
+        unsigned long long spins = 0;
+        while (v < target) {
+            int ab;
+            asm volatile("ld.relaxed.gpu.s32 %0, [%1];" : "=r"(ab) : "l"(&g->abort) : "memory");
+            if (ab) {
+                good = 0;
+                break;
             }
+            if (++spins > (1ull << 26)) {  // a few seconds
+                atomicExch(&g->abort, 1);
+                good = 0;
+                break;
+            }
+            if (spins > 32) __nanosleep(32);
+            asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(&g->count) : "memory");
         }
-        __threadfence();
         ok = good;
     }
     __syncthreads();
     return ok != 0;
+}
+
+// row (within a virtual block) of tree thread tp's j-th row: the graph kernels' blk_row
+__device__ __forceinline__ int tree_row(int tp, int j) { return (tp >> 5) * (32 * kRowsPerThread) + j * 32 + (tp & 31); }
+
+// block_tree over the partials of threads 0..kT-1 of a kPT-thread block; valid in warp 0
+__device__ __forceinline__ double tree256(double v, double* sm) {
+    if (threadIdx.x < kT) sm[threadIdx.x] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x < 32) {
+        s = sm[threadIdx.x];
+#pragma unroll
+        for (int k = 1; k < kT / 32; ++k) s = s + sm[threadIdx.x + 32 * k];
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off);
+    }
+    __syncthreads();
+    return s;
+}
+
+__device__ __forceinline__ float tree256f(float v, float* sm) {
+    if (threadIdx.x < kT) sm[threadIdx.x] = v;
+    __syncthreads();
+    float s = 0.0f;
+    if (threadIdx.x < 32) {
+        s = sm[threadIdx.x];
+#pragma unroll
+        for (int k = 1; k < kT / 32; ++k) s = s + sm[threadIdx.x + 32 * k];
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off);
+    }
+    __syncthreads();
+    return s;
+}
+
+// final_tree over nvb partials, broadcast to every thread of the block
+__device__ __forceinline__ double final_all(const double* part, int nvb, double* sm, double* cell) {
+    double a = 0.0;
+    if (threadIdx.x < kT)
+        for (int i = threadIdx.x; i < nvb; i += kT) a = a + __ldcg(&part[i]);
+    const double s = tree256(a, sm);
+    if (threadIdx.x == 0) *cell = s;
+    __syncthreads();
+    const double r = *cell;
+    __syncthreads();
+    return r;
 }
 
 __device__ __forceinline__ double spmv_row_cg(const MeshView& m, const double* __restrict__ val, const double* x,
@@ -790,53 +838,51 @@ __device__ __forceinline__ double spmv_row_cg(const MeshView& m, const double* _
     return s;
 }
 
-__device__ __forceinline__ int vrow(int vb, int j) {
-    return vb * kRowsPerBlock + (threadIdx.x >> 5) * (32 * kRowsPerThread) + j * 32 + (threadIdx.x & 31);
-}
-
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(kPT, 1)
     k_pcg_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
                      double* dinv, double* r, double* p, double* q, double* z, double* pa, double* pb, GridBar* gb,
                      int nvb) {
-    __shared__ double sma[kT], smb[kT];
-    const int n = m.n;
+    __shared__ double sA[kPT], sB[kPT], sm[kT], sm2[kT], cell;
+    const int n = m.n, T = threadIdx.x;
     const SolverParams prm = L.bs->prm;
     double* x = prm.x;
-    const unsigned int G = gridDim.x;
+    const unsigned long long G = gridDim.x;
+    unsigned long long epoch = 0;
     // init: r = b - A x, z = p = dinv r, r.z, r.r
-    for (int vb = blockIdx.x; vb < nvb; vb += G) {
-        double arz = 0.0, arr = 0.0;
-#pragma unroll
-        for (int j = 0; j < kRowsPerThread; ++j) {
-            const int i = vrow(vb, j);
-            if (i >= n) continue;
+    for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
+        const int i = vb * kRowsPerBlock + T;
+        double ri = 0.0, zi = 0.0;
+        if (i < n) {
             const double di = 1.0 / __ldg(&val[__ldg(&m.diag_pos[i])]);
             dinv[i] = di;
-            const double ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
-            const double zi = di * ri;
+            ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
+            zi = di * ri;
             r[i] = ri;
             p[i] = zi;
-            arz = fma(ri, zi, arz);
-            arr = fma(ri, ri, arr);
         }
-        const double ba = block_tree(arz, sma), bb = block_tree(arr, smb);
-        if (threadIdx.x == 0) {
+        sA[T] = ri;
+        sB[T] = zi;
+        __syncthreads();
+        double arz = 0.0, arr = 0.0;
+        if (T < kT)
+#pragma unroll
+            for (int j = 0; j < kRowsPerThread; ++j) {
+                const int rr = tree_row(T, j);
+                if (vb * kRowsPerBlock + rr >= n) continue;
+                arz = fma(sA[rr], sB[rr], arz);
+                arr = fma(sA[rr], sA[rr], arr);
+            }
+        const double ba = tree256(arz, sm), bb = tree256(arr, sm2);
+        if (T == 0) {
             pa[vb] = ba;
             pb[vb] = bb;
         }
     }
-    bool aborted = !grid_sync(gb, G);
-    __shared__ double s_rz, s_rr, s_a, s_b2;
+    bool aborted = !grid_sync(gb, ++epoch * G);
     double rz = 0.0, rr = 0.0;
     if (!aborted) {
-        const double rzb = final_tree(pa, nvb, sma), rrb = final_tree(pb, nvb, smb);
-        if (threadIdx.x == 0) {
-            s_rz = rzb;
-            s_rr = rrb;
-        }
-        __syncthreads();
-        rz = s_rz;
-        rr = s_rr;
+        rz = final_all(pa, nvb, sm, &cell);
+        rr = final_all(pb, nvb, sm, &cell);
     }
     const double res0 = sqrt(rr);
     double tol = prm.rel_tol * res0;
@@ -849,64 +895,73 @@ __global__ void __launch_bounds__(kT)
         status = FVGB_ERR_NOT_CONVERGED;
     }
     while (!done) {
-        for (int vb = blockIdx.x; vb < nvb; vb += G) {
-            double acc = 0.0;
-#pragma unroll
-            for (int j = 0; j < kRowsPerThread; ++j) {
-                const int i = vrow(vb, j);
-                if (i >= n) continue;
-                const double qi = spmv_row_cg(m, val, p, i);
+        // q = A p, p.q
+        for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
+            const int i = vb * kRowsPerBlock + T;
+            double pi = 0.0, qi = 0.0;
+            if (i < n) {
+                qi = spmv_row_cg(m, val, p, i);
                 q[i] = qi;
-                acc = fma(__ldcg(&p[i]), qi, acc);
+                pi = __ldcg(&p[i]);
             }
-            const double ba = block_tree(acc, sma);
-            if (threadIdx.x == 0) pa[vb] = ba;
+            sA[T] = pi;
+            sB[T] = qi;
+            __syncthreads();
+            double acc = 0.0;
+            if (T < kT)
+#pragma unroll
+                for (int j = 0; j < kRowsPerThread; ++j) {
+                    const int rw = tree_row(T, j);
+                    if (vb * kRowsPerBlock + rw < n) acc = fma(sA[rw], sB[rw], acc);
+                }
+            const double ba = tree256(acc, sm);
+            if (T == 0) pa[vb] = ba;
         }
-        if (!grid_sync(gb, G)) {
+        if (!grid_sync(gb, ++epoch * G)) {
             aborted = true;
             break;
         }
-        const double pqb = final_tree(pa, nvb, sma);
-        if (threadIdx.x == 0) s_a = pqb;
-        __syncthreads();
-        const double pq = s_a;
+        const double pq = final_all(pa, nvb, sm, &cell);
         const double alpha = rz / pq;
         if (pq == 0.0 || !isfinite(alpha)) {
             status = FVGB_ERR_BREAKDOWN;
             break;
         }
-        for (int vb = blockIdx.x; vb < nvb; vb += G) {
-            double arz = 0.0, arr = 0.0;
-#pragma unroll
-            for (int j = 0; j < kRowsPerThread; ++j) {
-                const int i = vrow(vb, j);
-                if (i >= n) continue;
+        // x += alpha p, r -= alpha q, z = dinv r, r.z, r.r
+        for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
+            const int i = vb * kRowsPerBlock + T;
+            double ri = 0.0, zi = 0.0;
+            if (i < n) {
                 x[i] = fma(alpha, __ldcg(&p[i]), __ldcg(&x[i]));
-                const double ri = fma(-alpha, __ldcg(&q[i]), __ldcg(&r[i]));
+                ri = fma(-alpha, __ldcg(&q[i]), __ldcg(&r[i]));
                 r[i] = ri;
-                const double zi = __ldcg(&dinv[i]) * ri;
+                zi = __ldcg(&dinv[i]) * ri;
                 z[i] = zi;
-                arz = fma(ri, zi, arz);
-                arr = fma(ri, ri, arr);
             }
-            const double ba = block_tree(arz, sma), bb = block_tree(arr, smb);
-            if (threadIdx.x == 0) {
+            sA[T] = ri;
+            sB[T] = zi;
+            __syncthreads();
+            double arz = 0.0, arr = 0.0;
+            if (T < kT)
+#pragma unroll
+                for (int j = 0; j < kRowsPerThread; ++j) {
+                    const int rw = tree_row(T, j);
+                    if (vb * kRowsPerBlock + rw >= n) continue;
+                    arz = fma(sA[rw], sB[rw], arz);
+                    arr = fma(sA[rw], sA[rw], arr);
+                }
+            const double ba = tree256(arz, sm), bb = tree256(arr, sm2);
+            if (T == 0) {
                 pa[vb] = ba;
                 pb[vb] = bb;
             }
         }
-        if (!grid_sync(gb, G)) {
+        if (!grid_sync(gb, ++epoch * G)) {
             aborted = true;
             break;
         }
-        const double rznb = final_tree(pa, nvb, sma), rrb = final_tree(pb, nvb, smb);
-        if (threadIdx.x == 0) {
-            s_a = rznb;
-            s_b2 = rrb;
-        }
-        __syncthreads();
-        const double rzn = s_a;
-        rr = s_b2;
+        const double rzn = final_all(pa, nvb, sm, &cell);
+        rr = final_all(pb, nvb, sm, &cell);
         res = sqrt(rr);
         ++iter;
         const double beta = rzn / rz;
@@ -920,24 +975,329 @@ __global__ void __launch_bounds__(kT)
             status = FVGB_ERR_NOT_CONVERGED;
             break;
         }
-        for (int vb = blockIdx.x; vb < nvb; vb += G) {
-#pragma unroll
-            for (int j = 0; j < kRowsPerThread; ++j) {
-                const int i = vrow(vb, j);
-                if (i >= n) continue;
-                p[i] = fma(beta, __ldcg(&p[i]), __ldcg(&z[i]));
-            }
+        // p = z + beta p
+        for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
+            const int i = vb * kRowsPerBlock + T;
+            if (i < n) p[i] = fma(beta, __ldcg(&p[i]), __ldcg(&z[i]));
         }
-        if (!grid_sync(gb, G)) {
+        if (!grid_sync(gb, ++epoch * G)) {
             aborted = true;
             break;
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (blockIdx.x == 0 && T == 0) {
         CaseState* cs = &L.cases[0];
         cs->res0 = res0;
         cs->res = res;
         cs->iter = iter;
+        cs->status = aborted ? FVGB_ERR_CUDA : status;
+    }
+}
+
+// Mixed-precision solve in one cooperative launch: the algorithm, arithmetic
+// and decisions of the graph kernels (k_ir_prepare ... k_ir_reliable_dir).  An
+// inner iteration takes two grid barriers: the direction update p = z + beta p
+// is folded into the SpMV, which forms the new direction of every row it reads
+// from the previous direction and z (double-buffered p: the new one goes to the
+// other buffer while other blocks still read the old).
+struct DirMode {
+    int kind;  // 0: p as stored, 1: p = z, 2: p = coef*p + z
+    float coef;
+};
+
+__device__ __forceinline__ float dir_of(const DirMode& d, float pold, float zv) {
+    return d.kind == 0 ? pold : (d.kind == 1 ? zv : fmaf(d.coef, pold, zv));
+}
+
+__device__ __forceinline__ float spmv_row_diff_dir(const MeshView& m, const float* __restrict__ a, const float* pold,
+                                                   const float* zz, const DirMode& d, int i, float xi, float ei) {
+    const int slice = i >> 5, lane = i & 31;
+    const int b0 = __ldg(&m.m_ptr[slice]);
+    const int base = b0 + lane;
+    const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+    float v[8], xv[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = 0.0f;
+        xv[k] = 0.0f;
+        if (k < w) {
+            const int cidx = __ldg(&m.m_col[base + k * 32]);
+            v[k] = __ldg(&a[base + k * 32]);
+            xv[k] = dir_of(d, __ldcg(&pold[cidx]), d.kind == 0 ? 0.0f : __ldcg(&zz[cidx]));
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (k < w) s = fmaf(v[k], xv[k] - xi, s);
+    for (int k = 8; k < w; ++k) {
+        const int cidx = __ldg(&m.m_col[base + k * 32]);
+        const float xc = dir_of(d, __ldcg(&pold[cidx]), d.kind == 0 ? 0.0f : __ldcg(&zz[cidx]));
+        s = fmaf(__ldg(&a[base + k * 32]), xc - xi, s);
+    }
+    return fmaf(ei, xi, s);
+}
+
+__global__ void __launch_bounds__(kPT, 1)
+    k_ir_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
+                    float* a32, float* ev, float* dinv, float* rh, float* y, float* pbuf0, float* pbuf1, float* z,
+                    float* q, double* pa, double* pb, double* pc, GridBar* gb, int nvb) {
+    __shared__ double sD[kPT], sm[kT], sm2[kT], sm3[kT], cell;
+    __shared__ float sF1[kPT], sF2[kPT], smf[kT];
+    __shared__ unsigned int sflags;
+    const int n = m.n, T = threadIdx.x;
+    const SolverParams prm = L.bs->prm;
+    double* x = prm.x;
+    const unsigned long long G = gridDim.x;
+    unsigned long long epoch = 0;
+    CaseState* cs = &L.cases[0];
+    bool aborted = false;
+    // prepare: dinv, a32, ev, sign flags, |D^-1/2 (b - A x0)|
+    if (T == 0) sflags = 0u;
+    __syncthreads();
+    for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
+        const int i = vb * kRowsPerBlock + T;
+        double ri = 0.0;
+        float di = 0.0f;
+        if (i < n) {
+            const double d = __ldg(&val[__ldg(&m.diag_pos[i])]);
+            atomicOr(&sflags, d > 0.0 ? 1u : (d < 0.0 ? 2u : 4u));
+            di = (float)(1.0 / d);
+            dinv[i] = di;
+            const double sg = d < 0.0 ? -1.0 : 1.0;
+            const int slice = i >> 5, lane = i & 31;
+            const int b0 = __ldg(&m.m_ptr[slice]);
+            const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+            double e = 0.0;
+            for (int kk = 0; kk < w; ++kk) {
+                const int pos = b0 + kk * 32 + lane;
+                const int code = __ldg(&m.m_code[pos]);
+                if (code == FVGB_PAD) {
+                    a32[pos] = 0.0f;
+                    continue;
+                }
+                const double av = __ldg(&val[pos]);
+                e = e + av;
+                a32[pos] = code == -1 ? 0.0f : (float)(sg * av);
+            }
+            ev[i] = (float)(sg * e);
+            ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
+        }
+        sD[T] = ri;
+        sF1[T] = di;
+        __syncthreads();
+        double asr = 0.0;
+        if (T < kT)
+#pragma unroll
+            for (int j = 0; j < kRowsPerThread; ++j) {
+                const int rw = tree_row(T, j);
+                if (vb * kRowsPerBlock + rw < n) asr = fma(sD[rw] * (double)fabsf(sF1[rw]), sD[rw], asr);
+            }
+        const double ba = tree256(asr, sm);
+        if (T == 0) pa[vb] = ba;
+    }
+    if (T == 0 && sflags) atomicOr(&cs->signflags, sflags);
+    aborted = !grid_sync(gb, ++epoch * G);
+    double sres = aborted ? 0.0 : sqrt(final_all(pa, nvb, sm, &cell));
+    double sig = 1.0, isig = 1.0;
+    const unsigned int flags = *(volatile unsigned int*)&cs->signflags;
+    // refinement state (the graph path keeps it in CaseState)
+    double res0 = 0.0, res = 0.0, tol = 0.0, rho = 0.0, rho_prev = 0.0, itol = 0.0;
+    int total = 0, outer = 0, inner_it = 0, status = FVGB_OK;
+    float* pcur = pbuf0;
+    float* pnext = pbuf1;
+    DirMode dm{0, 0.0f};
+    bool first = true, done = aborted, inner = false;
+    while (!done) {
+        if (!first) {
+            // x += y / sig
+            for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
+                const int i = vb * kRowsPerBlock + T;
+                if (i < n) x[i] = fma((double)__ldcg(&y[i]), isig, __ldcg(&x[i]));
+            }
+            if (!grid_sync(gb, ++epoch * G)) {
+                aborted = true;
+                break;
+            }
+        }
+        // residual: r = b - A x (FP64), rh = sign*(float)(sig r), y = 0, z = |dinv| rh
+        double nsig, nisig;
+        residual_scale(sres, &nsig, &nisig);
+        for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
+            const int i = vb * kRowsPerBlock + T;
+            double ri = 0.0;
+            float di = 0.0f, rhi = 0.0f, zi = 0.0f;
+            if (i < n) {
+                ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
+                di = __ldcg(&dinv[i]);
+                rhi = (float)(ri * nsig);
+                if (di < 0.0f) rhi = -rhi;
+                rh[i] = rhi;
+                y[i] = 0.0f;
+                zi = fabsf(di) * rhi;
+                z[i] = zi;
+                if (first) pcur[i] = zi;
+            }
+            sD[T] = ri;
+            sF1[T] = rhi;
+            sF2[T] = di;
+            __syncthreads();
+            double arr = 0.0, asr = 0.0;
+            float arho = 0.0f;
+            if (T < kT)
+#pragma unroll
+                for (int j = 0; j < kRowsPerThread; ++j) {
+                    const int rw = tree_row(T, j);
+                    if (vb * kRowsPerBlock + rw >= n) continue;
+                    const double rv = sD[rw];
+                    arr = fma(rv, rv, arr);
+                    asr = fma(rv * (double)fabsf(sF2[rw]), rv, asr);
+                    arho = fmaf(sF1[rw], fabsf(sF2[rw]) * sF1[rw], arho);
+                }
+            const double ba = tree256(arr, sm), bc = tree256(asr, sm3);
+            const float bb = tree256f(arho, smf);
+            if (T == 0) {
+                pa[vb] = ba;
+                pb[vb] = (double)bb;
+                pc[vb] = bc;
+            }
+        }
+        if (!grid_sync(gb, ++epoch * G)) {
+            aborted = true;
+            break;
+        }
+        {
+            const double rr = final_all(pa, nvb, sm, &cell);
+            const double nrho = final_all(pb, nvb, sm, &cell);
+            const double sr2 = final_all(pc, nvb, sm, &cell);
+            res = sqrt(rr);
+            if (!first) outer += 1;
+            if (first) {
+                res0 = res;
+                tol = prm.rel_tol * res;
+                if (prm.abs_tol > tol) tol = prm.abs_tol;
+                if ((flags & 4u) || flags == 3u) {
+                    status = FVGB_ERR_UNSUPPORTED;
+                    done = true;
+                }
+            }
+            if (!done) {
+                if (!isfinite(res)) {
+                    status = FVGB_ERR_BREAKDOWN;
+                    done = true;
+                } else if (!(res > tol) || res == 0.0) {
+                    done = true;
+                } else if (outer >= prm.max_outer || total >= prm.max_iter) {
+                    status = FVGB_ERR_NOT_CONVERGED;
+                    done = true;
+                }
+            }
+            const double g = nsig * isig;
+            const double rho_rec = rho * g * g;
+            const bool restart = first || inner_it == 0 || nrho > 4.0 * rho_rec;
+            const float frel = restart ? -1.0f : (float)((nrho / rho_prev) * (sig * nisig));
+            sig = nsig;
+            isig = nisig;
+            sres = sqrt(sr2);
+            rho = nrho;
+            const double dr = prm.inner_rel_tol * prm.inner_rel_tol;
+            const double dt = (tol / res) * (tol / res);
+            itol = rho * (dr > dt ? dr : dt);
+            inner_it = 0;
+            inner = !done && rho > itol && prm.inner_max_iter > 0 && total < prm.max_iter;
+            dm = first ? DirMode{0, 0.0f} : (frel < 0.0f ? DirMode{1, 0.0f} : DirMode{2, frel});
+            first = false;
+        }
+        if (done) break;
+        while (inner) {
+            // direction (into pnext unless p is taken as stored), q = A p, p.q
+            for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
+                const int i = vb * kRowsPerBlock + T;
+                float pi = 0.0f, qi = 0.0f;
+                if (i < n) {
+                    pi = dir_of(dm, __ldcg(&pcur[i]), dm.kind == 0 ? 0.0f : __ldcg(&z[i]));
+                    if (dm.kind != 0) pnext[i] = pi;
+                    qi = spmv_row_diff_dir(m, a32, pcur, z, dm, i, pi, __ldg(&ev[i]));
+                    q[i] = qi;
+                }
+                sF1[T] = pi;
+                sF2[T] = qi;
+                __syncthreads();
+                float acc = 0.0f;
+                if (T < kT)
+#pragma unroll
+                    for (int j = 0; j < kRowsPerThread; ++j) {
+                        const int rw = tree_row(T, j);
+                        if (vb * kRowsPerBlock + rw < n) acc = fmaf(sF1[rw], sF2[rw], acc);
+                    }
+                const float ba = tree256f(acc, smf);
+                if (T == 0) pa[vb] = (double)ba;
+            }
+            if (dm.kind != 0) {
+                float* t = pcur;
+                pcur = pnext;
+                pnext = t;
+            }
+            if (!grid_sync(gb, ++epoch * G)) {
+                aborted = true;
+                break;
+            }
+            const double pq = final_all(pa, nvb, sm, &cell);
+            const double alpha = rho / pq;
+            if (pq == 0.0 || !isfinite(alpha)) {
+                inner = false;
+                if (inner_it == 0) {
+                    status = FVGB_ERR_BREAKDOWN;
+                    done = true;
+                }
+                break;
+            }
+            const float fa = (float)alpha;
+            // y += alpha p, rh -= alpha q, z = |dinv| rh, rh.z
+            for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
+                const int i = vb * kRowsPerBlock + T;
+                float ri = 0.0f, zi = 0.0f;
+                if (i < n) {
+                    y[i] = fmaf(fa, __ldcg(&pcur[i]), __ldcg(&y[i]));
+                    ri = fmaf(-fa, __ldcg(&q[i]), __ldcg(&rh[i]));
+                    rh[i] = ri;
+                    zi = fabsf(__ldcg(&dinv[i])) * ri;
+                    z[i] = zi;
+                }
+                sF1[T] = ri;
+                sF2[T] = zi;
+                __syncthreads();
+                float acc = 0.0f;
+                if (T < kT)
+#pragma unroll
+                    for (int j = 0; j < kRowsPerThread; ++j) {
+                        const int rw = tree_row(T, j);
+                        if (vb * kRowsPerBlock + rw < n) acc = fmaf(sF1[rw], sF2[rw], acc);
+                    }
+                const float ba = tree256f(acc, smf);
+                if (T == 0) pa[vb] = (double)ba;
+            }
+            if (!grid_sync(gb, ++epoch * G)) {
+                aborted = true;
+                break;
+            }
+            const double rhon = final_all(pa, nvb, sm, &cell);
+            const float fbeta = (float)(rhon / rho);
+            rho_prev = rho;
+            rho = rhon;
+            inner_it += 1;
+            total += 1;
+            inner = rhon > itol && inner_it < prm.inner_max_iter && total < prm.max_iter;
+            dm = DirMode{2, fbeta};
+        }
+        if (aborted) break;
+    }
+    if (blockIdx.x == 0 && T == 0) {
+        cs->res0 = res0;
+        cs->res = res;
+        cs->iter = 0;
+        cs->total = total;
+        cs->outer = outer;
         cs->status = aborted ? FVGB_ERR_CUDA : status;
     }
 }
@@ -983,7 +1343,8 @@ struct SolverCache {
     cudaGraphExec_t g64 = nullptr, gmix = nullptr;
     fvgb_solver_stats* h_stats = nullptr;  // pinned [ncases]
     GridBar* bar = nullptr;
-    int persistent_grid = 0;               // co-resident blocks of k_pcg_persistent (0: not set up)
+    float *pf2 = nullptr, *zf = nullptr;   // second direction buffer and z of the persistent mixed solve
+    int pgrid_fp64 = 0, pgrid_mixed = 0;   // co-resident blocks of the persistent kernels (0: not asked yet)
     int32_t* h_active = nullptr;           // pinned copy of n_active for the host-driven loop
 };
 
@@ -1109,6 +1470,8 @@ fvgb_status build_mixed(SolverCache* c) {
     if (e == cudaSuccess) e = calloc_dev(c, &c->y, n);
     if (e == cudaSuccess) e = calloc_dev(c, &c->pf, n);
     if (e == cudaSuccess) e = calloc_dev(c, &c->qf, n);
+    if (e == cudaSuccess) e = calloc_dev(c, &c->pf2, n);
+    if (e == cudaSuccess) e = calloc_dev(c, &c->zf, n);
     if (e != cudaSuccess) return cuda_fail(e, "mixed CG workspace");
     MeshView m = mesh->v;
     Layout L = c->L;
@@ -1162,27 +1525,36 @@ fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
     return FVGB_OK;
 }
 
-// FP64 single-case solves of small systems run as one persistent cooperative
-// kernel (launch latency dominates their iterations); everything else runs the
-// graph.  cfg->kernel_mode: 0 automatic, 1 graph, 2 persistent when possible,
+// Single-case solves of small systems run as one persistent cooperative kernel
+// (launch latency dominates their iterations); everything else runs the graph.
+// cfg->kernel_mode: 0 automatic, 1 graph, 2 persistent when possible,
 // 3 host-driven loop (see host_loop).
-bool use_persistent(SolverCache* c, const fvgb_solver_cfg* cfg) {
-    if (cfg->precision != FVGB_PREC_FP64 || c->ncases != 1 || cfg->kernel_mode == 1) return false;
-    if (cfg->kernel_mode != 2 && c->n > (1 << 20)) return false;
-    if (c->persistent_grid == 0) {
+int persistent_grid(SolverCache* c, bool mixed) {
+    int& g = mixed ? c->pgrid_mixed : c->pgrid_fp64;
+    if (g == 0) {
         int dev = 0, sms = 0, per_sm = 0, coop = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent, kT, 0);
-        if (!coop || per_sm <= 0 || cudaMalloc(&c->bar, sizeof(GridBar)) != cudaSuccess) {
-            c->persistent_grid = -1;
-        } else {
-            c->allocs.push_back(c->bar);
-            c->persistent_grid = sms * per_sm;
-        }
+        if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ir_persistent, kPT, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent, kPT, 0);
+        g = (!coop || per_sm <= 0) ? -1 : sms * per_sm;
     }
-    return c->persistent_grid > 0;
+    return g;
+}
+
+bool use_persistent(SolverCache* c, const fvgb_solver_cfg* cfg) {
+    if (c->ncases != 1 || cfg->kernel_mode == 1 || cfg->kernel_mode == 3) return false;
+    if (cfg->kernel_mode != 2 && c->n > (1 << 20)) return false;
+    if (persistent_grid(c, cfg->precision == FVGB_PREC_MIXED_IR) <= 0) return false;
+    if (!c->bar) {
+        if (cudaMalloc(&c->bar, sizeof(GridBar)) != cudaSuccess) {
+            c->bar = nullptr;
+            return false;
+        }
+        c->allocs.push_back(c->bar);
+    }
+    return true;
 }
 
 // FP64 CG driven from the host: three launches per iteration and a read of the
@@ -1244,10 +1616,18 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
         const double* val = c->ls->values;
         const double* b = c->ls->rhs;
         int nvb = c->nb;
+        const bool mixed = cfg->precision == FVGB_PREC_MIXED_IR;
+        const int pg = persistent_grid(c, mixed);
+        const int grid = nvb < pg ? nvb : pg;
         FVGB_CUDA_TRY(cudaMemsetAsync(c->bar, 0, sizeof(GridBar), s));
-        void* args[] = {&L, &m, &val, &b, &c->dinv, &c->r, &c->p, &c->q, &c->z, &c->pa, &c->pb, &c->bar, &nvb};
-        const int grid = c->nb < c->persistent_grid ? c->nb : c->persistent_grid;
-        FVGB_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_pcg_persistent, dim3(grid), dim3(kT), args, 0, s));
+        if (mixed) {
+            void* args[] = {&L,    &m,     &val,   &b,    &c->ah, &c->ev, &c->dinvf, &c->rh, &c->y,
+                            &c->pf, &c->pf2, &c->zf, &c->qf, &c->pa, &c->pb, &c->pc,    &c->bar, &nvb};
+            FVGB_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_ir_persistent, dim3(grid), dim3(kPT), args, 0, s));
+        } else {
+            void* args[] = {&L, &m, &val, &b, &c->dinv, &c->r, &c->p, &c->q, &c->z, &c->pa, &c->pb, &c->bar, &nvb};
+            FVGB_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_pcg_persistent, dim3(grid), dim3(kPT), args, 0, s));
+        }
         k_finish<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L);
         FVGB_LAUNCH_CHECK("fvgb_solve: finish");
         return FVGB_OK;

@@ -371,7 +371,8 @@ typedef struct fvgb_serve_request {
     double D;
     double dt;
     int32_t precision;         /* FVGB_PREC_FP64 or FVGB_PREC_MIXED_IR                */
-    int32_t kernel_mode;       /* fvgb_solver_cfg.kernel_mode of every solve          */
+    int32_t kernel_mode;       /* fvgb_solver_cfg.kernel_mode of every solve; 0 picks
+                                  the graph path (requests overlap on the device)     */
     double* T_out;
 } fvgb_serve_request;
 typedef struct fvgb_serve_result {

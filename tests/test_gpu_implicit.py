@@ -211,6 +211,27 @@ def test_persistent_graph_and_host_loop_agree(cuda):
         assert out[0][1:] == other[1:]
 
 
+@pytest.mark.parametrize("shape", [(40, 32, 24), (7, 5, 3)])
+def test_mixed_persistent_and_graph_agree(cuda, shape):
+    """The cooperative mixed-precision solve (two grid barriers per inner
+    iteration, the direction folded into the SpMV) gives the bits of the graph
+    of kernels and of the oracle."""
+    hm, dm, T, o, ls, v, r = solve_case(*shape)
+    kw = dict(rel_tol=1e-9, inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50)
+    out = []
+    for mode in (1, 2):
+        x = T.internal.clone()
+        st = ls.solve(x, precision=abi.PREC_MIXED_IR, kernel_mode=mode, max_iter=4000, **kw)
+        assert st.status == abi.OK
+        out.append((x.cpu().numpy(), st.num_iter, st.num_outer, st.final_res_norm))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert out[0][1:] == out[1][1:]
+    xo = np.full(hm.n, 300.0)
+    so = o.solve(v, r, xo, precision=1, max_iter=4000, **kw)
+    assert (so.num_iter, so.num_outer) == out[0][1:3]
+    np.testing.assert_array_equal(out[0][0], xo)
+
+
 def test_host_loop_is_fp64_only(cuda):
     hm, dm, T, o, ls, v, r = solve_case(6, 6, 6)
     with pytest.raises(RuntimeError):
