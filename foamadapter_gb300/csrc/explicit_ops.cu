@@ -18,39 +18,87 @@ __device__ __forceinline__ int gwidth(const MeshView& m, int slice) {
     return (__ldg(&m.g_ptr[slice + 1]) - __ldg(&m.g_ptr[slice])) >> 5;
 }
 
+// F >= 0.0 with IEEE semantics (true for +0 and -0 and +inf, false for NaN),
+// decided on the bit pattern so it costs no FP64 instruction: GB300 issues
+// FP64 at 2 lanes per clock per SM, which bounds every FP64 face loop here.
+__device__ __forceinline__ bool nonneg(double F) {
+    const long long u = __double_as_longlong(F);
+    return u >= 0 ? u <= 0x7ff0000000000000LL : u == (long long)0x8000000000000000ULL;
+}
+
+// s - x is by definition s + (-x); negating the addend (a sign-bit flip) lets
+// the owner/neighbour accumulation be ONE FP64 addition instead of an addition
+// and a subtraction of which one is selected.
+__device__ __forceinline__ double signed_term(bool plus, double x) { return plus ? x : -x; }
+
 // ---------------------------------------------------------------- interpolation
+// Face kernels: a thread handles kFPT faces spaced a block apart (coalesced
+// across the block) and issues the loads of all of them before the dependent
+// cell gathers, so each thread keeps several faces' bytes in flight.
+constexpr int kFPT = 4;
+
+__device__ __forceinline__ int face_of(int k) { return (blockIdx.x * kFPT + k) * blockDim.x + threadIdx.x; }
+
 template <int NC>
-__global__ void k_interp_linear(MeshView m, const double* __restrict__ src,
-                                const double* __restrict__ src_b, double* __restrict__ dst) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f < m.nif) {
-        int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
-        double w = __ldg(&m.w[f]);
+__global__ void __launch_bounds__(kThreads)
+    k_interp_linear(MeshView m, const double* __restrict__ src, const double* __restrict__ src_b,
+                    double* __restrict__ dst) {
+    int P[kFPT], N[kFPT];
+    double w[kFPT];
 #pragma unroll
-        for (int k = 0; k < NC; ++k) {
-            double sN = __ldg(&src[N * NC + k]);
-            dst[f * NC + k] = w * (__ldg(&src[P * NC + k]) - sN) + sN;
+    for (int k = 0; k < kFPT; ++k) {
+        const int f = face_of(k);
+        P[k] = N[k] = 0;
+        w[k] = 0.0;
+        if (f < m.nif) {
+            P[k] = __ldg(&m.own[f]);
+            N[k] = __ldg(&m.nei[f]);
+            w[k] = __ldg(&m.w[f]);
         }
-    } else if (f < m.nif + m.nbf) {
-        int b = f - m.nif;
+    }
 #pragma unroll
-        for (int k = 0; k < NC; ++k) dst[f * NC + k] = __ldg(&src_b[b * NC + k]);
+    for (int k = 0; k < kFPT; ++k) {
+        const int f = face_of(k);
+        if (f < m.nif) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const double sN = __ldg(&src[N[k] * NC + c]);
+                dst[f * NC + c] = w[k] * (__ldg(&src[P[k] * NC + c]) - sN) + sN;
+            }
+        } else if (f < m.nif + m.nbf) {
+            const int b = f - m.nif;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) dst[f * NC + c] = __ldg(&src_b[b * NC + c]);
+        }
     }
 }
 
 template <int NC>
-__global__ void k_interp_upwind(MeshView m, const double* __restrict__ flux,
-                                const double* __restrict__ src, const double* __restrict__ src_b,
-                                double* __restrict__ dst) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f < m.nif) {
-        int c = __ldg(&flux[f]) >= 0.0 ? __ldg(&m.own[f]) : __ldg(&m.nei[f]);
+__global__ void __launch_bounds__(kThreads)
+    k_interp_upwind(MeshView m, const double* __restrict__ flux, const double* __restrict__ src,
+                    const double* __restrict__ src_b, double* __restrict__ dst) {
+    int cidx[kFPT];
 #pragma unroll
-        for (int k = 0; k < NC; ++k) dst[f * NC + k] = __ldg(&src[c * NC + k]);
-    } else if (f < m.nif + m.nbf) {
-        int b = f - m.nif;
+    for (int k = 0; k < kFPT; ++k) {
+        const int f = face_of(k);
+        cidx[k] = 0;
+        if (f < m.nif) {
+            const double F = __ldg(&flux[f]);
+            const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
+            cidx[k] = nonneg(F) ? P : N;
+        }
+    }
 #pragma unroll
-        for (int k = 0; k < NC; ++k) dst[f * NC + k] = __ldg(&src_b[b * NC + k]);
+    for (int k = 0; k < kFPT; ++k) {
+        const int f = face_of(k);
+        if (f < m.nif) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) dst[f * NC + c] = __ldg(&src[cidx[k] * NC + c]);
+        } else if (f < m.nif + m.nbf) {
+            const int b = f - m.nif;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) dst[f * NC + c] = __ldg(&src_b[b * NC + c]);
+        }
     }
 }
 
@@ -103,10 +151,9 @@ __device__ __forceinline__ void div_entry(const MeshView& m, int code, double F,
         const double Town = isOwner ? Tc[k] : To[k];
         const double Tnei = isOwner ? To[k] : Tc[k];
         double tf;
-        if (SCHEME == FVGB_SCHEME_UPWIND) tf = F >= 0.0 ? Town : Tnei;
+        if (SCHEME == FVGB_SCHEME_UPWIND) tf = nonneg(F) ? Town : Tnei;
         else tf = wf * (Town - Tnei) + Tnei;
-        const double fl = F * tf;
-        s[k] = isOwner ? s[k] + fl : s[k] - fl;
+        s[k] = s[k] + signed_term(isOwner, F * tf);
     }
 }
 
@@ -214,18 +261,9 @@ __device__ __forceinline__ void grad_entry(const MeshView& m, int code, double T
     const double Town = isOwner ? Tc : To;
     const double Tnei = isOwner ? To : Tc;
     const double tf = wf * (Town - Tnei) + Tnei;
-    const double v0 = S[0] * tf;
-    const double v1 = S[1] * tf;
-    const double v2 = S[2] * tf;
-    if (isOwner) {
-        g0 = g0 + v0;
-        g1 = g1 + v1;
-        g2 = g2 + v2;
-    } else {
-        g0 = g0 - v0;
-        g1 = g1 - v1;
-        g2 = g2 - v2;
-    }
+    g0 = g0 + signed_term(isOwner, S[0] * tf);
+    g1 = g1 + signed_term(isOwner, S[1] * tf);
+    g2 = g2 + signed_term(isOwner, S[2] * tf);
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -285,10 +323,12 @@ __device__ __forceinline__ void lap_entry(const MeshView& m, int code, double g,
         for (int k = 0; k < NC; ++k) s[k] = s[k] + g * (To[k] - Tc[k]);
         return;
     }
+    const bool isOwner = code >= 0;
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
-        if (code >= 0) s[k] = s[k] + g * (To[k] - Tc[k]);
-        else s[k] = s[k] - g * (Tc[k] - To[k]);
+        // owner: s + g*(To - Tc); neighbour: s - g*(Tc - To), the reference's face flux
+        const double a = isOwner ? To[k] : Tc[k], b = isOwner ? Tc[k] : To[k];
+        s[k] = s[k] + signed_term(isOwner, g * (a - b));
     }
 }
 
@@ -345,14 +385,30 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // --------------------------------------------------------------------- snGrad
-__global__ void k_sngrad(MeshView m, const double* __restrict__ phi,
-                         const double* __restrict__ phi_b, double* __restrict__ out) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f < m.nif) {
-        out[f] = __ldg(&m.delta[f]) * (__ldg(&phi[__ldg(&m.nei[f])]) - __ldg(&phi[__ldg(&m.own[f])]));
-    } else if (f < m.nif + m.nbf) {
-        const int b = f - m.nif;
-        out[f] = __ldg(&m.bdelta[b]) * (__ldg(&phi_b[b]) - __ldg(&phi[__ldg(&m.bcells[b])]));
+__global__ void __launch_bounds__(kThreads)
+    k_sngrad(MeshView m, const double* __restrict__ phi, const double* __restrict__ phi_b, double* __restrict__ out) {
+    int P[kFPT], N[kFPT];
+    double d[kFPT];
+#pragma unroll
+    for (int k = 0; k < kFPT; ++k) {
+        const int f = face_of(k);
+        P[k] = N[k] = 0;
+        d[k] = 0.0;
+        if (f < m.nif) {
+            P[k] = __ldg(&m.own[f]);
+            N[k] = __ldg(&m.nei[f]);
+            d[k] = __ldg(&m.delta[f]);
+        } else if (f < m.nif + m.nbf) {
+            const int b = f - m.nif;
+            P[k] = __ldg(&m.bcells[b]);
+            d[k] = __ldg(&m.bdelta[b]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kFPT; ++k) {
+        const int f = face_of(k);
+        if (f < m.nif) out[f] = d[k] * (__ldg(&phi[N[k]]) - __ldg(&phi[P[k]]));
+        else if (f < m.nif + m.nbf) out[f] = d[k] * (__ldg(&phi_b[f - m.nif]) - __ldg(&phi[P[k]]));
     }
 }
 
@@ -370,8 +426,9 @@ extern "C" fvgb_status fvgb_interp_linear(const fvgb_mesh* m, int32_t nc, const 
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     if (nf == 0) return FVGB_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    if (nc == 1) k_interp_linear<1><<<grid_for(nf, kThreads), kThreads, 0, s>>>(m->v, src, src_b, dst);
-    else k_interp_linear<3><<<grid_for(nf, kThreads), kThreads, 0, s>>>(m->v, src, src_b, dst);
+    const unsigned g = grid_for(nf, kThreads * kFPT);
+    if (nc == 1) k_interp_linear<1><<<g, kThreads, 0, s>>>(m->v, src, src_b, dst);
+    else k_interp_linear<3><<<g, kThreads, 0, s>>>(m->v, src, src_b, dst);
     FVGB_LAUNCH_CHECK("fvgb_interp_linear");
     return FVGB_OK;
 }
@@ -384,10 +441,9 @@ extern "C" fvgb_status fvgb_interp_upwind(const fvgb_mesh* m, int32_t nc, const 
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     if (nf == 0) return FVGB_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    if (nc == 1)
-        k_interp_upwind<1><<<grid_for(nf, kThreads), kThreads, 0, s>>>(m->v, flux, src, src_b, dst);
-    else
-        k_interp_upwind<3><<<grid_for(nf, kThreads), kThreads, 0, s>>>(m->v, flux, src, src_b, dst);
+    const unsigned g = grid_for(nf, kThreads * kFPT);
+    if (nc == 1) k_interp_upwind<1><<<g, kThreads, 0, s>>>(m->v, flux, src, src_b, dst);
+    else k_interp_upwind<3><<<g, kThreads, 0, s>>>(m->v, flux, src, src_b, dst);
     FVGB_LAUNCH_CHECK("fvgb_interp_upwind");
     return FVGB_OK;
 }
@@ -445,7 +501,7 @@ extern "C" fvgb_status fvgb_sngrad(const fvgb_mesh* m, const double* phi, const 
     FVGB_CHECK_ARG(phi && out && (phi_b || m->v.nbf == 0), "fvgb_sngrad: null field");
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     if (nf == 0) return FVGB_OK;
-    k_sngrad<<<grid_for(nf, kThreads), kThreads, 0, (cudaStream_t)stream>>>(m->v, phi, phi_b, out);
+    k_sngrad<<<grid_for(nf, kThreads * kFPT), kThreads, 0, (cudaStream_t)stream>>>(m->v, phi, phi_b, out);
     FVGB_LAUNCH_CHECK("fvgb_sngrad");
     return FVGB_OK;
 }
