@@ -838,11 +838,21 @@ __device__ __forceinline__ double spmv_row_cg(const MeshView& m, const double* _
     return s;
 }
 
+// Thread 0 of every block keeps the solver scalars; the other threads read
+// what a phase needs from shared memory after a barrier (FP64 division and
+// square root are long FP64 sequences: evaluated by every thread they would
+// cost more FP64 issue than the iteration's arithmetic).
+struct PcgShared {
+    double alpha, beta;
+    int done;
+};
+
 __global__ void __launch_bounds__(kPT, 1)
     k_pcg_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
                      double* dinv, double* r, double* p, double* q, double* z, double* pa, double* pb, GridBar* gb,
                      int nvb) {
     __shared__ double sA[kPT], sB[kPT], sm[kT], sm2[kT], cell;
+    __shared__ PcgShared sh;
     const int n = m.n, T = threadIdx.x;
     const SolverParams prm = L.bs->prm;
     double* x = prm.x;
@@ -879,21 +889,26 @@ __global__ void __launch_bounds__(kPT, 1)
         }
     }
     bool aborted = !grid_sync(gb, ++epoch * G);
-    double rz = 0.0, rr = 0.0;
+    // solver scalars: meaningful in thread 0 only
+    double rz = 0.0, res0 = 0.0, res = 0.0, tol = 0.0;
+    int iter = 0, status = FVGB_OK;
     if (!aborted) {
         rz = final_all(pa, nvb, sm, &cell);
-        rr = final_all(pb, nvb, sm, &cell);
+        const double rr = final_all(pb, nvb, sm, &cell);
+        if (T == 0) {
+            res0 = res = sqrt(rr);
+            tol = prm.rel_tol * res0;
+            if (prm.abs_tol > tol) tol = prm.abs_tol;
+            bool done = !(res0 > tol) || res0 == 0.0;
+            if (!done && prm.max_iter <= 0) {
+                done = true;
+                status = FVGB_ERR_NOT_CONVERGED;
+            }
+            sh.done = done;
+        }
+        __syncthreads();
     }
-    const double res0 = sqrt(rr);
-    double tol = prm.rel_tol * res0;
-    if (prm.abs_tol > tol) tol = prm.abs_tol;
-    double res = res0;
-    int iter = 0, status = FVGB_OK;
-    bool done = aborted || !(res0 > tol) || res0 == 0.0;
-    if (!done && prm.max_iter <= 0) {
-        done = true;
-        status = FVGB_ERR_NOT_CONVERGED;
-    }
+    bool done = aborted || sh.done;
     while (!done) {
         // q = A p, p.q
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
@@ -922,11 +937,18 @@ __global__ void __launch_bounds__(kPT, 1)
             break;
         }
         const double pq = final_all(pa, nvb, sm, &cell);
-        const double alpha = rz / pq;
-        if (pq == 0.0 || !isfinite(alpha)) {
-            status = FVGB_ERR_BREAKDOWN;
-            break;
+        if (T == 0) {
+            const double alpha = rz / pq;
+            sh.alpha = alpha;
+            sh.done = 0;
+            if (pq == 0.0 || !isfinite(alpha)) {
+                status = FVGB_ERR_BREAKDOWN;
+                sh.done = 1;
+            }
         }
+        __syncthreads();
+        if (sh.done) break;
+        const double alpha = sh.alpha;
         // x += alpha p, r -= alpha q, z = dinv r, r.z, r.r
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
             const int i = vb * kRowsPerBlock + T;
@@ -961,20 +983,27 @@ __global__ void __launch_bounds__(kPT, 1)
             break;
         }
         const double rzn = final_all(pa, nvb, sm, &cell);
-        rr = final_all(pb, nvb, sm, &cell);
-        res = sqrt(rr);
-        ++iter;
-        const double beta = rzn / rz;
-        rz = rzn;
-        if (!isfinite(res)) {
-            status = FVGB_ERR_BREAKDOWN;
-            break;
+        const double rr = final_all(pb, nvb, sm, &cell);
+        if (T == 0) {
+            res = sqrt(rr);
+            ++iter;
+            sh.beta = rzn / rz;
+            rz = rzn;
+            int d = 0;
+            if (!isfinite(res)) {
+                status = FVGB_ERR_BREAKDOWN;
+                d = 1;
+            } else if (!(res > tol)) {
+                d = 1;
+            } else if (iter >= prm.max_iter) {
+                status = FVGB_ERR_NOT_CONVERGED;
+                d = 1;
+            }
+            sh.done = d;
         }
-        if (!(res > tol)) break;
-        if (iter >= prm.max_iter) {
-            status = FVGB_ERR_NOT_CONVERGED;
-            break;
-        }
+        __syncthreads();
+        if (sh.done) break;
+        const double beta = sh.beta;
         // p = z + beta p
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
             const int i = vb * kRowsPerBlock + T;
@@ -1038,6 +1067,15 @@ __device__ __forceinline__ float spmv_row_diff_dir(const MeshView& m, const floa
     return fmaf(ei, xi, s);
 }
 
+// Scalars of the refinement live in thread 0 of every block (the graph path
+// keeps them in CaseState); what the phases need is broadcast here.
+struct IrShared {
+    double nsig, isig;  // scale of the residual being formed; 1/scale of the current y
+    float fa;           // alpha of the current inner iteration
+    DirMode dm;         // how the next SpMV forms the direction
+    int done, inner, brk;
+};
+
 __global__ void __launch_bounds__(kPT, 1)
     k_ir_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
                     float* a32, float* ev, float* dinv, float* rh, float* y, float* pbuf0, float* pbuf1, float* z,
@@ -1045,6 +1083,7 @@ __global__ void __launch_bounds__(kPT, 1)
     __shared__ double sD[kPT], sm[kT], sm2[kT], sm3[kT], cell;
     __shared__ float sF1[kPT], sF2[kPT], smf[kT];
     __shared__ unsigned int sflags;
+    __shared__ IrShared sh;
     const int n = m.n, T = threadIdx.x;
     const SolverParams prm = L.bs->prm;
     double* x = prm.x;
@@ -1096,45 +1135,58 @@ __global__ void __launch_bounds__(kPT, 1)
         const double ba = tree256(asr, sm);
         if (T == 0) pa[vb] = ba;
     }
+    __syncthreads();
     if (T == 0 && sflags) atomicOr(&cs->signflags, sflags);
     aborted = !grid_sync(gb, ++epoch * G);
-    double sres = aborted ? 0.0 : sqrt(final_all(pa, nvb, sm, &cell));
-    double sig = 1.0, isig = 1.0;
-    const unsigned int flags = *(volatile unsigned int*)&cs->signflags;
-    // refinement state (the graph path keeps it in CaseState)
-    double res0 = 0.0, res = 0.0, tol = 0.0, rho = 0.0, rho_prev = 0.0, itol = 0.0;
+    // refinement state, meaningful in thread 0 only
+    double sres = 0.0, sig = 1.0, isig = 1.0, res0 = 0.0, res = 0.0, tol = 0.0, rho = 0.0, rho_prev = 0.0,
+           itol = 0.0;
     int total = 0, outer = 0, inner_it = 0, status = FVGB_OK;
+    unsigned int flags = 0u;
+    if (!aborted) {
+        const double s2 = final_all(pa, nvb, sm, &cell);
+        if (T == 0) {
+            sres = sqrt(s2);
+            flags = *(volatile unsigned int*)&cs->signflags;
+        }
+    }
     float* pcur = pbuf0;
     float* pnext = pbuf1;
-    DirMode dm{0, 0.0f};
-    bool first = true, done = aborted, inner = false;
+    bool first = true;
+    bool done = aborted;
     while (!done) {
         if (!first) {
             // x += y / sig
+            const double is = sh.isig;
             for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
                 const int i = vb * kRowsPerBlock + T;
-                if (i < n) x[i] = fma((double)__ldcg(&y[i]), isig, __ldcg(&x[i]));
+                if (i < n) x[i] = fma((double)__ldcg(&y[i]), is, __ldcg(&x[i]));
             }
             if (!grid_sync(gb, ++epoch * G)) {
                 aborted = true;
                 break;
             }
         }
+        if (T == 0) {
+            double nsig, nisig;
+            residual_scale(sres, &nsig, &nisig);
+            sh.nsig = nsig;
+        }
+        __syncthreads();
+        const double nsig_all = sh.nsig;
         // residual: r = b - A x (FP64), rh = sign*(float)(sig r), y = 0, z = |dinv| rh
-        double nsig, nisig;
-        residual_scale(sres, &nsig, &nisig);
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
             const int i = vb * kRowsPerBlock + T;
             double ri = 0.0;
-            float di = 0.0f, rhi = 0.0f, zi = 0.0f;
+            float di = 0.0f, rhi = 0.0f;
             if (i < n) {
                 ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
                 di = __ldcg(&dinv[i]);
-                rhi = (float)(ri * nsig);
+                rhi = (float)(ri * nsig_all);
                 if (di < 0.0f) rhi = -rhi;
                 rh[i] = rhi;
                 y[i] = 0.0f;
-                zi = fabsf(di) * rhi;
+                const float zi = fabsf(di) * rhi;
                 z[i] = zi;
                 if (first) pcur[i] = zi;
             }
@@ -1166,10 +1218,13 @@ __global__ void __launch_bounds__(kPT, 1)
             aborted = true;
             break;
         }
-        {
-            const double rr = final_all(pa, nvb, sm, &cell);
-            const double nrho = final_all(pb, nvb, sm, &cell);
-            const double sr2 = final_all(pc, nvb, sm, &cell);
+        const double rr = final_all(pa, nvb, sm, &cell);
+        const double nrho = final_all(pb, nvb, sm, &cell);
+        const double sr2 = final_all(pc, nvb, sm, &cell);
+        if (T == 0) {
+            double nsig, nisig;
+            residual_scale(sres, &nsig, &nisig);
+            bool d = false;
             res = sqrt(rr);
             if (!first) outer += 1;
             if (first) {
@@ -1178,18 +1233,18 @@ __global__ void __launch_bounds__(kPT, 1)
                 if (prm.abs_tol > tol) tol = prm.abs_tol;
                 if ((flags & 4u) || flags == 3u) {
                     status = FVGB_ERR_UNSUPPORTED;
-                    done = true;
+                    d = true;
                 }
             }
-            if (!done) {
+            if (!d) {
                 if (!isfinite(res)) {
                     status = FVGB_ERR_BREAKDOWN;
-                    done = true;
+                    d = true;
                 } else if (!(res > tol) || res == 0.0) {
-                    done = true;
+                    d = true;
                 } else if (outer >= prm.max_outer || total >= prm.max_iter) {
                     status = FVGB_ERR_NOT_CONVERGED;
-                    done = true;
+                    d = true;
                 }
             }
             const double g = nsig * isig;
@@ -1204,12 +1259,17 @@ __global__ void __launch_bounds__(kPT, 1)
             const double dt = (tol / res) * (tol / res);
             itol = rho * (dr > dt ? dr : dt);
             inner_it = 0;
-            inner = !done && rho > itol && prm.inner_max_iter > 0 && total < prm.max_iter;
-            dm = first ? DirMode{0, 0.0f} : (frel < 0.0f ? DirMode{1, 0.0f} : DirMode{2, frel});
-            first = false;
+            sh.inner = !d && rho > itol && prm.inner_max_iter > 0 && total < prm.max_iter;
+            sh.done = d;
+            sh.isig = isig;
+            sh.dm = first ? DirMode{0, 0.0f} : (frel < 0.0f ? DirMode{1, 0.0f} : DirMode{2, frel});
         }
+        __syncthreads();
+        first = false;
+        done = sh.done;
         if (done) break;
-        while (inner) {
+        while (sh.inner) {
+            const DirMode dm = sh.dm;
             // direction (into pnext unless p is taken as stored), q = A p, p.q
             for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
                 const int i = vb * kRowsPerBlock + T;
@@ -1243,16 +1303,23 @@ __global__ void __launch_bounds__(kPT, 1)
                 break;
             }
             const double pq = final_all(pa, nvb, sm, &cell);
-            const double alpha = rho / pq;
-            if (pq == 0.0 || !isfinite(alpha)) {
-                inner = false;
-                if (inner_it == 0) {
-                    status = FVGB_ERR_BREAKDOWN;
-                    done = true;
+            if (T == 0) {
+                const double alpha = rho / pq;
+                sh.brk = 0;
+                if (pq == 0.0 || !isfinite(alpha)) {
+                    sh.brk = 1;
+                    sh.inner = 0;
+                    if (inner_it == 0) {
+                        status = FVGB_ERR_BREAKDOWN;
+                        sh.done = 1;
+                    }
+                } else {
+                    sh.fa = (float)alpha;
                 }
-                break;
             }
-            const float fa = (float)alpha;
+            __syncthreads();
+            if (sh.brk) break;
+            const float fa = sh.fa;
             // y += alpha p, rh -= alpha q, z = |dinv| rh, rh.z
             for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
                 const int i = vb * kRowsPerBlock + T;
@@ -1282,15 +1349,19 @@ __global__ void __launch_bounds__(kPT, 1)
                 break;
             }
             const double rhon = final_all(pa, nvb, sm, &cell);
-            const float fbeta = (float)(rhon / rho);
-            rho_prev = rho;
-            rho = rhon;
-            inner_it += 1;
-            total += 1;
-            inner = rhon > itol && inner_it < prm.inner_max_iter && total < prm.max_iter;
-            dm = DirMode{2, fbeta};
+            if (T == 0) {
+                const float fbeta = (float)(rhon / rho);
+                rho_prev = rho;
+                rho = rhon;
+                inner_it += 1;
+                total += 1;
+                sh.inner = rhon > itol && inner_it < prm.inner_max_iter && total < prm.max_iter;
+                sh.dm = DirMode{2, fbeta};
+            }
+            __syncthreads();
         }
         if (aborted) break;
+        done = sh.done;
     }
     if (blockIdx.x == 0 && T == 0) {
         cs->res0 = res0;
