@@ -376,6 +376,15 @@ def run_explicit(args):
     L, h, s = abi.lib(), dm.handle, torch.cuda.current_stream().cuda_stream
     P = abi.ptr
     bc = T.bc_struct()
+    # FP64 operations of the reference's face loop (each face's value and flux formed
+    # once, added to the owner and subtracted from the neighbour, then the 1/V scale)
+    fp64 = {"interp_linear": 3 * nif, "interp_upwind": 0, "div_upwind": 3 * nif + 2 * nbf + 2 * n,
+            "div_linear": 6 * nif + 2 * nbf + 2 * n, "grad": 12 * nif + 6 * nbf + 6 * n,
+            "laplacian": 5 * nif + 4 * nbf + 2 * n, "sngrad": 2 * (nif + nbf),
+            "advect_euler": 3 * nif + 2 * nbf + 4 * n}
+    sm_mhz = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("sm_max_mhz", 2070.0) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else 2070.0
+    fp64_peak = 2 * torch.cuda.get_device_properties(0).multi_processor_count * sm_mhz * 1e6
     ops = {
         "interp_linear": (lambda: L.fvgb_interp_linear(h, 1, P(T.internal), P(T.boundary), P(fout), s),
                           24 * nif + 8 * n + 16 * nbf),
@@ -414,9 +423,12 @@ def run_explicit(args):
             times.append(e0.elapsed_time(e1))
         us = 1e3 * float(np.median(times))
         gbs = nbytes / (us * 1e-6) / 1e9
-        res[name] = {"us": us, "alg_bytes": nbytes, "GBps": gbs, "frac_of_peak": gbs / peak}
+        res[name] = {"us": us, "alg_bytes": nbytes, "GBps": gbs, "frac_of_peak": gbs / peak,
+                     "fp64_ops": fp64[name], "fp64_frac_of_peak": fp64[name] / (us * 1e-6) / fp64_peak}
     return {"workload": f"explicit operators, {args.explicit_n}^3 jittered box, one launch each, L2 flushed",
             "n": n, "n_ifaces": nif, "n_bfaces": nbf, "peak_GBps": peak, "peak_source": peak_kind,
+            "fp64_peak_ops_per_s": fp64_peak,
+            "fp64_peak_source": "2 FP64 lanes per clock per SM (ncu peak_sustained) x SMs x max SM clock",
             "timing": "median of CUDA-event times of single launches, 512 MB written between launches",
             "ops": res}
 
