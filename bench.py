@@ -213,9 +213,16 @@ def run_gpu(args, rank, world):
     abi.check(L.fvgb_solve_kernel_times(ls.handle, abi.ptr(T.internal), 30, kt, stream))
     # ---- FP64 vs mixed-precision solve of one step's system
     mixed = compare_precisions(torch, abi, L, ls, T, T_old, tarr, bc, dm, hm, stream)
+    # ---- the autotuner's choices for this system (timed at its first solve)
+    chosen, tms = (C.c_int32 * 4)(), (C.c_float * 16)()
+    abi.check(L.fvgb_solve_tuning(ls.handle, None, chosen, tms))
+    kinds = ["fp64_spmv", "fp64_update", "fp32_spmv", "fp32_update"]
+    tuning = {k: {"min_blocks_per_sm": int(chosen[i]),
+                  "ms_by_min_blocks": {str(b): round(float(tms[4 * i + j]), 5) for j, b in enumerate((2, 4, 6, 8))}}
+              for i, k in enumerate(kinds)}
     result = dict(ms=ms, iters=iters, e2e_ms=e2e_ms, e2e_iters=e2e_iters, kt=list(kt), clocks=clk.summary(),
                   mixed=mixed, face_updates=face_updates, warm_iters=[s.num_iter for s in warm_stats],
-                  mesh_bytes=dm.device_bytes())
+                  mesh_bytes=dm.device_bytes(), tuning=tuning)
     return hm, result
 
 
@@ -750,6 +757,7 @@ def main():
         "clocks": r["clocks"],
         "pcg_iterations_per_step": r["iters"],
         "mixed_precision": r["mixed"],
+        "autotune": r["tuning"],
     }
     if not args.no_cpu and world == 1:
         from oracle.pyoracle import set_threads  # noqa: F401

@@ -111,6 +111,7 @@ _SIGS = {
     "fvgb_solve": (C.c_int, [vp, vp, C.POINTER(SolverCfg), C.POINTER(SolverStats), vp]),
     "fvgb_solve_async": (C.c_int, [vp, vp, C.POINTER(SolverCfg), vp, vp]),
     "fvgb_solve_kernel_times": (C.c_int, [vp, vp, i32, vp, vp]),
+    "fvgb_solve_tuning": (C.c_int, [vp, vp, vp, vp]),
     "fvgb_batch_create": (C.c_int, [vp, i32, vp, C.POINTER(vp)]),
     "fvgb_batch_destroy": (C.c_int, [vp]),
     "fvgb_batch_solve": (C.c_int, [vp, vp, C.POINTER(SolverCfg), vp, vp]),

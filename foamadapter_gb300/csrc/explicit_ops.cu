@@ -26,10 +26,13 @@ __device__ __forceinline__ bool nonneg(double F) {
     return u >= 0 ? u <= 0x7ff0000000000000LL : u == (long long)0x8000000000000000ULL;
 }
 
-// s - x is by definition s + (-x); negating the addend (a sign-bit flip) lets
-// the owner/neighbour accumulation be ONE FP64 addition instead of an addition
-// and a subtraction of which one is selected.
-__device__ __forceinline__ double signed_term(bool plus, double x) { return plus ? x : -x; }
+// s - x is by definition s + (-x); negating the addend lets the owner/neighbour
+// accumulation be ONE FP64 addition instead of an addition and a subtraction of
+// which one is selected.  The negation is an integer XOR of the sign bit (IEEE
+// negation exactly), so it issues no FP64 instruction either.
+__device__ __forceinline__ double signed_term(bool plus, double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (plus ? 0LL : (long long)0x8000000000000000ULL));
+}
 
 // ---------------------------------------------------------------- interpolation
 // Face kernels: a thread handles kFPT faces spaced a block apart (coalesced

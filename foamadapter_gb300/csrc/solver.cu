@@ -36,6 +36,8 @@
 
 #include "internal.cuh"
 
+#include <algorithm>
+
 namespace {
 
 constexpr int kT = 256;
@@ -261,7 +263,8 @@ __global__ void __launch_bounds__(kT)
         cudaGraphSetConditional(h, ld_volatile(&L.bs->n_active) > 0 ? 1u : 0u);
 }
 
-__global__ void __launch_bounds__(kT)
+template <int MINB>
+__global__ void __launch_bounds__(kT, MINB)
     k_pcg_spmv(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ p,
                double* __restrict__ q, double* __restrict__ pa) {
     const Blk k = blk_info(L);
@@ -291,7 +294,8 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
-__global__ void __launch_bounds__(kT)
+template <int MINB>
+__global__ void __launch_bounds__(kT, MINB)
     k_pcg_update(Layout L, const double* __restrict__ dinv, const double* __restrict__ p,
                  const double* __restrict__ q, double* __restrict__ r, double* __restrict__ z,
                  double* __restrict__ pa, double* __restrict__ pb, cudaGraphConditionalHandle h, int setc) {
@@ -608,7 +612,8 @@ __device__ __forceinline__ void inner_stop(const Layout& L, CaseState* cs) {
 }
 
 // q = (D_s A) p in the difference form; p.q -> alpha
-__global__ void __launch_bounds__(kT)
+template <int MINB>
+__global__ void __launch_bounds__(kT, MINB)
     k_ir_spmv(Layout L, MeshView m, const float* __restrict__ a32, const float* __restrict__ ev,
               const float* __restrict__ p, float* __restrict__ q, double* __restrict__ pa) {
     const Blk k = blk_info(L);
@@ -645,10 +650,11 @@ __global__ void __launch_bounds__(kT)
 }
 
 // y += alpha p, rh -= alpha q, rho = rh . (|dinv| rh)
-__global__ void __launch_bounds__(kT)
+template <int MINB>
+__global__ void __launch_bounds__(kT, MINB)
     k_ir_update(Layout L, const float* __restrict__ dinv, const float* __restrict__ p, const float* __restrict__ q,
                 float* __restrict__ y, float* __restrict__ rh, double* __restrict__ pa,
-                cudaGraphConditionalHandle h_inner) {
+                cudaGraphConditionalHandle h_inner, int setc) {
     __shared__ double sma[kT];
     __shared__ float smf[kT];
     const Blk k = blk_info(L);
@@ -682,7 +688,7 @@ __global__ void __launch_bounds__(kT)
             }
         }
     }
-    if (arrive_last(&L.bs->gcounter, gridDim.x) && threadIdx.x == 0)
+    if (arrive_last(&L.bs->gcounter, gridDim.x) && threadIdx.x == 0 && setc)
         cudaGraphSetConditional(h_inner, ld_volatile(&L.bs->n_inner) > 0 ? 1u : 0u);
 }
 
@@ -714,6 +720,66 @@ __global__ void __launch_bounds__(kT) k_ir_xupdate(Layout L, const float* __rest
         if (i >= k.end) continue;
         x[i] = fma((double)__ldg(&y[i]), isig, x[i]);
     }
+}
+
+// State for timing the FP32 kernels outside a solve: every case's inner solve
+// active with rho = 1, a direction of pseudo-random O(1) values.
+__global__ void k_tune_mixed_state(Layout L, float* __restrict__ p, float* __restrict__ rh, float* __restrict__ y) {
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (threadIdx.x == 0 && blockIdx.x == __ldg(&L.case_blk0[k.c])) {
+        cs->inner_active = 1;
+        cs->rho = 1.0;
+        cs->itol = 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const unsigned int hsh = (unsigned int)i * 2654435761u;
+        p[i] = 0.5f + (float)(hsh >> 8) * (1.0f / 16777216.0f);
+        rh[i] = 1.0f;
+        y[i] = 0.0f;
+    }
+}
+
+// ------------------------------------------------------------ kernel variants
+// The SpMV and update kernels of both solves exist in launch-bound variants
+// (minimum resident blocks per SM 2, 4, 6, 8: a register budget of 128, 64,
+// 42, 32 per thread).  They execute the same instructions in the same order on
+// the same data, so every variant gives the same bits; which one is fastest
+// depends on the mesh (row width, size against L2).  The autotuner below times
+// them on the system being solved and the graphs are built with the winner.
+constexpr int kNumVariants = 4;
+constexpr int kVariantMinBlocks[kNumVariants] = {2, 4, 6, 8};
+enum { kTuneSpmv64 = 0, kTuneUpdate64 = 1, kTuneSpmvMixed = 2, kTuneUpdateMixed = 3, kTuneKinds = 4 };
+
+const void* variant_fn(int kind, int v) {
+    switch (kind * kNumVariants + v) {
+        case 0: return (const void*)k_pcg_spmv<2>;
+        case 1: return (const void*)k_pcg_spmv<4>;
+        case 2: return (const void*)k_pcg_spmv<6>;
+        case 3: return (const void*)k_pcg_spmv<8>;
+        case 4: return (const void*)k_pcg_update<2>;
+        case 5: return (const void*)k_pcg_update<4>;
+        case 6: return (const void*)k_pcg_update<6>;
+        case 7: return (const void*)k_pcg_update<8>;
+        case 8: return (const void*)k_ir_spmv<2>;
+        case 9: return (const void*)k_ir_spmv<4>;
+        case 10: return (const void*)k_ir_spmv<6>;
+        case 11: return (const void*)k_ir_spmv<8>;
+        case 12: return (const void*)k_ir_update<2>;
+        case 13: return (const void*)k_ir_update<4>;
+        case 14: return (const void*)k_ir_update<6>;
+        default: return (const void*)k_ir_update<8>;
+    }
+}
+
+// Launch of a kernel variant; the arguments are passed with the kernel's exact parameter types.
+template <class... A>
+cudaError_t launch_variant(const void* fn, unsigned grid, cudaStream_t s, A... args) {
+    void* a[] = {(void*)&args...};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(kT), a, 0, s);
 }
 
 // ------------------------------------------------------ persistent solves (one case)
@@ -1416,6 +1482,10 @@ struct SolverCache {
     GridBar* bar = nullptr;
     float *pf2 = nullptr, *zf = nullptr;   // second direction buffer and z of the persistent mixed solve
     int pgrid_fp64 = 0, pgrid_mixed = 0;   // co-resident blocks of the persistent kernels (0: not asked yet)
+    int variant[kTuneKinds] = {1, 1, 1, 1};  // chosen launch-bound variant per kernel kind
+    int forced[kTuneKinds] = {-1, -1, -1, -1};
+    bool tuned64 = false, tunedmx = false;
+    float tune_ms[kTuneKinds][kNumVariants] = {};
     int32_t* h_active = nullptr;           // pinned copy of n_active for the host-driven loop
 };
 
@@ -1492,14 +1562,85 @@ fvgb_status cache_create(const fvgb_ls* ls, int ncases, const int32_t* ranges, S
     return FVGB_OK;
 }
 
-fvgb_status build_fp64(SolverCache* c) {
-    const size_t n = (size_t)c->n;
-    cudaError_t e = calloc_dev(c, &c->dinv, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->r, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->p, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->q, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->z, n);
-    if (e != cudaSuccess) return cuda_fail(e, "FP64 CG workspace");
+// ---------------------------------------------------------------- autotuner
+// Median of 3 timed launches (after one untimed) of `fn` on a private stream.
+float time_launch(const void* fn, unsigned grid, void** args, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1) {
+    float best[3] = {0, 0, 0};
+    cudaLaunchKernel(fn, dim3(grid), dim3(kT), args, 0, s);
+    for (int r = 0; r < 3; ++r) {
+        cudaEventRecord(e0, s);
+        cudaLaunchKernel(fn, dim3(grid), dim3(kT), args, 0, s);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&best[r], e0, e1);
+    }
+    std::sort(best, best + 3);
+    return best[1];
+}
+
+// Systems smaller than this keep the default variants (their solves run as a
+// persistent kernel or are launch bound).
+constexpr int kTuneMinRows = 1 << 18;
+
+void pick(SolverCache* c, int kind) {
+    int b = 1;
+    for (int v = 0; v < kNumVariants; ++v)
+        if (c->tune_ms[kind][v] > 0.0f && c->tune_ms[kind][v] < c->tune_ms[kind][b]) b = v;
+    c->variant[kind] = c->forced[kind] >= 0 ? c->forced[kind] : b;
+}
+
+// Times the FP64 SpMV and update variants on this system: CG iterations from a
+// zero vector (a scratch x, never the caller's), the solver state reset by the
+// next solve's parameter kernel.
+fvgb_status tune_fp64(SolverCache* c) {
+    c->tuned64 = true;
+    if (c->n >= kTuneMinRows) {
+        FVGB_CUDA_TRY(cudaDeviceSynchronize());  // the system's assembly may still run on the caller's stream
+        double* tmp = nullptr;
+        cudaStream_t s = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        cudaError_t e = cudaMalloc(&tmp, sizeof(double) * (size_t)c->n);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(tmp, 0, sizeof(double) * (size_t)c->n, s);
+        if (e == cudaSuccess) {
+            SolverParams prm{};
+            prm.x = tmp;
+            prm.max_iter = 1 << 30;
+            MeshView m = c->ls->mesh->v;
+            Layout L = c->L;
+            const double* val = c->ls->values;
+            const double* b = c->ls->rhs;
+            const cudaGraphConditionalHandle h{};
+            int setc = 0;
+            const unsigned nb = (unsigned)c->nb;
+            k_set_params<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L, c->ncases, prm);
+            k_pcg_init<<<nb, kT, 0, s>>>(c->L, m, val, b, c->dinv, c->r, c->p, c->pa, c->pb, h, 0);
+            void* a_spmv[] = {&L, &m, &val, &c->p, &c->q, &c->pa};
+            void* a_upd[] = {&L, &c->dinv, &c->p, &c->q, &c->r, &c->z, &c->pa, &c->pb, (void*)&h, &setc};
+            for (int v = 0; v < kNumVariants; ++v)
+                c->tune_ms[kTuneSpmv64][v] = time_launch(variant_fn(kTuneSpmv64, v), nb, a_spmv, s, e0, e1);
+            for (int v = 0; v < kNumVariants; ++v)
+                c->tune_ms[kTuneUpdate64][v] = time_launch(variant_fn(kTuneUpdate64, v), nb, a_upd, s, e0, e1);
+            e = cudaStreamSynchronize(s);
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (s) cudaStreamDestroy(s);
+        if (tmp) cudaFree(tmp);
+        if (e != cudaSuccess) return cuda_fail(e, "FP64 CG autotuning");
+    }
+    pick(c, kTuneSpmv64);
+    pick(c, kTuneUpdate64);
+    return FVGB_OK;
+}
+
+fvgb_status graph_fp64(SolverCache* c) {
+    if (c->g64) {
+        cudaGraphExecDestroy(c->g64);
+        c->g64 = nullptr;
+    }
     const fvgb_ls* ls = c->ls;
     MeshView m = ls->mesh->v;
     Layout L = c->L;
@@ -1512,7 +1653,7 @@ fvgb_status build_fp64(SolverCache* c) {
     const double* b = ls->rhs;
     const unsigned nb = (unsigned)c->nb;
     int setc = 1;
-    e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
     void* a_init[] = {&L, &m, &val, &b, &c->dinv, &c->r, &c->p, &c->pa, &c->pb, &h, &setc};
     void* a_spmv[] = {&L, &m, &val, &c->p, &c->q, &c->pa};
     void* a_upd[] = {&L, &c->dinv, &c->p, &c->q, &c->r, &c->z, &c->pa, &c->pb, &h, &setc};
@@ -1520,8 +1661,10 @@ fvgb_status build_fp64(SolverCache* c) {
     void* a_fin[] = {&L};
     if (e == cudaSuccess) e = add_kernel(g, &n0, nullptr, (void*)k_pcg_init, nb, kT, a_init);
     if (e == cudaSuccess) e = add_while(g, &n1, &n0, h, &body);
-    if (e == cudaSuccess) e = add_kernel(body, &b0, nullptr, (void*)k_pcg_spmv, nb, kT, a_spmv);
-    if (e == cudaSuccess) e = add_kernel(body, &b1, &b0, (void*)k_pcg_update, nb, kT, a_upd);
+    if (e == cudaSuccess)
+        e = add_kernel(body, &b0, nullptr, (void*)variant_fn(kTuneSpmv64, c->variant[kTuneSpmv64]), nb, kT, a_spmv);
+    if (e == cudaSuccess)
+        e = add_kernel(body, &b1, &b0, (void*)variant_fn(kTuneUpdate64, c->variant[kTuneUpdate64]), nb, kT, a_upd);
     if (e == cudaSuccess) e = add_kernel(body, &b2, &b1, (void*)k_pcg_dir, nb, kT, a_dir);
     if (e == cudaSuccess) e = add_kernel(g, &n2, &n1, (void*)k_finish, grid_for(c->ncases, 128), 128, a_fin);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->g64, g, 0);
@@ -1530,20 +1673,80 @@ fvgb_status build_fp64(SolverCache* c) {
     return FVGB_OK;
 }
 
-fvgb_status build_mixed(SolverCache* c) {
+fvgb_status build_fp64(SolverCache* c) {
     const size_t n = (size_t)c->n;
+    if (!c->dinv) {
+        cudaError_t e = calloc_dev(c, &c->dinv, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->r, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->p, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->q, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->z, n);
+        if (e != cudaSuccess) return cuda_fail(e, "FP64 CG workspace");
+    }
+    if (!c->tuned64) {
+        fvgb_status st = tune_fp64(c);
+        if (st != FVGB_OK) return st;
+    }
+    return graph_fp64(c);
+}
+
+// Times the FP32 SpMV and update variants of the mixed solve on this system
+// (after the preparation kernel, from a zero scratch vector).
+fvgb_status tune_mixed(SolverCache* c) {
+    c->tunedmx = true;
+    if (c->n >= kTuneMinRows) {
+        FVGB_CUDA_TRY(cudaDeviceSynchronize());
+        double* tmp = nullptr;
+        cudaStream_t s = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        cudaError_t e = cudaMalloc(&tmp, sizeof(double) * (size_t)c->n);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(tmp, 0, sizeof(double) * (size_t)c->n, s);
+        if (e == cudaSuccess) {
+            SolverParams prm{};
+            prm.x = tmp;
+            prm.max_iter = 1 << 30;
+            prm.inner_max_iter = 1 << 30;
+            prm.max_outer = 1 << 30;
+            prm.inner_rel_tol = 0.5;
+            MeshView m = c->ls->mesh->v;
+            Layout L = c->L;
+            const double* val = c->ls->values;
+            const double* b = c->ls->rhs;
+            const cudaGraphConditionalHandle h{};
+            int setc = 0;
+            const unsigned nb = (unsigned)c->nb;
+            k_set_params<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L, c->ncases, prm);
+            k_ir_prepare<<<nb, kT, 0, s>>>(c->L, m, val, b, c->ah, c->ev, c->dinvf, c->pa);
+            k_tune_mixed_state<<<nb, kT, 0, s>>>(c->L, c->pf, c->rh, c->y);
+            void* a_spmv[] = {&L, &m, &c->ah, &c->ev, &c->pf, &c->qf, &c->pa};
+            void* a_upd[] = {&L, &c->dinvf, &c->pf, &c->qf, &c->y, &c->rh, &c->pa, (void*)&h, &setc};
+            for (int v = 0; v < kNumVariants; ++v)
+                c->tune_ms[kTuneSpmvMixed][v] = time_launch(variant_fn(kTuneSpmvMixed, v), nb, a_spmv, s, e0, e1);
+            for (int v = 0; v < kNumVariants; ++v)
+                c->tune_ms[kTuneUpdateMixed][v] = time_launch(variant_fn(kTuneUpdateMixed, v), nb, a_upd, s, e0, e1);
+            e = cudaStreamSynchronize(s);
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (s) cudaStreamDestroy(s);
+        if (tmp) cudaFree(tmp);
+        if (e != cudaSuccess) return cuda_fail(e, "mixed CG autotuning");
+    }
+    pick(c, kTuneSpmvMixed);
+    pick(c, kTuneUpdateMixed);
+    return FVGB_OK;
+}
+
+fvgb_status graph_mixed(SolverCache* c) {
+    if (c->gmix) {
+        cudaGraphExecDestroy(c->gmix);
+        c->gmix = nullptr;
+    }
     const fvgb_ls* ls = c->ls;
     const fvgb_mesh* mesh = ls->mesh;
-    cudaError_t e = calloc_dev(c, &c->ah, (size_t)mesh->m_len);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->dinvf, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->ev, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->rh, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->y, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->pf, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->qf, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->pf2, n);
-    if (e == cudaSuccess) e = calloc_dev(c, &c->zf, n);
-    if (e != cudaSuccess) return cuda_fail(e, "mixed CG workspace");
     MeshView m = mesh->v;
     Layout L = c->L;
     cudaGraph_t g = nullptr;
@@ -1552,14 +1755,15 @@ fvgb_status build_mixed(SolverCache* c) {
     const double* val = ls->values;
     const double* b = ls->rhs;
     const unsigned nb = (unsigned)c->nb;
-    e = cudaGraphConditionalHandleCreate(&ho, g, 0, cudaGraphCondAssignDefault);
+    int setc = 1;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&ho, g, 0, cudaGraphCondAssignDefault);
     if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
     cudaGraphNode_t n_prep, n_res0, n_outer, n_fin, o_inner, o_x, o_res, o_dir, i_spmv, i_upd, i_dir;
     cudaGraph_t obody = nullptr, ibody = nullptr;
     void* a_prep[] = {&L, &m, &val, &b, &c->ah, &c->ev, &c->dinvf, &c->pa};
     void* a_res[] = {&L, &m, &val, &b, &c->dinvf, &c->rh, &c->y, &c->pf, &c->pa, &c->pb, &c->pc, &ho, &hi};
     void* a_spmv[] = {&L, &m, &c->ah, &c->ev, &c->pf, &c->qf, &c->pa};
-    void* a_upd[] = {&L, &c->dinvf, &c->pf, &c->qf, &c->y, &c->rh, &c->pa, &hi};
+    void* a_upd[] = {&L, &c->dinvf, &c->pf, &c->qf, &c->y, &c->rh, &c->pa, &hi, &setc};
     void* a_dir[] = {&L, &c->dinvf, &c->rh, &c->pf};
     void* a_x[] = {&L, &c->y};
     void* a_rdir[] = {&L, &c->dinvf, &c->rh, &c->pf};
@@ -1568,8 +1772,12 @@ fvgb_status build_mixed(SolverCache* c) {
     if (e == cudaSuccess) e = add_kernel(g, &n_res0, &n_prep, (void*)k_ir_residual<true>, nb, kT, a_res);
     if (e == cudaSuccess) e = add_while(g, &n_outer, &n_res0, ho, &obody);
     if (e == cudaSuccess) e = add_while(obody, &o_inner, nullptr, hi, &ibody);
-    if (e == cudaSuccess) e = add_kernel(ibody, &i_spmv, nullptr, (void*)k_ir_spmv, nb, kT, a_spmv);
-    if (e == cudaSuccess) e = add_kernel(ibody, &i_upd, &i_spmv, (void*)k_ir_update, nb, kT, a_upd);
+    if (e == cudaSuccess)
+        e = add_kernel(ibody, &i_spmv, nullptr, (void*)variant_fn(kTuneSpmvMixed, c->variant[kTuneSpmvMixed]), nb,
+                       kT, a_spmv);
+    if (e == cudaSuccess)
+        e = add_kernel(ibody, &i_upd, &i_spmv, (void*)variant_fn(kTuneUpdateMixed, c->variant[kTuneUpdateMixed]),
+                       nb, kT, a_upd);
     if (e == cudaSuccess) e = add_kernel(ibody, &i_dir, &i_upd, (void*)k_ir_dir, nb, kT, a_dir);
     if (e == cudaSuccess) e = add_kernel(obody, &o_x, &o_inner, (void*)k_ir_xupdate, nb, kT, a_x);
     if (e == cudaSuccess) e = add_kernel(obody, &o_res, &o_x, (void*)k_ir_residual<false>, nb, kT, a_res);
@@ -1579,6 +1787,27 @@ fvgb_status build_mixed(SolverCache* c) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(e, "mixed CG graph");
     return FVGB_OK;
+}
+
+fvgb_status build_mixed(SolverCache* c) {
+    const size_t n = (size_t)c->n;
+    if (!c->ah) {
+        cudaError_t e = calloc_dev(c, &c->ah, (size_t)c->ls->mesh->m_len);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->dinvf, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->ev, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->rh, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->y, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->pf, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->qf, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->pf2, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->zf, n);
+        if (e != cudaSuccess) return cuda_fail(e, "mixed CG workspace");
+    }
+    if (!c->tunedmx) {
+        fvgb_status st = tune_mixed(c);
+        if (st != FVGB_OK) return st;
+    }
+    return graph_mixed(c);
 }
 
 fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
@@ -1647,8 +1876,10 @@ fvgb_status host_loop(SolverCache* c, cudaStream_t s) {
         FVGB_CUDA_TRY(cudaMemcpyAsync(c->h_active, &c->L.bs->n_active, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         FVGB_CUDA_TRY(cudaStreamSynchronize(s));
         if (*c->h_active <= 0) break;  // the update kernel retires every case by max_iter at the latest
-        k_pcg_spmv<<<nb, kT, 0, s>>>(c->L, m, val, c->p, c->q, c->pa);
-        k_pcg_update<<<nb, kT, 0, s>>>(c->L, c->dinv, c->p, c->q, c->r, c->z, c->pa, c->pb, h, 0);
+        launch_variant(variant_fn(kTuneSpmv64, c->variant[kTuneSpmv64]), nb, s, c->L, m, val, (const double*)c->p,
+                       c->q, c->pa);
+        launch_variant(variant_fn(kTuneUpdate64, c->variant[kTuneUpdate64]), nb, s, c->L, (const double*)c->dinv,
+                       (const double*)c->p, (const double*)c->q, c->r, c->z, c->pa, c->pb, h, 0);
         k_pcg_dir<<<nb, kT, 0, s>>>(c->L, c->z, c->p);
         FVGB_LAUNCH_CHECK("fvgb_solve: iteration");
     }
@@ -1803,6 +2034,37 @@ extern "C" fvgb_status fvgb_batch_solve(fvgb_batch* b, double* x, const fvgb_sol
     return sync_stats(b->c, stats, (cudaStream_t)stream);
 }
 
+// Launch-bound variants of the CG kernels: the autotuner's measurements and
+// choices for this system, optionally forcing a variant per kernel kind.
+extern "C" fvgb_status fvgb_solve_tuning(fvgb_ls* ls, const int32_t* force, int32_t* chosen, float* ms) {
+    fvgb_clear_error();
+    FVGB_CHECK_ARG(ls && chosen && ms, "fvgb_solve_tuning: null argument");
+    FVGB_CHECK_ARG(ls->ncomp == 1, "fvgb_solve_tuning: scalar systems only");
+    if (force)
+        for (int k = 0; k < kTuneKinds; ++k)
+            FVGB_CHECK_ARG(force[k] >= -1 && force[k] < kNumVariants, "fvgb_solve_tuning: bad variant");
+    SolverCache* c = nullptr;
+    fvgb_status st = single_cache(ls, &c);
+    if (st != FVGB_OK) return st;
+    FVGB_CUDA_TRY(cudaDeviceSynchronize());  // no solve of this system in flight while its graphs are rebuilt
+    if (force)
+        for (int k = 0; k < kTuneKinds; ++k) c->forced[k] = force[k];
+    st = build_fp64(c);  // allocates and tunes once, then (re)builds the graph
+    if (st == FVGB_OK) st = build_mixed(c);
+    if (st != FVGB_OK) return st;
+    if (force) {
+        for (int k = 0; k < kTuneKinds; ++k) pick(c, k);
+        st = graph_fp64(c);
+        if (st == FVGB_OK) st = graph_mixed(c);
+        if (st != FVGB_OK) return st;
+    }
+    for (int k = 0; k < kTuneKinds; ++k) {
+        chosen[k] = kVariantMinBlocks[c->variant[k]];
+        for (int v = 0; v < kNumVariants; ++v) ms[k * kNumVariants + v] = c->tune_ms[k][v];
+    }
+    return FVGB_OK;
+}
+
 // Per-kernel timing of the FP64 CG iteration (outside any graph): runs init and
 // `iters` iterations on a private copy of x with CUDA events around each kernel
 // and returns the mean milliseconds of [spmv, update, direction, init].  A
@@ -1843,9 +2105,11 @@ extern "C" fvgb_status fvgb_solve_kernel_times(fvgb_ls* ls, const double* x0, in
     cudaEventRecord(ev[1], s);
     for (int it = 0; it < iters; ++it) {
         cudaEventRecord(ev[2], s);
-        k_pcg_spmv<<<nb, kT, 0, s>>>(c->L, m, ls->values, c->p, c->q, c->pa);
+        launch_variant(variant_fn(kTuneSpmv64, c->variant[kTuneSpmv64]), nb, s, c->L, m, (const double*)ls->values,
+                       (const double*)c->p, c->q, c->pa);
         cudaEventRecord(ev[3], s);
-        k_pcg_update<<<nb, kT, 0, s>>>(c->L, c->dinv, c->p, c->q, c->r, c->z, c->pa, c->pb, h, 0);
+        launch_variant(variant_fn(kTuneUpdate64, c->variant[kTuneUpdate64]), nb, s, c->L, (const double*)c->dinv,
+                       (const double*)c->p, (const double*)c->q, c->r, c->z, c->pa, c->pb, h, 0);
         cudaEventRecord(ev[4], s);
         k_pcg_dir<<<nb, kT, 0, s>>>(c->L, c->z, c->p);
         cudaEventRecord(ev[5], s);

@@ -298,6 +298,15 @@ fvgb_status fvgb_batch_solve(fvgb_batch* batch, double* x, const fvgb_solver_cfg
 fvgb_status fvgb_batch_solve_async(fvgb_batch* batch, double* x, const fvgb_solver_cfg* cfg,
                                    fvgb_solver_stats* stats_dev, fvgb_stream stream);
 
+/* Autotuner of the CG kernels (no counterpart in the reference): at the first
+ * solve of a system with at least 2^18 rows the SpMV and update kernels of the
+ * FP64 and mixed solves are timed in four launch-bound variants (at least 2, 4,
+ * 6, 8 resident blocks per SM) and the solve graphs use the fastest; all
+ * variants give the same bits.  chosen[4]: the minimum-blocks value in use for
+ * [FP64 SpMV, FP64 update, FP32 SpMV, FP32 update]; ms[16]: the measured median
+ * milliseconds per kind and variant (0 where not measured).  force[4] (or NULL):
+ * a variant index 0..3 per kind, -1 to keep the tuned choice. */
+fvgb_status fvgb_solve_tuning(fvgb_ls* ls, const int32_t* force, int32_t* chosen, float* ms);
 /* Measurement aid (no reference counterpart): runs the FP64 CG init and
  * `iters` iterations outside the graph on a private copy of x0, with CUDA
  * events around each kernel; ms_out[4] = mean milliseconds of

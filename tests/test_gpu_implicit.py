@@ -260,3 +260,33 @@ def test_mixed_tiny_residual_is_scale_invariant(cuda):
     so = o.solve(v2, r2, xo, precision=1, **kw)
     assert so.status == 0 and so.num_iter == s2.num_iter
     np.testing.assert_array_equal(x2.cpu().numpy(), xo)
+
+
+def test_kernel_variants_give_the_same_bits(cuda):
+    """The autotuner's launch-bound variants of the SpMV and update kernels
+    (fvgb_solve_tuning) execute the same arithmetic: forcing each variant gives
+    identical FP64 and mixed-precision solves."""
+    import ctypes as C
+
+    hm, dm, T, o, ls, v, r = solve_case(40, 32, 24)
+    L = abi.lib()
+    chosen = (C.c_int32 * 4)()
+    ms = (C.c_float * 16)()
+    out = {}
+    for var in range(4):
+        force = (C.c_int32 * 4)(var, var, var, var)
+        abi.check(L.fvgb_solve_tuning(ls.handle, force, chosen, ms))
+        assert list(chosen) == [(2, 4, 6, 8)[var]] * 4
+        for prec in (abi.PREC_FP64, abi.PREC_MIXED_IR):
+            x = T.internal.clone()
+            st = ls.solve(x, rel_tol=1e-9, max_iter=3000, precision=prec, kernel_mode=1)
+            assert st.status == abi.OK
+            out.setdefault(prec, []).append((x.cpu().numpy(), st.num_iter, st.final_res_norm))
+    for prec, runs in out.items():
+        for run in runs[1:]:
+            np.testing.assert_array_equal(runs[0][0], run[0])
+            assert runs[0][1:] == run[1:]
+    # back to the tuned choice
+    force = (C.c_int32 * 4)(-1, -1, -1, -1)
+    abi.check(L.fvgb_solve_tuning(ls.handle, force, chosen, ms))
+    assert all(c in (2, 4, 6, 8) for c in chosen)
