@@ -107,7 +107,9 @@ inline fvgb_status cuda_fail(cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return cuda_fail(e_, where);   \
     } while (0)
 
-inline unsigned grid_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+// at least one block: every kernel bounds-checks its index, and a zero-block
+// launch is a configuration error (empty boundary or face sets are legal)
+inline unsigned grid_for(int64_t n, int threads) { return n > 0 ? (unsigned)((n + threads - 1) / threads) : 1u; }
 
 // Builds a PatchTable from a host array of per-patch types; false if invalid.
 inline bool make_patch_table(const fvgb_mesh* m, const int32_t* types, PatchTable* t) {

@@ -168,7 +168,10 @@ __global__ void __launch_bounds__(kT)
         st->res = res0;
         st->tol = tol;
         bool done = !(res0 > tol) || res0 == 0.0;
-        if (!done && st->max_iter <= 0) {
+        if (!isfinite(res0)) {  // NaN or inf in b or x: not "converged"
+            done = true;
+            st->status = FVGB_ERR_BREAKDOWN;
+        } else if (!done && st->max_iter <= 0) {
             done = true;
             st->status = FVGB_ERR_NOT_CONVERGED;
         }

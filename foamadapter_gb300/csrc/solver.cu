@@ -252,7 +252,10 @@ __global__ void __launch_bounds__(kT)
             cs->res = res0;
             cs->tol = tol;
             bool done = !(res0 > tol) || res0 == 0.0;
-            if (!done && prm.max_iter <= 0) {
+            if (!isfinite(res0)) {  // NaN or inf in b or x: not "converged"
+                done = true;
+                cs->status = FVGB_ERR_BREAKDOWN;
+            } else if (!done && prm.max_iter <= 0) {
                 done = true;
                 cs->status = FVGB_ERR_NOT_CONVERGED;
             }
@@ -966,7 +969,10 @@ __global__ void __launch_bounds__(kPT, 1)
             tol = prm.rel_tol * res0;
             if (prm.abs_tol > tol) tol = prm.abs_tol;
             bool done = !(res0 > tol) || res0 == 0.0;
-            if (!done && prm.max_iter <= 0) {
+            if (!isfinite(res0)) {
+                done = true;
+                status = FVGB_ERR_BREAKDOWN;
+            } else if (!done && prm.max_iter <= 0) {
                 done = true;
                 status = FVGB_ERR_NOT_CONVERGED;
             }

@@ -522,7 +522,8 @@ static int32_t solve_fp64(const or_csr* A, const double* val, const double* b, d
     if (cfg->abs_tol > tol) tol = cfg->abs_tol;
     int32_t it = 0, status = ST_OK;
     int done = !(res > tol) || res == 0.0;
-    if (!done && cfg->max_iter <= 0) { done = 1; status = ST_NOT_CONVERGED; }
+    if (!isfinite(res)) { done = 1; status = ST_BREAKDOWN; }
+    else if (!done && cfg->max_iter <= 0) { done = 1; status = ST_NOT_CONVERGED; }
     while (!done) {
         /* q = A p ; pq */
 #pragma omp parallel for schedule(static)
