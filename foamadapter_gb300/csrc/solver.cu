@@ -1152,7 +1152,7 @@ __global__ void __launch_bounds__(kPT, 1)
     k_ir_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
                     float* a32, float* ev, float* dinv, float* rh, float* y, float* pbuf0, float* pbuf1, float* z,
                     float* q, double* pa, double* pb, double* pc, GridBar* gb, int nvb) {
-    __shared__ double sD[kPT], sm[kT], sm2[kT], sm3[kT], cell;
+    __shared__ double sD[kPT], sm[kT], sm3[kT], cell;
     __shared__ float sF1[kPT], sF2[kPT], smf[kT];
     __shared__ unsigned int sflags;
     __shared__ IrShared sh;
@@ -1446,6 +1446,18 @@ __global__ void __launch_bounds__(kPT, 1)
 }
 
 // ---------------------------------------------------------------- graph glue
+cudaError_t add_kernel_deps(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, size_t ndeps,
+                            void* func, unsigned grid, unsigned block, void** args) {
+    cudaKernelNodeParams kp{};
+    kp.func = func;
+    kp.gridDim = dim3(grid);
+    kp.blockDim = dim3(block);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    return cudaGraphAddKernelNode(node, g, deps, ndeps, &kp);
+}
+
 cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* dep, void* func, unsigned grid,
                        unsigned block, void** args) {
     cudaKernelNodeParams kp{};
@@ -1642,18 +1654,15 @@ fvgb_status tune_fp64(SolverCache* c) {
     return FVGB_OK;
 }
 
-fvgb_status graph_fp64(SolverCache* c) {
-    if (c->g64) {
-        cudaGraphExecDestroy(c->g64);
-        c->g64 = nullptr;
-    }
+// The FP64 solve as graph nodes in `g` after `deps`: init, a device-side while
+// loop over (SpMV, update, direction), the statistics; *last = the final node.
+cudaError_t add_fp64_nodes(SolverCache* c, cudaGraph_t g, const cudaGraphNode_t* deps, size_t ndeps,
+                           cudaGraphNode_t* last) {
     const fvgb_ls* ls = c->ls;
     MeshView m = ls->mesh->v;
     Layout L = c->L;
-    cudaGraph_t g = nullptr;
-    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle h;
-    cudaGraphNode_t n0, n1, n2, b0, b1, b2;
+    cudaGraphNode_t n0, n1, b0, b1, b2;
     cudaGraph_t body;
     const double* val = ls->values;
     const double* b = ls->rhs;
@@ -1665,14 +1674,26 @@ fvgb_status graph_fp64(SolverCache* c) {
     void* a_upd[] = {&L, &c->dinv, &c->p, &c->q, &c->r, &c->z, &c->pa, &c->pb, &h, &setc};
     void* a_dir[] = {&L, &c->z, &c->p};
     void* a_fin[] = {&L};
-    if (e == cudaSuccess) e = add_kernel(g, &n0, nullptr, (void*)k_pcg_init, nb, kT, a_init);
+    if (e == cudaSuccess) e = add_kernel_deps(g, &n0, deps, ndeps, (void*)k_pcg_init, nb, kT, a_init);
     if (e == cudaSuccess) e = add_while(g, &n1, &n0, h, &body);
     if (e == cudaSuccess)
         e = add_kernel(body, &b0, nullptr, (void*)variant_fn(kTuneSpmv64, c->variant[kTuneSpmv64]), nb, kT, a_spmv);
     if (e == cudaSuccess)
         e = add_kernel(body, &b1, &b0, (void*)variant_fn(kTuneUpdate64, c->variant[kTuneUpdate64]), nb, kT, a_upd);
     if (e == cudaSuccess) e = add_kernel(body, &b2, &b1, (void*)k_pcg_dir, nb, kT, a_dir);
-    if (e == cudaSuccess) e = add_kernel(g, &n2, &n1, (void*)k_finish, grid_for(c->ncases, 128), 128, a_fin);
+    if (e == cudaSuccess) e = add_kernel(g, last, &n1, (void*)k_finish, grid_for(c->ncases, 128), 128, a_fin);
+    return e;
+}
+
+fvgb_status graph_fp64(SolverCache* c) {
+    if (c->g64) {
+        cudaGraphExecDestroy(c->g64);
+        c->g64 = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t last;
+    cudaError_t e = add_fp64_nodes(c, g, nullptr, 0, &last);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->g64, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(e, "FP64 CG graph");
@@ -1746,17 +1767,12 @@ fvgb_status tune_mixed(SolverCache* c) {
     return FVGB_OK;
 }
 
-fvgb_status graph_mixed(SolverCache* c) {
-    if (c->gmix) {
-        cudaGraphExecDestroy(c->gmix);
-        c->gmix = nullptr;
-    }
+// The mixed-precision solve as graph nodes in `g` after `deps` (see add_fp64_nodes).
+cudaError_t add_mixed_nodes(SolverCache* c, cudaGraph_t g, const cudaGraphNode_t* deps, size_t ndeps,
+                            cudaGraphNode_t* last) {
     const fvgb_ls* ls = c->ls;
-    const fvgb_mesh* mesh = ls->mesh;
-    MeshView m = mesh->v;
+    MeshView m = ls->mesh->v;
     Layout L = c->L;
-    cudaGraph_t g = nullptr;
-    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle ho, hi;
     const double* val = ls->values;
     const double* b = ls->rhs;
@@ -1764,7 +1780,7 @@ fvgb_status graph_mixed(SolverCache* c) {
     int setc = 1;
     cudaError_t e = cudaGraphConditionalHandleCreate(&ho, g, 0, cudaGraphCondAssignDefault);
     if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
-    cudaGraphNode_t n_prep, n_res0, n_outer, n_fin, o_inner, o_x, o_res, o_dir, i_spmv, i_upd, i_dir;
+    cudaGraphNode_t n_prep, n_res0, n_outer, o_inner, o_x, o_res, o_dir, i_spmv, i_upd, i_dir;
     cudaGraph_t obody = nullptr, ibody = nullptr;
     void* a_prep[] = {&L, &m, &val, &b, &c->ah, &c->ev, &c->dinvf, &c->pa};
     void* a_res[] = {&L, &m, &val, &b, &c->dinvf, &c->rh, &c->y, &c->pf, &c->pa, &c->pb, &c->pc, &ho, &hi};
@@ -1774,7 +1790,7 @@ fvgb_status graph_mixed(SolverCache* c) {
     void* a_x[] = {&L, &c->y};
     void* a_rdir[] = {&L, &c->dinvf, &c->rh, &c->pf};
     void* a_fin[] = {&L};
-    if (e == cudaSuccess) e = add_kernel(g, &n_prep, nullptr, (void*)k_ir_prepare, nb, kT, a_prep);
+    if (e == cudaSuccess) e = add_kernel_deps(g, &n_prep, deps, ndeps, (void*)k_ir_prepare, nb, kT, a_prep);
     if (e == cudaSuccess) e = add_kernel(g, &n_res0, &n_prep, (void*)k_ir_residual<true>, nb, kT, a_res);
     if (e == cudaSuccess) e = add_while(g, &n_outer, &n_res0, ho, &obody);
     if (e == cudaSuccess) e = add_while(obody, &o_inner, nullptr, hi, &ibody);
@@ -1788,7 +1804,19 @@ fvgb_status graph_mixed(SolverCache* c) {
     if (e == cudaSuccess) e = add_kernel(obody, &o_x, &o_inner, (void*)k_ir_xupdate, nb, kT, a_x);
     if (e == cudaSuccess) e = add_kernel(obody, &o_res, &o_x, (void*)k_ir_residual<false>, nb, kT, a_res);
     if (e == cudaSuccess) e = add_kernel(obody, &o_dir, &o_res, (void*)k_ir_reliable_dir, nb, kT, a_rdir);
-    if (e == cudaSuccess) e = add_kernel(g, &n_fin, &n_outer, (void*)k_finish, grid_for(c->ncases, 128), 128, a_fin);
+    if (e == cudaSuccess) e = add_kernel(g, last, &n_outer, (void*)k_finish, grid_for(c->ncases, 128), 128, a_fin);
+    return e;
+}
+
+fvgb_status graph_mixed(SolverCache* c) {
+    if (c->gmix) {
+        cudaGraphExecDestroy(c->gmix);
+        c->gmix = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t last;
+    cudaError_t e = add_mixed_nodes(c, g, nullptr, 0, &last);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&c->gmix, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(e, "mixed CG graph");
@@ -2038,6 +2066,93 @@ extern "C" fvgb_status fvgb_batch_solve(fvgb_batch* b, double* x, const fvgb_sol
     fvgb_status st = fvgb_batch_solve_async(b, x, cfg, nullptr, stream);
     if (st != FVGB_OK) return st;
     return sync_stats(b->c, stats, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------- step graphs
+struct fvgb_step {
+    cudaGraphExec_t exec = nullptr;
+};
+
+// One implicit time step as ONE CUDA graph: psi -> psi_old copy, assembly, the
+// solve (all cases of `batch`, or the whole system), boundary update.  The
+// plain launches are stream-captured; the solve's nodes (with their device-side
+// while loops) are added to the capture graph directly.
+extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fvgb_term* terms, int32_t nterms,
+                                        double dt, const fvgb_bc* bc, double* psi, double* psi_b, double* psi_old,
+                                        const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev, fvgb_step** out) {
+    fvgb_clear_error();
+    FVGB_CHECK_ARG(ls && terms && nterms > 0 && bc && psi && cfg && out, "fvgb_step_create: null argument");
+    FVGB_CHECK_ARG(ls->ncomp == 1, "fvgb_step_create: scalar systems only");
+    FVGB_CHECK_ARG(!batch || batch->c->ls == ls, "fvgb_step_create: the batch belongs to another system");
+    fvgb_status fst = check_cfg(cfg);
+    if (fst != FVGB_OK) return fst;
+    FVGB_CHECK_ARG(cfg->kernel_mode != 3, "fvgb_step_create: the host-driven loop cannot be part of a graph");
+    SolverCache* c = batch ? batch->c : nullptr;
+    if (!c) {
+        fst = single_cache(ls, &c);
+        if (fst != FVGB_OK) return fst;
+    }
+    const bool mixed = cfg->precision == FVGB_PREC_MIXED_IR;
+    fst = mixed ? build_mixed(c) : build_fp64(c);  // workspace and tuning happen before the capture
+    if (fst != FVGB_OK) return fst;
+    SolverParams prm{};
+    prm.x = psi;
+    prm.stats_out = stats_dev;
+    prm.rel_tol = cfg->rel_tol;
+    prm.abs_tol = cfg->abs_tol;
+    prm.inner_rel_tol = cfg->inner_rel_tol;
+    prm.max_iter = cfg->max_iter;
+    prm.inner_max_iter = cfg->inner_max_iter;
+    prm.max_outer = cfg->max_outer;
+    cudaStream_t cs = nullptr;
+    FVGB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    const bool capturing = e == cudaSuccess;
+    if (e == cudaSuccess && psi_old)
+        e = cudaMemcpyAsync(psi_old, psi, sizeof(double) * (size_t)c->n, cudaMemcpyDeviceToDevice, cs);
+    if (e == cudaSuccess) fst = fvgb_assemble(ls, terms, nterms, dt, bc, psi_b, (fvgb_stream)cs);
+    if (e == cudaSuccess && fst == FVGB_OK) {
+        k_set_params<<<grid_for(c->ncases, 128), 128, 0, cs>>>(c->L, c->ncases, prm);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && fst == FVGB_OK) {
+        cudaStreamCaptureStatus cst;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
+        cudaGraphNode_t last;
+        if (e == cudaSuccess) e = mixed ? add_mixed_nodes(c, cg, deps, nd, &last) : add_fp64_nodes(c, cg, deps, nd, &last);
+        if (e == cudaSuccess)
+            e = cudaStreamUpdateCaptureDependencies(cs, &last, nullptr, 1, cudaStreamSetCaptureDependencies);
+    }
+    if (e == cudaSuccess && fst == FVGB_OK) fst = fvgb_bc_correct(ls->mesh, 1, bc, psi, psi_b, (fvgb_stream)cs);
+    if (capturing) {
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess && fst == FVGB_OK) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (fst != FVGB_OK) return fst;
+    if (e != cudaSuccess) return cuda_fail(e, "fvgb_step_create");
+    *out = new fvgb_step{exec};
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_step_launch(fvgb_step* step, fvgb_stream stream) {
+    FVGB_CHECK_ARG(step && step->exec, "fvgb_step_launch: null step");
+    FVGB_CUDA_TRY(cudaGraphLaunch(step->exec, (cudaStream_t)stream));
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_step_destroy(fvgb_step* step) {
+    if (!step) return FVGB_OK;
+    if (step->exec) cudaGraphExecDestroy(step->exec);
+    delete step;
+    return FVGB_OK;
 }
 
 // Launch-bound variants of the CG kernels: the autotuner's measurements and

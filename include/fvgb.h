@@ -298,6 +298,21 @@ fvgb_status fvgb_batch_solve(fvgb_batch* batch, double* x, const fvgb_solver_cfg
 fvgb_status fvgb_batch_solve_async(fvgb_batch* batch, double* x, const fvgb_solver_cfg* cfg,
                                    fvgb_solver_stats* stats_dev, fvgb_stream stream);
 
+/* One implicit time step as one CUDA graph (no counterpart in the reference;
+ * the steps of dsl::solve, expression.hpp:143-153, captured once): copy psi to
+ * psi_old (skipped when psi_old is NULL; a DDT term's cell field is psi_old),
+ * assemble `terms` with `bc`, solve every case of `batch` (or the whole system
+ * when batch is NULL) into psi with `cfg` (graph path; kernel_mode 3 is not
+ * allowed), update psi_b from psi.  The graph keeps the pointers it was created
+ * with; per-case statistics of every launch go to stats_dev (device, may be
+ * NULL).  fvgb_step_launch enqueues it on a stream. */
+typedef struct fvgb_step fvgb_step;
+fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fvgb_term* terms, int32_t nterms, double dt,
+                             const fvgb_bc* bc, double* psi, double* psi_b, double* psi_old,
+                             const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev, fvgb_step** out);
+fvgb_status fvgb_step_launch(fvgb_step* step, fvgb_stream stream);
+fvgb_status fvgb_step_destroy(fvgb_step* step);
+
 /* Autotuner of the CG kernels (no counterpart in the reference): at the first
  * solve of a system with at least 2^18 rows the SpMV and update kernels of the
  * FP64 and mixed solves are timed in four launch-bound variants (at least 2, 4,
