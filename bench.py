@@ -550,6 +550,21 @@ def run_batch(args):
         out[name] = {"case_steps_per_s": len(cases) * args.batch_steps / sec, "s": sec,
                      "all_ok": all(x.status == 0 for x in stl),
                      "iters_last_step_mean": float(np.mean([x.num_iter for x in stl]))}
+    # the same packed mixed step as ONE CUDA graph per time step (fvgb_step_*)
+    step = C.c_void_p()
+    abi.check(L.fvgb_step_create(ls.handle, batch.handle, terms, 2, 0.01, C.byref(bc), abi.ptr(T.internal),
+                                 abi.ptr(T.boundary), abi.ptr(T_old), C.byref(cfg_mixed), stats_dev.data_ptr(),
+                                 C.byref(step)))
+    T.internal.fill_(300.0)
+    abi.check(L.fvgb_step_launch(step, s))                    # warm-up
+    T.internal.fill_(300.0)
+    sec = timed(lambda: abi.check(L.fvgb_step_launch(step, s)), args.batch_steps)
+    st = stats_dev.cpu().numpy().tobytes()
+    stl = [abi.SolverStats.from_buffer_copy(st[i * 32:(i + 1) * 32]) for i in range(len(cases))]
+    out["packed_mixed_step_graph"] = {"case_steps_per_s": len(cases) * args.batch_steps / sec, "s": sec,
+                                      "all_ok": all(x.status == 0 for x in stl),
+                                      "iters_last_step_mean": float(np.mean([x.num_iter for x in stl]))}
+    abi.check(L.fvgb_step_destroy(step))
     # one case at a time, plain FP64 (a sample of cases, every case its own mesh/system/launches)
     sample = cases[:: max(1, len(cases) // args.alone_cases)][: args.alone_cases]
     solo = []

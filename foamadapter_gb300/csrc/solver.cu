@@ -1489,6 +1489,7 @@ cudaError_t add_while(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* dep
 struct SolverCache {
     const fvgb_ls* ls = nullptr;
     int n = 0, nb = 0, ncases = 0;
+    bool whole = false;  // one case covering rows [0, n): the persistent kernels' assumption
     Layout L{};
     std::vector<void*> allocs;
     double *dinv = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *pa = nullptr, *pb = nullptr;
@@ -1539,6 +1540,7 @@ fvgb_status cache_create(const fvgb_ls* ls, int ncases, const int32_t* ranges, S
     c->ls = ls;
     c->n = ls->mesh->v.n;
     c->ncases = ncases;
+    c->whole = ncases == 1 && ranges[0] == 0 && ranges[1] == c->n;
     std::vector<int32_t> blk_case, blk_row0, case_end(ncases), case_blk0(ncases + 1);
     for (int k = 0; k < ncases; ++k) {
         case_blk0[k] = (int32_t)blk_case.size();
@@ -1878,7 +1880,7 @@ int persistent_grid(SolverCache* c, bool mixed) {
 }
 
 bool use_persistent(SolverCache* c, const fvgb_solver_cfg* cfg) {
-    if (c->ncases != 1 || cfg->kernel_mode == 1 || cfg->kernel_mode == 3) return false;
+    if (!c->whole || cfg->kernel_mode == 1 || cfg->kernel_mode == 3) return false;
     if (cfg->kernel_mode != 2 && c->n > (1 << 20)) return false;
     if (persistent_grid(c, cfg->precision == FVGB_PREC_MIXED_IR) <= 0) return false;
     if (!c->bar) {
