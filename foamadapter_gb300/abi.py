@@ -68,7 +68,10 @@ class ServerCfg(C.Structure):
 
 class ServeRequest(C.Structure):
     _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("steps", i32), ("U", dbl * 3), ("D", dbl), ("dt", dbl),
-                ("precision", i32), ("kernel_mode", i32), ("T_out", vp)]
+                ("precision", i32), ("kernel_mode", i32), ("flags", i32), ("reserved", i32), ("T_out", vp)]
+
+
+SERVE_REASSEMBLE = 1
 
 
 class ServeResult(C.Structure):
@@ -104,6 +107,7 @@ _SIGS = {
     "fvgb_ls_create": (C.c_int, [vp, i32, C.POINTER(vp)]),
     "fvgb_ls_destroy": (C.c_int, [vp]),
     "fvgb_assemble": (C.c_int, [vp, C.POINTER(Term), i32, dbl, C.POINTER(BC), vp, vp]),
+    "fvgb_assemble_rhs": (C.c_int, [vp, C.POINTER(Term), i32, dbl, C.POINTER(BC), vp, vp]),
     "fvgb_set_reference": (C.c_int, [vp, i32, dbl, vp]),
     "fvgb_apply_operator": (C.c_int, [vp, vp, vp, vp]),
     "fvgb_ls_diag": (C.c_int, [vp, vp, vp]),

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(kThreads)
     k_assemble(MeshView m, TermPack tp, PatchTable pt, double dtInv,
                const double* __restrict__ ref, const double* __restrict__ psi_b,
                double* __restrict__ values, double* __restrict__ rhs, double* __restrict__ bmat,
-               double* __restrict__ brhs) {
+               double* __restrict__ brhs, int rhs_only) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.n) return;
     const int slice = c >> 5, lane = c & 31;
@@ -160,6 +160,7 @@ __global__ void __launch_bounds__(kThreads)
                     bmat[b] = bmat[b] + mm;
                     continue;
                 }
+                if (rhs_only) continue;  // internal faces only feed the matrix
                 const bool isOwner = code >= 0;
                 const int f = isOwner ? code : -code - 1;
                 if (lap) {
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(kThreads)
     }
 #pragma unroll
     for (int k = 0; k < NC; ++k) rhs[c * NC + k] = r[k];
+    if (rhs_only) return;
 
     // ---- pass 2: the row's slots
     const int mbase = __ldg(&m.m_ptr[slice]);
@@ -307,9 +309,9 @@ extern "C" fvgb_status fvgb_ls_destroy(fvgb_ls* ls) {
     return FVGB_OK;
 }
 
-extern "C" fvgb_status fvgb_assemble(fvgb_ls* ls, const fvgb_term* terms, int32_t nterms,
-                                     double dt, const fvgb_bc* psi_bc, const double* psi_b,
-                                     fvgb_stream stream) {
+namespace {
+fvgb_status assemble(fvgb_ls* ls, const fvgb_term* terms, int32_t nterms, double dt, const fvgb_bc* psi_bc,
+                     const double* psi_b, fvgb_stream stream, int rhs_only) {
     FVGB_CHECK_ARG(ls && (terms || nterms == 0), "fvgb_assemble: null argument");
     FVGB_CHECK_ARG(nterms >= 0 && nterms <= FVGB_MAX_TERMS, "fvgb_assemble: 0..8 terms");
     const fvgb_mesh* m = ls->mesh;
@@ -359,12 +361,32 @@ extern "C" fvgb_status fvgb_assemble(fvgb_ls* ls, const fvgb_term* terms, int32_
     cudaStream_t s = (cudaStream_t)stream;
     if (ls->ncomp == 1)
         k_assemble<1><<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, tp, pt, dtInv, ref, psi_b,
-                                                                     ls->values, ls->rhs, ls->bmat, ls->brhs);
+                                                                     ls->values, ls->rhs, ls->bmat, ls->brhs,
+                                                                     rhs_only);
     else
         k_assemble<3><<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, tp, pt, dtInv, ref, psi_b,
-                                                                     ls->values, ls->rhs, ls->bmat, ls->brhs);
+                                                                     ls->values, ls->rhs, ls->bmat, ls->brhs,
+                                                                     rhs_only);
     FVGB_LAUNCH_CHECK("fvgb_assemble");
+    if (!rhs_only) ++ls->version;
     return FVGB_OK;
+}
+}  // namespace
+
+extern "C" fvgb_status fvgb_assemble(fvgb_ls* ls, const fvgb_term* terms, int32_t nterms,
+                                     double dt, const fvgb_bc* psi_bc, const double* psi_b,
+                                     fvgb_stream stream) {
+    return assemble(ls, terms, nterms, dt, psi_bc, psi_b, stream, 0);
+}
+
+// The same terms with the matrix kept: only rhs and the boundary coefficients
+// are recomputed (their values are what fvgb_assemble would write; the matrix
+// values it would write are those already there when the implicit terms, dt,
+// mesh and boundary types are unchanged).
+extern "C" fvgb_status fvgb_assemble_rhs(fvgb_ls* ls, const fvgb_term* terms, int32_t nterms,
+                                         double dt, const fvgb_bc* psi_bc, const double* psi_b,
+                                         fvgb_stream stream) {
+    return assemble(ls, terms, nterms, dt, psi_bc, psi_b, stream, 1);
 }
 
 extern "C" fvgb_status fvgb_set_reference(fvgb_ls* ls, int32_t ref_cell, double ref_value,
@@ -374,6 +396,7 @@ extern "C" fvgb_status fvgb_set_reference(fvgb_ls* ls, int32_t ref_cell, double 
     FVGB_CHECK_ARG(ref_cell >= 0 && ref_cell < ls->mesh->v.n, "fvgb_set_reference: cell out of range");
     k_set_reference<<<1, 32, 0, (cudaStream_t)stream>>>(ls->mesh->v, ref_cell, ref_value, ls->values, ls->rhs);
     FVGB_LAUNCH_CHECK("fvgb_set_reference");
+    ++ls->version;
     return FVGB_OK;
 }
 

@@ -82,6 +82,7 @@ struct fvgb_ls {
     double* bmat = nullptr;    // [nbf]
     double* brhs = nullptr;    // [nbf*ncomp]
     SolverCache* solver = nullptr;
+    uint64_t version = 1;      // bumped whenever `values` change (assembly, SetReference)
 };
 
 // Per-call patch table passed to kernels by value.

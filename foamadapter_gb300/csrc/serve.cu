@@ -198,7 +198,11 @@ fvgb_status enqueue_step(Slot* s, int k) {
         {FVGB_TERM_LAPLACIAN, 0, -1.0, nullptr, s->gamma},
     };
     fvgb_bc bc{s->types, s->ref};
-    fvgb_status st = fvgb_assemble(s->ls, terms, 3, s->dt, &bc, s->Tb, s->stream);
+    // the implicit part (ddt + diffusion) is the same every step: after the first
+    // step only the rhs is assembled, and the solve keeps its FP32 matrix copy
+    const bool full = s->steps_done + k == 0 || (r.flags & FVGB_SERVE_REASSEMBLE);
+    fvgb_status st = full ? fvgb_assemble(s->ls, terms, 3, s->dt, &bc, s->Tb, s->stream)
+                          : fvgb_assemble_rhs(s->ls, terms, 3, s->dt, &bc, s->Tb, s->stream);
     if (st != FVGB_OK) return st;
     // the graph path by default: requests overlap on the device, which one
     // cooperative (persistent) kernel per request would serialise

@@ -48,7 +48,8 @@ struct SolverParams {
     double* x;
     fvgb_solver_stats* stats_out;  // device pointer [ncases] or null
     double rel_tol, abs_tol, inner_rel_tol;
-    int32_t max_iter, inner_max_iter, max_outer, pad;
+    int32_t max_iter, inner_max_iter, max_outer;
+    int32_t convert;  // mixed: form the FP32 matrix (0: the copy of an unchanged matrix is still valid)
 };
 
 struct CaseState {
@@ -439,11 +440,13 @@ __device__ __host__ __forceinline__ void residual_scale(double sres, double* sig
 // the magnitude the first residual is scaled by.
 __global__ void __launch_bounds__(kT)
     k_ir_prepare(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
-                 float* __restrict__ a32, float* __restrict__ ev, float* __restrict__ dinv, double* __restrict__ pa) {
+                 float* __restrict__ a32, float* __restrict__ ev, float* __restrict__ dinv, double* __restrict__ r0,
+                 double* __restrict__ pa) {
     __shared__ double sma[kT];
     const Blk k = blk_info(L);
     CaseState* cs = &L.cases[k.c];
     const double* __restrict__ x = L.bs->prm.x;
+    const bool convert = L.bs->prm.convert != 0;
     unsigned int f = 0;
     double asr = 0.0;
 #pragma unroll
@@ -452,26 +455,32 @@ __global__ void __launch_bounds__(kT)
         if (i >= k.end) continue;
         const double d = __ldg(&val[__ldg(&m.diag_pos[i])]);
         f |= d > 0.0 ? 1u : (d < 0.0 ? 2u : 4u);
-        const float di = (float)(1.0 / d);
-        dinv[i] = di;
-        const double sg = d < 0.0 ? -1.0 : 1.0;
-        const int slice = i >> 5, lane = i & 31;
-        const int b0 = __ldg(&m.m_ptr[slice]);
-        const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
-        double e = 0.0;
-        for (int kk = 0; kk < w; ++kk) {
-            const int pos = b0 + kk * 32 + lane;
-            const int code = __ldg(&m.m_code[pos]);
-            if (code == FVGB_PAD) {
-                a32[pos] = 0.0f;
-                continue;
+        float di;
+        if (convert) {
+            di = (float)(1.0 / d);
+            dinv[i] = di;
+            const double sg = d < 0.0 ? -1.0 : 1.0;
+            const int slice = i >> 5, lane = i & 31;
+            const int b0 = __ldg(&m.m_ptr[slice]);
+            const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+            double e = 0.0;
+            for (int kk = 0; kk < w; ++kk) {
+                const int pos = b0 + kk * 32 + lane;
+                const int code = __ldg(&m.m_code[pos]);
+                if (code == FVGB_PAD) {
+                    a32[pos] = 0.0f;
+                    continue;
+                }
+                const double a = __ldg(&val[pos]);
+                e = e + a;
+                a32[pos] = code == -1 ? 0.0f : (float)(sg * a);
             }
-            const double a = __ldg(&val[pos]);
-            e = e + a;
-            a32[pos] = code == -1 ? 0.0f : (float)(sg * a);
+            ev[i] = (float)(sg * e);
+        } else {
+            di = dinv[i];
         }
-        ev[i] = (float)(sg * e);
         const double ri = __ldg(&b[i]) - spmv_row(m, val, x, i);
+        r0[i] = ri;  // the first refinement step takes it from here
         asr = fma(ri * (double)fabsf(di), ri, asr);
     }
     f = __reduce_or_sync(0xffffffffu, f);
@@ -493,7 +502,8 @@ __global__ void __launch_bounds__(kT)
 template <bool FIRST>
 __global__ void __launch_bounds__(kT)
     k_ir_residual(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
-                  const float* __restrict__ dinv, float* __restrict__ rh, float* __restrict__ y,
+                  const double* __restrict__ r0, const float* __restrict__ dinv, float* __restrict__ rh,
+                  float* __restrict__ y,
                   float* __restrict__ p, double* __restrict__ pa, double* __restrict__ pb, double* __restrict__ pc,
                   cudaGraphConditionalHandle h_outer, cudaGraphConditionalHandle h_inner) {
     __shared__ double sma[kT], smb[kT], smc[kT];
@@ -510,7 +520,7 @@ __global__ void __launch_bounds__(kT)
         for (int j = 0; j < kRowsPerThread; ++j) {
             const int i = blk_row(k, j);
             if (i >= k.end) continue;
-            const double ri = __ldg(&b[i]) - spmv_row(m, val, x, i);
+            const double ri = FIRST ? r0[i] : __ldg(&b[i]) - spmv_row(m, val, x, i);
             arr = fma(ri, ri, arr);
             const float di = __ldg(&dinv[i]);
             asr = fma(ri * (double)fabsf(di), ri, asr);
@@ -1150,8 +1160,8 @@ struct IrShared {
 
 __global__ void __launch_bounds__(kPT, 1)
     k_ir_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
-                    float* a32, float* ev, float* dinv, float* rh, float* y, float* pbuf0, float* pbuf1, float* z,
-                    float* q, double* pa, double* pb, double* pc, GridBar* gb, int nvb) {
+                    float* a32, float* ev, float* dinv, double* r0, float* rh, float* y, float* pbuf0, float* pbuf1,
+                    float* z, float* q, double* pa, double* pb, double* pc, GridBar* gb, int nvb) {
     __shared__ double sD[kPT], sm[kT], sm3[kT], cell;
     __shared__ float sF1[kPT], sF2[kPT], smf[kT];
     __shared__ unsigned int sflags;
@@ -1173,26 +1183,31 @@ __global__ void __launch_bounds__(kPT, 1)
         if (i < n) {
             const double d = __ldg(&val[__ldg(&m.diag_pos[i])]);
             atomicOr(&sflags, d > 0.0 ? 1u : (d < 0.0 ? 2u : 4u));
-            di = (float)(1.0 / d);
-            dinv[i] = di;
-            const double sg = d < 0.0 ? -1.0 : 1.0;
-            const int slice = i >> 5, lane = i & 31;
-            const int b0 = __ldg(&m.m_ptr[slice]);
-            const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
-            double e = 0.0;
-            for (int kk = 0; kk < w; ++kk) {
-                const int pos = b0 + kk * 32 + lane;
-                const int code = __ldg(&m.m_code[pos]);
-                if (code == FVGB_PAD) {
-                    a32[pos] = 0.0f;
-                    continue;
+            if (prm.convert) {
+                di = (float)(1.0 / d);
+                dinv[i] = di;
+                const double sg = d < 0.0 ? -1.0 : 1.0;
+                const int slice = i >> 5, lane = i & 31;
+                const int b0 = __ldg(&m.m_ptr[slice]);
+                const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+                double e = 0.0;
+                for (int kk = 0; kk < w; ++kk) {
+                    const int pos = b0 + kk * 32 + lane;
+                    const int code = __ldg(&m.m_code[pos]);
+                    if (code == FVGB_PAD) {
+                        a32[pos] = 0.0f;
+                        continue;
+                    }
+                    const double av = __ldg(&val[pos]);
+                    e = e + av;
+                    a32[pos] = code == -1 ? 0.0f : (float)(sg * av);
                 }
-                const double av = __ldg(&val[pos]);
-                e = e + av;
-                a32[pos] = code == -1 ? 0.0f : (float)(sg * av);
+                ev[i] = (float)(sg * e);
+            } else {
+                di = __ldcg(&dinv[i]);
             }
-            ev[i] = (float)(sg * e);
             ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
+            r0[i] = ri;
         }
         sD[T] = ri;
         sF1[T] = di;
@@ -1252,7 +1267,7 @@ __global__ void __launch_bounds__(kPT, 1)
             double ri = 0.0;
             float di = 0.0f, rhi = 0.0f;
             if (i < n) {
-                ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
+                ri = first ? __ldcg(&r0[i]) : __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
                 di = __ldcg(&dinv[i]);
                 rhi = (float)(ri * nsig_all);
                 if (di < 0.0f) rhi = -rhi;
@@ -1500,6 +1515,8 @@ struct SolverCache {
     fvgb_solver_stats* h_stats = nullptr;  // pinned [ncases]
     GridBar* bar = nullptr;
     float *pf2 = nullptr, *zf = nullptr;   // second direction buffer and z of the persistent mixed solve
+    double* r0 = nullptr;                   // mixed: first FP64 residual, from the preparation kernel
+    uint64_t converted_version = 0;        // fvgb_ls::version the FP32 matrix copy was formed from
     int pgrid_fp64 = 0, pgrid_mixed = 0;   // co-resident blocks of the persistent kernels (0: not asked yet)
     int variant[kTuneKinds] = {1, 1, 1, 1};  // chosen launch-bound variant per kernel kind
     int forced[kTuneKinds] = {-1, -1, -1, -1};
@@ -1740,6 +1757,7 @@ fvgb_status tune_mixed(SolverCache* c) {
             prm.inner_max_iter = 1 << 30;
             prm.max_outer = 1 << 30;
             prm.inner_rel_tol = 0.5;
+            prm.convert = 1;
             MeshView m = c->ls->mesh->v;
             Layout L = c->L;
             const double* val = c->ls->values;
@@ -1748,7 +1766,7 @@ fvgb_status tune_mixed(SolverCache* c) {
             int setc = 0;
             const unsigned nb = (unsigned)c->nb;
             k_set_params<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L, c->ncases, prm);
-            k_ir_prepare<<<nb, kT, 0, s>>>(c->L, m, val, b, c->ah, c->ev, c->dinvf, c->pa);
+            k_ir_prepare<<<nb, kT, 0, s>>>(c->L, m, val, b, c->ah, c->ev, c->dinvf, c->r0, c->pa);
             k_tune_mixed_state<<<nb, kT, 0, s>>>(c->L, c->pf, c->rh, c->y);
             void* a_spmv[] = {&L, &m, &c->ah, &c->ev, &c->pf, &c->qf, &c->pa};
             void* a_upd[] = {&L, &c->dinvf, &c->pf, &c->qf, &c->y, &c->rh, &c->pa, (void*)&h, &setc};
@@ -1784,8 +1802,8 @@ cudaError_t add_mixed_nodes(SolverCache* c, cudaGraph_t g, const cudaGraphNode_t
     if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
     cudaGraphNode_t n_prep, n_res0, n_outer, o_inner, o_x, o_res, o_dir, i_spmv, i_upd, i_dir;
     cudaGraph_t obody = nullptr, ibody = nullptr;
-    void* a_prep[] = {&L, &m, &val, &b, &c->ah, &c->ev, &c->dinvf, &c->pa};
-    void* a_res[] = {&L, &m, &val, &b, &c->dinvf, &c->rh, &c->y, &c->pf, &c->pa, &c->pb, &c->pc, &ho, &hi};
+    void* a_prep[] = {&L, &m, &val, &b, &c->ah, &c->ev, &c->dinvf, &c->r0, &c->pa};
+    void* a_res[] = {&L, &m, &val, &b, &c->r0, &c->dinvf, &c->rh, &c->y, &c->pf, &c->pa, &c->pb, &c->pc, &ho, &hi};
     void* a_spmv[] = {&L, &m, &c->ah, &c->ev, &c->pf, &c->qf, &c->pa};
     void* a_upd[] = {&L, &c->dinvf, &c->pf, &c->qf, &c->y, &c->rh, &c->pa, &hi, &setc};
     void* a_dir[] = {&L, &c->dinvf, &c->rh, &c->pf};
@@ -1837,6 +1855,7 @@ fvgb_status build_mixed(SolverCache* c) {
         if (e == cudaSuccess) e = calloc_dev(c, &c->qf, n);
         if (e == cudaSuccess) e = calloc_dev(c, &c->pf2, n);
         if (e == cudaSuccess) e = calloc_dev(c, &c->zf, n);
+        if (e == cudaSuccess) e = calloc_dev(c, &c->r0, n);
         if (e != cudaSuccess) return cuda_fail(e, "mixed CG workspace");
     }
     if (!c->tunedmx) {
@@ -1945,6 +1964,8 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
     prm.max_iter = cfg->max_iter;
     prm.inner_max_iter = cfg->inner_max_iter;
     prm.max_outer = cfg->max_outer;
+    prm.convert = c->converted_version != c->ls->version ? 1 : 0;
+    if (cfg->precision == FVGB_PREC_MIXED_IR) c->converted_version = c->ls->version;
     k_set_params<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L, c->ncases, prm);
     FVGB_LAUNCH_CHECK("fvgb_solve: parameters");
     if (cfg->kernel_mode == 3) return host_loop(c, s);
@@ -1959,8 +1980,9 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
         const int grid = nvb < pg ? nvb : pg;
         FVGB_CUDA_TRY(cudaMemsetAsync(c->bar, 0, sizeof(GridBar), s));
         if (mixed) {
-            void* args[] = {&L,    &m,     &val,   &b,    &c->ah, &c->ev, &c->dinvf, &c->rh, &c->y,
-                            &c->pf, &c->pf2, &c->zf, &c->qf, &c->pa, &c->pb, &c->pc,    &c->bar, &nvb};
+            // k_ir_persistent(L, m, val, b, a32, ev, dinv, r0, rh, y, pbuf0, pbuf1, z, q, pa, pb, pc, gb, nvb)
+            void* args[] = {&L,     &m,    &val,   &b,     &c->ah, &c->ev, &c->dinvf, &c->r0, &c->rh, &c->y,
+                            &c->pf, &c->pf2, &c->zf, &c->qf, &c->pa, &c->pb, &c->pc,   &c->bar, &nvb};
             FVGB_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_ir_persistent, dim3(grid), dim3(kPT), args, 0, s));
         } else {
             void* args[] = {&L, &m, &val, &b, &c->dinv, &c->r, &c->p, &c->q, &c->z, &c->pa, &c->pb, &c->bar, &nvb};
@@ -2106,6 +2128,7 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
     prm.max_iter = cfg->max_iter;
     prm.inner_max_iter = cfg->inner_max_iter;
     prm.max_outer = cfg->max_outer;
+    prm.convert = 1;  // the graph assembles the matrix every launch
     cudaStream_t cs = nullptr;
     FVGB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t graph = nullptr;

@@ -224,6 +224,14 @@ fvgb_status fvgb_ls_destroy(fvgb_ls* ls);
  * psi_bc / psi_b: boundary condition and current boundary values of psi. */
 fvgb_status fvgb_assemble(fvgb_ls* ls, const fvgb_term* terms, int32_t nterms, double dt,
                           const fvgb_bc* psi_bc, const double* psi_b, fvgb_stream stream);
+/* The same assembly with the matrix kept (no counterpart in the reference,
+ * which reassembles every step): only rhs and the boundary coefficients are
+ * recomputed.  Valid when the implicit terms, dt, mesh and boundary types are
+ * those of the last fvgb_assemble (e.g. a time step whose implicit part does
+ * not change); the result is then identical to a full assembly.  A solve that
+ * follows reuses its FP32 copy of the unchanged matrix. */
+fvgb_status fvgb_assemble_rhs(fvgb_ls* ls, const fvgb_term* terms, int32_t nterms, double dt,
+                              const fvgb_bc* psi_bc, const double* psi_b, fvgb_stream stream);
 /* PDESolver::SetReference (expression.hpp:102-111): rhs[r] += a_rr*value; a_rr += a_rr. */
 fvgb_status fvgb_set_reference(fvgb_ls* ls, int32_t ref_cell, double ref_value,
                                fvgb_stream stream);
@@ -389,6 +397,7 @@ typedef struct fvgb_server_cfg {
  * (explicit upwind convection, implicit diffusion, zero-gradient walls, initial
  * Gaussian blob at the centre); dt <= 0 picks 0.5*h/|U|.  T_out: optional HOST
  * buffer [nx*ny*nz] that receives the final field. */
+enum { FVGB_SERVE_REASSEMBLE = 1 };
 typedef struct fvgb_serve_request {
     int32_t nx, ny, nz, steps;
     double U[3];
@@ -397,6 +406,11 @@ typedef struct fvgb_serve_request {
     int32_t precision;         /* FVGB_PREC_FP64 or FVGB_PREC_MIXED_IR                */
     int32_t kernel_mode;       /* fvgb_solver_cfg.kernel_mode of every solve; 0 picks
                                   the graph path (requests overlap on the device)     */
+    int32_t flags;             /* FVGB_SERVE_REASSEMBLE: assemble the whole system every
+                                  step (the reference's dsl::solve); otherwise the
+                                  matrix is assembled once and each later step
+                                  assembles only the rhs (same results)              */
+    int32_t reserved;
     double* T_out;
 } fvgb_serve_request;
 typedef struct fvgb_serve_result {

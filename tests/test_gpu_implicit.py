@@ -290,3 +290,50 @@ def test_kernel_variants_give_the_same_bits(cuda):
     force = (C.c_int32 * 4)(-1, -1, -1, -1)
     abi.check(L.fvgb_solve_tuning(ls.handle, force, chosen, ms))
     assert all(c in (2, 4, 6, 8) for c in chosen)
+
+
+def test_rhs_only_assembly_and_reused_fp32_matrix(cuda):
+    """fvgb_assemble_rhs with unchanged implicit terms writes exactly what a full
+    assembly writes, and a mixed solve after it (FP32 matrix copy kept) gives the
+    bits of a solve on a freshly assembled system."""
+    import ctypes as C
+
+    hm, k, bcs, dt = heat_case(14, 12, 10)
+    o = Oracle(hm)
+    kf = o.interp_linear(1, k, k[hm.bcells].copy())
+
+    def setup():
+        dm = DeviceMesh(hm)
+        T = neon.VolumeField(dm, np.full(hm.n, 300.0), bcs)
+        return dm, T, neon.SurfaceField(dm, kf), neon.LinearSystem(dm)
+
+    L, s = abi.lib(), torch.cuda.current_stream().cuda_stream
+    kw = dict(rel_tol=1e-9, precision=abi.PREC_MIXED_IR, inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50)
+    # system A: step 1 full assembly + solve, step 2 rhs-only assembly + solve (reused FP32 matrix)
+    dm, T, gamma, ls = setup()
+    old = T.internal.clone()
+    terms = (abi.Term * 2)(*[t.struct() for t in (neon.ddt(old), neon.laplacian(gamma, -1.0))])
+    bc = T.bc_struct()
+    abi.check(L.fvgb_assemble(ls.handle, terms, 2, dt, C.byref(bc), abi.ptr(T.boundary), s))
+    ls.solve(T.internal, **kw)
+    T.correctBoundaryConditions()
+    old.copy_(T.internal)
+    abi.check(L.fvgb_assemble_rhs(ls.handle, terms, 2, dt, C.byref(bc), abi.ptr(T.boundary), s))
+    got = [t.cpu().numpy() for t in ls.export()]
+    x_a = T.internal.clone()
+    st_a = ls.solve(x_a, **kw)
+    # system B: the same second step with a full assembly on a fresh system
+    dm2, T2, gamma2, ls2 = setup()
+    T2.internal.copy_(old)
+    T2.correctBoundaryConditions()
+    old2 = old.clone()
+    terms2 = (abi.Term * 2)(*[t.struct() for t in (neon.ddt(old2), neon.laplacian(gamma2, -1.0))])
+    bc2 = T2.bc_struct()
+    abi.check(L.fvgb_assemble(ls2.handle, terms2, 2, dt, C.byref(bc2), abi.ptr(T2.boundary), s))
+    want = [t.cpu().numpy() for t in ls2.export()]
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b)
+    x_b = T2.internal.clone()
+    st_b = ls2.solve(x_b, **kw)
+    assert (st_a.num_iter, st_a.num_outer) == (st_b.num_iter, st_b.num_outer)
+    np.testing.assert_array_equal(x_a.cpu().numpy(), x_b.cpu().numpy())

@@ -88,9 +88,10 @@ def make_server(budget=8 << 30, streams=4, max_active=64):
     return h
 
 
-def submit(server, nx, ny, nz, steps, U, D, precision=abi.PREC_FP64):
+def submit(server, nx, ny, nz, steps, U, D, precision=abi.PREC_FP64, flags=0):
     out = np.zeros(nx * ny * nz)
-    req = abi.ServeRequest(nx, ny, nz, steps, (C.c_double * 3)(*U), D, 0.0, precision, 0, out.ctypes.data)
+    req = abi.ServeRequest(nx=nx, ny=ny, nz=nz, steps=steps, U=(C.c_double * 3)(*U), D=D, dt=0.0,
+                           precision=precision, kernel_mode=0, flags=flags, T_out=out.ctypes.data)
     rid = C.c_int64()
     st = abi.lib().fvgb_server_submit(server, C.byref(req), C.byref(rid))
     return st, rid.value, out
@@ -177,3 +178,20 @@ def test_server_budget_and_cancel(cuda):
     abi.lib().fvgb_server_destroy(sv)
     assert res[r1].status == abi.ERR_CANCELLED and res[r2].status == abi.ERR_CANCELLED
     assert res[r1].steps_done < 400
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED_IR])
+def test_rhs_only_steps_equal_full_reassembly(cuda, precision):
+    """Served requests assemble the matrix once and only the rhs afterwards (the
+    mixed solve then keeps its FP32 matrix copy); the results are those of a
+    full reassembly every step, bit for bit."""
+    outs = []
+    for flags in (0, abi.SERVE_REASSEMBLE):
+        sv = make_server()
+        subs = [submit(sv, *r, precision=precision, flags=flags) for r in REQS]
+        res = drain(sv, len(REQS))
+        abi.check(abi.lib().fvgb_server_destroy(sv))
+        assert all(res[rid].status == abi.OK for _, rid, _ in subs)
+        outs.append([o.copy() for _, _, o in subs])
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
