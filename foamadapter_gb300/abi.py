@@ -49,7 +49,11 @@ class Term(C.Structure):
 
 class SolverCfg(C.Structure):
     _fields_ = [("rel_tol", dbl), ("abs_tol", dbl), ("max_iter", i32), ("precision", i32),
-                ("inner_rel_tol", dbl), ("inner_max_iter", i32), ("max_outer", i32), ("kernel_mode", i32)]
+                ("inner_rel_tol", dbl), ("inner_max_iter", i32), ("max_outer", i32), ("kernel_mode", i32),
+                ("flags", i32)]
+
+
+SOLVE_NO_TUNE = 1
 
 
 class SolverStats(C.Structure):

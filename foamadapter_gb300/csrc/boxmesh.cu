@@ -321,8 +321,9 @@ extern "C" fvgb_status fvgb_mesh_create_boxes(const fvgb_box_spec* specs, int32_
     k_fill_ptr<<<grid_for(nslices + 1, 256), 256, 0, st>>>(g_ptr, nslices, kGW);
     k_fill_ptr<<<grid_for(nslices + 1, 256), 256, 0, st>>>(m_ptr, nslices, kMW);
     k_box_cells<<<grid_for(N, 256), 256, 0, st>>>(d_boxes, d_slice_box, (int)N, (int)NIF, o);
+    // no synchronisation: asynchronous copies from pageable host memory are staged
+    // before the call returns, so the host vectors may go out of scope
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors above go out of scope
     if (e != cudaSuccess) {
         free_mesh_partial(m);
         return cuda_fail(e, "fvgb_mesh_create_boxes: build");

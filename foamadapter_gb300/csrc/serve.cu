@@ -56,6 +56,7 @@ struct Slot {
     fvgb_solver_stats* stats_host = nullptr; // pinned [kChunk]
     cudaEvent_t done_ev = nullptr;
     int32_t inflight = 0;                    // steps of the chunk in flight
+    int32_t final_status = FVGB_OK;          // set when the request is retiring
     int32_t types[6] = {FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT,
                         FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT, FVGB_BC_FIXED_GRADIENT};
     double dt = 0;
@@ -82,6 +83,7 @@ struct fvgb_server {
     bool stop = false;
     int device = 0;
     Clock::time_point t0;
+    std::vector<Slot*> retiring;            // result copy enqueued, waiting for its event
     std::vector<Slot*> graveyard;           // retired, memory not yet released
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
@@ -206,19 +208,35 @@ fvgb_status enqueue_step(Slot* s, int k) {
     if (st != FVGB_OK) return st;
     // the graph path by default: requests overlap on the device, which one
     // cooperative (persistent) kernel per request would serialise
-    fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, 0.1, 1000, 50, r.kernel_mode == 0 ? 1 : r.kernel_mode};
+    fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, 0.1, 1000, 50, r.kernel_mode == 0 ? 1 : r.kernel_mode,
+                        FVGB_SOLVE_NO_TUNE};  // tuning would synchronise the device under every request
     st = fvgb_solve_async(s->ls, s->T, &cfg, s->stats_dev + k, s->stream);
     if (st != FVGB_OK) return st;
     return fvgb_bc_correct(s->mesh, 1, &bc, s->T, s->Tb, s->stream);
 }
 
+void report(fvgb_server* sv, Slot* s);
+
+// Enqueue the result copy and an event after it; the loop reports the request
+// once the event has completed (no stream synchronisation in the loop).
 void finish(fvgb_server* sv, Slot* s, int32_t status) {
     if (status == FVGB_OK && s->req.T_out && s->mesh) {
         // the box occupies rows [0, nx*ny*nz) of its own mesh
         const size_t rn = (size_t)s->req.nx * s->req.ny * s->req.nz;
         cudaMemcpyAsync(s->req.T_out, s->T, sizeof(double) * rn, cudaMemcpyDeviceToHost, s->stream);
     }
-    if (s->stream) cudaStreamSynchronize(s->stream);  // result copy done before the caller sees it
+    s->final_status = status;
+    if (s->stream && s->done_ev && cudaEventRecord(s->done_ev, s->stream) == cudaSuccess) {
+        sv->retiring.push_back(s);
+        return;
+    }
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    report(sv, s);
+}
+
+// The request's result is in the caller's buffer: publish it.
+void report(fvgb_server* sv, Slot* s) {
+    const int32_t status = s->final_status;
     fvgb_serve_result res{};
     res.id = s->id;
     res.status = status;
@@ -233,11 +251,12 @@ void finish(fvgb_server* sv, Slot* s, int32_t status) {
     sv->done.push_back(res);
 }
 
-// One device synchronisation for many retired requests; then their memory and
-// budget are returned.
+// Releasing device memory synchronises the device (cudaFree), which would stall
+// every request's queued work: it is done only when the loop is idle or when the
+// next waiting request needs budget that retired requests still hold, one
+// synchronisation for all of them.
 void release_graveyard(fvgb_server* sv, bool force) {
-    if (sv->graveyard.empty()) return;
-    if (!force && sv->graveyard.size() < 16) return;
+    if (sv->graveyard.empty() || !force) return;
     cudaDeviceSynchronize();
     int64_t freed = 0;
     for (Slot* s : sv->graveyard) {
@@ -258,8 +277,10 @@ void run(fvgb_server* sv) {
         std::vector<int64_t> cancels;
         {
             std::unique_lock<std::mutex> lk(sv->mu);
-            sv->cv.wait(lk, [&] { return sv->stop || !sv->waiting.empty() || !sv->active.empty(); });
-            if (sv->stop && sv->waiting.empty() && sv->active.empty()) break;
+            sv->cv.wait(lk, [&] {
+                return sv->stop || !sv->waiting.empty() || !sv->active.empty() || !sv->retiring.empty();
+            });
+            if (sv->stop && sv->waiting.empty() && sv->active.empty() && sv->retiring.empty()) break;
             cancels.swap(sv->cancel_ids);
             // cancel waiting requests
             for (auto it = sv->waiting.begin(); it != sv->waiting.end();) {
@@ -305,8 +326,21 @@ void run(fvgb_server* sv) {
             }
             sv->active.swap(keep);
         }
-        // advance every request whose previous chunk finished
+        // publish requests whose result copy has completed
         bool progressed = !admit.empty();
+        {
+            std::vector<Slot*> still;
+            for (Slot* s : sv->retiring) {
+                if (cudaEventQuery(s->done_ev) == cudaErrorNotReady) {
+                    still.push_back(s);
+                } else {
+                    report(sv, s);
+                    progressed = true;
+                }
+            }
+            sv->retiring.swap(still);
+        }
+        // advance every request whose previous chunk finished
         std::vector<Slot*> keep;
         for (Slot* s : sv->active) {
             if (s->inflight > 0) {
@@ -351,7 +385,7 @@ void run(fvgb_server* sv) {
             // release now if nothing runs, or if the next waiting request is held back
             // by budget that retired requests still hold
             std::lock_guard<std::mutex> lk(sv->mu);
-            flush = sv->active.empty() ||
+            flush = (sv->active.empty() && sv->retiring.empty()) ||
                     (!sv->waiting.empty() && sv->used + sv->waiting.front()->bytes > sv->cfg.budget_bytes);
         }
         release_graveyard(sv, flush);

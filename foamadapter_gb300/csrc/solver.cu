@@ -1629,9 +1629,9 @@ void pick(SolverCache* c, int kind) {
 // Times the FP64 SpMV and update variants on this system: CG iterations from a
 // zero vector (a scratch x, never the caller's), the solver state reset by the
 // next solve's parameter kernel.
-fvgb_status tune_fp64(SolverCache* c) {
+fvgb_status tune_fp64(SolverCache* c, bool measure) {
     c->tuned64 = true;
-    if (c->n >= kTuneMinRows) {
+    if (measure && c->n >= kTuneMinRows) {
         FVGB_CUDA_TRY(cudaDeviceSynchronize());  // the system's assembly may still run on the caller's stream
         double* tmp = nullptr;
         cudaStream_t s = nullptr;
@@ -1719,7 +1719,7 @@ fvgb_status graph_fp64(SolverCache* c) {
     return FVGB_OK;
 }
 
-fvgb_status build_fp64(SolverCache* c) {
+fvgb_status build_fp64(SolverCache* c, bool measure = true) {
     const size_t n = (size_t)c->n;
     if (!c->dinv) {
         cudaError_t e = calloc_dev(c, &c->dinv, n);
@@ -1730,7 +1730,7 @@ fvgb_status build_fp64(SolverCache* c) {
         if (e != cudaSuccess) return cuda_fail(e, "FP64 CG workspace");
     }
     if (!c->tuned64) {
-        fvgb_status st = tune_fp64(c);
+        fvgb_status st = tune_fp64(c, measure);
         if (st != FVGB_OK) return st;
     }
     return graph_fp64(c);
@@ -1738,9 +1738,9 @@ fvgb_status build_fp64(SolverCache* c) {
 
 // Times the FP32 SpMV and update variants of the mixed solve on this system
 // (after the preparation kernel, from a zero scratch vector).
-fvgb_status tune_mixed(SolverCache* c) {
+fvgb_status tune_mixed(SolverCache* c, bool measure) {
     c->tunedmx = true;
-    if (c->n >= kTuneMinRows) {
+    if (measure && c->n >= kTuneMinRows) {
         FVGB_CUDA_TRY(cudaDeviceSynchronize());
         double* tmp = nullptr;
         cudaStream_t s = nullptr;
@@ -1843,7 +1843,7 @@ fvgb_status graph_mixed(SolverCache* c) {
     return FVGB_OK;
 }
 
-fvgb_status build_mixed(SolverCache* c) {
+fvgb_status build_mixed(SolverCache* c, bool measure = true) {
     const size_t n = (size_t)c->n;
     if (!c->ah) {
         cudaError_t e = calloc_dev(c, &c->ah, (size_t)c->ls->mesh->m_len);
@@ -1859,7 +1859,7 @@ fvgb_status build_mixed(SolverCache* c) {
         if (e != cudaSuccess) return cuda_fail(e, "mixed CG workspace");
     }
     if (!c->tunedmx) {
-        fvgb_status st = tune_mixed(c);
+        fvgb_status st = tune_mixed(c, measure);
         if (st != FVGB_OK) return st;
     }
     return graph_mixed(c);
@@ -1871,6 +1871,7 @@ fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
     FVGB_CHECK_ARG(cfg->rel_tol >= 0 && cfg->abs_tol >= 0, "fvgb_solve: negative tolerance");
     FVGB_CHECK_ARG(cfg->max_iter >= 0 && cfg->max_iter <= 100000000, "fvgb_solve: bad max_iter");
     FVGB_CHECK_ARG(cfg->kernel_mode >= 0 && cfg->kernel_mode <= 3, "fvgb_solve: bad kernel_mode");
+    FVGB_CHECK_ARG((cfg->flags & ~FVGB_SOLVE_NO_TUNE) == 0, "fvgb_solve: unknown flags");
     FVGB_CHECK_ARG(cfg->kernel_mode != 3 || cfg->precision == FVGB_PREC_FP64,
                    "fvgb_solve: the host-driven loop (kernel_mode 3) is FP64 only");
     if (cfg->precision == FVGB_PREC_MIXED_IR)
@@ -1947,12 +1948,13 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
                    cudaStream_t s) {
     fvgb_status stt = check_cfg(cfg);
     if (stt != FVGB_OK) return stt;
+    const bool measure = !(cfg->flags & FVGB_SOLVE_NO_TUNE);
     if (cfg->precision == FVGB_PREC_FP64 && !c->g64) {
-        stt = build_fp64(c);
+        stt = build_fp64(c, measure);
         if (stt != FVGB_OK) return stt;
     }
     if (cfg->precision == FVGB_PREC_MIXED_IR && !c->gmix) {
-        stt = build_mixed(c);
+        stt = build_mixed(c, measure);
         if (stt != FVGB_OK) return stt;
     }
     SolverParams prm{};
@@ -2117,7 +2119,8 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
         if (fst != FVGB_OK) return fst;
     }
     const bool mixed = cfg->precision == FVGB_PREC_MIXED_IR;
-    fst = mixed ? build_mixed(c) : build_fp64(c);  // workspace and tuning happen before the capture
+    const bool measure = !(cfg->flags & FVGB_SOLVE_NO_TUNE);
+    fst = mixed ? build_mixed(c, measure) : build_fp64(c, measure);  // workspace and tuning before the capture
     if (fst != FVGB_OK) return fst;
     SolverParams prm{};
     prm.x = psi;

@@ -266,7 +266,10 @@ typedef struct fvgb_solver_cfg {
     int32_t kernel_mode;       /* 0 automatic, 1 graph of kernels, 2 one persistent
                                   cooperative kernel (FP64 single case), 3 host-driven
                                   loop (FP64; blocks the caller); same results          */
+    int32_t flags;             /* FVGB_SOLVE_NO_TUNE: default kernel variants, no timing
+                                  at the first solve (the timing synchronises the device) */
 } fvgb_solver_cfg;
+enum { FVGB_SOLVE_NO_TUNE = 1 };
 
 /* SolverStats {initResNorm, finalResNorm, numIter} (expression.hpp:155-158). */
 typedef struct fvgb_solver_stats {
