@@ -287,6 +287,7 @@ extern "C" fvgb_status fvgb_ls_create(const fvgb_mesh* mesh, int32_t ncomp, fvgb
     if (e == cudaSuccess) e = cudaMemset(ls->rhs, 0, sizeof(double) * (size_t)(n * ncomp));
     if (e == cudaSuccess) e = cudaMemset(ls->bmat, 0, sizeof(double) * (size_t)(nbf > 0 ? nbf : 1));
     if (e == cudaSuccess) e = cudaMemset(ls->brhs, 0, sizeof(double) * (size_t)(nbf > 0 ? nbf * ncomp : 1));
+    if (e == cudaSuccess) e = settle_creation();
     if (e != cudaSuccess) {
         fvgb_ls_destroy(ls);
         return cuda_fail(e, "fvgb_ls_create");

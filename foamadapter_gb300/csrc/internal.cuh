@@ -108,6 +108,14 @@ inline fvgb_status cuda_fail(cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return cuda_fail(e_, where);   \
     } while (0)
 
+// Creation paths upload with cudaMemcpy and clear with cudaMemset: both run on
+// the legacy default stream, which is not ordered with a caller's non-blocking
+// streams, and both may return before the data is in place (pageable uploads
+// return once staged; memsets are asynchronous).  They end with this wait on
+// the legacy stream only, so kernels the caller then launches on any stream
+// see the data.
+inline cudaError_t settle_creation() { return cudaStreamSynchronize(0); }
+
 // at least one block: every kernel bounds-checks its index, and a zero-block
 // launch is a configuration error (empty boundary or face sets are legal)
 inline unsigned grid_for(int64_t n, int threads) { return n > 0 ? (unsigned)((n + threads - 1) / threads) : 1u; }

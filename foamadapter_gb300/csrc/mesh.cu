@@ -270,6 +270,7 @@ extern "C" fvgb_status fvgb_mesh_create(const fvgb_mesh_desc* d, fvgb_mesh** out
     UP(v.nei_pos, nei_pos.data(), nif);
     if (e == cudaSuccess) e = upload<int32_t>(m, &m->csr_pos, csr_pos.data(), nnz);
 #undef UP
+    if (e == cudaSuccess) e = settle_creation();
     if (e != cudaSuccess) {
         free_mesh(m);
         return cuda_fail(e, "fvgb_mesh_create: upload");

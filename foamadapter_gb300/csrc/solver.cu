@@ -1590,6 +1590,7 @@ fvgb_status cache_create(const fvgb_ls* ls, int ncases, const int32_t* ranges, S
     if (e == cudaSuccess) e = calloc_dev(c, &c->pb, (size_t)c->nb);
     if (e == cudaSuccess) e = calloc_dev(c, &c->pc, (size_t)c->nb);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_stats, sizeof(fvgb_solver_stats) * (size_t)ncases);
+    if (e == cudaSuccess) e = settle_creation();
     if (e != cudaSuccess) {
         fvgb_solver_cache_free(c);
         return cuda_fail(e, "solver workspace");
@@ -1727,6 +1728,7 @@ fvgb_status build_fp64(SolverCache* c, bool measure = true) {
         if (e == cudaSuccess) e = calloc_dev(c, &c->p, n);
         if (e == cudaSuccess) e = calloc_dev(c, &c->q, n);
         if (e == cudaSuccess) e = calloc_dev(c, &c->z, n);
+        if (e == cudaSuccess) e = settle_creation();
         if (e != cudaSuccess) return cuda_fail(e, "FP64 CG workspace");
     }
     if (!c->tuned64) {
@@ -1856,6 +1858,7 @@ fvgb_status build_mixed(SolverCache* c, bool measure = true) {
         if (e == cudaSuccess) e = calloc_dev(c, &c->pf2, n);
         if (e == cudaSuccess) e = calloc_dev(c, &c->zf, n);
         if (e == cudaSuccess) e = calloc_dev(c, &c->r0, n);
+        if (e == cudaSuccess) e = settle_creation();
         if (e != cudaSuccess) return cuda_fail(e, "mixed CG workspace");
     }
     if (!c->tunedmx) {
