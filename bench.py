@@ -75,6 +75,18 @@ def aggregate_replicas(local_ms: float, local_e2e_ms: float, local_units: float,
     return float(t[0]), float(t[1]), float(u[0])
 
 
+def fp64_issue_peak():
+    """FP64 lanes per second: 2 per clock per SM (ncu's peak_sustained of the DFMA
+    counter on GB300) x SMs x the maximum SM clock of MEASURED_PEAKS.json."""
+    import torch
+
+    mhz = 2070.0
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        mhz = float(json.loads(p.read_text()).get("sm_max_mhz", mhz))
+    return 2.0 * torch.cuda.get_device_properties(0).multi_processor_count * mhz * 1e6
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -770,6 +782,10 @@ def main():
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": traffic, "alg_bytes_per_launch": ab["pcg_spmv"],
                      "kernel_ms": {"spmv": r["kt"][0], "update": r["kt"][1], "dir": r["kt"][2]},
+                     # GB300 issues FP64 at 2 lanes per clock per SM: the SpMV's DFMAs (one per
+                     # stored slot, one per row for p.Ap) bound it together with HBM
+                     "fp64_ops_per_launch": hm.nnz + hm.n,
+                     "fp64_frac_of_issue_peak": (hm.nnz + hm.n) / (r["kt"][0] * 1e-3) / fp64_issue_peak(),
                      "iteration_GBps": ab["pcg_iteration"] / (sum(r["kt"][:3]) * 1e-3) / 1e9},
         "e2e": {"value": e2e_value, "unit": "face-updates/s", "h2d_bytes_per_step": 8 * hm.n,
                 "d2h_bytes_per_step": 8 * hm.n},

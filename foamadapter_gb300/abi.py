@@ -50,7 +50,10 @@ class Term(C.Structure):
 class SolverCfg(C.Structure):
     _fields_ = [("rel_tol", dbl), ("abs_tol", dbl), ("max_iter", i32), ("precision", i32),
                 ("inner_rel_tol", dbl), ("inner_max_iter", i32), ("max_outer", i32), ("kernel_mode", i32),
-                ("flags", i32)]
+                ("flags", i32), ("method", i32)]
+
+
+SOLVER_CG, SOLVER_BICGSTAB = 0, 1
 
 
 SOLVE_NO_TUNE = 1

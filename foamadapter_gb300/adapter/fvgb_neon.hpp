@@ -337,6 +337,7 @@ struct SolverConfig {
     double innerRelTol = 0.1;
     int innerMaxIter = 1000;
     int maxOuter = 50;
+    bool bicgstab = false;  // solver "BiCGStab" (fvSolution.cpp:25-26) instead of "CG"
 };
 
 class LinearSystem {
@@ -377,7 +378,8 @@ public:
         if (needRef_) check(fvgb_set_reference(ls_.handle(), refCell_, refValue_, st));
         fvgb_solver_cfg cfg{c.relTol, c.tolerance, c.maxIter,
                             c.mixedPrecision ? FVGB_PREC_MIXED_IR : FVGB_PREC_FP64, c.innerRelTol,
-                            c.innerMaxIter, c.maxOuter};
+                            c.innerMaxIter, c.maxOuter, 0, 0,
+                            c.bicgstab ? FVGB_SOLVER_BICGSTAB : FVGB_SOLVER_CG};
         fvgb_solver_stats s{};
         fvgb_status r = fvgb_solve(ls_.handle(), psi_.internalVector().data(), &cfg, &s, st);
         if (r != FVGB_OK && r != FVGB_ERR_NOT_CONVERGED) check(r);  // non-convergence is not an error

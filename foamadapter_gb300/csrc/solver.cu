@@ -56,13 +56,14 @@ struct CaseState {
     double rz, alpha, beta, res0, res, tol;
     double rho, rho_prev, itol;
     double sres, sig, isig;     // mixed: |s r| of the latest residual; power-of-two scale of rhat and 1/scale
+    double omega;               // BiCGStab
     float falpha, fbeta, frel;  // frel: direction factor after a reliable update (-1: restart)
     int32_t iter, status, total, outer, inner_it;
     int32_t active;        // FP64: iterating; mixed: refinement loop running
     int32_t inner_active;  // mixed: inner CG running
     unsigned int counter;  // arrivals of this case's blocks
     unsigned int signflags;
-    int32_t pad;
+    int32_t half;          // BiCGStab: converged at the half step, x update pending
 };
 
 struct BatchState {
@@ -405,6 +406,258 @@ __global__ void k_set_params(Layout L, int ncases, SolverParams prm) {
         cs->signflags = 0u;
         cs->counter = 0u;
     }
+}
+
+// ------------------------------------------------------------- BiCGStab (FP64)
+// Jacobi-preconditioned BiCGStab with right preconditioning, Ginkgo's
+// solver::Bicgstab as FoamAdapter selects it (fvSolution.cpp:25-26, 106-142),
+// for nonsymmetric systems (implicit convection).  One iteration, five kernels:
+//   k_bi_dir:    p = r + beta (p - omega v), y = D^-1 p
+//   k_bi_spmv1:  v = A y, alpha = rho / (rr, v)
+//   k_bi_s:      s = r - alpha v, z = D^-1 s, |s| (converged: half step)
+//   k_bi_spmv2:  half step: x += alpha y, done; else t = A z, omega = (t,s)/(t,t)
+//   k_bi_update: x += alpha y + omega z, r = s - omega t, rho = (rr, r), |r|
+// rr is the shadow residual (the initial r).  Scalars are formed by the last
+// block of each case, every dot product by the same tree as the CG kernels.
+__global__ void __launch_bounds__(kT)
+    k_bi_init(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
+              double* __restrict__ dinv, double* __restrict__ r, double* __restrict__ rr, double* __restrict__ p,
+              double* __restrict__ v, double* __restrict__ pa, cudaGraphConditionalHandle h) {
+    __shared__ double sma[kT];
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    const double* __restrict__ x = L.bs->prm.x;
+    double arr = 0.0;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        dinv[i] = 1.0 / __ldg(&val[__ldg(&m.diag_pos[i])]);
+        const double ri = __ldg(&b[i]) - spmv_row(m, val, x, i);
+        r[i] = ri;
+        rr[i] = ri;
+        p[i] = 0.0;
+        v[i] = 0.0;
+        arr = fma(ri, ri, arr);
+    }
+    const double ba = block_tree(arr, sma);
+    if (threadIdx.x == 0) pa[blockIdx.x] = ba;
+    if (arrive_last(&cs->counter, k.nbc)) {
+        const double rr2 = final_tree(pa + k.blk0, k.nbc, sma);
+        if (threadIdx.x == 0) {
+            const SolverParams& prm = L.bs->prm;
+            const double res0 = sqrt(rr2);
+            double tol = prm.rel_tol * res0;
+            if (prm.abs_tol > tol) tol = prm.abs_tol;
+            cs->res0 = cs->res = res0;
+            cs->tol = tol;
+            cs->rho = rr2;  // (rr, r) with rr = r
+            cs->rho_prev = 1.0;
+            cs->alpha = 1.0;
+            cs->omega = 1.0;
+            cs->beta = rr2;  // (rho / 1) (1 / 1)
+            cs->half = 0;
+            bool done = !(res0 > tol) || res0 == 0.0;
+            if (!isfinite(res0)) {
+                done = true;
+                cs->status = FVGB_ERR_BREAKDOWN;
+            } else if (!done && prm.max_iter <= 0) {
+                done = true;
+                cs->status = FVGB_ERR_NOT_CONVERGED;
+            }
+            if (done) case_done(L.bs, cs);
+        }
+    }
+    if (arrive_last(&L.bs->gcounter, gridDim.x) && threadIdx.x == 0)
+        cudaGraphSetConditional(h, ld_volatile(&L.bs->n_active) > 0 ? 1u : 0u);
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bi_dir(Layout L, const double* __restrict__ dinv, const double* __restrict__ r, const double* __restrict__ v,
+             double* __restrict__ p, double* __restrict__ y) {
+    const Blk k = blk_info(L);
+    const CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->active)) return;
+    const double beta = cs->beta, omega = cs->omega;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const double pi = fma(beta, fma(-omega, __ldg(&v[i]), p[i]), __ldg(&r[i]));
+        p[i] = pi;
+        y[i] = __ldg(&dinv[i]) * pi;
+    }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bi_spmv1(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ y,
+               const double* __restrict__ rr, double* __restrict__ v, double* __restrict__ pa) {
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->active)) return;
+    __shared__ double sma[kT];
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const double vi = spmv_row(m, val, y, i);
+        v[i] = vi;
+        acc = fma(__ldg(&rr[i]), vi, acc);
+    }
+    const double ba = block_tree(acc, sma);
+    if (threadIdx.x == 0) pa[blockIdx.x] = ba;
+    if (!arrive_last(&cs->counter, k.nbc)) return;
+    const double rv = final_tree(pa + k.blk0, k.nbc, sma);
+    if (threadIdx.x == 0) {
+        const double alpha = cs->rho / rv;
+        cs->alpha = alpha;
+        if (rv == 0.0 || !isfinite(alpha)) {
+            cs->status = FVGB_ERR_BREAKDOWN;
+            case_done(L.bs, cs);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bi_s(Layout L, const double* __restrict__ dinv, const double* __restrict__ r, const double* __restrict__ v,
+           double* __restrict__ sv, double* __restrict__ z, double* __restrict__ pa) {
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->active)) return;
+    __shared__ double sma[kT];
+    const double alpha = cs->alpha;
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const double si = fma(-alpha, __ldg(&v[i]), __ldg(&r[i]));
+        sv[i] = si;
+        z[i] = __ldg(&dinv[i]) * si;
+        acc = fma(si, si, acc);
+    }
+    const double ba = block_tree(acc, sma);
+    if (threadIdx.x == 0) pa[blockIdx.x] = ba;
+    if (!arrive_last(&cs->counter, k.nbc)) return;
+    const double ss = final_tree(pa + k.blk0, k.nbc, sma);
+    if (threadIdx.x == 0) {
+        const double sres = sqrt(ss);
+        if (!isfinite(sres)) {
+            cs->res = sres;
+            cs->status = FVGB_ERR_BREAKDOWN;
+            case_done(L.bs, cs);
+        } else if (!(sres > cs->tol)) {
+            cs->res = sres;
+            cs->half = 1;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bi_spmv2(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ z,
+               const double* __restrict__ sv, const double* __restrict__ y, double* __restrict__ t,
+               double* __restrict__ pa, double* __restrict__ pb) {
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->active)) return;
+    __shared__ double sma[kT], smb[kT];
+    if (ld_volatile(&cs->half)) {  // converged at the half step: x += alpha y, done
+        double* __restrict__ x = L.bs->prm.x;
+        const double alpha = cs->alpha;
+#pragma unroll
+        for (int j = 0; j < kRowsPerThread; ++j) {
+            const int i = blk_row(k, j);
+            if (i >= k.end) continue;
+            x[i] = fma(alpha, __ldg(&y[i]), x[i]);
+        }
+        if (arrive_last(&cs->counter, k.nbc) && threadIdx.x == 0) {
+            cs->iter += 1;
+            case_done(L.bs, cs);
+        }
+        return;
+    }
+    double ats = 0.0, att = 0.0;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const double ti = spmv_row(m, val, z, i);
+        t[i] = ti;
+        ats = fma(ti, __ldg(&sv[i]), ats);
+        att = fma(ti, ti, att);
+    }
+    const double ba = block_tree(ats, sma), bb = block_tree(att, smb);
+    if (threadIdx.x == 0) {
+        pa[blockIdx.x] = ba;
+        pb[blockIdx.x] = bb;
+    }
+    if (!arrive_last(&cs->counter, k.nbc)) return;
+    const double ts = final_tree(pa + k.blk0, k.nbc, sma), tt = final_tree(pb + k.blk0, k.nbc, smb);
+    if (threadIdx.x == 0) {
+        const double omega = ts / tt;
+        cs->omega = omega;
+        if (tt == 0.0 || !isfinite(omega) || omega == 0.0) {
+            cs->status = FVGB_ERR_BREAKDOWN;
+            case_done(L.bs, cs);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bi_update(Layout L, const double* __restrict__ y, const double* __restrict__ z, const double* __restrict__ sv,
+                const double* __restrict__ t, const double* __restrict__ rr, double* __restrict__ r,
+                double* __restrict__ pa, double* __restrict__ pb, cudaGraphConditionalHandle h) {
+    __shared__ double sma[kT], smb[kT];
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (ld_volatile(&cs->active)) {
+        double* __restrict__ x = L.bs->prm.x;
+        const double alpha = cs->alpha, omega = cs->omega;
+        double arho = 0.0, arr = 0.0;
+#pragma unroll
+        for (int j = 0; j < kRowsPerThread; ++j) {
+            const int i = blk_row(k, j);
+            if (i >= k.end) continue;
+            x[i] = fma(omega, __ldg(&z[i]), fma(alpha, __ldg(&y[i]), x[i]));
+            const double ri = fma(-omega, __ldg(&t[i]), __ldg(&sv[i]));
+            r[i] = ri;
+            arho = fma(__ldg(&rr[i]), ri, arho);
+            arr = fma(ri, ri, arr);
+        }
+        const double ba = block_tree(arho, sma), bb = block_tree(arr, smb);
+        if (threadIdx.x == 0) {
+            pa[blockIdx.x] = ba;
+            pb[blockIdx.x] = bb;
+        }
+        if (arrive_last(&cs->counter, k.nbc)) {
+            const double rho = final_tree(pa + k.blk0, k.nbc, sma), rr2 = final_tree(pb + k.blk0, k.nbc, smb);
+            if (threadIdx.x == 0) {
+                const double res = sqrt(rr2);
+                cs->res = res;
+                cs->iter += 1;
+                cs->rho_prev = cs->rho;
+                cs->rho = rho;
+                cs->beta = (rho / cs->rho_prev) * (alpha / omega);
+                bool done = false;
+                if (!isfinite(res)) {
+                    cs->status = FVGB_ERR_BREAKDOWN;
+                    done = true;
+                } else if (!(res > cs->tol)) {
+                    done = true;
+                } else if (cs->iter >= L.bs->prm.max_iter) {
+                    cs->status = FVGB_ERR_NOT_CONVERGED;
+                    done = true;
+                } else if (rho == 0.0) {
+                    cs->status = FVGB_ERR_BREAKDOWN;
+                    done = true;
+                }
+                if (done) case_done(L.bs, cs);
+            }
+        }
+    }
+    if (arrive_last(&L.bs->gcounter, gridDim.x) && threadIdx.x == 0)
+        cudaGraphSetConditional(h, ld_volatile(&L.bs->n_active) > 0 ? 1u : 0u);
 }
 
 // --------------------------------------------------- mixed precision (FP32 inner)
@@ -1511,7 +1764,8 @@ struct SolverCache {
     double* pc = nullptr;
     float *ah = nullptr, *dinvf = nullptr, *ev = nullptr, *rh = nullptr, *y = nullptr, *pf = nullptr,
           *qf = nullptr;
-    cudaGraphExec_t g64 = nullptr, gmix = nullptr;
+    cudaGraphExec_t g64 = nullptr, gmix = nullptr, gbi = nullptr;
+    double *bi_rr = nullptr, *bi_v = nullptr, *bi_y = nullptr, *bi_s = nullptr, *bi_t = nullptr;  // BiCGStab
     fvgb_solver_stats* h_stats = nullptr;  // pinned [ncases]
     GridBar* bar = nullptr;
     float *pf2 = nullptr, *zf = nullptr;   // second direction buffer and z of the persistent mixed solve
@@ -1533,6 +1787,7 @@ void fvgb_solver_cache_free(SolverCache* c) {
     if (!c) return;
     if (c->g64) cudaGraphExecDestroy(c->g64);
     if (c->gmix) cudaGraphExecDestroy(c->gmix);
+    if (c->gbi) cudaGraphExecDestroy(c->gbi);
     for (void* p : c->allocs) cudaFree(p);
     if (c->h_stats) cudaFreeHost(c->h_stats);
     if (c->h_active) cudaFreeHost(c->h_active);
@@ -1868,6 +2123,66 @@ fvgb_status build_mixed(SolverCache* c, bool measure = true) {
     return graph_mixed(c);
 }
 
+// The BiCGStab solve as graph nodes in `g` after `deps` (see add_fp64_nodes).
+cudaError_t add_bicgstab_nodes(SolverCache* c, cudaGraph_t g, const cudaGraphNode_t* deps, size_t ndeps,
+                               cudaGraphNode_t* last) {
+    const fvgb_ls* ls = c->ls;
+    MeshView m = ls->mesh->v;
+    Layout L = c->L;
+    cudaGraphConditionalHandle h;
+    cudaGraphNode_t n0, n1, b0, b1, b2, b3, b4;
+    cudaGraph_t body;
+    const double* val = ls->values;
+    const double* b = ls->rhs;
+    const unsigned nb = (unsigned)c->nb;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    // r, p, z: the CG vectors; rr, v, y, s, t: BiCGStab's own
+    void* a_init[] = {&L, &m, &val, &b, &c->dinv, &c->r, &c->bi_rr, &c->p, &c->bi_v, &c->pa, &h};
+    void* a_dir[] = {&L, &c->dinv, &c->r, &c->bi_v, &c->p, &c->bi_y};
+    void* a_sp1[] = {&L, &m, &val, &c->bi_y, &c->bi_rr, &c->bi_v, &c->pa};
+    void* a_s[] = {&L, &c->dinv, &c->r, &c->bi_v, &c->bi_s, &c->z, &c->pa};
+    void* a_sp2[] = {&L, &m, &val, &c->z, &c->bi_s, &c->bi_y, &c->bi_t, &c->pa, &c->pb};
+    void* a_upd[] = {&L, &c->bi_y, &c->z, &c->bi_s, &c->bi_t, &c->bi_rr, &c->r, &c->pa, &c->pb, &h};
+    void* a_fin[] = {&L};
+    if (e == cudaSuccess) e = add_kernel_deps(g, &n0, deps, ndeps, (void*)k_bi_init, nb, kT, a_init);
+    if (e == cudaSuccess) e = add_while(g, &n1, &n0, h, &body);
+    if (e == cudaSuccess) e = add_kernel(body, &b0, nullptr, (void*)k_bi_dir, nb, kT, a_dir);
+    if (e == cudaSuccess) e = add_kernel(body, &b1, &b0, (void*)k_bi_spmv1, nb, kT, a_sp1);
+    if (e == cudaSuccess) e = add_kernel(body, &b2, &b1, (void*)k_bi_s, nb, kT, a_s);
+    if (e == cudaSuccess) e = add_kernel(body, &b3, &b2, (void*)k_bi_spmv2, nb, kT, a_sp2);
+    if (e == cudaSuccess) e = add_kernel(body, &b4, &b3, (void*)k_bi_update, nb, kT, a_upd);
+    if (e == cudaSuccess) e = add_kernel(g, last, &n1, (void*)k_finish, grid_for(c->ncases, 128), 128, a_fin);
+    return e;
+}
+
+fvgb_status build_bicgstab(SolverCache* c) {
+    const size_t n = (size_t)c->n;
+    cudaError_t e = cudaSuccess;
+    if (!c->dinv) e = calloc_dev(c, &c->dinv, n);
+    if (e == cudaSuccess && !c->r) e = calloc_dev(c, &c->r, n);
+    if (e == cudaSuccess && !c->p) e = calloc_dev(c, &c->p, n);
+    if (e == cudaSuccess && !c->z) e = calloc_dev(c, &c->z, n);
+    if (e == cudaSuccess && !c->bi_rr) e = calloc_dev(c, &c->bi_rr, n);
+    if (e == cudaSuccess && !c->bi_v) e = calloc_dev(c, &c->bi_v, n);
+    if (e == cudaSuccess && !c->bi_y) e = calloc_dev(c, &c->bi_y, n);
+    if (e == cudaSuccess && !c->bi_s) e = calloc_dev(c, &c->bi_s, n);
+    if (e == cudaSuccess && !c->bi_t) e = calloc_dev(c, &c->bi_t, n);
+    if (e == cudaSuccess) e = settle_creation();
+    if (e != cudaSuccess) return cuda_fail(e, "BiCGStab workspace");
+    if (c->gbi) {
+        cudaGraphExecDestroy(c->gbi);
+        c->gbi = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t last;
+    e = add_bicgstab_nodes(c, g, nullptr, 0, &last);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->gbi, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "BiCGStab graph");
+    return FVGB_OK;
+}
+
 fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
     FVGB_CHECK_ARG(cfg->precision == FVGB_PREC_FP64 || cfg->precision == FVGB_PREC_MIXED_IR,
                    "fvgb_solve: unknown precision");
@@ -1875,6 +2190,12 @@ fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
     FVGB_CHECK_ARG(cfg->max_iter >= 0 && cfg->max_iter <= 100000000, "fvgb_solve: bad max_iter");
     FVGB_CHECK_ARG(cfg->kernel_mode >= 0 && cfg->kernel_mode <= 3, "fvgb_solve: bad kernel_mode");
     FVGB_CHECK_ARG((cfg->flags & ~FVGB_SOLVE_NO_TUNE) == 0, "fvgb_solve: unknown flags");
+    FVGB_CHECK_ARG(cfg->method == FVGB_SOLVER_CG || cfg->method == FVGB_SOLVER_BICGSTAB, "fvgb_solve: unknown method");
+    if (cfg->method == FVGB_SOLVER_BICGSTAB) {
+        if (cfg->precision != FVGB_PREC_FP64)
+            return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_solve: BiCGStab runs in FP64 only");
+        FVGB_CHECK_ARG(cfg->kernel_mode != 3, "fvgb_solve: the host-driven loop is CG only");
+    }
     FVGB_CHECK_ARG(cfg->kernel_mode != 3 || cfg->precision == FVGB_PREC_FP64,
                    "fvgb_solve: the host-driven loop (kernel_mode 3) is FP64 only");
     if (cfg->precision == FVGB_PREC_MIXED_IR)
@@ -1952,11 +2273,15 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
     fvgb_status stt = check_cfg(cfg);
     if (stt != FVGB_OK) return stt;
     const bool measure = !(cfg->flags & FVGB_SOLVE_NO_TUNE);
-    if (cfg->precision == FVGB_PREC_FP64 && !c->g64) {
+    if (cfg->method == FVGB_SOLVER_BICGSTAB && !c->gbi) {
+        stt = build_bicgstab(c);
+        if (stt != FVGB_OK) return stt;
+    }
+    if (cfg->method == FVGB_SOLVER_CG && cfg->precision == FVGB_PREC_FP64 && !c->g64) {
         stt = build_fp64(c, measure);
         if (stt != FVGB_OK) return stt;
     }
-    if (cfg->precision == FVGB_PREC_MIXED_IR && !c->gmix) {
+    if (cfg->method == FVGB_SOLVER_CG && cfg->precision == FVGB_PREC_MIXED_IR && !c->gmix) {
         stt = build_mixed(c, measure);
         if (stt != FVGB_OK) return stt;
     }
@@ -1973,6 +2298,10 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
     if (cfg->precision == FVGB_PREC_MIXED_IR) c->converted_version = c->ls->version;
     k_set_params<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L, c->ncases, prm);
     FVGB_LAUNCH_CHECK("fvgb_solve: parameters");
+    if (cfg->method == FVGB_SOLVER_BICGSTAB) {
+        FVGB_CUDA_TRY(cudaGraphLaunch(c->gbi, s));
+        return FVGB_OK;
+    }
     if (cfg->kernel_mode == 3) return host_loop(c, s);
     if (use_persistent(c, cfg)) {
         MeshView m = c->ls->mesh->v;
@@ -2123,7 +2452,8 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
     }
     const bool mixed = cfg->precision == FVGB_PREC_MIXED_IR;
     const bool measure = !(cfg->flags & FVGB_SOLVE_NO_TUNE);
-    fst = mixed ? build_mixed(c, measure) : build_fp64(c, measure);  // workspace and tuning before the capture
+    const bool bicg = cfg->method == FVGB_SOLVER_BICGSTAB;
+    fst = bicg ? build_bicgstab(c) : (mixed ? build_mixed(c, measure) : build_fp64(c, measure));
     if (fst != FVGB_OK) return fst;
     SolverParams prm{};
     prm.x = psi;
@@ -2155,7 +2485,9 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
         size_t nd = 0;
         e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
         cudaGraphNode_t last;
-        if (e == cudaSuccess) e = mixed ? add_mixed_nodes(c, cg, deps, nd, &last) : add_fp64_nodes(c, cg, deps, nd, &last);
+        if (e == cudaSuccess)
+            e = bicg ? add_bicgstab_nodes(c, cg, deps, nd, &last)
+                     : (mixed ? add_mixed_nodes(c, cg, deps, nd, &last) : add_fp64_nodes(c, cg, deps, nd, &last));
         if (e == cudaSuccess)
             e = cudaStreamUpdateCaptureDependencies(cs, &last, nullptr, 1, cudaStreamSetCaptureDependencies);
     }

@@ -251,9 +251,10 @@ class LinearSystem:
         return v, r, bm[:hm.nbf], br[:hm.nbf * self.ncomp]
 
     def solve(self, x: torch.Tensor, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=abi.PREC_FP64,
-              inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,), kernel_mode=0):
+              inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,), kernel_mode=0,
+              method=abi.SOLVER_CG, flags=0):
         cfg = abi.SolverCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer,
-                            kernel_mode)
+                            kernel_mode, flags, method)
         st = abi.SolverStats()
         abi.check(abi.lib().fvgb_solve(self.handle, abi.ptr(x), C.byref(cfg), C.byref(st), _stream()),
                   allow=allow)
@@ -284,8 +285,10 @@ class Batch:
         self.handle = h
 
     def solve(self, x: torch.Tensor, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=abi.PREC_FP64,
-              inner_rel_tol=1e-3, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,)):
-        cfg = abi.SolverCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer)
+              inner_rel_tol=1e-3, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,),
+              method=abi.SOLVER_CG):
+        cfg = abi.SolverCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer, 0, 0,
+                            method)
         stats = (abi.SolverStats * self.ncases)()
         abi.check(abi.lib().fvgb_batch_solve(self.handle, abi.ptr(x), C.byref(cfg), stats, _stream()), allow=allow)
         return list(stats)

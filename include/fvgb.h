@@ -268,8 +268,12 @@ typedef struct fvgb_solver_cfg {
                                   loop (FP64; blocks the caller); same results          */
     int32_t flags;             /* FVGB_SOLVE_NO_TUNE: default kernel variants, no timing
                                   at the first solve (the timing synchronises the device) */
+    int32_t method;            /* FVGB_SOLVER_CG (Ginkgo Cg) or FVGB_SOLVER_BICGSTAB
+                                  (Ginkgo Bicgstab, fvSolution.cpp:25-26: nonsymmetric
+                                  systems; FP64, graph path)                             */
 } fvgb_solver_cfg;
 enum { FVGB_SOLVE_NO_TUNE = 1 };
+enum { FVGB_SOLVER_CG = 0, FVGB_SOLVER_BICGSTAB = 1 };
 
 /* SolverStats {initResNorm, finalResNorm, numIter} (expression.hpp:155-158). */
 typedef struct fvgb_solver_stats {

@@ -779,8 +779,118 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
     return status;
 }
 
+/* ------------------------------------------------------------- BiCGStab
+ * Jacobi-preconditioned BiCGStab (Ginkgo's solver::Bicgstab as FoamAdapter
+ * selects it, fvSolution.cpp:25-26, 106-142), right preconditioning, FP64,
+ * in the operation order of the GPU kernels (solver.cu BiCGStab section); every
+ * dot product by the GPU's reduction tree.
+ *   r = b - A x, rr = r, p = v = 0, rho = (rr, r), rho_prev = alpha = omega = 1
+ *   loop: beta = (rho/rho_prev)(alpha/omega); p = r + beta (p - omega v); y = D^-1 p
+ *         v = A y; alpha = rho / (rr, v); s = r - alpha v
+ *         |s| converged: x += alpha y, stop
+ *         z = D^-1 s; t = A z; omega = (t, s) / (t, t)
+ *         x += alpha y + omega z; r = s - omega t; rho_prev = rho; rho = (rr, r); |r| */
+static double dot64(int32_t n, const double* a, const double* b, double* part) {
+    int32_t nb = nblocks_of(n);
+#pragma omp parallel for schedule(static)
+    for (int32_t blk = 0; blk < nb; ++blk) {
+        double tp[RED_THREADS];
+        for (int t = 0; t < RED_THREADS; ++t) {
+            double acc = 0.0;
+            for (int j = 0; j < RED_ROWS_PER_THREAD; ++j) {
+                int32_t i = red_row(blk, t, j);
+                if (i < n) acc = fma(a[i], b[i], acc);
+            }
+            tp[t] = acc;
+        }
+        part[blk] = block_tree(tp);
+    }
+    return final_tree(nb, part);
+}
+
+static void spmv_all(const or_csr* A, const double* val, const double* x, double* out) {
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < A->n; ++i) {
+        double s;
+        spmv_row_fma(A, val, x, i, &s);
+        out[i] = s;
+    }
+}
+
+static int32_t solve_bicgstab(const or_csr* A, const double* val, const double* b, double* x,
+                              const or_solver_cfg* cfg, or_solver_stats* st) {
+    const int32_t n = A->n, nb = nblocks_of(n);
+    double *dinv = zalloc(n), *r = zalloc(n), *rr = zalloc(n), *p = zalloc(n), *v = zalloc(n);
+    double *y = zalloc(n), *s = zalloc(n), *z = zalloc(n), *t = zalloc(n), *part = zalloc(nb);
+    for (int32_t i = 0; i < n; ++i) dinv[i] = 1.0 / val[A->row_offs[i] + A->diag_off[i]];
+    spmv_all(A, val, x, t);
+    for (int32_t i = 0; i < n; ++i) {
+        r[i] = b[i] - t[i];
+        rr[i] = r[i];
+    }
+    double rho = dot64(n, rr, r, part);
+    double res0 = sqrt(dot64(n, r, r, part)), res = res0;
+    double tol = cfg->rel_tol * res0;
+    if (cfg->abs_tol > tol) tol = cfg->abs_tol;
+    double rho_prev = 1.0, alpha = 1.0, omega = 1.0;
+    int32_t it = 0, status = ST_OK;
+    int done = !(res > tol) || res == 0.0;
+    if (!isfinite(res)) { done = 1; status = ST_BREAKDOWN; }
+    else if (!done && cfg->max_iter <= 0) { done = 1; status = ST_NOT_CONVERGED; }
+    while (!done) {
+        const double beta = (rho / rho_prev) * (alpha / omega);
+        for (int32_t i = 0; i < n; ++i) {
+            p[i] = fma(beta, fma(-omega, v[i], p[i]), r[i]);
+            y[i] = dinv[i] * p[i];
+        }
+        spmv_all(A, val, y, v);
+        const double rv = dot64(n, rr, v, part);
+        alpha = rho / rv;
+        if (rv == 0.0 || !isfinite(alpha)) { status = ST_BREAKDOWN; break; }
+        for (int32_t i = 0; i < n; ++i) {
+            s[i] = fma(-alpha, v[i], r[i]);
+            z[i] = dinv[i] * s[i];
+        }
+        const double sres = sqrt(dot64(n, s, s, part));
+        if (!isfinite(sres)) { status = ST_BREAKDOWN; res = sres; break; }
+        if (!(sres > tol)) {  /* converged at the half step */
+            for (int32_t i = 0; i < n; ++i) x[i] = fma(alpha, y[i], x[i]);
+            ++it;
+            res = sres;
+            break;
+        }
+        spmv_all(A, val, z, t);
+        const double ts = dot64(n, t, s, part), tt = dot64(n, t, t, part);
+        omega = ts / tt;
+        if (tt == 0.0 || !isfinite(omega) || omega == 0.0) { status = ST_BREAKDOWN; break; }
+        for (int32_t i = 0; i < n; ++i) {
+            x[i] = fma(omega, z[i], fma(alpha, y[i], x[i]));
+            r[i] = fma(-omega, t[i], s[i]);
+        }
+        rho_prev = rho;
+        rho = dot64(n, rr, r, part);
+        res = sqrt(dot64(n, r, r, part));
+        ++it;
+        if (!isfinite(res)) { status = ST_BREAKDOWN; break; }
+        if (!(res > tol)) break;
+        if (it >= cfg->max_iter) { status = ST_NOT_CONVERGED; break; }
+        if (rho == 0.0) { status = ST_BREAKDOWN; break; }
+    }
+    st->init_res_norm = res0;
+    st->final_res_norm = res;
+    st->num_iter = it;
+    st->num_outer = 0;
+    st->status = status;
+    free(dinv); free(r); free(rr); free(p); free(v); free(y); free(s); free(z); free(t); free(part);
+    return status;
+}
+
 int32_t or_solve(const or_csr* A, const double* values, const double* rhs, double* x,
                  const or_solver_cfg* cfg, or_solver_stats* stats) {
+    if (cfg->method == 1) {
+        if (cfg->precision != 0) { stats->status = ST_UNSUPPORTED; return ST_UNSUPPORTED; }
+        return solve_bicgstab(A, values, rhs, x, cfg, stats);
+    }
     if (cfg->precision == 1) return solve_mixed(A, values, rhs, x, cfg, stats);
     return solve_fp64(A, values, rhs, x, cfg, stats);
 }

@@ -32,7 +32,8 @@ class OrTerm(C.Structure):
 
 class OrCfg(C.Structure):
     _fields_ = [("rel_tol", dbl), ("abs_tol", dbl), ("max_iter", i32), ("precision", i32),
-                ("inner_rel_tol", dbl), ("inner_max_iter", i32), ("max_outer", i32)]
+                ("inner_rel_tol", dbl), ("inner_max_iter", i32), ("max_outer", i32), ("method", i32),
+                ("pad", i32)]
 
 
 class OrStats(C.Structure):
@@ -158,8 +159,8 @@ class Oracle:
         return out
 
     def solve(self, values, rhs, x, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=0,
-              inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50):
-        cfg = OrCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer)
+              inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50, method=0):
+        cfg = OrCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer, method)
         st = OrStats()
         self.L.or_solve(C.byref(self.csr()), p(values), p(rhs), p(x), C.byref(cfg), C.byref(st))
         return st

@@ -337,3 +337,62 @@ def test_rhs_only_assembly_and_reused_fp32_matrix(cuda):
     st_b = ls2.solve(x_b, **kw)
     assert (st_a.num_iter, st_a.num_outer) == (st_b.num_iter, st_b.num_outer)
     np.testing.assert_array_equal(x_a.cpu().numpy(), x_b.cpu().numpy())
+
+
+def convection_case(nx=13, ny=11, nz=9, seed=5):
+    hm = mesh.box(nx, ny, nz, jitter=0.1, seed=seed)
+    dm = DeviceMesh(hm)
+    o = Oracle(hm)
+    rng = np.random.default_rng(seed)
+    U = np.array([1.0, 0.4, -0.2])
+    F = o.flux_vec(np.tile(U, hm.n), np.tile(U, hm.nbf))
+    bcs = [("fixedValue", 1.0)] + [("zeroGradient", 0.0)] * (hm.npatch - 1)
+    T = neon.VolumeField(dm, rng.random(hm.n), bcs)
+    ls = neon.LinearSystem(dm)
+    ls.assemble([neon.ddt(T.internal.clone()), neon.div(neon.SurfaceField(dm, F), "upwind"),
+                 neon.laplacian(neon.SurfaceField(dm, np.full(hm.nif + hm.nbf, 1e-2)), -1.0)], 0.05, T)
+    v, r, _, _ = [t.cpu().numpy() for t in ls.export()]
+    return hm, dm, T, o, ls, v, r
+
+
+def test_bicgstab_bit_exact_on_nonsymmetric_system(cuda):
+    """Implicit upwind convection makes the system nonsymmetric: BiCGStab (Ginkgo's
+    Bicgstab, fvSolution.cpp:25-26) against the oracle's restatement, bit for bit."""
+    hm, dm, T, o, ls, v, r = convection_case()
+    x = T.internal.clone()
+    st = ls.solve(x, rel_tol=1e-10, max_iter=500, method=abi.SOLVER_BICGSTAB)
+    xo = T.host().copy()
+    so = o.solve(v, r, xo, rel_tol=1e-10, max_iter=500, method=1)
+    assert st.status == so.status == abi.OK and st.num_iter == so.num_iter > 3
+    assert (st.init_res_norm, st.final_res_norm) == (so.init_res_norm, so.final_res_norm)
+    np.testing.assert_array_equal(x.cpu().numpy(), xo)
+    true = np.linalg.norm(o.apply_operator(v, r, 1, xo))
+    assert true <= 1e-9 * so.init_res_norm
+    # iteration cap and the FP64-only rule
+    st = ls.solve(T.internal.clone(), rel_tol=1e-14, max_iter=2, method=abi.SOLVER_BICGSTAB)
+    assert st.status == abi.ERR_NOT_CONVERGED and st.num_iter == 2
+    with pytest.raises(RuntimeError):
+        ls.solve(T.internal.clone(), precision=abi.PREC_MIXED_IR, method=abi.SOLVER_BICGSTAB)
+
+
+def test_bicgstab_batch_equals_alone(cuda):
+    parts = [mesh.box(7, 6, 5, jitter=0.1, seed=s) for s in (1, 2, 3)]
+    big, ranges, _ = mesh.concat(parts)
+    ranges = np.asarray(ranges, np.int32)
+    dm = DeviceMesh(big)
+    o = Oracle(big)
+    U = np.array([0.3, -1.0, 0.5])
+    F = o.flux_vec(np.tile(U, big.n), np.tile(U, big.nbf))
+    T = neon.VolumeField(dm, np.full(big.n, 0.5), [("fixedValue", 1.0)] * big.npatch)
+    ls = neon.LinearSystem(dm)
+    ls.assemble([neon.ddt(T.internal.clone()), neon.div(neon.SurfaceField(dm, F), "upwind"),
+                 neon.laplacian(neon.SurfaceField(dm, np.full(big.nif + big.nbf, 1e-2)), -1.0)], 0.1, T)
+    x = T.internal.clone()
+    stats = neon.Batch(ls, ranges).solve(x, rel_tol=1e-10, max_iter=500, method=abi.SOLVER_BICGSTAB)
+    for k in range(len(ranges) // 2):
+        lo, hi = int(ranges[2 * k]), int(ranges[2 * k + 1])
+        y = T.internal.clone()
+        s1 = neon.Batch(ls, np.asarray([lo, hi], np.int32)).solve(y, rel_tol=1e-10, max_iter=500,
+                                                                  method=abi.SOLVER_BICGSTAB)
+        assert stats[k].status == s1[0].status == abi.OK and stats[k].num_iter == s1[0].num_iter
+        np.testing.assert_array_equal(x[lo:hi].cpu().numpy(), y[lo:hi].cpu().numpy())

@@ -54,3 +54,34 @@ def test_mixed_is_exactly_scale_invariant():
     assert (s1.num_iter, s1.num_outer) == (s2.num_iter, s2.num_outer)
     assert s2.init_res_norm == s1.init_res_norm * sc and s2.final_res_norm == s1.final_res_norm * sc
     np.testing.assert_array_equal(x2, x1 * sc)
+
+
+def convection_system(nx=10, ny=9, nz=7, seed=4):
+    """ddt + implicit upwind convection - laplacian: a nonsymmetric system."""
+    hm = mesh.box(nx, ny, nz, jitter=0.1, seed=seed)
+    o = Oracle(hm)
+    rng = np.random.default_rng(seed)
+    U = np.array([1.0, 0.4, -0.2])
+    F = o.flux_vec(np.tile(U, hm.n), np.tile(U, hm.nbf))
+    gamma = np.full(hm.nif + hm.nbf, 1e-2)
+    types = np.asarray([FIXED_VALUE] + [FIXED_GRADIENT] * (hm.npatch - 1), np.int32)
+    ref = np.zeros(hm.nbf)
+    ref[hm.patch_slice("xmin")] = 1.0
+    T = rng.random(hm.n)
+    Tb = np.zeros(hm.nbf)
+    o.bc_correct(1, types, ref, T, Tb)
+    DIV = 2
+    v, r, _, _ = o.assemble(1, [(DDT, 0, 1.0, T.copy(), None), (DIV, 1, 1.0, None, F), (LAP, 0, -1.0, None, gamma)],
+                            0.05, types, ref, Tb)
+    return o, v, r, T
+
+
+def test_bicgstab_solves_nonsymmetric_system():
+    o, v, r, T = convection_system()
+    x = T.copy()
+    st = o.solve(v, r, x, rel_tol=1e-10, max_iter=500, method=1)
+    assert st.status == 0 and 0 < st.num_iter < 500
+    true = np.linalg.norm(o.apply_operator(v, r, 1, x))
+    assert true <= 1e-9 * st.init_res_norm
+    # the mixed-precision BiCGStab is not provided
+    assert o.solve(v, r, T.copy(), method=1, precision=1).status == 6
