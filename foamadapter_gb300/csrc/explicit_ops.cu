@@ -446,6 +446,26 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+template <int NC>
+__global__ void __launch_bounds__(kThreads)
+    k_fx_div_upwind(MeshView m, const double* __restrict__ flux, const double* __restrict__ phi,
+                    const double* __restrict__ phi_b, double* __restrict__ fx) {
+#pragma unroll
+    for (int k = 0; k < kFPT; ++k) {
+        const int f = face_of(k);
+        if (f < m.nif) {
+            const double F = __ldg(&flux[f]);
+            const int cu = nonneg(F) ? __ldg(&m.own[f]) : __ldg(&m.nei[f]);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) fx[f * NC + c] = F * __ldg(&phi[cu * NC + c]);
+        } else if (f < m.nif + m.nbf) {
+            const double F = __ldg(&flux[f]);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) fx[f * NC + c] = F * __ldg(&phi_b[(f - m.nif) * NC + c]);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads)
     k_fx_grad(MeshView m, const double* __restrict__ phi, const double* __restrict__ phi_b, double* __restrict__ fx) {
 #pragma unroll
@@ -529,6 +549,47 @@ __global__ void __launch_bounds__(kThreads)
     for (int k = 0; k < NC; ++k) out[c * NC + k] = out[c * NC + k] + s[k] * sc;
 }
 
+// The fused upwind advection step on a face-flux buffer: the divergence as in
+// k_gather_fx (coefficient 1), then the forward-Euler update and the boundary
+// correction of k_advect_euler.
+__global__ void __launch_bounds__(kThreads)
+    k_advect_gather(MeshView m, PatchTable pt, const double* __restrict__ fx, const double* __restrict__ Told,
+                    const double* __restrict__ Told_b, double dt, const double* __restrict__ ref,
+                    double* __restrict__ Tnew, double* __restrict__ Tnew_b) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n) return;
+    Entries e;
+    load_entries(m, c, e);
+    double v[kG];
+#pragma unroll
+    for (int j = 0; j < kG; ++j) v[j] = e.code[j] == FVGB_PAD ? 0.0 : __ldg(&fx[entry_face(e.code[j])]);
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < kG; ++j) {
+        if (e.code[j] == FVGB_PAD) break;
+        s = s + signed_term(e.code[j] >= 0, v[j]);
+    }
+    for (int j = kG; j < e.width; ++j) {
+        const int cd = __ldg(&m.g_code[e.base + j * 32]);
+        if (cd == FVGB_PAD) break;
+        s = s + signed_term(cd >= 0, __ldg(&fx[entry_face(cd)]));
+    }
+    const double dv = 0.0 + s * __ldg(&m.invV[c]);
+    const double tn = __ldg(&Told[c]) - dt * dv;
+    Tnew[c] = tn;
+    for (int j = e.width - 1; j >= 0; --j) {
+        const int code = j < kG ? e.code[j] : __ldg(&m.g_code[e.base + j * 32]);
+        if (code == FVGB_PAD) continue;
+        if (code < m.nif) break;
+        const int b = code - m.nif;
+        const int t = pt.type[__ldg(&m.bpatch[b])];
+        double bv = __ldg(&Told_b[b]);
+        if (t == FVGB_BC_FIXED_VALUE) bv = __ldg(&ref[b]);
+        else if (t == FVGB_BC_FIXED_GRADIENT) bv = tn + __ldg(&ref[b]) / __ldg(&m.bdelta[b]);
+        Tnew_b[b] = bv;
+    }
+}
+
 // Face buffer from the stream-ordered pool (no device synchronisation); the
 // pool keeps its memory between calls.  nullptr when it cannot be had: the
 // caller then runs the one-pass gather, which needs none.
@@ -599,14 +660,17 @@ extern "C" fvgb_status fvgb_div_explicit(const fvgb_mesh* m, int32_t scheme, int
     cudaStream_t s = (cudaStream_t)stream;
     const unsigned g = grid_for(m->v.n, kThreads);
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
-    double* fx = scheme == FVGB_SCHEME_LINEAR ? face_buffer((size_t)(nf * nc), s) : nullptr;
+    double* fx = face_buffer((size_t)(nf * nc), s);
     if (fx) {
         const unsigned gf = grid_for(nf, kThreads * kFPT);
+        const bool up = scheme == FVGB_SCHEME_UPWIND;
         if (nc == 1) {
-            k_fx_div_linear<1><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
+            if (up) k_fx_div_upwind<1><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
+            else k_fx_div_linear<1><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
             k_gather_fx<1><<<g, kThreads, 0, s>>>(m->v, fx, coeff, unit, out);
         } else {
-            k_fx_div_linear<3><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
+            if (up) k_fx_div_upwind<3><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
+            else k_fx_div_linear<3><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
             k_gather_fx<3><<<g, kThreads, 0, s>>>(m->v, fx, coeff, unit, out);
         }
         FVGB_LAUNCH_CHECK("fvgb_div_explicit");
@@ -695,8 +759,19 @@ extern "C" fvgb_status fvgb_advect_euler_step(const fvgb_mesh* m, const double* 
     PatchTable pt;
     FVGB_CHECK_ARG(make_patch_table(m, bc->patch_type, &pt), "fvgb_advect_euler_step: bad patch types");
     FVGB_CHECK_ARG(bc->ref || !patch_table_needs_ref(pt), "fvgb_advect_euler_step: ref is null");
-    k_advect_euler<<<grid_for(m->v.n, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
-        m->v, pt, flux, T_old, T_old_b, dt, bc->ref, T_new, T_new_b);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+    double* fx = face_buffer((size_t)nf, s);
+    if (fx) {
+        k_fx_div_upwind<1><<<grid_for(nf, kThreads * kFPT), kThreads, 0, s>>>(m->v, flux, T_old, T_old_b, fx);
+        k_advect_gather<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, fx, T_old, T_old_b, dt, bc->ref,
+                                                                          T_new, T_new_b);
+        FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
+        cudaFreeAsync(fx, s);
+        return FVGB_OK;
+    }
+    k_advect_euler<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, flux, T_old, T_old_b, dt, bc->ref,
+                                                                   T_new, T_new_b);
     FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
     return FVGB_OK;
 }
