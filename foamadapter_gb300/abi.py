@@ -126,6 +126,11 @@ _SIGS = {
     "fvgb_step_create": (C.c_int, [vp, vp, C.POINTER(Term), i32, dbl, C.POINTER(BC), vp, vp, vp,
                                    C.POINTER(SolverCfg), vp, C.POINTER(vp)]),
     "fvgb_step_launch": (C.c_int, [vp, vp]),
+    "fvgb_polymesh_read": (C.c_int, [C.c_char_p, C.POINTER(vp), vp]),
+    "fvgb_polymesh_patch": (C.c_int, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p)]),
+    "fvgb_polymesh_free": (C.c_int, [vp]),
+    "fvgb_field_read": (C.c_int, [C.c_char_p, i32, vp]),
+    "fvgb_field_write": (C.c_int, [C.c_char_p, C.c_char_p, vp, vp, vp]),
     "fvgb_step_destroy": (C.c_int, [vp]),
     "fvgb_batch_create": (C.c_int, [vp, i32, vp, C.POINTER(vp)]),
     "fvgb_batch_destroy": (C.c_int, [vp]),

@@ -495,6 +495,27 @@ fvgb_status fvgb_geometry_compute(int32_t n_points, const double* points, int32_
                                   int32_t n_ifaces, const int32_t* neighbour,
                                   int32_t n_bfaces, fvgb_mesh_arrays* out);
 
+/* ------------------------------------------------------- OpenFOAM files (HOST)
+ * The steps before and after the hot path: FoamAdapter's MeshAdapter builds the
+ * mesh from Foam::fvMesh (meshAdapter.cpp:59-136) and writers.cpp:9-135 write
+ * NeoN fields as OpenFOAM fields.  ASCII format; binary files are reported as
+ * FVGB_ERR_UNSUPPORTED. */
+typedef struct fvgb_polymesh fvgb_polymesh;
+/* Read `dir` (a constant/polyMesh directory: points, faces, owner, neighbour,
+ * boundary) and compute its geometry (as fvgb_geometry_compute); *desc points
+ * into arrays owned by *out until fvgb_polymesh_free. */
+fvgb_status fvgb_polymesh_read(const char* dir, fvgb_polymesh** out, fvgb_mesh_desc* desc);
+/* Name and type of non-empty patch p, as written in `boundary` (valid until free). */
+fvgb_status fvgb_polymesh_patch(const fvgb_polymesh* pm, int32_t p, const char** name, const char** type);
+fvgb_status fvgb_polymesh_free(fvgb_polymesh* pm);
+/* internalField of a volScalarField file (uniform or nonuniform List<scalar>) into values[n]. */
+fvgb_status fvgb_field_read(const char* path, int32_t n, double* values);
+/* Write a volScalarField: internalField [n_cells], boundaryField with a
+ * calculated value per non-empty patch from boundary [n_bfaces] (flat, patch
+ * order) and type empty for empty patches; 17 significant digits. */
+fvgb_status fvgb_field_write(const char* path, const char* object, const fvgb_polymesh* pm,
+                             const double* internal, const double* boundary);
+
 #ifdef __cplusplus
 }
 #endif
