@@ -79,6 +79,7 @@ class ServeRequest(C.Structure):
 
 
 SERVE_REASSEMBLE = 1
+IO_BINARY, IO_SURFACE = 1, 2
 
 
 class ServeResult(C.Structure):
@@ -128,9 +129,11 @@ _SIGS = {
     "fvgb_step_launch": (C.c_int, [vp, vp]),
     "fvgb_polymesh_read": (C.c_int, [C.c_char_p, C.POINTER(vp), vp]),
     "fvgb_polymesh_patch": (C.c_int, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p)]),
+    "fvgb_polymesh_geometry": (C.c_int, [vp, C.POINTER(i32), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
     "fvgb_polymesh_free": (C.c_int, [vp]),
-    "fvgb_field_read": (C.c_int, [C.c_char_p, i32, vp]),
-    "fvgb_field_write": (C.c_int, [C.c_char_p, C.c_char_p, vp, vp, vp]),
+    "fvgb_field_read": (C.c_int, [C.c_char_p, i32, i32, vp]),
+    "fvgb_field_read_bc": (C.c_int, [C.c_char_p, vp, i32, vp, vp, vp]),
+    "fvgb_field_write": (C.c_int, [C.c_char_p, C.c_char_p, vp, i32, vp, vp, i32]),
     "fvgb_step_destroy": (C.c_int, [vp]),
     "fvgb_batch_create": (C.c_int, [vp, i32, vp, C.POINTER(vp)]),
     "fvgb_batch_destroy": (C.c_int, [vp]),

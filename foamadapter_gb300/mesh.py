@@ -141,6 +141,86 @@ def from_polymesh(points: np.ndarray, faces: list, owner: np.ndarray, neighbour:
     return _to_host(a, n_cells, nif, nbf, len(names), names), np.asarray(order, np.int64)
 
 
+def _copy(ptr, count: int, ctype=C.c_double) -> np.ndarray:
+    if count == 0:
+        return np.zeros(0, np.float64 if ctype is C.c_double else np.int32)
+    return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ctype)), shape=(count,)).copy()
+
+
+class PolyMesh:
+    """An OpenFOAM case mesh read from its constant/polyMesh directory
+    (fvgb_polymesh_read, ascii or binary), with the field files that belong to it.
+
+    ``host`` is the HostMesh MeshAdapter would build from the Foam::fvMesh
+    (meshAdapter.cpp:59-136); ``patch_types`` are the polyMesh patch types of
+    the non-empty patches.  Field files: ``read_field`` (internalField),
+    ``read_bc`` (boundaryField mapped as readers.hpp:43-95) and ``write_field``
+    (writers.cpp:9-135: calculated patches, empty patches kept).
+    """
+
+    def __init__(self, directory):
+        L = abi.lib()
+        self.handle = C.c_void_p()
+        d = abi.MeshDesc()
+        abi.check(L.fvgb_polymesh_read(str(directory).encode(), C.byref(self.handle), C.byref(d)))
+        n, nif, nbf, npatch = d.n_cells, d.n_ifaces, d.n_bfaces, d.n_patches
+        names, types = [], []
+        for p in range(npatch):
+            nm, ty = C.c_char_p(), C.c_char_p()
+            abi.check(L.fvgb_polymesh_patch(self.handle, p, C.byref(nm), C.byref(ty)))
+            names.append(nm.value.decode())
+            types.append(ty.value.decode())
+        npts, pts, cf, bcf = C.c_int32(), C.c_void_p(), C.c_void_p(), C.c_void_p()
+        abi.check(L.fvgb_polymesh_geometry(self.handle, C.byref(npts), C.byref(pts), C.byref(cf), C.byref(bcf)))
+        i32 = C.c_int32
+        self.host = HostMesh(
+            n=n, nif=nif, nbf=nbf, npatch=npatch, V=_copy(d.cell_volumes, n),
+            C=_copy(d.cell_centres, 3 * n).reshape(-1, 3), own=_copy(d.owner, nif, i32),
+            nei=_copy(d.neighbour, nif, i32), Sf=_copy(d.face_areas, 3 * nif).reshape(-1, 3),
+            Cf=_copy(cf, 3 * nif).reshape(-1, 3), magSf=_copy(d.mag_face_areas, nif), w=_copy(d.weights, nif),
+            delta=_copy(d.delta_coeffs, nif), bcells=_copy(d.bface_cells, nbf, i32),
+            bSf=_copy(d.bface_areas, 3 * nbf).reshape(-1, 3), bCf=_copy(bcf, 3 * nbf).reshape(-1, 3),
+            bmagSf=_copy(d.bmag_face_areas, nbf), bw=_copy(d.bweights, nbf), bdelta=_copy(d.bdelta_coeffs, nbf),
+            patch_offsets=_copy(d.patch_offsets, npatch + 1, i32), patch_names=names,
+            points=_copy(pts, 3 * npts.value).reshape(-1, 3))
+        self.patch_types = types
+
+    def read_field(self, path, ncomp: int = 1, surface: bool = False) -> np.ndarray:
+        """internalField values, [n] or [n, 3] (n = cells, or internal faces for a surface field)."""
+        n = self.host.nif if surface else self.host.n
+        out = np.zeros(n * ncomp)
+        abi.check(abi.lib().fvgb_field_read(str(path).encode(), n, ncomp, abi.ptr(out)))
+        return out if ncomp == 1 else out.reshape(n, ncomp)
+
+    def read_bc(self, path, ncomp: int = 1):
+        """(patch types [npatch] as fvgb_bc_type, ref [nbf*ncomp], boundary values [nbf*ncomp])."""
+        h = self.host
+        types = np.zeros(max(1, h.npatch), np.int32)
+        ref, bval = np.zeros(max(1, h.nbf * ncomp)), np.zeros(max(1, h.nbf * ncomp))
+        abi.check(abi.lib().fvgb_field_read_bc(str(path).encode(), self.handle, ncomp, abi.ptr(types),
+                                               abi.ptr(ref), abi.ptr(bval)))
+        return types[:h.npatch], ref[:h.nbf * ncomp], bval[:h.nbf * ncomp]
+
+    def write_field(self, path, obj: str, internal, boundary, ncomp: int = 1, surface: bool = False,
+                    binary: bool = False):
+        internal = np.ascontiguousarray(internal, np.float64).reshape(-1)
+        boundary = np.ascontiguousarray(boundary, np.float64).reshape(-1)
+        flags = (abi.IO_BINARY if binary else 0) | (abi.IO_SURFACE if surface else 0)
+        abi.check(abi.lib().fvgb_field_write(str(path).encode(), obj.encode(), self.handle, ncomp,
+                                             abi.ptr(internal), abi.ptr(boundary), flags))
+
+    def close(self):
+        if self.handle:
+            abi.lib().fvgb_polymesh_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def concat(meshes: list, align: int = 32) -> tuple[HostMesh, np.ndarray, list]:
     """Pack independent meshes into one block-diagonal mesh.
 

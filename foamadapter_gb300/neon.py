@@ -19,7 +19,7 @@ import numpy as np
 import torch
 
 from . import abi
-from .mesh import DeviceMesh, HostMesh
+from .mesh import DeviceMesh, HostMesh, PolyMesh
 
 _SCHEMES = {"linear": abi.SCHEME_LINEAR, "upwind": abi.SCHEME_UPWIND}
 _BC = {"calculated": abi.BC_CALCULATED, "fixedValue": abi.BC_FIXED_VALUE,
@@ -82,6 +82,30 @@ class VolumeField:
 
     def host(self):
         return self.internal.cpu().numpy()
+
+
+_BC_NAME = {abi.BC_CALCULATED: "calculated", abi.BC_FIXED_VALUE: "fixedValue",
+            abi.BC_FIXED_GRADIENT: "fixedGradient"}
+
+
+def read_vol_field(mesh: DeviceMesh, poly: PolyMesh, path, ncomp: int = 1, name: str = "") -> VolumeField:
+    """A VolumeField from an OpenFOAM field file: its internalField and the
+    boundary conditions of its boundaryField, as FoamAdapter's constructFrom
+    builds one (readers.hpp:110-126, the mapping of readers.hpp:43-95)."""
+    internal = poly.read_field(path, ncomp)
+    types, ref, _ = poly.read_bc(path, ncomp)
+    hm = mesh.host
+    bcs = [(_BC_NAME[int(t)], ref[int(hm.patch_offsets[p]) * ncomp:int(hm.patch_offsets[p + 1]) * ncomp])
+           for p, t in enumerate(types)]
+    return VolumeField(mesh, internal, bcs, ncomp=ncomp, name=name)
+
+
+def write(field: VolumeField, poly: PolyMesh, path, binary: bool = False):
+    """Write a VolumeField as an OpenFOAM field file with calculated patches
+    holding its boundary values (writers.cpp:67-135)."""
+    nb = field.mesh.nbf * field.ncomp
+    poly.write_field(path, field.name or str(path).rsplit("/", 1)[-1], field.host(),
+                     field.boundary.cpu().numpy()[:nb], ncomp=field.ncomp, binary=binary)
 
 
 class SurfaceField:

@@ -497,24 +497,49 @@ fvgb_status fvgb_geometry_compute(int32_t n_points, const double* points, int32_
 
 /* ------------------------------------------------------- OpenFOAM files (HOST)
  * The steps before and after the hot path: FoamAdapter's MeshAdapter builds the
- * mesh from Foam::fvMesh (meshAdapter.cpp:59-136) and writers.cpp:9-135 write
- * NeoN fields as OpenFOAM fields.  ASCII format; binary files are reported as
- * FVGB_ERR_UNSUPPORTED. */
+ * mesh from Foam::fvMesh (meshAdapter.cpp:59-136), readVolBoundaryConditions
+ * maps a field's boundaryField to boundary conditions (readers.hpp:31-108) and
+ * writers.cpp:9-135 write NeoN fields as OpenFOAM fields.  Ascii and binary
+ * formats (binary: little-endian, 32/64-bit labels and scalars as the header's
+ * arch declares).  Not thread-safe per handle; no device memory is touched. */
 typedef struct fvgb_polymesh fvgb_polymesh;
+enum { FVGB_IO_BINARY = 1, FVGB_IO_SURFACE = 2 };
 /* Read `dir` (a constant/polyMesh directory: points, faces, owner, neighbour,
  * boundary) and compute its geometry (as fvgb_geometry_compute); *desc points
- * into arrays owned by *out until fvgb_polymesh_free. */
+ * into arrays owned by *out until fvgb_polymesh_free.  Faces are ordered
+ * internal first, then the non-empty patches in file order; empty patches are
+ * left out of the flat boundary (fvPatch sizes them 0). */
 fvgb_status fvgb_polymesh_read(const char* dir, fvgb_polymesh** out, fvgb_mesh_desc* desc);
 /* Name and type of non-empty patch p, as written in `boundary` (valid until free). */
 fvgb_status fvgb_polymesh_patch(const fvgb_polymesh* pm, int32_t p, const char** name, const char** type);
+/* The points [n_points*3] and the internal [n_ifaces*3] and boundary
+ * [n_bfaces*3] face centres (valid until free). */
+fvgb_status fvgb_polymesh_geometry(const fvgb_polymesh* pm, int32_t* n_points, const double** points,
+                                   const double** face_centres, const double** bface_centres);
 fvgb_status fvgb_polymesh_free(fvgb_polymesh* pm);
-/* internalField of a volScalarField file (uniform or nonuniform List<scalar>) into values[n]. */
-fvgb_status fvgb_field_read(const char* path, int32_t n, double* values);
-/* Write a volScalarField: internalField [n_cells], boundaryField with a
- * calculated value per non-empty patch from boundary [n_bfaces] (flat, patch
- * order) and type empty for empty patches; 17 significant digits. */
-fvgb_status fvgb_field_write(const char* path, const char* object, const fvgb_polymesh* pm,
-                             const double* internal, const double* boundary);
+/* internalField of a field file into values[n*ncomp] (ncomp 1: List<scalar>,
+ * 3: List<vector>; uniform or nonuniform).  n is n_cells for a volume field,
+ * n_ifaces for a surface field. */
+fvgb_status fvgb_field_read(const char* path, int32_t n, int32_t ncomp, double* values);
+/* boundaryField of a field file as boundary conditions of the non-empty
+ * patches of pm, by patch name, then patch group, then quoted regular
+ * expression: patch_type[n_patches] (fvgb_bc_type) and ref[n_bfaces*ncomp]
+ * (host; what fvgb_bc.ref holds on the device).  Mapping (readers.hpp:43-95):
+ * fixedValue -> FIXED_VALUE with its value; zeroGradient -> FIXED_GRADIENT 0;
+ * fixedGradient -> FIXED_GRADIENT with the patch's `value` entry as the
+ * reference takes it; noSlip -> FIXED_VALUE 0; calculated and
+ * extrapolatedCalculated -> CALCULATED; any other type FVGB_ERR_UNSUPPORTED.
+ * boundary[n_bfaces*ncomp] (may be NULL) receives each patch's `value` entry
+ * where it has one, else 0. */
+fvgb_status fvgb_field_read_bc(const char* path, const fvgb_polymesh* pm, int32_t ncomp, int32_t* patch_type,
+                               double* ref, double* boundary);
+/* Write a field file: internalField [n*ncomp] (n = n_cells, or n_ifaces with
+ * FVGB_IO_SURFACE), boundaryField with a calculated value per non-empty patch
+ * from boundary [n_bfaces*ncomp] (flat, patch order) and type empty for empty
+ * patches.  Ascii uses 17 significant digits (every double round-trips);
+ * FVGB_IO_BINARY writes the lists as raw little-endian doubles. */
+fvgb_status fvgb_field_write(const char* path, const char* object, const fvgb_polymesh* pm, int32_t ncomp,
+                             const double* internal, const double* boundary, int32_t flags);
 
 #ifdef __cplusplus
 }

@@ -40,6 +40,17 @@ def load_polymesh(case: str):
     return hm, d
 
 
+def unpack_reference_files(root):
+    """The reference's committed OpenFOAM case files (foam_files.npz), as they
+    were, under root/<case>/..."""
+    d = np.load(GOLDEN / "foam_files.npz")
+    for key in d.files:
+        p = root / key.replace("__", "/")
+        p.parent.mkdir(parents=True, exist_ok=True)
+        p.write_bytes(d[key].tobytes())
+    return root
+
+
 @pytest.fixture(scope="session")
 def cuda():
     import torch

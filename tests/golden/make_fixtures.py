@@ -4,6 +4,9 @@ Reads the ascii OpenFOAM cases under the reference checkout's ``test/`` tree
 (polyMesh points/faces/owner/neighbour/boundary and the field files of
 ``test/setup_operator/0``) and writes them as small ``.npz`` files next to this
 script, so that the tests run where the reference checkout is absent.
+``foam_files.npz`` keeps the unparsed bytes of the small polyMesh and field
+files (key: the path with "/" written as "__"), the input of the tests of the
+library's own OpenFOAM file reader.
 Run:  python tests/golden/make_fixtures.py [/path/to/reference]
 """
 from __future__ import annotations
@@ -102,6 +105,16 @@ def main(ref: Path):
                 arrays["field_" + name] = read_internal_field(z / name)
         np.savez_compressed(HERE / f"{case}.npz", **arrays)
         print(case, {k: v.shape for k, v in arrays.items()})
+    files = {}
+    for case in CASES[:3]:
+        for name in ("points", "faces", "owner", "neighbour", "boundary"):
+            files[f"{case}/constant/polyMesh/{name}"] = None
+    for rel in ("setup_operator/0/T", "setup_operator/0/U", "setup_operator/0/phi", "setup_operator/0/divT_Serial",
+                "setup_operator/0/gradT_Serial", "setup_stencil3D/0/T", "setup_unstructuredMesh/0/T"):
+        files[rel] = None
+    raw = {k.replace("/", "__"): np.frombuffer((ref / "test" / k).read_bytes(), np.uint8) for k in files}
+    np.savez_compressed(HERE / "foam_files.npz", **raw)
+    print("foam_files", {k: v.size for k, v in raw.items()})
 
 
 if __name__ == "__main__":

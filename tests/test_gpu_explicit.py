@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import load_polymesh
+from conftest import load_polymesh, unpack_reference_files
 from foamadapter_gb300 import abi, mesh, neon
 from foamadapter_gb300.mesh import DeviceMesh
 from oracle.pyoracle import Oracle
@@ -102,6 +102,33 @@ def test_golden_div_grad_on_gpu(cuda):
     assert np.max(np.abs(out.cpu().numpy() - g)) / np.abs(g).max() < 2e-15
     grad = neon.GaussGreenGrad(dm).grad(T).cpu().numpy().reshape(-1, 3)
     np.testing.assert_allclose(grad, d["field_gradT_Serial"], rtol=0, atol=1e-15 * np.abs(grad).max())
+
+
+def test_golden_case_from_openfoam_files(cuda, tmp_path):
+    """The same case read from the reference's own OpenFOAM files (polyMesh,
+    0/T with its zeroGradient walls, 0/phi), the result written as field files
+    (ascii and binary) and read back bit for bit."""
+    root = unpack_reference_files(tmp_path)
+    pm = mesh.PolyMesh(root / "setup_operator" / "constant" / "polyMesh")
+    case = root / "setup_operator" / "0"
+    dm = DeviceMesh(pm.host)
+    T = neon.read_vol_field(dm, pm, case / "T", name="T")
+    _, _, phib = pm.read_bc(case / "phi")
+    flux = np.concatenate([pm.read_field(case / "phi", surface=True), phib])
+    div = neon.VolumeField(dm, np.zeros(pm.host.n), name="divT")
+    neon.GaussGreenDiv(dm, ("Gauss", "linear")).div(div.internal, neon.SurfaceField(dm, flux), T, 1.0)
+    _, d = load_polymesh("setup_operator")
+    g = d["field_divT_Serial"]
+    assert np.max(np.abs(div.host() - g)) / np.abs(g).max() < 2e-15
+    grad = neon.GaussGreenGrad(dm).grad(T).cpu().numpy()
+    np.testing.assert_allclose(grad.reshape(-1, 3), d["field_gradT_Serial"], rtol=0,
+                               atol=1e-15 * np.abs(grad).max())
+    div.correctBoundaryConditions()
+    for binary in (False, True):
+        neon.write(div, pm, tmp_path / "divT", binary=binary)
+        np.testing.assert_array_equal(pm.read_field(tmp_path / "divT"), div.host())
+        back = neon.read_vol_field(dm, pm, tmp_path / "divT")
+        np.testing.assert_array_equal(back.boundary.cpu().numpy(), div.boundary.cpu().numpy())
 
 
 def advection_case(n=64):
