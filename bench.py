@@ -400,6 +400,7 @@ def run_explicit(args):
     fp64 = {"interp_linear": 3 * nif, "interp_upwind": 0, "div_upwind": 3 * nif + 2 * nbf + 2 * n,
             "div_linear": 6 * nif + 2 * nbf + 2 * n, "grad": 12 * nif + 6 * nbf + 6 * n,
             "laplacian": 5 * nif + 4 * nbf + 2 * n, "sngrad": 2 * (nif + nbf),
+            "laplacian_corrected": 34 * nif + 10 * nbf + 8 * n,
             "advect_euler": 3 * nif + 2 * nbf + 4 * n}
     sm_mhz = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("sm_max_mhz", 2070.0) \
         if (ROOT / "MEASURED_PEAKS.json").exists() else 2070.0
@@ -419,6 +420,11 @@ def run_explicit(args):
                       24 * nif + 28 * nbfa + 24 * n),
         "sngrad": (lambda: L.fvgb_sngrad(h, P(T.internal), P(T.boundary), P(fout), s),
                    24 * nif + 8 * n + 28 * nbf),
+        # Gauss linear corrected: the laplacian's arrays, the gradient's (Sf, w, Sf_b, T_b),
+        # the correction vectors and |Sf|, and the cell gradient written and read once
+        "laplacian_corrected": (lambda: L.fvgb_laplacian_explicit_corrected(h, 1, P(gamma), P(T.internal),
+                                                                           P(T.boundary), 1.0, P(out), s),
+                                88 * nif + 28 * nbfa + 32 * nbf + 72 * n),
         "advect_euler": (lambda: L.fvgb_advect_euler_step(h, P(F), P(T.internal), P(T.boundary), 1e-3, C.byref(bc),
                                                           P(T2), P(Tb2), s),
                          16 * nif + 12 * nbfa + 24 * n),

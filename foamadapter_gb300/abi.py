@@ -18,7 +18,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfvgb.so"
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_CUDA, ERR_UNSUPPORTED, \
     ERR_BUDGET, ERR_CANCELLED = range(9)
 BC_CALCULATED, BC_FIXED_VALUE, BC_FIXED_GRADIENT = 0, 1, 2
-SCHEME_LINEAR, SCHEME_UPWIND = 0, 1
+SCHEME_LINEAR, SCHEME_UPWIND, SCHEME_CORRECTED = 0, 1, 2
 TERM_DDT, TERM_LAPLACIAN, TERM_DIV, TERM_SOURCE, TERM_EXPLICIT, TERM_DIV_FLUX, TERM_DIV_EXPLICIT = range(7)
 PREC_FP64, PREC_MIXED_IR = 0, 1
 
@@ -111,6 +111,9 @@ _SIGS = {
     "fvgb_grad": (C.c_int, [vp, vp, vp, dbl, vp, vp]),
     "fvgb_laplacian_explicit": (C.c_int, [vp, i32, vp, vp, vp, dbl, vp, vp]),
     "fvgb_sngrad": (C.c_int, [vp, vp, vp, vp, vp]),
+    "fvgb_laplacian_explicit_corrected": (C.c_int, [vp, i32, vp, vp, vp, dbl, vp, vp]),
+    "fvgb_sngrad_corrected": (C.c_int, [vp, vp, vp, vp, vp]),
+    "fvgb_nonorth_flux": (C.c_int, [vp, i32, vp, vp, vp, dbl, vp, vp]),
     "fvgb_advect_euler_step": (C.c_int, [vp, vp, vp, vp, dbl, C.POINTER(BC), vp, vp, vp]),
     "fvgb_ls_create": (C.c_int, [vp, i32, C.POINTER(vp)]),
     "fvgb_ls_destroy": (C.c_int, [vp]),
@@ -146,6 +149,8 @@ _SIGS = {
     "fvgb_flux_vec": (C.c_int, [vp, vp, vp, vp, vp]),
     "fvgb_piso_face_update": (C.c_int, [vp, vp, vp, vp, vp]),
     "fvgb_piso_velocity_update": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
+    "fvgb_piso_ddt_corr": (C.c_int, [vp, vp, vp, vp, vp, vp, dbl, vp, vp]),
+    "fvgb_piso_constrain_pressure": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
     "fvgb_server_create": (C.c_int, [C.POINTER(ServerCfg), C.POINTER(vp)]),
     "fvgb_server_submit": (C.c_int, [vp, C.POINTER(ServeRequest), P_i64]),
     "fvgb_server_cancel": (C.c_int, [vp, i64]),

@@ -52,14 +52,24 @@ class Advection:
 
 
 class CavityPiso:
-    """Lid-driven cavity, neoIcoFoam PISO (no momentum predictor, no
-    non-orthogonal correctors), pressure reference cell 0 = 0."""
+    """Lid-driven cavity, neoIcoFoam PISO (no momentum predictor), pressure
+    reference cell 0 = 0.
+
+    The defaults are the reference's loop.  ``ddt_corr`` adds
+    fvc::interpolate(rAU)*fvc::ddtCorr(U, phi) to phiHbyA, ``corrected`` makes
+    laplacian(rAUf, p) `Gauss linear corrected` (its face-flux correction, taken
+    with the pressure the matrix was assembled with, enters the new face flux
+    as in pEqn.flux()), and ``n_non_orth`` runs that many extra non-orthogonal
+    pressure correctors: icoFoam's loop, which neoIcoFoam.cpp:127-137 leaves as
+    TODOs."""
 
     def __init__(self, n=512, jitter=0.05, seed=12345, nu=0.01, dt=5e-4, n_corr=2, lid=(1.0, 0.0, 0.0),
-                 precision=abi.PREC_FP64, p_rel_tol=1e-8, p_max_iter=20000, inner_rel_tol=0.1):
+                 precision=abi.PREC_FP64, p_rel_tol=1e-8, p_max_iter=20000, inner_rel_tol=0.1,
+                 ddt_corr=False, corrected=False, n_non_orth=0):
         self.hm = hm = mesh.box(n, n, 1, 1.0, 1.0, 1.0 / n, jitter=jitter, seed=seed, two_d=True)
         self.dm = dm = DeviceMesh(hm)
         self.dt, self.n_corr = dt, n_corr
+        self.ddt_corr, self.corrected, self.n_non_orth = ddt_corr, corrected, n_non_orth
         self.cfg = abi.SolverCfg(p_rel_tol, 0.0, p_max_iter, precision, inner_rel_tol, 2000, 50)
         ubcs = [("noSlip", 0.0), ("noSlip", 0.0), ("noSlip", 0.0), ("fixedValue", list(lid))]
         self.U = neon.VolumeField(dm, np.zeros(3 * hm.n), ubcs, ncomp=3, name="U")
@@ -76,6 +86,10 @@ class CavityPiso:
         self.phiHbyA = neon.SurfaceField(dm)
         self.assignable = np.zeros(hm.npatch, np.int32)   # every U patch is a fixed value
         self.stats = []
+        self.phi_old = torch.zeros_like(self.phi.values)
+        self.U_old_b = torch.zeros_like(self.U.boundary)
+        self.p_pre = torch.zeros_like(self.p.internal)
+        self.pb_pre = torch.zeros_like(self.p.boundary)
         L, dmh = abi.lib(), dm.handle
         abi.check(L.fvgb_flux_vec(dmh, abi.ptr(self.U.internal), abi.ptr(self.U.boundary), abi.ptr(self.phi.values),
                                   _s()))
@@ -83,6 +97,9 @@ class CavityPiso:
     def step(self):
         L, dmh, s = abi.lib(), self.dm.handle, _s()
         self.U_old.copy_(self.U.internal)
+        if self.ddt_corr:
+            self.U_old_b.copy_(self.U.boundary)
+            self.phi_old.copy_(self.phi.values)
         self.UEqn.assemble([neon.ddt(self.U_old), neon.div(self.phi, "linear"), neon.laplacian(self.nu, -1.0)],
                            self.dt, self.U)
         for _ in range(self.n_corr):
@@ -96,15 +113,30 @@ class CavityPiso:
                                            abi.ptr(self.rAUf.values), s))
             abi.check(L.fvgb_flux_vec(dmh, abi.ptr(self.HbyA.internal), abi.ptr(self.HbyA.boundary),
                                       abi.ptr(self.phiHbyA.values), s))
-            self.pEqn.assemble([neon.laplacian(self.rAUf), neon.div_flux(self.phiHbyA, -1.0)], self.dt, self.p)
-            self.pEqn.setReference(0, 0.0)
-            st = abi.SolverStats()
-            r = L.fvgb_solve(self.pEqn.handle, abi.ptr(self.p.internal), C.byref(self.cfg), C.byref(st), s)
-            abi.check(r, allow=(abi.ERR_NOT_CONVERGED,))
-            self.stats.append((st.num_iter, st.num_outer, st.init_res_norm, st.final_res_norm, st.status))
-            self.p.correctBoundaryConditions()
-            abi.check(L.fvgb_piso_face_update(self.pEqn.handle, abi.ptr(self.phiHbyA.values), abi.ptr(self.p.internal),
-                                              abi.ptr(self.phi.values), s))
+            if self.ddt_corr:
+                abi.check(L.fvgb_piso_ddt_corr(dmh, abi.ptr(self.U.types), abi.ptr(self.U_old),
+                                               abi.ptr(self.U_old_b), abi.ptr(self.phi_old),
+                                               abi.ptr(self.rAUf.values), self.dt, abi.ptr(self.phiHbyA.values), s))
+            for k in range(self.n_non_orth + 1):
+                final = k == self.n_non_orth
+                lap = neon.laplacian(self.rAUf, 1.0, "corrected" if self.corrected else "uncorrected",
+                                     field=self.p.internal)
+                self.pEqn.assemble([lap, neon.div_flux(self.phiHbyA, -1.0)], self.dt, self.p)
+                self.pEqn.setReference(0, 0.0)
+                if final and self.corrected:
+                    self.p_pre.copy_(self.p.internal)
+                    self.pb_pre.copy_(self.p.boundary)
+                st = abi.SolverStats()
+                r = L.fvgb_solve(self.pEqn.handle, abi.ptr(self.p.internal), C.byref(self.cfg), C.byref(st), s)
+                abi.check(r, allow=(abi.ERR_NOT_CONVERGED,))
+                self.stats.append((st.num_iter, st.num_outer, st.init_res_norm, st.final_res_norm, st.status))
+                self.p.correctBoundaryConditions()
+                if final:
+                    abi.check(L.fvgb_piso_face_update(self.pEqn.handle, abi.ptr(self.phiHbyA.values),
+                                                      abi.ptr(self.p.internal), abi.ptr(self.phi.values), s))
+                    if self.corrected:
+                        abi.check(L.fvgb_nonorth_flux(dmh, 1, abi.ptr(self.rAUf.values), abi.ptr(self.p_pre),
+                                                      abi.ptr(self.pb_pre), -1.0, abi.ptr(self.phi.values), s))
             abi.check(L.fvgb_piso_velocity_update(dmh, abi.ptr(self.HbyA.internal), abi.ptr(self.rAU.internal),
                                                   abi.ptr(self.p.internal), abi.ptr(self.p.boundary),
                                                   abi.ptr(self.U.internal), s))

@@ -338,6 +338,14 @@ fvgb_status assemble(fvgb_ls* ls, const fvgb_term* terms, int32_t nterms, double
             FVGB_CHECK_ARG(t.face, "fvgb_assemble: laplacian/div need a surface field");
             needs_b = true;
         }
+        if (t.kind == FVGB_TERM_LAPLACIAN) {
+            FVGB_CHECK_ARG(t.scheme == 0 || t.scheme == FVGB_SCHEME_CORRECTED, "fvgb_assemble: unknown laplacian scheme");
+            if (t.scheme == FVGB_SCHEME_CORRECTED) {
+                FVGB_CHECK_ARG(t.cell, "fvgb_assemble: a corrected laplacian needs the current field");
+                FVGB_CHECK_ARG(m->v.corr || m->v.nif == 0,
+                               "fvgb_assemble: corrected laplacian on a mesh created without cell centres");
+            }
+        }
         if (t.kind == FVGB_TERM_DIV)
             FVGB_CHECK_ARG(t.scheme == FVGB_SCHEME_LINEAR || t.scheme == FVGB_SCHEME_UPWIND,
                            "fvgb_assemble: unknown div scheme");
@@ -369,6 +377,13 @@ fvgb_status assemble(fvgb_ls* ls, const fvgb_term* terms, int32_t nterms, double
                                                                      ls->values, ls->rhs, ls->bmat, ls->brhs,
                                                                      rhs_only);
     FVGB_LAUNCH_CHECK("fvgb_assemble");
+    // explicit non-orthogonal corrections of corrected laplacians, after all terms, in term order
+    for (int i = 0; i < nterms; ++i) {
+        const fvgb_term& t = terms[i];
+        if (t.kind != FVGB_TERM_LAPLACIAN || t.scheme != FVGB_SCHEME_CORRECTED || m->v.nif == 0) continue;
+        const fvgb_status st = nonorth_rhs(m, ls->ncomp, t.face, t.cell, psi_b, -t.coeff, ls->rhs, s);
+        if (st != FVGB_OK) return st;
+    }
     if (!rhs_only) ++ls->version;
     return FVGB_OK;
 }

@@ -509,7 +509,100 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-// out_c += (sum over the cell's faces, ascending, of +-fx_f) * scale
+// ------------------------------------------- non-orthogonal correction
+// OpenFOAM's correctedSnGrad: snGrad_f = delta_f (T_N - T_P) + k_f . (grad T)_f,
+// k_f the mesh's correction vector, (grad T)_f the linear interpolation
+// w (g_P - g_N) + g_N of the Gauss linear cell gradient; boundary faces of the
+// (non-coupled) patches carry no correction.  The gradient of each of the NC
+// components comes from k_fx_gradc + k_gather_fx<3*NC>: for NC = 1 the
+// operations of fvgb_grad exactly.
+template <int NC>
+__global__ void __launch_bounds__(kThreads)
+    k_fx_gradc(MeshView m, const double* __restrict__ phi, const double* __restrict__ phi_b, double* __restrict__ fx) {
+#pragma unroll
+    for (int k = 0; k < kFPT; ++k) {
+        const int f = face_of(k);
+        if (f < m.nif) {
+            const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
+            const double wf = __ldg(&m.w[f]);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const double Tn = __ldg(&phi[N * NC + c]);
+                const double tf = wf * (__ldg(&phi[P * NC + c]) - Tn) + Tn;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) fx[(f * NC + c) * 3 + d] = __ldg(&m.Sf[3 * f + d]) * tf;
+            }
+        } else if (f < m.nif + m.nbf) {
+            const int b = f - m.nif;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const double tb = __ldg(&phi_b[b * NC + c]);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) fx[(f * NC + c) * 3 + d] = __ldg(&m.bSf[3 * b + d]) * tb;
+            }
+        }
+    }
+}
+
+enum CorrMode { kCorrLaplacian = 0, kCorrOnly = 1, kCorrSnGrad = 2 };
+
+// kCorrLaplacian: gamma_f|Sf|delta_f (T_N - T_P) + gamma_f|Sf| (k . grad_f),
+//                 boundary faces gamma_b|Sf_b|delta_b (T_b - T_P) (as k_fx_lap);
+// kCorrOnly:      gamma_f|Sf| (k . grad_f), boundary faces 0 (faceFluxCorrection);
+// kCorrSnGrad:    delta_f (T_N - T_P) + k . grad_f, boundary delta_b (T_b - T_P).
+// grad: [n][NC][3]; k . g summed x, y, z in that order.
+template <int NC, int MODE>
+__global__ void __launch_bounds__(kThreads)
+    k_fx_corr(MeshView m, const double* __restrict__ gamma, const double* __restrict__ phi,
+              const double* __restrict__ phi_b, const double* __restrict__ grad, double* __restrict__ fx) {
+#pragma unroll
+    for (int k = 0; k < kFPT; ++k) {
+        const int f = face_of(k);
+        if (f < m.nif) {
+            const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
+            const double wf = __ldg(&m.w[f]);
+            const double k0 = __ldg(&m.corr[3 * f]), k1 = __ldg(&m.corr[3 * f + 1]), k2 = __ldg(&m.corr[3 * f + 2]);
+            const double gm = MODE == kCorrSnGrad ? 1.0 : __ldg(&gamma[f]) * __ldg(&m.magSf[f]);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                double gf[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const double gn = __ldg(&grad[(N * NC + c) * 3 + d]);
+                    gf[d] = wf * (__ldg(&grad[(P * NC + c) * 3 + d]) - gn) + gn;
+                }
+                const double kg = (k0 * gf[0] + k1 * gf[1]) + k2 * gf[2];
+                const double dT = __ldg(&phi[N * NC + c]) - __ldg(&phi[P * NC + c]);
+                if (MODE == kCorrLaplacian)
+                    fx[f * NC + c] = __ldg(&gamma[f]) * __ldg(&m.geo[f]) * dT + gm * kg;
+                else if (MODE == kCorrOnly)
+                    fx[f * NC + c] = gm * kg;
+                else
+                    fx[f * NC + c] = __ldg(&m.delta[f]) * dT + kg;
+            }
+        } else if (f < m.nif + m.nbf) {
+            const int b = f - m.nif;
+            const int P = __ldg(&m.bcells[b]);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const double dT = __ldg(&phi_b[b * NC + c]) - __ldg(&phi[P * NC + c]);
+                if (MODE == kCorrLaplacian) fx[f * NC + c] = __ldg(&gamma[f]) * __ldg(&m.bgeo[b]) * dT;
+                else if (MODE == kCorrOnly) fx[f * NC + c] = 0.0;
+                else fx[f * NC + c] = __ldg(&m.bdelta[b]) * dT;
+            }
+        }
+    }
+}
+
+// out_f += coeff * fx_f on the internal faces
+__global__ void __launch_bounds__(kThreads)
+    k_axpy_faces(int64_t count, double coeff, const double* __restrict__ fx, double* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) out[i] = out[i] + coeff * __ldg(&fx[i]);
+}
+
+// out_c += (sum over the cell's faces, ascending, of +-fx_f) * scale, with
+// scale = coeff/V_c (mode 0), 1/V_c (mode 1: coeff 1) or coeff (mode 2: volume integrated)
 template <int NC>
 __global__ void __launch_bounds__(kThreads)
     k_gather_fx(MeshView m, const double* __restrict__ fx, double coeff, int unit, double* __restrict__ out) {
@@ -544,7 +637,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
         for (int k = 0; k < NC; ++k) s[k] = s[k] + signed_term(cd >= 0, __ldg(&fx[f * NC + k]));
     }
-    const double sc = unit ? __ldg(&m.invV[c]) : coeff / __ldg(&m.V[c]);
+    const double sc = unit == 1 ? __ldg(&m.invV[c]) : unit == 2 ? coeff : coeff / __ldg(&m.V[c]);
 #pragma unroll
     for (int k = 0; k < NC; ++k) out[c * NC + k] = out[c * NC + k] + s[k] * sc;
 }
@@ -595,7 +688,9 @@ __global__ void __launch_bounds__(kThreads)
 // caller then runs the one-pass gather, which needs none.
 double* face_buffer(size_t count, cudaStream_t s) {
     static bool pool_ready = false;
-    if (!pool_ready) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (!pool_ready && cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+        // not while a graph is being captured (there the allocation becomes a graph memory node)
         int dev = 0;
         cudaMemPool_t pool;
         if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
@@ -612,7 +707,66 @@ double* face_buffer(size_t count, cudaStream_t s) {
     return p;
 }
 
+// The Gauss linear gradient of every component of psi into grad [n*nc*3]
+// (zeroed first), on a face buffer.
+fvgb_status gauss_grad_components(const fvgb_mesh* m, int nc, const double* psi, const double* psi_b, double* grad,
+                                  cudaStream_t s) {
+    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+    double* fx = face_buffer((size_t)(nf * nc * 3), s);
+    if (!fx) return fvgb_fail(FVGB_ERR_OOM, "non-orthogonal correction: no face buffer");
+    cudaMemsetAsync(grad, 0, sizeof(double) * (size_t)m->v.n * nc * 3, s);
+    const unsigned gf = grid_for(nf, kThreads * kFPT), g = grid_for(m->v.n, kThreads);
+    if (nc == 1) {
+        k_fx_gradc<1><<<gf, kThreads, 0, s>>>(m->v, psi, psi_b, fx);
+        k_gather_fx<3><<<g, kThreads, 0, s>>>(m->v, fx, 1.0, 1, grad);
+    } else {
+        k_fx_gradc<3><<<gf, kThreads, 0, s>>>(m->v, psi, psi_b, fx);
+        k_gather_fx<9><<<g, kThreads, 0, s>>>(m->v, fx, 1.0, 1, grad);
+    }
+    cudaFreeAsync(fx, s);
+    return FVGB_OK;
+}
+
+// One corrected face pass (MODE) of psi into a face buffer fx [nf*nc]; the
+// caller frees fx.  nullptr with the error set when buffers cannot be had.
+template <int MODE>
+double* corrected_faces(const fvgb_mesh* m, int nc, const double* gamma, const double* psi, const double* psi_b,
+                        cudaStream_t s) {
+    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+    double* grad = face_buffer((size_t)m->v.n * nc * 3, s);
+    if (!grad) {
+        fvgb_fail(FVGB_ERR_OOM, "non-orthogonal correction: no gradient buffer");
+        return nullptr;
+    }
+    if (gauss_grad_components(m, nc, psi, psi_b, grad, s) != FVGB_OK) {
+        cudaFreeAsync(grad, s);
+        return nullptr;
+    }
+    double* fx = face_buffer((size_t)(nf * nc), s);
+    if (fx) {
+        const unsigned gf = grid_for(nf, kThreads * kFPT);
+        if (nc == 1) k_fx_corr<1, MODE><<<gf, kThreads, 0, s>>>(m->v, gamma, psi, psi_b, grad, fx);
+        else k_fx_corr<3, MODE><<<gf, kThreads, 0, s>>>(m->v, gamma, psi, psi_b, grad, fx);
+    } else {
+        fvgb_fail(FVGB_ERR_OOM, "non-orthogonal correction: no face buffer");
+    }
+    cudaFreeAsync(grad, s);
+    return fx;
+}
+
 }  // namespace
+
+fvgb_status nonorth_rhs(const fvgb_mesh* m, int nc, const double* gamma, const double* psi, const double* psi_b,
+                        double coeff, double* out, cudaStream_t s) {
+    double* fx = corrected_faces<kCorrOnly>(m, nc, gamma, psi, psi_b, s);
+    if (!fx) return FVGB_ERR_OOM;
+    const unsigned g = grid_for(m->v.n, kThreads);
+    if (nc == 1) k_gather_fx<1><<<g, kThreads, 0, s>>>(m->v, fx, coeff, 2, out);
+    else k_gather_fx<3><<<g, kThreads, 0, s>>>(m->v, fx, coeff, 2, out);
+    cudaFreeAsync(fx, s);
+    FVGB_LAUNCH_CHECK("non-orthogonal correction");
+    return FVGB_OK;
+}
 
 // ==================================================================== C ABI
 #define CHECK_MESH_NC(m, nc, name)                                                         \
@@ -745,6 +899,61 @@ extern "C" fvgb_status fvgb_sngrad(const fvgb_mesh* m, const double* phi, const 
     if (nf == 0) return FVGB_OK;
     k_sngrad<<<grid_for(nf, kThreads * kFPT), kThreads, 0, (cudaStream_t)stream>>>(m->v, phi, phi_b, out);
     FVGB_LAUNCH_CHECK("fvgb_sngrad");
+    return FVGB_OK;
+}
+
+#define CHECK_CORRECTED(m, name) \
+    FVGB_CHECK_ARG((m)->v.corr || (m)->v.nif == 0, name ": the mesh was created without cell centres")
+
+extern "C" fvgb_status fvgb_laplacian_explicit_corrected(const fvgb_mesh* m, int32_t nc, const double* gamma,
+                                                         const double* phi, const double* phi_b, double coeff,
+                                                         double* out, fvgb_stream stream) {
+    fvgb_clear_error();
+    CHECK_MESH_NC(m, nc, "fvgb_laplacian_explicit_corrected");
+    CHECK_CORRECTED(m, "fvgb_laplacian_explicit_corrected");
+    FVGB_CHECK_ARG(gamma && phi && out && (phi_b || m->v.nbf == 0), "fvgb_laplacian_explicit_corrected: null field");
+    cudaStream_t s = (cudaStream_t)stream;
+    double* fx = corrected_faces<kCorrLaplacian>(m, nc, gamma, phi, phi_b, s);
+    if (!fx) return FVGB_ERR_OOM;
+    const unsigned g = grid_for(m->v.n, kThreads);
+    if (nc == 1) k_gather_fx<1><<<g, kThreads, 0, s>>>(m->v, fx, coeff, coeff == 1.0, out);
+    else k_gather_fx<3><<<g, kThreads, 0, s>>>(m->v, fx, coeff, coeff == 1.0, out);
+    cudaFreeAsync(fx, s);
+    FVGB_LAUNCH_CHECK("fvgb_laplacian_explicit_corrected");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_sngrad_corrected(const fvgb_mesh* m, const double* phi, const double* phi_b, double* out,
+                                             fvgb_stream stream) {
+    fvgb_clear_error();
+    FVGB_CHECK_ARG(m, "fvgb_sngrad_corrected: null mesh");
+    CHECK_CORRECTED(m, "fvgb_sngrad_corrected");
+    FVGB_CHECK_ARG(phi && out && (phi_b || m->v.nbf == 0), "fvgb_sngrad_corrected: null field");
+    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+    if (nf == 0) return FVGB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    double* fx = corrected_faces<kCorrSnGrad>(m, 1, nullptr, phi, phi_b, s);
+    if (!fx) return FVGB_ERR_OOM;
+    cudaMemcpyAsync(out, fx, sizeof(double) * (size_t)nf, cudaMemcpyDeviceToDevice, s);
+    cudaFreeAsync(fx, s);
+    FVGB_LAUNCH_CHECK("fvgb_sngrad_corrected");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_nonorth_flux(const fvgb_mesh* m, int32_t nc, const double* gamma, const double* phi,
+                                         const double* phi_b, double coeff, double* out, fvgb_stream stream) {
+    fvgb_clear_error();
+    CHECK_MESH_NC(m, nc, "fvgb_nonorth_flux");
+    CHECK_CORRECTED(m, "fvgb_nonorth_flux");
+    FVGB_CHECK_ARG(gamma && phi && out && (phi_b || m->v.nbf == 0), "fvgb_nonorth_flux: null field");
+    if (m->v.nif == 0) return FVGB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    double* fx = corrected_faces<kCorrOnly>(m, nc, gamma, phi, phi_b, s);
+    if (!fx) return FVGB_ERR_OOM;
+    const int64_t cnt = (int64_t)m->v.nif * nc;
+    k_axpy_faces<<<grid_for(cnt, kThreads), kThreads, 0, s>>>(cnt, coeff, fx, out);
+    cudaFreeAsync(fx, s);
+    FVGB_LAUNCH_CHECK("fvgb_nonorth_flux");
     return FVGB_OK;
 }
 

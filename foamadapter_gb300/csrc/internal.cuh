@@ -43,6 +43,7 @@ struct MeshView {
     const double* w;
     const double* delta;
     const double* geo;       // |Sf| * delta
+    const double* corr;      // [nif*3] non-orthogonal correction vectors (null: mesh without cell centres)
     const int32_t* bcells;
     const double* bSf;
     const double* bmagSf;
@@ -118,6 +119,12 @@ inline cudaError_t settle_creation() { return cudaStreamSynchronize(0); }
 
 // at least one block: every kernel bounds-checks its index, and a zero-block
 // launch is a configuration error (empty boundary or face sets are legal)
+// out_c += coeff * sum over the cell's faces (ascending, +- as owner/neighbour)
+// of (gamma_f*|Sf|)*(k_f . gT_f): the explicit part of a corrected laplacian of
+// psi, volume integrated (explicit_ops.cu).
+fvgb_status nonorth_rhs(const fvgb_mesh* m, int nc, const double* gamma, const double* psi, const double* psi_b,
+                        double coeff, double* out, cudaStream_t s);
+
 inline unsigned grid_for(int64_t n, int threads) { return n > 0 ? (unsigned)((n + threads - 1) / threads) : 1u; }
 
 // Builds a PatchTable from a host array of per-patch types; false if invalid.

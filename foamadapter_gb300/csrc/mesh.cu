@@ -232,6 +232,21 @@ extern "C" fvgb_status fvgb_mesh_create(const fvgb_mesh_desc* d, fvgb_mesh** out
     for (int32_t c = 0; c < n; ++c) invV[c] = 1.0 / d->cell_volumes[c];
     for (int32_t f = 0; f < nif; ++f) geo[f] = d->mag_face_areas[f] * d->delta_coeffs[f];
     for (int32_t b = 0; b < nbf; ++b) bgeo[b] = d->bmag_face_areas[b] * d->bdelta_coeffs[b];
+    // non-orthogonal correction vectors k_f = Sf/|Sf| - d_f*delta_f, d_f = C_N - C_P
+    // (OpenFOAM's nonOrthCorrectionVectors), when the cell centres are given
+    std::vector<double> corr;
+    if (d->cell_centres) {
+        corr.resize(3 * (size_t)nif);
+        const double* C = d->cell_centres;
+        for (int32_t f = 0; f < nif; ++f) {
+            const int64_t P = d->owner[f], N = d->neighbour[f];
+            for (int i = 0; i < 3; ++i) {
+                const double nf = d->face_areas[3 * (int64_t)f + i] / d->mag_face_areas[f];
+                const double df = C[3 * N + i] - C[3 * P + i];
+                corr[3 * (size_t)f + i] = nf - df * d->delta_coeffs[f];
+            }
+        }
+    }
     std::vector<int32_t> bpatch(nbf);
     for (int32_t p = 0; p < np; ++p)
         for (int32_t b = d->patch_offsets[p]; b < d->patch_offsets[p + 1]; ++b) bpatch[b] = p;
@@ -253,6 +268,7 @@ extern "C" fvgb_status fvgb_mesh_create(const fvgb_mesh_desc* d, fvgb_mesh** out
     UP(v.w, d->weights, nif);
     UP(v.delta, d->delta_coeffs, nif);
     UP(v.geo, geo.data(), nif);
+    if (d->cell_centres) UP(v.corr, corr.data(), 3 * (int64_t)nif);
     UP(v.bcells, d->bface_cells, nbf);
     UP(v.bSf, d->bface_areas, 3 * (int64_t)nbf);
     UP(v.bmagSf, d->bmag_face_areas, nbf);

@@ -149,7 +149,88 @@ __global__ void __launch_bounds__(kThreads)
     U[3 * c + 2] = __ldg(&H[3 * c + 2]) - ra * gr2;
 }
 
+// fvc::interpolate(rAU)*fvc::ddtCorr(U, phi) with Euler ddt (OpenFOAM's
+// EulerDdtScheme::fvcDdtPhiCorr and ddtCorrCoeff for ddtPhiCoeff < 0):
+//   d = phi_old - Sf . U_old_f,  c = 1 - min(|d| / (|phi_old| + 1e-15), 1),
+//   out += rAUf * ((c / dt) * d);  c = 0 on patches where U is a fixed value.
+// Sf . U_old_f as k_flux_vec forms it.
+__global__ void k_ddt_corr(MeshView m, PatchTable pt, const double* __restrict__ U, const double* __restrict__ U_b,
+                           const double* __restrict__ phi_old, const double* __restrict__ rAUf, double rdt,
+                           double* __restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    double fU;
+    if (f < m.nif) {
+        const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
+        const double w = __ldg(&m.w[f]);
+        double t[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double uN = __ldg(&U[3 * N + k]);
+            t[k] = w * (__ldg(&U[3 * P + k]) - uN) + uN;
+        }
+        fU = __ldg(&m.Sf[3 * f]) * t[0] + __ldg(&m.Sf[3 * f + 1]) * t[1] + __ldg(&m.Sf[3 * f + 2]) * t[2];
+    } else if (f < m.nif + m.nbf) {
+        const int b = f - m.nif;
+        if (pt.type[__ldg(&m.bpatch[b])] == FVGB_BC_FIXED_VALUE) return;
+        fU = __ldg(&m.bSf[3 * b]) * __ldg(&U_b[3 * b]) + __ldg(&m.bSf[3 * b + 1]) * __ldg(&U_b[3 * b + 1]) +
+             __ldg(&m.bSf[3 * b + 2]) * __ldg(&U_b[3 * b + 2]);
+    } else {
+        return;
+    }
+    const double po = __ldg(&phi_old[f]);
+    const double d = po - fU;
+    const double c = 1.0 - fmin(fabs(d) / (fabs(po) + 1e-15), 1.0);
+    out[f] = out[f] + __ldg(&rAUf[f]) * ((c * rdt) * d);
+}
+
+// Foam::constrainPressure: on fixedFluxPressure patches the pressure's fixed
+// gradient becomes (phiHbyA_b - Sf_b . U_b) / (|Sf_b| * rAUf_b).
+__global__ void k_constrain_pressure(MeshView m, FlagTable ft, const double* __restrict__ phiHbyA,
+                                     const double* __restrict__ U_b, const double* __restrict__ rAUf,
+                                     double* __restrict__ p_ref) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= m.nbf) return;
+    if (!ft.flag[__ldg(&m.bpatch[b])]) return;
+    const double fU = __ldg(&m.bSf[3 * b]) * __ldg(&U_b[3 * b]) + __ldg(&m.bSf[3 * b + 1]) * __ldg(&U_b[3 * b + 1]) +
+                      __ldg(&m.bSf[3 * b + 2]) * __ldg(&U_b[3 * b + 2]);
+    const int f = m.nif + b;
+    p_ref[b] = (__ldg(&phiHbyA[f]) - fU) / (__ldg(&m.bmagSf[b]) * __ldg(&rAUf[f]));
+}
+
 }  // namespace
+
+extern "C" fvgb_status fvgb_piso_ddt_corr(const fvgb_mesh* mesh, const int32_t* U_patch_type, const double* U_old,
+                                          const double* U_old_b, const double* phi_old, const double* rAUf, double dt,
+                                          double* phiHbyA, fvgb_stream stream) {
+    fvgb_clear_error();
+    FVGB_CHECK_ARG(mesh && U_patch_type && U_old && phi_old && rAUf && phiHbyA && (U_old_b || mesh->v.nbf == 0),
+                   "fvgb_piso_ddt_corr: null argument");
+    FVGB_CHECK_ARG(dt > 0, "fvgb_piso_ddt_corr: dt must be positive");
+    PatchTable pt;
+    FVGB_CHECK_ARG(make_patch_table(mesh, U_patch_type, &pt), "fvgb_piso_ddt_corr: bad patch types");
+    const int64_t nf = (int64_t)mesh->v.nif + mesh->v.nbf;
+    if (nf == 0) return FVGB_OK;
+    k_ddt_corr<<<grid_for(nf, kThreads), kThreads, 0, (cudaStream_t)stream>>>(mesh->v, pt, U_old, U_old_b, phi_old,
+                                                                              rAUf, 1.0 / dt, phiHbyA);
+    FVGB_LAUNCH_CHECK("fvgb_piso_ddt_corr");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_piso_constrain_pressure(const fvgb_mesh* mesh, const int32_t* patch_fixed_flux,
+                                                    const double* phiHbyA, const double* U_b, const double* rAUf,
+                                                    double* p_ref, fvgb_stream stream) {
+    fvgb_clear_error();
+    FVGB_CHECK_ARG(mesh && patch_fixed_flux, "fvgb_piso_constrain_pressure: null argument");
+    if (mesh->v.nbf == 0) return FVGB_OK;
+    FVGB_CHECK_ARG(phiHbyA && U_b && rAUf && p_ref, "fvgb_piso_constrain_pressure: null field");
+    FlagTable ft;
+    ft.n = mesh->v.npatch;
+    for (int i = 0; i < ft.n; ++i) ft.flag[i] = patch_fixed_flux[i] ? 1 : 0;
+    k_constrain_pressure<<<grid_for(mesh->v.nbf, kThreads), kThreads, 0, (cudaStream_t)stream>>>(
+        mesh->v, ft, phiHbyA, U_b, rAUf, p_ref);
+    FVGB_LAUNCH_CHECK("fvgb_piso_constrain_pressure");
+    return FVGB_OK;
+}
 
 extern "C" fvgb_status fvgb_piso_rau_hbya(const fvgb_ls* ueqn, const double* U, double* rAU,
                                           double* HbyA, fvgb_stream stream) {

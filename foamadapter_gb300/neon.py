@@ -165,26 +165,53 @@ class GaussGreenGrad:
         return out
 
 
+def _corrected(scheme) -> bool:
+    """True for a `corrected` snGrad scheme ("Gauss linear corrected", "corrected")."""
+    toks = scheme if isinstance(scheme, (list, tuple)) else str(scheme).split()
+    if "corrected" in toks:
+        return True
+    if "uncorrected" in toks or not toks or toks in (["Gauss", "linear"], ["linear"]):
+        return False
+    raise ValueError(f"unsupported snGrad scheme {scheme!r}")
+
+
 class GaussGreenLaplacian:
+    """scheme: "Gauss linear uncorrected" or "Gauss linear corrected" (tokens or a string)."""
+
     def __init__(self, mesh: DeviceMesh, scheme=("Gauss", "linear", "uncorrected")):
         self.mesh = mesh
+        self.corrected = _corrected(scheme)
 
     def laplacian(self, out: torch.Tensor, gamma: SurfaceField, phi: VolumeField, coeff: float = 1.0):
-        abi.check(abi.lib().fvgb_laplacian_explicit(self.mesh.handle, phi.ncomp, abi.ptr(gamma.values),
-                                                    abi.ptr(phi.internal), abi.ptr(phi.boundary),
-                                                    float(coeff), abi.ptr(out), _stream()))
+        fn = abi.lib().fvgb_laplacian_explicit_corrected if self.corrected else abi.lib().fvgb_laplacian_explicit
+        abi.check(fn(self.mesh.handle, phi.ncomp, abi.ptr(gamma.values), abi.ptr(phi.internal),
+                     abi.ptr(phi.boundary), float(coeff), abi.ptr(out), _stream()))
         return out
 
 
 class FaceNormalGradient:
+    """scheme: "uncorrected" or "corrected"."""
+
     def __init__(self, mesh: DeviceMesh, scheme="uncorrected"):
         self.mesh = mesh
+        self.corrected = _corrected(scheme)
 
     def faceNormalGrad(self, phi: VolumeField, out: SurfaceField | None = None):
         out = out or SurfaceField(self.mesh)
-        abi.check(abi.lib().fvgb_sngrad(self.mesh.handle, abi.ptr(phi.internal), abi.ptr(phi.boundary),
-                                        abi.ptr(out.values), _stream()))
+        fn = abi.lib().fvgb_sngrad_corrected if self.corrected else abi.lib().fvgb_sngrad
+        abi.check(fn(self.mesh.handle, abi.ptr(phi.internal), abi.ptr(phi.boundary), abi.ptr(out.values),
+                     _stream()))
         return out
+
+
+def nonorth_flux(gamma: SurfaceField, phi: VolumeField, coeff: float = 1.0, out: SurfaceField | None = None):
+    """faceFluxCorrection of laplacian(gamma, phi) with the corrected scheme,
+    out_f += coeff*(gamma_f|Sf|)(k_f . grad(phi)_f) on the internal faces."""
+    mesh = phi.mesh
+    out = out or SurfaceField(mesh, ncomp=phi.ncomp)
+    abi.check(abi.lib().fvgb_nonorth_flux(mesh.handle, phi.ncomp, abi.ptr(gamma.values), abi.ptr(phi.internal),
+                                          abi.ptr(phi.boundary), float(coeff), abi.ptr(out.values), _stream()))
+    return out
 
 
 def createSparsity(mesh: DeviceMesh):
@@ -209,7 +236,14 @@ def ddt(old: torch.Tensor, coeff: float = 1.0) -> Term:
     return Term(abi.TERM_DDT, coeff, cell=old)
 
 
-def laplacian(gamma: SurfaceField, coeff: float = 1.0) -> Term:
+def laplacian(gamma: SurfaceField, coeff: float = 1.0, scheme="uncorrected",
+              field: torch.Tensor | None = None) -> Term:
+    """Implicit laplacian(gamma, psi).  With a corrected scheme, `field` is the
+    current psi whose explicit non-orthogonal correction goes to the rhs."""
+    if _corrected(scheme):
+        if field is None:
+            raise ValueError("a corrected laplacian needs the current field")
+        return Term(abi.TERM_LAPLACIAN, coeff, scheme=abi.SCHEME_CORRECTED, cell=field, face=gamma.values)
     return Term(abi.TERM_LAPLACIAN, coeff, face=gamma.values)
 
 

@@ -143,7 +143,11 @@ fvgb_status fvgb_bc_correct(const fvgb_mesh* mesh, int32_t ncomp, const fvgb_bc*
                             const double* internal, double* boundary, fvgb_stream stream);
 
 /* ------------------------------------------------------- explicit operators */
-typedef enum fvgb_scheme { FVGB_SCHEME_LINEAR = 0, FVGB_SCHEME_UPWIND = 1 } fvgb_scheme;
+typedef enum fvgb_scheme {
+    FVGB_SCHEME_LINEAR = 0,
+    FVGB_SCHEME_UPWIND = 1,
+    FVGB_SCHEME_CORRECTED = 2  /* laplacian: Gauss linear corrected (non-orthogonal correction) */
+} fvgb_scheme;
 
 /* SurfaceInterpolation linear (NeoN; reference call sites neoIcoFoam.cpp:118-124,
  * test_operators.cpp:52-58):  dst_f = w_f*(src_P - src_N) + src_N on internal
@@ -170,10 +174,29 @@ fvgb_status fvgb_grad(const fvgb_mesh* mesh, const double* phi, const double* ph
 fvgb_status fvgb_laplacian_explicit(const fvgb_mesh* mesh, int32_t ncomp, const double* gamma,
                                     const double* phi, const double* phi_b, double coeff,
                                     double* out, fvgb_stream stream);
+/* The same with the `Gauss linear corrected` scheme (OpenFOAM's correctedSnGrad,
+ * test/setup_stencil3D/system/fvSchemes:43): flux_f = gamma_f*(|Sf|*delta_f)*(T_N - T_P)
+ * + (gamma_f*|Sf|)*(k_f . gT_f), where k_f = Sf/|Sf| - (C_N - C_P)*delta_f is the
+ * face's non-orthogonal correction vector, gT_f = w_f*(g_P - g_N) + g_N and g the
+ * Gauss linear gradient of T (as fvgb_grad, per component); boundary faces as
+ * uncorrected.  Needs a mesh created with cell centres (FVGB_ERR_INVALID_ARG
+ * otherwise).  Takes stream-ordered scratch memory for the gradient. */
+fvgb_status fvgb_laplacian_explicit_corrected(const fvgb_mesh* mesh, int32_t ncomp, const double* gamma,
+                                              const double* phi, const double* phi_b, double coeff,
+                                              double* out, fvgb_stream stream);
+/* faceFluxCorrection of a corrected laplacian: out_f += coeff*(gamma_f*|Sf|)*(k_f . gT_f)
+ * on the internal faces [n_ifaces*ncomp] (boundary faces carry none).  The flux a
+ * pressure equation's solution adds to the face velocity (pEqn.flux()). */
+fvgb_status fvgb_nonorth_flux(const fvgb_mesh* mesh, int32_t ncomp, const double* gamma, const double* phi,
+                              const double* phi_b, double coeff, double* out, fvgb_stream stream);
 /* FaceNormalGradient uncorrected (bench_explicitOperators.cpp:455-479):
  * out_f = delta_f*(T_N - T_P), out_b = delta_b*(T_b - T_P); overwritten. */
 fvgb_status fvgb_sngrad(const fvgb_mesh* mesh, const double* phi, const double* phi_b,
                         double* out, fvgb_stream stream);
+/* FaceNormalGradient corrected: out_f = delta_f*(T_N - T_P) + k_f . gT_f (as above),
+ * boundary faces delta_b*(T_b - T_P); overwritten. */
+fvgb_status fvgb_sngrad_corrected(const fvgb_mesh* mesh, const double* phi, const double* phi_b,
+                                  double* out, fvgb_stream stream);
 /* Fused explicit step of  ddt(T) + div(phi, T) = 0, Gauss upwind, forward Euler
  * (test_advection.cpp:116-170): T_new_P = T_old_P - dt*(div_P) with div_P the
  * fvgb_div_explicit value for coeff 1; then the boundary values of T_new are
@@ -188,7 +211,11 @@ typedef struct fvgb_ls fvgb_ls;
 
 typedef enum fvgb_term_kind {
     FVGB_TERM_DDT = 0,             /* implicit Euler ddt  (DdtOperator)                */
-    FVGB_TERM_LAPLACIAN = 1,       /* implicit laplacian(gamma, psi) uncorrected       */
+    FVGB_TERM_LAPLACIAN = 1,       /* implicit laplacian(gamma, psi); scheme CORRECTED adds
+                                      the non-orthogonal correction of `cell` (the current
+                                      psi, boundary values psi_b) to the rhs:
+                                      b -= coeff*sum_f(+-(gamma_f*|Sf|)*(k_f . gT_f)), after
+                                      all terms, in term order                          */
     FVGB_TERM_DIV = 2,             /* implicit div(flux, psi), linear or upwind        */
     FVGB_TERM_SOURCE = 3,          /* implicit source: diag += coeff*s_P*V_P           */
     FVGB_TERM_EXPLICIT = 4,        /* rhs -= coeff*E_P (E already volume integrated)   */
@@ -206,7 +233,8 @@ typedef enum fvgb_term_kind {
  * b = sum coeff_t b_t (EXPLICIT: b -= coeff*E).  Terms are applied in array order. */
 typedef struct fvgb_term {
     int32_t kind;
-    int32_t scheme;        /* DIV: FVGB_SCHEME_LINEAR or FVGB_SCHEME_UPWIND           */
+    int32_t scheme;        /* DIV: FVGB_SCHEME_LINEAR or FVGB_SCHEME_UPWIND;
+                              LAPLACIAN: 0 (uncorrected) or FVGB_SCHEME_CORRECTED        */
     double coeff;          /* operator scaling                                        */
     const double* cell;    /* DDT: old-time psi [n*ncomp]; SOURCE: s [n] or NULL (=1);
                               EXPLICIT: E [n*ncomp]; DIV_EXPLICIT: the convected field  */
@@ -384,6 +412,23 @@ fvgb_status fvgb_piso_face_update(const fvgb_ls* peqn, const double* phiHbyA, co
 fvgb_status fvgb_piso_velocity_update(const fvgb_mesh* mesh, const double* HbyA,
                                       const double* rAU, const double* p, const double* p_b,
                                       double* U, fvgb_stream stream);
+/* The two steps the reference's PISO leaves as TODOs (neoIcoFoam.cpp:127-137),
+ * with OpenFOAM's semantics.  ddtCorr: phiHbyA += fvc::interpolate(rAU) *
+ * fvc::ddtCorr(U, phi) for Euler ddt,
+ *   phiHbyA_f += rAUf_f*((c_f/dt)*d_f),  d_f = phi_old_f - Sf_f . U_old_f,
+ *   c_f = 1 - min(|d_f| / (|phi_old_f| + 1e-15), 1),
+ * U_old_f linearly interpolated (boundary faces: U_old_b), c = 0 on the faces of
+ * patches whose U_patch_type is FVGB_BC_FIXED_VALUE; rAUf [n_ifaces+n_bfaces]. */
+fvgb_status fvgb_piso_ddt_corr(const fvgb_mesh* mesh, const int32_t* U_patch_type, const double* U_old,
+                               const double* U_old_b, const double* phi_old, const double* rAUf, double dt,
+                               double* phiHbyA, fvgb_stream stream);
+/* constrainPressure: on the patches flagged in patch_fixed_flux (host
+ * [n_patches]; fixedFluxPressure, a FIXED_GRADIENT patch of p) the gradient
+ * becomes p_ref_b = (phiHbyA_b - Sf_b . U_b) / (|Sf_b| * rAUf_b); other
+ * patches' entries of p_ref are left as they are. */
+fvgb_status fvgb_piso_constrain_pressure(const fvgb_mesh* mesh, const int32_t* patch_fixed_flux,
+                                         const double* phiHbyA, const double* U_b, const double* rAUf,
+                                         double* p_ref, fvgb_stream stream);
 
 /* ----------------------------------------------------------------- serving */
 /* A serving loop for scalar advection-diffusion solves (no counterpart in the

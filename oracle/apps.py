@@ -16,9 +16,10 @@ CALC, FIXED_VALUE, FIXED_GRADIENT = 0, 1, 2
 
 class CavityPisoCPU:
     def __init__(self, hm, nu=0.01, dt=5e-4, n_corr=2, lid=(1.0, 0.0, 0.0), precision=0, p_rel_tol=1e-8,
-                 p_max_iter=20000, inner_rel_tol=0.1):
+                 p_max_iter=20000, inner_rel_tol=0.1, ddt_corr=False, corrected=False, n_non_orth=0):
         self.hm, self.o = hm, Oracle(hm)
         self.dt, self.n_corr = dt, n_corr
+        self.ddt_corr, self.corrected, self.n_non_orth = ddt_corr, corrected, n_non_orth
         self.solve_kw = dict(rel_tol=p_rel_tol, max_iter=p_max_iter, precision=precision,
                              inner_rel_tol=inner_rel_tol, inner_max_iter=2000, max_outer=50)
         n, nbf = hm.n, hm.nbf
@@ -41,7 +42,7 @@ class CavityPisoCPU:
 
     def step(self):
         o, hm = self.o, self.hm
-        U_old = self.U.copy()
+        U_old, Ub_old, phi_old = self.U.copy(), self.Ub.copy(), self.phi.copy()
         v, r, _, _ = o.assemble(3, [(DDT, 0, 1.0, U_old, None), (DIV, LINEAR, 1.0, None, self.phi),
                                     (LAP, 0, -1.0, None, self.nu)], self.dt, self.Utypes, self.Uref, self.Ub)
         for _ in range(self.n_corr):
@@ -52,13 +53,21 @@ class CavityPisoCPU:
             o.constrain_hbya(self.assignable, self.Ub, Hb)
             rAUf = o.interp_linear(1, rAU, rAUb)
             phiHbyA = o.flux_vec(H, Hb)
-            pv, pr, pbm, pbr = o.assemble(1, [(LAP, 0, 1.0, None, rAUf), (DIV_FLUX, 0, -1.0, None, phiHbyA)],
-                                          self.dt, self.zg, self.z1, self.pb)
-            o.set_reference(pv, pr, 0, 0.0)
-            st = o.solve(pv, pr, self.p, **self.solve_kw)
-            self.stats.append((st.num_iter, st.num_outer, st.init_res_norm, st.final_res_norm, st.status))
-            o.bc_correct(1, self.zg, self.z1, self.p, self.pb)
-            self.phi = o.face_update(pv, pbm, pbr, phiHbyA, self.p)
+            if self.ddt_corr:
+                o.ddt_corr(self.Utypes, U_old, Ub_old, phi_old, rAUf, self.dt, phiHbyA)
+            for k in range(self.n_non_orth + 1):
+                lap = (LAP, 2, 1.0, self.p.copy(), rAUf) if self.corrected else (LAP, 0, 1.0, None, rAUf)
+                pv, pr, pbm, pbr = o.assemble(1, [lap, (DIV_FLUX, 0, -1.0, None, phiHbyA)],
+                                              self.dt, self.zg, self.z1, self.pb)
+                o.set_reference(pv, pr, 0, 0.0)
+                p_pre, pb_pre = self.p.copy(), self.pb.copy()
+                st = o.solve(pv, pr, self.p, **self.solve_kw)
+                self.stats.append((st.num_iter, st.num_outer, st.init_res_norm, st.final_res_norm, st.status))
+                o.bc_correct(1, self.zg, self.z1, self.p, self.pb)
+                if k == self.n_non_orth:
+                    self.phi = o.face_update(pv, pbm, pbr, phiHbyA, self.p)
+                    if self.corrected:
+                        o.nonorth_flux(1, rAUf, p_pre, pb_pre, -1.0, self.phi)
             self.U = o.velocity_update(H, rAU, self.p, self.pb)
             o.bc_correct(3, self.Utypes, self.Uref, self.U, self.Ub)
 

@@ -171,6 +171,129 @@ void or_sngrad(const or_mesh* m, const double* phi, const double* phi_b, double*
         out[m->nif + b] = m->bdelta[b] * (phi_b[b] - phi[m->bcells[b]]);
 }
 
+/* ---- non-orthogonal correction (OpenFOAM's correctedSnGrad, the method of
+ * the `Gauss linear corrected` laplacian, test/setup_stencil3D/system/fvSchemes:43;
+ * NeoN's own implementation is not in the reference checkout, so parity is on
+ * the published method):
+ *   k_f      = Sf/|Sf| - (C_N - C_P)*delta_f      (nonOrthCorrectionVectors)
+ *   snGrad_f = delta_f*(T_N - T_P) + k_f . gT_f,  gT_f = w*(g_P - g_N) + g_N,
+ * g the Gauss linear cell gradient (or_grad, per component); boundary faces of
+ * non-coupled patches carry no correction. */
+void or_nonorth_vectors(const or_mesh* m, const double* C, double* k) {
+    for (int32_t f = 0; f < m->nif; ++f) {
+        const int32_t P = m->own[f], N = m->nei[f];
+        for (int i = 0; i < 3; ++i) {
+            double nf = m->Sf[3 * f + i] / m->magSf[f];
+            double df = C[3 * N + i] - C[3 * P + i];
+            k[3 * f + i] = nf - df * m->delta[f];
+        }
+    }
+}
+
+/* grad[(c*nc + j)*3 + d]: or_grad of component j */
+static double* grad_components(const or_mesh* m, int32_t nc, const double* phi, const double* phi_b) {
+    double* grad = zalloc((size_t)m->n * nc * 3);
+    double* pj = zalloc((size_t)m->n);
+    double* pbj = zalloc((size_t)m->nbf);
+    double* gj = zalloc((size_t)m->n * 3);
+    for (int32_t j = 0; j < nc; ++j) {
+        for (int32_t c = 0; c < m->n; ++c) pj[c] = phi[c * nc + j];
+        for (int32_t b = 0; b < m->nbf; ++b) pbj[b] = phi_b[b * nc + j];
+        memset(gj, 0, sizeof(double) * (size_t)m->n * 3);
+        or_grad(m, pj, pbj, 1.0, gj);
+        for (int32_t c = 0; c < m->n; ++c)
+            for (int d = 0; d < 3; ++d) grad[(c * nc + j) * 3 + d] = gj[3 * c + d];
+    }
+    free(gj);
+    free(pbj);
+    free(pj);
+    return grad;
+}
+
+/* k_f . gT_f of component j on internal face f, summed x, y, z in that order */
+static double corr_kg(const or_mesh* m, const double* k, const double* grad, int32_t nc, int32_t f, int32_t j) {
+    const int32_t P = m->own[f], N = m->nei[f];
+    double gf[3];
+    for (int d = 0; d < 3; ++d) {
+        double gn = grad[(N * nc + j) * 3 + d];
+        gf[d] = m->w[f] * (grad[(P * nc + j) * 3 + d] - gn) + gn;
+    }
+    return (k[3 * f] * gf[0] + k[3 * f + 1] * gf[1]) + k[3 * f + 2] * gf[2];
+}
+
+/* GaussGreenLaplacian corrected: flux_f = gamma*(|Sf|*delta)*(T_N - T_P) +
+ * (gamma*|Sf|)*(k . gT_f); boundary faces uncorrected; out += res*(coeff/V). */
+void or_laplacian_corrected(const or_mesh* m, int32_t nc, const double* k, const double* gamma,
+                            const double* phi, const double* phi_b, double coeff, double* out) {
+    double* grad = grad_components(m, nc, phi, phi_b);
+    double* res = zalloc((size_t)m->n * nc);
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t P = m->own[f], N = m->nei[f];
+        double g = gamma[f] * (m->magSf[f] * m->delta[f]);
+        double gm = gamma[f] * m->magSf[f];
+        for (int32_t j = 0; j < nc; ++j) {
+            double fl = g * (phi[N * nc + j] - phi[P * nc + j]) + gm * corr_kg(m, k, grad, nc, f, j);
+            res[P * nc + j] += fl;
+            res[N * nc + j] -= fl;
+        }
+    }
+    for (int32_t b = 0; b < m->nbf; ++b) {
+        int32_t P = m->bcells[b];
+        double g = gamma[m->nif + b] * (m->bmagSf[b] * m->bdelta[b]);
+        for (int32_t j = 0; j < nc; ++j) res[P * nc + j] += g * (phi_b[b * nc + j] - phi[P * nc + j]);
+    }
+    for (int32_t c = 0; c < m->n; ++c) {
+        double s = coeff / m->V[c];
+        for (int32_t j = 0; j < nc; ++j) out[c * nc + j] += res[c * nc + j] * s;
+    }
+    free(res);
+    free(grad);
+}
+
+void or_sngrad_corrected(const or_mesh* m, const double* k, const double* phi, const double* phi_b, double* out) {
+    double* grad = grad_components(m, 1, phi, phi_b);
+    for (int32_t f = 0; f < m->nif; ++f)
+        out[f] = m->delta[f] * (phi[m->nei[f]] - phi[m->own[f]]) + corr_kg(m, k, grad, 1, f, 0);
+    for (int32_t b = 0; b < m->nbf; ++b)
+        out[m->nif + b] = m->bdelta[b] * (phi_b[b] - phi[m->bcells[b]]);
+    free(grad);
+}
+
+/* faceFluxCorrection: out_f += coeff*((gamma*|Sf|)*(k . gT_f)) on internal faces */
+void or_nonorth_flux(const or_mesh* m, int32_t nc, const double* k, const double* gamma, const double* phi,
+                     const double* phi_b, double coeff, double* out) {
+    double* grad = grad_components(m, nc, phi, phi_b);
+    for (int32_t f = 0; f < m->nif; ++f) {
+        double gm = gamma[f] * m->magSf[f];
+        for (int32_t j = 0; j < nc; ++j) out[f * nc + j] += coeff * (gm * corr_kg(m, k, grad, nc, f, j));
+    }
+    free(grad);
+}
+
+/* The explicit part of a corrected implicit laplacian, volume integrated:
+ * rhs_P += coeff * sum_f(+-(gamma*|Sf|)*(k . gT_f)), faces in order (a
+ * boundary face adds 0). */
+void or_nonorth_rhs(const or_mesh* m, int32_t nc, const double* k, const double* gamma, const double* psi,
+                    const double* psi_b, double coeff, double* rhs) {
+    double* grad = grad_components(m, nc, psi, psi_b);
+    double* res = zalloc((size_t)m->n * nc);
+    for (int32_t f = 0; f < m->nif; ++f) {
+        int32_t P = m->own[f], N = m->nei[f];
+        double gm = gamma[f] * m->magSf[f];
+        for (int32_t j = 0; j < nc; ++j) {
+            double fl = gm * corr_kg(m, k, grad, nc, f, j);
+            res[P * nc + j] += fl;
+            res[N * nc + j] -= fl;
+        }
+    }
+    for (int32_t b = 0; b < m->nbf; ++b)
+        for (int32_t j = 0; j < nc; ++j) res[m->bcells[b] * nc + j] += 0.0;
+    for (int32_t c = 0; c < m->n; ++c)
+        for (int32_t j = 0; j < nc; ++j) rhs[c * nc + j] += res[c * nc + j] * coeff;
+    free(res);
+    free(grad);
+}
+
 /* ddt(T) + div(phi,T) = 0, upwind, forward Euler: T_new = T_old - dt*div(T_old) */
 void or_advect_euler(const or_mesh* m, const double* flux, const double* T_old,
                      const double* T_old_b, double dt, const int32_t* patch_type,
@@ -938,6 +1061,37 @@ void or_flux_vec(const or_mesh* m, const double* U, const double* U_b, double* o
     for (int32_t b = 0; b < m->nbf; ++b)
         out[m->nif + b] = m->bSf[3 * b] * U_b[3 * b] + m->bSf[3 * b + 1] * U_b[3 * b + 1] +
                           m->bSf[3 * b + 2] * U_b[3 * b + 2];
+}
+
+/* fvc::interpolate(rAU)*fvc::ddtCorr(U, phi), Euler (OpenFOAM's
+ * EulerDdtScheme::fvcDdtPhiCorr with ddtCorrCoeff for ddtPhiCoeff < 0; the
+ * reference's PISO leaves it as a TODO, neoIcoFoam.cpp:127-130):
+ * d = phi_old - Sf.U_old_f, c = 1 - min(|d|/(|phi_old| + 1e-15), 1),
+ * out += rAUf*((c/dt)*d); c = 0 on fixed-value U patches. */
+void or_ddt_corr(const or_mesh* m, const int32_t* U_patch_type, const double* U, const double* U_b,
+                 const double* phi_old, const double* rAUf, double dt, double* out) {
+    const double rdt = 1.0 / dt;
+    const int32_t nf = m->nif + m->nbf;
+    double* fU = zalloc((size_t)nf);
+    or_flux_vec(m, U, U_b, fU);
+    for (int32_t f = 0; f < nf; ++f) {
+        if (f >= m->nif && face_bc(m, U_patch_type, f - m->nif) == BC_FIXED_VALUE) continue;
+        double d = phi_old[f] - fU[f];
+        double c = 1.0 - fmin(fabs(d) / (fabs(phi_old[f]) + 1e-15), 1.0);
+        out[f] += rAUf[f] * ((c * rdt) * d);
+    }
+    free(fU);
+}
+
+/* constrainPressure (neoIcoFoam.cpp:135-137 TODO): on fixedFluxPressure patches
+ * p_ref_b = (phiHbyA_b - Sf_b.U_b) / (|Sf_b|*rAUf_b) */
+void or_constrain_pressure(const or_mesh* m, const int32_t* patch_fixed_flux, const double* phiHbyA,
+                           const double* U_b, const double* rAUf, double* p_ref) {
+    for (int32_t b = 0; b < m->nbf; ++b) {
+        if (!face_bc(m, patch_fixed_flux, b)) continue;
+        double fU = m->bSf[3 * b] * U_b[3 * b] + m->bSf[3 * b + 1] * U_b[3 * b + 1] + m->bSf[3 * b + 2] * U_b[3 * b + 2];
+        p_ref[b] = (phiHbyA[m->nif + b] - fU) / (m->bmagSf[b] * rAUf[m->nif + b]);
+    }
 }
 
 /* updateFaceVelocity (pressureVelocityCoupling.cpp:131-197) */

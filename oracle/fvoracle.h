@@ -72,6 +72,15 @@ void or_grad(const or_mesh* m, const double* phi, const double* phi_b, double co
 void or_laplacian(const or_mesh* m, int32_t ncomp, const double* gamma, const double* phi,
                   const double* phi_b, double coeff, double* out);
 void or_sngrad(const or_mesh* m, const double* phi, const double* phi_b, double* out);
+/* non-orthogonal correction (corrected scheme); k = or_nonorth_vectors [nif*3] */
+void or_nonorth_vectors(const or_mesh* m, const double* C, double* k);
+void or_laplacian_corrected(const or_mesh* m, int32_t ncomp, const double* k, const double* gamma,
+                            const double* phi, const double* phi_b, double coeff, double* out);
+void or_sngrad_corrected(const or_mesh* m, const double* k, const double* phi, const double* phi_b, double* out);
+void or_nonorth_flux(const or_mesh* m, int32_t ncomp, const double* k, const double* gamma, const double* phi,
+                     const double* phi_b, double coeff, double* out);
+void or_nonorth_rhs(const or_mesh* m, int32_t ncomp, const double* k, const double* gamma, const double* psi,
+                    const double* psi_b, double coeff, double* rhs);
 void or_advect_euler(const or_mesh* m, const double* flux, const double* T_old,
                      const double* T_old_b, double dt, const int32_t* patch_type,
                      const double* ref, double* T_new, double* T_new_b);
@@ -95,6 +104,10 @@ void or_rau_hbya(const or_mesh* m, const or_csr* A, const double* values, const 
 void or_constrain_hbya(const or_mesh* m, const int32_t* patch_assignable, const double* U_b,
                        double* HbyA_b);
 void or_flux_vec(const or_mesh* m, const double* U, const double* U_b, double* out);
+void or_ddt_corr(const or_mesh* m, const int32_t* U_patch_type, const double* U, const double* U_b,
+                 const double* phi_old, const double* rAUf, double dt, double* out);
+void or_constrain_pressure(const or_mesh* m, const int32_t* patch_fixed_flux, const double* phiHbyA,
+                           const double* U_b, const double* rAUf, double* p_ref);
 void or_face_update(const or_mesh* m, const or_csr* A, const double* values, const double* bmat,
                     const double* brhs, const double* phiHbyA, const double* p, double* phi);
 void or_velocity_update(const or_mesh* m, const double* HbyA, const double* rAU, const double* p,

@@ -76,6 +76,7 @@ class Oracle:
         self.m = OrMesh(hm.n, hm.nif, hm.nbf, hm.npatch, *[x.ctypes.data for x in k])
         self.L = lib()
         self._csr = None
+        self._k = None
 
     # ---------------------------------------------------------------- explicit
     def bc_correct(self, ncomp, types, ref, internal, boundary):
@@ -107,6 +108,30 @@ class Oracle:
     def sngrad(self, phi, phi_b):
         out = np.zeros(self.hm.nif + self.hm.nbf)
         self.L.or_sngrad(C.byref(self.m), p(phi), p(phi_b), p(out))
+        return out
+
+    def nonorth_vectors(self):
+        """[nif*3] non-orthogonal correction vectors from the cell centres."""
+        if self._k is None:
+            hm = self.hm
+            cc = np.ascontiguousarray(hm.C, np.float64).reshape(-1)
+            self._k = np.zeros(max(1, 3 * hm.nif))
+            self.L.or_nonorth_vectors(C.byref(self.m), p(cc), p(self._k))
+        return self._k
+
+    def laplacian_corrected(self, ncomp, gamma, phi, phi_b, coeff, out):
+        self.L.or_laplacian_corrected(C.byref(self.m), ncomp, p(self.nonorth_vectors()), p(gamma), p(phi),
+                                      p(phi_b), dbl(coeff), p(out))
+        return out
+
+    def sngrad_corrected(self, phi, phi_b):
+        out = np.zeros(self.hm.nif + self.hm.nbf)
+        self.L.or_sngrad_corrected(C.byref(self.m), p(self.nonorth_vectors()), p(phi), p(phi_b), p(out))
+        return out
+
+    def nonorth_flux(self, ncomp, gamma, phi, phi_b, coeff, out):
+        self.L.or_nonorth_flux(C.byref(self.m), ncomp, p(self.nonorth_vectors()), p(gamma), p(phi), p(phi_b),
+                               dbl(coeff), p(out))
         return out
 
     def advect_euler(self, flux, T, Tb, dt, types, ref):
@@ -148,6 +173,11 @@ class Oracle:
         t = np.asarray(types, np.int32)
         self.L.or_assemble(C.byref(self.m), C.byref(A), ncomp, arr, len(terms), dbl(dt), p(t), p(ref),
                            p(psi_b), p(values), p(rhs), p(bmat), p(brhs))
+        # corrected laplacians: their explicit non-orthogonal part, after all terms, in term order
+        for kind, scheme, coeff, cell, face in terms:
+            if kind == 1 and scheme == 2 and hm.nif > 0:
+                self.L.or_nonorth_rhs(C.byref(self.m), ncomp, p(self.nonorth_vectors()), p(face), p(cell),
+                                      p(psi_b), dbl(-coeff), p(rhs))
         return values, rhs, bmat[:hm.nbf], brhs[:hm.nbf * ncomp]
 
     def set_reference(self, values, rhs, cell, value):
@@ -190,6 +220,16 @@ class Oracle:
         U = np.zeros(3 * self.hm.n)
         self.L.or_velocity_update(C.byref(self.m), p(H), p(rAU), p(pp), p(p_b), p(U))
         return U
+
+    def ddt_corr(self, U_types, U, U_b, phi_old, rAUf, dt, out):
+        t = np.asarray(U_types, np.int32)
+        self.L.or_ddt_corr(C.byref(self.m), p(t), p(U), p(U_b), p(phi_old), p(rAUf), dbl(dt), p(out))
+        return out
+
+    def constrain_pressure(self, fixed_flux, phiHbyA, U_b, rAUf, p_ref):
+        fl = np.asarray(fixed_flux, np.int32)
+        self.L.or_constrain_pressure(C.byref(self.m), p(fl), p(phiHbyA), p(U_b), p(rAUf), p(p_ref))
+        return p_ref
 
 
 def dot_tree(a: np.ndarray, b: np.ndarray) -> float:
