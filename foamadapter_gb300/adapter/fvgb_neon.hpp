@@ -244,30 +244,76 @@ private:
     const UnstructuredMesh& m_;
 };
 
+// snGrad correction of a scheme: "Gauss linear corrected" / "corrected" -> true,
+// "Gauss linear uncorrected" / "uncorrected" -> false.
+inline bool corrected_of(const std::string& scheme) {
+    const bool has_un = scheme.find("uncorrected") != std::string::npos;
+    if (!has_un && scheme.find("corrected") != std::string::npos) return true;
+    if (has_un || scheme.empty() || scheme == "Gauss linear" || scheme == "linear") return false;
+    throw Error(FVGB_ERR_UNSUPPORTED, "unknown snGrad scheme " + scheme);
+}
+
 class GaussGreenLaplacian {
 public:
-    explicit GaussGreenLaplacian(const UnstructuredMesh& m) : m_(m) {}
+    explicit GaussGreenLaplacian(const UnstructuredMesh& m, const std::string& scheme = "Gauss linear uncorrected")
+        : m_(m), corrected_(corrected_of(scheme)) {}
     void laplacian(DeviceArray<double>& out, const SurfaceField& gamma, const VolumeField& phi, double coeff = 1.0,
                    cudaStream_t st = nullptr) const {
-        check(fvgb_laplacian_explicit(m_.handle(), phi.ncomp(), gamma.internalVector().data(),
-                                      phi.internalVector().data(), phi.boundaryValues().data(), coeff, out.data(),
-                                      st));
+        auto fn = corrected_ ? fvgb_laplacian_explicit_corrected : fvgb_laplacian_explicit;
+        check(fn(m_.handle(), phi.ncomp(), gamma.internalVector().data(), phi.internalVector().data(),
+                 phi.boundaryValues().data(), coeff, out.data(), st));
     }
 
 private:
     const UnstructuredMesh& m_;
+    bool corrected_;
 };
 
 class FaceNormalGradient {
 public:
-    explicit FaceNormalGradient(const UnstructuredMesh& m) : m_(m) {}
+    explicit FaceNormalGradient(const UnstructuredMesh& m, const std::string& scheme = "uncorrected")
+        : m_(m), corrected_(corrected_of(scheme)) {}
     void faceNormalGrad(const VolumeField& phi, SurfaceField& out, cudaStream_t st = nullptr) const {
-        check(fvgb_sngrad(m_.handle(), phi.internalVector().data(), phi.boundaryValues().data(),
-                          out.internalVector().data(), st));
+        auto fn = corrected_ ? fvgb_sngrad_corrected : fvgb_sngrad;
+        check(fn(m_.handle(), phi.internalVector().data(), phi.boundaryValues().data(), out.internalVector().data(),
+                 st));
     }
 
 private:
     const UnstructuredMesh& m_;
+    bool corrected_;
+};
+
+// An OpenFOAM case mesh read from constant/polyMesh (ascii or binary); desc()
+// feeds UnstructuredMesh, readField/write the case's field files.
+class PolyMesh {
+public:
+    explicit PolyMesh(const std::string& dir) {
+        fvgb_polymesh* p = nullptr;
+        check(fvgb_polymesh_read(dir.c_str(), &p, &desc_));
+        h_.reset(p);
+    }
+    const fvgb_mesh_desc& desc() const { return desc_; }
+    fvgb_polymesh* handle() const { return h_.get(); }
+    // internalField [n*ncomp] on the host (n: cells, or internal faces for a surface field)
+    std::vector<double> readField(const std::string& path, int ncomp = 1, bool surface = false) const {
+        const int32_t n = surface ? desc_.n_ifaces : desc_.n_cells;
+        std::vector<double> v((size_t)n * ncomp);
+        check(fvgb_field_read(path.c_str(), n, ncomp, v.data()));
+        return v;
+    }
+    void write(const std::string& path, const std::string& object, int ncomp, const std::vector<double>& internal,
+               const std::vector<double>& boundary, int flags = 0) const {
+        check(fvgb_field_write(path.c_str(), object.c_str(), h_.get(), ncomp, internal.data(), boundary.data(),
+                               flags));
+    }
+
+private:
+    struct Free {
+        void operator()(fvgb_polymesh* p) const { fvgb_polymesh_free(p); }
+    };
+    std::unique_ptr<fvgb_polymesh, Free> h_;
+    fvgb_mesh_desc desc_{};
 };
 
 // ------------------------------------------------------------------- dsl
@@ -301,6 +347,14 @@ inline Expression ddt(const DeviceArray<double>& old) {
 }
 inline Expression laplacian(const SurfaceField& gamma) {
     return {{fvgb_term{FVGB_TERM_LAPLACIAN, 0, 1.0, nullptr, gamma.internalVector().data()}}};
+}
+// laplacian(gamma, psi) with a scheme; "Gauss linear corrected" adds the
+// non-orthogonal correction of psi's current values to the right-hand side.
+inline Expression laplacian(const SurfaceField& gamma, const VolumeField& psi,
+                            const std::string& scheme = "Gauss linear uncorrected") {
+    if (!corrected_of(scheme)) return laplacian(gamma);
+    return {{fvgb_term{FVGB_TERM_LAPLACIAN, FVGB_SCHEME_CORRECTED, 1.0, psi.internalVector().data(),
+                       gamma.internalVector().data()}}};
 }
 inline Expression div(const SurfaceField& flux, const std::string& scheme = "linear") {
     return {{fvgb_term{FVGB_TERM_DIV, scheme_of(scheme), 1.0, nullptr, flux.internalVector().data()}}};

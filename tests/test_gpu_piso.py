@@ -106,3 +106,53 @@ def test_cavity_mixed_pressure_matches_fp64(cuda):
     dU = np.abs(a.U.host() - b.U.host()).max()
     dp = np.abs(a.p.host() - b.p.host()).max()
     assert dU < 1e-6 and dp < 1e-6 * max(1.0, np.abs(a.p.host()).max())
+
+
+def test_ddt_corr_and_constrain_pressure_bit_exact(cuda):
+    hm = mesh.box(9, 8, 6, jitter=0.15, seed=22)
+    dm, o = DeviceMesh(hm), Oracle(hm)
+    rng = np.random.default_rng(1)
+    nf = hm.nif + hm.nbf
+    ubcs = [("fixedValue", rng.standard_normal(3)), ("noSlip", 0.0), ("zeroGradient", 0.0),
+            ("fixedValue", [1.0, 0.0, 0.0]), ("calculated", rng.standard_normal(3)), ("zeroGradient", 0.0)]
+    U = neon.VolumeField(dm, rng.standard_normal(3 * hm.n), ubcs, ncomp=3)
+    phi_old = rng.standard_normal(nf)
+    phi_old[::7] = 0.0                                   # |phi_old| = 0: the 1e-15 guard
+    rAUf = np.exp(rng.standard_normal(nf))
+    base = rng.standard_normal(nf)
+    out = neon.dev(base)
+    L, s = abi.lib(), torch.cuda.current_stream().cuda_stream
+    d_phi_old, d_rAUf = neon.dev(phi_old), neon.dev(rAUf)   # held until the kernels have run
+    abi.check(L.fvgb_piso_ddt_corr(dm.handle, abi.ptr(U.types), abi.ptr(U.internal), abi.ptr(U.boundary),
+                                   abi.ptr(d_phi_old), abi.ptr(d_rAUf), 2e-3, abi.ptr(out), s))
+    ref = o.ddt_corr(U.types, U.host(), U.boundary.cpu().numpy()[:3 * hm.nbf].copy(), phi_old, rAUf, 2e-3,
+                     base.copy())
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+    fixed = np.concatenate([np.arange(int(hm.patch_offsets[p]), int(hm.patch_offsets[p + 1]))
+                            for p in (0, 1, 3)]) + hm.nif
+    np.testing.assert_array_equal(ref[fixed], base[fixed])  # no correction where U is a fixed value
+    # constrainPressure on two fixedFluxPressure patches
+    flags = np.asarray([0, 1, 0, 0, 1, 0], np.int32)
+    phiHbyA = rng.standard_normal(nf)
+    pref = rng.standard_normal(hm.nbf)
+    dref, d_phiHbyA = neon.dev(pref), neon.dev(phiHbyA)
+    abi.check(L.fvgb_piso_constrain_pressure(dm.handle, abi.ptr(flags), abi.ptr(d_phiHbyA),
+                                             abi.ptr(U.boundary), abi.ptr(d_rAUf), abi.ptr(dref), s))
+    oref = o.constrain_pressure(flags, phiHbyA, U.boundary.cpu().numpy()[:3 * hm.nbf].copy(), rAUf, pref.copy())
+    np.testing.assert_array_equal(dref.cpu().numpy(), oref)
+
+
+@pytest.mark.parametrize("opts", [dict(ddt_corr=True), dict(corrected=True, n_non_orth=1),
+                                  dict(ddt_corr=True, corrected=True, n_non_orth=1)])
+def test_cavity_icofoam_options_bit_exact(cuda, opts):
+    """icoFoam's ddtCorr and non-orthogonal pressure correctors, which the
+    reference's loop leaves out, on a strongly jittered cavity: GPU = oracle."""
+    gpu = apps.CavityPiso(n=20, jitter=0.25, seed=5, dt=5e-3, n_corr=2, **opts)
+    cpu = CavityPisoCPU(gpu.hm, dt=5e-3, n_corr=2, **opts)
+    for _ in range(3):
+        gpu.step()
+        cpu.step()
+    assert [s[0] for s in gpu.stats] == [s[0] for s in cpu.stats]
+    np.testing.assert_array_equal(gpu.p.host(), cpu.p)
+    np.testing.assert_array_equal(gpu.U.host(), cpu.U)
+    np.testing.assert_array_equal(gpu.phi.host(), cpu.phi)

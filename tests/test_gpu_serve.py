@@ -150,8 +150,8 @@ def test_served_matches_python_driver(cuda):
     x, y, z = (hm.C[:, 0] - 0.5), (hm.C[:, 1] - 0.5), (hm.C[:, 2] - 0.5)
     T = neon.VolumeField(dm, np.exp(-(x * x + y * y + z * z) / (2 * 0.1 * 0.1)), [("zeroGradient", 0.0)] * 6)
     F = neon.SurfaceField(dm)
-    abi.check(abi.lib().fvgb_flux_vec(dm.handle, abi.ptr(neon.dev(np.tile(U, hm.n))),
-                                      abi.ptr(neon.dev(np.tile(U, hm.nbf))), abi.ptr(F.values),
+    Uc, Ub = neon.dev(np.tile(U, hm.n)), neon.dev(np.tile(U, hm.nbf))  # held until the kernel has run
+    abi.check(abi.lib().fvgb_flux_vec(dm.handle, abi.ptr(Uc), abi.ptr(Ub), abi.ptr(F.values),
                                       torch.cuda.current_stream().cuda_stream))
     gam = neon.SurfaceField(dm, np.full(hm.nif + hm.nbf, D))
     dt = 0.5 * (1.0 / max(nx, ny, nz)) / np.linalg.norm(U)

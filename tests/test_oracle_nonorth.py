@@ -73,3 +73,24 @@ def test_corrected_implicit_laplacian_reproduces_explicit_one():
     Ax_b = o.apply_operator(values, rhs, 1, T)
     lap = o.laplacian_corrected(1, gamma, T, Tb, 1.0, np.zeros(hm.n)) * hm.V
     np.testing.assert_allclose(Ax_b, lap, rtol=0, atol=1e-10 * np.abs(lap).max())
+
+
+@pytest.mark.parametrize("corrected,ddt_corr,n_non_orth", [(False, False, 0), (True, False, 0), (True, True, 1),
+                                                           (False, True, 0)])
+def test_cavity_loop_keeps_continuity(corrected, ddt_corr, n_non_orth):
+    """phi = phiHbyA - pEqn.flux() conserves mass in every cell to the pressure
+    solver's tolerance, with or without the corrected laplacian (its face-flux
+    correction taken with the pressure the matrix was assembled with) and ddtCorr."""
+    from oracle.apps import CavityPisoCPU
+
+    hm = mesh.box(14, 13, 1, 1.0, 1.0, 1.0 / 14, jitter=0.25, seed=5, two_d=True)
+    cpu = CavityPisoCPU(hm, dt=5e-3, n_corr=2, p_rel_tol=1e-12, ddt_corr=ddt_corr, corrected=corrected,
+                        n_non_orth=n_non_orth)
+    for _ in range(3):
+        cpu.step()
+    assert len(cpu.stats) == 3 * 2 * (n_non_orth + 1)
+    div = np.zeros(hm.n)
+    np.add.at(div, hm.own, cpu.phi[:hm.nif])
+    np.subtract.at(div, hm.nei, cpu.phi[:hm.nif])
+    np.add.at(div, hm.bcells, cpu.phi[hm.nif:])
+    assert np.abs(div).max() < 1e-9 * np.abs(cpu.phi).max()
