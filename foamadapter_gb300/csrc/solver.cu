@@ -58,6 +58,7 @@ struct CaseState {
     double sres, sig, isig;     // mixed: |s r| of the latest residual; power-of-two scale of rhat and 1/scale
     double omega;               // BiCGStab
     float falpha, fbeta, frel;  // frel: direction factor after a reliable update (-1: restart)
+    float fomega;               // mixed BiCGStab
     int32_t iter, status, total, outer, inner_it;
     int32_t active;        // FP64: iterating; mixed: refinement loop running
     int32_t inner_active;  // mixed: inner CG running
@@ -988,6 +989,314 @@ __global__ void __launch_bounds__(kT) k_ir_xupdate(Layout L, const float* __rest
     }
 }
 
+// ------------------------------------------------ mixed-precision BiCGStab
+// FP64 iterative refinement around a restarted FP32 BiCGStab (Jacobi, right
+// preconditioning) on the row-sign-normalised FP32 system of the mixed CG
+// (k_ir_prepare: a32, ev, dinv; difference-form SpMV; power-of-two residual
+// scale).  Each refinement step: r = b - A x in FP64, rh = sign*(float)(sig r),
+// then BiCGStab on (D_s A) e = rh from e = 0 with shadow residual rh, until
+// |r_inner|^2 <= itol = |rh|^2 max(inner_rel_tol^2, (tol/|r|)^2), the FP32
+// recursion breaks down, or the iteration caps are hit; x += e / sig.
+// Inner vectors (FP32): rh = r, rr (shadow), p, v, yv = |dinv| p, s, z =
+// |dinv| s, t, e.  Dots: per-thread fmaf, FP32 block trees, FP64 sums of the
+// block partials (as the mixed CG).
+
+// refinement step: r = b - A x (FP64) or the preparation's r0 (FIRST), |r|;
+// rh = rr = sign*(float)(sig r); p = v = e = 0; rho = rh.rh
+template <bool FIRST>
+__global__ void __launch_bounds__(kT)
+    k_mb_residual(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
+                  const double* __restrict__ r0, const float* __restrict__ dinv, float* __restrict__ rh,
+                  float* __restrict__ rr, float* __restrict__ p, float* __restrict__ v, float* __restrict__ e,
+                  double* __restrict__ pa, double* __restrict__ pb, double* __restrict__ pc,
+                  cudaGraphConditionalHandle h_outer, cudaGraphConditionalHandle h_inner) {
+    __shared__ double sma[kT], smb[kT], smc[kT];
+    __shared__ float smf[kT];
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (FIRST || ld_volatile(&cs->active)) {
+        const double* __restrict__ x = L.bs->prm.x;
+        double sig, isig;
+        residual_scale(cs->sres, &sig, &isig);
+        double arr = 0.0, asr = 0.0;
+        float arho = 0.0f;
+#pragma unroll
+        for (int j = 0; j < kRowsPerThread; ++j) {
+            const int i = blk_row(k, j);
+            if (i >= k.end) continue;
+            const double ri = FIRST ? r0[i] : __ldg(&b[i]) - spmv_row(m, val, x, i);
+            arr = fma(ri, ri, arr);
+            const float di = __ldg(&dinv[i]);
+            asr = fma(ri * (double)fabsf(di), ri, asr);
+            float rhi = (float)(ri * sig);
+            if (di < 0.0f) rhi = -rhi;
+            rh[i] = rhi;
+            rr[i] = rhi;
+            p[i] = 0.0f;
+            v[i] = 0.0f;
+            e[i] = 0.0f;
+            arho = fmaf(rhi, rhi, arho);
+        }
+        const double ba = block_tree(arr, sma);
+        const double bc = block_tree(asr, smc);
+        const float bb = block_tree_f(arho, smf);
+        if (threadIdx.x == 0) {
+            pa[blockIdx.x] = ba;
+            pb[blockIdx.x] = (double)bb;
+            pc[blockIdx.x] = bc;
+        }
+        if (arrive_last(&cs->counter, k.nbc)) {
+            const double rr2 = final_tree(pa + k.blk0, k.nbc, sma), rho = final_tree(pb + k.blk0, k.nbc, smb);
+            const double sr2 = final_tree(pc + k.blk0, k.nbc, smc);
+            if (threadIdx.x == 0) {
+                const SolverParams& prm = L.bs->prm;
+                const double res = sqrt(rr2);
+                if (!FIRST) cs->outer += 1;
+                cs->res = res;
+                bool done = false;
+                if (FIRST) {
+                    cs->res0 = res;
+                    double tol = prm.rel_tol * res;
+                    if (prm.abs_tol > tol) tol = prm.abs_tol;
+                    cs->tol = tol;
+                    const unsigned int sf = cs->signflags;
+                    if ((sf & 4u) || sf == 3u) {
+                        cs->status = FVGB_ERR_UNSUPPORTED;
+                        done = true;
+                    }
+                }
+                if (!done) {
+                    if (!isfinite(res)) {
+                        cs->status = FVGB_ERR_BREAKDOWN;
+                        done = true;
+                    } else if (!(res > cs->tol) || res == 0.0) {
+                        done = true;
+                    } else if (cs->outer >= prm.max_outer || cs->total >= prm.max_iter) {
+                        cs->status = FVGB_ERR_NOT_CONVERGED;
+                        done = true;
+                    }
+                }
+                cs->sig = sig;
+                cs->isig = isig;
+                cs->sres = sqrt(sr2);
+                cs->rho = rho;
+                cs->rho_prev = 1.0;
+                cs->alpha = 1.0;
+                cs->omega = 1.0;
+                cs->falpha = 1.0f;
+                cs->fomega = 1.0f;
+                cs->fbeta = 0.0f;  // p = r on the first inner iteration
+                cs->half = 0;
+                const double dr = prm.inner_rel_tol * prm.inner_rel_tol;
+                const double dt = (cs->tol / res) * (cs->tol / res);
+                cs->itol = rho * (dr > dt ? dr : dt);
+                cs->inner_it = 0;
+                const bool inner = !done && rho > cs->itol && prm.inner_max_iter > 0 && cs->total < prm.max_iter;
+                cs->inner_active = inner ? 1 : 0;
+                if (inner) atomicAdd(&L.bs->n_inner, 1);
+                if (done) case_done(L.bs, cs);
+            }
+        }
+    }
+    if (arrive_last(&L.bs->gcounter, gridDim.x) && threadIdx.x == 0) {
+        cudaGraphSetConditional(h_inner, ld_volatile(&L.bs->n_inner) > 0 ? 1u : 0u);
+        cudaGraphSetConditional(h_outer, ld_volatile(&L.bs->n_active) > 0 ? 1u : 0u);
+    }
+}
+
+// an FP32 breakdown ends the inner solve; before its first iteration it ends the case
+__device__ __forceinline__ void mb_breakdown(const Layout& L, CaseState* cs) {
+    inner_stop(L, cs);
+    if (cs->inner_it == 0) {
+        cs->status = FVGB_ERR_BREAKDOWN;
+        case_done(L.bs, cs);
+    }
+}
+
+// p = r + beta (p - omega v), yv = |dinv| p
+__global__ void __launch_bounds__(kT)
+    k_mb_dir(Layout L, const float* __restrict__ dinv, const float* __restrict__ rh, const float* __restrict__ v,
+             float* __restrict__ p, float* __restrict__ yv) {
+    const Blk k = blk_info(L);
+    const CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->inner_active)) return;
+    const float fb = cs->fbeta, fo = cs->fomega;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const float pi = fmaf(fb, fmaf(-fo, __ldg(&v[i]), p[i]), __ldg(&rh[i]));
+        p[i] = pi;
+        yv[i] = fabsf(__ldg(&dinv[i])) * pi;
+    }
+}
+
+// v = (D_s A) yv, alpha = rho / (rr . v)
+__global__ void __launch_bounds__(kT)
+    k_mb_spmv1(Layout L, MeshView m, const float* __restrict__ a32, const float* __restrict__ ev,
+               const float* __restrict__ yv, const float* __restrict__ rr, float* __restrict__ v,
+               double* __restrict__ pa) {
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->inner_active)) return;
+    __shared__ double sma[kT];
+    __shared__ float smf[kT];
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const float vi = spmv_row_diff(m, a32, yv, i, __ldg(&yv[i]), __ldg(&ev[i]));
+        v[i] = vi;
+        acc = fmaf(__ldg(&rr[i]), vi, acc);
+    }
+    const float ba = block_tree_f(acc, smf);
+    if (threadIdx.x == 0) pa[blockIdx.x] = (double)ba;
+    if (!arrive_last(&cs->counter, k.nbc)) return;
+    const double rv = final_tree(pa + k.blk0, k.nbc, sma);
+    if (threadIdx.x == 0) {
+        const double alpha = cs->rho / rv;
+        if (rv == 0.0 || !isfinite(alpha)) {
+            mb_breakdown(L, cs);
+        } else {
+            cs->alpha = alpha;
+            cs->falpha = (float)alpha;
+        }
+    }
+}
+
+// s = r - alpha v, z = |dinv| s, |s|^2 (at or below itol: the half step ends the inner solve)
+__global__ void __launch_bounds__(kT)
+    k_mb_s(Layout L, const float* __restrict__ dinv, const float* __restrict__ rh, const float* __restrict__ v,
+           float* __restrict__ sv, float* __restrict__ z, double* __restrict__ pa) {
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->inner_active)) return;
+    __shared__ double sma[kT];
+    __shared__ float smf[kT];
+    const float fa = cs->falpha;
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const float si = fmaf(-fa, __ldg(&v[i]), __ldg(&rh[i]));
+        sv[i] = si;
+        z[i] = fabsf(__ldg(&dinv[i])) * si;
+        acc = fmaf(si, si, acc);
+    }
+    const float ba = block_tree_f(acc, smf);
+    if (threadIdx.x == 0) pa[blockIdx.x] = (double)ba;
+    if (!arrive_last(&cs->counter, k.nbc)) return;
+    const double ss = final_tree(pa + k.blk0, k.nbc, sma);
+    if (threadIdx.x == 0) {
+        if (!isfinite(ss)) mb_breakdown(L, cs);
+        else if (!(ss > cs->itol)) cs->half = 1;
+    }
+}
+
+// half step: e += alpha yv, inner solve done; else t = (D_s A) z, omega = (t.s)/(t.t)
+__global__ void __launch_bounds__(kT)
+    k_mb_spmv2(Layout L, MeshView m, const float* __restrict__ a32, const float* __restrict__ ev,
+               const float* __restrict__ z, const float* __restrict__ sv, const float* __restrict__ yv,
+               float* __restrict__ t, float* __restrict__ e, double* __restrict__ pa, double* __restrict__ pb) {
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->inner_active)) return;
+    __shared__ double sma[kT], smb[kT];
+    __shared__ float smf[kT], smg[kT];
+    if (ld_volatile(&cs->half)) {
+        const float fa = cs->falpha;
+#pragma unroll
+        for (int j = 0; j < kRowsPerThread; ++j) {
+            const int i = blk_row(k, j);
+            if (i >= k.end) continue;
+            e[i] = fmaf(fa, __ldg(&yv[i]), e[i]);
+        }
+        if (arrive_last(&cs->counter, k.nbc) && threadIdx.x == 0) {
+            cs->inner_it += 1;
+            cs->total += 1;
+            cs->half = 0;
+            inner_stop(L, cs);
+        }
+        return;
+    }
+    float ats = 0.0f, att = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const float ti = spmv_row_diff(m, a32, z, i, __ldg(&z[i]), __ldg(&ev[i]));
+        t[i] = ti;
+        ats = fmaf(ti, __ldg(&sv[i]), ats);
+        att = fmaf(ti, ti, att);
+    }
+    const float ba = block_tree_f(ats, smf), bb = block_tree_f(att, smg);
+    if (threadIdx.x == 0) {
+        pa[blockIdx.x] = (double)ba;
+        pb[blockIdx.x] = (double)bb;
+    }
+    if (!arrive_last(&cs->counter, k.nbc)) return;
+    const double ts = final_tree(pa + k.blk0, k.nbc, sma), tt = final_tree(pb + k.blk0, k.nbc, smb);
+    if (threadIdx.x == 0) {
+        const double omega = ts / tt;
+        if (tt == 0.0 || !isfinite(omega) || omega == 0.0) {
+            mb_breakdown(L, cs);
+        } else {
+            cs->omega = omega;
+            cs->fomega = (float)omega;
+        }
+    }
+}
+
+// e += alpha yv + omega z, r = s - omega t, rho = rr . r, |r|^2
+__global__ void __launch_bounds__(kT)
+    k_mb_update(Layout L, const float* __restrict__ yv, const float* __restrict__ z, const float* __restrict__ sv,
+                const float* __restrict__ t, const float* __restrict__ rr, float* __restrict__ rh,
+                float* __restrict__ e, double* __restrict__ pa, double* __restrict__ pb,
+                cudaGraphConditionalHandle h_inner) {
+    __shared__ double sma[kT], smb[kT];
+    __shared__ float smf[kT], smg[kT];
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (ld_volatile(&cs->inner_active)) {
+        const float fa = cs->falpha, fo = cs->fomega;
+        float arho = 0.0f, arr = 0.0f;
+#pragma unroll
+        for (int j = 0; j < kRowsPerThread; ++j) {
+            const int i = blk_row(k, j);
+            if (i >= k.end) continue;
+            e[i] = fmaf(fo, __ldg(&z[i]), fmaf(fa, __ldg(&yv[i]), e[i]));
+            const float ri = fmaf(-fo, __ldg(&t[i]), __ldg(&sv[i]));
+            rh[i] = ri;
+            arho = fmaf(__ldg(&rr[i]), ri, arho);
+            arr = fmaf(ri, ri, arr);
+        }
+        const float ba = block_tree_f(arho, smf), bb = block_tree_f(arr, smg);
+        if (threadIdx.x == 0) {
+            pa[blockIdx.x] = (double)ba;
+            pb[blockIdx.x] = (double)bb;
+        }
+        if (arrive_last(&cs->counter, k.nbc)) {
+            const double rho = final_tree(pa + k.blk0, k.nbc, sma), r2 = final_tree(pb + k.blk0, k.nbc, smb);
+            if (threadIdx.x == 0) {
+                const SolverParams& prm = L.bs->prm;
+                cs->inner_it += 1;
+                cs->total += 1;
+                const double beta = (rho / cs->rho) * (cs->alpha / cs->omega);
+                cs->rho_prev = cs->rho;
+                cs->rho = rho;
+                cs->fbeta = (float)beta;
+                const bool more = r2 > cs->itol && isfinite(r2) && rho != 0.0 && isfinite(beta) &&
+                                  cs->inner_it < prm.inner_max_iter && cs->total < prm.max_iter;
+                if (!more) inner_stop(L, cs);
+            }
+        }
+    }
+    if (arrive_last(&L.bs->gcounter, gridDim.x) && threadIdx.x == 0)
+        cudaGraphSetConditional(h_inner, ld_volatile(&L.bs->n_inner) > 0 ? 1u : 0u);
+}
+
 // State for timing the FP32 kernels outside a solve: every case's inner solve
 // active with rho = 1, a direction of pseudo-random O(1) values.
 __global__ void k_tune_mixed_state(Layout L, float* __restrict__ p, float* __restrict__ rh, float* __restrict__ y) {
@@ -1764,7 +2073,8 @@ struct SolverCache {
     double* pc = nullptr;
     float *ah = nullptr, *dinvf = nullptr, *ev = nullptr, *rh = nullptr, *y = nullptr, *pf = nullptr,
           *qf = nullptr;
-    cudaGraphExec_t g64 = nullptr, gmix = nullptr, gbi = nullptr;
+    cudaGraphExec_t g64 = nullptr, gmix = nullptr, gbi = nullptr, gmb = nullptr;
+    float *mb_rr = nullptr, *mb_yv = nullptr, *mb_t = nullptr;  // mixed BiCGStab (with rh, y, pf, qf, pf2, zf)
     double *bi_rr = nullptr, *bi_v = nullptr, *bi_y = nullptr, *bi_s = nullptr, *bi_t = nullptr;  // BiCGStab
     fvgb_solver_stats* h_stats = nullptr;  // pinned [ncases]
     GridBar* bar = nullptr;
@@ -1788,6 +2098,7 @@ void fvgb_solver_cache_free(SolverCache* c) {
     if (c->g64) cudaGraphExecDestroy(c->g64);
     if (c->gmix) cudaGraphExecDestroy(c->gmix);
     if (c->gbi) cudaGraphExecDestroy(c->gbi);
+    if (c->gmb) cudaGraphExecDestroy(c->gmb);
     for (void* p : c->allocs) cudaFree(p);
     if (c->h_stats) cudaFreeHost(c->h_stats);
     if (c->h_active) cudaFreeHost(c->h_active);
@@ -2100,7 +2411,7 @@ fvgb_status graph_mixed(SolverCache* c) {
     return FVGB_OK;
 }
 
-fvgb_status build_mixed(SolverCache* c, bool measure = true) {
+fvgb_status alloc_mixed(SolverCache* c) {
     const size_t n = (size_t)c->n;
     if (!c->ah) {
         cudaError_t e = calloc_dev(c, &c->ah, (size_t)c->ls->mesh->m_len);
@@ -2116,6 +2427,12 @@ fvgb_status build_mixed(SolverCache* c, bool measure = true) {
         if (e == cudaSuccess) e = settle_creation();
         if (e != cudaSuccess) return cuda_fail(e, "mixed CG workspace");
     }
+    return FVGB_OK;
+}
+
+fvgb_status build_mixed(SolverCache* c, bool measure = true) {
+    fvgb_status ast = alloc_mixed(c);
+    if (ast != FVGB_OK) return ast;
     if (!c->tunedmx) {
         fvgb_status st = tune_mixed(c, measure);
         if (st != FVGB_OK) return st;
@@ -2183,6 +2500,72 @@ fvgb_status build_bicgstab(SolverCache* c) {
     return FVGB_OK;
 }
 
+// The mixed-precision BiCGStab as graph nodes in `g` after `deps`: the
+// preparation of the FP32 system, the first refinement step, then
+// while (refining) { while (inner) { dir, spmv1, s, spmv2, update }; x += e/sig;
+// refinement step }.  Vectors: rh = r, y = e, pf = p, qf = v, pf2 = s, zf = z.
+cudaError_t add_mixed_bicgstab_nodes(SolverCache* c, cudaGraph_t g, const cudaGraphNode_t* deps, size_t ndeps,
+                                     cudaGraphNode_t* last) {
+    const fvgb_ls* ls = c->ls;
+    MeshView m = ls->mesh->v;
+    Layout L = c->L;
+    cudaGraphConditionalHandle ho, hi;
+    const double* val = ls->values;
+    const double* b = ls->rhs;
+    const unsigned nb = (unsigned)c->nb;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&ho, g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, g, 0, cudaGraphCondAssignDefault);
+    cudaGraphNode_t n_prep, n_res0, n_outer, o_inner, o_x, o_res, i0, i1, i2, i3, i4;
+    cudaGraph_t obody = nullptr, ibody = nullptr;
+    void* a_prep[] = {&L, &m, &val, &b, &c->ah, &c->ev, &c->dinvf, &c->r0, &c->pa};
+    void* a_res[] = {&L,     &m,     &val,  &b,     &c->r0, &c->dinvf, &c->rh, &c->mb_rr,
+                     &c->pf, &c->qf, &c->y, &c->pa, &c->pb, &c->pc,    &ho,    &hi};
+    void* a_dir[] = {&L, &c->dinvf, &c->rh, &c->qf, &c->pf, &c->mb_yv};
+    void* a_sp1[] = {&L, &m, &c->ah, &c->ev, &c->mb_yv, &c->mb_rr, &c->qf, &c->pa};
+    void* a_s[] = {&L, &c->dinvf, &c->rh, &c->qf, &c->pf2, &c->zf, &c->pa};
+    void* a_sp2[] = {&L, &m, &c->ah, &c->ev, &c->zf, &c->pf2, &c->mb_yv, &c->mb_t, &c->y, &c->pa, &c->pb};
+    void* a_upd[] = {&L, &c->mb_yv, &c->zf, &c->pf2, &c->mb_t, &c->mb_rr, &c->rh, &c->y, &c->pa, &c->pb, &hi};
+    void* a_x[] = {&L, &c->y};
+    void* a_fin[] = {&L};
+    if (e == cudaSuccess) e = add_kernel_deps(g, &n_prep, deps, ndeps, (void*)k_ir_prepare, nb, kT, a_prep);
+    if (e == cudaSuccess) e = add_kernel(g, &n_res0, &n_prep, (void*)k_mb_residual<true>, nb, kT, a_res);
+    if (e == cudaSuccess) e = add_while(g, &n_outer, &n_res0, ho, &obody);
+    if (e == cudaSuccess) e = add_while(obody, &o_inner, nullptr, hi, &ibody);
+    if (e == cudaSuccess) e = add_kernel(ibody, &i0, nullptr, (void*)k_mb_dir, nb, kT, a_dir);
+    if (e == cudaSuccess) e = add_kernel(ibody, &i1, &i0, (void*)k_mb_spmv1, nb, kT, a_sp1);
+    if (e == cudaSuccess) e = add_kernel(ibody, &i2, &i1, (void*)k_mb_s, nb, kT, a_s);
+    if (e == cudaSuccess) e = add_kernel(ibody, &i3, &i2, (void*)k_mb_spmv2, nb, kT, a_sp2);
+    if (e == cudaSuccess) e = add_kernel(ibody, &i4, &i3, (void*)k_mb_update, nb, kT, a_upd);
+    if (e == cudaSuccess) e = add_kernel(obody, &o_x, &o_inner, (void*)k_ir_xupdate, nb, kT, a_x);
+    if (e == cudaSuccess) e = add_kernel(obody, &o_res, &o_x, (void*)k_mb_residual<false>, nb, kT, a_res);
+    if (e == cudaSuccess) e = add_kernel(g, last, &n_outer, (void*)k_finish, grid_for(c->ncases, 128), 128, a_fin);
+    return e;
+}
+
+fvgb_status build_mixed_bicgstab(SolverCache* c) {
+    fvgb_status st = alloc_mixed(c);
+    if (st != FVGB_OK) return st;
+    const size_t n = (size_t)c->n;
+    cudaError_t e = cudaSuccess;
+    if (!c->mb_rr) e = calloc_dev(c, &c->mb_rr, n);
+    if (e == cudaSuccess && !c->mb_yv) e = calloc_dev(c, &c->mb_yv, n);
+    if (e == cudaSuccess && !c->mb_t) e = calloc_dev(c, &c->mb_t, n);
+    if (e == cudaSuccess) e = settle_creation();
+    if (e != cudaSuccess) return cuda_fail(e, "mixed BiCGStab workspace");
+    if (c->gmb) {
+        cudaGraphExecDestroy(c->gmb);
+        c->gmb = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t last;
+    e = add_mixed_bicgstab_nodes(c, g, nullptr, 0, &last);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->gmb, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "mixed BiCGStab graph");
+    return FVGB_OK;
+}
+
 fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
     FVGB_CHECK_ARG(cfg->precision == FVGB_PREC_FP64 || cfg->precision == FVGB_PREC_MIXED_IR,
                    "fvgb_solve: unknown precision");
@@ -2191,11 +2574,8 @@ fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
     FVGB_CHECK_ARG(cfg->kernel_mode >= 0 && cfg->kernel_mode <= 3, "fvgb_solve: bad kernel_mode");
     FVGB_CHECK_ARG((cfg->flags & ~FVGB_SOLVE_NO_TUNE) == 0, "fvgb_solve: unknown flags");
     FVGB_CHECK_ARG(cfg->method == FVGB_SOLVER_CG || cfg->method == FVGB_SOLVER_BICGSTAB, "fvgb_solve: unknown method");
-    if (cfg->method == FVGB_SOLVER_BICGSTAB) {
-        if (cfg->precision != FVGB_PREC_FP64)
-            return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_solve: BiCGStab runs in FP64 only");
+    if (cfg->method == FVGB_SOLVER_BICGSTAB)
         FVGB_CHECK_ARG(cfg->kernel_mode != 3, "fvgb_solve: the host-driven loop is CG only");
-    }
     FVGB_CHECK_ARG(cfg->kernel_mode != 3 || cfg->precision == FVGB_PREC_FP64,
                    "fvgb_solve: the host-driven loop (kernel_mode 3) is FP64 only");
     if (cfg->precision == FVGB_PREC_MIXED_IR)
@@ -2273,8 +2653,13 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
     fvgb_status stt = check_cfg(cfg);
     if (stt != FVGB_OK) return stt;
     const bool measure = !(cfg->flags & FVGB_SOLVE_NO_TUNE);
-    if (cfg->method == FVGB_SOLVER_BICGSTAB && !c->gbi) {
+    const bool mixed_ir = cfg->precision == FVGB_PREC_MIXED_IR;
+    if (cfg->method == FVGB_SOLVER_BICGSTAB && !mixed_ir && !c->gbi) {
         stt = build_bicgstab(c);
+        if (stt != FVGB_OK) return stt;
+    }
+    if (cfg->method == FVGB_SOLVER_BICGSTAB && mixed_ir && !c->gmb) {
+        stt = build_mixed_bicgstab(c);
         if (stt != FVGB_OK) return stt;
     }
     if (cfg->method == FVGB_SOLVER_CG && cfg->precision == FVGB_PREC_FP64 && !c->g64) {
@@ -2299,7 +2684,7 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
     k_set_params<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L, c->ncases, prm);
     FVGB_LAUNCH_CHECK("fvgb_solve: parameters");
     if (cfg->method == FVGB_SOLVER_BICGSTAB) {
-        FVGB_CUDA_TRY(cudaGraphLaunch(c->gbi, s));
+        FVGB_CUDA_TRY(cudaGraphLaunch(mixed_ir ? c->gmb : c->gbi, s));
         return FVGB_OK;
     }
     if (cfg->kernel_mode == 3) return host_loop(c, s);
@@ -2453,7 +2838,8 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
     const bool mixed = cfg->precision == FVGB_PREC_MIXED_IR;
     const bool measure = !(cfg->flags & FVGB_SOLVE_NO_TUNE);
     const bool bicg = cfg->method == FVGB_SOLVER_BICGSTAB;
-    fst = bicg ? build_bicgstab(c) : (mixed ? build_mixed(c, measure) : build_fp64(c, measure));
+    fst = bicg ? (mixed ? build_mixed_bicgstab(c) : build_bicgstab(c))
+               : (mixed ? build_mixed(c, measure) : build_fp64(c, measure));
     if (fst != FVGB_OK) return fst;
     SolverParams prm{};
     prm.x = psi;
@@ -2486,7 +2872,8 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
         e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
         cudaGraphNode_t last;
         if (e == cudaSuccess)
-            e = bicg ? add_bicgstab_nodes(c, cg, deps, nd, &last)
+            e = bicg ? (mixed ? add_mixed_bicgstab_nodes(c, cg, deps, nd, &last)
+                              : add_bicgstab_nodes(c, cg, deps, nd, &last))
                      : (mixed ? add_mixed_nodes(c, cg, deps, nd, &last) : add_fp64_nodes(c, cg, deps, nd, &last));
         if (e == cudaSuccess)
             e = cudaStreamUpdateCaptureDependencies(cs, &last, nullptr, 1, cudaStreamSetCaptureDependencies);

@@ -298,7 +298,8 @@ typedef struct fvgb_solver_cfg {
                                   at the first solve (the timing synchronises the device) */
     int32_t method;            /* FVGB_SOLVER_CG (Ginkgo Cg) or FVGB_SOLVER_BICGSTAB
                                   (Ginkgo Bicgstab, fvSolution.cpp:25-26: nonsymmetric
-                                  systems; FP64, graph path)                             */
+                                  systems; graph path; MIXED_IR: FP32 inner BiCGStab,
+                                  restarted every refinement step)                       */
 } fvgb_solver_cfg;
 enum { FVGB_SOLVE_NO_TUNE = 1 };
 enum { FVGB_SOLVER_CG = 0, FVGB_SOLVER_BICGSTAB = 1 };

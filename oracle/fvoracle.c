@@ -792,14 +792,13 @@ static double residual_step(const or_csr* A, const double* val, const double* b,
     return sqrt(final_tree(nb, part));
 }
 
-static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, double* x,
-                           const or_solver_cfg* cfg, or_solver_stats* st) {
-    const int32_t n = A->n, nb = nblocks_of(n), nnz = A->nnz;
-    float* dinv = (float*)calloc(n ? n : 1, sizeof(float));
-    float* ev = (float*)calloc(n ? n : 1, sizeof(float));
-    float* a32 = (float*)calloc((size_t)(nnz ? nnz : 1), sizeof(float));
+/* The row-sign-normalised FP32 system (solver.cu k_ir_prepare): dinv = (float)(1/a_ii),
+ * a32 = (float)(sign*a_ij) off the diagonal (0 on it), ev = (float)(sign*e_i), e_i the
+ * FP64 row sum in column order.  Returns the sign flags: bit0 a positive diagonal,
+ * bit1 negative, bit2 zero/NaN. */
+static unsigned prepare_f32(const or_csr* A, const double* val, float* dinv, float* ev, float* a32) {
     unsigned flags = 0;
-    for (int32_t i = 0; i < n; ++i) {
+    for (int32_t i = 0; i < A->n; ++i) {
         double d = val[A->row_offs[i] + A->diag_off[i]];
         flags |= d > 0.0 ? 1u : (d < 0.0 ? 2u : 4u);
         dinv[i] = (float)(1.0 / d);
@@ -810,6 +809,27 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
         }
         ev[i] = (float)(sg * e);
     }
+    return flags;
+}
+
+/* q = (D_s A) x in the difference form, fmaf chain in column order */
+static void spmv_diff_f(const or_csr* A, const float* a32, const float* ev, const float* x, float* q) {
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < A->n; ++i) {
+        const float xi = x[i];
+        float acc = 0.0f;
+        for (int32_t j = A->row_offs[i]; j < A->row_offs[i + 1]; ++j) acc = fmaf(a32[j], x[A->col[j]] - xi, acc);
+        q[i] = fmaf(ev[i], xi, acc);
+    }
+}
+
+static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, double* x,
+                           const or_solver_cfg* cfg, or_solver_stats* st) {
+    const int32_t n = A->n, nb = nblocks_of(n), nnz = A->nnz;
+    float* dinv = (float*)calloc(n ? n : 1, sizeof(float));
+    float* ev = (float*)calloc(n ? n : 1, sizeof(float));
+    float* a32 = (float*)calloc((size_t)(nnz ? nnz : 1), sizeof(float));
+    unsigned flags = prepare_f32(A, val, dinv, ev, a32);
     if ((flags & 4u) || flags == 3u) {
         free(dinv); free(ev); free(a32);
         st->status = ST_UNSUPPORTED;
@@ -1008,10 +1028,129 @@ static int32_t solve_bicgstab(const or_csr* A, const double* val, const double* 
     return status;
 }
 
+/* ---------------------------------------------------- mixed-precision BiCGStab
+ * FP64 iterative refinement around a restarted FP32 BiCGStab on the
+ * row-sign-normalised system (solver.cu mixed BiCGStab section, same operation
+ * order): each refinement step r = b - A x, rh = sign*(float)(sig r), then from
+ * e = 0, rr = rh, p = v = 0, rho = rh.rh, fbeta = 0, alpha = omega = 1:
+ *   p = r + beta (p - omega v); yv = |dinv| p; v = A32 yv; alpha = rho/(rr.v)
+ *   s = r - alpha v; z = |dinv| s; |s|^2 <= itol: e += alpha yv, stop
+ *   t = A32 z; omega = (t.s)/(t.t); e += alpha yv + omega z; r = s - omega t
+ *   beta = (rr.r / rho)(alpha/omega); stop when |r|^2 <= itol
+ * itol = rho0 max(inner_rel_tol^2, (tol/|r|)^2); x += e / sig. */
+static int32_t solve_mixed_bicgstab(const or_csr* A, const double* val, const double* b, double* x,
+                                    const or_solver_cfg* cfg, or_solver_stats* st) {
+    const int32_t n = A->n, nb = nblocks_of(n), nnz = A->nnz;
+    const size_t nn = n ? (size_t)n : 1;
+    float* dinv = (float*)calloc(nn, sizeof(float));
+    float* ev = (float*)calloc(nn, sizeof(float));
+    float* a32 = (float*)calloc((size_t)(nnz ? nnz : 1), sizeof(float));
+    unsigned flags = prepare_f32(A, val, dinv, ev, a32);
+    double *part = zalloc(nb), *part2 = zalloc(nb);
+    float *r = (float*)calloc(nn, sizeof(float)), *rr = (float*)calloc(nn, sizeof(float));
+    float *p = (float*)calloc(nn, sizeof(float)), *v = (float*)calloc(nn, sizeof(float));
+    float *yv = (float*)calloc(nn, sizeof(float)), *sv = (float*)calloc(nn, sizeof(float));
+    float *z = (float*)calloc(nn, sizeof(float)), *t = (float*)calloc(nn, sizeof(float));
+    float *e = (float*)calloc(nn, sizeof(float)), *scratch = (float*)calloc(nn, sizeof(float));
+    const double dr = cfg->inner_rel_tol * cfg->inner_rel_tol;
+    int32_t total = 0, outer = 0, status = ST_OK;
+    double res, res0, tol, sres, sig, isig;
+    residual_step(A, val, b, x, dinv, 1.0, r, scratch, part, part2, n, nb, &sres);
+    residual_scale(sres, &sig, &isig);
+    res = residual_step(A, val, b, x, dinv, sig, r, scratch, part, part2, n, nb, &sres);
+    res0 = res;
+    tol = cfg->rel_tol * res0;
+    if (cfg->abs_tol > tol) tol = cfg->abs_tol;
+    int done = 0;
+    if ((flags & 4u) || flags == 3u) { status = ST_UNSUPPORTED; done = 1; }
+    else if (!isfinite(res)) { status = ST_BREAKDOWN; done = 1; }
+    else if (!(res > tol) || res == 0.0) done = 1;
+    else if (cfg->max_outer <= 0 || cfg->max_iter <= 0) { status = ST_NOT_CONVERGED; done = 1; }
+    for (;;) {
+        /* the inner solve of this refinement step */
+        for (int32_t i = 0; i < n; ++i) { rr[i] = r[i]; p[i] = 0.0f; v[i] = 0.0f; e[i] = 0.0f; }
+        double rho = dot_tree_f(n, r, r, part), alpha = 1.0, omega = 1.0;
+        float fa = 1.0f, fo = 1.0f, fb = 0.0f;
+        double itol;
+        { double dt = (tol / res) * (tol / res); itol = rho * (dr > dt ? dr : dt); }
+        int32_t inner_it = 0;
+        int inner = !done && rho > itol && cfg->inner_max_iter > 0 && total < cfg->max_iter;
+        while (inner) {
+            for (int32_t i = 0; i < n; ++i) {
+                p[i] = fmaf(fb, fmaf(-fo, v[i], p[i]), r[i]);
+                yv[i] = fabsf(dinv[i]) * p[i];
+            }
+            spmv_diff_f(A, a32, ev, yv, v);
+            double rv = dot_tree_f(n, rr, v, part);
+            double al = rho / rv;
+            if (rv == 0.0 || !isfinite(al)) {
+                if (inner_it == 0) { status = ST_BREAKDOWN; done = 1; }
+                break;
+            }
+            alpha = al;
+            fa = (float)alpha;
+            for (int32_t i = 0; i < n; ++i) {
+                sv[i] = fmaf(-fa, v[i], r[i]);
+                z[i] = fabsf(dinv[i]) * sv[i];
+            }
+            double ss = dot_tree_f(n, sv, sv, part);
+            if (!isfinite(ss)) {
+                if (inner_it == 0) { status = ST_BREAKDOWN; done = 1; }
+                break;
+            }
+            if (!(ss > itol)) { /* half step */
+                for (int32_t i = 0; i < n; ++i) e[i] = fmaf(fa, yv[i], e[i]);
+                ++inner_it;
+                ++total;
+                break;
+            }
+            spmv_diff_f(A, a32, ev, z, t);
+            double ts = dot_tree_f(n, t, sv, part), tt = dot_tree_f(n, t, t, part2);
+            double om = ts / tt;
+            if (tt == 0.0 || !isfinite(om) || om == 0.0) {
+                if (inner_it == 0) { status = ST_BREAKDOWN; done = 1; }
+                break;
+            }
+            omega = om;
+            fo = (float)omega;
+            for (int32_t i = 0; i < n; ++i) {
+                e[i] = fmaf(fo, z[i], fmaf(fa, yv[i], e[i]));
+                r[i] = fmaf(-fo, t[i], sv[i]);
+            }
+            double rhon = dot_tree_f(n, rr, r, part), r2 = dot_tree_f(n, r, r, part2);
+            ++inner_it;
+            ++total;
+            double beta = (rhon / rho) * (alpha / omega);
+            rho = rhon;
+            fb = (float)beta;
+            int more = r2 > itol && isfinite(r2) && rho != 0.0 && isfinite(beta) && inner_it < cfg->inner_max_iter &&
+                       total < cfg->max_iter;
+            if (!more) break;
+        }
+        if (done) break;
+        for (int32_t i = 0; i < n; ++i) x[i] = fma((double)e[i], isig, x[i]);
+        residual_scale(sres, &sig, &isig);
+        res = residual_step(A, val, b, x, dinv, sig, r, scratch, part, part2, n, nb, &sres);
+        ++outer;
+        if (!isfinite(res)) { status = ST_BREAKDOWN; done = 1; }
+        else if (!(res > tol) || res == 0.0) done = 1;
+        else if (outer >= cfg->max_outer || total >= cfg->max_iter) { status = ST_NOT_CONVERGED; done = 1; }
+        if (done) break;
+    }
+    st->init_res_norm = res0;
+    st->final_res_norm = res;
+    st->num_iter = total;
+    st->num_outer = outer;
+    st->status = status;
+    free(dinv); free(ev); free(a32); free(part); free(part2); free(r); free(rr); free(p); free(v); free(yv);
+    free(sv); free(z); free(t); free(e); free(scratch);
+    return status;
+}
+
 int32_t or_solve(const or_csr* A, const double* values, const double* rhs, double* x,
                  const or_solver_cfg* cfg, or_solver_stats* stats) {
     if (cfg->method == 1) {
-        if (cfg->precision != 0) { stats->status = ST_UNSUPPORTED; return ST_UNSUPPORTED; }
+        if (cfg->precision == 1) return solve_mixed_bicgstab(A, values, rhs, x, cfg, stats);
         return solve_bicgstab(A, values, rhs, x, cfg, stats);
     }
     if (cfg->precision == 1) return solve_mixed(A, values, rhs, x, cfg, stats);

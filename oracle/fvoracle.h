@@ -49,7 +49,7 @@ typedef struct or_solver_cfg {
     int32_t max_iter, precision;
     double inner_rel_tol;
     int32_t inner_max_iter, max_outer;
-    int32_t method, pad; /* 0 CG, 1 BiCGStab (FP64 only) */
+    int32_t method, pad; /* 0 CG, 1 BiCGStab (FP64 or mixed) */
 } or_solver_cfg;
 
 typedef struct or_solver_stats {

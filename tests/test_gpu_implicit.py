@@ -368,14 +368,35 @@ def test_bicgstab_bit_exact_on_nonsymmetric_system(cuda):
     np.testing.assert_array_equal(x.cpu().numpy(), xo)
     true = np.linalg.norm(o.apply_operator(v, r, 1, xo))
     assert true <= 1e-9 * so.init_res_norm
-    # iteration cap and the FP64-only rule
+    # iteration cap
     st = ls.solve(T.internal.clone(), rel_tol=1e-14, max_iter=2, method=abi.SOLVER_BICGSTAB)
     assert st.status == abi.ERR_NOT_CONVERGED and st.num_iter == 2
-    with pytest.raises(RuntimeError):
-        ls.solve(T.internal.clone(), precision=abi.PREC_MIXED_IR, method=abi.SOLVER_BICGSTAB)
 
 
-def test_bicgstab_batch_equals_alone(cuda):
+@pytest.mark.parametrize("rel_tol", [1e-8, 1e-12])
+def test_mixed_bicgstab_bit_exact(cuda, rel_tol):
+    """FP32 inner BiCGStab with FP64 refinement against the oracle's restatement,
+    bit for bit (iterate, inner and outer counts, norms), reaching the FP64
+    residual; a second solve of the unchanged system reuses the FP32 copy."""
+    hm, dm, T, o, ls, v, r = convection_case(nx=21, ny=19, nz=17)
+    for _ in range(2):
+        x = T.internal.clone()
+        st = ls.solve(x, rel_tol=rel_tol, max_iter=3000, precision=abi.PREC_MIXED_IR, method=abi.SOLVER_BICGSTAB)
+        xo = T.host().copy()
+        so = o.solve(v, r, xo, rel_tol=rel_tol, max_iter=3000, precision=1, method=1)
+        assert st.status == so.status == abi.OK
+        assert (st.num_iter, st.num_outer) == (so.num_iter, so.num_outer) and st.num_outer > 1
+        assert (st.init_res_norm, st.final_res_norm) == (so.init_res_norm, so.final_res_norm)
+        np.testing.assert_array_equal(x.cpu().numpy(), xo)
+        assert np.linalg.norm(o.apply_operator(v, r, 1, xo)) <= rel_tol * so.init_res_norm
+    # caps: refinement steps and total inner iterations
+    st = ls.solve(T.internal.clone(), rel_tol=1e-14, max_iter=3000, max_outer=2, precision=abi.PREC_MIXED_IR,
+                  method=abi.SOLVER_BICGSTAB, allow=(abi.ERR_NOT_CONVERGED,))
+    assert st.status == abi.ERR_NOT_CONVERGED and st.num_outer == 2
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED_IR])
+def test_bicgstab_batch_equals_alone(cuda, precision):
     parts = [mesh.box(7, 6, 5, jitter=0.1, seed=s) for s in (1, 2, 3)]
     big, ranges, _ = mesh.concat(parts)
     ranges = np.asarray(ranges, np.int32)
@@ -388,11 +409,13 @@ def test_bicgstab_batch_equals_alone(cuda):
     ls.assemble([neon.ddt(T.internal.clone()), neon.div(neon.SurfaceField(dm, F), "upwind"),
                  neon.laplacian(neon.SurfaceField(dm, np.full(big.nif + big.nbf, 1e-2)), -1.0)], 0.1, T)
     x = T.internal.clone()
-    stats = neon.Batch(ls, ranges).solve(x, rel_tol=1e-10, max_iter=500, method=abi.SOLVER_BICGSTAB)
+    stats = neon.Batch(ls, ranges).solve(x, rel_tol=1e-10, max_iter=500, precision=precision,
+                                         method=abi.SOLVER_BICGSTAB)
     for k in range(len(ranges) // 2):
         lo, hi = int(ranges[2 * k]), int(ranges[2 * k + 1])
         y = T.internal.clone()
         s1 = neon.Batch(ls, np.asarray([lo, hi], np.int32)).solve(y, rel_tol=1e-10, max_iter=500,
+                                                                  precision=precision,
                                                                   method=abi.SOLVER_BICGSTAB)
         assert stats[k].status == s1[0].status == abi.OK and stats[k].num_iter == s1[0].num_iter
         np.testing.assert_array_equal(x[lo:hi].cpu().numpy(), y[lo:hi].cpu().numpy())

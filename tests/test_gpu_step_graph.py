@@ -24,9 +24,10 @@ def packed_case(seed=3):
     return big, np.asarray(ranges, np.int32), dm, T, gamma
 
 
+@pytest.mark.parametrize("method", [abi.SOLVER_CG, abi.SOLVER_BICGSTAB])
 @pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED_IR])
 @pytest.mark.parametrize("batched", [True, False])
-def test_step_graph_equals_separate_calls(cuda, precision, batched):
+def test_step_graph_equals_separate_calls(cuda, precision, batched, method):
     L, s = abi.lib(), torch.cuda.current_stream().cuda_stream
     out = []
     for use_graph in (False, True):
@@ -37,7 +38,7 @@ def test_step_graph_equals_separate_calls(cuda, precision, batched):
         bc = T.bc_struct()
         batch = neon.Batch(ls, ranges) if batched else None
         ncases = len(ranges) // 2 if batched else 1
-        cfg = abi.SolverCfg(1e-9, 0.0, 2000, precision, 0.1, 1000, 50, 1)
+        cfg = abi.SolverCfg(1e-9, 0.0, 2000, precision, 0.1, 1000, 50, 1, 0, method)
         stats = torch.zeros(ncases * 8, dtype=torch.int32, device="cuda")  # fvgb_solver_stats is 32 bytes
         if use_graph:
             step = C.c_void_p()

@@ -83,5 +83,30 @@ def test_bicgstab_solves_nonsymmetric_system():
     assert st.status == 0 and 0 < st.num_iter < 500
     true = np.linalg.norm(o.apply_operator(v, r, 1, x))
     assert true <= 1e-9 * st.init_res_norm
-    # the mixed-precision BiCGStab is not provided
-    assert o.solve(v, r, T.copy(), method=1, precision=1).status == 6
+
+
+
+@pytest.mark.parametrize("rel_tol", [1e-8, 1e-12])
+def test_mixed_bicgstab_reaches_the_fp64_residual(rel_tol):
+    """FP32 inner BiCGStab in FP64 refinement: the FP64 residual of the result
+    reaches rel_tol, and the solution agrees with the FP64 BiCGStab's."""
+    o, v, r, T = convection_system()
+    x64 = T.copy()
+    s64 = o.solve(v, r, x64, rel_tol=rel_tol, max_iter=2000, method=1)
+    xm = T.copy()
+    sm = o.solve(v, r, xm, rel_tol=rel_tol, max_iter=2000, method=1, precision=1)
+    assert sm.status == 0 and sm.num_outer >= 1 and sm.init_res_norm == s64.init_res_norm
+    true = np.linalg.norm(o.apply_operator(v, r, 1, xm))
+    assert true <= rel_tol * sm.init_res_norm
+    assert sm.final_res_norm <= rel_tol * sm.init_res_norm
+    assert np.abs(xm - x64).max() <= 10 * rel_tol * np.abs(x64).max()
+
+
+def test_mixed_bicgstab_scale_invariance():
+    """A power-of-two scale of the system scales every iterate exactly."""
+    o, v, r, T = convection_system(seed=6)
+    x1, x2 = T.copy(), T.copy() * 2.0 ** -40
+    s1 = o.solve(v, r, x1, rel_tol=1e-9, max_iter=2000, method=1, precision=1)
+    s2 = o.solve(v, r * 2.0 ** -40, x2, rel_tol=1e-9, max_iter=2000, method=1, precision=1)
+    assert s1.status == s2.status == 0 and s1.num_iter == s2.num_iter
+    np.testing.assert_array_equal(x2, x1 * 2.0 ** -40)
