@@ -309,8 +309,12 @@ class LinearSystem:
         return v, r, bm[:hm.nbf], br[:hm.nbf * self.ncomp]
 
     def solve(self, x: torch.Tensor, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=abi.PREC_FP64,
-              inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,), kernel_mode=0,
+              inner_rel_tol=None, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,), kernel_mode=0,
               method=abi.SOLVER_CG, flags=0):
+        """inner_rel_tol (mixed precision) defaults to 0.1 for CG and 0.01 for the
+        restarted inner BiCGStab, the fastest settings measured on 128^3 systems."""
+        if inner_rel_tol is None:
+            inner_rel_tol = 0.01 if method == abi.SOLVER_BICGSTAB else 0.1
         cfg = abi.SolverCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer,
                             kernel_mode, flags, method)
         st = abi.SolverStats()
