@@ -2082,7 +2082,10 @@ struct SolverCache {
     double* r0 = nullptr;                   // mixed: first FP64 residual, from the preparation kernel
     uint64_t converted_version = 0;        // fvgb_ls::version the FP32 matrix copy was formed from
     int pgrid_fp64 = 0, pgrid_mixed = 0;   // co-resident blocks of the persistent kernels (0: not asked yet)
-    int variant[kTuneKinds] = {1, 1, 1, 1};  // chosen launch-bound variant per kernel kind
+    // chosen launch-bound variant per kernel kind; untuned solves (small systems,
+    // FVGB_SOLVE_NO_TUNE) use the 128^3 heat system's choices: at least 8 resident
+    // blocks per SM for the FP64 kernels and the FP32 update, 6 for the FP32 SpMV
+    int variant[kTuneKinds] = {3, 3, 2, 3};
     int forced[kTuneKinds] = {-1, -1, -1, -1};
     bool tuned64 = false, tunedmx = false;
     float tune_ms[kTuneKinds][kNumVariants] = {};
