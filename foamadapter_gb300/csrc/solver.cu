@@ -361,11 +361,20 @@ __global__ void __launch_bounds__(kT)
     const CaseState* cs = &L.cases[k.c];
     if (!ld_volatile(&cs->active)) return;
     const double beta = cs->beta;
+    double pv[kRowsPerThread], zv[kRowsPerThread];
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {  // every load first
+        const int i = blk_row(k, j);
+        pv[j] = zv[j] = 0.0;
+        if (i >= k.end) continue;
+        pv[j] = p[i];
+        zv[j] = __ldg(&z[i]);  // z = dinv*r, stored by the update
+    }
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int i = blk_row(k, j);
         if (i >= k.end) continue;
-        p[i] = fma(beta, p[i], __ldg(&z[i]));  // z = dinv*r, stored by the update
+        p[i] = fma(beta, pv[j], zv[j]);
     }
 }
 
@@ -929,15 +938,27 @@ __global__ void __launch_bounds__(kT, MINB)
     if (ld_volatile(&cs->inner_active)) {
         const float fa = cs->falpha;
         float acc = 0.0f;
+        float pv[kRowsPerThread], qv[kRowsPerThread], yv[kRowsPerThread], rv[kRowsPerThread],
+            dv[kRowsPerThread];
+#pragma unroll
+        for (int j = 0; j < kRowsPerThread; ++j) {  // every load first
+            const int i = blk_row(k, j);
+            pv[j] = qv[j] = yv[j] = rv[j] = dv[j] = 0.0f;
+            if (i >= k.end) continue;
+            pv[j] = __ldg(&p[i]);
+            qv[j] = __ldg(&q[i]);
+            dv[j] = __ldg(&dinv[i]);
+            yv[j] = y[i];
+            rv[j] = rh[i];
+        }
 #pragma unroll
         for (int j = 0; j < kRowsPerThread; ++j) {
             const int i = blk_row(k, j);
             if (i >= k.end) continue;
-            const float pi = __ldg(&p[i]);
-            y[i] = fmaf(fa, pi, y[i]);
-            const float ri = fmaf(-fa, __ldg(&q[i]), rh[i]);
+            y[i] = fmaf(fa, pv[j], yv[j]);
+            const float ri = fmaf(-fa, qv[j], rv[j]);
             rh[i] = ri;
-            acc = fmaf(ri, fabsf(__ldg(&dinv[i])) * ri, acc);
+            acc = fmaf(ri, fabsf(dv[j]) * ri, acc);
         }
         const float ba = block_tree_f(acc, smf);
         if (threadIdx.x == 0) pa[blockIdx.x] = (double)ba;
@@ -966,11 +987,21 @@ __global__ void __launch_bounds__(kT)
     const CaseState* cs = &L.cases[k.c];
     if (!ld_volatile(&cs->inner_active)) return;
     const float fb = cs->fbeta;
+    float pv[kRowsPerThread], dv[kRowsPerThread], rv[kRowsPerThread];
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {  // every load first
+        const int i = blk_row(k, j);
+        pv[j] = dv[j] = rv[j] = 0.0f;
+        if (i >= k.end) continue;
+        pv[j] = p[i];
+        dv[j] = __ldg(&dinv[i]);
+        rv[j] = __ldg(&rh[i]);
+    }
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int i = blk_row(k, j);
         if (i >= k.end) continue;
-        p[i] = fmaf(fb, p[i], fabsf(__ldg(&dinv[i])) * __ldg(&rh[i]));
+        p[i] = fmaf(fb, pv[j], fabsf(dv[j]) * rv[j]);
     }
 }
 
