@@ -546,11 +546,15 @@ __global__ void __launch_bounds__(kThreads)
 
 enum CorrMode { kCorrLaplacian = 0, kCorrOnly = 1, kCorrSnGrad = 2 };
 
-// kCorrLaplacian: gamma_f|Sf|delta_f (T_N - T_P) + gamma_f|Sf| (k . grad_f),
+// kCorrLaplacian: fma(gamma_f|Sf|delta_f, T_N - T_P, gamma_f|Sf| (k . grad_f)),
 //                 boundary faces gamma_b|Sf_b|delta_b (T_b - T_P) (as k_fx_lap);
 // kCorrOnly:      gamma_f|Sf| (k . grad_f), boundary faces 0 (faceFluxCorrection);
-// kCorrSnGrad:    delta_f (T_N - T_P) + k . grad_f, boundary delta_b (T_b - T_P).
-// grad: [n][NC][3]; k . g summed x, y, z in that order.
+// kCorrSnGrad:    fma(delta_f, T_N - T_P, k . grad_f), boundary delta_b (T_b - T_P).
+// grad: [n][NC][3]; grad_f = fma(w, g_P - g_N, g_N) per direction and
+// k . grad_f = fma(k_z, g_z, fma(k_y, g_y, k_x g_x)): fused multiply-adds, 14
+// FP64 operations per face and component where separate roundings took 20 (the
+// pass is bound by GB300's FP64 issue rate).  With k = 0 the flux is exactly the
+// uncorrected one: fma(a, b, 0) rounds a*b once, as the plain product does.
 template <int NC, int MODE>
 __global__ void __launch_bounds__(kThreads)
     k_fx_corr(MeshView m, const double* __restrict__ gamma, const double* __restrict__ phi,
@@ -569,16 +573,16 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     const double gn = __ldg(&grad[(N * NC + c) * 3 + d]);
-                    gf[d] = wf * (__ldg(&grad[(P * NC + c) * 3 + d]) - gn) + gn;
+                    gf[d] = fma(wf, __ldg(&grad[(P * NC + c) * 3 + d]) - gn, gn);
                 }
-                const double kg = (k0 * gf[0] + k1 * gf[1]) + k2 * gf[2];
+                const double kg = fma(k2, gf[2], fma(k1, gf[1], k0 * gf[0]));
                 const double dT = __ldg(&phi[N * NC + c]) - __ldg(&phi[P * NC + c]);
                 if (MODE == kCorrLaplacian)
-                    fx[f * NC + c] = __ldg(&gamma[f]) * __ldg(&m.geo[f]) * dT + gm * kg;
+                    fx[f * NC + c] = fma(__ldg(&gamma[f]) * __ldg(&m.geo[f]), dT, gm * kg);
                 else if (MODE == kCorrOnly)
                     fx[f * NC + c] = gm * kg;
                 else
-                    fx[f * NC + c] = __ldg(&m.delta[f]) * dT + kg;
+                    fx[f * NC + c] = fma(__ldg(&m.delta[f]), dT, kg);
             }
         } else if (f < m.nif + m.nbf) {
             const int b = f - m.nif;

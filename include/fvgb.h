@@ -175,11 +175,12 @@ fvgb_status fvgb_laplacian_explicit(const fvgb_mesh* mesh, int32_t ncomp, const 
                                     const double* phi, const double* phi_b, double coeff,
                                     double* out, fvgb_stream stream);
 /* The same with the `Gauss linear corrected` scheme (OpenFOAM's correctedSnGrad,
- * test/setup_stencil3D/system/fvSchemes:43): flux_f = gamma_f*(|Sf|*delta_f)*(T_N - T_P)
- * + (gamma_f*|Sf|)*(k_f . gT_f), where k_f = Sf/|Sf| - (C_N - C_P)*delta_f is the
- * face's non-orthogonal correction vector, gT_f = w_f*(g_P - g_N) + g_N and g the
- * Gauss linear gradient of T (as fvgb_grad, per component); boundary faces as
- * uncorrected.  Needs a mesh created with cell centres (FVGB_ERR_INVALID_ARG
+ * test/setup_stencil3D/system/fvSchemes:43): flux_f = fma(gamma_f*(|Sf|*delta_f),
+ * T_N - T_P, (gamma_f*|Sf|)*(k_f . gT_f)), where k_f = Sf/|Sf| - (C_N - C_P)*delta_f
+ * is the face's non-orthogonal correction vector, gT_f = fma(w_f, g_P - g_N, g_N)
+ * per direction, k . gT = fma(k_z, gT_z, fma(k_y, gT_y, k_x*gT_x)) and g the Gauss
+ * linear gradient of T (as fvgb_grad, per component); boundary faces as
+ * uncorrected (with k = 0 the flux is exactly the uncorrected one).  Needs a mesh created with cell centres (FVGB_ERR_INVALID_ARG
  * otherwise).  Takes stream-ordered scratch memory for the gradient. */
 fvgb_status fvgb_laplacian_explicit_corrected(const fvgb_mesh* mesh, int32_t ncomp, const double* gamma,
                                               const double* phi, const double* phi_b, double coeff,
@@ -193,7 +194,7 @@ fvgb_status fvgb_nonorth_flux(const fvgb_mesh* mesh, int32_t ncomp, const double
  * out_f = delta_f*(T_N - T_P), out_b = delta_b*(T_b - T_P); overwritten. */
 fvgb_status fvgb_sngrad(const fvgb_mesh* mesh, const double* phi, const double* phi_b,
                         double* out, fvgb_stream stream);
-/* FaceNormalGradient corrected: out_f = delta_f*(T_N - T_P) + k_f . gT_f (as above),
+/* FaceNormalGradient corrected: out_f = fma(delta_f, T_N - T_P, k_f . gT_f) (as above),
  * boundary faces delta_b*(T_b - T_P); overwritten. */
 fvgb_status fvgb_sngrad_corrected(const fvgb_mesh* mesh, const double* phi, const double* phi_b,
                                   double* out, fvgb_stream stream);

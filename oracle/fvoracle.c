@@ -176,7 +176,8 @@ void or_sngrad(const or_mesh* m, const double* phi, const double* phi_b, double*
  * NeoN's own implementation is not in the reference checkout, so parity is on
  * the published method):
  *   k_f      = Sf/|Sf| - (C_N - C_P)*delta_f      (nonOrthCorrectionVectors)
- *   snGrad_f = delta_f*(T_N - T_P) + k_f . gT_f,  gT_f = w*(g_P - g_N) + g_N,
+ *   snGrad_f = delta_f*(T_N - T_P) + k_f . gT_f,  gT_f = w*(g_P - g_N) + g_N
+ *   (evaluated with fused multiply-adds, as corr_kg and the callers spell out),
  * g the Gauss linear cell gradient (or_grad, per component); boundary faces of
  * non-coupled patches carry no correction. */
 void or_nonorth_vectors(const or_mesh* m, const double* C, double* k) {
@@ -210,19 +211,20 @@ static double* grad_components(const or_mesh* m, int32_t nc, const double* phi, 
     return grad;
 }
 
-/* k_f . gT_f of component j on internal face f, summed x, y, z in that order */
+/* k_f . gT_f of component j on internal face f with fused multiply-adds:
+ * gT = fma(w, g_P - g_N, g_N) per direction, k.gT = fma(k_z, g_z, fma(k_y, g_y, k_x g_x)) */
 static double corr_kg(const or_mesh* m, const double* k, const double* grad, int32_t nc, int32_t f, int32_t j) {
     const int32_t P = m->own[f], N = m->nei[f];
     double gf[3];
     for (int d = 0; d < 3; ++d) {
         double gn = grad[(N * nc + j) * 3 + d];
-        gf[d] = m->w[f] * (grad[(P * nc + j) * 3 + d] - gn) + gn;
+        gf[d] = fma(m->w[f], grad[(P * nc + j) * 3 + d] - gn, gn);
     }
-    return (k[3 * f] * gf[0] + k[3 * f + 1] * gf[1]) + k[3 * f + 2] * gf[2];
+    return fma(k[3 * f + 2], gf[2], fma(k[3 * f + 1], gf[1], k[3 * f] * gf[0]));
 }
 
-/* GaussGreenLaplacian corrected: flux_f = gamma*(|Sf|*delta)*(T_N - T_P) +
- * (gamma*|Sf|)*(k . gT_f); boundary faces uncorrected; out += res*(coeff/V). */
+/* GaussGreenLaplacian corrected: flux_f = fma(gamma*(|Sf|*delta), T_N - T_P,
+ * (gamma*|Sf|)*(k . gT_f)); boundary faces uncorrected; out += res*(coeff/V). */
 void or_laplacian_corrected(const or_mesh* m, int32_t nc, const double* k, const double* gamma,
                             const double* phi, const double* phi_b, double coeff, double* out) {
     double* grad = grad_components(m, nc, phi, phi_b);
@@ -232,7 +234,7 @@ void or_laplacian_corrected(const or_mesh* m, int32_t nc, const double* k, const
         double g = gamma[f] * (m->magSf[f] * m->delta[f]);
         double gm = gamma[f] * m->magSf[f];
         for (int32_t j = 0; j < nc; ++j) {
-            double fl = g * (phi[N * nc + j] - phi[P * nc + j]) + gm * corr_kg(m, k, grad, nc, f, j);
+            double fl = fma(g, phi[N * nc + j] - phi[P * nc + j], gm * corr_kg(m, k, grad, nc, f, j));
             res[P * nc + j] += fl;
             res[N * nc + j] -= fl;
         }
@@ -253,7 +255,7 @@ void or_laplacian_corrected(const or_mesh* m, int32_t nc, const double* k, const
 void or_sngrad_corrected(const or_mesh* m, const double* k, const double* phi, const double* phi_b, double* out) {
     double* grad = grad_components(m, 1, phi, phi_b);
     for (int32_t f = 0; f < m->nif; ++f)
-        out[f] = m->delta[f] * (phi[m->nei[f]] - phi[m->own[f]]) + corr_kg(m, k, grad, 1, f, 0);
+        out[f] = fma(m->delta[f], phi[m->nei[f]] - phi[m->own[f]], corr_kg(m, k, grad, 1, f, 0));
     for (int32_t b = 0; b < m->nbf; ++b)
         out[m->nif + b] = m->bdelta[b] * (phi_b[b] - phi[m->bcells[b]]);
     free(grad);
