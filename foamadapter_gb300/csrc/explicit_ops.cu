@@ -8,6 +8,8 @@
 // gather list, so every cell sees the same sequence of IEEE operations and the
 // result is bit-identical to the Serial face loop, with no atomics.  This file
 // is compiled with -fmad=false so no multiply-add is contracted.
+#include <atomic>
+
 #include "internal.cuh"
 
 namespace {
@@ -691,9 +693,10 @@ __global__ void __launch_bounds__(kThreads)
 // pool keeps its memory between calls.  nullptr when it cannot be had: the
 // caller then runs the one-pass gather, which needs none.
 double* face_buffer(size_t count, cudaStream_t s) {
-    static bool pool_ready = false;
+    static std::atomic<bool> pool_ready{false};  // the setting is idempotent: a racing second setter is harmless
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    if (!pool_ready && cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+    if (!pool_ready.load(std::memory_order_acquire) && cudaStreamIsCapturing(s, &cap) == cudaSuccess &&
+        cap == cudaStreamCaptureStatusNone) {
         // not while a graph is being captured (there the allocation becomes a graph memory node)
         int dev = 0;
         cudaMemPool_t pool;
@@ -701,7 +704,7 @@ double* face_buffer(size_t count, cudaStream_t s) {
             uint64_t keep = ~0ull;
             cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
         }
-        pool_ready = true;
+        pool_ready.store(true, std::memory_order_release);
     }
     double* p = nullptr;
     if (cudaMallocAsync((void**)&p, sizeof(double) * (count ? count : 1), s) != cudaSuccess) {

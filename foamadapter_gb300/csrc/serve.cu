@@ -62,7 +62,7 @@ struct Slot {
     double dt = 0;
 };
 
-__attribute__((unused)) int64_t nbf_of(const fvgb_serve_request& r) {
+int64_t nbf_of(const fvgb_serve_request& r) {
     return 2LL * ((int64_t)r.ny * r.nz + (int64_t)r.nx * r.nz + (int64_t)r.nx * r.ny);
 }
 
