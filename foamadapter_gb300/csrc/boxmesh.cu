@@ -53,6 +53,7 @@ struct MeshOut {
     double *bSf, *bmagSf, *bdelta, *bgeo;
     int32_t* bpatch;
     int32_t *g_code, *g_other, *m_col, *m_code, *diag_pos, *own_pos, *nei_pos;
+    int16_t* m_off;  // column - row per slot, or null (a box with nx*ny > 32767)
 };
 
 constexpr int kGW = 6;  // gather-list width (every box cell has 6 faces)
@@ -81,6 +82,7 @@ __global__ void k_box_cells(const BoxDev* __restrict__ boxes, const int32_t* __r
         }
         for (int k = 0; k < kMW; ++k) {
             o.m_col[mbase + k * 32] = c;
+            if (o.m_off) o.m_off[mbase + k * 32] = 0;
             o.m_code[mbase + k * 32] = k == 0 ? -1 : FVGB_PAD;
         }
         o.diag_pos[c] = mbase;
@@ -178,10 +180,12 @@ __global__ void k_box_cells(const BoxDev* __restrict__ boxes, const int32_t* __r
     for (int q = 0; q < nlo; ++q, ++s) {  // lo_o is ascending: c-sz < c-sy < c-1
         const int pos = mbase + s * 32;
         o.m_col[pos] = lo_o[q];
+        if (o.m_off) o.m_off[pos] = (int16_t)(lo_o[q] - c);
         o.m_code[pos] = -lo_f[q] - 2;
         o.nei_pos[lo_f[q]] = pos;
     }
     o.m_col[mbase + s * 32] = c;
+    if (o.m_off) o.m_off[mbase + s * 32] = 0;
     o.m_code[mbase + s * 32] = -1;
     o.diag_pos[c] = mbase + s * 32;
     ++s;
@@ -189,12 +193,14 @@ __global__ void k_box_cells(const BoxDev* __restrict__ boxes, const int32_t* __r
         if (up_f[d] < 0) continue;
         const int pos = mbase + s * 32;
         o.m_col[pos] = up_n[d];
+        if (o.m_off) o.m_off[pos] = (int16_t)(up_n[d] - c);
         o.m_code[pos] = up_f[d];
         o.own_pos[up_f[d]] = pos;
         ++s;
     }
     for (; s < kMW; ++s) {
         o.m_col[mbase + s * 32] = c;
+        if (o.m_off) o.m_off[mbase + s * 32] = 0;
         o.m_code[mbase + s * 32] = FVGB_PAD;
     }
 }
@@ -303,6 +309,16 @@ extern "C" fvgb_status fvgb_mesh_create_boxes(const fvgb_box_spec* specs, int32_
     A(&o.g_code, N * kGW);
     A(&o.g_other, N * kGW);
     A(&o.m_col, N * kMW);
+    // 16-bit column offsets fit when every box's largest neighbour offset does:
+    // nx*ny (z neighbours) for a box more than one cell thick, else nx, else 1
+    bool off_fits = true;
+    for (int q = 0; q < nboxes; ++q) {
+        const fvgb_box_spec& b = specs[q];
+        const int64_t span = b.nz > 1 ? (int64_t)b.nx * b.ny : (b.ny > 1 ? (int64_t)b.nx : 1);
+        off_fits = off_fits && span <= 32767;
+    }
+    o.m_off = nullptr;
+    if (off_fits) A(&o.m_off, N * kMW);
     A(&o.m_code, N * kMW);
     A(&o.diag_pos, N);
     A(&o.own_pos, NIF);
@@ -348,6 +364,7 @@ extern "C" fvgb_status fvgb_mesh_create_boxes(const fvgb_box_spec* specs, int32_
     v.g_other = o.g_other;
     v.m_ptr = m_ptr;
     v.m_col = o.m_col;
+    v.m_off = o.m_off;
     v.m_code = o.m_code;
     v.diag_pos = o.diag_pos;
     v.own_pos = o.own_pos;

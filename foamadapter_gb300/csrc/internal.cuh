@@ -55,6 +55,8 @@ struct MeshView {
     const int32_t* g_other;
     const int32_t* m_ptr;
     const int32_t* m_col;
+    const int16_t* m_off;    // [m_len] column - row of every slot when all fit in 16 bits (banded
+                             // meshes), else null: the SpMVs then read 2 instead of 4 bytes per slot
     const int32_t* m_code;
     const int32_t* diag_pos;
     const int32_t* own_pos;
@@ -124,6 +126,12 @@ inline cudaError_t settle_creation() { return cudaStreamSynchronize(0); }
 // psi, volume integrated (explicit_ops.cu).
 fvgb_status nonorth_rhs(const fvgb_mesh* m, int nc, const double* gamma, const double* psi, const double* psi_b,
                         double coeff, double* out, cudaStream_t s);
+
+// Column of matrix slot `pos` of row i (sliced ELL): from the 16-bit offset when
+// the mesh has them, else from the 32-bit column array.  Same column either way.
+__device__ __forceinline__ int slot_col(const MeshView& m, int pos, int i) {
+    return m.m_off ? i + (int)__ldg(&m.m_off[pos]) : __ldg(&m.m_col[pos]);
+}
 
 inline unsigned grid_for(int64_t n, int threads) { return n > 0 ? (unsigned)((n + threads - 1) / threads) : 1u; }
 

@@ -192,6 +192,25 @@ extern "C" fvgb_status fvgb_mesh_create(const fvgb_mesh_desc* d, fvgb_mesh** out
             }
         }
     }
+    // 16-bit column offsets when every slot's column is within +-32767 of its row
+    std::vector<int16_t> s_off(ms.len, 0);
+    bool off_fits = true;
+    for (int32_t sl = 0; sl < m->nslices && off_fits; ++sl) {
+        int32_t w = (ms.ptr[sl + 1] - ms.ptr[sl]) / kSlice;
+        for (int32_t l = 0; l < kSlice && off_fits; ++l) {
+            const int32_t r = sl * kSlice + l;
+            if (r >= n) continue;
+            for (int32_t k = 0; k < w; ++k) {
+                const int64_t pos = (int64_t)ms.ptr[sl] + (int64_t)k * kSlice + l;
+                const int64_t off = (int64_t)s_col[pos] - r;
+                if (off < -32767 || off > 32767) {
+                    off_fits = false;
+                    break;
+                }
+                s_off[pos] = (int16_t)off;
+            }
+        }
+    }
     for (int32_t c = 0; c < n; ++c) diag_pos[c] = (int32_t)sell_pos(ms, c, m->h_diag_off[c]);
     for (int32_t f = 0; f < nif; ++f) {
         own_pos[f] = (int32_t)sell_pos(ms, d->owner[f], m->h_own_off[f]);
@@ -280,6 +299,7 @@ extern "C" fvgb_status fvgb_mesh_create(const fvgb_mesh_desc* d, fvgb_mesh** out
     UP(v.g_other, sg_other.data(), gs.len);
     UP(v.m_ptr, ms.ptr.data(), (int64_t)ms.ptr.size());
     UP(v.m_col, s_col.data(), ms.len);
+    if (off_fits) UP(v.m_off, s_off.data(), ms.len);
     UP(v.m_code, s_code.data(), ms.len);
     UP(v.diag_pos, diag_pos.data(), n);
     UP(v.own_pos, own_pos.data(), nif);

@@ -97,7 +97,7 @@ int64_t estimate_bytes(const fvgb_serve_request& r) {
     const int64_t nif = (int64_t)(r.nx - 1) * r.ny * r.nz + (int64_t)r.nx * (r.ny - 1) * r.nz +
                         (int64_t)r.nx * r.ny * (r.nz - 1);
     const int64_t nbf = nbf_of(r);
-    const int64_t mesh = 16 * n + 72 * nif + 64 * nbf + 4 * 6 * 2 * n + 4 * 7 * 2 * n + 4 * n;
+    const int64_t mesh = 16 * n + 72 * nif + 64 * nbf + 4 * 6 * 2 * n + 4 * 7 * 2 * n + 2 * 7 * n + 4 * n;
     const int64_t system = 8 * 7 * n + 8 * n + 16 * nbf;
     const int64_t solver = r.precision == FVGB_PREC_MIXED_IR ? (8 + 28 + 16) * n : 40 * n;
     const int64_t fields = 16 * n + 8 * nbf + 16 * (nif + nbf) + 24 * (n + nbf) + 8 * nbf;

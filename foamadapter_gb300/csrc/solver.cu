@@ -158,6 +158,19 @@ __device__ __forceinline__ bool arrive_last(unsigned int* counter, unsigned int 
 
 __device__ __forceinline__ int ld_volatile(const int32_t* p) { return *(const volatile int32_t*)p; }
 
+// Columns of a row's first 8 slots (the row itself past its width), the
+// offset or column array chosen once per row so the index loads are issued
+// together.
+__device__ __forceinline__ void slot_cols(const MeshView& m, int base, int w, int i, int* col) {
+    if (m.m_off) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) col[k] = k < w ? i + (int)__ldg(&m.m_off[base + k * 32]) : i;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) col[k] = k < w ? __ldg(&m.m_col[base + k * 32]) : i;
+    }
+}
+
 // Row sum of a sliced-ELL row, fma chain in slot (= column) order.  The slot
 // loads of the first 8 slots are issued before the dependent gathers.
 __device__ __forceinline__ double spmv_row(const MeshView& m, const double* __restrict__ val,
@@ -166,6 +179,8 @@ __device__ __forceinline__ double spmv_row(const MeshView& m, const double* __re
     const int b0 = __ldg(&m.m_ptr[slice]);
     const int base = b0 + lane;
     const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+    int col[8];
+    slot_cols(m, base, w, i, col);
     double v[8], xv[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -173,14 +188,14 @@ __device__ __forceinline__ double spmv_row(const MeshView& m, const double* __re
         xv[k] = 0.0;
         if (k < w) {
             v[k] = __ldg(&val[base + k * 32]);
-            xv[k] = __ldg(&x[__ldg(&m.m_col[base + k * 32])]);
+            xv[k] = __ldg(&x[col[k]]);
         }
     }
     double s = 0.0;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         if (k < w) s = fma(v[k], xv[k], s);
-    for (int k = 8; k < w; ++k) s = fma(__ldg(&val[base + k * 32]), __ldg(&x[__ldg(&m.m_col[base + k * 32])]), s);
+    for (int k = 8; k < w; ++k) s = fma(__ldg(&val[base + k * 32]), __ldg(&x[slot_col(m, base + k * 32, i)]), s);
     return s;
 }
 
@@ -192,6 +207,8 @@ __device__ __forceinline__ float spmv_row_diff(const MeshView& m, const float* _
     const int b0 = __ldg(&m.m_ptr[slice]);
     const int base = b0 + lane;
     const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+    int col[8];
+    slot_cols(m, base, w, i, col);
     float v[8], xv[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -199,14 +216,14 @@ __device__ __forceinline__ float spmv_row_diff(const MeshView& m, const float* _
         xv[k] = 0.0f;
         if (k < w) {
             v[k] = __ldg(&a[base + k * 32]);
-            xv[k] = __ldg(&x[__ldg(&m.m_col[base + k * 32])]);
+            xv[k] = __ldg(&x[col[k]]);
         }
     }
     float s = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         if (k < w) s = fmaf(v[k], xv[k] - xi, s);
-    for (int k = 8; k < w; ++k) s = fmaf(__ldg(&a[base + k * 32]), __ldg(&x[__ldg(&m.m_col[base + k * 32])]) - xi, s);
+    for (int k = 8; k < w; ++k) s = fmaf(__ldg(&a[base + k * 32]), __ldg(&x[slot_col(m, base + k * 32, i)]) - xi, s);
     return fmaf(ei, xi, s);
 }
 
@@ -1492,6 +1509,8 @@ __device__ __forceinline__ double spmv_row_cg(const MeshView& m, const double* _
     const int b0 = __ldg(&m.m_ptr[slice]);
     const int base = b0 + lane;
     const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+    int col[8];
+    slot_cols(m, base, w, i, col);
     double v[8], xv[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -1499,14 +1518,14 @@ __device__ __forceinline__ double spmv_row_cg(const MeshView& m, const double* _
         xv[k] = 0.0;
         if (k < w) {
             v[k] = __ldg(&val[base + k * 32]);
-            xv[k] = __ldcg(&x[__ldg(&m.m_col[base + k * 32])]);
+            xv[k] = __ldcg(&x[col[k]]);
         }
     }
     double s = 0.0;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         if (k < w) s = fma(v[k], xv[k], s);
-    for (int k = 8; k < w; ++k) s = fma(__ldg(&val[base + k * 32]), __ldcg(&x[__ldg(&m.m_col[base + k * 32])]), s);
+    for (int k = 8; k < w; ++k) s = fma(__ldg(&val[base + k * 32]), __ldcg(&x[slot_col(m, base + k * 32, i)]), s);
     return s;
 }
 
@@ -1719,15 +1738,16 @@ __device__ __forceinline__ float spmv_row_diff_dir(const MeshView& m, const floa
     const int b0 = __ldg(&m.m_ptr[slice]);
     const int base = b0 + lane;
     const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+    int col[8];
+    slot_cols(m, base, w, i, col);
     float v[8], xv[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         v[k] = 0.0f;
         xv[k] = 0.0f;
         if (k < w) {
-            const int cidx = __ldg(&m.m_col[base + k * 32]);
             v[k] = __ldg(&a[base + k * 32]);
-            xv[k] = dir_of(d, __ldcg(&pold[cidx]), d.kind == 0 ? 0.0f : __ldcg(&zz[cidx]));
+            xv[k] = dir_of(d, __ldcg(&pold[col[k]]), d.kind == 0 ? 0.0f : __ldcg(&zz[col[k]]));
         }
     }
     float s = 0.0f;
@@ -1735,7 +1755,7 @@ __device__ __forceinline__ float spmv_row_diff_dir(const MeshView& m, const floa
     for (int k = 0; k < 8; ++k)
         if (k < w) s = fmaf(v[k], xv[k] - xi, s);
     for (int k = 8; k < w; ++k) {
-        const int cidx = __ldg(&m.m_col[base + k * 32]);
+        const int cidx = slot_col(m, base + k * 32, i);
         const float xc = dir_of(d, __ldcg(&pold[cidx]), d.kind == 0 ? 0.0f : __ldcg(&zz[cidx]));
         s = fmaf(__ldg(&a[base + k * 32]), xc - xi, s);
     }
