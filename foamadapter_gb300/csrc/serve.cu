@@ -161,7 +161,7 @@ fvgb_status setup(fvgb_server* sv, Slot* s) {
         if (e == cudaSuccess) e = cudaMalloc(p, sizeof(double) * (count ? count : 1));
     };
     A(&s->T, n);
-    A(&s->Told, n);
+    if (r.flags & FVGB_SERVE_REASSEMBLE) A(&s->Told, n);
     A(&s->Tb, nbf);
     A(&s->F, nf);
     A(&s->gamma, nf);
@@ -192,11 +192,20 @@ fvgb_status setup(fvgb_server* sv, Slot* s) {
 
 fvgb_status enqueue_step(Slot* s, int k) {
     const fvgb_serve_request& r = s->req;
-    cudaError_t e = cudaMemcpyAsync(s->Told, s->T, sizeof(double) * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream);
-    if (e != cudaSuccess) return fvgb_fail(FVGB_ERR_CUDA, "server: copy");
+    // The old field: the reference's pattern (FVGB_SERVE_REASSEMBLE) keeps a copy of
+    // it, as NeoN's oldTime field is stored every step.  Otherwise it is T itself:
+    // the assembly reads it before the solve overwrites T (its initial guess) in
+    // place, so no copy is needed.  Same values, same bits.
+    const double* old = s->T;
+    if (r.flags & FVGB_SERVE_REASSEMBLE) {
+        if (cudaMemcpyAsync(s->Told, s->T, sizeof(double) * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream) !=
+            cudaSuccess)
+            return fvgb_fail(FVGB_ERR_CUDA, "server: copy");
+        old = s->Told;
+    }
     fvgb_term terms[3] = {
-        {FVGB_TERM_DDT, 0, 1.0, s->Told, nullptr},
-        {FVGB_TERM_DIV_EXPLICIT, FVGB_SCHEME_UPWIND, 1.0, s->Told, s->F},
+        {FVGB_TERM_DDT, 0, 1.0, old, nullptr},
+        {FVGB_TERM_DIV_EXPLICIT, FVGB_SCHEME_UPWIND, 1.0, old, s->F},
         {FVGB_TERM_LAPLACIAN, 0, -1.0, nullptr, s->gamma},
     };
     fvgb_bc bc{s->types, s->ref};

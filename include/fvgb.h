@@ -460,10 +460,12 @@ typedef struct fvgb_serve_request {
     int32_t precision;         /* FVGB_PREC_FP64 or FVGB_PREC_MIXED_IR                */
     int32_t kernel_mode;       /* fvgb_solver_cfg.kernel_mode of every solve; 0 picks
                                   the graph path (requests overlap on the device)     */
-    int32_t flags;             /* FVGB_SERVE_REASSEMBLE: assemble the whole system every
-                                  step (the reference's dsl::solve); otherwise the
-                                  matrix is assembled once and each later step
-                                  assembles only the rhs (same results)              */
+    int32_t flags;             /* FVGB_SERVE_REASSEMBLE: the reference's step pattern
+                                  (dsl::solve): a copy of the old-time field and the
+                                  whole system assembled every step; otherwise the
+                                  matrix is assembled once, each later step assembles
+                                  only the rhs and reads the old field in place (same
+                                  results)                                            */
     int32_t reserved;
     double* T_out;
 } fvgb_serve_request;
