@@ -32,7 +32,7 @@
 namespace {
 
 constexpr int kT = 256;
-constexpr int kRowsPerThread = 4;
+constexpr int kRowsPerThread = 8;
 constexpr int kRowsPerBlock = kT * kRowsPerThread;
 constexpr int kMaxRows = 262144;
 constexpr int kMaxBlocks = kMaxRows / kRowsPerBlock;

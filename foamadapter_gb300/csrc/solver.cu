@@ -14,7 +14,7 @@
 // Batches.  A system may hold several independent cases (a block-diagonal
 // matrix); case c owns rows [begin_c, end_c).  Every kernel is ONE launch
 // over all cases: a block map assigns each 256-thread block to one case and
-// 1024 consecutive rows of it, every case keeps its own CG scalars, and
+// 2048 consecutive rows of it, every case keeps its own CG scalars, and
 // converged cases idle.  A single solve is a batch of one case.
 //
 // Each solve is one CUDA graph: an init kernel, a device-side WHILE
@@ -41,7 +41,7 @@
 namespace {
 
 constexpr int kT = 256;
-constexpr int kRowsPerThread = 4;
+constexpr int kRowsPerThread = 8;
 constexpr int kRowsPerBlock = kT * kRowsPerThread;
 
 struct SolverParams {
@@ -955,27 +955,31 @@ __global__ void __launch_bounds__(kT, MINB)
     if (ld_volatile(&cs->inner_active)) {
         const float fa = cs->falpha;
         float acc = 0.0f;
-        float pv[kRowsPerThread], qv[kRowsPerThread], yv[kRowsPerThread], rv[kRowsPerThread],
-            dv[kRowsPerThread];
+        constexpr int G = 4;  // rows whose loads are issued together (more spill at 32-40 registers)
+        static_assert(kRowsPerThread % G == 0, "rows per thread in whole load groups");
 #pragma unroll
-        for (int j = 0; j < kRowsPerThread; ++j) {  // every load first
-            const int i = blk_row(k, j);
-            pv[j] = qv[j] = yv[j] = rv[j] = dv[j] = 0.0f;
-            if (i >= k.end) continue;
-            pv[j] = __ldg(&p[i]);
-            qv[j] = __ldg(&q[i]);
-            dv[j] = __ldg(&dinv[i]);
-            yv[j] = y[i];
-            rv[j] = rh[i];
-        }
+        for (int j0 = 0; j0 < kRowsPerThread; j0 += G) {
+            float pv[G], qv[G], yv[G], rv[G], dv[G];
 #pragma unroll
-        for (int j = 0; j < kRowsPerThread; ++j) {
-            const int i = blk_row(k, j);
-            if (i >= k.end) continue;
-            y[i] = fmaf(fa, pv[j], yv[j]);
-            const float ri = fmaf(-fa, qv[j], rv[j]);
-            rh[i] = ri;
-            acc = fmaf(ri, fabsf(dv[j]) * ri, acc);
+            for (int u = 0; u < G; ++u) {  // every load of the group first
+                const int i = blk_row(k, j0 + u);
+                pv[u] = qv[u] = yv[u] = rv[u] = dv[u] = 0.0f;
+                if (i >= k.end) continue;
+                pv[u] = __ldg(&p[i]);
+                qv[u] = __ldg(&q[i]);
+                dv[u] = __ldg(&dinv[i]);
+                yv[u] = y[i];
+                rv[u] = rh[i];
+            }
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                const int i = blk_row(k, j0 + u);
+                if (i >= k.end) continue;
+                y[i] = fmaf(fa, pv[u], yv[u]);
+                const float ri = fmaf(-fa, qv[u], rv[u]);
+                rh[i] = ri;
+                acc = fmaf(ri, fabsf(dv[u]) * ri, acc);
+            }
         }
         const float ba = block_tree_f(acc, smf);
         if (threadIdx.x == 0) pa[blockIdx.x] = (double)ba;
@@ -1408,10 +1412,11 @@ cudaError_t launch_variant(const void* fn, unsigned grid, cudaStream_t s, A... a
 // ------------------------------------------------------ persistent solves (one case)
 // For systems small enough that launch latency dominates an iteration, ONE
 // cooperative launch runs the whole solve.  A persistent block has 1024 threads
-// and walks the 1024-row virtual blocks vb = blockIdx.x, blockIdx.x + gridDim.x,
-// ...; thread t computes row vb*1024 + t.  Dot products are staged in shared
-// memory and summed by 256 "tree threads" with exactly the row assignment and
-// order of the graph kernels (4 rows per thread, then the block tree), so the
+// and walks the 2048-row virtual blocks vb = blockIdx.x, blockIdx.x + gridDim.x,
+// ...; thread t computes rows vb*2048 + t and vb*2048 + 1024 + t.  Dot products
+// are staged in shared memory and summed by 256 "tree threads" with exactly the
+// row assignment and order of the graph kernels (8 rows per thread, then the
+// block tree), so the
 // per-virtual-block partials, and after a grid barrier the final trees that
 // EVERY block computes over all partials, are the bits of the graph path; all
 // blocks then take identical decisions.  Data written during the kernel is
@@ -1419,6 +1424,8 @@ cudaError_t launch_variant(const void* fn, unsigned grid, cudaStream_t s, A... a
 // time-out a block raises the abort flag, every block leaves at its next
 // barrier and the solve reports FVGB_ERR_CUDA.
 constexpr int kPT = 1024;
+constexpr int kRowsPerPT = kRowsPerBlock / kPT;  // rows of a virtual block per persistent thread
+static_assert(kRowsPerBlock % kPT == 0, "a virtual block is a whole number of rows per thread");
 
 struct GridBar {
     unsigned long long count;  // arrivals since the launch (never reset inside it)
@@ -1542,7 +1549,7 @@ __global__ void __launch_bounds__(kPT, 1)
     k_pcg_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
                      double* dinv, double* r, double* p, double* q, double* z, double* pa, double* pb, GridBar* gb,
                      int nvb) {
-    __shared__ double sA[kPT], sB[kPT], sm[kT], sm2[kT], cell;
+    __shared__ double sA[kRowsPerBlock], sB[kRowsPerBlock], sm[kT], sm2[kT], cell;
     __shared__ PcgShared sh;
     const int n = m.n, T = threadIdx.x;
     const SolverParams prm = L.bs->prm;
@@ -1551,18 +1558,21 @@ __global__ void __launch_bounds__(kPT, 1)
     unsigned long long epoch = 0;
     // init: r = b - A x, z = p = dinv r, r.z, r.r
     for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-        const int i = vb * kRowsPerBlock + T;
-        double ri = 0.0, zi = 0.0;
-        if (i < n) {
-            const double di = 1.0 / __ldg(&val[__ldg(&m.diag_pos[i])]);
-            dinv[i] = di;
-            ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
-            zi = di * ri;
-            r[i] = ri;
-            p[i] = zi;
+        for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+            const int t = T + h * kPT;
+            const int i = vb * kRowsPerBlock + t;
+            double ri = 0.0, zi = 0.0;
+            if (i < n) {
+                const double di = 1.0 / __ldg(&val[__ldg(&m.diag_pos[i])]);
+                dinv[i] = di;
+                ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
+                zi = di * ri;
+                r[i] = ri;
+                p[i] = zi;
+            }
+            sA[t] = ri;
+            sB[t] = zi;
         }
-        sA[T] = ri;
-        sB[T] = zi;
         __syncthreads();
         double arz = 0.0, arr = 0.0;
         if (T < kT)
@@ -1606,15 +1616,18 @@ __global__ void __launch_bounds__(kPT, 1)
     while (!done) {
         // q = A p, p.q
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-            const int i = vb * kRowsPerBlock + T;
-            double pi = 0.0, qi = 0.0;
-            if (i < n) {
-                qi = spmv_row_cg(m, val, p, i);
-                q[i] = qi;
-                pi = __ldcg(&p[i]);
+            for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                const int t = T + h * kPT;
+                const int i = vb * kRowsPerBlock + t;
+                double pi = 0.0, qi = 0.0;
+                if (i < n) {
+                    qi = spmv_row_cg(m, val, p, i);
+                    q[i] = qi;
+                    pi = __ldcg(&p[i]);
+                }
+                sA[t] = pi;
+                sB[t] = qi;
             }
-            sA[T] = pi;
-            sB[T] = qi;
             __syncthreads();
             double acc = 0.0;
             if (T < kT)
@@ -1645,17 +1658,20 @@ __global__ void __launch_bounds__(kPT, 1)
         const double alpha = sh.alpha;
         // x += alpha p, r -= alpha q, z = dinv r, r.z, r.r
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-            const int i = vb * kRowsPerBlock + T;
-            double ri = 0.0, zi = 0.0;
-            if (i < n) {
-                x[i] = fma(alpha, __ldcg(&p[i]), __ldcg(&x[i]));
-                ri = fma(-alpha, __ldcg(&q[i]), __ldcg(&r[i]));
-                r[i] = ri;
-                zi = __ldcg(&dinv[i]) * ri;
-                z[i] = zi;
+            for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                const int t = T + h * kPT;
+                const int i = vb * kRowsPerBlock + t;
+                double ri = 0.0, zi = 0.0;
+                if (i < n) {
+                    x[i] = fma(alpha, __ldcg(&p[i]), __ldcg(&x[i]));
+                    ri = fma(-alpha, __ldcg(&q[i]), __ldcg(&r[i]));
+                    r[i] = ri;
+                    zi = __ldcg(&dinv[i]) * ri;
+                    z[i] = zi;
+                }
+                sA[t] = ri;
+                sB[t] = zi;
             }
-            sA[T] = ri;
-            sB[T] = zi;
             __syncthreads();
             double arz = 0.0, arr = 0.0;
             if (T < kT)
@@ -1700,8 +1716,11 @@ __global__ void __launch_bounds__(kPT, 1)
         const double beta = sh.beta;
         // p = z + beta p
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-            const int i = vb * kRowsPerBlock + T;
-            if (i < n) p[i] = fma(beta, __ldcg(&p[i]), __ldcg(&z[i]));
+            for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                const int t = T + h * kPT;
+                const int i = vb * kRowsPerBlock + t;
+                if (i < n) p[i] = fma(beta, __ldcg(&p[i]), __ldcg(&z[i]));
+            }
         }
         if (!grid_sync(gb, ++epoch * G)) {
             aborted = true;
@@ -1775,8 +1794,8 @@ __global__ void __launch_bounds__(kPT, 1)
     k_ir_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
                     float* a32, float* ev, float* dinv, double* r0, float* rh, float* y, float* pbuf0, float* pbuf1,
                     float* z, float* q, double* pa, double* pb, double* pc, GridBar* gb, int nvb) {
-    __shared__ double sD[kPT], sm[kT], sm3[kT], cell;
-    __shared__ float sF1[kPT], sF2[kPT], smf[kT];
+    __shared__ double sD[kRowsPerBlock], sm[kT], sm3[kT], cell;
+    __shared__ float sF1[kRowsPerBlock], sF2[kRowsPerBlock], smf[kT];
     __shared__ unsigned int sflags;
     __shared__ IrShared sh;
     const int n = m.n, T = threadIdx.x;
@@ -1790,40 +1809,43 @@ __global__ void __launch_bounds__(kPT, 1)
     if (T == 0) sflags = 0u;
     __syncthreads();
     for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-        const int i = vb * kRowsPerBlock + T;
-        double ri = 0.0;
-        float di = 0.0f;
-        if (i < n) {
-            const double d = __ldg(&val[__ldg(&m.diag_pos[i])]);
-            atomicOr(&sflags, d > 0.0 ? 1u : (d < 0.0 ? 2u : 4u));
-            if (prm.convert) {
-                di = (float)(1.0 / d);
-                dinv[i] = di;
-                const double sg = d < 0.0 ? -1.0 : 1.0;
-                const int slice = i >> 5, lane = i & 31;
-                const int b0 = __ldg(&m.m_ptr[slice]);
-                const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
-                double e = 0.0;
-                for (int kk = 0; kk < w; ++kk) {
-                    const int pos = b0 + kk * 32 + lane;
-                    const int code = __ldg(&m.m_code[pos]);
-                    if (code == FVGB_PAD) {
-                        a32[pos] = 0.0f;
-                        continue;
+        for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+            const int t = T + h * kPT;
+            const int i = vb * kRowsPerBlock + t;
+            double ri = 0.0;
+            float di = 0.0f;
+            if (i < n) {
+                const double d = __ldg(&val[__ldg(&m.diag_pos[i])]);
+                atomicOr(&sflags, d > 0.0 ? 1u : (d < 0.0 ? 2u : 4u));
+                if (prm.convert) {
+                    di = (float)(1.0 / d);
+                    dinv[i] = di;
+                    const double sg = d < 0.0 ? -1.0 : 1.0;
+                    const int slice = i >> 5, lane = i & 31;
+                    const int b0 = __ldg(&m.m_ptr[slice]);
+                    const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+                    double e = 0.0;
+                    for (int kk = 0; kk < w; ++kk) {
+                        const int pos = b0 + kk * 32 + lane;
+                        const int code = __ldg(&m.m_code[pos]);
+                        if (code == FVGB_PAD) {
+                            a32[pos] = 0.0f;
+                            continue;
+                        }
+                        const double av = __ldg(&val[pos]);
+                        e = e + av;
+                        a32[pos] = code == -1 ? 0.0f : (float)(sg * av);
                     }
-                    const double av = __ldg(&val[pos]);
-                    e = e + av;
-                    a32[pos] = code == -1 ? 0.0f : (float)(sg * av);
+                    ev[i] = (float)(sg * e);
+                } else {
+                    di = __ldcg(&dinv[i]);
                 }
-                ev[i] = (float)(sg * e);
-            } else {
-                di = __ldcg(&dinv[i]);
+                ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
+                r0[i] = ri;
             }
-            ri = __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
-            r0[i] = ri;
+            sD[t] = ri;
+            sF1[t] = di;
         }
-        sD[T] = ri;
-        sF1[T] = di;
         __syncthreads();
         double asr = 0.0;
         if (T < kT)
@@ -1859,8 +1881,11 @@ __global__ void __launch_bounds__(kPT, 1)
             // x += y / sig
             const double is = sh.isig;
             for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-                const int i = vb * kRowsPerBlock + T;
-                if (i < n) x[i] = fma((double)__ldcg(&y[i]), is, __ldcg(&x[i]));
+                for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                    const int t = T + h * kPT;
+                    const int i = vb * kRowsPerBlock + t;
+                    if (i < n) x[i] = fma((double)__ldcg(&y[i]), is, __ldcg(&x[i]));
+                }
             }
             if (!grid_sync(gb, ++epoch * G)) {
                 aborted = true;
@@ -1876,23 +1901,26 @@ __global__ void __launch_bounds__(kPT, 1)
         const double nsig_all = sh.nsig;
         // residual: r = b - A x (FP64), rh = sign*(float)(sig r), y = 0, z = |dinv| rh
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-            const int i = vb * kRowsPerBlock + T;
-            double ri = 0.0;
-            float di = 0.0f, rhi = 0.0f;
-            if (i < n) {
-                ri = first ? __ldcg(&r0[i]) : __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
-                di = __ldcg(&dinv[i]);
-                rhi = (float)(ri * nsig_all);
-                if (di < 0.0f) rhi = -rhi;
-                rh[i] = rhi;
-                y[i] = 0.0f;
-                const float zi = fabsf(di) * rhi;
-                z[i] = zi;
-                if (first) pcur[i] = zi;
+            for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                const int t = T + h * kPT;
+                const int i = vb * kRowsPerBlock + t;
+                double ri = 0.0;
+                float di = 0.0f, rhi = 0.0f;
+                if (i < n) {
+                    ri = first ? __ldcg(&r0[i]) : __ldg(&b[i]) - spmv_row_cg(m, val, x, i);
+                    di = __ldcg(&dinv[i]);
+                    rhi = (float)(ri * nsig_all);
+                    if (di < 0.0f) rhi = -rhi;
+                    rh[i] = rhi;
+                    y[i] = 0.0f;
+                    const float zi = fabsf(di) * rhi;
+                    z[i] = zi;
+                    if (first) pcur[i] = zi;
+                }
+                sD[t] = ri;
+                sF1[t] = rhi;
+                sF2[t] = di;
             }
-            sD[T] = ri;
-            sF1[T] = rhi;
-            sF2[T] = di;
             __syncthreads();
             double arr = 0.0, asr = 0.0;
             float arho = 0.0f;
@@ -1972,16 +2000,19 @@ __global__ void __launch_bounds__(kPT, 1)
             const DirMode dm = sh.dm;
             // direction (into pnext unless p is taken as stored), q = A p, p.q
             for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-                const int i = vb * kRowsPerBlock + T;
-                float pi = 0.0f, qi = 0.0f;
-                if (i < n) {
-                    pi = dir_of(dm, __ldcg(&pcur[i]), dm.kind == 0 ? 0.0f : __ldcg(&z[i]));
-                    if (dm.kind != 0) pnext[i] = pi;
-                    qi = spmv_row_diff_dir(m, a32, pcur, z, dm, i, pi, __ldg(&ev[i]));
-                    q[i] = qi;
+                for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                    const int t = T + h * kPT;
+                    const int i = vb * kRowsPerBlock + t;
+                    float pi = 0.0f, qi = 0.0f;
+                    if (i < n) {
+                        pi = dir_of(dm, __ldcg(&pcur[i]), dm.kind == 0 ? 0.0f : __ldcg(&z[i]));
+                        if (dm.kind != 0) pnext[i] = pi;
+                        qi = spmv_row_diff_dir(m, a32, pcur, z, dm, i, pi, __ldg(&ev[i]));
+                        q[i] = qi;
+                    }
+                    sF1[t] = pi;
+                    sF2[t] = qi;
                 }
-                sF1[T] = pi;
-                sF2[T] = qi;
                 __syncthreads();
                 float acc = 0.0f;
                 if (T < kT)
@@ -2022,17 +2053,20 @@ __global__ void __launch_bounds__(kPT, 1)
             const float fa = sh.fa;
             // y += alpha p, rh -= alpha q, z = |dinv| rh, rh.z
             for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-                const int i = vb * kRowsPerBlock + T;
-                float ri = 0.0f, zi = 0.0f;
-                if (i < n) {
-                    y[i] = fmaf(fa, __ldcg(&pcur[i]), __ldcg(&y[i]));
-                    ri = fmaf(-fa, __ldcg(&q[i]), __ldcg(&rh[i]));
-                    rh[i] = ri;
-                    zi = fabsf(__ldcg(&dinv[i])) * ri;
-                    z[i] = zi;
+                for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                    const int t = T + h * kPT;
+                    const int i = vb * kRowsPerBlock + t;
+                    float ri = 0.0f, zi = 0.0f;
+                    if (i < n) {
+                        y[i] = fmaf(fa, __ldcg(&pcur[i]), __ldcg(&y[i]));
+                        ri = fmaf(-fa, __ldcg(&q[i]), __ldcg(&rh[i]));
+                        rh[i] = ri;
+                        zi = fabsf(__ldcg(&dinv[i])) * ri;
+                        z[i] = zi;
+                    }
+                    sF1[t] = ri;
+                    sF2[t] = zi;
                 }
-                sF1[T] = ri;
-                sF2[T] = zi;
                 __syncthreads();
                 float acc = 0.0f;
                 if (T < kT)

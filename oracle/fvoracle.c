@@ -26,7 +26,7 @@ enum { TERM_DDT = 0, TERM_LAPLACIAN = 1, TERM_DIV = 2, TERM_SOURCE = 3, TERM_EXP
 enum { ST_OK = 0, ST_NOT_CONVERGED = 3, ST_BREAKDOWN = 4, ST_UNSUPPORTED = 6 };
 
 #define RED_THREADS 256
-#define RED_ROWS_PER_THREAD 4
+#define RED_ROWS_PER_THREAD 8
 #define RED_ROWS_PER_BLOCK (RED_THREADS * RED_ROWS_PER_THREAD)
 
 void or_set_threads(int32_t nthreads) {
