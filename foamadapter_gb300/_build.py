@@ -37,7 +37,7 @@ CU_UNITS = {
     "boxmesh.cu": ["-fmad=false"],
     "serve.cu": [],
 }
-CPP_UNITS = ["common.cpp", "meshgen.cpp", "foamio.cpp"]
+CPP_UNITS = ["common.cpp", "meshgen.cpp", "foamio.cpp", "foamdict.cpp"]
 HEADERS = [INCLUDE / "fvgb.h", CSRC / "internal.cuh", CSRC / "fvgb_host_common.h"]
 
 

@@ -21,6 +21,7 @@ BC_CALCULATED, BC_FIXED_VALUE, BC_FIXED_GRADIENT = 0, 1, 2
 SCHEME_LINEAR, SCHEME_UPWIND, SCHEME_CORRECTED = 0, 1, 2
 TERM_DDT, TERM_LAPLACIAN, TERM_DIV, TERM_SOURCE, TERM_EXPLICIT, TERM_DIV_FLUX, TERM_DIV_EXPLICIT = range(7)
 PREC_FP64, PREC_MIXED_IR = 0, 1
+TOK_WORD, TOK_STRING, TOK_LABEL, TOK_SCALAR, TOK_PUNCT = 1, 2, 3, 4, 5
 
 vp = C.c_void_p
 i32 = C.c_int32
@@ -161,6 +162,28 @@ _SIGS = {
     "fvgb_box_build": (C.c_int, [C.POINTER(BoxSpec), C.POINTER(MeshArrays)]),
     "fvgb_geometry_compute": (C.c_int, [i32, vp, i32, i32, vp, vp, vp, i32, vp, i32,
                                         C.POINTER(MeshArrays)]),
+    "fvgb_dict_read": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+    "fvgb_dict_parse": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(vp)]),
+    "fvgb_dict_create": (C.c_int, [C.POINTER(vp)]),
+    "fvgb_dict_copy": (C.c_int, [vp, C.POINTER(vp)]),
+    "fvgb_dict_free": (C.c_int, [vp]),
+    "fvgb_dict_size": (i32, [vp]),
+    "fvgb_dict_key": (C.c_char_p, [vp, i32]),
+    "fvgb_dict_is_pattern": (i32, [vp, i32]),
+    "fvgb_dict_find": (i32, [vp, C.c_char_p]),
+    "fvgb_dict_sub": (vp, [vp, i32]),
+    "fvgb_dict_ntokens": (i32, [vp, i32]),
+    "fvgb_dict_token": (C.c_int, [vp, i32, i32, P_i32, C.POINTER(C.c_char_p), P_i64, C.POINTER(dbl)]),
+    "fvgb_dict_set": (C.c_int, [vp, C.c_char_p, C.c_char_p]),
+    "fvgb_dict_set_dict": (C.c_int, [vp, C.c_char_p, vp, C.POINTER(vp)]),
+    "fvgb_dict_remove": (C.c_int, [vp, C.c_char_p]),
+    "fvgb_dict_write": (C.c_int, [vp, C.c_char_p, i64, P_i64]),
+    "fvgb_fvsolution_update_solver": (C.c_int, [vp]),
+    "fvgb_fvsolution_update_preconditioner": (C.c_int, [vp]),
+    "fvgb_fvsolution_update_criteria": (C.c_int, [vp]),
+    "fvgb_fvsolution_map": (C.c_int, [vp, C.POINTER(vp)]),
+    "fvgb_solver_cfg_from_dict": (C.c_int, [vp, C.POINTER(SolverCfg)]),
+    "fvgb_scheme_from_dict": (C.c_int, [vp, C.c_char_p, C.c_char_p, P_i32]),
 }
 
 _lib = None

@@ -12,6 +12,7 @@
 //   FaceNormalGradient(mesh).faceNormalGrad(T, out)
 //   PDESolver(dsl::imp::ddt(T) - dsl::imp::laplacian(gamma, T), T, dt).solve()
 //   computeRAUandHByA, constrainHbyA, flux, updateFaceVelocity, updateVelocity
+//   readFoamDictionary(path), mapFvSolution(dict), solverConfig(dict)
 // Errors are C++ exceptions (fvgb::Error), as NeoN reports them; fields own
 // device storage (RAII), operators borrow the mesh, outputs are caller-owned
 // and accumulated into with a coefficient.
@@ -19,7 +20,10 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
+#include <cctype>
 #include <cstdint>
+#include <cstdio>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -477,6 +481,215 @@ inline void updateVelocity(const UnstructuredMesh& m, const DeviceArray<double>&
                            const VolumeField& p, VolumeField& U, cudaStream_t st = nullptr) {
     check(fvgb_piso_velocity_update(m.handle(), HbyA.data(), rAU.data(), p.internalVector().data(),
                                     p.boundaryValues().data(), U.internalVector().data(), st));
+}
+
+// ------------------------------------------------ NeoN::Dictionary (host)
+// FoamAdapter::convert(Foam::dictionary) (src/auxiliary/foamDictionary.cpp:
+// 68-91, convert.cpp:17-45) over libfvgb's dictionary reader: get<T> gives a
+// label (int64_t / int) for one integer token, a scalar (double) for one
+// number, a word (std::string) for one word or quoted string, a Vec3 for
+// (x y z), a bool for yes/no/on/off/true/false, the TokenList for anything
+// else.  Copying an owned Dictionary copies its entries (NeoN::Dictionary has
+// value semantics); subDict returns a view into its parent, as the reference's
+// Dictionary& does, valid until that entry is replaced or removed.
+using Vec3 = std::array<double, 3>;
+struct Token {
+    int32_t kind;  // FVGB_TOK_*
+    std::string text;
+    int64_t label;
+    double scalar;
+};
+using TokenList = std::vector<Token>;
+
+class Dictionary {
+public:
+    Dictionary() {
+        check(fvgb_dict_create(&h_));
+        owned_ = true;
+    }
+    static Dictionary read(const std::string& path) {
+        fvgb_dict* d = nullptr;
+        check(fvgb_dict_read(path.c_str(), &d));
+        return Dictionary(d, true);
+    }
+    static Dictionary parse(const std::string& text, const std::string& includeDir = ".") {
+        fvgb_dict* d = nullptr;
+        check(fvgb_dict_parse(text.c_str(), includeDir.c_str(), &d));
+        return Dictionary(d, true);
+    }
+    Dictionary(const Dictionary& o) : owned_(o.owned_) {
+        if (o.owned_) check(fvgb_dict_copy(o.h_, &h_));
+        else h_ = o.h_;
+    }
+    Dictionary& operator=(const Dictionary& o) {
+        if (this != &o) {
+            Dictionary t(o);
+            std::swap(h_, t.h_);
+            std::swap(owned_, t.owned_);
+        }
+        return *this;
+    }
+    Dictionary(Dictionary&& o) noexcept : h_(o.h_), owned_(o.owned_) { o.h_ = nullptr, o.owned_ = false; }
+    ~Dictionary() {
+        if (owned_ && h_) fvgb_dict_free(h_);
+    }
+
+    bool contains(const std::string& key) const { return fvgb_dict_find(h_, key.c_str()) >= 0; }
+    bool isDict(const std::string& key) const { return fvgb_dict_sub(h_, at(key)) != nullptr; }
+    Dictionary subDict(const std::string& key) const {
+        fvgb_dict* s = fvgb_dict_sub(h_, at(key));
+        if (!s) throw Error(FVGB_ERR_INVALID_ARG, "Dictionary::subDict: " + key + " is not a sub-dictionary");
+        return Dictionary(s, false);
+    }
+    std::vector<std::string> keys() const {
+        std::vector<std::string> k;
+        for (int32_t i = 0; i < fvgb_dict_size(h_); ++i) k.emplace_back(fvgb_dict_key(h_, i));
+        return k;
+    }
+    TokenList tokens(const std::string& key) const {
+        const int32_t i = at(key);
+        const int32_t n = fvgb_dict_ntokens(h_, i);
+        if (n < 0) throw Error(FVGB_ERR_INVALID_ARG, "Dictionary: " + key + " is a sub-dictionary");
+        TokenList t;
+        for (int32_t j = 0; j < n; ++j) {
+            Token k{};
+            const char* txt = nullptr;
+            check(fvgb_dict_token(h_, i, j, &k.kind, &txt, &k.label, &k.scalar));
+            k.text = txt;
+            t.push_back(k);
+        }
+        return t;
+    }
+    template <class T>
+    T get(const std::string& key) const;
+
+    void insert(const std::string& key, const std::string& word) {
+        bool plain = !word.empty() && (std::isalpha((unsigned char)word[0]) || word[0] == '_');
+        for (char c : word)
+            if (std::isspace((unsigned char)c) || c == ';' || c == '{' || c == '}' || c == '(' || c == ')' ||
+                c == '"' || c == '[' || c == ']')
+                plain = false;
+        check(fvgb_dict_set(h_, key.c_str(), (plain ? word : "\"" + word + "\"").c_str()));
+    }
+    void insert(const std::string& key, const char* word) { insert(key, std::string(word)); }
+    void insert(const std::string& key, double v) {
+        char b[64];
+        std::snprintf(b, sizeof b, "%.17g", v);
+        std::string t = b;
+        if (t.find_first_of(".eEni") == std::string::npos) t += ".0";  // keep it a scalar token
+        check(fvgb_dict_set(h_, key.c_str(), t.c_str()));
+    }
+    void insert(const std::string& key, int64_t v) { check(fvgb_dict_set(h_, key.c_str(), std::to_string(v).c_str())); }
+    void insert(const std::string& key, int v) { insert(key, (int64_t)v); }
+    void insert(const std::string& key, bool v) { check(fvgb_dict_set(h_, key.c_str(), v ? "true" : "false")); }
+    void insert(const std::string& key, const Dictionary& d) { check(fvgb_dict_set_dict(h_, key.c_str(), d.h_, nullptr)); }
+    void remove(const std::string& key) { check(fvgb_dict_remove(h_, key.c_str())); }
+    fvgb_dict* handle() const { return h_; }
+
+private:
+    Dictionary(fvgb_dict* h, bool owned) : h_(h), owned_(owned) {}
+    int32_t at(const std::string& key) const {
+        const int32_t i = fvgb_dict_find(h_, key.c_str());
+        if (i < 0) throw Error(FVGB_ERR_INVALID_ARG, "Dictionary: no entry " + key);
+        return i;
+    }
+    const Token& single(const std::string& key, TokenList& t) const {
+        t = tokens(key);
+        if (t.size() != 1) throw Error(FVGB_ERR_INVALID_ARG, "Dictionary: " + key + " is not a single token");
+        return t[0];
+    }
+    friend Dictionary mapFvSolution(const Dictionary&);
+    fvgb_dict* h_ = nullptr;
+    bool owned_ = false;
+};
+
+template <>
+inline int64_t Dictionary::get<int64_t>(const std::string& key) const {
+    TokenList t;
+    const Token& k = single(key, t);
+    if (k.kind != FVGB_TOK_LABEL) throw Error(FVGB_ERR_INVALID_ARG, "Dictionary: " + key + " is not a label");
+    return k.label;
+}
+template <>
+inline int Dictionary::get<int>(const std::string& key) const { return (int)get<int64_t>(key); }
+template <>
+inline double Dictionary::get<double>(const std::string& key) const {
+    TokenList t;
+    const Token& k = single(key, t);
+    if (k.kind != FVGB_TOK_SCALAR && k.kind != FVGB_TOK_LABEL)
+        throw Error(FVGB_ERR_INVALID_ARG, "Dictionary: " + key + " is not a number");
+    return k.scalar;
+}
+template <>
+inline std::string Dictionary::get<std::string>(const std::string& key) const {
+    TokenList t;
+    const Token& k = single(key, t);
+    if (k.kind != FVGB_TOK_WORD && k.kind != FVGB_TOK_STRING)
+        throw Error(FVGB_ERR_INVALID_ARG, "Dictionary: " + key + " is not a word");
+    return k.text;
+}
+template <>
+inline bool Dictionary::get<bool>(const std::string& key) const {
+    const std::string w = get<std::string>(key);
+    if (w == "yes" || w == "on" || w == "true") return true;
+    if (w == "no" || w == "off" || w == "false" || w == "none") return false;
+    throw Error(FVGB_ERR_INVALID_ARG, "Dictionary: " + key + " is not a switch");
+}
+template <>
+inline Vec3 Dictionary::get<Vec3>(const std::string& key) const {
+    const TokenList t = tokens(key);
+    if (t.size() != 5 || t[0].text != "(" || t[4].text != ")")
+        throw Error(FVGB_ERR_INVALID_ARG, "Dictionary: " + key + " is not a vector");
+    Vec3 v{};
+    for (int c = 0; c < 3; ++c) {
+        if (t[c + 1].kind != FVGB_TOK_SCALAR && t[c + 1].kind != FVGB_TOK_LABEL)
+            throw Error(FVGB_ERR_INVALID_ARG, "Dictionary: " + key + " is not a vector");
+        v[c] = t[c + 1].scalar;
+    }
+    return v;
+}
+template <>
+inline TokenList Dictionary::get<TokenList>(const std::string& key) const { return tokens(key); }
+
+inline Dictionary readFoamDictionary(const std::string& path) { return Dictionary::read(path); }
+
+// fvSolution.cpp:19-159
+inline void updateSolver(Dictionary& d) { check(fvgb_fvsolution_update_solver(d.handle())); }
+inline void updatePreconditioner(Dictionary& d) { check(fvgb_fvsolution_update_preconditioner(d.handle())); }
+inline void updateCriteria(Dictionary& d) { check(fvgb_fvsolution_update_criteria(d.handle())); }
+inline Dictionary mapFvSolution(const Dictionary& solverDict) {
+    fvgb_dict* m = nullptr;
+    check(fvgb_fvsolution_map(solverDict.handle(), &m));
+    return Dictionary(m, true);
+}
+// A Ginkgo-form solver entry (mapFvSolution's output) as PDESolver::solve's configuration.
+inline SolverConfig solverConfig(const Dictionary& mapped) {
+    fvgb_solver_cfg c{};
+    check(fvgb_solver_cfg_from_dict(mapped.handle(), &c));
+    SolverConfig s;
+    s.relTol = c.rel_tol;
+    s.tolerance = c.abs_tol;
+    s.maxIter = c.max_iter;
+    s.mixedPrecision = c.precision == FVGB_PREC_MIXED_IR;
+    s.innerRelTol = c.inner_rel_tol;
+    s.innerMaxIter = c.inner_max_iter;
+    s.maxOuter = c.max_outer;
+    s.bicgstab = c.method == FVGB_SOLVER_BICGSTAB;
+    return s;
+}
+// PDESolver::solve configured by the case's fvSolution as the reference reads
+// it (expression.hpp:141-153): the entry solvers/<psi.name>; an entry in
+// OpenFOAM form (solver PCG; ...) is mapped by mapFvSolution first.
+inline SolverStats solve(PDESolver& eqn, const Dictionary& fvSolution, cudaStream_t st = nullptr) {
+    Dictionary entry = fvSolution.subDict("solvers").subDict(eqn.getField().name);
+    const bool ginkgo = entry.contains("solver") && entry.get<std::string>("solver") == "Ginkgo";
+    return eqn.solve(solverConfig(ginkgo ? entry : mapFvSolution(entry)), st);
+}
+// The FVGB_SCHEME_* value fvSchemes gives `name` in `section` (own entry, else default).
+inline int scheme(const Dictionary& fvSchemes, const std::string& section, const std::string& name) {
+    int32_t s = 0;
+    check(fvgb_scheme_from_dict(fvSchemes.handle(), section.c_str(), name.c_str(), &s));
+    return s;
 }
 
 }  // namespace fvgb

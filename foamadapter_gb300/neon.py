@@ -382,7 +382,20 @@ class PDESolver:
     def setReference(self, cell: int, value: float):
         self.ref = (cell, value)
 
-    def solve(self, **cfg):
+    def solve(self, fvSolution=None, **cfg):
+        """Assemble, set the reference, solve, correct the boundary values.
+        With ``fvSolution`` (a ``dictionary.Dictionary`` of the case's
+        system/fvSolution), the entry solvers/<psi.name> configures the solve,
+        as PDESolver::solve reads it (expression.hpp:141-153); an entry in
+        OpenFOAM form (solver PCG; ...) is mapped by mapFvSolution first.
+        Keyword arguments override the entry."""
+        if fvSolution is not None:
+            from . import dictionary
+
+            entry = fvSolution.subDict("solvers").subDict(self.psi.name)
+            if not (entry.contains("solver") and entry.get("solver") == "Ginkgo"):
+                entry = dictionary.map_fv_solution(entry)
+            cfg = {**dictionary.solver_config(entry), **cfg}
         self.assemble()
         if self.ref is not None:
             self.ls.setReference(*self.ref)

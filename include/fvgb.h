@@ -590,6 +590,85 @@ fvgb_status fvgb_field_read_bc(const char* path, const fvgb_polymesh* pm, int32_
 fvgb_status fvgb_field_write(const char* path, const char* object, const fvgb_polymesh* pm, int32_t ncomp,
                              const double* internal, const double* boundary, int32_t flags);
 
+/* ---------------------------------------------- OpenFOAM dictionaries (host)
+ * system/fvSolution, system/fvSchemes and other OpenFOAM dictionaries, read
+ * without OpenFOAM.  Replaces Foam::dictionary + FoamAdapter::convert
+ * (src/auxiliary/foamDictionary.cpp:68-91, convert.cpp:17-45), which turn a
+ * case's dictionaries into NeoN::Dictionary (setup.cpp:107-109).  A primitive
+ * entry is kept as its token list; sub-dictionaries nest.  Supported syntax:
+ * comments, quoted strings, lists "( ... )", words with balanced parentheses
+ * (div(phi,T)), #include / #includeIfPresent / #sinclude, #inputMode,
+ * #remove, $name inside a value and $name; as an entry, quoted (regular
+ * expression) keywords.  Directives that run code give FVGB_ERR_UNSUPPORTED.
+ * A handle returned by read/parse/create/copy/map is a top-level dictionary
+ * and is released with fvgb_dict_free; fvgb_dict_sub returns a borrowed
+ * sub-dictionary that lives as long as its entry. */
+typedef struct fvgb_dict fvgb_dict;
+enum {
+    FVGB_TOK_WORD = 1,    /* word (yes/no/true/false included)          */
+    FVGB_TOK_STRING = 2,  /* quoted string, quotes removed              */
+    FVGB_TOK_LABEL = 3,   /* integer (label, and scalar = its value)    */
+    FVGB_TOK_SCALAR = 4,  /* floating-point number                      */
+    FVGB_TOK_PUNCT = 5    /* ( ) [ ] of a list                          */
+};
+fvgb_status fvgb_dict_read(const char* path, fvgb_dict** out);
+fvgb_status fvgb_dict_parse(const char* text, const char* include_dir, fvgb_dict** out);
+fvgb_status fvgb_dict_create(fvgb_dict** out);
+fvgb_status fvgb_dict_copy(const fvgb_dict* d, fvgb_dict** out);
+fvgb_status fvgb_dict_free(fvgb_dict* d);
+int32_t fvgb_dict_size(const fvgb_dict* d);
+const char* fvgb_dict_key(const fvgb_dict* d, int32_t i);       /* null when out of range */
+int32_t fvgb_dict_is_pattern(const fvgb_dict* d, int32_t i);
+/* Index of the entry a lookup finds (plain keyword, else the last-defined
+ * matching pattern), -1 if none. */
+int32_t fvgb_dict_find(const fvgb_dict* d, const char* keyword);
+fvgb_dict* fvgb_dict_sub(const fvgb_dict* d, int32_t i);        /* null for a primitive entry */
+int32_t fvgb_dict_ntokens(const fvgb_dict* d, int32_t i);       /* -1 for a sub-dictionary */
+fvgb_status fvgb_dict_token(const fvgb_dict* d, int32_t i, int32_t j, int32_t* kind, const char** text,
+                            int64_t* label, double* scalar);
+/* Insert or replace a primitive entry; value is its text ("PCG", "1e-6",
+ * "(1 2 3)", "\"solver::Cg\"", "$name" expands in d's scope). */
+fvgb_status fvgb_dict_set(fvgb_dict* d, const char* keyword, const char* value);
+/* Insert or replace a sub-dictionary: a copy of src, or empty if src is null. */
+fvgb_status fvgb_dict_set_dict(fvgb_dict* d, const char* keyword, const fvgb_dict* src, fvgb_dict** sub);
+fvgb_status fvgb_dict_remove(fvgb_dict* d, const char* keyword);  /* no-op when absent */
+/* Dictionary text (OpenFOAM syntax) into buf[cap] (NUL-terminated,
+ * truncated); *len = the full length. */
+fvgb_status fvgb_dict_write(const fvgb_dict* d, char* buf, int64_t cap, int64_t* len);
+
+/* FoamAdapter's fvSolution mapping, in place (fvSolution.cpp:19-142):
+ * update_solver: PCG -> Ginkgo solver::Cg, PBiCG -> solver::Bicg, PBiCGStab
+ *   and smoothSolver -> solver::Bicgstab, GAMG -> solver::Multigrid;
+ * update_preconditioner: none given -> DIC; DIC -> preconditioner::Jacobi
+ *   {max_block_size 1}; DILU -> preconditioner::Ilu {reverse_apply false;
+ *   factorization {type factorization::ParIlu}}; smoother removed; a
+ *   preconditioner dictionary whose type is a dictionary -> UNSUPPORTED;
+ * update_criteria: criteria {iteration 1000} plus relTol ->
+ *   relative_residual_norm, maxIter -> iteration, tolerance ->
+ *   absolute_residual_norm (the fvSolution keywords are removed).
+ * fvgb_fvsolution_map = mapFvSolution (fvSolution.cpp:145-159): a mapped copy,
+ * or a plain copy when the entry names a configFile. */
+fvgb_status fvgb_fvsolution_update_solver(fvgb_dict* solver_dict);
+fvgb_status fvgb_fvsolution_update_preconditioner(fvgb_dict* solver_dict);
+fvgb_status fvgb_fvsolution_update_criteria(fvgb_dict* solver_dict);
+fvgb_status fvgb_fvsolution_map(const fvgb_dict* solver_dict, fvgb_dict** mapped);
+/* A mapped (Ginkgo-form) solver entry as a solver configuration: type
+ * solver::Cg or solver::Bicgstab, preconditioner::Jacobi with max_block_size
+ * 1, criteria iteration / relative_residual_norm / absolute_residual_norm.
+ * This library's own keywords: precision FP64|mixed, innerRelTol,
+ * innerMaxIter, maxOuter.  Other solvers and preconditioners (Bicg,
+ * Multigrid, Ilu, none, block Jacobi) and configFile: FVGB_ERR_UNSUPPORTED. */
+fvgb_status fvgb_solver_cfg_from_dict(const fvgb_dict* mapped, fvgb_solver_cfg* cfg);
+/* The scheme fvSchemes gives `name` in `section` (its own entry, else
+ * default): divSchemes / gradSchemes "Gauss linear" -> FVGB_SCHEME_LINEAR,
+ * "Gauss upwind" -> FVGB_SCHEME_UPWIND; laplacianSchemes "Gauss linear
+ * uncorrected" -> 0, "Gauss linear corrected" -> FVGB_SCHEME_CORRECTED;
+ * snGradSchemes uncorrected -> 0, corrected -> FVGB_SCHEME_CORRECTED;
+ * interpolationSchemes linear / upwind; ddtSchemes Euler -> 0.  No entry or
+ * "none": FVGB_ERR_INVALID_ARG; other schemes: FVGB_ERR_UNSUPPORTED. */
+fvgb_status fvgb_scheme_from_dict(const fvgb_dict* fv_schemes, const char* section, const char* name,
+                                  int32_t* scheme);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,18 @@ def unpack_reference_files(root):
     return root
 
 
+def unpack_reference_dicts(root):
+    """The reference cases' system dictionaries (foam_dicts.npz), as they were,
+    under root/<test|tutorials>/<case>/system/..."""
+    d = np.load(GOLDEN / "foam_dicts.npz")
+    for item in d["_names"]:
+        key, rel = str(item).split("=", 1)
+        p = root / rel
+        p.parent.mkdir(parents=True, exist_ok=True)
+        p.write_bytes(d[key].tobytes())
+    return root
+
+
 @pytest.fixture(scope="session")
 def cuda():
     import torch

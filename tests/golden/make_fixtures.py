@@ -6,7 +6,10 @@ Reads the ascii OpenFOAM cases under the reference checkout's ``test/`` tree
 script, so that the tests run where the reference checkout is absent.
 ``foam_files.npz`` keeps the unparsed bytes of the small polyMesh and field
 files (key: the path with "/" written as "__"), the input of the tests of the
-library's own OpenFOAM file reader.
+library's own OpenFOAM file reader; ``foam_dicts.npz`` keeps the cases'
+``system/`` dictionaries (fvSolution, fvSchemes, controlDict, blockMeshDict,
+simulationParameters, testDictionary) the same way, for the dictionary
+reader's tests.
 Run:  python tests/golden/make_fixtures.py [/path/to/reference]
 """
 from __future__ import annotations
@@ -115,6 +118,13 @@ def main(ref: Path):
     raw = {k.replace("/", "__"): np.frombuffer((ref / "test" / k).read_bytes(), np.uint8) for k in files}
     np.savez_compressed(HERE / "foam_files.npz", **raw)
     print("foam_files", {k: v.size for k, v in raw.items()})
+    # the cases' system dictionaries, unparsed (input of the dictionary reader's tests)
+    dicts = sorted(p.relative_to(ref).as_posix() for top in ("test", "tutorials")
+                   for p in (ref / top).glob("*/system/*") if p.is_file() and p.suffix != ".json")
+    raw = {k.replace("/", "__").replace("-", "_"): np.frombuffer((ref / k).read_bytes(), np.uint8) for k in dicts}
+    names = {k.replace("/", "__").replace("-", "_"): k for k in dicts}
+    np.savez_compressed(HERE / "foam_dicts.npz", _names=np.asarray([f"{a}={b}" for a, b in names.items()]), **raw)
+    print("foam_dicts", len(raw))
 
 
 if __name__ == "__main__":
