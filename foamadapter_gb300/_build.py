@@ -36,6 +36,7 @@ CU_UNITS = {
     "noalloc.cu": ["-fmad=false"],
     "boxmesh.cu": ["-fmad=false"],
     "serve.cu": [],
+    "amg.cu": [],
 }
 CPP_UNITS = ["common.cpp", "meshgen.cpp", "foamio.cpp", "foamdict.cpp"]
 HEADERS = [INCLUDE / "fvgb.h", CSRC / "internal.cuh", CSRC / "fvgb_host_common.h"]

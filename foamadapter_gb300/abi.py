@@ -51,10 +51,11 @@ class Term(C.Structure):
 class SolverCfg(C.Structure):
     _fields_ = [("rel_tol", dbl), ("abs_tol", dbl), ("max_iter", i32), ("precision", i32),
                 ("inner_rel_tol", dbl), ("inner_max_iter", i32), ("max_outer", i32), ("kernel_mode", i32),
-                ("flags", i32), ("method", i32)]
+                ("flags", i32), ("method", i32), ("preconditioner", i32)]
 
 
 SOLVER_CG, SOLVER_BICGSTAB = 0, 1
+PRECOND_JACOBI, PRECOND_MULTIGRID = 0, 1
 
 
 SOLVE_NO_TUNE = 1
@@ -184,6 +185,9 @@ _SIGS = {
     "fvgb_fvsolution_map": (C.c_int, [vp, C.POINTER(vp)]),
     "fvgb_solver_cfg_from_dict": (C.c_int, [vp, C.POINTER(SolverCfg)]),
     "fvgb_scheme_from_dict": (C.c_int, [vp, C.c_char_p, C.c_char_p, P_i32]),
+    "fvgb_amg_apply": (C.c_int, [vp, vp, vp, vp]),
+    "fvgb_amg_info": (C.c_int, [vp, P_i32, vp, vp, i32]),
+    "fvgb_pgm_aggregate": (C.c_int, [i32, vp, vp, vp, vp, P_i32]),
 }
 
 _lib = None

@@ -396,6 +396,7 @@ struct SolverConfig {
     int innerMaxIter = 1000;
     int maxOuter = 50;
     bool bicgstab = false;  // solver "BiCGStab" (fvSolution.cpp:25-26) instead of "CG"
+    bool multigrid = false; // preconditioner solver::Multigrid (FP64 CG) instead of Jacobi
 };
 
 class LinearSystem {
@@ -438,7 +439,8 @@ public:
                             c.mixedPrecision ? FVGB_PREC_MIXED_IR : FVGB_PREC_FP64,
                             c.innerRelTol > 0 ? c.innerRelTol : (c.bicgstab ? 0.01 : 0.1),
                             c.innerMaxIter, c.maxOuter, 0, 0,
-                            c.bicgstab ? FVGB_SOLVER_BICGSTAB : FVGB_SOLVER_CG};
+                            c.bicgstab ? FVGB_SOLVER_BICGSTAB : FVGB_SOLVER_CG,
+                            c.multigrid ? FVGB_PRECOND_MULTIGRID : FVGB_PRECOND_JACOBI};
         fvgb_solver_stats s{};
         fvgb_status r = fvgb_solve(ls_.handle(), psi_.internalVector().data(), &cfg, &s, st);
         if (r != FVGB_OK && r != FVGB_ERR_NOT_CONVERGED) check(r);  // non-convergence is not an error
@@ -675,6 +677,7 @@ inline SolverConfig solverConfig(const Dictionary& mapped) {
     s.innerMaxIter = c.inner_max_iter;
     s.maxOuter = c.max_outer;
     s.bicgstab = c.method == FVGB_SOLVER_BICGSTAB;
+    s.multigrid = c.preconditioner == FVGB_PRECOND_MULTIGRID;
     return s;
 }
 // PDESolver::solve configured by the case's fvSolution as the reference reads

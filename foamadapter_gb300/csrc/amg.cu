@@ -1,0 +1,896 @@
+// Multigrid-preconditioned CG (FP64) for a single scalar system.
+//
+// The reference selects it through a Ginkgo configuration: solver::Cg whose
+// preconditioner is solver::Multigrid with multigrid::Pgm levels
+// (tutorials/cylinder2D/system/gko/config.mg.json; GAMG in an fvSolution maps
+// to Ginkgo's multigrid, src/compatibility/fvSolution.cpp:27).  Ginkgo is not
+// part of the reference checkout; this is this library's own aggregation AMG
+// built on the published parallel-graph-match (PGM) idea:
+//
+// Setup, symbolic (host, once per system, from the first matrix solved):
+//  * PGM aggregation (pgm_aggregate): strength |a_ij| between rows; in up to
+//    15 rounds every unaggregated row picks its strongest unaggregated
+//    neighbour (ties: the lower index) and mutual picks become pairs; the
+//    rounds stop when at most 5% of the rows are left or no pair forms.  A row
+//    left over joins the aggregate of its strongest aggregated neighbour, or
+//    stays alone.  Aggregates are numbered by their lowest row.
+//  * Galerkin coarse matrix A_c = P^T A P for the piecewise-constant P: its
+//    pattern and, for each coarse entry, the fine entries it sums (fine rows
+//    ascending, entries in row order).  Levels are added until at most
+//    kCoarseRows rows remain, the aggregation stops shrinking the system
+//    (more than 90% of the rows left), or kMaxLevels is reached.
+// Setup, numeric (device, whenever the matrix values changed): the coarse
+// values by those fixed sums, the Jacobi diagonals, and the inverse of the
+// coarsest matrix by Gauss-Jordan elimination in one block (no pivoting: the
+// matrix is symmetric positive definite).
+// V-cycle z = M r: per level one damped-Jacobi sweep from zero (weight 0.9),
+// the residual, restriction by aggregate sums, the coarser level, then the
+// coarse correction and one more damped-Jacobi sweep; the coarsest level is
+// solved exactly with the dense inverse.  Pre- and post-smoothing are the same
+// symmetric sweep, so M is symmetric positive definite and CG applies.
+//
+// The solve is one CUDA graph (init, a device-side while loop over the CG
+// iteration with the V-cycle inside, bounded by max_iter).  Its stopping test
+// and statistics are those of the Jacobi-PCG (Ginkgo criteria: ||r|| below
+// max(rel_tol ||r_0||, abs_tol)).  Every reduction has a fixed order, so a
+// solve is deterministic; its iterates are not those of the Jacobi-PCG.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace {
+
+constexpr int kT = 256;
+constexpr int kCoarseRows = 256;
+constexpr int kMaxLevels = 25;
+constexpr double kOmega = 0.9;
+constexpr int kPgmRounds = 15;
+constexpr double kPgmLeftRatio = 0.05;
+
+struct HostCsr {
+    int n = 0;
+    std::vector<int> rp, ci;
+    std::vector<double> v;
+};
+
+// ------------------------------------------------------------ PGM (host)
+int pgm_aggregate(int n, const int* rp, const int* ci, const double* v, std::vector<int>& agg) {
+    agg.assign(n, -1);
+    std::vector<int> pick(n, -1);
+    std::vector<int> tmp(n, -1);  // provisional aggregate id of each row
+    int next = 0, left = n;
+    for (int round = 0; round < kPgmRounds; ++round) {
+        for (int i = 0; i < n; ++i) {
+            pick[i] = -1;
+            if (tmp[i] >= 0) continue;
+            double best = 0.0;
+            for (int k = rp[i]; k < rp[i + 1]; ++k) {
+                const int j = ci[k];
+                if (j == i || tmp[j] >= 0) continue;
+                const double w = std::fabs(v[k]);
+                if (w > best || (w == best && w > 0.0 && (pick[i] < 0 || j < pick[i]))) {
+                    best = w;
+                    pick[i] = j;
+                }
+            }
+        }
+        int formed = 0;
+        for (int i = 0; i < n; ++i) {
+            const int j = pick[i];
+            if (tmp[i] < 0 && j > i && pick[j] == i) {
+                tmp[i] = tmp[j] = next++;
+                ++formed;
+                left -= 2;
+            }
+        }
+        if (formed == 0 || left <= kPgmLeftRatio * n) break;
+    }
+    // rows left over: the strongest aggregated neighbour's aggregate, else alone
+    std::vector<int> late(n, -1);
+    for (int i = 0; i < n; ++i) {
+        if (tmp[i] >= 0) continue;
+        double best = 0.0;
+        int to = -1;
+        for (int k = rp[i]; k < rp[i + 1]; ++k) {
+            const int j = ci[k];
+            if (j == i || tmp[j] < 0) continue;
+            const double w = std::fabs(v[k]);
+            if (w > best || (w == best && w > 0.0 && (to < 0 || j < to))) {
+                best = w;
+                to = j;
+            }
+        }
+        late[i] = to >= 0 ? tmp[to] : -1;
+    }
+    for (int i = 0; i < n; ++i)
+        if (tmp[i] < 0) tmp[i] = late[i] >= 0 ? late[i] : next++;
+    // number the aggregates by their lowest row
+    std::vector<int> renum(next, -1);
+    int nc = 0;
+    for (int i = 0; i < n; ++i) {
+        if (renum[tmp[i]] < 0) renum[tmp[i]] = nc++;
+        agg[i] = renum[tmp[i]];
+    }
+    return nc;
+}
+
+// A_c = P^T A P: pattern (columns ascending), values, and for every coarse
+// entry the fine entries it sums (gptr/gsrc), in the order they are summed.
+void galerkin(const HostCsr& A, const std::vector<int>& agg, int nc, HostCsr& Ac, std::vector<int>& mptr,
+              std::vector<int>& mem, std::vector<int>& gptr, std::vector<int>& gsrc) {
+    mptr.assign(nc + 1, 0);
+    for (int i = 0; i < A.n; ++i) ++mptr[agg[i] + 1];
+    for (int c = 0; c < nc; ++c) mptr[c + 1] += mptr[c];
+    mem.assign(A.n, 0);
+    {
+        std::vector<int> fill(mptr.begin(), mptr.end() - 1);
+        for (int i = 0; i < A.n; ++i) mem[fill[agg[i]]++] = i;  // ascending within an aggregate
+    }
+    Ac.n = nc;
+    Ac.rp.assign(nc + 1, 0);
+    Ac.ci.clear();
+    Ac.v.clear();
+    gptr.assign(1, 0);
+    gsrc.clear();
+    gsrc.reserve(A.ci.size());
+    std::vector<std::pair<int, int>> items;  // (coarse column, fine entry) in summation order
+    for (int c = 0; c < nc; ++c) {
+        items.clear();
+        for (int m = mptr[c]; m < mptr[c + 1]; ++m) {
+            const int i = mem[m];
+            for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) items.emplace_back(agg[A.ci[k]], k);
+        }
+        std::stable_sort(items.begin(), items.end(),
+                         [](const std::pair<int, int>& a, const std::pair<int, int>& b) { return a.first < b.first; });
+        size_t s = 0;
+        while (s < items.size()) {
+            const int col = items[s].first;
+            double sum = 0.0;
+            size_t e = s;
+            while (e < items.size() && items[e].first == col) {
+                sum += A.v[items[e].second];
+                gsrc.push_back(items[e].second);
+                ++e;
+            }
+            Ac.ci.push_back(col);
+            Ac.v.push_back(sum);
+            gptr.push_back((int)gsrc.size());
+            s = e;
+        }
+        Ac.rp[c + 1] = (int)Ac.ci.size();
+    }
+}
+
+// ------------------------------------------------------------ device state
+struct AmgState {
+    double* x;
+    double rel_tol, abs_tol;
+    int32_t max_iter;
+    double rz, alpha, beta, res0, res, tol;
+    int32_t iter, status, done;
+    unsigned counter;
+    fvgb_solver_stats* stats_out;  // device, or null
+    fvgb_solver_stats stats;
+};
+
+struct Level {
+    int n = 0, nnz = 0;
+    int *rp = nullptr, *ci = nullptr, *dpos = nullptr;  // levels >= 1 (level 0: the mesh's sliced ELL)
+    double *val = nullptr, *dinv = nullptr;
+    int* agg = nullptr;                    // [n], when a coarser level follows
+    int *mptr = nullptr, *mem = nullptr;   // members of the next level's rows
+    int *gptr = nullptr, *gsrc = nullptr;  // sums forming the next level's values
+    int nnz_next = 0;
+    double *b = nullptr, *x = nullptr, *xo = nullptr, *r = nullptr;
+};
+
+}  // namespace
+
+struct AmgCache {
+    const fvgb_ls* ls = nullptr;
+    uint64_t version = 0;
+    std::vector<Level> lv;
+    int nc = 0;            // rows of the coarsest level
+    double* ainv = nullptr;  // [nc*nc] inverse of the coarsest matrix
+    double *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *part = nullptr;
+    AmgState* st = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<void*> allocs;
+    int nblk = 0;
+};
+
+namespace {
+
+template <class T>
+cudaError_t dev_alloc(AmgCache* c, T** p, size_t count) {
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+    if (e == cudaSuccess) c->allocs.push_back(*p);
+    return e;
+}
+
+template <class T>
+cudaError_t upload(AmgCache* c, T** p, const std::vector<T>& h) {
+    cudaError_t e = dev_alloc(c, p, h.size());
+    if (e == cudaSuccess && !h.empty()) e = cudaMemcpy(*p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice);
+    return e;
+}
+
+// ------------------------------------------------------------ row access
+struct EllRows {  // level 0: the system's sliced-ELL matrix
+    MeshView m;
+    const double* val;
+    template <class F>
+    __device__ __forceinline__ void each(int i, F f) const {
+        const int slice = i >> 5;
+        const int b0 = __ldg(&m.m_ptr[slice]);
+        const int base = b0 + (i & 31);
+        const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+        for (int k = 0; k < w; ++k) {
+            const int pos = base + k * 32;
+            f(slot_col(m, pos, i), __ldg(&val[pos]));
+        }
+    }
+};
+
+struct CsrRows {
+    const int* rp;
+    const int* ci;
+    const double* val;
+    template <class F>
+    __device__ __forceinline__ void each(int i, F f) const {
+        for (int k = __ldg(&rp[i]); k < __ldg(&rp[i + 1]); ++k) f(__ldg(&ci[k]), __ldg(&val[k]));
+    }
+};
+
+// ------------------------------------------------------------ reductions
+__device__ __forceinline__ double block_sum(double v, double* sm) {
+    sm[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = kT / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+        __syncthreads();
+    }
+    const double r = sm[0];
+    __syncthreads();
+    return r;
+}
+
+// Block partial into part[blockIdx.x]; true in the last block to arrive, which
+// then sums part[0..gridDim.x) in index order (the same tree every time).
+__device__ __forceinline__ bool arrive(AmgState* st, double* part, double partial, double* sm, double* total) {
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = partial;
+        __threadfence();
+        last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s = 0.0;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += kT) s += __ldcg(&part[k]);
+    *total = block_sum(s, sm);
+    if (threadIdx.x == 0) st->counter = 0;
+    return true;
+}
+
+__device__ __forceinline__ volatile const int32_t& done_flag(const AmgState* st) { return st->done; }
+
+// ------------------------------------------------------------ numeric setup
+__global__ void __launch_bounds__(kT) k_dinv_ell(MeshView m, const double* __restrict__ val, double* __restrict__ dinv) {
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i < m.n) dinv[i] = 1.0 / __ldg(&val[__ldg(&m.diag_pos[i])]);
+}
+
+__global__ void __launch_bounds__(kT)
+    k_galerkin(int nnz_c, const int* __restrict__ gptr, const int* __restrict__ gsrc, const double* __restrict__ vf,
+               double* __restrict__ vc) {
+    const int k = blockIdx.x * kT + threadIdx.x;
+    if (k >= nnz_c) return;
+    double s = 0.0;
+    for (int t = __ldg(&gptr[k]); t < __ldg(&gptr[k + 1]); ++t) s += __ldg(&vf[__ldg(&gsrc[t])]);
+    vc[k] = s;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_dinv_csr(int n, const int* __restrict__ dpos, const double* __restrict__ val, double* __restrict__ dinv) {
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i < n) dinv[i] = 1.0 / __ldg(&val[__ldg(&dpos[i])]);
+}
+
+__global__ void __launch_bounds__(kT)
+    k_dense(int n, const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ val,
+            double* __restrict__ a) {
+    const int i = blockIdx.x;
+    for (int j = threadIdx.x; j < n; j += kT) a[(size_t)i * n + j] = 0.0;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = rp[i]; k < rp[i + 1]; ++k) a[(size_t)i * n + ci[k]] = val[k];
+}
+
+// In-place Gauss-Jordan inverse of an n x n SPD matrix, one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_gauss_jordan(int n, double* __restrict__ a) {
+    extern __shared__ double f[];  // [n]: column k of the step
+    for (int k = 0; k < n; ++k) {
+        const double piv = a[(size_t)k * n + k];
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) f[i] = a[(size_t)i * n + k];
+        __syncthreads();
+        const double ip = 1.0 / piv;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) a[(size_t)k * n + j] = (j == k ? 1.0 : a[(size_t)k * n + j]) * ip;
+        __syncthreads();
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            const int i = t / n, j = t - i * n;
+            if (i == k) continue;
+            const double akj = a[(size_t)k * n + j];
+            a[(size_t)i * n + j] = (j == k ? 0.0 : a[(size_t)i * n + j]) - f[i] * akj;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ V-cycle
+// x = w D^-1 b (one sweep from zero); r = b - A x
+template <class R>
+__global__ void __launch_bounds__(kT)
+    k_pre(const AmgState* st, R rows, int n, const double* __restrict__ dinv, const double* __restrict__ b,
+          double* __restrict__ x, double* __restrict__ r) {
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i >= n) return;
+    const double bi = __ldg(&b[i]);
+    x[i] = kOmega * __ldg(&dinv[i]) * bi;
+    double s = 0.0;
+    rows.each(i, [&](int j, double a) { s = fma(a, kOmega * __ldg(&dinv[j]) * __ldg(&b[j]), s); });
+    r[i] = bi - s;
+}
+
+// b_c[I] = sum of r over the rows of aggregate I
+__global__ void __launch_bounds__(kT)
+    k_restrict(const AmgState* st, int nc, const int* __restrict__ mptr, const int* __restrict__ mem,
+               const double* __restrict__ r, double* __restrict__ bc) {
+    if (done_flag(st)) return;
+    const int c = blockIdx.x * kT + threadIdx.x;
+    if (c >= nc) return;
+    double s = 0.0;
+    for (int k = __ldg(&mptr[c]); k < __ldg(&mptr[c + 1]); ++k) s += __ldg(&r[__ldg(&mem[k])]);
+    bc[c] = s;
+}
+
+// x = A_c^-1 b on the coarsest level, one warp per row
+__global__ void __launch_bounds__(kT)
+    k_coarse(const AmgState* st, int n, const double* __restrict__ ainv, const double* __restrict__ b,
+             double* __restrict__ x) {
+    if (done_flag(st)) return;
+    const int row = blockIdx.x * (kT / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double s = 0.0;
+    for (int j = lane; j < n; j += 32) s = fma(__ldg(&ainv[(size_t)row * n + j]), __ldg(&b[j]), s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[row] = s;
+}
+
+// y = x + P xc; out = y + w D^-1 (b - A y)
+template <class R>
+__global__ void __launch_bounds__(kT)
+    k_post(const AmgState* st, R rows, int n, const double* __restrict__ dinv, const double* __restrict__ b,
+           const double* __restrict__ x, const double* __restrict__ xc, const int* __restrict__ agg,
+           double* __restrict__ out) {
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i >= n) return;
+    const double yi = __ldg(&x[i]) + __ldg(&xc[__ldg(&agg[i])]);
+    double s = 0.0;
+    rows.each(i, [&](int j, double a) { s = fma(a, __ldg(&x[j]) + __ldg(&xc[__ldg(&agg[j])]), s); });
+    out[i] = fma(kOmega * __ldg(&dinv[i]), __ldg(&b[i]) - s, yi);
+}
+
+// ------------------------------------------------------------ CG
+__global__ void k_params(AmgState* st, double* x, double rel_tol, double abs_tol, int max_iter,
+                         fvgb_solver_stats* out) {
+    st->x = x;
+    st->rel_tol = rel_tol;
+    st->abs_tol = abs_tol;
+    st->max_iter = max_iter;
+    st->stats_out = out;
+    st->counter = 0;
+    st->done = 0;
+}
+
+// r = b - A x, ||r||
+__global__ void __launch_bounds__(kT)
+    k_init(AmgState* st, EllRows A, int n, const double* __restrict__ b, double* __restrict__ r, double* part) {
+    __shared__ double sm[kT];
+    const int i = blockIdx.x * kT + threadIdx.x;
+    const double* x = st->x;
+    double ri = 0.0;
+    if (i < n) {
+        double s = 0.0;
+        A.each(i, [&](int j, double a) { s = fma(a, x[j], s); });
+        ri = __ldg(&b[i]) - s;
+        r[i] = ri;
+    }
+    double tot;
+    if (arrive(st, part, block_sum(ri * ri, sm), sm, &tot) && threadIdx.x == 0) {
+        const double res = sqrt(tot);
+        st->res0 = st->res = res;
+        st->iter = 0;
+        st->status = FVGB_OK;
+        double tol = st->rel_tol * res;
+        if (st->abs_tol > tol) tol = st->abs_tol;
+        st->tol = tol;
+        int done = !(res > tol) || res == 0.0;
+        if (!isfinite(res)) {
+            done = 1;
+            st->status = FVGB_ERR_BREAKDOWN;
+        } else if (!done && st->max_iter <= 0) {
+            done = 1;
+            st->status = FVGB_ERR_NOT_CONVERGED;
+        }
+        st->done = done;
+    }
+}
+
+// p = z, rz = r.z (first direction)
+__global__ void __launch_bounds__(kT)
+    k_first_dir(AmgState* st, int n, const double* __restrict__ r, const double* __restrict__ z, double* __restrict__ p,
+                double* part) {
+    __shared__ double sm[kT];
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        const double zi = z[i];
+        p[i] = zi;
+        v = r[i] * zi;
+    }
+    double tot;
+    if (arrive(st, part, block_sum(v, sm), sm, &tot) && threadIdx.x == 0) st->rz = tot;
+}
+
+// q = A p, alpha = rz / p.q
+__global__ void __launch_bounds__(kT)
+    k_spmv(AmgState* st, EllRows A, int n, const double* __restrict__ p, double* __restrict__ q, double* part) {
+    __shared__ double sm[kT];
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        double s = 0.0;
+        A.each(i, [&](int j, double a) { s = fma(a, __ldg(&p[j]), s); });
+        q[i] = s;
+        v = __ldg(&p[i]) * s;
+    }
+    double tot;
+    if (arrive(st, part, block_sum(v, sm), sm, &tot) && threadIdx.x == 0) {
+        const double alpha = st->rz / tot;
+        st->alpha = alpha;
+        if (tot == 0.0 || !isfinite(alpha)) {
+            st->status = FVGB_ERR_BREAKDOWN;
+            st->done = 1;
+        }
+    }
+}
+
+// x += alpha p, r -= alpha q, ||r||, convergence
+__global__ void __launch_bounds__(kT)
+    k_update(AmgState* st, int n, const double* __restrict__ p, const double* __restrict__ q, double* __restrict__ r,
+             double* part) {
+    __shared__ double sm[kT];
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    const double alpha = st->alpha;
+    double* x = st->x;
+    double v = 0.0;
+    if (i < n) {
+        x[i] = fma(alpha, __ldg(&p[i]), x[i]);
+        const double ri = fma(-alpha, __ldg(&q[i]), r[i]);
+        r[i] = ri;
+        v = ri * ri;
+    }
+    double tot;
+    if (arrive(st, part, block_sum(v, sm), sm, &tot) && threadIdx.x == 0) {
+        const double res = sqrt(tot);
+        st->res = res;
+        st->iter += 1;
+        if (!isfinite(res)) {
+            st->status = FVGB_ERR_BREAKDOWN;
+            st->done = 1;
+        } else if (res <= st->tol) {
+            st->done = 1;
+        } else if (st->iter >= st->max_iter) {
+            st->status = FVGB_ERR_NOT_CONVERGED;
+            st->done = 1;
+        }
+    }
+}
+
+// beta = r.z / rz_old
+__global__ void __launch_bounds__(kT)
+    k_rz(AmgState* st, int n, const double* __restrict__ r, const double* __restrict__ z, double* part) {
+    __shared__ double sm[kT];
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    const double v = i < n ? __ldg(&r[i]) * __ldg(&z[i]) : 0.0;
+    double tot;
+    if (arrive(st, part, block_sum(v, sm), sm, &tot) && threadIdx.x == 0) {
+        st->beta = tot / st->rz;
+        st->rz = tot;
+        if (!isfinite(st->beta)) {
+            st->status = FVGB_ERR_BREAKDOWN;
+            st->done = 1;
+        }
+    }
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(kT)
+    k_dir(const AmgState* st, int n, const double* __restrict__ z, double* __restrict__ p) {
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i < n) p[i] = fma(st->beta, p[i], __ldg(&z[i]));
+}
+
+__global__ void k_cond(AmgState* st, cudaGraphConditionalHandle h) {
+    cudaGraphSetConditional(h, st->done ? 0u : 1u);
+}
+
+__global__ void k_stats(AmgState* st) {
+    fvgb_solver_stats s{};
+    s.init_res_norm = st->res0;
+    s.final_res_norm = st->res;
+    s.num_iter = st->iter;
+    s.num_outer = 0;
+    s.status = st->status;
+    st->stats = s;
+    if (st->stats_out) *st->stats_out = s;
+}
+
+// ------------------------------------------------------------ host side
+fvgb_status symbolic(AmgCache* c, cudaStream_t s) {
+    const fvgb_ls* ls = c->ls;
+    const fvgb_mesh* mesh = ls->mesh;
+    const int n = mesh->v.n, nnz = mesh->nnz;
+    if ((int)mesh->h_row_offs.size() != n + 1 || (int)mesh->h_col.size() != nnz)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: the mesh keeps no host sparsity pattern (device-built boxes)");
+    // level 0 in CSR on the host: pattern from the mesh, values from the device
+    std::vector<int> csr_pos(nnz);
+    std::vector<double> slots(mesh->m_len);
+    FVGB_CUDA_TRY(cudaStreamSynchronize(s));
+    FVGB_CUDA_TRY(cudaMemcpy(csr_pos.data(), mesh->csr_pos, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+    FVGB_CUDA_TRY(cudaMemcpy(slots.data(), ls->values, sizeof(double) * mesh->m_len, cudaMemcpyDeviceToHost));
+    HostCsr A;
+    A.n = n;
+    A.rp = mesh->h_row_offs;
+    A.ci = mesh->h_col;
+    A.v.resize(nnz);
+    for (int k = 0; k < nnz; ++k) A.v[k] = slots[csr_pos[k]];
+    c->lv.clear();
+    c->lv.emplace_back();
+    c->lv[0].n = n;
+    c->lv[0].nnz = nnz;
+    bool top = true;
+    while ((int)c->lv.size() < kMaxLevels && A.n > kCoarseRows) {
+        std::vector<int> agg;
+        const int nc = pgm_aggregate(A.n, A.rp.data(), A.ci.data(), A.v.data(), agg);
+        if (nc > 0.9 * A.n) break;
+        HostCsr Ac;
+        std::vector<int> mptr, mem, gptr, gsrc;
+        galerkin(A, agg, nc, Ac, mptr, mem, gptr, gsrc);
+        Level& L = c->lv.back();
+        if (top)  // level 0's sums read the sliced-ELL slots
+            for (int& k : gsrc) k = csr_pos[k];
+        top = false;
+        cudaError_t e = upload(c, &L.agg, agg);
+        if (e == cudaSuccess) e = upload(c, &L.mptr, mptr);
+        if (e == cudaSuccess) e = upload(c, &L.mem, mem);
+        if (e == cudaSuccess) e = upload(c, &L.gptr, gptr);
+        if (e == cudaSuccess) e = upload(c, &L.gsrc, gsrc);
+        if (e != cudaSuccess) return cuda_fail(e, "multigrid setup");
+        L.nnz_next = (int)Ac.ci.size();
+        Level C;
+        C.n = Ac.n;
+        C.nnz = (int)Ac.ci.size();
+        std::vector<int> dpos(Ac.n, -1);
+        for (int i = 0; i < Ac.n; ++i)
+            for (int k = Ac.rp[i]; k < Ac.rp[i + 1]; ++k)
+                if (Ac.ci[k] == i) dpos[i] = k;
+        for (int i = 0; i < Ac.n; ++i)
+            if (dpos[i] < 0) return fvgb_fail(FVGB_ERR_INVALID_ARG, "multigrid: a coarse row without a diagonal entry");
+        e = upload(c, &C.rp, Ac.rp);
+        if (e == cudaSuccess) e = upload(c, &C.ci, Ac.ci);
+        if (e == cudaSuccess) e = upload(c, &C.dpos, dpos);
+        if (e == cudaSuccess) e = dev_alloc(c, &C.val, (size_t)C.nnz);
+        if (e != cudaSuccess) return cuda_fail(e, "multigrid setup");
+        c->lv.push_back(C);
+        A = std::move(Ac);
+    }
+    if (c->lv.size() < 2) return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: the system does not coarsen (too small?)");
+    c->nc = c->lv.back().n;
+    if (c->nc > 1024) return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: the coarsest level keeps above 1024 rows");
+    for (size_t l = 0; l < c->lv.size(); ++l) {
+        Level& L = c->lv[l];
+        cudaError_t e = dev_alloc(c, &L.dinv, (size_t)L.n);
+        if (e == cudaSuccess) e = dev_alloc(c, &L.x, (size_t)L.n);
+        if (e == cudaSuccess) e = dev_alloc(c, &L.xo, (size_t)L.n);
+        if (e == cudaSuccess) e = dev_alloc(c, &L.r, (size_t)L.n);
+        if (e == cudaSuccess && l > 0) e = dev_alloc(c, &L.b, (size_t)L.n);
+        if (e != cudaSuccess) return cuda_fail(e, "multigrid vectors");
+    }
+    c->nblk = (int)grid_for(n, kT);
+    cudaError_t e = dev_alloc(c, &c->ainv, (size_t)c->nc * c->nc);
+    if (e == cudaSuccess) e = dev_alloc(c, &c->r, (size_t)n);
+    if (e == cudaSuccess) e = dev_alloc(c, &c->p, (size_t)n);
+    if (e == cudaSuccess) e = dev_alloc(c, &c->q, (size_t)n);
+    if (e == cudaSuccess) e = dev_alloc(c, &c->z, (size_t)n);
+    if (e == cudaSuccess) e = dev_alloc(c, &c->part, (size_t)c->nblk);
+    if (e == cudaSuccess) e = dev_alloc(c, &c->st, 1);
+    if (e == cudaSuccess) e = cudaMemset(c->st, 0, sizeof(AmgState));
+    if (e != cudaSuccess) return cuda_fail(e, "multigrid vectors");
+    FVGB_CUDA_TRY(settle_creation());
+    return FVGB_OK;
+}
+
+fvgb_status numeric(AmgCache* c, cudaStream_t s) {
+    const fvgb_ls* ls = c->ls;
+    const MeshView m = ls->mesh->v;
+    k_dinv_ell<<<grid_for(m.n, kT), kT, 0, s>>>(m, ls->values, c->lv[0].dinv);
+    for (size_t l = 0; l + 1 < c->lv.size(); ++l) {
+        const Level& F = c->lv[l];
+        Level& C = c->lv[l + 1];
+        const double* vf = l == 0 ? ls->values : F.val;
+        k_galerkin<<<grid_for(C.nnz, kT), kT, 0, s>>>(C.nnz, F.gptr, F.gsrc, vf, C.val);
+        k_dinv_csr<<<grid_for(C.n, kT), kT, 0, s>>>(C.n, C.dpos, C.val, C.dinv);
+    }
+    const Level& B = c->lv.back();
+    k_dense<<<B.n, kT, 0, s>>>(B.n, B.rp, B.ci, B.val, c->ainv);
+    k_gauss_jordan<<<1, 1024, sizeof(double) * B.n, s>>>(B.n, c->ainv);
+    FVGB_LAUNCH_CHECK("multigrid numeric setup");
+    c->version = ls->version;
+    return FVGB_OK;
+}
+
+cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* dep, void* func, unsigned grid,
+                       unsigned block, void** args, unsigned smem = 0) {
+    cudaKernelNodeParams kp{};
+    kp.func = func;
+    kp.gridDim = dim3(grid);
+    kp.blockDim = dim3(block);
+    kp.sharedMemBytes = smem;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    const bool has_dep = dep && *dep;  // a null predecessor node means: no dependency
+    return cudaGraphAddKernelNode(node, g, has_dep ? dep : nullptr, has_dep ? 1 : 0, &kp);
+}
+
+// The V-cycle z = M r as a chain of kernel nodes after *prev.
+struct VcycleArgs {
+    std::vector<std::vector<void*>> args;
+    std::vector<EllRows> ell;
+    std::vector<CsrRows> csr;
+    std::vector<int> ns;
+    std::vector<const double*> bs;
+    std::vector<double*> outs;
+    std::vector<double*> xcs;
+};
+
+cudaError_t add_vcycle(AmgCache* c, cudaGraph_t g, cudaGraphNode_t* prev, const double* r_in, double* z_out,
+                       VcycleArgs& va) {
+    const size_t L = c->lv.size();
+    va.ell.assign(1, EllRows{c->ls->mesh->v, c->ls->values});
+    va.csr.resize(L);
+    for (size_t l = 1; l < L; ++l) va.csr[l] = CsrRows{c->lv[l].rp, c->lv[l].ci, c->lv[l].val};
+    va.ns.resize(L);
+    va.bs.resize(L);
+    va.outs.resize(L);
+    va.xcs.resize(L);
+    va.args.clear();
+    va.args.reserve(4 * L + 4);
+    for (size_t l = 0; l < L; ++l) {
+        va.ns[l] = c->lv[l].n;
+        va.bs[l] = l == 0 ? r_in : c->lv[l].b;
+        va.outs[l] = l == 0 ? z_out : c->lv[l].xo;
+    }
+    cudaError_t e = cudaSuccess;
+    cudaGraphNode_t node;
+    // down
+    for (size_t l = 0; l + 1 < L && e == cudaSuccess; ++l) {
+        Level& F = c->lv[l];
+        if (l == 0) {
+            va.args.push_back({&c->st, &va.ell[0], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &F.r});
+            e = add_kernel(g, &node, prev, (void*)k_pre<EllRows>, grid_for(F.n, kT), kT, va.args.back().data());
+        } else {
+            va.args.push_back({&c->st, &va.csr[l], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &F.r});
+            e = add_kernel(g, &node, prev, (void*)k_pre<CsrRows>, grid_for(F.n, kT), kT, va.args.back().data());
+        }
+        *prev = node;
+        if (e != cudaSuccess) break;
+        va.args.push_back({&c->st, &va.ns[l + 1], &F.mptr, &F.mem, &F.r, &c->lv[l + 1].b});
+        e = add_kernel(g, &node, prev, (void*)k_restrict, grid_for(va.ns[l + 1], kT), kT, va.args.back().data());
+        *prev = node;
+    }
+    // coarsest
+    if (e == cudaSuccess) {
+        Level& B = c->lv[L - 1];
+        va.args.push_back({&c->st, &va.ns[L - 1], &c->ainv, &B.b, &B.xo});
+        e = add_kernel(g, &node, prev, (void*)k_coarse, grid_for(B.n, kT / 32), kT, va.args.back().data());
+        *prev = node;
+    }
+    // up
+    for (size_t l = L - 1; l-- > 0 && e == cudaSuccess;) {
+        Level& F = c->lv[l];
+        va.xcs[l] = c->lv[l + 1].xo;
+        if (l == 0) {
+            va.args.push_back({&c->st, &va.ell[0], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &va.xcs[l], &F.agg, &va.outs[l]});
+            e = add_kernel(g, &node, prev, (void*)k_post<EllRows>, grid_for(F.n, kT), kT, va.args.back().data());
+        } else {
+            va.args.push_back({&c->st, &va.csr[l], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &va.xcs[l], &F.agg, &va.outs[l]});
+            e = add_kernel(g, &node, prev, (void*)k_post<CsrRows>, grid_for(F.n, kT), kT, va.args.back().data());
+        }
+        *prev = node;
+    }
+    return e;
+}
+
+fvgb_status build_graph(AmgCache* c) {
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    const fvgb_ls* ls = c->ls;
+    EllRows A{ls->mesh->v, ls->values};
+    int n = ls->mesh->v.n;
+    const unsigned nb = (unsigned)c->nblk;
+    const double* b = ls->rhs;
+    cudaGraph_t g = nullptr;
+    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    cudaGraphNode_t prev = nullptr, node;
+    VcycleArgs v0, v1;
+    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part};
+    void* a_first[] = {&c->st, &n, &c->r, &c->z, &c->p, &c->part};
+    void* a_cond[] = {&c->st, &h};
+    void* a_spmv[] = {&c->st, &A, &n, &c->p, &c->q, &c->part};
+    void* a_upd[] = {&c->st, &n, &c->p, &c->q, &c->r, &c->part};
+    void* a_rz[] = {&c->st, &n, &c->r, &c->z, &c->part};
+    void* a_dir[] = {&c->st, &n, &c->z, &c->p};
+    void* a_stats[] = {&c->st};
+    if (e == cudaSuccess) e = add_kernel(g, &node, nullptr, (void*)k_init, nb, kT, a_init);
+    prev = node;
+    if (e == cudaSuccess) e = add_vcycle(c, g, &prev, c->r, c->z, v0);
+    if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_first_dir, nb, kT, a_first);
+    prev = node;
+    if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_cond, 1, 1, a_cond);
+    prev = node;
+    cudaGraph_t body = nullptr;
+    if (e == cudaSuccess) {
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        e = cudaGraphAddNode(&node, g, &prev, nullptr, 1, &np);
+        if (e == cudaSuccess) body = np.conditional.phGraph_out[0];
+        prev = node;
+    }
+    cudaGraphNode_t bprev = nullptr, bnode;
+    if (e == cudaSuccess) e = add_kernel(body, &bnode, nullptr, (void*)k_spmv, nb, kT, a_spmv);
+    bprev = bnode;
+    if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_update, nb, kT, a_upd);
+    bprev = bnode;
+    if (e == cudaSuccess) e = add_vcycle(c, body, &bprev, c->r, c->z, v1);
+    if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_rz, nb, kT, a_rz);
+    bprev = bnode;
+    if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_dir, nb, kT, a_dir);
+    bprev = bnode;
+    if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_cond, 1, 1, a_cond);
+    if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_stats, 1, 1, a_stats);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "multigrid CG graph");
+    return FVGB_OK;
+}
+
+fvgb_status prepare(fvgb_ls* ls, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    FVGB_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
+    if (!ls->amg) {
+        if (cs != cudaStreamCaptureStatusNone)
+            return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: the first solve (setup) cannot be stream-captured");
+        AmgCache* c = new AmgCache();
+        c->ls = ls;
+        fvgb_status st = symbolic(c, s);
+        if (st == FVGB_OK) st = build_graph(c);
+        if (st != FVGB_OK) {
+            fvgb_amg_free(c);
+            return st;
+        }
+        ls->amg = c;
+    }
+    AmgCache* c = ls->amg;
+    if (c->version != ls->version) return numeric(c, s);
+    return FVGB_OK;
+}
+
+}  // namespace
+
+void fvgb_amg_free(AmgCache* c) {
+    if (!c) return;
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    for (void* p : c->allocs) cudaFree(p);
+    delete c;
+}
+
+fvgb_status fvgb_amg_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev,
+                                 cudaStream_t s) {
+    if (ls->ncomp != 1) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_solve: scalar systems only");
+    if (cfg->precision != FVGB_PREC_FP64 || cfg->method != FVGB_SOLVER_CG)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: FP64 CG only");
+    fvgb_status st = prepare(ls, s);
+    if (st != FVGB_OK) return st;
+    AmgCache* c = ls->amg;
+    k_params<<<1, 1, 0, s>>>(c->st, x, cfg->rel_tol, cfg->abs_tol, cfg->max_iter, stats_dev);
+    FVGB_LAUNCH_CHECK("multigrid params");
+    FVGB_CUDA_TRY(cudaGraphLaunch(c->graph, s));
+    return FVGB_OK;
+}
+
+fvgb_status fvgb_amg_sync_stats(fvgb_ls* ls, fvgb_solver_stats* out, cudaStream_t s) {
+    AmgCache* c = ls->amg;
+    fvgb_solver_stats h{};
+    FVGB_CUDA_TRY(cudaMemcpyAsync(&h, &c->st->stats, sizeof h, cudaMemcpyDeviceToHost, s));
+    FVGB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (out) *out = h;
+    return (fvgb_status)(h.status == FVGB_ERR_NOT_CONVERGED ? FVGB_ERR_NOT_CONVERGED
+                                                             : (h.status == FVGB_OK ? FVGB_OK : h.status));
+}
+
+extern "C" fvgb_status fvgb_amg_apply(fvgb_ls* ls, const double* r, double* z, fvgb_stream stream) {
+    FVGB_CHECK_ARG(ls && r && z, "fvgb_amg_apply: null argument");
+    FVGB_CHECK_ARG(ls->ncomp == 1, "fvgb_amg_apply: scalar systems only");
+    cudaStream_t s = (cudaStream_t)stream;
+    fvgb_status st = prepare(ls, s);
+    if (st != FVGB_OK) return st;
+    AmgCache* c = ls->amg;
+    // a one-off graph of the V-cycle alone, with the done flag cleared
+    k_params<<<1, 1, 0, s>>>(c->st, nullptr, 0.0, 0.0, 0, nullptr);
+    cudaGraph_t g = nullptr;
+    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t prev = nullptr;
+    VcycleArgs va;
+    cudaError_t e = add_vcycle(c, g, &prev, r, z, va);
+    cudaGraphExec_t ge = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+    if (e == cudaSuccess) e = cudaGraphLaunch(ge, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (ge) cudaGraphExecDestroy(ge);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "fvgb_amg_apply");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_amg_info(fvgb_ls* ls, int32_t* nlevels, int32_t* rows, int64_t* nnz, int32_t cap) {
+    FVGB_CHECK_ARG(ls && nlevels, "fvgb_amg_info: null argument");
+    if (!ls->amg) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_amg_info: no multigrid hierarchy yet (solve first)");
+    const AmgCache* c = ls->amg;
+    *nlevels = (int32_t)c->lv.size();
+    for (int32_t l = 0; l < *nlevels && l < cap; ++l) {
+        if (rows) rows[l] = c->lv[l].n;
+        if (nnz) nnz[l] = c->lv[l].nnz;
+    }
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_pgm_aggregate(int32_t n, const int32_t* row_offs, const int32_t* cols,
+                                          const double* values, int32_t* agg, int32_t* n_coarse) {
+    FVGB_CHECK_ARG(n >= 0 && row_offs && cols && values && agg && n_coarse, "fvgb_pgm_aggregate: null argument");
+    std::vector<int> a;
+    *n_coarse = pgm_aggregate(n, row_offs, cols, values, a);
+    std::memcpy(agg, a.data(), sizeof(int32_t) * (size_t)n);
+    return FVGB_OK;
+}

@@ -302,6 +302,7 @@ extern "C" fvgb_status fvgb_ls_destroy(fvgb_ls* ls) {
     if (!ls) return FVGB_OK;
     cudaDeviceSynchronize();
     if (ls->solver) fvgb_solver_cache_free(ls->solver);
+    if (ls->amg) fvgb_amg_free(ls->amg);
     cudaFree(ls->values);
     cudaFree(ls->rhs);
     cudaFree(ls->bmat);

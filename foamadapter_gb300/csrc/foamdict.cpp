@@ -765,11 +765,16 @@ extern "C" fvgb_status fvgb_solver_cfg_from_dict(const fvgb_dict* d, fvgb_solver
     else if (w == "solver::Bicgstab") c.method = FVGB_SOLVER_BICGSTAB;
     else return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("solver entry: " + w + " is not implemented (Cg, Bicgstab are)").c_str());
     const fvgb_dict::Entry* pe = entry_of(d, "preconditioner");
-    if (!pe || !pe->sub) return fvgb_fail(FVGB_ERR_UNSUPPORTED, "solver entry: only preconditioner::Jacobi with max_block_size 1 is implemented");
+    const char* kPrecMsg =
+        "solver entry: preconditioner::Jacobi with max_block_size 1 and solver::Multigrid (with CG) are implemented";
+    if (!pe || !pe->sub) return fvgb_fail(FVGB_ERR_UNSUPPORTED, kPrecMsg);
     double mbs = 0.0;
-    if (!word_of(pe->sub.get(), "type", w) || w != "preconditioner::Jacobi" ||
-        !number_of(pe->sub.get(), "max_block_size", mbs) || mbs != 1.0)
-        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "solver entry: only preconditioner::Jacobi with max_block_size 1 is implemented");
+    if (word_of(pe->sub.get(), "type", w) && w == "solver::Multigrid" && c.method == FVGB_SOLVER_CG) {
+        c.preconditioner = FVGB_PRECOND_MULTIGRID;
+    } else if (!word_of(pe->sub.get(), "type", w) || w != "preconditioner::Jacobi" ||
+               !number_of(pe->sub.get(), "max_block_size", mbs) || mbs != 1.0) {
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, kPrecMsg);
+    }
     const fvgb_dict::Entry* ce = entry_of(d, "criteria");
     if (ce && ce->sub) {
         double v = 0.0;

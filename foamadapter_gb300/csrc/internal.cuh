@@ -76,6 +76,7 @@ struct fvgb_mesh {
 };
 
 struct SolverCache;  // solver.cu
+struct AmgCache;     // amg.cu
 
 struct fvgb_ls {
     const fvgb_mesh* mesh = nullptr;
@@ -85,8 +86,15 @@ struct fvgb_ls {
     double* bmat = nullptr;    // [nbf]
     double* brhs = nullptr;    // [nbf*ncomp]
     SolverCache* solver = nullptr;
+    AmgCache* amg = nullptr;   // multigrid hierarchy (amg.cu), built at the first multigrid solve
     uint64_t version = 1;      // bumped whenever `values` change (assembly, SetReference)
 };
+
+// amg.cu: multigrid-preconditioned CG (cfg->preconditioner == FVGB_PRECOND_MULTIGRID)
+void fvgb_amg_free(AmgCache* c);
+fvgb_status fvgb_amg_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev,
+                                 cudaStream_t s);
+fvgb_status fvgb_amg_sync_stats(fvgb_ls* ls, fvgb_solver_stats* out, cudaStream_t s);
 
 // Per-call patch table passed to kernels by value.
 struct PatchTable {

@@ -2843,6 +2843,10 @@ extern "C" fvgb_status fvgb_solve_async(fvgb_ls* ls, double* x, const fvgb_solve
                                         fvgb_solver_stats* stats_dev, fvgb_stream stream) {
     FVGB_CHECK_ARG(ls && x && cfg, "fvgb_solve: null argument");
     FVGB_CHECK_ARG(ls->ncomp == 1, "fvgb_solve: scalar systems only");
+    FVGB_CHECK_ARG(cfg->preconditioner == FVGB_PRECOND_JACOBI || cfg->preconditioner == FVGB_PRECOND_MULTIGRID,
+                   "fvgb_solve: unknown preconditioner");
+    if (cfg->preconditioner == FVGB_PRECOND_MULTIGRID)
+        return fvgb_amg_solve_async(ls, x, cfg, stats_dev, (cudaStream_t)stream);
     SolverCache* c = nullptr;
     fvgb_status st = single_cache(ls, &c);
     if (st != FVGB_OK) return st;
@@ -2853,6 +2857,7 @@ extern "C" fvgb_status fvgb_solve(fvgb_ls* ls, double* x, const fvgb_solver_cfg*
                                   fvgb_stream stream) {
     fvgb_status st = fvgb_solve_async(ls, x, cfg, nullptr, stream);
     if (st != FVGB_OK) return st;
+    if (cfg->preconditioner == FVGB_PRECOND_MULTIGRID) return fvgb_amg_sync_stats(ls, stats, (cudaStream_t)stream);
     return sync_stats(ls->solver, stats, (cudaStream_t)stream);
 }
 

@@ -223,7 +223,7 @@ def solver_config(mapped: Dictionary) -> dict:
     abi.check(abi.lib().fvgb_solver_cfg_from_dict(mapped.handle, C.byref(cfg)))
     return dict(rel_tol=cfg.rel_tol, abs_tol=cfg.abs_tol, max_iter=cfg.max_iter, precision=cfg.precision,
                 inner_rel_tol=cfg.inner_rel_tol, inner_max_iter=cfg.inner_max_iter, max_outer=cfg.max_outer,
-                method=cfg.method)
+                method=cfg.method, preconditioner=cfg.preconditioner)
 
 
 def scheme(fv_schemes: Dictionary, section: str, name: str) -> int:

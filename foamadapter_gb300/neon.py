@@ -310,13 +310,15 @@ class LinearSystem:
 
     def solve(self, x: torch.Tensor, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=abi.PREC_FP64,
               inner_rel_tol=None, inner_max_iter=1000, max_outer=50, allow=(abi.ERR_NOT_CONVERGED,), kernel_mode=0,
-              method=abi.SOLVER_CG, flags=0):
+              method=abi.SOLVER_CG, flags=0, preconditioner=abi.PRECOND_JACOBI):
         """inner_rel_tol (mixed precision) defaults to 0.1 for CG and 0.01 for the
-        restarted inner BiCGStab, the fastest settings measured on 128^3 systems."""
+        restarted inner BiCGStab, the fastest settings measured on 128^3 systems.
+        preconditioner=abi.PRECOND_MULTIGRID: FP64 CG with the aggregation
+        multigrid V-cycle (single systems)."""
         if inner_rel_tol is None:
             inner_rel_tol = 0.01 if method == abi.SOLVER_BICGSTAB else 0.1
         cfg = abi.SolverCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer,
-                            kernel_mode, flags, method)
+                            kernel_mode, flags, method, preconditioner)
         st = abi.SolverStats()
         abi.check(abi.lib().fvgb_solve(self.handle, abi.ptr(x), C.byref(cfg), C.byref(st), _stream()),
                   allow=allow)

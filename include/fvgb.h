@@ -301,9 +301,15 @@ typedef struct fvgb_solver_cfg {
                                   (Ginkgo Bicgstab, fvSolution.cpp:25-26: nonsymmetric
                                   systems; graph path; MIXED_IR: FP32 inner BiCGStab,
                                   restarted every refinement step)                       */
+    int32_t preconditioner;    /* FVGB_PRECOND_JACOBI (Ginkgo Jacobi, block size 1) or
+                                  FVGB_PRECOND_MULTIGRID (Ginkgo Multigrid with PGM
+                                  aggregation as tutorials/cylinder2D/system/gko/
+                                  config.mg.json selects it; FP64 CG, single systems,
+                                  fvgb_solve / fvgb_solve_async only)                    */
 } fvgb_solver_cfg;
 enum { FVGB_SOLVE_NO_TUNE = 1 };
 enum { FVGB_SOLVER_CG = 0, FVGB_SOLVER_BICGSTAB = 1 };
+enum { FVGB_PRECOND_JACOBI = 0, FVGB_PRECOND_MULTIGRID = 1 };
 
 /* SolverStats {initResNorm, finalResNorm, numIter} (expression.hpp:155-158). */
 typedef struct fvgb_solver_stats {
@@ -373,6 +379,24 @@ fvgb_status fvgb_solve_tuning(fvgb_ls* ls, const int32_t* force, int32_t* chosen
  * [spmv + p.Ap, x/r update + r.z, direction update, init].  Synchronous. */
 fvgb_status fvgb_solve_kernel_times(fvgb_ls* ls, const double* x0, int32_t iters, double* ms_out,
                                     fvgb_stream stream);
+
+/* Multigrid (cfg->preconditioner = FVGB_PRECOND_MULTIGRID): the hierarchy is
+ * built at the first such solve of a system (PGM aggregation and Galerkin
+ * pattern on the host from that matrix; it synchronises the stream and cannot
+ * be stream-captured), and its values are recomputed on the device whenever
+ * the matrix changed.  fvgb_amg_apply: z = M r, one V-cycle of the current
+ * matrix (synchronous; a measurement and test aid).  fvgb_amg_info: number of
+ * levels and rows / nonzeros per level (cap entries of each). */
+fvgb_status fvgb_amg_apply(fvgb_ls* ls, const double* r, double* z, fvgb_stream stream);
+fvgb_status fvgb_amg_info(fvgb_ls* ls, int32_t* nlevels, int32_t* rows, int64_t* nnz, int32_t cap);
+/* The aggregation step of the multigrid setup on a HOST CSR matrix: agg[n]
+ * receives the aggregate of every row, *n_coarse their number.  Strength
+ * |a_ij|; up to 15 rounds of mutual strongest-neighbour pairing (ties: lower
+ * index) until at most 5% of the rows are left; left-over rows join their
+ * strongest aggregated neighbour or stay alone; aggregates are numbered by
+ * their lowest row. */
+fvgb_status fvgb_pgm_aggregate(int32_t n, const int32_t* row_offs, const int32_t* cols, const double* values,
+                               int32_t* agg, int32_t* n_coarse);
 
 /* FP64 Jacobi-CG that allocates nothing.  No counterpart in the reference: it
  * exists for callers that cannot call cudaMalloc (a solver embedded in a host
@@ -654,7 +678,9 @@ fvgb_status fvgb_fvsolution_update_criteria(fvgb_dict* solver_dict);
 fvgb_status fvgb_fvsolution_map(const fvgb_dict* solver_dict, fvgb_dict** mapped);
 /* A mapped (Ginkgo-form) solver entry as a solver configuration: type
  * solver::Cg or solver::Bicgstab, preconditioner::Jacobi with max_block_size
- * 1, criteria iteration / relative_residual_norm / absolute_residual_norm.
+ * 1 (or, with solver::Cg, a preconditioner dictionary of type
+ * solver::Multigrid), criteria iteration / relative_residual_norm /
+ * absolute_residual_norm.
  * This library's own keywords: precision FP64|mixed, innerRelTol,
  * innerMaxIter, maxOuter.  Other solvers and preconditioners (Bicg,
  * Multigrid, Ilu, none, block Jacobi) and configFile: FVGB_ERR_UNSUPPORTED. */
