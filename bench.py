@@ -264,6 +264,34 @@ def compare_precisions(torch, abi, L, ls, T, T_old, tarr, bc, dm, hm, stream):
         abi.check(L.fvgb_apply_operator(ls.handle, abi.ptr(x), abi.ptr(r), stream))
         out[name] = {"ms": best, "iters": st.num_iter, "outer": st.num_outer,
                      "rel_residual": float(torch.linalg.vector_norm(r).item() / st.init_res_norm)}
+    # FP64 CG with the multigrid preconditioner (Ginkgo Multigrid + PGM as the
+    # reference's cylinder2D configuration selects it): first solve with the
+    # setup, then best of 3 with the hierarchy cached, then after a
+    # re-assembly (coarse values recomputed on the device)
+    cfg = abi.SolverCfg(HEAT["rel_tol"], 0.0, 4000, abi.PREC_FP64, 0.0, 0, 0, 0, 0, abi.SOLVER_CG,
+                        abi.PRECOND_MULTIGRID)
+    times = []
+    for rep in range(5):
+        if rep == 4:
+            abi.check(L.fvgb_assemble(ls.handle, tarr, 2, HEAT["dt"], C.byref(bc), abi.ptr(T.boundary), stream))
+        x = T_old.clone()
+        st = abi.SolverStats()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        abi.check(L.fvgb_solve(ls.handle, abi.ptr(x), C.byref(cfg), C.byref(st), stream))
+        torch.cuda.synchronize()
+        times.append(1e3 * (time.perf_counter() - t0))
+    r = torch.empty_like(x)
+    abi.check(L.fvgb_apply_operator(ls.handle, abi.ptr(x), abi.ptr(r), stream))
+    nl = C.c_int32()
+    rows = (C.c_int32 * 32)()
+    abi.check(L.fvgb_amg_info(ls.handle, C.byref(nl), rows, None, 32))
+    out["fp64_multigrid"] = {"ms": min(times[1:4]), "first_solve_ms_with_setup": times[0],
+                             "solve_after_reassembly_ms": times[4], "iters": st.num_iter,
+                             "levels": [int(rows[i]) for i in range(nl.value)],
+                             "rel_residual": float(torch.linalg.vector_norm(r).item() / st.init_res_norm),
+                             "max_abs_err_vs_fp64": float((x - sols["fp64"]).abs().max().item()),
+                             "speedup_vs_fp64_jacobi": out["fp64"]["ms"] / min(times[1:4])}
     d = (sols["mixed"] - sols["fp64"]).abs()
     out["speedup"] = out["fp64"]["ms"] / out["mixed"]["ms"]
     out["max_abs_err_vs_fp64"] = float(d.max().item())
@@ -524,11 +552,12 @@ def run_cavity(args):
     nsteps = args.cavity_steps
     out = {}
     fields = {}
-    for name, prec in (("fp64", abi.PREC_FP64), ("mixed", abi.PREC_MIXED_IR)):
-        case = apps.CavityPiso(n=512, precision=prec)
+    for name, prec, pc in (("fp64", abi.PREC_FP64, abi.PRECOND_JACOBI), ("mixed", abi.PREC_MIXED_IR, abi.PRECOND_JACOBI),
+                           ("fp64_multigrid", abi.PREC_FP64, abi.PRECOND_MULTIGRID)):
+        case = apps.CavityPiso(n=512, precision=prec, preconditioner=pc)
         case.step()                                     # warm-up (builds the solver graphs)
         torch.cuda.synchronize()
-        case = apps.CavityPiso(n=512, precision=prec)
+        case = apps.CavityPiso(n=512, precision=prec, preconditioner=pc)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(nsteps):
@@ -541,13 +570,69 @@ def run_cavity(args):
                      "all_solves_ok": all(s[4] == abi.OK for s in case.stats),
                      "max_final_rel_residual": max(s[3] / s[2] if s[2] > 0 else 0.0 for s in case.stats)}
         fields[name] = (case.p.host(), case.U.host())
-    (p64, U64), (pm, Um) = fields["fp64"], fields["mixed"]
+    (p64, U64), (pm, Um), (pg, Ug) = fields["fp64"], fields["mixed"], fields["fp64_multigrid"]
+
+    def err(p, U):
+        return {"p_max": float(np.abs(p - p64).max()),
+                "p_l2_rel": float(np.linalg.norm(p - p64) / max(np.linalg.norm(p64), 1e-300)),
+                "U_max": float(np.abs(U - U64).max()),
+                "U_l2_rel": float(np.linalg.norm(U - U64) / max(np.linalg.norm(U64), 1e-300))}
+
     out["speedup_step"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
-    out["err_vs_fp64"] = {"p_max": float(np.abs(pm - p64).max()), "p_l2_rel": float(np.linalg.norm(pm - p64) / max(
-        np.linalg.norm(p64), 1e-300)), "U_max": float(np.abs(Um - U64).max()),
-        "U_l2_rel": float(np.linalg.norm(Um - U64) / max(np.linalg.norm(U64), 1e-300))}
+    out["err_vs_fp64"] = err(pm, Um)
+    out["speedup_step_multigrid"] = out["fp64"]["ms_per_step"] / out["fp64_multigrid"]["ms_per_step"]
+    out["err_vs_fp64_multigrid"] = err(pg, Ug)
     return {"workload": f"lid-driven cavity PISO 512x512x1, +-5% jitter, dt 5e-4, 2 correctors, {nsteps} steps",
             "pressure_solve_to": "1e-8 relative FP64 residual", **out}
+
+
+def run_multigrid(args):
+    """The multigrid preconditioner on the 128^3 heat system: the hierarchy,
+    one V-cycle (fvgb_amg_apply, a plain graph whose kernels ncu can capture
+    one by one) and the whole CG solve against the Jacobi-PCG."""
+    import torch
+
+    from foamadapter_gb300 import abi, neon
+    from foamadapter_gb300.mesh import DeviceMesh
+
+    hm, k = heat_inputs(args.n)
+    dm = DeviceMesh(hm)
+    bcs = [("fixedValue", HEAT["Twall"])] + [("zeroGradient", 0.0)] * (hm.npatch - 1)
+    T = neon.VolumeField(dm, np.full(hm.n, HEAT["T0"]), bcs)
+    kf = neon.VolumeField(dm, k, [("zeroGradient", 0.0)] * hm.npatch)
+    gamma = neon.SurfaceInterpolation(dm, "linear").interpolate(kf)
+    ls = neon.LinearSystem(dm)
+    ls.assemble([neon.ddt(T.internal.clone()), neon.laplacian(gamma, -1.0)], HEAT["dt"], T)
+    L = abi.lib()
+    x0 = T.internal.clone()
+    out = {}
+    # --profile: the V-cycles only (no conditional graphs, so ncu can capture every kernel)
+    for name, pc in () if args.profile else (("jacobi", abi.PRECOND_JACOBI), ("multigrid", abi.PRECOND_MULTIGRID)):
+        times = []
+        for rep in range(4):
+            x = x0.clone()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = ls.solve(x, rel_tol=HEAT["rel_tol"], max_iter=4000, preconditioner=pc)
+            torch.cuda.synchronize()
+            times.append(1e3 * (time.perf_counter() - t0))
+        out[name] = {"ms": min(times[1:]), "first_ms": times[0], "iters": st.num_iter}
+    r = torch.randn(hm.n, dtype=torch.float64, device="cuda")
+    z = torch.zeros_like(r)
+    reps = args.explicit_reps
+    for _ in range(2):
+        abi.check(L.fvgb_amg_apply(ls.handle, abi.ptr(r), abi.ptr(z), None))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        abi.check(L.fvgb_amg_apply(ls.handle, abi.ptr(r), abi.ptr(z), None))
+    vms = 1e3 * (time.perf_counter() - t0) / max(1, reps)
+    nl = C.c_int32()
+    rows, nnz = (C.c_int32 * 32)(), (C.c_int64 * 32)()
+    abi.check(L.fvgb_amg_info(ls.handle, C.byref(nl), rows, nnz, 32))
+    return {"workload": f"multigrid-preconditioned CG on the {args.n}^3 heat system, to 1e-8",
+            "levels": [[int(rows[i]), int(nnz[i])] for i in range(nl.value)],
+            "vcycle_ms_incl_graph_build": vms, **out,
+            "speedup_solve": out["jacobi"]["ms"] / out["multigrid"]["ms"] if out else None}
 
 
 def batch_cases(ncases, seed=4):
@@ -792,7 +877,7 @@ def main():
     ap.add_argument("--ref-max-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity", "batch", "serve", "explicit",
-                                                           "convection"])
+                                                           "convection", "multigrid"])
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--seq-requests", type=int, default=400)
     ap.add_argument("--serve-streams", type=int, default=64)
@@ -826,7 +911,7 @@ def main():
         torch.distributed.barrier()
     if args.workload != "heat":
         fn = {"advection": run_advection, "cavity": run_cavity, "batch": run_batch, "serve": run_serve,
-              "explicit": run_explicit, "convection": run_convection}[args.workload]
+              "explicit": run_explicit, "convection": run_convection, "multigrid": run_multigrid}[args.workload]
         if rank == 0:
             print(json.dumps(fn(args)))
         return

@@ -65,12 +65,13 @@ class CavityPiso:
 
     def __init__(self, n=512, jitter=0.05, seed=12345, nu=0.01, dt=5e-4, n_corr=2, lid=(1.0, 0.0, 0.0),
                  precision=abi.PREC_FP64, p_rel_tol=1e-8, p_max_iter=20000, inner_rel_tol=0.1,
-                 ddt_corr=False, corrected=False, n_non_orth=0):
+                 ddt_corr=False, corrected=False, n_non_orth=0, preconditioner=abi.PRECOND_JACOBI):
         self.hm = hm = mesh.box(n, n, 1, 1.0, 1.0, 1.0 / n, jitter=jitter, seed=seed, two_d=True)
         self.dm = dm = DeviceMesh(hm)
         self.dt, self.n_corr = dt, n_corr
         self.ddt_corr, self.corrected, self.n_non_orth = ddt_corr, corrected, n_non_orth
-        self.cfg = abi.SolverCfg(p_rel_tol, 0.0, p_max_iter, precision, inner_rel_tol, 2000, 50)
+        self.cfg = abi.SolverCfg(p_rel_tol, 0.0, p_max_iter, precision, inner_rel_tol, 2000, 50, 0, 0,
+                                 abi.SOLVER_CG, preconditioner)
         ubcs = [("noSlip", 0.0), ("noSlip", 0.0), ("noSlip", 0.0), ("fixedValue", list(lid))]
         self.U = neon.VolumeField(dm, np.zeros(3 * hm.n), ubcs, ncomp=3, name="U")
         self.p = neon.VolumeField(dm, np.zeros(hm.n), [("zeroGradient", 0.0)] * 4, name="p")

@@ -13,7 +13,10 @@
 //    neighbour (ties: the lower index) and mutual picks become pairs; the
 //    rounds stop when at most 5% of the rows are left or no pair forms.  A row
 //    left over joins the aggregate of its strongest aggregated neighbour, or
-//    stays alone.  Aggregates are numbered by their lowest row.
+//    stays alone.  Aggregates are numbered by their lowest row.  Each level
+//    applies it twice (double pairwise aggregation, as in Notay's AGMG): the
+//    pairs are matched again on their Galerkin matrix, so a level keeps about
+//    a quarter of the rows and the hierarchy has half as many levels.
 //  * Galerkin coarse matrix A_c = P^T A P for the piecewise-constant P: its
 //    pattern and, for each coarse entry, the fine entries it sums (fine rows
 //    ascending, entries in row order).  Levels are added until at most
@@ -50,6 +53,7 @@ constexpr int kMaxLevels = 25;
 constexpr double kOmega = 0.9;
 constexpr int kPgmRounds = 15;
 constexpr double kPgmLeftRatio = 0.05;
+constexpr int kTailRows = 0;  // levels this small run in the single-block tail (0: the coarsest only)
 
 struct HostCsr {
     int n = 0;
@@ -177,16 +181,21 @@ struct AmgState {
     fvgb_solver_stats stats;
 };
 
+// Levels >= 1 are stored sliced ELL like the system matrix (32-row slices,
+// column-major inside a slice, padding slots: column = row, value 0).
 struct Level {
     int n = 0, nnz = 0;
-    int *rp = nullptr, *ci = nullptr, *dpos = nullptr;  // levels >= 1 (level 0: the mesh's sliced ELL)
+    int *sptr = nullptr, *scol = nullptr, *dpos = nullptr;  // levels >= 1 (level 0: the mesh's sliced ELL)
     double *val = nullptr, *dinv = nullptr;
     int* agg = nullptr;                    // [n], when a coarser level follows
     int *mptr = nullptr, *mem = nullptr;   // members of the next level's rows
     int *gptr = nullptr, *gsrc = nullptr;  // sums forming the next level's values
+    int* gdst = nullptr;                   // the next level's slot of each sum
     int nnz_next = 0;
     double *b = nullptr, *x = nullptr, *xo = nullptr, *r = nullptr;
 };
+
+struct TailLevel;
 
 }  // namespace
 
@@ -198,6 +207,8 @@ struct AmgCache {
     double* ainv = nullptr;  // [nc*nc] inverse of the coarsest matrix
     double *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *part = nullptr;
     AmgState* st = nullptr;
+    int tail_from = 1;             // first level run by the single-block tail
+    TailLevel* tail = nullptr;     // device descriptors of levels tail_from..L-1
     cudaGraphExec_t graph = nullptr;
     std::vector<void*> allocs;
     int nblk = 0;
@@ -220,6 +231,8 @@ cudaError_t upload(AmgCache* c, T** p, const std::vector<T>& h) {
 }
 
 // ------------------------------------------------------------ row access
+// Row i of a sliced-ELL matrix: f(column, value) for every slot, the column
+// and value loads of the first 8 slots issued before the caller's gathers.
 struct EllRows {  // level 0: the system's sliced-ELL matrix
     MeshView m;
     const double* val;
@@ -229,20 +242,50 @@ struct EllRows {  // level 0: the system's sliced-ELL matrix
         const int b0 = __ldg(&m.m_ptr[slice]);
         const int base = b0 + (i & 31);
         const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
-        for (int k = 0; k < w; ++k) {
-            const int pos = base + k * 32;
-            f(slot_col(m, pos, i), __ldg(&val[pos]));
+        int col[8];
+        double a[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            col[k] = i;
+            a[k] = 0.0;
+            if (k < w) {
+                col[k] = slot_col(m, base + k * 32, i);
+                a[k] = __ldg(&val[base + k * 32]);
+            }
         }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (k < w) f(col[k], a[k]);
+        for (int k = 8; k < w; ++k) f(slot_col(m, base + k * 32, i), __ldg(&val[base + k * 32]));
     }
 };
 
-struct CsrRows {
-    const int* rp;
-    const int* ci;
+struct SellRows {  // levels >= 1
+    const int* ptr;
+    const int* col;
     const double* val;
     template <class F>
     __device__ __forceinline__ void each(int i, F f) const {
-        for (int k = __ldg(&rp[i]); k < __ldg(&rp[i + 1]); ++k) f(__ldg(&ci[k]), __ldg(&val[k]));
+        const int slice = i >> 5;
+        const int b0 = __ldg(&ptr[slice]);
+        const int base = b0 + (i & 31);
+        const int w = (__ldg(&ptr[slice + 1]) - b0) >> 5;
+        constexpr int P = 16;  // coarse rows hold up to ~20 entries
+        int c[P];
+        double a[P];
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            c[k] = i;
+            a[k] = 0.0;
+            if (k < w) {
+                c[k] = __ldg(&col[base + k * 32]);
+                a[k] = __ldg(&val[base + k * 32]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < P; ++k)
+            if (k < w) f(c[k], a[k]);
+        for (int k = P; k < w; ++k) f(__ldg(&col[base + k * 32]), __ldg(&val[base + k * 32]));
     }
 };
 
@@ -287,13 +330,13 @@ __global__ void __launch_bounds__(kT) k_dinv_ell(MeshView m, const double* __res
 }
 
 __global__ void __launch_bounds__(kT)
-    k_galerkin(int nnz_c, const int* __restrict__ gptr, const int* __restrict__ gsrc, const double* __restrict__ vf,
-               double* __restrict__ vc) {
+    k_galerkin(int nnz_c, const int* __restrict__ gptr, const int* __restrict__ gsrc, const int* __restrict__ gdst,
+               const double* __restrict__ vf, double* __restrict__ vc) {
     const int k = blockIdx.x * kT + threadIdx.x;
     if (k >= nnz_c) return;
     double s = 0.0;
     for (int t = __ldg(&gptr[k]); t < __ldg(&gptr[k + 1]); ++t) s += __ldg(&vf[__ldg(&gsrc[t])]);
-    vc[k] = s;
+    vc[__ldg(&gdst[k])] = s;
 }
 
 __global__ void __launch_bounds__(kT)
@@ -302,14 +345,12 @@ __global__ void __launch_bounds__(kT)
     if (i < n) dinv[i] = 1.0 / __ldg(&val[__ldg(&dpos[i])]);
 }
 
-__global__ void __launch_bounds__(kT)
-    k_dense(int n, const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ val,
-            double* __restrict__ a) {
+// dense copy of the coarsest level (padding slots add 0 to the diagonal)
+__global__ void __launch_bounds__(kT) k_dense(int n, SellRows rows, double* __restrict__ a) {
     const int i = blockIdx.x;
     for (int j = threadIdx.x; j < n; j += kT) a[(size_t)i * n + j] = 0.0;
     __syncthreads();
-    if (threadIdx.x == 0)
-        for (int k = rp[i]; k < rp[i + 1]; ++k) a[(size_t)i * n + ci[k]] = val[k];
+    if (threadIdx.x == 0) rows.each(i, [&](int j, double v) { a[(size_t)i * n + j] += v; });
 }
 
 // In-place Gauss-Jordan inverse of an n x n SPD matrix, one block of 1024 threads.
@@ -334,59 +375,124 @@ __global__ void __launch_bounds__(1024) k_gauss_jordan(int n, double* __restrict
 }
 
 // ------------------------------------------------------------ V-cycle
-// x = w D^-1 b (one sweep from zero); r = b - A x
+// Level 0's pre-smoothing sweep from zero: x = w D^-1 b
+__global__ void __launch_bounds__(kT)
+    k_smooth0(const AmgState* st, int n, const double* __restrict__ dinv, const double* __restrict__ b,
+              double* __restrict__ x) {
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i < n) x[i] = kOmega * __ldg(&dinv[i]) * __ldg(&b[i]);
+}
+
+// r = b - A x
 template <class R>
 __global__ void __launch_bounds__(kT)
-    k_pre(const AmgState* st, R rows, int n, const double* __restrict__ dinv, const double* __restrict__ b,
-          double* __restrict__ x, double* __restrict__ r) {
+    k_resid(const AmgState* st, R rows, int n, const double* __restrict__ b, const double* __restrict__ x,
+            double* __restrict__ r) {
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
     if (i >= n) return;
-    const double bi = __ldg(&b[i]);
-    x[i] = kOmega * __ldg(&dinv[i]) * bi;
     double s = 0.0;
-    rows.each(i, [&](int j, double a) { s = fma(a, kOmega * __ldg(&dinv[j]) * __ldg(&b[j]), s); });
-    r[i] = bi - s;
+    rows.each(i, [&](int j, double a) { s = fma(a, __ldg(&x[j]), s); });
+    r[i] = __ldg(&b[i]) - s;
 }
 
-// b_c[I] = sum of r over the rows of aggregate I
+// b_c[I] = sum of r over the rows of aggregate I, and the coarse level's
+// pre-smoothing sweep from zero x_c = w D_c^-1 b_c
 __global__ void __launch_bounds__(kT)
     k_restrict(const AmgState* st, int nc, const int* __restrict__ mptr, const int* __restrict__ mem,
-               const double* __restrict__ r, double* __restrict__ bc) {
+               const double* __restrict__ r, const double* __restrict__ dinv_c, double* __restrict__ bc,
+               double* __restrict__ xc) {
     if (done_flag(st)) return;
     const int c = blockIdx.x * kT + threadIdx.x;
     if (c >= nc) return;
     double s = 0.0;
     for (int k = __ldg(&mptr[c]); k < __ldg(&mptr[c + 1]); ++k) s += __ldg(&r[__ldg(&mem[k])]);
     bc[c] = s;
+    xc[c] = kOmega * __ldg(&dinv_c[c]) * s;
 }
 
-// x = A_c^-1 b on the coarsest level, one warp per row
-__global__ void __launch_bounds__(kT)
-    k_coarse(const AmgState* st, int n, const double* __restrict__ ainv, const double* __restrict__ b,
-             double* __restrict__ x) {
+// The small levels t..L-1 of a V-cycle in one block of 1024 threads: their
+// kernels would each be a few blocks that wait on latency, so one block runs
+// the same steps with barriers between them.  Level t's b and x (its
+// pre-smoothing sweep) come from the restriction above it; its xo is the
+// correction handed back up.
+struct TailLevel {
+    int n;
+    SellRows A;
+    const double* dinv;
+    const int* agg;   // to level l+1
+    const int* mptr;  // members of level l+1's rows
+    const int* mem;
+    double *b, *x, *xo, *r;
+};
+
+__global__ void __launch_bounds__(1024)
+    k_tail(const AmgState* st, const TailLevel* __restrict__ lv, int nl, const double* __restrict__ ainv) {
     if (done_flag(st)) return;
-    const int row = blockIdx.x * (kT / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
-    if (row >= n) return;
-    double s = 0.0;
-    for (int j = lane; j < n; j += 32) s = fma(__ldg(&ainv[(size_t)row * n + j]), __ldg(&b[j]), s);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) x[row] = s;
+    const int T = threadIdx.x, NT = blockDim.x;
+    for (int l = 0; l + 1 < nl; ++l) {  // down
+        const TailLevel& F = lv[l];
+        const TailLevel& C = lv[l + 1];
+        for (int i = T; i < F.n; i += NT) {
+            double s = 0.0;
+            F.A.each(i, [&](int j, double a) { s = fma(a, F.x[j], s); });
+            F.r[i] = F.b[i] - s;
+        }
+        __syncthreads();
+        for (int c = T; c < C.n; c += NT) {
+            double s = 0.0;
+            for (int k = F.mptr[c]; k < F.mptr[c + 1]; ++k) s += F.r[F.mem[k]];
+            C.b[c] = s;
+            C.x[c] = kOmega * C.dinv[c] * s;
+        }
+        __syncthreads();
+    }
+    {  // coarsest: xo = A^-1 b, a warp per row
+        const TailLevel& B = lv[nl - 1];
+        const int lane = T & 31;
+        for (int row = T >> 5; row < B.n; row += NT >> 5) {
+            double s = 0.0;
+            for (int j = lane; j < B.n; j += 32) s = fma(__ldg(&ainv[(size_t)row * B.n + j]), B.b[j], s);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) B.xo[row] = s;
+        }
+        __syncthreads();
+    }
+    for (int l = nl - 2; l >= 0; --l) {  // up
+        const TailLevel& F = lv[l];
+        const TailLevel& C = lv[l + 1];
+        for (int i = T; i < F.n; i += NT) F.r[i] = F.x[i] + C.xo[F.agg[i]];
+        __syncthreads();
+        for (int i = T; i < F.n; i += NT) {
+            double s = 0.0;
+            F.A.each(i, [&](int j, double a) { s = fma(a, F.r[j], s); });
+            F.xo[i] = fma(kOmega * F.dinv[i], F.b[i] - s, F.r[i]);
+        }
+        __syncthreads();
+    }
 }
 
-// y = x + P xc; out = y + w D^-1 (b - A y)
+// y = x + P xc
+__global__ void __launch_bounds__(kT)
+    k_prolong(const AmgState* st, int n, const double* __restrict__ x, const double* __restrict__ xc,
+              const int* __restrict__ agg, double* __restrict__ y) {
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i < n) y[i] = __ldg(&x[i]) + __ldg(&xc[__ldg(&agg[i])]);
+}
+
+// out = y + w D^-1 (b - A y)
 template <class R>
 __global__ void __launch_bounds__(kT)
     k_post(const AmgState* st, R rows, int n, const double* __restrict__ dinv, const double* __restrict__ b,
-           const double* __restrict__ x, const double* __restrict__ xc, const int* __restrict__ agg,
-           double* __restrict__ out) {
+           const double* __restrict__ y, double* __restrict__ out) {
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
     if (i >= n) return;
-    const double yi = __ldg(&x[i]) + __ldg(&xc[__ldg(&agg[i])]);
     double s = 0.0;
-    rows.each(i, [&](int j, double a) { s = fma(a, __ldg(&x[j]) + __ldg(&xc[__ldg(&agg[j])]), s); });
-    out[i] = fma(kOmega * __ldg(&dinv[i]), __ldg(&b[i]) - s, yi);
+    rows.each(i, [&](int j, double a) { s = fma(a, __ldg(&y[j]), s); });
+    out[i] = fma(kOmega * __ldg(&dinv[i]), __ldg(&b[i]) - s, __ldg(&y[i]));
 }
 
 // ------------------------------------------------------------ CG
@@ -573,18 +679,37 @@ fvgb_status symbolic(AmgCache* c, cudaStream_t s) {
     c->lv.emplace_back();
     c->lv[0].n = n;
     c->lv[0].nnz = nnz;
-    bool top = true;
+    std::vector<int> slot_of = csr_pos;  // the current level's slot of each of its CSR entries
     while ((int)c->lv.size() < kMaxLevels && A.n > kCoarseRows) {
+        // two rounds of pairwise matching per level (double pairwise): the pairs
+        // of the first round are matched again on their Galerkin matrix, so a
+        // level has about a quarter of the rows and half as many levels are
+        // needed
         std::vector<int> agg;
-        const int nc = pgm_aggregate(A.n, A.rp.data(), A.ci.data(), A.v.data(), agg);
+        int nc = pgm_aggregate(A.n, A.rp.data(), A.ci.data(), A.v.data(), agg);
         if (nc > 0.9 * A.n) break;
+        if (nc > kCoarseRows) {
+            HostCsr A1;
+            std::vector<int> m1, e1, g1, s1, agg2;
+            galerkin(A, agg, nc, A1, m1, e1, g1, s1);
+            const int nc2 = pgm_aggregate(A1.n, A1.rp.data(), A1.ci.data(), A1.v.data(), agg2);
+            if (nc2 <= 0.9 * nc) {
+                for (int& a : agg) a = agg2[a];
+                nc = nc2;
+                // aggregates numbered by their lowest row again
+                std::vector<int> renum(nc, -1);
+                int k = 0;
+                for (int& a : agg) {
+                    if (renum[a] < 0) renum[a] = k++;
+                    a = renum[a];
+                }
+            }
+        }
         HostCsr Ac;
         std::vector<int> mptr, mem, gptr, gsrc;
         galerkin(A, agg, nc, Ac, mptr, mem, gptr, gsrc);
         Level& L = c->lv.back();
-        if (top)  // level 0's sums read the sliced-ELL slots
-            for (int& k : gsrc) k = csr_pos[k];
-        top = false;
+        for (int& k : gsrc) k = slot_of[k];  // the sums read the fine level's sliced-ELL slots
         cudaError_t e = upload(c, &L.agg, agg);
         if (e == cudaSuccess) e = upload(c, &L.mptr, mptr);
         if (e == cudaSuccess) e = upload(c, &L.mem, mem);
@@ -595,18 +720,36 @@ fvgb_status symbolic(AmgCache* c, cudaStream_t s) {
         Level C;
         C.n = Ac.n;
         C.nnz = (int)Ac.ci.size();
-        std::vector<int> dpos(Ac.n, -1);
-        for (int i = 0; i < Ac.n; ++i)
-            for (int k = Ac.rp[i]; k < Ac.rp[i + 1]; ++k)
-                if (Ac.ci[k] == i) dpos[i] = k;
+        // sliced ELL of the coarse matrix; gdst: the slot of each CSR entry
+        const int ns = (Ac.n + 31) / 32;
+        std::vector<int> sptr(ns + 1, 0);
+        for (int sl = 0; sl < ns; ++sl) {
+            int w = 0;
+            for (int i = sl * 32; i < std::min(Ac.n, sl * 32 + 32); ++i) w = std::max(w, Ac.rp[i + 1] - Ac.rp[i]);
+            sptr[sl + 1] = sptr[sl] + 32 * w;
+        }
+        std::vector<int> scol(sptr[ns]), gdst(C.nnz), dpos(Ac.n, -1);
+        for (int i = 0; i < Ac.n; ++i) {
+            const int base = sptr[i / 32] + (i & 31), w = (sptr[i / 32 + 1] - sptr[i / 32]) / 32;
+            for (int k = 0; k < w; ++k) scol[base + 32 * k] = i;  // padding
+            for (int k = Ac.rp[i]; k < Ac.rp[i + 1]; ++k) {
+                const int pos = base + 32 * (k - Ac.rp[i]);
+                scol[pos] = Ac.ci[k];
+                gdst[k] = pos;
+                if (Ac.ci[k] == i) dpos[i] = pos;
+            }
+        }
         for (int i = 0; i < Ac.n; ++i)
             if (dpos[i] < 0) return fvgb_fail(FVGB_ERR_INVALID_ARG, "multigrid: a coarse row without a diagonal entry");
-        e = upload(c, &C.rp, Ac.rp);
-        if (e == cudaSuccess) e = upload(c, &C.ci, Ac.ci);
+        e = upload(c, &L.gdst, gdst);
+        if (e == cudaSuccess) e = upload(c, &C.sptr, sptr);
+        if (e == cudaSuccess) e = upload(c, &C.scol, scol);
         if (e == cudaSuccess) e = upload(c, &C.dpos, dpos);
-        if (e == cudaSuccess) e = dev_alloc(c, &C.val, (size_t)C.nnz);
+        if (e == cudaSuccess) e = dev_alloc(c, &C.val, (size_t)std::max(1, sptr[ns]));
+        if (e == cudaSuccess) e = cudaMemset(C.val, 0, sizeof(double) * (size_t)std::max(1, sptr[ns]));
         if (e != cudaSuccess) return cuda_fail(e, "multigrid setup");
         c->lv.push_back(C);
+        slot_of = std::move(gdst);
         A = std::move(Ac);
     }
     if (c->lv.size() < 2) return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: the system does not coarsen (too small?)");
@@ -620,6 +763,20 @@ fvgb_status symbolic(AmgCache* c, cudaStream_t s) {
         if (e == cudaSuccess) e = dev_alloc(c, &L.r, (size_t)L.n);
         if (e == cudaSuccess && l > 0) e = dev_alloc(c, &L.b, (size_t)L.n);
         if (e != cudaSuccess) return cuda_fail(e, "multigrid vectors");
+    }
+    {
+        const int L = (int)c->lv.size();
+        int t = 1;
+        while (t < L - 1 && c->lv[t].n > kTailRows) ++t;
+        c->tail_from = t;
+        std::vector<TailLevel> tl;
+        for (int l = t; l < L; ++l) {
+            const Level& V = c->lv[l];
+            tl.push_back(TailLevel{V.n, SellRows{V.sptr, V.scol, V.val}, V.dinv, V.agg, V.mptr, V.mem, V.b, V.x, V.xo,
+                                   V.r});
+        }
+        cudaError_t e = upload(c, &c->tail, tl);
+        if (e != cudaSuccess) return cuda_fail(e, "multigrid setup");
     }
     c->nblk = (int)grid_for(n, kT);
     cudaError_t e = dev_alloc(c, &c->ainv, (size_t)c->nc * c->nc);
@@ -643,11 +800,11 @@ fvgb_status numeric(AmgCache* c, cudaStream_t s) {
         const Level& F = c->lv[l];
         Level& C = c->lv[l + 1];
         const double* vf = l == 0 ? ls->values : F.val;
-        k_galerkin<<<grid_for(C.nnz, kT), kT, 0, s>>>(C.nnz, F.gptr, F.gsrc, vf, C.val);
+        k_galerkin<<<grid_for(C.nnz, kT), kT, 0, s>>>(C.nnz, F.gptr, F.gsrc, F.gdst, vf, C.val);
         k_dinv_csr<<<grid_for(C.n, kT), kT, 0, s>>>(C.n, C.dpos, C.val, C.dinv);
     }
     const Level& B = c->lv.back();
-    k_dense<<<B.n, kT, 0, s>>>(B.n, B.rp, B.ci, B.val, c->ainv);
+    k_dense<<<B.n, kT, 0, s>>>(B.n, SellRows{B.sptr, B.scol, B.val}, c->ainv);
     k_gauss_jordan<<<1, 1024, sizeof(double) * B.n, s>>>(B.n, c->ainv);
     FVGB_LAUNCH_CHECK("multigrid numeric setup");
     c->version = ls->version;
@@ -667,71 +824,76 @@ cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* de
     return cudaGraphAddKernelNode(node, g, has_dep ? dep : nullptr, has_dep ? 1 : 0, &kp);
 }
 
-// The V-cycle z = M r as a chain of kernel nodes after *prev.
+// The V-cycle z = M r as a chain of kernel nodes after *prev: levels
+// 0..t-1 one kernel per step, levels t..L-1 in the single-block tail.
 struct VcycleArgs {
     std::vector<std::vector<void*>> args;
     std::vector<EllRows> ell;
-    std::vector<CsrRows> csr;
+    std::vector<SellRows> sell;
     std::vector<int> ns;
     std::vector<const double*> bs;
     std::vector<double*> outs;
     std::vector<double*> xcs;
+    int nl_tail = 0;
+    const TailLevel* tail = nullptr;
 };
 
 cudaError_t add_vcycle(AmgCache* c, cudaGraph_t g, cudaGraphNode_t* prev, const double* r_in, double* z_out,
                        VcycleArgs& va) {
     const size_t L = c->lv.size();
+    const size_t t = (size_t)c->tail_from;
     va.ell.assign(1, EllRows{c->ls->mesh->v, c->ls->values});
-    va.csr.resize(L);
-    for (size_t l = 1; l < L; ++l) va.csr[l] = CsrRows{c->lv[l].rp, c->lv[l].ci, c->lv[l].val};
+    va.sell.resize(L);
+    for (size_t l = 1; l < L; ++l) va.sell[l] = SellRows{c->lv[l].sptr, c->lv[l].scol, c->lv[l].val};
     va.ns.resize(L);
     va.bs.resize(L);
     va.outs.resize(L);
     va.xcs.resize(L);
     va.args.clear();
-    va.args.reserve(4 * L + 4);
+    va.args.reserve(6 * L + 4);
     for (size_t l = 0; l < L; ++l) {
         va.ns[l] = c->lv[l].n;
         va.bs[l] = l == 0 ? r_in : c->lv[l].b;
         va.outs[l] = l == 0 ? z_out : c->lv[l].xo;
     }
+    va.nl_tail = (int)(L - t);
+    va.tail = c->tail;
     cudaError_t e = cudaSuccess;
     cudaGraphNode_t node;
-    // down
-    for (size_t l = 0; l + 1 < L && e == cudaSuccess; ++l) {
+    auto add = [&](void* fn, unsigned grid, unsigned block) {
+        if (e != cudaSuccess) return;
+        e = add_kernel(g, &node, prev, fn, grid, block, va.args.back().data());
+        if (e == cudaSuccess) *prev = node;
+    };
+    for (size_t l = 0; l < t && e == cudaSuccess; ++l) {  // down
         Level& F = c->lv[l];
         if (l == 0) {
-            va.args.push_back({&c->st, &va.ell[0], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &F.r});
-            e = add_kernel(g, &node, prev, (void*)k_pre<EllRows>, grid_for(F.n, kT), kT, va.args.back().data());
+            va.args.push_back({&c->st, &va.ns[0], &F.dinv, &va.bs[0], &F.x});
+            add((void*)k_smooth0, grid_for(F.n, kT), kT);
+            va.args.push_back({&c->st, &va.ell[0], &va.ns[0], &va.bs[0], &F.x, &F.r});
+            add((void*)k_resid<EllRows>, grid_for(F.n, kT), kT);
         } else {
-            va.args.push_back({&c->st, &va.csr[l], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &F.r});
-            e = add_kernel(g, &node, prev, (void*)k_pre<CsrRows>, grid_for(F.n, kT), kT, va.args.back().data());
+            va.args.push_back({&c->st, &va.sell[l], &va.ns[l], &va.bs[l], &F.x, &F.r});
+            add((void*)k_resid<SellRows>, grid_for(F.n, kT), kT);
         }
-        *prev = node;
-        if (e != cudaSuccess) break;
-        va.args.push_back({&c->st, &va.ns[l + 1], &F.mptr, &F.mem, &F.r, &c->lv[l + 1].b});
-        e = add_kernel(g, &node, prev, (void*)k_restrict, grid_for(va.ns[l + 1], kT), kT, va.args.back().data());
-        *prev = node;
+        Level& C = c->lv[l + 1];
+        va.args.push_back({&c->st, &va.ns[l + 1], &F.mptr, &F.mem, &F.r, &C.dinv, &C.b, &C.x});
+        add((void*)k_restrict, grid_for(C.n, kT), kT);
     }
-    // coarsest
-    if (e == cudaSuccess) {
-        Level& B = c->lv[L - 1];
-        va.args.push_back({&c->st, &va.ns[L - 1], &c->ainv, &B.b, &B.xo});
-        e = add_kernel(g, &node, prev, (void*)k_coarse, grid_for(B.n, kT / 32), kT, va.args.back().data());
-        *prev = node;
-    }
-    // up
-    for (size_t l = L - 1; l-- > 0 && e == cudaSuccess;) {
+    va.args.push_back({&c->st, &va.tail, &va.nl_tail, &c->ainv});
+    add((void*)k_tail, 1, 1024);
+    for (size_t l = t; l-- > 0 && e == cudaSuccess;) {  // up
         Level& F = c->lv[l];
         va.xcs[l] = c->lv[l + 1].xo;
+        va.args.push_back({&c->st, &va.ns[l], &F.x, &va.xcs[l], &F.agg, &F.r});  // y = x + P xc into F.r
+        add((void*)k_prolong, grid_for(F.n, kT), kT);
         if (l == 0) {
-            va.args.push_back({&c->st, &va.ell[0], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &va.xcs[l], &F.agg, &va.outs[l]});
-            e = add_kernel(g, &node, prev, (void*)k_post<EllRows>, grid_for(F.n, kT), kT, va.args.back().data());
+            va.args.push_back({&c->st, &va.ell[0], &va.ns[l], &F.dinv, &va.bs[l], &F.r, &va.outs[l]});
+            add((void*)k_post<EllRows>, grid_for(F.n, kT), kT);
         } else {
-            va.args.push_back({&c->st, &va.csr[l], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &va.xcs[l], &F.agg, &va.outs[l]});
-            e = add_kernel(g, &node, prev, (void*)k_post<CsrRows>, grid_for(F.n, kT), kT, va.args.back().data());
+            va.args.push_back({&c->st, &va.sell[l], &va.ns[l], &F.dinv, &va.bs[l], &F.r, &va.outs[l]});
+            add((void*)k_post<SellRows>, grid_for(F.n, kT), kT);
         }
-        *prev = node;
     }
     return e;
 }

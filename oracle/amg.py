@@ -13,6 +13,8 @@ library's aggregation is checked exactly and its V-cycle to rounding:
   index) and mutual picks form pairs, until at most 5% of the rows are left or
   no pair forms; a row left over joins its strongest aggregated neighbour's
   aggregate or stays alone; aggregates numbered by their lowest row;
+* two matchings per level (the pairs matched again on their Galerkin
+  matrix, double pairwise aggregation);
 * Galerkin coarse matrices P^T A P with the piecewise-constant P, levels until
   at most 256 rows remain, a level keeps more than 90% of the rows, or 25
   levels;
@@ -97,6 +99,19 @@ def hierarchy(rp, ci, v):
         agg, nc = pgm_aggregate(A.shape[0], A.indptr, A.indices, A.data)
         if nc > 0.9 * A.shape[0]:
             break
+        if nc > COARSE_ROWS:  # double pairwise: match the pairs again on their Galerkin matrix
+            P1 = sp.csr_matrix((np.ones(A.shape[0]), (np.arange(A.shape[0]), agg)), shape=(A.shape[0], nc))
+            A1 = (P1.T @ A @ P1).tocsr()
+            A1.sort_indices()
+            agg2, nc2 = pgm_aggregate(nc, A1.indptr, A1.indices, A1.data)
+            if nc2 <= 0.9 * nc:
+                agg = agg2[agg]
+                _, first = np.unique(agg, return_index=True)
+                order = np.argsort(first)          # aggregates numbered by their lowest row
+                renum = np.empty(nc2, np.int64)
+                renum[order] = np.arange(nc2)
+                agg = renum[agg].astype(np.int32)
+                nc = nc2
         P = sp.csr_matrix((np.ones(A.shape[0]), (np.arange(A.shape[0]), agg)), shape=(A.shape[0], nc))
         levels.append((A, agg, P))
         A = (P.T @ A @ P).tocsr()
