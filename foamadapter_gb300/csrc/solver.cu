@@ -2894,6 +2894,8 @@ extern "C" fvgb_status fvgb_batch_destroy(fvgb_batch* b) {
 extern "C" fvgb_status fvgb_batch_solve_async(fvgb_batch* b, double* x, const fvgb_solver_cfg* cfg,
                                               fvgb_solver_stats* stats_dev, fvgb_stream stream) {
     FVGB_CHECK_ARG(b && x && cfg, "fvgb_batch_solve: null argument");
+    if (cfg->preconditioner != FVGB_PRECOND_JACOBI)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_batch_solve: the multigrid preconditioner solves single systems only");
     return launch(b->c, x, cfg, stats_dev, (cudaStream_t)stream);
 }
 
@@ -2919,6 +2921,8 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
     fvgb_clear_error();
     FVGB_CHECK_ARG(ls && terms && nterms > 0 && bc && psi && cfg && out, "fvgb_step_create: null argument");
     FVGB_CHECK_ARG(ls->ncomp == 1, "fvgb_step_create: scalar systems only");
+    if (cfg->preconditioner != FVGB_PRECOND_JACOBI)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_step_create: step graphs use the Jacobi preconditioner");
     FVGB_CHECK_ARG(!batch || batch->c->ls == ls, "fvgb_step_create: the batch belongs to another system");
     fvgb_status fst = check_cfg(cfg);
     if (fst != FVGB_OK) return fst;
