@@ -184,6 +184,7 @@ _SIGS = {
     "fvgb_fvsolution_update_criteria": (C.c_int, [vp]),
     "fvgb_fvsolution_map": (C.c_int, [vp, C.POINTER(vp)]),
     "fvgb_solver_cfg_from_dict": (C.c_int, [vp, C.POINTER(SolverCfg)]),
+    "fvgb_solver_cfg_from_json": (C.c_int, [C.c_char_p, C.POINTER(SolverCfg)]),
     "fvgb_scheme_from_dict": (C.c_int, [vp, C.c_char_p, C.c_char_p, P_i32]),
     "fvgb_amg_apply": (C.c_int, [vp, vp, vp, vp]),
     "fvgb_amg_info": (C.c_int, [vp, P_i32, vp, vp, i32]),

@@ -664,10 +664,21 @@ inline Dictionary mapFvSolution(const Dictionary& solverDict) {
     check(fvgb_fvsolution_map(solverDict.handle(), &m));
     return Dictionary(m, true);
 }
-// A Ginkgo-form solver entry (mapFvSolution's output) as PDESolver::solve's configuration.
-inline SolverConfig solverConfig(const Dictionary& mapped) {
+inline SolverConfig solverConfigOf(const fvgb_solver_cfg& c);
+// A Ginkgo-form solver entry (mapFvSolution's output) as PDESolver::solve's
+// configuration; an entry naming a configFile reads that Ginkgo JSON file,
+// relative to configDir (the case's system directory).
+inline SolverConfig solverConfig(const Dictionary& mapped, const std::string& configDir = "") {
     fvgb_solver_cfg c{};
-    check(fvgb_solver_cfg_from_dict(mapped.handle(), &c));
+    if (mapped.contains("configFile")) {
+        if (configDir.empty()) throw Error(FVGB_ERR_INVALID_ARG, "solverConfig: configFile needs the case's system directory");
+        check(fvgb_solver_cfg_from_json((configDir + "/" + mapped.get<std::string>("configFile")).c_str(), &c));
+    } else {
+        check(fvgb_solver_cfg_from_dict(mapped.handle(), &c));
+    }
+    return solverConfigOf(c);
+}
+inline SolverConfig solverConfigOf(const fvgb_solver_cfg& c) {
     SolverConfig s;
     s.relTol = c.rel_tol;
     s.tolerance = c.abs_tol;

@@ -756,7 +756,7 @@ extern "C" fvgb_status fvgb_solver_cfg_from_dict(const fvgb_dict* d, fvgb_solver
     c.max_outer = 50;
     c.method = FVGB_SOLVER_CG;
     if (entry_of(d, "configFile"))
-        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "solver entry: configFile (a Ginkgo JSON file) is not read here");
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "solver entry: configFile names a Ginkgo JSON file: fvgb_solver_cfg_from_json");
     std::string w;
     if (word_of(d, "solver", w) && w != "Ginkgo")
         return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("solver entry: solver " + w + " (map it with fvgb_fvsolution_map first)").c_str());
@@ -794,6 +794,221 @@ extern "C" fvgb_status fvgb_solver_cfg_from_dict(const fvgb_dict* d, fvgb_solver
     if (c.inner_rel_tol <= 0.0) c.inner_rel_tol = c.method == FVGB_SOLVER_BICGSTAB ? 0.01 : 0.1;
     *cfg = c;
     return FVGB_OK;
+}
+
+// ------------------------------------------------- Ginkgo JSON configurations
+// The configFile of a solver entry (fvSolution.cpp:145-152) is a Ginkgo JSON
+// configuration, e.g. tutorials/cylinder2D/system/gko/config.mg.json.  A small
+// JSON reader (objects, arrays, strings, numbers, true/false/null) and the
+// mapping of the keys this library implements.
+namespace {
+
+struct Json {
+    enum Kind { NUL, BOOL, NUM, STR, ARR, OBJ } kind = NUL;
+    bool b = false;
+    double num = 0.0;
+    std::string str;
+    std::vector<Json> arr;
+    std::vector<std::pair<std::string, Json>> obj;
+    const Json* get(const char* k) const {
+        for (const auto& kv : obj)
+            if (kv.first == k) return &kv.second;
+        return nullptr;
+    }
+};
+
+struct JsonParser {
+    const std::string& s;
+    size_t i = 0;
+    int depth = 0;
+    explicit JsonParser(const std::string& t) : s(t) {}
+    void ws() {
+        while (i < s.size() && std::isspace((unsigned char)s[i])) ++i;
+    }
+    bool lit(const char* w) {
+        const size_t n = std::strlen(w);
+        if (s.compare(i, n, w) != 0) return false;
+        i += n;
+        return true;
+    }
+    bool string(std::string& out) {
+        if (i >= s.size() || s[i] != '"') return false;
+        ++i;
+        out.clear();
+        while (i < s.size() && s[i] != '"') {
+            if (s[i] == '\\' && i + 1 < s.size()) {
+                ++i;
+                const char e = s[i];
+                out.push_back(e == 'n' ? '\n' : e == 't' ? '\t' : e);
+            } else {
+                out.push_back(s[i]);
+            }
+            ++i;
+        }
+        if (i >= s.size()) return false;
+        ++i;
+        return true;
+    }
+    bool value(Json& v) {
+        if (++depth > 64) return false;
+        ws();
+        bool ok = false;
+        if (i >= s.size()) {
+            ok = false;
+        } else if (s[i] == '{') {
+            v.kind = Json::OBJ;
+            ++i;
+            ws();
+            if (i < s.size() && s[i] == '}') {
+                ++i;
+                ok = true;
+            } else {
+                for (;;) {
+                    ws();
+                    std::string k;
+                    Json x;
+                    if (!string(k)) break;
+                    ws();
+                    if (i >= s.size() || s[i] != ':') break;
+                    ++i;
+                    if (!value(x)) break;
+                    v.obj.emplace_back(k, std::move(x));
+                    ws();
+                    if (i < s.size() && s[i] == ',') {
+                        ++i;
+                        continue;
+                    }
+                    if (i < s.size() && s[i] == '}') {
+                        ++i;
+                        ok = true;
+                    }
+                    break;
+                }
+            }
+        } else if (s[i] == '[') {
+            v.kind = Json::ARR;
+            ++i;
+            ws();
+            if (i < s.size() && s[i] == ']') {
+                ++i;
+                ok = true;
+            } else {
+                for (;;) {
+                    Json x;
+                    if (!value(x)) break;
+                    v.arr.push_back(std::move(x));
+                    ws();
+                    if (i < s.size() && s[i] == ',') {
+                        ++i;
+                        continue;
+                    }
+                    if (i < s.size() && s[i] == ']') {
+                        ++i;
+                        ok = true;
+                    }
+                    break;
+                }
+            }
+        } else if (s[i] == '"') {
+            v.kind = Json::STR;
+            ok = string(v.str);
+        } else if (lit("true")) {
+            v.kind = Json::BOOL;
+            v.b = ok = true;
+        } else if (lit("false")) {
+            v.kind = Json::BOOL;
+            ok = true;
+        } else if (lit("null")) {
+            ok = true;
+        } else {
+            const char* b0 = s.c_str() + i;
+            char* end = nullptr;
+            v.num = std::strtod(b0, &end);
+            if (end != b0) {
+                v.kind = Json::NUM;
+                i += (size_t)(end - b0);
+                ok = true;
+            }
+        }
+        --depth;
+        return ok;
+    }
+};
+
+fvgb_status cfg_from_json(const Json& j, fvgb_solver_cfg* out) {
+    fvgb_solver_cfg c{};
+    c.max_iter = 1000;
+    c.precision = FVGB_PREC_FP64;
+    c.inner_max_iter = 1000;
+    c.max_outer = 50;
+    const Json* t = j.get("type");
+    if (!t || t->kind != Json::STR) return fvgb_fail(FVGB_ERR_INVALID_ARG, "Ginkgo config: no solver type");
+    if (t->str == "solver::Cg") c.method = FVGB_SOLVER_CG;
+    else if (t->str == "solver::Bicgstab") c.method = FVGB_SOLVER_BICGSTAB;
+    else return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("Ginkgo config: " + t->str + " is not implemented (Cg, Bicgstab are)").c_str());
+    const Json* p = j.get("preconditioner");
+    const Json* pt = p ? p->get("type") : nullptr;
+    if (!pt || pt->kind != Json::STR)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: an unpreconditioned solver is not implemented");
+    if (pt->str == "preconditioner::Jacobi") {
+        const Json* mbs = p->get("max_block_size");
+        if (!mbs || mbs->kind != Json::NUM || mbs->num != 1.0)
+            return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: Jacobi with max_block_size 1 only");
+    } else if (pt->str == "solver::Multigrid" && c.method == FVGB_SOLVER_CG) {
+        const Json* lv = p->get("mg_level");
+        if (lv && lv->kind == Json::ARR)
+            for (const Json& l : lv->arr) {
+                const Json* lt = l.get("type");
+                if (!lt || lt->kind != Json::STR || lt->str != "multigrid::Pgm")
+                    return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: multigrid levels other than multigrid::Pgm");
+            }
+        c.preconditioner = FVGB_PRECOND_MULTIGRID;
+    } else {
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("Ginkgo config: preconditioner " + pt->str + " is not implemented").c_str());
+    }
+    const Json* cr = j.get("criteria");
+    if (cr && cr->kind == Json::ARR) {
+        for (const Json& k : cr->arr) {
+            const Json* ct = k.get("type");
+            if (!ct || ct->kind != Json::STR) return fvgb_fail(FVGB_ERR_INVALID_ARG, "Ginkgo config: criterion without type");
+            if (ct->str == "Iteration") {
+                const Json* m = k.get("max_iters");
+                if (!m || m->kind != Json::NUM) return fvgb_fail(FVGB_ERR_INVALID_ARG, "Ginkgo config: Iteration without max_iters");
+                c.max_iter = (int32_t)m->num;
+            } else if (ct->str == "ResidualNorm") {
+                const Json* f = k.get("reduction_factor");
+                const Json* b = k.get("baseline");
+                if (!f || f->kind != Json::NUM)
+                    return fvgb_fail(FVGB_ERR_INVALID_ARG, "Ginkgo config: ResidualNorm without reduction_factor");
+                const std::string base = (b && b->kind == Json::STR) ? b->str : "rhs_norm";
+                if (base == "absolute") c.abs_tol = f->num;
+                else if (base == "initial_resnorm") c.rel_tol = f->num;
+                else
+                    return fvgb_fail(FVGB_ERR_UNSUPPORTED,
+                                     "Ginkgo config: ResidualNorm baseline rhs_norm (the default) is not implemented; "
+                                     "use absolute or initial_resnorm");
+            } else {
+                return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("Ginkgo config: criterion " + ct->str + " is not implemented").c_str());
+            }
+        }
+    }
+    c.inner_rel_tol = c.method == FVGB_SOLVER_BICGSTAB ? 0.01 : 0.1;
+    *out = c;
+    return FVGB_OK;
+}
+
+}  // namespace
+
+extern "C" fvgb_status fvgb_solver_cfg_from_json(const char* path, fvgb_solver_cfg* cfg) {
+    if (!path || !cfg) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_solver_cfg_from_json: null argument");
+    std::string text;
+    if (!read_file(path, text)) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_solver_cfg_from_json: cannot read the file");
+    Json j;
+    JsonParser ps(text);
+    if (!ps.value(j) || j.kind != Json::OBJ) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_solver_cfg_from_json: malformed JSON");
+    ps.ws();
+    if (ps.i != text.size()) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_solver_cfg_from_json: text after the JSON object");
+    return cfg_from_json(j, cfg);
 }
 
 // ------------------------------------------------------------ fvSchemes

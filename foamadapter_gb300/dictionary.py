@@ -216,11 +216,32 @@ def map_fv_solution(solver_dict: Dictionary) -> Dictionary:
     return Dictionary(h.value)
 
 
-def solver_config(mapped: Dictionary) -> dict:
+def solver_config(mapped: Dictionary, config_dir=None) -> dict:
     """Keyword arguments of ``neon.LinearSystem.solve`` for a Ginkgo-form
-    solver entry (``map_fv_solution`` output, or written that way)."""
+    solver entry (``map_fv_solution`` output, or written that way).  An entry
+    naming a ``configFile`` (a Ginkgo JSON configuration) reads that file,
+    relative to ``config_dir`` (the case's system directory)."""
     cfg = abi.SolverCfg()
-    abi.check(abi.lib().fvgb_solver_cfg_from_dict(mapped.handle, C.byref(cfg)))
+    if mapped.contains("configFile"):
+        if config_dir is None:
+            raise ValueError("solver_config: the entry names a configFile; give config_dir")
+        from pathlib import Path
+
+        path = Path(config_dir) / str(mapped.get("configFile"))
+        abi.check(abi.lib().fvgb_solver_cfg_from_json(str(path).encode(), C.byref(cfg)))
+    else:
+        abi.check(abi.lib().fvgb_solver_cfg_from_dict(mapped.handle, C.byref(cfg)))
+    return _kwargs(cfg)
+
+
+def ginkgo_config(path) -> dict:
+    """Keyword arguments of ``neon.LinearSystem.solve`` for a Ginkgo JSON configuration file."""
+    cfg = abi.SolverCfg()
+    abi.check(abi.lib().fvgb_solver_cfg_from_json(str(path).encode(), C.byref(cfg)))
+    return _kwargs(cfg)
+
+
+def _kwargs(cfg) -> dict:
     return dict(rel_tol=cfg.rel_tol, abs_tol=cfg.abs_tol, max_iter=cfg.max_iter, precision=cfg.precision,
                 inner_rel_tol=cfg.inner_rel_tol, inner_max_iter=cfg.inner_max_iter, max_outer=cfg.max_outer,
                 method=cfg.method, preconditioner=cfg.preconditioner)

@@ -683,8 +683,18 @@ fvgb_status fvgb_fvsolution_map(const fvgb_dict* solver_dict, fvgb_dict** mapped
  * absolute_residual_norm.
  * This library's own keywords: precision FP64|mixed, innerRelTol,
  * innerMaxIter, maxOuter.  Other solvers and preconditioners (Bicg,
- * Multigrid, Ilu, none, block Jacobi) and configFile: FVGB_ERR_UNSUPPORTED. */
+ * Multigrid as a solver, Ilu, none, block Jacobi): FVGB_ERR_UNSUPPORTED; an
+ * entry naming a configFile too (read that file with
+ * fvgb_solver_cfg_from_json). */
 fvgb_status fvgb_solver_cfg_from_dict(const fvgb_dict* mapped, fvgb_solver_cfg* cfg);
+/* A Ginkgo JSON configuration (the configFile of a solver entry, e.g.
+ * tutorials/cylinder2D/system/gko/config.mg.json) as a solver configuration:
+ * type solver::Cg / solver::Bicgstab; preconditioner preconditioner::Jacobi
+ * (max_block_size 1) or, with Cg, solver::Multigrid with multigrid::Pgm
+ * levels; criteria Iteration (max_iters) and ResidualNorm (reduction_factor,
+ * baseline absolute or initial_resnorm; Ginkgo's default baseline rhs_norm:
+ * FVGB_ERR_UNSUPPORTED). */
+fvgb_status fvgb_solver_cfg_from_json(const char* path, fvgb_solver_cfg* cfg);
 /* The scheme fvSchemes gives `name` in `section` (its own entry, else
  * default): divSchemes / gradSchemes "Gauss linear" -> FVGB_SCHEME_LINEAR,
  * "Gauss upwind" -> FVGB_SCHEME_UPWIND; laplacianSchemes "Gauss linear

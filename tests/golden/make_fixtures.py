@@ -120,7 +120,8 @@ def main(ref: Path):
     print("foam_files", {k: v.size for k, v in raw.items()})
     # the cases' system dictionaries, unparsed (input of the dictionary reader's tests)
     dicts = sorted(p.relative_to(ref).as_posix() for top in ("test", "tutorials")
-                   for p in (ref / top).glob("*/system/*") if p.is_file() and p.suffix != ".json")
+                   for p in [*(ref / top).glob("*/system/*"), *(ref / top).glob("*/system/gko/*.json")]
+                   if p.is_file())
     raw = {k.replace("/", "__").replace("-", "_"): np.frombuffer((ref / k).read_bytes(), np.uint8) for k in dicts}
     names = {k.replace("/", "__").replace("-", "_"): k for k in dicts}
     np.savez_compressed(HERE / "foam_dicts.npz", _names=np.asarray([f"{a}={b}" for a, b in names.items()]), **raw)

@@ -166,9 +166,8 @@ def test_solver_config_rejects_what_is_not_built(ref):
         solver_config(Dictionary.parse("solver PCG;"))  # not mapped
     cfg = Dictionary.parse("configFile \"gko/config.bj.json\";")
     assert map_fv_solution(cfg).keys() == ["configFile"]
-    with pytest.raises(abi.FvgbError) as e:
-        solver_config(cfg)
-    assert e.value.status == abi.ERR_UNSUPPORTED
+    with pytest.raises(ValueError):
+        solver_config(cfg)  # a configFile needs the directory it is relative to
 
 
 def test_solver_config_extensions():
@@ -340,3 +339,41 @@ def test_pde_solver_configured_by_fv_solution(cuda, ref):
     assert results[0][0] == results[1][0]
     assert np.array_equal(results[0][1], results[1][1])
     torch.cuda.synchronize()
+
+
+def test_ginkgo_json_configs(ref, tmp_path):
+    """The reference's own Ginkgo configurations (tutorials/cylinder2D/system/gko)."""
+    from foamadapter_gb300.dictionary import ginkgo_config
+
+    gko = ref / "tutorials/cylinder2D/system/gko"
+    mg = ginkgo_config(gko / "config.mg.json")
+    assert mg["method"] == abi.SOLVER_CG and mg["preconditioner"] == abi.PRECOND_MULTIGRID
+    assert mg["max_iter"] == 100 and mg["abs_tol"] == 1e-5 and mg["rel_tol"] == 0.0
+    for name in ("config.bj.json", "p.config.bj.json"):  # ResidualNorm with Ginkgo's default baseline rhs_norm
+        with pytest.raises(abi.FvgbError) as e:
+            ginkgo_config(gko / name)
+        assert e.value.status == abi.ERR_UNSUPPORTED
+    (tmp_path / "ok.json").write_text(
+        '{"type": "solver::Bicgstab", "preconditioner": {"type": "preconditioner::Jacobi", "max_block_size": 1},'
+        ' "criteria": [{"type": "Iteration", "max_iters": 77},'
+        ' {"type": "ResidualNorm", "reduction_factor": 1e-9, "baseline": "initial_resnorm"}]}')
+    c = ginkgo_config(tmp_path / "ok.json")
+    assert c["method"] == abi.SOLVER_BICGSTAB and c["max_iter"] == 77 and c["rel_tol"] == 1e-9
+    assert c["preconditioner"] == abi.PRECOND_JACOBI
+    for text, status in (('{"type": "solver::Cg"', abi.ERR_INVALID_ARG),
+                         ('{"type": "solver::Gmres", "preconditioner": {"type": "preconditioner::Jacobi", '
+                          '"max_block_size": 1}}', abi.ERR_UNSUPPORTED),
+                         ('{"type": "solver::Cg", "preconditioner": {"type": "preconditioner::Jacobi", '
+                          '"max_block_size": 32}}', abi.ERR_UNSUPPORTED),
+                         ('{"type": "solver::Cg"}', abi.ERR_UNSUPPORTED)):
+        (tmp_path / "bad.json").write_text(text)
+        with pytest.raises(abi.FvgbError) as e:
+            ginkgo_config(tmp_path / "bad.json")
+        assert e.value.status == status, text
+    # a solver entry naming the file
+    entry = Dictionary.parse('configFile "gko/config.mg.json";')
+    assert map_fv_solution(entry).keys() == ["configFile"]
+    assert solver_config(entry, config_dir=ref / "tutorials/cylinder2D/system")["preconditioner"] == \
+        abi.PRECOND_MULTIGRID
+    with pytest.raises(ValueError):
+        solver_config(entry)
