@@ -482,6 +482,21 @@ __global__ void __launch_bounds__(kT)
     if (i < n) y[i] = __ldg(&x[i]) + __ldg(&xc[__ldg(&agg[i])]);
 }
 
+// y = x + P xc; out = y + w D^-1 (b - A y), y formed on the fly (coarse
+// levels, where a launch costs more than the extra dependent load)
+__global__ void __launch_bounds__(kT)
+    k_post_fused(const AmgState* st, SellRows rows, int n, const double* __restrict__ dinv,
+                 const double* __restrict__ b, const double* __restrict__ x, const double* __restrict__ xc,
+                 const int* __restrict__ agg, double* __restrict__ out) {
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i >= n) return;
+    const double yi = __ldg(&x[i]) + __ldg(&xc[__ldg(&agg[i])]);
+    double s = 0.0;
+    rows.each(i, [&](int j, double a) { s = fma(a, __ldg(&x[j]) + __ldg(&xc[__ldg(&agg[j])]), s); });
+    out[i] = fma(kOmega * __ldg(&dinv[i]), __ldg(&b[i]) - s, yi);
+}
+
 // out = y + w D^-1 (b - A y)
 template <class R>
 __global__ void __launch_bounds__(kT)
@@ -507,9 +522,10 @@ __global__ void k_params(AmgState* st, double* x, double rel_tol, double abs_tol
     st->done = 0;
 }
 
-// r = b - A x, ||r||
+// r = b - A x, ||r||; x0 = w D^-1 r (the V-cycle's first sweep)
 __global__ void __launch_bounds__(kT)
-    k_init(AmgState* st, EllRows A, int n, const double* __restrict__ b, double* __restrict__ r, double* part) {
+    k_init(AmgState* st, EllRows A, int n, const double* __restrict__ b, double* __restrict__ r, double* part,
+           const double* __restrict__ dinv0, double* __restrict__ x0) {
     __shared__ double sm[kT];
     const int i = blockIdx.x * kT + threadIdx.x;
     const double* x = st->x;
@@ -519,6 +535,7 @@ __global__ void __launch_bounds__(kT)
         A.each(i, [&](int j, double a) { s = fma(a, x[j], s); });
         ri = __ldg(&b[i]) - s;
         r[i] = ri;
+        x0[i] = kOmega * __ldg(&dinv0[i]) * ri;
     }
     double tot;
     if (arrive(st, part, block_sum(ri * ri, sm), sm, &tot) && threadIdx.x == 0) {
@@ -582,10 +599,10 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
-// x += alpha p, r -= alpha q, ||r||, convergence
+// x += alpha p, r -= alpha q, ||r||, convergence; x0 = w D^-1 r (the V-cycle's first sweep)
 __global__ void __launch_bounds__(kT)
     k_update(AmgState* st, int n, const double* __restrict__ p, const double* __restrict__ q, double* __restrict__ r,
-             double* part) {
+             double* part, const double* __restrict__ dinv0, double* __restrict__ x0) {
     __shared__ double sm[kT];
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
@@ -596,6 +613,7 @@ __global__ void __launch_bounds__(kT)
         x[i] = fma(alpha, __ldg(&p[i]), x[i]);
         const double ri = fma(-alpha, __ldg(&q[i]), r[i]);
         r[i] = ri;
+        x0[i] = kOmega * __ldg(&dinv0[i]) * ri;
         v = ri * ri;
     }
     double tot;
@@ -839,7 +857,7 @@ struct VcycleArgs {
 };
 
 cudaError_t add_vcycle(AmgCache* c, cudaGraph_t g, cudaGraphNode_t* prev, const double* r_in, double* z_out,
-                       VcycleArgs& va) {
+                       VcycleArgs& va, bool first_sweep_done = false) {
     const size_t L = c->lv.size();
     const size_t t = (size_t)c->tail_from;
     va.ell.assign(1, EllRows{c->ls->mesh->v, c->ls->values});
@@ -868,8 +886,10 @@ cudaError_t add_vcycle(AmgCache* c, cudaGraph_t g, cudaGraphNode_t* prev, const 
     for (size_t l = 0; l < t && e == cudaSuccess; ++l) {  // down
         Level& F = c->lv[l];
         if (l == 0) {
-            va.args.push_back({&c->st, &va.ns[0], &F.dinv, &va.bs[0], &F.x});
-            add((void*)k_smooth0, grid_for(F.n, kT), kT);
+            if (!first_sweep_done) {  // the solve's CG kernels form x0 = w D^-1 r themselves
+                va.args.push_back({&c->st, &va.ns[0], &F.dinv, &va.bs[0], &F.x});
+                add((void*)k_smooth0, grid_for(F.n, kT), kT);
+            }
             va.args.push_back({&c->st, &va.ell[0], &va.ns[0], &va.bs[0], &F.x, &F.r});
             add((void*)k_resid<EllRows>, grid_for(F.n, kT), kT);
         } else {
@@ -885,14 +905,15 @@ cudaError_t add_vcycle(AmgCache* c, cudaGraph_t g, cudaGraphNode_t* prev, const 
     for (size_t l = t; l-- > 0 && e == cudaSuccess;) {  // up
         Level& F = c->lv[l];
         va.xcs[l] = c->lv[l + 1].xo;
-        va.args.push_back({&c->st, &va.ns[l], &F.x, &va.xcs[l], &F.agg, &F.r});  // y = x + P xc into F.r
-        add((void*)k_prolong, grid_for(F.n, kT), kT);
         if (l == 0) {
+            va.args.push_back({&c->st, &va.ns[l], &F.x, &va.xcs[l], &F.agg, &F.r});  // y = x + P xc into F.r
+            add((void*)k_prolong, grid_for(F.n, kT), kT);
             va.args.push_back({&c->st, &va.ell[0], &va.ns[l], &F.dinv, &va.bs[l], &F.r, &va.outs[l]});
             add((void*)k_post<EllRows>, grid_for(F.n, kT), kT);
         } else {
-            va.args.push_back({&c->st, &va.sell[l], &va.ns[l], &F.dinv, &va.bs[l], &F.r, &va.outs[l]});
-            add((void*)k_post<SellRows>, grid_for(F.n, kT), kT);
+            va.args.push_back({&c->st, &va.sell[l], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &va.xcs[l], &F.agg,
+                               &va.outs[l]});
+            add((void*)k_post_fused, grid_for(F.n, kT), kT);
         }
     }
     return e;
@@ -914,17 +935,17 @@ fvgb_status build_graph(AmgCache* c) {
     cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
     cudaGraphNode_t prev = nullptr, node;
     VcycleArgs v0, v1;
-    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part};
+    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &c->lv[0].x};
     void* a_first[] = {&c->st, &n, &c->r, &c->z, &c->p, &c->part};
     void* a_cond[] = {&c->st, &h};
     void* a_spmv[] = {&c->st, &A, &n, &c->p, &c->q, &c->part};
-    void* a_upd[] = {&c->st, &n, &c->p, &c->q, &c->r, &c->part};
+    void* a_upd[] = {&c->st, &n, &c->p, &c->q, &c->r, &c->part, &c->lv[0].dinv, &c->lv[0].x};
     void* a_rz[] = {&c->st, &n, &c->r, &c->z, &c->part};
     void* a_dir[] = {&c->st, &n, &c->z, &c->p};
     void* a_stats[] = {&c->st};
     if (e == cudaSuccess) e = add_kernel(g, &node, nullptr, (void*)k_init, nb, kT, a_init);
     prev = node;
-    if (e == cudaSuccess) e = add_vcycle(c, g, &prev, c->r, c->z, v0);
+    if (e == cudaSuccess) e = add_vcycle(c, g, &prev, c->r, c->z, v0, true);
     if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_first_dir, nb, kT, a_first);
     prev = node;
     if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_cond, 1, 1, a_cond);
@@ -945,7 +966,7 @@ fvgb_status build_graph(AmgCache* c) {
     bprev = bnode;
     if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_update, nb, kT, a_upd);
     bprev = bnode;
-    if (e == cudaSuccess) e = add_vcycle(c, body, &bprev, c->r, c->z, v1);
+    if (e == cudaSuccess) e = add_vcycle(c, body, &bprev, c->r, c->z, v1, true);
     if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_rz, nb, kT, a_rz);
     bprev = bnode;
     if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_dir, nb, kT, a_dir);

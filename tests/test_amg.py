@@ -206,7 +206,7 @@ def test_multigrid_rejected_by_batches(cuda):
 
     s = gpu_system(cuda, (12, 10, 8))
     n = s["hm"].n
-    b = neon.Batch(s["ls"], [(0, n)])
+    b = neon.Batch(s["ls"], [0, n])
     cfg = abi.SolverCfg(1e-8, 0.0, 100, abi.PREC_FP64, 0.1, 1000, 50, 0, 0, abi.SOLVER_CG, abi.PRECOND_MULTIGRID)
     x = s["x0"].clone()
     assert abi.lib().fvgb_batch_solve(b.handle, abi.ptr(x), C.byref(cfg), None, None) == abi.ERR_UNSUPPORTED
