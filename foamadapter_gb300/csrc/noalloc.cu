@@ -24,6 +24,7 @@
 // The arithmetic and the reduction tree are those of the graph-based FP64 solve
 // in solver.cu (same fma order per row, same 256-thread blocks and rows per thread), so the
 // iterates are the same bits.
+#include <climits>
 #include <cmath>
 #include <mutex>
 
@@ -32,10 +33,11 @@
 namespace {
 
 constexpr int kT = 256;
-constexpr int kRowsPerThread = 8;
-constexpr int kRowsPerBlock = kT * kRowsPerThread;
+constexpr int kRowsPerThread = 8;  // the most rows per thread (systems of 2^18 rows)
 constexpr int kMaxRows = 262144;
-constexpr int kMaxBlocks = kMaxRows / kRowsPerBlock;
+constexpr int kMaxBlocks = kMaxRows / (kT * 4);
+// rows per thread of the reduction tree, as the graph-based solve chooses it for a system of n rows
+__host__ __device__ inline int na_rows_per_thread(int n) { return n >= (1 << 15) ? 8 : 4; }
 constexpr int kMaxDevices = 64;
 
 struct NaState {
@@ -71,8 +73,9 @@ __host__ __device__ inline Scratch carve(double* base) {
 std::mutex g_mu;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
 
-__device__ __forceinline__ int red_row(int j) {
-    return blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5) * (32 * kRowsPerThread) + j * 32 + (threadIdx.x & 31);
+__device__ __forceinline__ int red_row(int j, int n) {
+    const int R = na_rows_per_thread(n);
+    return j < R ? blockIdx.x * (kT * R) + (threadIdx.x >> 5) * (32 * R) + j * 32 + (threadIdx.x & 31) : INT_MAX;
 }
 
 __device__ __forceinline__ double block_tree(double v, double* sm) {
@@ -140,7 +143,7 @@ __global__ void __launch_bounds__(kT)
     double arz = 0.0, arr = 0.0;
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
-        const int i = red_row(j);
+        const int i = red_row(j, n);
         if (i >= n) continue;
         const double di = 1.0 / __ldg(&val[__ldg(&ro[i]) + __ldg(&doff[i])]);
         S.dinv[i] = di;
@@ -188,7 +191,7 @@ __global__ void __launch_bounds__(kT)
     double acc = 0.0;
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
-        const int i = red_row(j);
+        const int i = red_row(j, n);
         if (i >= n) continue;
         const double qi = csr_row(ro, col, val, S.p, i);
         S.q[i] = qi;
@@ -217,7 +220,7 @@ __global__ void __launch_bounds__(kT) k_na_update(double* base, int n, double* _
     double arz = 0.0, arr = 0.0;
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
-        const int i = red_row(j);
+        const int i = red_row(j, n);
         if (i >= n) continue;
         x[i] = fma(alpha, S.p[i], x[i]);
         const double ri = fma(-alpha, S.q[i], S.r[i]);
@@ -262,7 +265,7 @@ __global__ void __launch_bounds__(kT) k_na_dir(double* base, int n) {
     const double beta = S.st->beta;
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
-        const int i = red_row(j);
+        const int i = red_row(j, n);
         if (i >= n) continue;
         S.p[i] = fma(beta, S.p[i], S.dinv[i] * S.r[i]);
     }
@@ -313,7 +316,8 @@ extern "C" fvgb_status fvgb_pcg_csr_noalloc(int32_t n, const int32_t* row_offs, 
     fvgb_status stt = scratch_for_current_device(&base);
     if (stt != FVGB_OK) return stt;
     cudaStream_t s = (cudaStream_t)stream;
-    const unsigned nb = (unsigned)((n + kRowsPerBlock - 1) / kRowsPerBlock);
+    const int rb = kT * na_rows_per_thread(n);
+    const unsigned nb = (unsigned)((n + rb - 1) / rb);
     k_na_reset<<<1, 32, 0, s>>>(base, cfg->rel_tol, cfg->abs_tol, cfg->max_iter);
     k_na_init<<<nb, kT, 0, s>>>(base, n, row_offs, col_idxs, diag_offset, values, rhs, x);
     FVGB_LAUNCH_CHECK("fvgb_pcg_csr_noalloc: init");

@@ -14,7 +14,7 @@
 // Batches.  A system may hold several independent cases (a block-diagonal
 // matrix); case c owns rows [begin_c, end_c).  Every kernel is ONE launch
 // over all cases: a block map assigns each 256-thread block to one case and
-// 2048 consecutive rows of it, every case keeps its own CG scalars, and
+// 256*R consecutive rows of it, every case keeps its own CG scalars, and
 // converged cases idle.  A single solve is a batch of one case.
 //
 // Each solve is one CUDA graph: an init kernel, a device-side WHILE
@@ -25,7 +25,7 @@
 // iteration.  Every loop is bounded by an iteration cap.
 //
 // Reductions are deterministic.  Block b of case c owns rows
-// row0_b + (t/32)*32R + j*32 + t%32 (thread t, j < R = kRowsPerThread); a
+// row0_b + (t/32)*32R + j*32 + t%32 (thread t, j < R = rows_per_thread(case rows)); a
 // thread sums its rows sequentially, warp 0 sums the 256 partials (lane l:
 // l, l+32, ..., l+224) and a xor butterfly finishes; the last block of the case
 // to arrive sums the case's block partials in index order with the same tree.
@@ -41,8 +41,19 @@
 namespace {
 
 constexpr int kT = 256;
-constexpr int kRowsPerThread = 8;
+constexpr int kRowsPerThread = 8;  // the most rows per thread of any case
 constexpr int kRowsPerBlock = kT * kRowsPerThread;
+
+// Rows per thread of a case's reduction tree: 8 (2048-row blocks, half the
+// block reductions) for cases of at least kBigCaseRows rows; 4 for smaller
+// cases, whose single solves run the persistent kernel and need the blocks
+// to fill the GPU.  A function of the case's own size, so a case solved in a
+// batch keeps the tree it has alone.  Measured on 512 cases of 4 k-262 k rows:
+// a threshold of 2^15 rows keeps 97% of the packed throughput of 8 rows
+// everywhere (7,797 against 8,006 case-steps/s) and speeds single small
+// solves up 8%; 2^18 speeds them up 27% but costs 13% packed.
+constexpr int kBigCaseRows = 1 << 15;
+__host__ __device__ inline int rows_per_thread(int64_t case_rows) { return case_rows >= kBigCaseRows ? 8 : 4; }
 
 struct SolverParams {
     double* x;
@@ -82,10 +93,11 @@ struct Layout {
     CaseState* cases;
     BatchState* bs;
     fvgb_solver_stats* stats;  // [ncases] internal copy for the synchronous API
+    const int32_t* case_rpt;   // [ncases] rows per thread of every case's tree
 };
 
 struct Blk {
-    int c, row0, end, nbc, blk0;
+    int c, row0, end, nbc, blk0, R;
 };
 
 __device__ __forceinline__ Blk blk_info(const Layout& L) {
@@ -95,11 +107,14 @@ __device__ __forceinline__ Blk blk_info(const Layout& L) {
     k.end = __ldg(&L.case_end[k.c]);
     k.blk0 = __ldg(&L.case_blk0[k.c]);
     k.nbc = __ldg(&L.case_blk0[k.c + 1]) - k.blk0;
+    k.R = __ldg(&L.case_rpt[k.c]);
     return k;
 }
 
+// Row j of this thread in its block; past the case's end (skipped by every
+// caller's `i >= k.end` test) when j is beyond the case's rows per thread.
 __device__ __forceinline__ int blk_row(const Blk& k, int j) {
-    return k.row0 + (threadIdx.x >> 5) * (32 * kRowsPerThread) + j * 32 + (threadIdx.x & 31);
+    return j < k.R ? k.row0 + (threadIdx.x >> 5) * (32 * k.R) + j * 32 + (threadIdx.x & 31) : INT_MAX;
 }
 
 // Block sum of one value per thread; result valid in warp 0 (every lane).
@@ -1412,11 +1427,11 @@ cudaError_t launch_variant(const void* fn, unsigned grid, cudaStream_t s, A... a
 // ------------------------------------------------------ persistent solves (one case)
 // For systems small enough that launch latency dominates an iteration, ONE
 // cooperative launch runs the whole solve.  A persistent block has 1024 threads
-// and walks the 2048-row virtual blocks vb = blockIdx.x, blockIdx.x + gridDim.x,
-// ...; thread t computes rows vb*2048 + t and vb*2048 + 1024 + t.  Dot products
-// are staged in shared memory and summed by 256 "tree threads" with exactly the
-// row assignment and order of the graph kernels (8 rows per thread, then the
-// block tree), so the
+// and walks the 256*R-row virtual blocks vb = blockIdx.x, blockIdx.x + gridDim.x,
+// ...; thread t computes rows vb*256R + t (and vb*256R + 1024 + t when R = 8).
+// Dot products are staged in shared memory and summed by 256 "tree threads"
+// with exactly the row assignment and order of the graph kernels (R rows per
+// thread, then the block tree), so the
 // per-virtual-block partials, and after a grid barrier the final trees that
 // EVERY block computes over all partials, are the bits of the graph path; all
 // blocks then take identical decisions.  Data written during the kernel is
@@ -1424,8 +1439,7 @@ cudaError_t launch_variant(const void* fn, unsigned grid, cudaStream_t s, A... a
 // time-out a block raises the abort flag, every block leaves at its next
 // barrier and the solve reports FVGB_ERR_CUDA.
 constexpr int kPT = 1024;
-constexpr int kRowsPerPT = kRowsPerBlock / kPT;  // rows of a virtual block per persistent thread
-static_assert(kRowsPerBlock % kPT == 0, "a virtual block is a whole number of rows per thread");
+static_assert((kT * 4) % kPT == 0, "a virtual block is a whole number of rows per thread");
 
 struct GridBar {
     unsigned long long count;  // arrivals since the launch (never reset inside it)
@@ -1464,7 +1478,8 @@ __device__ __forceinline__ bool grid_sync(GridBar* g, unsigned long long target)
 }
 
 // row (within a virtual block) of tree thread tp's j-th row: the graph kernels' blk_row
-__device__ __forceinline__ int tree_row(int tp, int j) { return (tp >> 5) * (32 * kRowsPerThread) + j * 32 + (tp & 31); }
+template <int R>
+__device__ __forceinline__ int tree_row(int tp, int j) { return (tp >> 5) * (32 * R) + j * 32 + (tp & 31); }
 
 // block_tree over the partials of threads 0..kT-1 of a kPT-thread block; valid in warp 0
 __device__ __forceinline__ double tree256(double v, double* sm) {
@@ -1545,11 +1560,12 @@ struct PcgShared {
     int done;
 };
 
+template <int R>
 __global__ void __launch_bounds__(kPT, 1)
     k_pcg_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
                      double* dinv, double* r, double* p, double* q, double* z, double* pa, double* pb, GridBar* gb,
                      int nvb) {
-    __shared__ double sA[kRowsPerBlock], sB[kRowsPerBlock], sm[kT], sm2[kT], cell;
+    __shared__ double sA[(kT * R)], sB[(kT * R)], sm[kT], sm2[kT], cell;
     __shared__ PcgShared sh;
     const int n = m.n, T = threadIdx.x;
     const SolverParams prm = L.bs->prm;
@@ -1558,9 +1574,9 @@ __global__ void __launch_bounds__(kPT, 1)
     unsigned long long epoch = 0;
     // init: r = b - A x, z = p = dinv r, r.z, r.r
     for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-        for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+        for (int h = 0; h < (kT * R / kPT); ++h) {  // the thread's rows T + h*kPT of the virtual block
             const int t = T + h * kPT;
-            const int i = vb * kRowsPerBlock + t;
+            const int i = vb * (kT * R) + t;
             double ri = 0.0, zi = 0.0;
             if (i < n) {
                 const double di = 1.0 / __ldg(&val[__ldg(&m.diag_pos[i])]);
@@ -1577,9 +1593,9 @@ __global__ void __launch_bounds__(kPT, 1)
         double arz = 0.0, arr = 0.0;
         if (T < kT)
 #pragma unroll
-            for (int j = 0; j < kRowsPerThread; ++j) {
-                const int rr = tree_row(T, j);
-                if (vb * kRowsPerBlock + rr >= n) continue;
+            for (int j = 0; j < R; ++j) {
+                const int rr = tree_row<R>(T, j);
+                if (vb * (kT * R) + rr >= n) continue;
                 arz = fma(sA[rr], sB[rr], arz);
                 arr = fma(sA[rr], sA[rr], arr);
             }
@@ -1616,9 +1632,9 @@ __global__ void __launch_bounds__(kPT, 1)
     while (!done) {
         // q = A p, p.q
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-            for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+            for (int h = 0; h < (kT * R / kPT); ++h) {  // the thread's rows T + h*kPT of the virtual block
                 const int t = T + h * kPT;
-                const int i = vb * kRowsPerBlock + t;
+                const int i = vb * (kT * R) + t;
                 double pi = 0.0, qi = 0.0;
                 if (i < n) {
                     qi = spmv_row_cg(m, val, p, i);
@@ -1632,9 +1648,9 @@ __global__ void __launch_bounds__(kPT, 1)
             double acc = 0.0;
             if (T < kT)
 #pragma unroll
-                for (int j = 0; j < kRowsPerThread; ++j) {
-                    const int rw = tree_row(T, j);
-                    if (vb * kRowsPerBlock + rw < n) acc = fma(sA[rw], sB[rw], acc);
+                for (int j = 0; j < R; ++j) {
+                    const int rw = tree_row<R>(T, j);
+                    if (vb * (kT * R) + rw < n) acc = fma(sA[rw], sB[rw], acc);
                 }
             const double ba = tree256(acc, sm);
             if (T == 0) pa[vb] = ba;
@@ -1658,9 +1674,9 @@ __global__ void __launch_bounds__(kPT, 1)
         const double alpha = sh.alpha;
         // x += alpha p, r -= alpha q, z = dinv r, r.z, r.r
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-            for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+            for (int h = 0; h < (kT * R / kPT); ++h) {  // the thread's rows T + h*kPT of the virtual block
                 const int t = T + h * kPT;
-                const int i = vb * kRowsPerBlock + t;
+                const int i = vb * (kT * R) + t;
                 double ri = 0.0, zi = 0.0;
                 if (i < n) {
                     x[i] = fma(alpha, __ldcg(&p[i]), __ldcg(&x[i]));
@@ -1676,9 +1692,9 @@ __global__ void __launch_bounds__(kPT, 1)
             double arz = 0.0, arr = 0.0;
             if (T < kT)
 #pragma unroll
-                for (int j = 0; j < kRowsPerThread; ++j) {
-                    const int rw = tree_row(T, j);
-                    if (vb * kRowsPerBlock + rw >= n) continue;
+                for (int j = 0; j < R; ++j) {
+                    const int rw = tree_row<R>(T, j);
+                    if (vb * (kT * R) + rw >= n) continue;
                     arz = fma(sA[rw], sB[rw], arz);
                     arr = fma(sA[rw], sA[rw], arr);
                 }
@@ -1716,9 +1732,9 @@ __global__ void __launch_bounds__(kPT, 1)
         const double beta = sh.beta;
         // p = z + beta p
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-            for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+            for (int h = 0; h < (kT * R / kPT); ++h) {  // the thread's rows T + h*kPT of the virtual block
                 const int t = T + h * kPT;
-                const int i = vb * kRowsPerBlock + t;
+                const int i = vb * (kT * R) + t;
                 if (i < n) p[i] = fma(beta, __ldcg(&p[i]), __ldcg(&z[i]));
             }
         }
@@ -1790,12 +1806,13 @@ struct IrShared {
     int done, inner, brk;
 };
 
+template <int R>
 __global__ void __launch_bounds__(kPT, 1)
     k_ir_persistent(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
                     float* a32, float* ev, float* dinv, double* r0, float* rh, float* y, float* pbuf0, float* pbuf1,
                     float* z, float* q, double* pa, double* pb, double* pc, GridBar* gb, int nvb) {
-    __shared__ double sD[kRowsPerBlock], sm[kT], sm3[kT], cell;
-    __shared__ float sF1[kRowsPerBlock], sF2[kRowsPerBlock], smf[kT];
+    __shared__ double sD[(kT * R)], sm[kT], sm3[kT], cell;
+    __shared__ float sF1[(kT * R)], sF2[(kT * R)], smf[kT];
     __shared__ unsigned int sflags;
     __shared__ IrShared sh;
     const int n = m.n, T = threadIdx.x;
@@ -1809,9 +1826,9 @@ __global__ void __launch_bounds__(kPT, 1)
     if (T == 0) sflags = 0u;
     __syncthreads();
     for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-        for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+        for (int h = 0; h < (kT * R / kPT); ++h) {  // the thread's rows T + h*kPT of the virtual block
             const int t = T + h * kPT;
-            const int i = vb * kRowsPerBlock + t;
+            const int i = vb * (kT * R) + t;
             double ri = 0.0;
             float di = 0.0f;
             if (i < n) {
@@ -1850,9 +1867,9 @@ __global__ void __launch_bounds__(kPT, 1)
         double asr = 0.0;
         if (T < kT)
 #pragma unroll
-            for (int j = 0; j < kRowsPerThread; ++j) {
-                const int rw = tree_row(T, j);
-                if (vb * kRowsPerBlock + rw < n) asr = fma(sD[rw] * (double)fabsf(sF1[rw]), sD[rw], asr);
+            for (int j = 0; j < R; ++j) {
+                const int rw = tree_row<R>(T, j);
+                if (vb * (kT * R) + rw < n) asr = fma(sD[rw] * (double)fabsf(sF1[rw]), sD[rw], asr);
             }
         const double ba = tree256(asr, sm);
         if (T == 0) pa[vb] = ba;
@@ -1881,9 +1898,9 @@ __global__ void __launch_bounds__(kPT, 1)
             // x += y / sig
             const double is = sh.isig;
             for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-                for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                for (int h = 0; h < (kT * R / kPT); ++h) {  // the thread's rows T + h*kPT of the virtual block
                     const int t = T + h * kPT;
-                    const int i = vb * kRowsPerBlock + t;
+                    const int i = vb * (kT * R) + t;
                     if (i < n) x[i] = fma((double)__ldcg(&y[i]), is, __ldcg(&x[i]));
                 }
             }
@@ -1901,9 +1918,9 @@ __global__ void __launch_bounds__(kPT, 1)
         const double nsig_all = sh.nsig;
         // residual: r = b - A x (FP64), rh = sign*(float)(sig r), y = 0, z = |dinv| rh
         for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-            for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+            for (int h = 0; h < (kT * R / kPT); ++h) {  // the thread's rows T + h*kPT of the virtual block
                 const int t = T + h * kPT;
-                const int i = vb * kRowsPerBlock + t;
+                const int i = vb * (kT * R) + t;
                 double ri = 0.0;
                 float di = 0.0f, rhi = 0.0f;
                 if (i < n) {
@@ -1926,9 +1943,9 @@ __global__ void __launch_bounds__(kPT, 1)
             float arho = 0.0f;
             if (T < kT)
 #pragma unroll
-                for (int j = 0; j < kRowsPerThread; ++j) {
-                    const int rw = tree_row(T, j);
-                    if (vb * kRowsPerBlock + rw >= n) continue;
+                for (int j = 0; j < R; ++j) {
+                    const int rw = tree_row<R>(T, j);
+                    if (vb * (kT * R) + rw >= n) continue;
                     const double rv = sD[rw];
                     arr = fma(rv, rv, arr);
                     asr = fma(rv * (double)fabsf(sF2[rw]), rv, asr);
@@ -2000,9 +2017,9 @@ __global__ void __launch_bounds__(kPT, 1)
             const DirMode dm = sh.dm;
             // direction (into pnext unless p is taken as stored), q = A p, p.q
             for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-                for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                for (int h = 0; h < (kT * R / kPT); ++h) {  // the thread's rows T + h*kPT of the virtual block
                     const int t = T + h * kPT;
-                    const int i = vb * kRowsPerBlock + t;
+                    const int i = vb * (kT * R) + t;
                     float pi = 0.0f, qi = 0.0f;
                     if (i < n) {
                         pi = dir_of(dm, __ldcg(&pcur[i]), dm.kind == 0 ? 0.0f : __ldcg(&z[i]));
@@ -2017,9 +2034,9 @@ __global__ void __launch_bounds__(kPT, 1)
                 float acc = 0.0f;
                 if (T < kT)
 #pragma unroll
-                    for (int j = 0; j < kRowsPerThread; ++j) {
-                        const int rw = tree_row(T, j);
-                        if (vb * kRowsPerBlock + rw < n) acc = fmaf(sF1[rw], sF2[rw], acc);
+                    for (int j = 0; j < R; ++j) {
+                        const int rw = tree_row<R>(T, j);
+                        if (vb * (kT * R) + rw < n) acc = fmaf(sF1[rw], sF2[rw], acc);
                     }
                 const float ba = tree256f(acc, smf);
                 if (T == 0) pa[vb] = (double)ba;
@@ -2053,9 +2070,9 @@ __global__ void __launch_bounds__(kPT, 1)
             const float fa = sh.fa;
             // y += alpha p, rh -= alpha q, z = |dinv| rh, rh.z
             for (int vb = blockIdx.x; vb < nvb; vb += (int)G) {
-                for (int h = 0; h < kRowsPerPT; ++h) {  // the thread's rows T + h*kPT of the virtual block
+                for (int h = 0; h < (kT * R / kPT); ++h) {  // the thread's rows T + h*kPT of the virtual block
                     const int t = T + h * kPT;
-                    const int i = vb * kRowsPerBlock + t;
+                    const int i = vb * (kT * R) + t;
                     float ri = 0.0f, zi = 0.0f;
                     if (i < n) {
                         y[i] = fmaf(fa, __ldcg(&pcur[i]), __ldcg(&y[i]));
@@ -2071,9 +2088,9 @@ __global__ void __launch_bounds__(kPT, 1)
                 float acc = 0.0f;
                 if (T < kT)
 #pragma unroll
-                    for (int j = 0; j < kRowsPerThread; ++j) {
-                        const int rw = tree_row(T, j);
-                        if (vb * kRowsPerBlock + rw < n) acc = fmaf(sF1[rw], sF2[rw], acc);
+                    for (int j = 0; j < R; ++j) {
+                        const int rw = tree_row<R>(T, j);
+                        if (vb * (kT * R) + rw < n) acc = fmaf(sF1[rw], sF2[rw], acc);
                     }
                 const float ba = tree256f(acc, smf);
                 if (T == 0) pa[vb] = (double)ba;
@@ -2212,21 +2229,25 @@ fvgb_status cache_create(const fvgb_ls* ls, int ncases, const int32_t* ranges, S
     c->n = ls->mesh->v.n;
     c->ncases = ncases;
     c->whole = ncases == 1 && ranges[0] == 0 && ranges[1] == c->n;
-    std::vector<int32_t> blk_case, blk_row0, case_end(ncases), case_blk0(ncases + 1);
+    std::vector<int32_t> blk_case, blk_row0, case_end(ncases), case_blk0(ncases + 1), case_rpt(ncases);
     for (int k = 0; k < ncases; ++k) {
         case_blk0[k] = (int32_t)blk_case.size();
         case_end[k] = ranges[2 * k + 1];
         const int32_t nr = ranges[2 * k + 1] - ranges[2 * k];
-        const int32_t nbk = nr > 0 ? (nr + kRowsPerBlock - 1) / kRowsPerBlock : 1;  // an empty case gets one idle block
+        case_rpt[k] = rows_per_thread(nr);
+        const int32_t rb = kT * case_rpt[k];
+        const int32_t nbk = nr > 0 ? (nr + rb - 1) / rb : 1;  // an empty case gets one idle block
         for (int32_t b = 0; b < nbk; ++b) {
             blk_case.push_back(k);
-            blk_row0.push_back(ranges[2 * k] + b * kRowsPerBlock);
+            blk_row0.push_back(ranges[2 * k] + b * rb);
         }
     }
     case_blk0[ncases] = (int32_t)blk_case.size();
     c->nb = (int)blk_case.size();
-    int32_t *d_bc = nullptr, *d_br = nullptr, *d_ce = nullptr, *d_cb = nullptr;
+    int32_t *d_bc = nullptr, *d_br = nullptr, *d_ce = nullptr, *d_cb = nullptr, *d_rpt = nullptr;
     cudaError_t e = calloc_dev(c, &d_bc, blk_case.size());
+    if (e == cudaSuccess) e = calloc_dev(c, &d_rpt, case_rpt.size());
+    if (e == cudaSuccess) e = cudaMemcpy(d_rpt, case_rpt.data(), 4 * case_rpt.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = calloc_dev(c, &d_br, blk_row0.size());
     if (e == cudaSuccess) e = calloc_dev(c, &d_ce, case_end.size());
     if (e == cudaSuccess) e = calloc_dev(c, &d_cb, case_blk0.size());
@@ -2249,7 +2270,7 @@ fvgb_status cache_create(const fvgb_ls* ls, int ncases, const int32_t* ranges, S
         fvgb_solver_cache_free(c);
         return cuda_fail(e, "solver workspace");
     }
-    c->L = Layout{d_bc, d_br, d_ce, d_cb, cs, bs, st};
+    c->L = Layout{d_bc, d_br, d_ce, d_cb, cs, bs, st, d_rpt};
     *out = c;
     return FVGB_OK;
 }
@@ -2684,8 +2705,8 @@ int persistent_grid(SolverCache* c, bool mixed) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ir_persistent, kPT, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent, kPT, 0);
+        if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ir_persistent<8>, kPT, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent<8>, kPT, 0);
         g = (!coop || per_sm <= 0) ? -1 : sms * per_sm;
     }
     return g;
@@ -2790,10 +2811,12 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
             // k_ir_persistent(L, m, val, b, a32, ev, dinv, r0, rh, y, pbuf0, pbuf1, z, q, pa, pb, pc, gb, nvb)
             void* args[] = {&L,     &m,    &val,   &b,     &c->ah, &c->ev, &c->dinvf, &c->r0, &c->rh, &c->y,
                             &c->pf, &c->pf2, &c->zf, &c->qf, &c->pa, &c->pb, &c->pc,   &c->bar, &nvb};
-            FVGB_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_ir_persistent, dim3(grid), dim3(kPT), args, 0, s));
+            const void* fn = rows_per_thread(c->n) == 8 ? (const void*)k_ir_persistent<8> : (const void*)k_ir_persistent<4>;
+            FVGB_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kPT), args, 0, s));
         } else {
             void* args[] = {&L, &m, &val, &b, &c->dinv, &c->r, &c->p, &c->q, &c->z, &c->pa, &c->pb, &c->bar, &nvb};
-            FVGB_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_pcg_persistent, dim3(grid), dim3(kPT), args, 0, s));
+            const void* fn = rows_per_thread(c->n) == 8 ? (const void*)k_pcg_persistent<8> : (const void*)k_pcg_persistent<4>;
+            FVGB_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kPT), args, 0, s));
         }
         k_finish<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L);
         FVGB_LAUNCH_CHECK("fvgb_solve: finish");

@@ -26,8 +26,12 @@ enum { TERM_DDT = 0, TERM_LAPLACIAN = 1, TERM_DIV = 2, TERM_SOURCE = 3, TERM_EXP
 enum { ST_OK = 0, ST_NOT_CONVERGED = 3, ST_BREAKDOWN = 4, ST_UNSUPPORTED = 6 };
 
 #define RED_THREADS 256
-#define RED_ROWS_PER_THREAD 8
+/* rows per thread of the reduction tree: 8 for systems of at least 2^18 rows,
+ * 4 below (the GPU solver's choice per case); set by or_solve for its system */
+static int g_red_rpt = 8;
+#define RED_ROWS_PER_THREAD g_red_rpt
 #define RED_ROWS_PER_BLOCK (RED_THREADS * RED_ROWS_PER_THREAD)
+static int red_rows_per_thread(int32_t n) { return n >= (1 << 15) ? 8 : 4; }
 
 void or_set_threads(int32_t nthreads) {
 #ifdef _OPENMP
@@ -1151,6 +1155,7 @@ static int32_t solve_mixed_bicgstab(const or_csr* A, const double* val, const do
 
 int32_t or_solve(const or_csr* A, const double* values, const double* rhs, double* x,
                  const or_solver_cfg* cfg, or_solver_stats* stats) {
+    g_red_rpt = red_rows_per_thread(A->n);
     if (cfg->method == 1) {
         if (cfg->precision == 1) return solve_mixed_bicgstab(A, values, rhs, x, cfg, stats);
         return solve_bicgstab(A, values, rhs, x, cfg, stats);
