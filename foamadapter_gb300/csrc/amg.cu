@@ -31,6 +31,13 @@
 // coarse correction and one more damped-Jacobi sweep; the coarsest level is
 // solved exactly with the dense inverse.  Pre- and post-smoothing are the same
 // symmetric sweep, so M is symmetric positive definite and CG applies.
+// Kernels: the first sweep of level 0 is formed by the CG kernels that produce
+// r (k_init, k_update), a coarse level's by the restriction that produces its
+// right-hand side; the residual is one gather per slot (k_resid); level 0
+// adds the coarse correction (k_prolong) before its second sweep (k_post),
+// coarser levels form it inside the sweep (k_post_fused); the coarsest level
+// runs in one block (k_tail, which can take more levels: kTailRows).  Coarse
+// levels are sliced ELL like the system matrix.
 //
 // The solve is one CUDA graph (init, a device-side while loop over the CG
 // iteration with the V-cycle inside, bounded by max_iter).  Its stopping test
