@@ -553,7 +553,8 @@ def run_cavity(args):
     out = {}
     fields = {}
     for name, prec, pc in (("fp64", abi.PREC_FP64, abi.PRECOND_JACOBI), ("mixed", abi.PREC_MIXED_IR, abi.PRECOND_JACOBI),
-                           ("fp64_multigrid", abi.PREC_FP64, abi.PRECOND_MULTIGRID)):
+                           ("fp64_multigrid", abi.PREC_FP64, abi.PRECOND_MULTIGRID),
+                           ("multigrid_fp32_vcycle", abi.PREC_MIXED_IR, abi.PRECOND_MULTIGRID)):
         case = apps.CavityPiso(n=512, precision=prec, preconditioner=pc)
         case.step()                                     # warm-up (builds the solver graphs)
         torch.cuda.synchronize()
@@ -582,6 +583,8 @@ def run_cavity(args):
     out["err_vs_fp64"] = err(pm, Um)
     out["speedup_step_multigrid"] = out["fp64"]["ms_per_step"] / out["fp64_multigrid"]["ms_per_step"]
     out["err_vs_fp64_multigrid"] = err(pg, Ug)
+    out["speedup_step_multigrid_fp32_vcycle"] = out["fp64"]["ms_per_step"] / out["multigrid_fp32_vcycle"]["ms_per_step"]
+    out["err_vs_fp64_multigrid_fp32_vcycle"] = err(*fields["multigrid_fp32_vcycle"])
     return {"workload": f"lid-driven cavity PISO 512x512x1, +-5% jitter, dt 5e-4, 2 correctors, {nsteps} steps",
             "pressure_solve_to": "1e-8 relative FP64 residual", **out}
 
@@ -607,13 +610,15 @@ def run_multigrid(args):
     x0 = T.internal.clone()
     out = {}
     # --profile: the V-cycles only (no conditional graphs, so ncu can capture every kernel)
-    for name, pc in () if args.profile else (("jacobi", abi.PRECOND_JACOBI), ("multigrid", abi.PRECOND_MULTIGRID)):
+    legs = (("jacobi", abi.PRECOND_JACOBI, abi.PREC_FP64), ("multigrid", abi.PRECOND_MULTIGRID, abi.PREC_FP64),
+            ("multigrid_fp32_vcycle", abi.PRECOND_MULTIGRID, abi.PREC_MIXED_IR))
+    for name, pc, prec in () if args.profile else legs:
         times = []
         for rep in range(4):
             x = x0.clone()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            st = ls.solve(x, rel_tol=HEAT["rel_tol"], max_iter=4000, preconditioner=pc)
+            st = ls.solve(x, rel_tol=HEAT["rel_tol"], max_iter=4000, preconditioner=pc, precision=prec)
             torch.cuda.synchronize()
             times.append(1e3 * (time.perf_counter() - t0))
         out[name] = {"ms": min(times[1:]), "first_ms": times[0], "iters": st.num_iter}
@@ -632,7 +637,8 @@ def run_multigrid(args):
     return {"workload": f"multigrid-preconditioned CG on the {args.n}^3 heat system, to 1e-8",
             "levels": [[int(rows[i]), int(nnz[i])] for i in range(nl.value)],
             "vcycle_ms_incl_graph_build": vms, **out,
-            "speedup_solve": out["jacobi"]["ms"] / out["multigrid"]["ms"] if out else None}
+            "speedup_solve": out["jacobi"]["ms"] / out["multigrid"]["ms"] if out else None,
+            "speedup_solve_fp32_vcycle": out["jacobi"]["ms"] / out["multigrid_fp32_vcycle"]["ms"] if out else None}
 
 
 def batch_cases(ncases, seed=4):

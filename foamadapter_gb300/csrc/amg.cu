@@ -48,6 +48,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "internal.cuh"
@@ -199,10 +200,33 @@ struct Level {
     int *gptr = nullptr, *gsrc = nullptr;  // sums forming the next level's values
     int* gdst = nullptr;                   // the next level's slot of each sum
     int nnz_next = 0;
+    int64_t slots = 0;                     // value slots (level 0: the system's m_len)
     double *b = nullptr, *x = nullptr, *xo = nullptr, *r = nullptr;
+    // FP32 copies for the FP32 V-cycle (allocated at the first mixed-precision solve)
+    float *valf = nullptr, *dinvf = nullptr, *bf = nullptr, *xf = nullptr, *xof = nullptr, *rf = nullptr;
+    // typed views used by the V-cycle builder
+    template <class T> T* vals() const;
+    template <class T> T* dinvs() const;
+    template <class T> T* bs() const;
+    template <class T> T* xs() const;
+    template <class T> T* xos() const;
+    template <class T> T* rs() const;
 };
+template <> double* Level::vals<double>() const { return val; }
+template <> float* Level::vals<float>() const { return valf; }
+template <> double* Level::dinvs<double>() const { return dinv; }
+template <> float* Level::dinvs<float>() const { return dinvf; }
+template <> double* Level::bs<double>() const { return b; }
+template <> float* Level::bs<float>() const { return bf; }
+template <> double* Level::xs<double>() const { return x; }
+template <> float* Level::xs<float>() const { return xf; }
+template <> double* Level::xos<double>() const { return xo; }
+template <> float* Level::xos<float>() const { return xof; }
+template <> double* Level::rs<double>() const { return r; }
+template <> float* Level::rs<float>() const { return rf; }
 
-struct TailLevel;
+template <class T>
+struct TailLevelT;
 
 }  // namespace
 
@@ -215,8 +239,14 @@ struct AmgCache {
     double *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *part = nullptr;
     AmgState* st = nullptr;
     int tail_from = 1;             // first level run by the single-block tail
-    TailLevel* tail = nullptr;     // device descriptors of levels tail_from..L-1
+    TailLevelT<double>* tail = nullptr;    // device descriptors of levels tail_from..L-1
     cudaGraphExec_t graph = nullptr;
+    // the FP32 V-cycle of mixed-precision solves
+    bool f32 = false;              // FP32 copies allocated
+    uint64_t f32_version = 0;      // matrix version the FP32 copies were made from
+    float* ainvf = nullptr;
+    TailLevelT<float>* tailf = nullptr;
+    cudaGraphExec_t graph32 = nullptr;
     std::vector<void*> allocs;
     int nblk = 0;
 };
@@ -238,11 +268,13 @@ cudaError_t upload(AmgCache* c, T** p, const std::vector<T>& h) {
 }
 
 // ------------------------------------------------------------ row access
-// Row i of a sliced-ELL matrix: f(column, value) for every slot, the column
-// and value loads of the first 8 slots issued before the caller's gathers.
-struct EllRows {  // level 0: the system's sliced-ELL matrix
+// Row i of a sliced-ELL matrix with values of type V: f(column, value) for
+// every slot, the column and value loads of the first slots issued before the
+// caller's gathers.
+template <class V>
+struct EllRowsT {  // level 0: the system's sliced-ELL matrix (or its FP32 copy)
     MeshView m;
-    const double* val;
+    const V* val;
     template <class F>
     __device__ __forceinline__ void each(int i, F f) const {
         const int slice = i >> 5;
@@ -250,11 +282,11 @@ struct EllRows {  // level 0: the system's sliced-ELL matrix
         const int base = b0 + (i & 31);
         const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
         int col[8];
-        double a[8];
+        V a[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             col[k] = i;
-            a[k] = 0.0;
+            a[k] = V(0);
             if (k < w) {
                 col[k] = slot_col(m, base + k * 32, i);
                 a[k] = __ldg(&val[base + k * 32]);
@@ -267,10 +299,11 @@ struct EllRows {  // level 0: the system's sliced-ELL matrix
     }
 };
 
-struct SellRows {  // levels >= 1
+template <class V>
+struct SellRowsT {  // levels >= 1
     const int* ptr;
     const int* col;
-    const double* val;
+    const V* val;
     template <class F>
     __device__ __forceinline__ void each(int i, F f) const {
         const int slice = i >> 5;
@@ -279,11 +312,11 @@ struct SellRows {  // levels >= 1
         const int w = (__ldg(&ptr[slice + 1]) - b0) >> 5;
         constexpr int P = 16;  // coarse rows hold up to ~20 entries
         int c[P];
-        double a[P];
+        V a[P];
 #pragma unroll
         for (int k = 0; k < P; ++k) {
             c[k] = i;
-            a[k] = 0.0;
+            a[k] = V(0);
             if (k < w) {
                 c[k] = __ldg(&col[base + k * 32]);
                 a[k] = __ldg(&val[base + k * 32]);
@@ -295,6 +328,12 @@ struct SellRows {  // levels >= 1
         for (int k = P; k < w; ++k) f(__ldg(&col[base + k * 32]), __ldg(&val[base + k * 32]));
     }
 };
+
+using EllRows = EllRowsT<double>;
+using SellRows = SellRowsT<double>;
+
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
 
 // ------------------------------------------------------------ reductions
 __device__ __forceinline__ double block_sum(double v, double* sm) {
@@ -382,6 +421,9 @@ __global__ void __launch_bounds__(1024) k_gauss_jordan(int n, double* __restrict
 }
 
 // ------------------------------------------------------------ V-cycle
+// The V-cycle kernels run in the type T of the V-cycle: double, or float for
+// the FP32 V-cycle of a mixed-precision solve (the CG around it stays FP64).
+
 // Level 0's pre-smoothing sweep from zero: x = w D^-1 b
 __global__ void __launch_bounds__(kT)
     k_smooth0(const AmgState* st, int n, const double* __restrict__ dinv, const double* __restrict__ b,
@@ -392,31 +434,30 @@ __global__ void __launch_bounds__(kT)
 }
 
 // r = b - A x
-template <class R>
+template <class R, class T>
 __global__ void __launch_bounds__(kT)
-    k_resid(const AmgState* st, R rows, int n, const double* __restrict__ b, const double* __restrict__ x,
-            double* __restrict__ r) {
+    k_resid(const AmgState* st, R rows, int n, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r) {
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
     if (i >= n) return;
-    double s = 0.0;
-    rows.each(i, [&](int j, double a) { s = fma(a, __ldg(&x[j]), s); });
+    T s = T(0);
+    rows.each(i, [&](int j, T a) { s = fmaT(a, __ldg(&x[j]), s); });
     r[i] = __ldg(&b[i]) - s;
 }
 
 // b_c[I] = sum of r over the rows of aggregate I, and the coarse level's
 // pre-smoothing sweep from zero x_c = w D_c^-1 b_c
+template <class T>
 __global__ void __launch_bounds__(kT)
     k_restrict(const AmgState* st, int nc, const int* __restrict__ mptr, const int* __restrict__ mem,
-               const double* __restrict__ r, const double* __restrict__ dinv_c, double* __restrict__ bc,
-               double* __restrict__ xc) {
+               const T* __restrict__ r, const T* __restrict__ dinv_c, T* __restrict__ bc, T* __restrict__ xc) {
     if (done_flag(st)) return;
     const int c = blockIdx.x * kT + threadIdx.x;
     if (c >= nc) return;
-    double s = 0.0;
+    T s = T(0);
     for (int k = __ldg(&mptr[c]); k < __ldg(&mptr[c + 1]); ++k) s += __ldg(&r[__ldg(&mem[k])]);
     bc[c] = s;
-    xc[c] = kOmega * __ldg(&dinv_c[c]) * s;
+    xc[c] = T(kOmega) * __ldg(&dinv_c[c]) * s;
 }
 
 // The small levels t..L-1 of a V-cycle in one block of 1024 threads: their
@@ -424,66 +465,69 @@ __global__ void __launch_bounds__(kT)
 // the same steps with barriers between them.  Level t's b and x (its
 // pre-smoothing sweep) come from the restriction above it; its xo is the
 // correction handed back up.
-struct TailLevel {
+template <class T>
+struct TailLevelT {
     int n;
-    SellRows A;
-    const double* dinv;
+    SellRowsT<T> A;
+    const T* dinv;
     const int* agg;   // to level l+1
     const int* mptr;  // members of level l+1's rows
     const int* mem;
-    double *b, *x, *xo, *r;
+    T *b, *x, *xo, *r;
 };
 
+template <class T>
 __global__ void __launch_bounds__(1024)
-    k_tail(const AmgState* st, const TailLevel* __restrict__ lv, int nl, const double* __restrict__ ainv) {
+    k_tail(const AmgState* st, const TailLevelT<T>* __restrict__ lv, int nl, const T* __restrict__ ainv) {
     if (done_flag(st)) return;
-    const int T = threadIdx.x, NT = blockDim.x;
+    const int Tt = threadIdx.x, NT = blockDim.x;
     for (int l = 0; l + 1 < nl; ++l) {  // down
-        const TailLevel& F = lv[l];
-        const TailLevel& C = lv[l + 1];
-        for (int i = T; i < F.n; i += NT) {
-            double s = 0.0;
-            F.A.each(i, [&](int j, double a) { s = fma(a, F.x[j], s); });
+        const TailLevelT<T>& F = lv[l];
+        const TailLevelT<T>& C = lv[l + 1];
+        for (int i = Tt; i < F.n; i += NT) {
+            T s = T(0);
+            F.A.each(i, [&](int j, T a) { s = fmaT(a, F.x[j], s); });
             F.r[i] = F.b[i] - s;
         }
         __syncthreads();
-        for (int c = T; c < C.n; c += NT) {
-            double s = 0.0;
+        for (int c = Tt; c < C.n; c += NT) {
+            T s = T(0);
             for (int k = F.mptr[c]; k < F.mptr[c + 1]; ++k) s += F.r[F.mem[k]];
             C.b[c] = s;
-            C.x[c] = kOmega * C.dinv[c] * s;
+            C.x[c] = T(kOmega) * C.dinv[c] * s;
         }
         __syncthreads();
     }
     {  // coarsest: xo = A^-1 b, a warp per row
-        const TailLevel& B = lv[nl - 1];
-        const int lane = T & 31;
-        for (int row = T >> 5; row < B.n; row += NT >> 5) {
-            double s = 0.0;
-            for (int j = lane; j < B.n; j += 32) s = fma(__ldg(&ainv[(size_t)row * B.n + j]), B.b[j], s);
+        const TailLevelT<T>& B = lv[nl - 1];
+        const int lane = Tt & 31;
+        for (int row = Tt >> 5; row < B.n; row += NT >> 5) {
+            T s = T(0);
+            for (int j = lane; j < B.n; j += 32) s = fmaT(__ldg(&ainv[(size_t)row * B.n + j]), B.b[j], s);
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             if (lane == 0) B.xo[row] = s;
         }
         __syncthreads();
     }
     for (int l = nl - 2; l >= 0; --l) {  // up
-        const TailLevel& F = lv[l];
-        const TailLevel& C = lv[l + 1];
-        for (int i = T; i < F.n; i += NT) F.r[i] = F.x[i] + C.xo[F.agg[i]];
+        const TailLevelT<T>& F = lv[l];
+        const TailLevelT<T>& C = lv[l + 1];
+        for (int i = Tt; i < F.n; i += NT) F.r[i] = F.x[i] + C.xo[F.agg[i]];
         __syncthreads();
-        for (int i = T; i < F.n; i += NT) {
-            double s = 0.0;
-            F.A.each(i, [&](int j, double a) { s = fma(a, F.r[j], s); });
-            F.xo[i] = fma(kOmega * F.dinv[i], F.b[i] - s, F.r[i]);
+        for (int i = Tt; i < F.n; i += NT) {
+            T s = T(0);
+            F.A.each(i, [&](int j, T a) { s = fmaT(a, F.r[j], s); });
+            F.xo[i] = fmaT(T(kOmega) * F.dinv[i], F.b[i] - s, F.r[i]);
         }
         __syncthreads();
     }
 }
 
 // y = x + P xc
+template <class T>
 __global__ void __launch_bounds__(kT)
-    k_prolong(const AmgState* st, int n, const double* __restrict__ x, const double* __restrict__ xc,
-              const int* __restrict__ agg, double* __restrict__ y) {
+    k_prolong(const AmgState* st, int n, const T* __restrict__ x, const T* __restrict__ xc,
+              const int* __restrict__ agg, T* __restrict__ y) {
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
     if (i < n) y[i] = __ldg(&x[i]) + __ldg(&xc[__ldg(&agg[i])]);
@@ -491,30 +535,35 @@ __global__ void __launch_bounds__(kT)
 
 // y = x + P xc; out = y + w D^-1 (b - A y), y formed on the fly (coarse
 // levels, where a launch costs more than the extra dependent load)
+template <class T>
 __global__ void __launch_bounds__(kT)
-    k_post_fused(const AmgState* st, SellRows rows, int n, const double* __restrict__ dinv,
-                 const double* __restrict__ b, const double* __restrict__ x, const double* __restrict__ xc,
-                 const int* __restrict__ agg, double* __restrict__ out) {
+    k_post_fused(const AmgState* st, SellRowsT<T> rows, int n, const T* __restrict__ dinv, const T* __restrict__ b,
+                 const T* __restrict__ x, const T* __restrict__ xc, const int* __restrict__ agg, T* __restrict__ out) {
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
     if (i >= n) return;
-    const double yi = __ldg(&x[i]) + __ldg(&xc[__ldg(&agg[i])]);
-    double s = 0.0;
-    rows.each(i, [&](int j, double a) { s = fma(a, __ldg(&x[j]) + __ldg(&xc[__ldg(&agg[j])]), s); });
-    out[i] = fma(kOmega * __ldg(&dinv[i]), __ldg(&b[i]) - s, yi);
+    const T yi = __ldg(&x[i]) + __ldg(&xc[__ldg(&agg[i])]);
+    T s = T(0);
+    rows.each(i, [&](int j, T a) { s = fmaT(a, __ldg(&x[j]) + __ldg(&xc[__ldg(&agg[j])]), s); });
+    out[i] = fmaT(T(kOmega) * __ldg(&dinv[i]), __ldg(&b[i]) - s, yi);
 }
 
-// out = y + w D^-1 (b - A y)
-template <class R>
+// out = y + w D^-1 (b - A y), stored as TO (level 0 hands z back as double)
+template <class R, class T, class TO>
 __global__ void __launch_bounds__(kT)
-    k_post(const AmgState* st, R rows, int n, const double* __restrict__ dinv, const double* __restrict__ b,
-           const double* __restrict__ y, double* __restrict__ out) {
+    k_post(const AmgState* st, R rows, int n, const T* __restrict__ dinv, const T* __restrict__ b,
+           const T* __restrict__ y, TO* __restrict__ out) {
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
     if (i >= n) return;
-    double s = 0.0;
-    rows.each(i, [&](int j, double a) { s = fma(a, __ldg(&y[j]), s); });
-    out[i] = fma(kOmega * __ldg(&dinv[i]), __ldg(&b[i]) - s, __ldg(&y[i]));
+    T s = T(0);
+    rows.each(i, [&](int j, T a) { s = fmaT(a, __ldg(&y[j]), s); });
+    out[i] = (TO)fmaT(T(kOmega) * __ldg(&dinv[i]), __ldg(&b[i]) - s, __ldg(&y[i]));
+}
+
+__global__ void __launch_bounds__(kT) k_to_float(int64_t count, const double* __restrict__ src, float* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x;
+    if (i < count) dst[i] = (float)src[i];
 }
 
 // ------------------------------------------------------------ CG
@@ -529,10 +578,25 @@ __global__ void k_params(AmgState* st, double* x, double rel_tol, double abs_tol
     st->done = 0;
 }
 
-// r = b - A x, ||r||; x0 = w D^-1 r (the V-cycle's first sweep)
+// The V-cycle's first sweep from the new residual r_i: x0 = w D^-1 r in FP64,
+// or, for the FP32 V-cycle (b0f set), b0 = (float) r and x0 = w D^-1 b0 in FP32.
+__device__ __forceinline__ void first_sweep(int i, double ri, const double* __restrict__ dinv0, double* __restrict__ x0,
+                                            const float* __restrict__ d0f, float* __restrict__ b0f,
+                                            float* __restrict__ x0f) {
+    if (b0f) {
+        const float bf = (float)ri;
+        b0f[i] = bf;
+        x0f[i] = float(kOmega) * __ldg(&d0f[i]) * bf;
+    } else {
+        x0[i] = kOmega * __ldg(&dinv0[i]) * ri;
+    }
+}
+
+// r = b - A x, ||r||; the V-cycle's first sweep
 __global__ void __launch_bounds__(kT)
     k_init(AmgState* st, EllRows A, int n, const double* __restrict__ b, double* __restrict__ r, double* part,
-           const double* __restrict__ dinv0, double* __restrict__ x0) {
+           const double* __restrict__ dinv0, double* __restrict__ x0, const float* __restrict__ d0f,
+           float* __restrict__ b0f, float* __restrict__ x0f) {
     __shared__ double sm[kT];
     const int i = blockIdx.x * kT + threadIdx.x;
     const double* x = st->x;
@@ -542,7 +606,7 @@ __global__ void __launch_bounds__(kT)
         A.each(i, [&](int j, double a) { s = fma(a, x[j], s); });
         ri = __ldg(&b[i]) - s;
         r[i] = ri;
-        x0[i] = kOmega * __ldg(&dinv0[i]) * ri;
+        first_sweep(i, ri, dinv0, x0, d0f, b0f, x0f);
     }
     double tot;
     if (arrive(st, part, block_sum(ri * ri, sm), sm, &tot) && threadIdx.x == 0) {
@@ -609,7 +673,8 @@ __global__ void __launch_bounds__(kT)
 // x += alpha p, r -= alpha q, ||r||, convergence; x0 = w D^-1 r (the V-cycle's first sweep)
 __global__ void __launch_bounds__(kT)
     k_update(AmgState* st, int n, const double* __restrict__ p, const double* __restrict__ q, double* __restrict__ r,
-             double* part, const double* __restrict__ dinv0, double* __restrict__ x0) {
+             double* part, const double* __restrict__ dinv0, double* __restrict__ x0, const float* __restrict__ d0f,
+             float* __restrict__ b0f, float* __restrict__ x0f) {
     __shared__ double sm[kT];
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
@@ -620,7 +685,7 @@ __global__ void __launch_bounds__(kT)
         x[i] = fma(alpha, __ldg(&p[i]), x[i]);
         const double ri = fma(-alpha, __ldg(&q[i]), r[i]);
         r[i] = ri;
-        x0[i] = kOmega * __ldg(&dinv0[i]) * ri;
+        first_sweep(i, ri, dinv0, x0, d0f, b0f, x0f);
         v = ri * ri;
     }
     double tot;
@@ -704,6 +769,7 @@ fvgb_status symbolic(AmgCache* c, cudaStream_t s) {
     c->lv.emplace_back();
     c->lv[0].n = n;
     c->lv[0].nnz = nnz;
+    c->lv[0].slots = mesh->m_len;
     std::vector<int> slot_of = csr_pos;  // the current level's slot of each of its CSR entries
     while ((int)c->lv.size() < kMaxLevels && A.n > kCoarseRows) {
         // two rounds of pairwise matching per level (double pairwise): the pairs
@@ -766,6 +832,7 @@ fvgb_status symbolic(AmgCache* c, cudaStream_t s) {
         }
         for (int i = 0; i < Ac.n; ++i)
             if (dpos[i] < 0) return fvgb_fail(FVGB_ERR_INVALID_ARG, "multigrid: a coarse row without a diagonal entry");
+        C.slots = std::max(1, sptr[ns]);
         e = upload(c, &L.gdst, gdst);
         if (e == cudaSuccess) e = upload(c, &C.sptr, sptr);
         if (e == cudaSuccess) e = upload(c, &C.scol, scol);
@@ -794,11 +861,11 @@ fvgb_status symbolic(AmgCache* c, cudaStream_t s) {
         int t = 1;
         while (t < L - 1 && c->lv[t].n > kTailRows) ++t;
         c->tail_from = t;
-        std::vector<TailLevel> tl;
+        std::vector<TailLevelT<double>> tl;
         for (int l = t; l < L; ++l) {
             const Level& V = c->lv[l];
-            tl.push_back(TailLevel{V.n, SellRows{V.sptr, V.scol, V.val}, V.dinv, V.agg, V.mptr, V.mem, V.b, V.x, V.xo,
-                                   V.r});
+            tl.push_back(TailLevelT<double>{V.n, SellRows{V.sptr, V.scol, V.val}, V.dinv, V.agg, V.mptr, V.mem, V.b,
+                                            V.x, V.xo, V.r});
         }
         cudaError_t e = upload(c, &c->tail, tl);
         if (e != cudaSuccess) return cuda_fail(e, "multigrid setup");
@@ -836,6 +903,43 @@ fvgb_status numeric(AmgCache* c, cudaStream_t s) {
     return FVGB_OK;
 }
 
+// FP32 copies of the level matrices, diagonals and coarsest inverse
+fvgb_status to_f32(AmgCache* c, cudaStream_t s) {
+    const fvgb_ls* ls = c->ls;
+    if (!c->f32) {
+        for (size_t l = 0; l < c->lv.size(); ++l) {
+            Level& V = c->lv[l];
+            cudaError_t e = dev_alloc(c, &V.valf, (size_t)V.slots);
+            if (e == cudaSuccess) e = dev_alloc(c, &V.dinvf, (size_t)V.n);
+            if (e == cudaSuccess) e = dev_alloc(c, &V.bf, (size_t)V.n);
+            if (e == cudaSuccess) e = dev_alloc(c, &V.xf, (size_t)V.n);
+            if (e == cudaSuccess) e = dev_alloc(c, &V.xof, (size_t)V.n);
+            if (e == cudaSuccess) e = dev_alloc(c, &V.rf, (size_t)V.n);
+            if (e != cudaSuccess) return cuda_fail(e, "multigrid FP32 copies");
+        }
+        cudaError_t e = dev_alloc(c, &c->ainvf, (size_t)c->nc * c->nc);
+        std::vector<TailLevelT<float>> tl;
+        for (int l = c->tail_from; l < (int)c->lv.size(); ++l) {
+            const Level& V = c->lv[l];
+            tl.push_back(TailLevelT<float>{V.n, SellRowsT<float>{V.sptr, V.scol, V.valf}, V.dinvf, V.agg, V.mptr, V.mem,
+                                           V.bf, V.xf, V.xof, V.rf});
+        }
+        if (e == cudaSuccess) e = upload(c, &c->tailf, tl);
+        if (e != cudaSuccess) return cuda_fail(e, "multigrid FP32 copies");
+        c->f32 = true;
+    }
+    for (size_t l = 0; l < c->lv.size(); ++l) {
+        const Level& V = c->lv[l];
+        const double* src = l == 0 ? ls->values : V.val;
+        k_to_float<<<grid_for(V.slots, kT), kT, 0, s>>>(V.slots, src, V.valf);
+        k_to_float<<<grid_for(V.n, kT), kT, 0, s>>>(V.n, V.dinv, V.dinvf);
+    }
+    k_to_float<<<grid_for((int64_t)c->nc * c->nc, kT), kT, 0, s>>>((int64_t)c->nc * c->nc, c->ainv, c->ainvf);
+    FVGB_LAUNCH_CHECK("multigrid FP32 copies");
+    c->f32_version = ls->version;
+    return FVGB_OK;
+}
+
 cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* dep, void* func, unsigned grid,
                        unsigned block, void** args, unsigned smem = 0) {
     cudaKernelNodeParams kp{};
@@ -850,39 +954,68 @@ cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* de
 }
 
 // The V-cycle z = M r as a chain of kernel nodes after *prev: levels
-// 0..t-1 one kernel per step, levels t..L-1 in the single-block tail.
+// 0..t-1 one kernel per step, levels t..L-1 in the single-block tail.  T is
+// the V-cycle's type; with T = float, level 0's b and x are FP32 copies the
+// CG kernels write and z comes back as double.
+template <class T>
 struct VcycleArgs {
     std::vector<std::vector<void*>> args;
-    std::vector<EllRows> ell;
-    std::vector<SellRows> sell;
+    std::vector<EllRowsT<T>> ell;
+    std::vector<SellRowsT<T>> sell;
     std::vector<int> ns;
-    std::vector<const double*> bs;
-    std::vector<double*> outs;
-    std::vector<double*> xcs;
+    std::vector<const T*> bs;
+    std::vector<T*> outs;
+    std::vector<T*> xcs;
+    std::vector<T*> dv, xv, rv, bv;
     int nl_tail = 0;
-    const TailLevel* tail = nullptr;
+    const TailLevelT<T>* tail = nullptr;
+    const T* ainv = nullptr;
 };
 
-cudaError_t add_vcycle(AmgCache* c, cudaGraph_t g, cudaGraphNode_t* prev, const double* r_in, double* z_out,
-                       VcycleArgs& va, bool first_sweep_done = false) {
+template <class T> const T* ainv_of(const AmgCache* c);
+template <> const double* ainv_of<double>(const AmgCache* c) { return c->ainv; }
+template <> const float* ainv_of<float>(const AmgCache* c) { return c->ainvf; }
+template <class T> const TailLevelT<T>* tail_of(const AmgCache* c);
+template <> const TailLevelT<double>* tail_of<double>(const AmgCache* c) { return c->tail; }
+template <> const TailLevelT<float>* tail_of<float>(const AmgCache* c) { return c->tailf; }
+
+// r_in: level 0's b (double* for T = double; the FP32 copy otherwise).
+// z_out: the result (always double).  first_sweep_done: level 0's x was
+// formed by the kernel that produced r_in.
+template <class T>
+cudaError_t add_vcycle(AmgCache* c, cudaGraph_t g, cudaGraphNode_t* prev, const T* r_in, double* z_out,
+                       VcycleArgs<T>& va, bool first_sweep_done = false) {
     const size_t L = c->lv.size();
     const size_t t = (size_t)c->tail_from;
-    va.ell.assign(1, EllRows{c->ls->mesh->v, c->ls->values});
+    if (!first_sweep_done && !std::is_same<T, double>::value) return cudaErrorInvalidValue;  // FP64 only
+    va.ell.assign(1, EllRowsT<T>{c->ls->mesh->v, c->lv[0].vals<T>() ? c->lv[0].vals<T>() : nullptr});
+    if (std::is_same<T, double>::value) va.ell[0].val = (const T*)c->ls->values;
     va.sell.resize(L);
-    for (size_t l = 1; l < L; ++l) va.sell[l] = SellRows{c->lv[l].sptr, c->lv[l].scol, c->lv[l].val};
+    for (size_t l = 1; l < L; ++l) va.sell[l] = SellRowsT<T>{c->lv[l].sptr, c->lv[l].scol, c->lv[l].vals<T>()};
     va.ns.resize(L);
     va.bs.resize(L);
     va.outs.resize(L);
     va.xcs.resize(L);
+    va.dv.resize(L);
+    va.xv.resize(L);
+    va.rv.resize(L);
+    va.bv.resize(L);
     va.args.clear();
     va.args.reserve(6 * L + 4);
     for (size_t l = 0; l < L; ++l) {
-        va.ns[l] = c->lv[l].n;
-        va.bs[l] = l == 0 ? r_in : c->lv[l].b;
-        va.outs[l] = l == 0 ? z_out : c->lv[l].xo;
+        const Level& V = c->lv[l];
+        va.ns[l] = V.n;
+        va.bs[l] = l == 0 ? r_in : V.bs<T>();
+        va.outs[l] = V.xos<T>();
+        va.dv[l] = V.dinvs<T>();
+        va.xv[l] = V.xs<T>();
+        va.rv[l] = V.rs<T>();
+        va.bv[l] = V.bs<T>();
     }
     va.nl_tail = (int)(L - t);
-    va.tail = c->tail;
+    va.tail = tail_of<T>(c);
+    va.ainv = ainv_of<T>(c);
+    double* z = z_out;
     cudaError_t e = cudaSuccess;
     cudaGraphNode_t node;
     auto add = [&](void* fn, unsigned grid, unsigned block) {
@@ -897,39 +1030,40 @@ cudaError_t add_vcycle(AmgCache* c, cudaGraph_t g, cudaGraphNode_t* prev, const 
                 va.args.push_back({&c->st, &va.ns[0], &F.dinv, &va.bs[0], &F.x});
                 add((void*)k_smooth0, grid_for(F.n, kT), kT);
             }
-            va.args.push_back({&c->st, &va.ell[0], &va.ns[0], &va.bs[0], &F.x, &F.r});
-            add((void*)k_resid<EllRows>, grid_for(F.n, kT), kT);
+            va.args.push_back({&c->st, &va.ell[0], &va.ns[0], &va.bs[0], &va.xv[0], &va.rv[0]});
+            add((void*)k_resid<EllRowsT<T>, T>, grid_for(F.n, kT), kT);
         } else {
-            va.args.push_back({&c->st, &va.sell[l], &va.ns[l], &va.bs[l], &F.x, &F.r});
-            add((void*)k_resid<SellRows>, grid_for(F.n, kT), kT);
+            va.args.push_back({&c->st, &va.sell[l], &va.ns[l], &va.bs[l], &va.xv[l], &va.rv[l]});
+            add((void*)k_resid<SellRowsT<T>, T>, grid_for(F.n, kT), kT);
         }
         Level& C = c->lv[l + 1];
-        va.args.push_back({&c->st, &va.ns[l + 1], &F.mptr, &F.mem, &F.r, &C.dinv, &C.b, &C.x});
-        add((void*)k_restrict, grid_for(C.n, kT), kT);
+        va.args.push_back({&c->st, &va.ns[l + 1], &F.mptr, &F.mem, &va.rv[l], &va.dv[l + 1], &va.bv[l + 1], &va.xv[l + 1]});
+        add((void*)k_restrict<T>, grid_for(C.n, kT), kT);
     }
-    va.args.push_back({&c->st, &va.tail, &va.nl_tail, &c->ainv});
-    add((void*)k_tail, 1, 1024);
+    va.args.push_back({&c->st, &va.tail, &va.nl_tail, &va.ainv});
+    add((void*)k_tail<T>, 1, 1024);
     for (size_t l = t; l-- > 0 && e == cudaSuccess;) {  // up
         Level& F = c->lv[l];
-        va.xcs[l] = c->lv[l + 1].xo;
+        va.xcs[l] = va.outs[l + 1];
         if (l == 0) {
-            va.args.push_back({&c->st, &va.ns[l], &F.x, &va.xcs[l], &F.agg, &F.r});  // y = x + P xc into F.r
-            add((void*)k_prolong, grid_for(F.n, kT), kT);
-            va.args.push_back({&c->st, &va.ell[0], &va.ns[l], &F.dinv, &va.bs[l], &F.r, &va.outs[l]});
-            add((void*)k_post<EllRows>, grid_for(F.n, kT), kT);
+            va.args.push_back({&c->st, &va.ns[l], &va.xv[l], &va.xcs[l], &F.agg, &va.rv[l]});  // y = x + P xc
+            add((void*)k_prolong<T>, grid_for(F.n, kT), kT);
+            va.args.push_back({&c->st, &va.ell[0], &va.ns[l], &va.dv[l], &va.bs[l], &va.rv[l], &z});
+            add((void*)k_post<EllRowsT<T>, T, double>, grid_for(F.n, kT), kT);
         } else {
-            va.args.push_back({&c->st, &va.sell[l], &va.ns[l], &F.dinv, &va.bs[l], &F.x, &va.xcs[l], &F.agg,
+            va.args.push_back({&c->st, &va.sell[l], &va.ns[l], &va.dv[l], &va.bs[l], &va.xv[l], &va.xcs[l], &F.agg,
                                &va.outs[l]});
-            add((void*)k_post_fused, grid_for(F.n, kT), kT);
+            add((void*)k_post_fused<T>, grid_for(F.n, kT), kT);
         }
     }
     return e;
 }
 
-fvgb_status build_graph(AmgCache* c) {
-    if (c->graph) {
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
+fvgb_status build_graph(AmgCache* c, bool f32) {
+    cudaGraphExec_t& out = f32 ? c->graph32 : c->graph;
+    if (out) {
+        cudaGraphExecDestroy(out);
+        out = nullptr;
     }
     const fvgb_ls* ls = c->ls;
     EllRows A{ls->mesh->v, ls->values};
@@ -941,18 +1075,25 @@ fvgb_status build_graph(AmgCache* c) {
     cudaGraphConditionalHandle h;
     cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
     cudaGraphNode_t prev = nullptr, node;
-    VcycleArgs v0, v1;
-    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &c->lv[0].x};
+    VcycleArgs<double> v0, v1;
+    VcycleArgs<float> f0, f1;
+    // FP64 V-cycle: the CG kernels write x0 (double); FP32: b0 and x0 as float
+    double* x0 = f32 ? nullptr : c->lv[0].x;
+    const float* d0f = f32 ? c->lv[0].dinvf : nullptr;
+    float* b0f = f32 ? c->lv[0].bf : nullptr;
+    float* x0f = f32 ? c->lv[0].xf : nullptr;
+    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &x0, &d0f, &b0f, &x0f};
     void* a_first[] = {&c->st, &n, &c->r, &c->z, &c->p, &c->part};
     void* a_cond[] = {&c->st, &h};
     void* a_spmv[] = {&c->st, &A, &n, &c->p, &c->q, &c->part};
-    void* a_upd[] = {&c->st, &n, &c->p, &c->q, &c->r, &c->part, &c->lv[0].dinv, &c->lv[0].x};
+    void* a_upd[] = {&c->st, &n, &c->p, &c->q, &c->r, &c->part, &c->lv[0].dinv, &x0, &d0f, &b0f, &x0f};
     void* a_rz[] = {&c->st, &n, &c->r, &c->z, &c->part};
     void* a_dir[] = {&c->st, &n, &c->z, &c->p};
     void* a_stats[] = {&c->st};
     if (e == cudaSuccess) e = add_kernel(g, &node, nullptr, (void*)k_init, nb, kT, a_init);
     prev = node;
-    if (e == cudaSuccess) e = add_vcycle(c, g, &prev, c->r, c->z, v0, true);
+    if (e == cudaSuccess)
+        e = f32 ? add_vcycle<float>(c, g, &prev, b0f, c->z, f0, true) : add_vcycle<double>(c, g, &prev, c->r, c->z, v0, true);
     if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_first_dir, nb, kT, a_first);
     prev = node;
     if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_cond, 1, 1, a_cond);
@@ -973,20 +1114,22 @@ fvgb_status build_graph(AmgCache* c) {
     bprev = bnode;
     if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_update, nb, kT, a_upd);
     bprev = bnode;
-    if (e == cudaSuccess) e = add_vcycle(c, body, &bprev, c->r, c->z, v1, true);
+    if (e == cudaSuccess)
+        e = f32 ? add_vcycle<float>(c, body, &bprev, b0f, c->z, f1, true)
+                : add_vcycle<double>(c, body, &bprev, c->r, c->z, v1, true);
     if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_rz, nb, kT, a_rz);
     bprev = bnode;
     if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_dir, nb, kT, a_dir);
     bprev = bnode;
     if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_cond, 1, 1, a_cond);
     if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_stats, 1, 1, a_stats);
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph, g, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(e, "multigrid CG graph");
     return FVGB_OK;
 }
 
-fvgb_status prepare(fvgb_ls* ls, cudaStream_t s) {
+fvgb_status prepare(fvgb_ls* ls, cudaStream_t s, bool f32 = false) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     FVGB_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
     if (!ls->amg) {
@@ -995,7 +1138,7 @@ fvgb_status prepare(fvgb_ls* ls, cudaStream_t s) {
         AmgCache* c = new AmgCache();
         c->ls = ls;
         fvgb_status st = symbolic(c, s);
-        if (st == FVGB_OK) st = build_graph(c);
+        if (st == FVGB_OK) st = build_graph(c, false);
         if (st != FVGB_OK) {
             fvgb_amg_free(c);
             return st;
@@ -1003,7 +1146,22 @@ fvgb_status prepare(fvgb_ls* ls, cudaStream_t s) {
         ls->amg = c;
     }
     AmgCache* c = ls->amg;
-    if (c->version != ls->version) return numeric(c, s);
+    if (c->version != ls->version) {
+        fvgb_status st = numeric(c, s);
+        if (st != FVGB_OK) return st;
+    }
+    if (f32) {
+        if (!c->f32 || c->f32_version != ls->version) {
+            const bool first = !c->f32;
+            fvgb_status st = to_f32(c, s);
+            if (st != FVGB_OK) return st;
+            if (first) {
+                FVGB_CUDA_TRY(cudaStreamSynchronize(s));
+                st = build_graph(c, true);
+                if (st != FVGB_OK) return st;
+            }
+        }
+    }
     return FVGB_OK;
 }
 
@@ -1012,6 +1170,7 @@ fvgb_status prepare(fvgb_ls* ls, cudaStream_t s) {
 void fvgb_amg_free(AmgCache* c) {
     if (!c) return;
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->graph32) cudaGraphExecDestroy(c->graph32);
     for (void* p : c->allocs) cudaFree(p);
     delete c;
 }
@@ -1019,14 +1178,17 @@ void fvgb_amg_free(AmgCache* c) {
 fvgb_status fvgb_amg_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev,
                                  cudaStream_t s) {
     if (ls->ncomp != 1) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_solve: scalar systems only");
-    if (cfg->precision != FVGB_PREC_FP64 || cfg->method != FVGB_SOLVER_CG)
-        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: FP64 CG only");
-    fvgb_status st = prepare(ls, s);
+    if (cfg->method != FVGB_SOLVER_CG)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: CG only");
+    // mixed precision: the CG, its residuals and its stopping test stay FP64;
+    // the V-cycle (the preconditioner) runs in FP32
+    const bool f32 = cfg->precision == FVGB_PREC_MIXED_IR;
+    fvgb_status st = prepare(ls, s, f32);
     if (st != FVGB_OK) return st;
     AmgCache* c = ls->amg;
     k_params<<<1, 1, 0, s>>>(c->st, x, cfg->rel_tol, cfg->abs_tol, cfg->max_iter, stats_dev);
     FVGB_LAUNCH_CHECK("multigrid params");
-    FVGB_CUDA_TRY(cudaGraphLaunch(c->graph, s));
+    FVGB_CUDA_TRY(cudaGraphLaunch(f32 ? c->graph32 : c->graph, s));
     return FVGB_OK;
 }
 
@@ -1052,8 +1214,8 @@ extern "C" fvgb_status fvgb_amg_apply(fvgb_ls* ls, const double* r, double* z, f
     cudaGraph_t g = nullptr;
     FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
     cudaGraphNode_t prev = nullptr;
-    VcycleArgs va;
-    cudaError_t e = add_vcycle(c, g, &prev, r, z, va);
+    VcycleArgs<double> va;
+    cudaError_t e = add_vcycle<double>(c, g, &prev, r, z, va);
     cudaGraphExec_t ge = nullptr;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
     if (e == cudaSuccess) e = cudaGraphLaunch(ge, s);

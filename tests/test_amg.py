@@ -189,12 +189,39 @@ def test_multigrid_follows_matrix_changes(cuda):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("dims", [(24, 20, 16), (64, 48, 1)])
+def test_fp32_vcycle_in_fp64_cg(cuda, dims):
+    """Mixed precision: the FP64 CG with the V-cycle in FP32 reaches the same
+    FP64 residual and the Jacobi-PCG solution; deterministic; the FP64
+    V-cycle solve is unchanged after it."""
+    s = gpu_system(cuda, dims)
+    torch, ls = s["torch"], s["ls"]
+    x64 = s["x0"].clone()
+    s64 = ls.solve(x64, rel_tol=1e-11, max_iter=500, preconditioner=abi.PRECOND_MULTIGRID)
+    xm = s["x0"].clone()
+    sm = ls.solve(xm, rel_tol=1e-11, max_iter=500, precision=abi.PREC_MIXED_IR,
+                  preconditioner=abi.PRECOND_MULTIGRID)
+    assert sm.status == abi.OK and sm.final_res_norm <= 1e-11 * sm.init_res_norm
+    assert sm.num_iter <= s64.num_iter + 3, (sm.num_iter, s64.num_iter)
+    import scipy.sparse as sp
+    A = sp.csr_matrix((s["v"], s["col"], s["ro"]))
+    x = xm.cpu().numpy()
+    x0 = s["x0"].cpu().numpy()
+    assert np.linalg.norm(s["rhs"] - A @ x) <= 1e-9 * np.linalg.norm(s["rhs"] - A @ x0)
+    assert float((xm - x64).abs().max()) <= 1e-8 * float(x64.abs().max())
+    xm2 = s["x0"].clone()
+    sm2 = ls.solve(xm2, rel_tol=1e-11, max_iter=500, precision=abi.PREC_MIXED_IR,
+                   preconditioner=abi.PRECOND_MULTIGRID)
+    assert sm2.num_iter == sm.num_iter and torch.equal(xm2, xm)
+    x64b = s["x0"].clone()
+    s64b = ls.solve(x64b, rel_tol=1e-11, max_iter=500, preconditioner=abi.PRECOND_MULTIGRID)
+    assert s64b.num_iter == s64.num_iter and torch.equal(x64b, x64)
+
+
+@pytest.mark.gpu
 def test_multigrid_rejects_what_it_does_not_cover(cuda):
     s = gpu_system(cuda, (12, 10, 8))
     x = s["x0"].clone()
-    with pytest.raises(abi.FvgbError) as e:
-        s["ls"].solve(x, precision=abi.PREC_MIXED_IR, preconditioner=abi.PRECOND_MULTIGRID)
-    assert e.value.status == abi.ERR_UNSUPPORTED
     with pytest.raises(abi.FvgbError) as e:
         s["ls"].solve(x, method=abi.SOLVER_BICGSTAB, preconditioner=abi.PRECOND_MULTIGRID)
     assert e.value.status == abi.ERR_UNSUPPORTED
