@@ -304,8 +304,10 @@ typedef struct fvgb_solver_cfg {
     int32_t preconditioner;    /* FVGB_PRECOND_JACOBI (Ginkgo Jacobi, block size 1) or
                                   FVGB_PRECOND_MULTIGRID (Ginkgo Multigrid with PGM
                                   aggregation as tutorials/cylinder2D/system/gko/
-                                  config.mg.json selects it; FP64 CG, single systems,
-                                  fvgb_solve / fvgb_solve_async only)                    */
+                                  config.mg.json selects it; CG, single systems,
+                                  fvgb_solve / fvgb_solve_async only; with
+                                  FVGB_PREC_MIXED_IR the V-cycle runs in FP32 inside
+                                  the FP64 CG)                                          */
 } fvgb_solver_cfg;
 enum { FVGB_SOLVE_NO_TUNE = 1 };
 enum { FVGB_SOLVER_CG = 0, FVGB_SOLVER_BICGSTAB = 1 };
