@@ -396,7 +396,8 @@ struct SolverConfig {
     int innerMaxIter = 1000;
     int maxOuter = 50;
     bool bicgstab = false;  // solver "BiCGStab" (fvSolution.cpp:25-26) instead of "CG"
-    bool multigrid = false; // preconditioner solver::Multigrid (FP64 CG) instead of Jacobi
+    bool multigrid = false; // preconditioner solver::Multigrid instead of Jacobi (CG; with
+                            // mixedPrecision the V-cycle runs in FP32 inside the FP64 CG)
 };
 
 class LinearSystem {

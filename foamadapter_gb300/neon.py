@@ -313,8 +313,9 @@ class LinearSystem:
               method=abi.SOLVER_CG, flags=0, preconditioner=abi.PRECOND_JACOBI):
         """inner_rel_tol (mixed precision) defaults to 0.1 for CG and 0.01 for the
         restarted inner BiCGStab, the fastest settings measured on 128^3 systems.
-        preconditioner=abi.PRECOND_MULTIGRID: FP64 CG with the aggregation
-        multigrid V-cycle (single systems)."""
+        preconditioner=abi.PRECOND_MULTIGRID: CG with the aggregation
+        multigrid V-cycle (single systems); with precision=abi.PREC_MIXED_IR
+        the V-cycle runs in FP32 inside the FP64 CG."""
         if inner_rel_tol is None:
             inner_rel_tol = 0.01 if method == abi.SOLVER_BICGSTAB else 0.1
         cfg = abi.SolverCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer,
