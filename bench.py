@@ -286,6 +286,24 @@ def compare_precisions(torch, abi, L, ls, T, T_old, tarr, bc, dm, hm, stream):
     nl = C.c_int32()
     rows = (C.c_int32 * 32)()
     abi.check(L.fvgb_amg_info(ls.handle, C.byref(nl), rows, None, 32))
+    # the same with the V-cycle in FP32 inside the FP64 CG (mixed precision)
+    cfg32 = abi.SolverCfg(HEAT["rel_tol"], 0.0, 4000, abi.PREC_MIXED_IR, 0.1, 1000, 50, 0, 0, abi.SOLVER_CG,
+                          abi.PRECOND_MULTIGRID)
+    t32 = []
+    for rep in range(4):
+        x32 = T_old.clone()
+        st32 = abi.SolverStats()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        abi.check(L.fvgb_solve(ls.handle, abi.ptr(x32), C.byref(cfg32), C.byref(st32), stream))
+        torch.cuda.synchronize()
+        t32.append(1e3 * (time.perf_counter() - t0))
+    r32 = torch.empty_like(x32)
+    abi.check(L.fvgb_apply_operator(ls.handle, abi.ptr(x32), abi.ptr(r32), stream))
+    out["multigrid_fp32_vcycle"] = {"ms": min(t32[1:]), "iters": st32.num_iter,
+                                    "rel_residual": float(torch.linalg.vector_norm(r32).item() / st32.init_res_norm),
+                                    "max_abs_err_vs_fp64": float((x32 - sols["fp64"]).abs().max().item()),
+                                    "speedup_vs_fp64_jacobi": out["fp64"]["ms"] / min(t32[1:])}
     out["fp64_multigrid"] = {"ms": min(times[1:4]), "first_solve_ms_with_setup": times[0],
                              "solve_after_reassembly_ms": times[4], "iters": st.num_iter,
                              "levels": [int(rows[i]) for i in range(nl.value)],
