@@ -34,10 +34,20 @@ sys.path.insert(0, str(ROOT))
 HEAT = dict(n=128, jitter=0.1, seed=12345, dt=0.01, sigma=0.5, T0=300.0, Twall=400.0, rel_tol=1e-8)
 
 
-def heat_inputs(n):
-    from foamadapter_gb300 import mesh
+def heat_inputs(n, oracle_mesh=False):
+    """The 128^3 (or n^3) jittered box and its lognormal conductivity.  With
+    oracle_mesh the arrays come from the oracle's own box builder (the same
+    bits), so a CPU-only leg never loads the GPU library."""
+    if oracle_mesh:
+        from oracle import build_oracle
+        from oracle.pyoracle import BoxMesh
 
-    hm = mesh.box(n, n, n, jitter=HEAT["jitter"], seed=HEAT["seed"])
+        build_oracle.build()
+        hm = BoxMesh(n, n, n, jitter=HEAT["jitter"], seed=HEAT["seed"])
+    else:
+        from foamadapter_gb300 import mesh
+
+        hm = mesh.box(n, n, n, jitter=HEAT["jitter"], seed=HEAT["seed"])
     rng = np.random.default_rng(HEAT["seed"])
     k = np.exp(HEAT["sigma"] * rng.standard_normal(hm.n))
     return hm, k
@@ -220,6 +230,9 @@ def run_gpu(args, rank, world):
     barrier()
     e2e_ms = e0.elapsed_time(e1)
     e2e_iters = [s.num_iter for s in read_stats(args.steps)]
+    # every e2e step started from h_in: h_out and the last step's iteration count are
+    # what the CPU oracle must reproduce from the same state
+    step_in, step_out = h_in.numpy().copy(), h_out.numpy().copy()
     # ---- per-kernel times for the roofline (outside the graph, same system)
     kt = (C.c_double * 4)()
     abi.check(L.fvgb_solve_kernel_times(ls.handle, abi.ptr(T.internal), 30, kt, stream))
@@ -234,7 +247,7 @@ def run_gpu(args, rank, world):
               for i, k in enumerate(kinds)}
     result = dict(ms=ms, iters=iters, e2e_ms=e2e_ms, e2e_iters=e2e_iters, kt=list(kt), clocks=clk.summary(),
                   mixed=mixed, face_updates=face_updates, warm_iters=[s.num_iter for s in warm_stats],
-                  mesh_bytes=dm.device_bytes(), tuning=tuning)
+                  mesh_bytes=dm.device_bytes(), tuning=tuning, step_in=step_in, step_out=step_out)
     return hm, result
 
 
@@ -319,8 +332,10 @@ def compare_precisions(torch, abi, L, ls, T, T_old, tarr, bc, dm, hm, stream):
 
 
 # ----------------------------------------------------------------------------- CPU (oracle)
-def cpu_steps(hm, k, nsteps, threads):
-    """The same heat-transfer steps on the host cores with the CPU oracle."""
+def cpu_steps(hm, k, nsteps, threads, T_start=None, first_only=False):
+    """The same heat-transfer steps on the host cores with the CPU oracle, from
+    T0 or from T_start.  Returns the step times, iteration counts, threads and
+    the field after the first step."""
     from oracle import build_oracle
     from oracle.pyoracle import Oracle, get_threads, set_threads
 
@@ -335,10 +350,10 @@ def cpu_steps(hm, k, nsteps, threads):
     types = np.asarray([1] + [2] * (hm.npatch - 1), np.int32)
     ref = np.zeros(nbf)
     ref[hm.patch_slice("xmin")] = HEAT["Twall"]
-    T = np.full(hm.n, HEAT["T0"])
+    T = np.full(hm.n, HEAT["T0"]) if T_start is None else np.array(T_start, dtype=np.float64)
     Tb = np.zeros(nbf)
     o.bc_correct(1, types, ref, T, Tb)
-    times, iters = [], []
+    times, iters, first = [], [], None
     for _ in range(nsteps):
         t0 = time.perf_counter()
         told = T.copy()
@@ -348,18 +363,21 @@ def cpu_steps(hm, k, nsteps, threads):
         o.bc_correct(1, types, ref, T, Tb)
         times.append(time.perf_counter() - t0)
         iters.append(st.num_iter)
-    return times, iters, get_threads()
+        if first is None:
+            first = T.copy()
+    return times, iters, get_threads(), first
 
 
 def run_reference(args, rank, world):
     """--impl reference: the oracle port of the reference's CPU path, all host threads."""
     if rank != 0:
         return
-    hm, k = heat_inputs(args.n)
+    hm, k = heat_inputs(args.n, oracle_mesh=True)
     nbfa = active_bfaces(hm)
-    w = min(args.warmup, 1)
+    # the GPU arm's own step sequence: W untimed steps from T0, then K timed ones
+    w = max(0, args.warmup)
     ksteps = max(1, min(args.steps, args.ref_max_steps))
-    times, iters, threads = cpu_steps(hm, k, w + ksteps, os.cpu_count())
+    times, iters, threads, _ = cpu_steps(hm, k, w + ksteps, os.cpu_count())
     t = sum(times[w:])
     val = (hm.nif + nbfa) * ksteps / t
     line = {
@@ -368,8 +386,8 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": workload_config(args),
         "cpu_baseline": {"value": val, "unit": "face-updates/s", "cores": threads, "kind": "port",
-                         "sample": f"{ksteps} implicit steps of the 128^3 case (assembly + FP64 Jacobi-PCG "
-                                   f"to 1e-8, iterations {iters[w:]}), OpenMP x{threads}"},
+                         "sample": f"steps {w + 1}-{w + ksteps} of the {args.n}^3 case from T0 (assembly + FP64 "
+                                   f"Jacobi-PCG to 1e-8, iterations {iters[w:]}), OpenMP x{threads}"},
         "e2e": {"value": val, "unit": "face-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -897,8 +915,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=HEAT["n"])
-    ap.add_argument("--cpu-steps", type=int, default=1)
-    ap.add_argument("--ref-max-steps", type=int, default=8)
+    ap.add_argument("--cpu-steps", type=int, default=12)
+    ap.add_argument("--ref-max-steps", type=int, default=1000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity", "batch", "serve", "explicit",
                                                            "convection", "multigrid"])
@@ -980,16 +998,24 @@ def main():
         "autotune": r["tuning"],
     }
     if not args.no_cpu and world == 1:
-        from oracle.pyoracle import set_threads  # noqa: F401
-
-        hm2, k = heat_inputs(args.n)
-        times, iters, threads = cpu_steps(hm2, k, args.cpu_steps, os.cpu_count())
+        # the oracle continues from the state the end-to-end steps started from
+        # (after W + K steps): its first step must give the GPU's step bit for bit,
+        # and the steps it times are as hard as the GPU's timed ones
+        hm2, k = heat_inputs(args.n, oracle_mesh=True)
+        times, iters, threads, first = cpu_steps(hm2, k, args.cpu_steps, os.cpu_count(), T_start=r["step_in"])
         t = sum(times)
+        exact = bool(np.array_equal(first, r["step_out"])) and iters[0] == r["e2e_iters"][-1]
+        line["parity"] = {"check": f"one {args.n}^3 step from the GPU's state after {args.warmup + args.steps} "
+                                   "steps, GPU (end-to-end call) vs CPU oracle",
+                          "result": "bit-exact" if exact else "MISMATCH",
+                          "iters_gpu": r["e2e_iters"][-1], "iters_oracle": iters[0],
+                          "max_abs_diff": float(np.abs(first - r["step_out"]).max())}
         line["cpu_baseline"] = {"value": fu * len(times) / t, "unit": "face-updates/s", "cores": threads,
                                 "kind": "port",
-                                "sample": f"{len(times)} implicit step(s) of the same {args.n}^3 case "
-                                          f"(assembly + FP64 Jacobi-PCG to 1e-8, {iters} iterations) on the "
-                                          f"CPU oracle, OpenMP x{threads}"}
+                                "sample": f"{len(times)} implicit steps of the same {args.n}^3 case from the GPU's "
+                                          f"state after {args.warmup + args.steps} steps (assembly + FP64 "
+                                          f"Jacobi-PCG to 1e-8, {iters} iterations) on the CPU oracle, "
+                                          f"OpenMP x{threads}"}
     print(json.dumps(line))
 
 

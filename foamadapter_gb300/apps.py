@@ -51,6 +51,40 @@ class Advection:
         self.T.boundary, self.Tb2 = self.Tb2, self.T.boundary
 
 
+class HeatTransfer:
+    """ddt(T) - laplacian(kappa, T) = 0 with implicit Euler, the time loop of
+    examples/heatTransfer/heatTransfer.cpp:60-83: every step assembles the
+    system from the old field, solves it with Jacobi-PCG and corrects the
+    boundary values.  Face conductivity is the linear interpolation of the cell
+    values; xmin is a fixed-value wall, every other patch zero-gradient."""
+
+    def __init__(self, hm, kappa, T0=300.0, Twall=400.0, dt=0.01, rel_tol=1e-8, max_iter=1000,
+                 precision=abi.PREC_FP64):
+        self.hm, self.dm = hm, DeviceMesh(hm)
+        self.dt = dt
+        self.cfg = abi.SolverCfg(rel_tol, 0.0, max_iter, precision, 0.1, 1000, 50)
+        bcs = [("fixedValue", Twall)] + [("zeroGradient", 0.0)] * (hm.npatch - 1)
+        self.T = neon.VolumeField(self.dm, np.full(hm.n, T0), bcs, name="T")
+        kf = neon.VolumeField(self.dm, kappa, [("zeroGradient", 0.0)] * hm.npatch)
+        self.gamma = neon.SurfaceInterpolation(self.dm, "linear").interpolate(kf)
+        self.T_old = self.T.internal.clone()
+        self.ls = neon.LinearSystem(self.dm)
+        self.terms = (abi.Term * 2)(*[t.struct() for t in (neon.ddt(self.T_old), neon.laplacian(self.gamma, -1.0))])
+        self.stats = []
+
+    def step(self):
+        L, s = abi.lib(), _s()
+        bc = self.T.bc_struct()
+        self.T_old.copy_(self.T.internal)
+        abi.check(L.fvgb_assemble(self.ls.handle, self.terms, 2, self.dt, C.byref(bc), abi.ptr(self.T.boundary), s))
+        st = abi.SolverStats()
+        abi.check(L.fvgb_solve(self.ls.handle, abi.ptr(self.T.internal), C.byref(self.cfg), C.byref(st), s),
+                  allow=(abi.ERR_NOT_CONVERGED,))
+        self.stats.append((st.num_iter, st.init_res_norm, st.final_res_norm, st.status))
+        abi.check(L.fvgb_bc_correct(self.dm.handle, 1, C.byref(bc), abi.ptr(self.T.internal),
+                                    abi.ptr(self.T.boundary), s))
+
+
 class CavityPiso:
     """Lid-driven cavity, neoIcoFoam PISO (no momentum predictor), pressure
     reference cell 0 = 0.

@@ -1151,6 +1151,11 @@ fvgb_status prepare(fvgb_ls* ls, cudaStream_t s, bool f32 = false) {
         if (st != FVGB_OK) return st;
     }
     if (f32) {
+        // the first FP32 V-cycle allocates its copies, uploads their descriptors and
+        // builds its graph: none of that may happen inside a caller's capture
+        if (!c->f32 && cs != cudaStreamCaptureStatusNone)
+            return fvgb_fail(FVGB_ERR_UNSUPPORTED,
+                             "multigrid: the first mixed-precision solve (FP32 setup) cannot be stream-captured");
         if (!c->f32 || c->f32_version != ls->version) {
             const bool first = !c->f32;
             fvgb_status st = to_f32(c, s);

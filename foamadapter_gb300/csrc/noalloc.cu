@@ -19,8 +19,10 @@
 //    other; the array keeps the last call's contents, so each call clears the
 //    counters it needs before use;
 //  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress, with that device current) and caches it; that
-//    first call should come before any stream capture.
+//    (cudaGetSymbolAddress, with that device current) and caches it;
+//  * every call is synchronous: it reads the solver state back between chunks
+//    of iterations, so it cannot run on a stream that is being captured into a
+//    CUDA graph and refuses one with FVGB_ERR_UNSUPPORTED before any work.
 // The arithmetic and the reduction tree are those of the graph-based FP64 solve
 // in solver.cu (same fma order per row, same 256-thread blocks and rows per thread), so the
 // iterates are the same bits.
@@ -312,10 +314,15 @@ extern "C" fvgb_status fvgb_pcg_csr_noalloc(int32_t n, const int32_t* row_offs, 
     FVGB_CHECK_ARG(cfg->precision == FVGB_PREC_FP64, "fvgb_pcg_csr_noalloc: FP64 precision only");
     FVGB_CHECK_ARG(cfg->rel_tol >= 0 && cfg->abs_tol >= 0 && cfg->max_iter >= 0,
                    "fvgb_pcg_csr_noalloc: bad tolerances or iteration cap");
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    FVGB_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED,
+                         "fvgb_pcg_csr_noalloc: synchronous, cannot be called on a capturing stream");
     double* base = nullptr;
     fvgb_status stt = scratch_for_current_device(&base);
     if (stt != FVGB_OK) return stt;
-    cudaStream_t s = (cudaStream_t)stream;
     const int rb = kT * na_rows_per_thread(n);
     const unsigned nb = (unsigned)((n + rb - 1) / rb);
     k_na_reset<<<1, 32, 0, s>>>(base, cfg->rel_tol, cfg->abs_tol, cfg->max_iter);
@@ -324,11 +331,11 @@ extern "C" fvgb_status fvgb_pcg_csr_noalloc(int32_t n, const int32_t* row_offs, 
     NaState host{};
     const double* st_dev = base + 4 * (size_t)kMaxRows + 2 * (size_t)kMaxBlocks;
     const int chunk = 16;
-    for (int launched = 0;; launched += chunk) {
+    for (int64_t launched = 0;; launched += chunk) {
         FVGB_CUDA_TRY(cudaMemcpyAsync(&host, st_dev, sizeof(NaState), cudaMemcpyDeviceToHost, s));
         FVGB_CUDA_TRY(cudaStreamSynchronize(s));
         if (host.done) break;
-        if (launched > cfg->max_iter + chunk)  // defensive: the device loop stops at max_iter
+        if (launched > (int64_t)cfg->max_iter + chunk)  // defensive: the device loop stops at max_iter
             return fvgb_fail(FVGB_ERR_CUDA, "fvgb_pcg_csr_noalloc: iteration bookkeeping lost");
         for (int k = 0; k < chunk; ++k) {
             k_na_spmv<<<nb, kT, 0, s>>>(base, n, row_offs, col_idxs, values);

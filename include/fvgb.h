@@ -411,8 +411,10 @@ fvgb_status fvgb_pgm_aggregate(int32_t n, const int32_t* row_offs, const int32_t
  * loads the library until the process exits), so n is limited to 262,144 rows
  * (larger n: FVGB_ERR_INVALID_ARG).  All calls on a device share that array:
  * calls that overlap on the GPU race.  The first call on a device looks up the
- * array's address; make that first call before any stream capture.
- * Synchronous; same criteria and the same iterates as fvgb_solve (FP64). */
+ * array's address.  Synchronous (it reads the solver state back between chunks
+ * of iterations): it must not be called on a stream that is being captured and
+ * refuses one with FVGB_ERR_UNSUPPORTED.  Same criteria and the same iterates
+ * as fvgb_solve (FP64). */
 fvgb_status fvgb_pcg_csr_noalloc(int32_t n, const int32_t* row_offs, const int32_t* col_idxs,
                                  const int32_t* diag_offset, const double* values,
                                  const double* rhs, double* x, const fvgb_solver_cfg* cfg,

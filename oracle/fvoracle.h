@@ -57,6 +57,21 @@ typedef struct or_solver_stats {
     int32_t num_iter, num_outer, status, reserved;
 } or_solver_stats;
 
+/* Caller-allocated HOST arrays of a hex box (boxmesh.c); C, Cf, bCf and points may be NULL. */
+typedef struct or_box_arrays {
+    double *V, *C;                                   /* [n], [3n]            */
+    int32_t *own, *nei;                              /* [nif]                */
+    double *Sf, *Cf, *magSf, *w, *delta;             /* [3nif] [3nif] [nif]  */
+    int32_t* bcells;                                 /* [nbf]                */
+    double *bSf, *bCf, *bmagSf, *bw, *bdelta;        /* [3nbf] [3nbf] [nbf]  */
+    int32_t* patch_offs;                             /* [npatch + 1]         */
+    double* points;                                  /* [3 n_points]         */
+} or_box_arrays;
+/* sizes: [n_points, n_cells, n_ifaces, n_bfaces (flat, non-empty), n_patches, n_faces_total] */
+int32_t or_box_sizes(int32_t nx, int32_t ny, int32_t nz, int32_t two_d, int64_t out[6]);
+int32_t or_box_build(int32_t nx, int32_t ny, int32_t nz, double lx, double ly, double lz, double jitter,
+                     uint64_t seed, int32_t two_d, or_box_arrays* out);
+
 void or_set_threads(int32_t nthreads);
 int32_t or_get_threads(void);
 

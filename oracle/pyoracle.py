@@ -21,6 +21,11 @@ class OrMesh(C.Structure):
                 ("bcells", vp), ("bSf", vp), ("bmagSf", vp), ("bw", vp), ("bdelta", vp), ("patch_offs", vp)]
 
 
+class OrBoxArrays(C.Structure):
+    _fields_ = [(name, vp) for name in ("V", "C", "own", "nei", "Sf", "Cf", "magSf", "w", "delta", "bcells", "bSf",
+                                        "bCf", "bmagSf", "bw", "bdelta", "patch_offs", "points")]
+
+
 class OrCsr(C.Structure):
     _fields_ = [("n", i32), ("nnz", i32), ("row_offs", vp), ("col", vp), ("diag_off", vp),
                 ("own_off", vp), ("nei_off", vp)]
@@ -54,6 +59,9 @@ def lib():
         _lib.or_sparsity.restype = i32
         _lib.or_solve.restype = i32
         _lib.or_get_threads.restype = i32
+        _lib.or_box_sizes.restype = i32
+        _lib.or_box_build.restype = i32
+        _lib.or_box_build.argtypes = [i32, i32, i32, dbl, dbl, dbl, dbl, C.c_uint64, i32, C.c_void_p]
     return _lib
 
 
@@ -232,6 +240,45 @@ class Oracle:
         fl = np.asarray(fixed_flux, np.int32)
         self.L.or_constrain_pressure(C.byref(self.m), p(fl), p(phiHbyA), p(U_b), p(rAUf), p(p_ref))
         return p_ref
+
+
+class BoxMesh:
+    """The arrays of a hex box as the oracle builds it (boxmesh.c), with the
+    attribute names of the library's host mesh: n, nif, nbf, npatch, V, C, own,
+    nei, Sf, Cf, magSf, w, delta, bcells, bSf, bCf, bmagSf, bw, bdelta,
+    patch_offsets, patch_names, points."""
+
+    def __init__(self, nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=0, two_d=False):
+        L = lib()
+        sz = (C.c_int64 * 6)()
+        if L.or_box_sizes(nx, ny, nz, 1 if two_d else 0, sz) != 0:
+            raise ValueError("bad box size")
+        npts, n, nif, nbf, npatch, _ = (int(v) for v in sz)
+        self.n, self.nif, self.nbf, self.npatch = n, nif, nbf, npatch
+        self.V, self.C = np.zeros(n), np.zeros((n, 3))
+        self.own, self.nei = np.zeros(nif, np.int32), np.zeros(nif, np.int32)
+        self.Sf, self.Cf = np.zeros((nif, 3)), np.zeros((nif, 3))
+        self.magSf, self.w, self.delta = np.zeros(nif), np.zeros(nif), np.zeros(nif)
+        self.bcells = np.zeros(nbf, np.int32)
+        self.bSf, self.bCf = np.zeros((nbf, 3)), np.zeros((nbf, 3))
+        self.bmagSf, self.bw, self.bdelta = np.zeros(nbf), np.zeros(nbf), np.zeros(nbf)
+        self.patch_offsets = np.zeros(npatch + 1, np.int32)
+        self.points = np.zeros((npts, 3))
+        self.patch_names = ["xmin", "xmax", "ymin", "ymax"] + ([] if two_d else ["zmin", "zmax"])
+        arr = OrBoxArrays(*[a.ctypes.data for a in (self.V, self.C, self.own, self.nei, self.Sf, self.Cf, self.magSf,
+                                                     self.w, self.delta, self.bcells, self.bSf, self.bCf, self.bmagSf,
+                                                     self.bw, self.bdelta, self.patch_offsets, self.points)])
+        r = L.or_box_build(nx, ny, nz, lx, ly, lz, jitter, seed, 1 if two_d else 0, C.byref(arr))
+        if r != 0:
+            raise ValueError(f"or_box_build failed ({r})")
+
+    @property
+    def nnz(self) -> int:
+        return self.n + 2 * self.nif
+
+    def patch_slice(self, name: str) -> slice:
+        p = self.patch_names.index(name)
+        return slice(int(self.patch_offsets[p]), int(self.patch_offsets[p + 1]))
 
 
 def dot_tree(a: np.ndarray, b: np.ndarray) -> float:

@@ -237,3 +237,30 @@ def test_multigrid_rejected_by_batches(cuda):
     cfg = abi.SolverCfg(1e-8, 0.0, 100, abi.PREC_FP64, 0.1, 1000, 50, 0, 0, abi.SOLVER_CG, abi.PRECOND_MULTIGRID)
     x = s["x0"].clone()
     assert abi.lib().fvgb_batch_solve(b.handle, abi.ptr(x), C.byref(cfg), None, None) == abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.gpu
+def test_first_mixed_multigrid_solve_refuses_capture(cuda):
+    """The first FP32 V-cycle sets up its copies and graph (allocations, a
+    synchronous upload): issued on a capturing stream after an uncaptured FP64
+    multigrid solve, it is refused with ERR_UNSUPPORTED before any GPU work, and
+    the same solve outside the capture then works."""
+    s = gpu_system(cuda, (12, 10, 8))
+    torch, ls = s["torch"], s["ls"]
+    x = s["x0"].clone()
+    assert ls.solve(x, rel_tol=1e-9, preconditioner=abi.PRECOND_MULTIGRID).status == abi.OK
+    cfg = abi.SolverCfg(1e-9, 0.0, 500, abi.PREC_MIXED_IR, 0.1, 1000, 50, 0, 0, abi.SOLVER_CG,
+                        abi.PRECOND_MULTIGRID)
+    stats = torch.zeros(8, dtype=torch.int32, device="cuda")
+    xm = s["x0"].clone()
+    g = torch.cuda.CUDAGraph()
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")            # the refused capture leaves an empty graph
+        with torch.cuda.graph(g):
+            status = abi.lib().fvgb_solve_async(ls.handle, abi.ptr(xm), C.byref(cfg), stats.data_ptr(),
+                                                torch.cuda.current_stream().cuda_stream)
+    assert status == abi.ERR_UNSUPPORTED
+    assert b"captured" in abi.lib().fvgb_last_error()
+    st = ls.solve(xm, rel_tol=1e-9, precision=abi.PREC_MIXED_IR, preconditioner=abi.PRECOND_MULTIGRID)
+    assert st.status == abi.OK

@@ -51,3 +51,22 @@ def test_polymesh_path_matches_box_builder():
     from conftest import load_polymesh  # noqa: F401  (fixture helper import keeps path setup)
     pts = hm.points
     assert pts is not None and len(pts) == 5 * 4 * 3
+
+
+@pytest.mark.parametrize("args,kw", [((7, 6, 5), dict(jitter=0.1, seed=9)),
+                                     ((16, 12, 1), dict(jitter=0.05, seed=3, two_d=True)),
+                                     ((5, 5, 1), dict(two_d=True)), ((1, 1, 1), {}), ((37, 1, 1), {}),
+                                     ((40, 32, 28), dict(jitter=0.1, seed=12345))])
+def test_oracle_box_builder_equals_library_builder(args, kw):
+    """The oracle's own box builder (oracle/boxmesh.c, used by the CPU legs of
+    the benchmark so that they never load the GPU library) produces the
+    library's host mesh arrays bit for bit."""
+    from oracle.pyoracle import BoxMesh
+
+    a, b = mesh.box(*args, **kw), BoxMesh(*args, **kw)
+    for f in ("V", "C", "own", "nei", "Sf", "Cf", "magSf", "w", "delta", "bcells", "bSf", "bCf", "bmagSf", "bw",
+              "bdelta", "patch_offsets", "points"):
+        x, y = np.asarray(getattr(a, f)), np.asarray(getattr(b, f))
+        assert x.shape == y.shape, f
+        np.testing.assert_array_equal(x, y, err_msg=f)
+    assert a.patch_names == b.patch_names and (a.n, a.nif, a.nbf, a.npatch) == (b.n, b.nif, b.nbf, b.npatch)

@@ -95,3 +95,37 @@ def test_noalloc_rejects_oversize_and_mixed(cuda):
     cfg.precision = abi.PREC_MIXED_IR
     status, _ = call_noalloc(4, (dummy_i, dummy_i, dummy_i), dummy_d, dummy_d, dummy_d, cfg)
     assert status == abi.ERR_INVALID_ARG
+
+
+def test_noalloc_without_iteration_cap(cuda):
+    """max_iter = INT32_MAX, a common way to say "no cap": the host-side
+    bookkeeping of launched iterations must not overflow."""
+    hm, dm, T, ls = heat_system(14, 12, 10)
+    pattern, values, rhs = csr_on_device(dm, ls)
+    x_ref = T.internal.clone()
+    ls.solve(x_ref, rel_tol=1e-8)
+    cfg = abi.SolverCfg(1e-8, 0.0, 2 ** 31 - 1, abi.PREC_FP64, 0.0, 0, 0)
+    x = T.internal.clone()
+    status, st = call_noalloc(hm.n, pattern, values, rhs, x, cfg)
+    assert status == abi.OK and st.num_iter > 10
+    torch.testing.assert_close(x, x_ref, rtol=0, atol=0)
+
+
+def test_noalloc_refuses_a_capturing_stream(cuda):
+    """The entry point is synchronous: on a stream being captured into a CUDA
+    graph it returns ERR_UNSUPPORTED before any GPU work, and works afterwards."""
+    import warnings
+
+    hm, dm, T, ls = heat_system(10, 9, 8)
+    pattern, values, rhs = csr_on_device(dm, ls)
+    cfg = abi.SolverCfg(1e-8, 0.0, 1000, abi.PREC_FP64, 0.0, 0, 0)
+    x = T.internal.clone()
+    g = torch.cuda.CUDAGraph()
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")            # the refused capture leaves an empty graph
+        with torch.cuda.graph(g):
+            status, _ = call_noalloc(hm.n, pattern, values, rhs, x, cfg)
+    assert status == abi.ERR_UNSUPPORTED
+    assert torch.equal(x, T.internal)
+    status, st = call_noalloc(hm.n, pattern, values, rhs, x, cfg)
+    assert status == abi.OK and st.num_iter > 5
