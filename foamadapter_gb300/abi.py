@@ -77,7 +77,8 @@ class ServerCfg(C.Structure):
 
 class ServeRequest(C.Structure):
     _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("steps", i32), ("U", dbl * 3), ("D", dbl), ("dt", dbl),
-                ("precision", i32), ("kernel_mode", i32), ("flags", i32), ("reserved", i32), ("T_out", vp)]
+                ("precision", i32), ("kernel_mode", i32), ("flags", i32), ("reserved", i32), ("T_out", vp),
+                ("T_init", vp)]
 
 
 SERVE_REASSEMBLE = 1

@@ -10,10 +10,14 @@
 // internal faces by owner then +x, +y, +z, boundary faces patch by patch
 // (xmin, xmax, ymin, ymax, zmin, zmax), each patch grouped by box.  Boxes start
 // at multiples of 32 cells; cells in the gaps are isolated placeholders
-// (volume 1, no faces).  Geometry is analytic (weights 0.5, delta 1/h, boundary
-// delta 2/h), so values can differ in the last bits from the triangle-
-// decomposition geometry of the host builder; every result computed on such a
-// mesh is reproducible on the same mesh.
+// (volume 1, no faces).  Geometry is OpenFOAM's triangle decomposition with
+// the host builder's order of operations (meshgen.cpp; compiled here without
+// contraction, and double division and square root are correctly rounded on
+// the GPU as on the host): face centres and areas from the face's four points
+// in face order, cell centres and volumes from pyramids on an estimated centre
+// with the faces in face-list order (owned, then neighboured), weights and
+// non-orthogonal delta coefficients from the cell centres.  The arrays are
+// therefore bit-identical to those of the host builder (mesh.box + concat).
 #include <cmath>
 #include <vector>
 
@@ -26,7 +30,151 @@ struct BoxDev {
     int32_t cell0, face0;
     int32_t bface0[6];
     double hx, hy, hz;
+    double lx, ly, lz;
 };
+
+// ---- OpenFOAM geometry of a box face, in the host builder's operation order
+struct D3 {
+    double x, y, z;
+};
+__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ D3 operator-(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ D3 operator*(double s, D3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ D3 operator/(D3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ double dot3(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ D3 cross3(D3 a, D3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ double mag3(D3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+// vertex (i, j, k) of an unjittered box (the far faces land exactly on l)
+__device__ __forceinline__ D3 box_pt(const BoxDev& b, int i, int j, int k) {
+    return {i == b.nx ? b.lx : (double)i * b.hx, j == b.ny ? b.ly : (double)j * b.hy,
+            k == b.nz ? b.lz : (double)k * b.hz};
+}
+
+// the face of direction d (0 x, 1 y, 2 z) at vertex index (i, j, k), normal +d,
+// or -d when flip (the min patches): its points in the host builder's order
+__device__ __forceinline__ void face_pts(const BoxDev& b, int d, int i, int j, int k, bool flip, D3 p[4]) {
+    D3 a, q, c, e;
+    if (d == 0) {
+        a = box_pt(b, i, j, k); q = box_pt(b, i, j + 1, k); c = box_pt(b, i, j + 1, k + 1); e = box_pt(b, i, j, k + 1);
+    } else if (d == 1) {
+        a = box_pt(b, i, j, k); q = box_pt(b, i, j, k + 1); c = box_pt(b, i + 1, j, k + 1); e = box_pt(b, i + 1, j, k);
+    } else {
+        a = box_pt(b, i, j, k); q = box_pt(b, i + 1, j, k); c = box_pt(b, i + 1, j + 1, k); e = box_pt(b, i, j + 1, k);
+    }
+    p[0] = a;
+    p[1] = flip ? e : q;
+    p[2] = c;
+    p[3] = flip ? q : e;
+}
+
+// face centre and area vector: triangles about the mean of the points
+__device__ __forceinline__ void face_geom(const D3 p[4], D3& fC, D3& fA) {
+    D3 cen = p[0];
+    cen = cen + p[1];
+    cen = cen + p[2];
+    cen = cen + p[3];
+    cen = cen / 4.0;
+    D3 sN{0.0, 0.0, 0.0}, sAc{0.0, 0.0, 0.0};
+    double sA = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const D3 a = p[q], nb = p[(q + 1) & 3];
+        const D3 c = a + nb + cen;
+        const D3 nr = cross3(nb - a, cen - a);
+        const double m = mag3(nr);
+        sN = sN + nr;
+        sA += m;
+        sAc = sAc + m * c;
+    }
+    if (sA < 1.0e-150) {
+        fC = cen;
+        fA = D3{0.0, 0.0, 0.0};
+    } else {
+        fC = ((1.0 / 3.0) * sAc) / sA;
+        fA = 0.5 * sN;
+    }
+}
+
+// the faces of cell (i, j, k) in the order they contribute to it on the host
+// (face-list order: owned internal +x +y +z, owned boundary by patch, then the
+// internal faces it neighbours, -z -y -x): direction, vertex index, flip, owner
+struct CellFace {
+    int d, i, j, k;
+    bool flip, owner;
+};
+__device__ __forceinline__ int cell_faces(const BoxDev& b, int i, int j, int k, CellFace f[6]) {
+    int n = 0;
+    if (i < b.nx - 1) f[n++] = {0, i + 1, j, k, false, true};
+    if (j < b.ny - 1) f[n++] = {1, i, j + 1, k, false, true};
+    if (k < b.nz - 1) f[n++] = {2, i, j, k + 1, false, true};
+    if (i == 0) f[n++] = {0, 0, j, k, true, true};
+    if (i == b.nx - 1) f[n++] = {0, b.nx, j, k, false, true};
+    if (j == 0) f[n++] = {1, i, 0, k, true, true};
+    if (j == b.ny - 1) f[n++] = {1, i, b.ny, k, false, true};
+    if (k == 0) f[n++] = {2, i, j, 0, true, true};
+    if (k == b.nz - 1) f[n++] = {2, i, j, b.nz, false, true};
+    if (k > 0) f[n++] = {2, i, j, k, false, false};
+    if (j > 0) f[n++] = {1, i, j, k, false, false};
+    if (i > 0) f[n++] = {0, i, j, k, false, false};
+    return n;
+}
+
+// centre and volume of cell (i, j, k): pyramids on the mean of its face centres
+__device__ __forceinline__ void cell_geom(const BoxDev& b, int i, int j, int k, D3& cc, double& vol) {
+    CellFace f[6];
+    const int nf = cell_faces(b, i, j, k, f);
+    D3 fC[6], fA[6];
+    D3 est{0.0, 0.0, 0.0};
+    for (int q = 0; q < nf; ++q) {
+        D3 p[4];
+        face_pts(b, f[q].d, f[q].i, f[q].j, f[q].k, f[q].flip, p);
+        face_geom(p, fC[q], fA[q]);
+        est = est + fC[q];
+    }
+    est = est / (double)nf;
+    D3 c{0.0, 0.0, 0.0};
+    double v = 0.0;
+    for (int q = 0; q < nf; ++q) {
+        const double pv = f[q].owner ? dot3(fA[q], fC[q] - est) : dot3(fA[q], est - fC[q]);
+        const D3 pc = (3.0 / 4.0) * fC[q] + (1.0 / 4.0) * est;
+        c = c + pv * pc;
+        v += pv;
+    }
+    cc = fabs(v) > 1.0e-300 ? c / v : est;
+    vol = v * (1.0 / 3.0);
+}
+
+__global__ void k_box_centres(const BoxDev* __restrict__ boxes, const int32_t* __restrict__ slice_box, int N,
+                              double* __restrict__ V, double* __restrict__ invV, double* __restrict__ Cc) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const int bi = slice_box[c >> 5];
+    int loc = -1;
+    BoxDev b;
+    if (bi >= 0) {
+        b = boxes[bi];
+        loc = c - b.cell0;
+        if (loc >= b.n) loc = -1;
+    }
+    if (loc < 0) {  // placeholder cell
+        V[c] = 1.0;
+        invV[c] = 1.0;
+        Cc[3 * c] = Cc[3 * c + 1] = Cc[3 * c + 2] = 0.0;
+        return;
+    }
+    const int i = loc % b.nx, j = (loc / b.nx) % b.ny, k = loc / (b.nx * b.ny);
+    D3 cc;
+    double vol;
+    cell_geom(b, i, j, k, cc, vol);
+    V[c] = vol;
+    invV[c] = 1.0 / vol;
+    Cc[3 * c] = cc.x;
+    Cc[3 * c + 1] = cc.y;
+    Cc[3 * c + 2] = cc.z;
+}
 
 // internal faces owned by cells before local cell (i,j,k) of the box
 __device__ __forceinline__ int32_t faces_before(const BoxDev& b, int i, int j, int k) {
@@ -60,7 +208,7 @@ constexpr int kGW = 6;  // gather-list width (every box cell has 6 faces)
 constexpr int kMW = 7;  // matrix row width
 
 __global__ void k_box_cells(const BoxDev* __restrict__ boxes, const int32_t* __restrict__ slice_box, int N,
-                            int nif, MeshOut o) {
+                            int nif, const double* __restrict__ Cc, MeshOut o) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= N) return;
     const int slice = c >> 5, lane = c & 31;
@@ -73,9 +221,7 @@ __global__ void k_box_cells(const BoxDev* __restrict__ boxes, const int32_t* __r
         loc = c - b.cell0;
         if (loc >= b.n) loc = -1;
     }
-    if (loc < 0) {  // placeholder: unit volume, no faces, diagonal-only row
-        o.V[c] = 1.0;
-        o.invV[c] = 1.0;
+    if (loc < 0) {  // placeholder: unit volume (k_box_centres), no faces, diagonal-only row
         for (int k = 0; k < kGW; ++k) {
             o.g_code[gbase + k * 32] = FVGB_PAD;
             o.g_other[gbase + k * 32] = 0;
@@ -91,32 +237,38 @@ __global__ void k_box_cells(const BoxDev* __restrict__ boxes, const int32_t* __r
     const int nx = b.nx, ny = b.ny, nz = b.nz;
     const int i = loc % nx, j = (loc / nx) % ny, k = loc / (nx * ny);
     const int sy = nx, sz = nx * ny;
-    const double ax = b.hy * b.hz, ay = b.hx * b.hz, az = b.hx * b.hy;
-    const double vol = (b.hx * b.hy) * b.hz;
-    o.V[c] = vol;
-    o.invV[c] = 1.0 / vol;
-    // upper faces owned by this cell
+    const D3 Co{Cc[3 * c], Cc[3 * c + 1], Cc[3 * c + 2]};
+    // upper faces owned by this cell: weights and delta coefficients as
+    // surfaceInterpolation::makeWeights / makeNonOrthDeltaCoeffs
     int32_t f = b.face0 + faces_before(b, i, j, k);
     const int32_t fx = i < nx - 1 ? f++ : -1;
     const int32_t fy = j < ny - 1 ? f++ : -1;
     const int32_t fz = k < nz - 1 ? f++ : -1;
     const int32_t up_f[3] = {fx, fy, fz};
     const int32_t up_n[3] = {c + 1, c + sy, c + sz};
-    const double up_a[3] = {ax, ay, az};
-    const double up_h[3] = {b.hx, b.hy, b.hz};
     for (int d = 0; d < 3; ++d) {
         const int32_t ff = up_f[d];
         if (ff < 0) continue;
+        D3 p[4], Cf, Sf;
+        face_pts(b, d, i + (d == 0), j + (d == 1), k + (d == 2), false, p);
+        face_geom(p, Cf, Sf);
+        const int32_t cn = up_n[d];
+        const D3 Cn{Cc[3 * cn], Cc[3 * cn + 1], Cc[3 * cn + 2]};
+        const double mS = mag3(Sf);
+        const double dOwn = fabs(dot3(Sf, Cf - Co));
+        const double dNei = fabs(dot3(Sf, Cn - Cf));
+        const D3 dl = Cn - Co;
+        const double nd = dot3(Sf / mS, dl), md = 0.05 * mag3(dl);
+        const double dc = 1.0 / (nd > md ? nd : md);
         o.own[ff] = c;
-        o.nei[ff] = up_n[d];
-        o.Sf[3 * ff] = d == 0 ? ax : 0.0;
-        o.Sf[3 * ff + 1] = d == 1 ? ay : 0.0;
-        o.Sf[3 * ff + 2] = d == 2 ? az : 0.0;
-        o.magSf[ff] = up_a[d];
-        o.w[ff] = 0.5;
-        const double dc = 1.0 / up_h[d];
+        o.nei[ff] = cn;
+        o.Sf[3 * ff] = Sf.x;
+        o.Sf[3 * ff + 1] = Sf.y;
+        o.Sf[3 * ff + 2] = Sf.z;
+        o.magSf[ff] = mS;
+        o.w[ff] = dNei / (dOwn + dNei);
         o.delta[ff] = dc;
-        o.geo[ff] = up_a[d] * dc;
+        o.geo[ff] = mS * dc;
     }
     // lower faces (this cell is the neighbour), ascending face index: -z, -y, -x
     int32_t lo_f[3], lo_o[3];
@@ -136,25 +288,33 @@ __global__ void k_box_cells(const BoxDev* __restrict__ boxes, const int32_t* __r
     // boundary faces of this cell, patch order
     int32_t bf[6];
     int nb = 0;
-    const double bdc[3] = {2.0 / b.hx, 2.0 / b.hy, 2.0 / b.hz};
-    auto bface = [&](int patch, int32_t idx, int d, double sign) {
+    // the face at vertex index (fi, fj, fk) of direction d; the min patches flip it
+    auto bface = [&](int patch, int32_t idx, int d, int fi, int fj, int fk) {
         const int32_t bb = b.bface0[patch] + idx;
+        D3 p[4], Cf, Sf;
+        face_pts(b, d, fi, fj, fk, (patch & 1) == 0, p);
+        face_geom(p, Cf, Sf);
+        const double mS = mag3(Sf);
+        const D3 nf = Sf / mS;
+        const D3 dl = dot3(nf, Cf - Co) * nf;
+        const double nd = dot3(nf, dl), md = 0.05 * mag3(dl);
+        const double dc = 1.0 / (nd > md ? nd : md);
         o.bcells[bb] = c;
-        o.bSf[3 * bb] = d == 0 ? sign * ax : 0.0;
-        o.bSf[3 * bb + 1] = d == 1 ? sign * ay : 0.0;
-        o.bSf[3 * bb + 2] = d == 2 ? sign * az : 0.0;
-        o.bmagSf[bb] = up_a[d];
-        o.bdelta[bb] = bdc[d];
-        o.bgeo[bb] = up_a[d] * bdc[d];
+        o.bSf[3 * bb] = Sf.x;
+        o.bSf[3 * bb + 1] = Sf.y;
+        o.bSf[3 * bb + 2] = Sf.z;
+        o.bmagSf[bb] = mS;
+        o.bdelta[bb] = dc;
+        o.bgeo[bb] = mS * dc;
         o.bpatch[bb] = patch;
         bf[nb++] = bb;
     };
-    if (i == 0) bface(0, j + ny * k, 0, -1.0);
-    if (i == nx - 1) bface(1, j + ny * k, 0, 1.0);
-    if (j == 0) bface(2, i + nx * k, 1, -1.0);
-    if (j == ny - 1) bface(3, i + nx * k, 1, 1.0);
-    if (k == 0) bface(4, i + nx * j, 2, -1.0);
-    if (k == nz - 1) bface(5, i + nx * j, 2, 1.0);
+    if (i == 0) bface(0, j + ny * k, 0, 0, j, k);
+    if (i == nx - 1) bface(1, j + ny * k, 0, nx, j, k);
+    if (j == 0) bface(2, i + nx * k, 1, i, 0, k);
+    if (j == ny - 1) bface(3, i + nx * k, 1, i, ny, k);
+    if (k == 0) bface(4, i + nx * j, 2, i, j, 0);
+    if (k == nz - 1) bface(5, i + nx * j, 2, i, j, nz);
     // gather list
     int g = 0;
     for (int q = 0; q < nlo; ++q, ++g) {
@@ -247,6 +407,9 @@ extern "C" fvgb_status fvgb_mesh_create_boxes(const fvgb_box_spec* specs, int32_
         b.hx = s.lx / s.nx;
         b.hy = s.ly / s.ny;
         b.hz = s.lz / s.nz;
+        b.lx = s.lx;
+        b.ly = s.ly;
+        b.lz = s.lz;
         const int64_t pf[6] = {(int64_t)s.ny * s.nz, (int64_t)s.ny * s.nz, (int64_t)s.nx * s.nz,
                                (int64_t)s.nx * s.nz, (int64_t)s.nx * s.ny, (int64_t)s.nx * s.ny};
         for (int p = 0; p < 6; ++p) nb_patch[p] += pf[p];
@@ -325,6 +488,8 @@ extern "C" fvgb_status fvgb_mesh_create_boxes(const fvgb_box_spec* specs, int32_
     A(&o.nei_pos, NIF);
     A(&d_slice_box, nslices);
     A(&d_boxes, nboxes);
+    double* d_centres = nullptr;  // cell centres, the weights' input
+    A(&d_centres, 3 * N);
     cudaStream_t st = (cudaStream_t)stream;
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_slice_box, slice_box.data(), 4 * (size_t)nslices, cudaMemcpyHostToDevice, st);
@@ -336,7 +501,8 @@ extern "C" fvgb_status fvgb_mesh_create_boxes(const fvgb_box_spec* specs, int32_
     }
     k_fill_ptr<<<grid_for(nslices + 1, 256), 256, 0, st>>>(g_ptr, nslices, kGW);
     k_fill_ptr<<<grid_for(nslices + 1, 256), 256, 0, st>>>(m_ptr, nslices, kMW);
-    k_box_cells<<<grid_for(N, 256), 256, 0, st>>>(d_boxes, d_slice_box, (int)N, (int)NIF, o);
+    k_box_centres<<<grid_for(N, 128), 128, 0, st>>>(d_boxes, d_slice_box, (int)N, o.V, o.invV, d_centres);
+    k_box_cells<<<grid_for(N, 128), 128, 0, st>>>(d_boxes, d_slice_box, (int)N, (int)NIF, d_centres, o);
     // no synchronisation: asynchronous copies from pageable host memory are staged
     // before the call returns, so the host vectors may go out of scope
     e = cudaGetLastError();

@@ -174,7 +174,13 @@ fvgb_status setup(fvgb_server* sv, Slot* s) {
     if (e != cudaSuccess) return fvgb_fail(FVGB_ERR_OOM, "server: request allocation");
     const int nn = s->n, rn = r.nx * r.ny * r.nz;
     k_fill<<<(nn + 255) / 256, 256, 0, s->stream>>>(s->T, nn, 0.0);
-    k_blob<<<(rn + 255) / 256, 256, 0, s->stream>>>(s->T, r.nx, r.ny, r.nz, range[0]);
+    if (r.T_init) {
+        if (cudaMemcpyAsync(s->T + range[0], r.T_init, sizeof(double) * (size_t)rn, cudaMemcpyHostToDevice,
+                            s->stream) != cudaSuccess)
+            return fvgb_fail(FVGB_ERR_CUDA, "server: initial field upload");
+    } else {
+        k_blob<<<(rn + 255) / 256, 256, 0, s->stream>>>(s->T, r.nx, r.ny, r.nz, range[0]);
+    }
     k_fill<<<(int)((nbf + 255) / 256 + 1), 256, 0, s->stream>>>(s->ref, (int)nbf, 0.0);
     k_fill<<<(int)((nf + 255) / 256), 256, 0, s->stream>>>(s->gamma, (int)nf, r.D);
     k_fill3<<<(nn + 255) / 256, 256, 0, s->stream>>>(s->U, nn, r.U[0], r.U[1], r.U[2]);

@@ -477,8 +477,10 @@ typedef struct fvgb_server_cfg {
 /* One request: the unit box [0,1]^3 with nx*ny*nz cells, a uniform velocity U,
  * diffusivity D, `steps` implicit steps of  ddt(T) + div(phi,T) - laplacian(D,T) = 0
  * (explicit upwind convection, implicit diffusion, zero-gradient walls, initial
- * Gaussian blob at the centre); dt <= 0 picks 0.5*h/|U|.  T_out: optional HOST
- * buffer [nx*ny*nz] that receives the final field. */
+ * Gaussian blob at the centre, or T_init); dt <= 0 picks 0.5*h/|U|.  T_out:
+ * optional HOST buffer [nx*ny*nz] that receives the final field.  T_init:
+ * optional HOST array [nx*ny*nz], the initial field instead of the blob; like
+ * T_out it must stay valid until the request's result is reported. */
 enum { FVGB_SERVE_REASSEMBLE = 1 };
 typedef struct fvgb_serve_request {
     int32_t nx, ny, nz, steps;
@@ -496,6 +498,7 @@ typedef struct fvgb_serve_request {
                                   results)                                            */
     int32_t reserved;
     double* T_out;
+    const double* T_init;
 } fvgb_serve_request;
 typedef struct fvgb_serve_result {
     int64_t id;

@@ -93,3 +93,39 @@ class HeatTransferCPU:
         st = self.o.solve(v, r, self.T, rel_tol=self.rel_tol, max_iter=self.max_iter)
         self.stats.append((st.num_iter, st.init_res_norm, st.final_res_norm, st.status))
         self.o.bc_correct(1, self.types, self.ref, self.T, self.Tb)
+
+
+class ServedRequestCPU:
+    """One request of the serving loop on the oracle: the unit box with nx*ny*nz
+    cells (unjittered), uniform velocity U, diffusivity D, and `steps` IMEX
+    steps of ddt(T) + div(phi, T) - laplacian(D, T) = 0 -- explicit upwind
+    convection of the old field, implicit ddt + diffusion, zero-gradient walls,
+    Jacobi-PCG (FP64 or mixed) to 1e-8 with the server's solver settings."""
+
+    def __init__(self, nx, ny, nz, U, D, dt, T0, precision=0):
+        from .pyoracle import BoxMesh
+
+        self.hm = hm = BoxMesh(nx, ny, nz)
+        self.o = o = Oracle(hm)
+        self.dt, self.precision = dt, precision
+        U = np.asarray(U, np.float64)
+        self.F = o.flux_vec(np.tile(U, hm.n), np.tile(U, hm.nbf))
+        self.gamma = np.full(hm.nif + hm.nbf, D)
+        self.types = np.full(hm.npatch, FIXED_GRADIENT, np.int32)
+        self.ref = np.zeros(hm.nbf)
+        self.T = np.array(T0, dtype=np.float64)
+        self.Tb = np.zeros(hm.nbf)
+        o.bc_correct(1, self.types, self.ref, self.T, self.Tb)
+        self.iters = 0
+
+    def step(self):
+        o = self.o
+        old = self.T.copy()
+        v, r, _, _ = o.assemble(1, [(DDT, 0, 1.0, old, None), (6, UPWIND, 1.0, old, self.F),
+                                    (LAP, 0, -1.0, None, self.gamma)], self.dt, self.types, self.ref, self.Tb)
+        st = o.solve(v, r, self.T, rel_tol=1e-8, max_iter=2000, precision=self.precision, inner_rel_tol=0.1,
+                     inner_max_iter=1000, max_outer=50)
+        if st.status != 0:
+            raise RuntimeError(f"oracle solve status {st.status}")
+        self.iters += st.num_iter
+        o.bc_correct(1, self.types, self.ref, self.T, self.Tb)

@@ -1,12 +1,12 @@
 """Device-built box meshes and the serving loop.
 
-* fvgb_mesh_create_boxes builds packed boxes on the device; its analytic
-  geometry must reproduce the host-built mesh's operators to round-off.
+* fvgb_mesh_create_boxes builds packed boxes on the device with the host
+  builder's OpenFOAM geometry and operation order: every operator and solve
+  on it gives the bits of the host-built mesh.
 * The server runs every request exactly as it would run alone: a request's
   final field is bit-identical whether it ran by itself or among others
-  (the continuous-batching equivalence the serving design promises), and it
-  agrees with the same IMEX steps driven through the Python API on a
-  host-built mesh to round-off.
+  (the continuous-batching equivalence the serving design promises), and
+  bit-identical to the CPU oracle running the same IMEX steps.
 """
 import ctypes as C
 import time
@@ -77,7 +77,7 @@ def test_device_boxes_match_host_boxes(cuda):
         ls.solve(x, rel_tol=1e-10)
         outs.append([a.cpu().numpy() for a in (F.values, div, grad, ls.apply(T.internal), x)])
     for a, b in zip(*outs):
-        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * max(1.0, np.abs(a).max()))
+        np.testing.assert_array_equal(a, b)
     abi.lib().fvgb_mesh_destroy(hdev)
 
 
@@ -88,10 +88,16 @@ def make_server(budget=8 << 30, streams=4, max_active=64):
     return h
 
 
-def submit(server, nx, ny, nz, steps, U, D, precision=abi.PREC_FP64, flags=0):
+_KEEP = []  # initial fields stay alive until their requests are reported
+
+
+def submit(server, nx, ny, nz, steps, U, D, precision=abi.PREC_FP64, flags=0, dt=0.0, T0=None):
     out = np.zeros(nx * ny * nz)
-    req = abi.ServeRequest(nx=nx, ny=ny, nz=nz, steps=steps, U=(C.c_double * 3)(*U), D=D, dt=0.0,
-                           precision=precision, kernel_mode=0, flags=flags, T_out=out.ctypes.data)
+    req = abi.ServeRequest(nx=nx, ny=ny, nz=nz, steps=steps, U=(C.c_double * 3)(*U), D=D, dt=dt,
+                           precision=precision, kernel_mode=0, flags=flags, T_out=out.ctypes.data,
+                           T_init=None if T0 is None else T0.ctypes.data)
+    if T0 is not None:
+        _KEEP.append(T0)
     rid = C.c_int64()
     st = abi.lib().fvgb_server_submit(server, C.byref(req), C.byref(rid))
     return st, rid.value, out
@@ -139,30 +145,38 @@ def test_served_results_same_alone_and_in_the_mix(cuda, precision):
         assert res[rid].finish_s >= res[rid].start_s >= res[rid].submit_s
 
 
-def test_served_matches_python_driver(cuda):
-    nx, ny, nz, steps, U, D = REQS[0]
-    sv = make_server()
-    st, rid, out = submit(sv, nx, ny, nz, steps, U, D)
-    drain(sv, 1)
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED_IR])
+def test_served_requests_match_the_oracle(cuda, precision):
+    """Every request of a mix (served together, and one of them also alone)
+    gives the oracle's field bit for bit after the same IMEX steps from the same
+    initial field, with the same total number of CG iterations."""
+    from oracle.apps import ServedRequestCPU
+
+    rng = np.random.default_rng(17)
+    reqs = []
+    for nx, ny, nz, steps, U, D in REQS:
+        dt = 0.5 * (1.0 / max(nx, ny, nz)) / float(np.sqrt(np.dot(U, U)))
+        reqs.append((nx, ny, nz, steps, U, D, dt, 1.0 + rng.random(nx * ny * nz)))
+    sv = make_server(streams=3)
+    subs = [submit(sv, nx, ny, nz, st, U, D, precision=precision, dt=dt, T0=T0)
+            for nx, ny, nz, st, U, D, dt, T0 in reqs]
+    res = drain(sv, len(subs))
     abi.lib().fvgb_server_destroy(sv)
-    hm = mesh.box(nx, ny, nz)
-    dm = DeviceMesh(hm)
-    x, y, z = (hm.C[:, 0] - 0.5), (hm.C[:, 1] - 0.5), (hm.C[:, 2] - 0.5)
-    T = neon.VolumeField(dm, np.exp(-(x * x + y * y + z * z) / (2 * 0.1 * 0.1)), [("zeroGradient", 0.0)] * 6)
-    F = neon.SurfaceField(dm)
-    Uc, Ub = neon.dev(np.tile(U, hm.n)), neon.dev(np.tile(U, hm.nbf))  # held until the kernel has run
-    abi.check(abi.lib().fvgb_flux_vec(dm.handle, abi.ptr(Uc), abi.ptr(Ub), abi.ptr(F.values),
-                                      torch.cuda.current_stream().cuda_stream))
-    gam = neon.SurfaceField(dm, np.full(hm.nif + hm.nbf, D))
-    dt = 0.5 * (1.0 / max(nx, ny, nz)) / np.linalg.norm(U)
-    ls = neon.LinearSystem(dm)
-    old = T.internal.clone()
-    for _ in range(steps):
-        old.copy_(T.internal)
-        ls.assemble([neon.ddt(old), neon.div_explicit(F, old), neon.laplacian(gam, -1.0)], dt, T)
-        ls.solve(T.internal, rel_tol=1e-8, max_iter=2000)
-        T.correctBoundaryConditions()
-    np.testing.assert_allclose(out, T.host(), rtol=1e-7, atol=1e-9)
+    sv = make_server()
+    nx, ny, nz, st, U, D, dt, T0 = reqs[1]
+    _, rid1, alone = submit(sv, nx, ny, nz, st, U, D, precision=precision, dt=dt, T0=T0)
+    res1 = drain(sv, 1)
+    abi.lib().fvgb_server_destroy(sv)
+    for (nx, ny, nz, steps, U, D, dt, T0), (status, rid, out) in zip(reqs, subs):
+        cpu = ServedRequestCPU(nx, ny, nz, U, D, dt, T0, precision=1 if precision == abi.PREC_MIXED_IR else 0)
+        for _ in range(steps):
+            cpu.step()
+        assert status == abi.OK and res[rid].status == abi.OK and res[rid].steps_done == steps
+        assert res[rid].total_iters == cpu.iters
+        np.testing.assert_array_equal(out, cpu.T)
+        if (nx, ny, nz) == reqs[1][:3]:
+            assert res1[rid1].total_iters == cpu.iters
+            np.testing.assert_array_equal(alone, cpu.T)
 
 
 def test_server_budget_and_cancel(cuda):
