@@ -432,17 +432,21 @@ def run_advection(args):
             "cpu_baseline": {"value": fu / cpu_s, "cores": 1, "kind": "port", "sample": "100 steps, serial"}}
 
 
-def run_explicit(args):
+def run_explicit(args, hm=None, dm=None):
     """Every explicit operator once per launch on the 128^3 jittered box, each launch
-    timed alone with CUDA events after an L2 flush, against the HBM roofline.
-    Algorithmic bytes: int32 labels, every listed array once at its width."""
+    timed alone with CUDA events after an L2 flush, against the HBM roofline and
+    GB300's FP64 issue rate.  Algorithmic bytes: int32 labels, every listed array
+    once at its width.  Each operator's floor is the larger of its bytes at the
+    measured HBM bandwidth and its FP64 operations at the FP64 issue rate."""
     import torch
 
     from foamadapter_gb300 import abi, neon
     from foamadapter_gb300.mesh import DeviceMesh
 
-    hm, k = heat_inputs(args.explicit_n)
-    dm = DeviceMesh(hm)
+    if hm is None:
+        hm, k = heat_inputs(args.explicit_n)
+    if dm is None:
+        dm = DeviceMesh(hm)
     n, nif, nbf = hm.n, hm.nif, hm.nbf
     nbfa = active_bfaces(hm)
     rng = np.random.default_rng(7)
@@ -512,9 +516,12 @@ def run_explicit(args):
             times.append(e0.elapsed_time(e1))
         us = 1e3 * float(np.median(times))
         gbs = nbytes / (us * 1e-6) / 1e9
+        floor_us = 1e6 * max(nbytes / (peak * 1e9), fp64[name] / fp64_peak)
         res[name] = {"us": us, "alg_bytes": nbytes, "GBps": gbs, "frac_of_peak": gbs / peak,
-                     "fp64_ops": fp64[name], "fp64_frac_of_peak": fp64[name] / (us * 1e-6) / fp64_peak}
-    return {"workload": f"explicit operators, {args.explicit_n}^3 jittered box, one launch each, L2 flushed",
+                     "fp64_ops": fp64[name], "fp64_frac_of_peak": fp64[name] / (us * 1e-6) / fp64_peak,
+                     "floor_us": floor_us, "bound": "hbm" if nbytes / (peak * 1e9) >= fp64[name] / fp64_peak
+                     else "fp64", "frac_of_floor": floor_us / us}
+    return {"workload": f"explicit operators, {round(hm.n ** (1 / 3))}^3 jittered box, one launch each, L2 flushed",
             "n": n, "n_ifaces": nif, "n_bfaces": nbf, "peak_GBps": peak, "peak_source": peak_kind,
             "fp64_peak_ops_per_s": fp64_peak,
             "fp64_peak_source": "2 FP64 lanes per clock per SM (ncu peak_sustained) x SMs x max SM clock",
@@ -579,8 +586,9 @@ def run_convection(args):
                         "BiCGStab + Jacobi to 1e-8", "n": hm.n, "dt": dt, **out}
 
 
-def run_cavity(args):
-    """Lid-driven cavity PISO on 512x512x1: FP64 vs mixed-precision pressure solve."""
+def run_cavity(args, multigrid=True):
+    """Lid-driven cavity PISO on 512x512x1: FP64 vs mixed-precision pressure solve
+    (and the multigrid CG with FP64 and FP32 V-cycles)."""
     import torch
 
     from foamadapter_gb300 import abi, apps
@@ -588,9 +596,11 @@ def run_cavity(args):
     nsteps = args.cavity_steps
     out = {}
     fields = {}
-    for name, prec, pc in (("fp64", abi.PREC_FP64, abi.PRECOND_JACOBI), ("mixed", abi.PREC_MIXED_IR, abi.PRECOND_JACOBI),
-                           ("fp64_multigrid", abi.PREC_FP64, abi.PRECOND_MULTIGRID),
-                           ("multigrid_fp32_vcycle", abi.PREC_MIXED_IR, abi.PRECOND_MULTIGRID)):
+    legs = [("fp64", abi.PREC_FP64, abi.PRECOND_JACOBI), ("mixed", abi.PREC_MIXED_IR, abi.PRECOND_JACOBI)]
+    if multigrid:
+        legs += [("fp64_multigrid", abi.PREC_FP64, abi.PRECOND_MULTIGRID),
+                 ("multigrid_fp32_vcycle", abi.PREC_MIXED_IR, abi.PRECOND_MULTIGRID)]
+    for name, prec, pc in legs:
         case = apps.CavityPiso(n=512, precision=prec, preconditioner=pc)
         case.step()                                     # warm-up (builds the solver graphs)
         torch.cuda.synchronize()
@@ -607,7 +617,7 @@ def run_cavity(args):
                      "all_solves_ok": all(s[4] == abi.OK for s in case.stats),
                      "max_final_rel_residual": max(s[3] / s[2] if s[2] > 0 else 0.0 for s in case.stats)}
         fields[name] = (case.p.host(), case.U.host())
-    (p64, U64), (pm, Um), (pg, Ug) = fields["fp64"], fields["mixed"], fields["fp64_multigrid"]
+    (p64, U64), (pm, Um) = fields["fp64"], fields["mixed"]
 
     def err(p, U):
         return {"p_max": float(np.abs(p - p64).max()),
@@ -617,6 +627,10 @@ def run_cavity(args):
 
     out["speedup_step"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
     out["err_vs_fp64"] = err(pm, Um)
+    if not multigrid:
+        return {"workload": f"lid-driven cavity PISO 512x512x1, +-5% jitter, dt 5e-4, 2 correctors, {nsteps} steps",
+                "pressure_solve_to": "1e-8 relative FP64 residual", **out}
+    pg, Ug = fields["fp64_multigrid"]
     out["speedup_step_multigrid"] = out["fp64"]["ms_per_step"] / out["fp64_multigrid"]["ms_per_step"]
     out["err_vs_fp64_multigrid"] = err(pg, Ug)
     out["speedup_step_multigrid_fp32_vcycle"] = out["fp64"]["ms_per_step"] / out["multigrid_fp32_vcycle"]["ms_per_step"]
@@ -902,6 +916,29 @@ def run_serve(args):
     return out
 
 
+def run_targets(args, hm):
+    """The other targets' evidence, measured in the default run: every explicit
+    operator on the same 128^3 box (HBM and FP64 fractions, floor), the 512^2
+    cavity's pressure solve FP64 vs mixed over the first PISO steps, and a
+    64-case slice of the batched workload."""
+    import copy
+
+    out = {}
+    a = copy.copy(args)
+    a.explicit_ops = "interp_linear,interp_upwind,div_upwind,div_linear,grad,laplacian,sngrad,advect_euler"
+    a.explicit_reps = 10
+    a.cavity_steps = 3
+    a.cases, a.batch_steps, a.alone_cases = 64, 10, 16
+    for key, fn in (("explicit_operators", lambda: run_explicit(a, hm=hm)),
+                    ("cavity_512_pressure_solve", lambda: run_cavity(a, multigrid=False)),
+                    ("batch_64_case_slice", lambda: run_batch(a))):
+        try:
+            out[key] = fn()
+        except Exception as e:  # the headline line is printed whatever a side measurement does
+            out[key] = {"error": repr(e)}
+    return out
+
+
 def workload_config(args):
     return {"workload": f"implicit heat transfer {args.n}^3 jittered hex box, FP64 Jacobi-PCG to 1e-8",
             "cells": args.n ** 3, "dt": HEAT["dt"], "parallelism": "replicas",
@@ -918,6 +955,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--ref-max-steps", type=int, default=1000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the other targets' measurements")
     ap.add_argument("--workload", default="heat", choices=["heat", "advection", "cavity", "batch", "serve", "explicit",
                                                            "convection", "multigrid"])
     ap.add_argument("--requests", type=int, default=400)
@@ -997,6 +1035,8 @@ def main():
         "mixed_precision": r["mixed"],
         "autotune": r["tuning"],
     }
+    if not args.no_extras and world == 1:
+        line["targets"] = run_targets(args, hm)
     if not args.no_cpu and world == 1:
         # the oracle continues from the state the end-to-end steps started from
         # (after W + K steps): its first step must give the GPU's step bit for bit,
