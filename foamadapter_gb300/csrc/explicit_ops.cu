@@ -21,20 +21,17 @@ __device__ __forceinline__ int gwidth(const MeshView& m, int slice) {
 }
 
 // F >= 0.0 with IEEE semantics (true for +0 and -0 and +inf, false for NaN),
-// decided on the bit pattern so it costs no FP64 instruction: GB300 issues
-// FP64 at 2 lanes per clock per SM, which bounds every FP64 face loop here.
+// decided on the bit pattern so it costs no FP64 instruction: GB300's FP64
+// issue rate bounds every FP64 face loop here.
 __device__ __forceinline__ bool nonneg(double F) {
     const long long u = __double_as_longlong(F);
     return u >= 0 ? u <= 0x7ff0000000000000LL : u == (long long)0x8000000000000000ULL;
 }
 
-// s - x is by definition s + (-x); negating the addend lets the owner/neighbour
-// accumulation be ONE FP64 addition instead of an addition and a subtraction of
-// which one is selected.  The negation is an integer XOR of the sign bit (IEEE
-// negation exactly), so it issues no FP64 instruction either.
-__device__ __forceinline__ double signed_term(bool plus, double x) {
-    return __longlong_as_double(__double_as_longlong(x) ^ (plus ? 0LL : (long long)0x8000000000000000ULL));
-}
+// The owner/neighbour accumulation s + x or s - x is ONE fused multiply-add,
+// fma(x, +-1, s) (facc): exactly the rounded sum or difference, with no branch
+// and no separate negation.  Every other exact sum and product is a DFMA too
+// (fadd, fsub, fmul): GB300 retires DFMA faster than DADD and DMUL.
 
 // ---------------------------------------------------------------- interpolation
 // Face kernels: a thread handles kFPT faces spaced a block apart (coalesced
@@ -68,7 +65,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 const double sN = __ldg(&src[N[k] * NC + c]);
-                dst[f * NC + c] = w[k] * (__ldg(&src[P[k] * NC + c]) - sN) + sN;
+                dst[f * NC + c] = fadd(m, fmul(m, w[k], fsub(m, __ldg(&src[P[k] * NC + c]), sN)), sN);
             }
         } else if (f < m.nif + m.nbf) {
             const int b = f - m.nif;
@@ -147,7 +144,7 @@ __device__ __forceinline__ void div_entry(const MeshView& m, int code, double F,
                                           const double* Tc, double* s) {
     if (code >= m.nif) {  // boundary face: value from the boundary field
 #pragma unroll
-        for (int k = 0; k < NC; ++k) s[k] = s[k] + F * To[k];
+        for (int k = 0; k < NC; ++k) s[k] = fadd(m, s[k], fmul(m, F, To[k]));
         return;
     }
     const bool isOwner = code >= 0;
@@ -157,8 +154,8 @@ __device__ __forceinline__ void div_entry(const MeshView& m, int code, double F,
         const double Tnei = isOwner ? To[k] : Tc[k];
         double tf;
         if (SCHEME == FVGB_SCHEME_UPWIND) tf = nonneg(F) ? Town : Tnei;
-        else tf = wf * (Town - Tnei) + Tnei;
-        s[k] = s[k] + signed_term(isOwner, F * tf);
+        else tf = fadd(m, fmul(m, wf, fsub(m, Town, Tnei)), Tnei);
+        s[k] = facc(m, s[k], isOwner, fmul(m, F, tf));
     }
 }
 
@@ -220,7 +217,7 @@ __global__ void __launch_bounds__(kThreads)
     div_cell<NC, SCHEME>(m, c, flux, phi, phi_b, s);
     const double sc = unit ? __ldg(&m.invV[c]) : coeff / __ldg(&m.V[c]);
 #pragma unroll
-    for (int k = 0; k < NC; ++k) out[c * NC + k] = out[c * NC + k] + s[k] * sc;
+    for (int k = 0; k < NC; ++k) out[c * NC + k] = fadd(m, out[c * NC + k], fmul(m, s[k], sc));
 }
 
 // Fused forward-Euler upwind advection step + boundary correction.
@@ -233,8 +230,8 @@ __global__ void __launch_bounds__(kThreads)
     if (c >= m.n) return;
     double s[1];
     div_cell<1, FVGB_SCHEME_UPWIND>(m, c, flux, Told, Told_b, s);
-    const double dv = 0.0 + s[0] * __ldg(&m.invV[c]);
-    const double tn = __ldg(&Told[c]) - dt * dv;
+    const double dv = fadd(m, m.k_zero, fmul(m, s[0], __ldg(&m.invV[c])));
+    const double tn = fsub(m, __ldg(&Told[c]), fmul(m, dt, dv));
     Tnew[c] = tn;
     // boundary faces of this cell (they follow its internal faces in the list)
     const int slice = c >> 5, lane = c & 31;
@@ -257,18 +254,18 @@ __global__ void __launch_bounds__(kThreads)
 __device__ __forceinline__ void grad_entry(const MeshView& m, int code, double To, double wf, const double* S,
                                            double Tc, double& g0, double& g1, double& g2) {
     if (code >= m.nif) {
-        g0 = g0 + S[0] * To;
-        g1 = g1 + S[1] * To;
-        g2 = g2 + S[2] * To;
+        g0 = fadd(m, g0, fmul(m, S[0], To));
+        g1 = fadd(m, g1, fmul(m, S[1], To));
+        g2 = fadd(m, g2, fmul(m, S[2], To));
         return;
     }
     const bool isOwner = code >= 0;
     const double Town = isOwner ? Tc : To;
     const double Tnei = isOwner ? To : Tc;
-    const double tf = wf * (Town - Tnei) + Tnei;
-    g0 = g0 + signed_term(isOwner, S[0] * tf);
-    g1 = g1 + signed_term(isOwner, S[1] * tf);
-    g2 = g2 + signed_term(isOwner, S[2] * tf);
+    const double tf = fadd(m, fmul(m, wf, fsub(m, Town, Tnei)), Tnei);
+    g0 = facc(m, g0, isOwner, fmul(m, S[0], tf));
+    g1 = facc(m, g1, isOwner, fmul(m, S[1], tf));
+    g2 = facc(m, g2, isOwner, fmul(m, S[2], tf));
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -312,9 +309,9 @@ __global__ void __launch_bounds__(kThreads)
         grad_entry(m, cd, __ldg(&(bnd ? phi_b : phi)[o]), bnd ? 0.0 : __ldg(&m.w[f]), Sv, Tc, g0, g1, g2);
     }
     const double sc = unit ? __ldg(&m.invV[c]) : coeff / __ldg(&m.V[c]);
-    out[3 * c] = out[3 * c] + g0 * sc;
-    out[3 * c + 1] = out[3 * c + 1] + g1 * sc;
-    out[3 * c + 2] = out[3 * c + 2] + g2 * sc;
+    out[3 * c] = fadd(m, out[3 * c], fmul(m, g0, sc));
+    out[3 * c + 1] = fadd(m, out[3 * c + 1], fmul(m, g1, sc));
+    out[3 * c + 2] = fadd(m, out[3 * c + 2], fmul(m, g2, sc));
 }
 
 // ------------------------------------------------------------------ laplacian
@@ -325,7 +322,7 @@ __device__ __forceinline__ void lap_entry(const MeshView& m, int code, double g,
                                           double* s) {
     if (code >= m.nif) {
 #pragma unroll
-        for (int k = 0; k < NC; ++k) s[k] = s[k] + g * (To[k] - Tc[k]);
+        for (int k = 0; k < NC; ++k) s[k] = fadd(m, s[k], fmul(m, g, fsub(m, To[k], Tc[k])));
         return;
     }
     const bool isOwner = code >= 0;
@@ -333,7 +330,7 @@ __device__ __forceinline__ void lap_entry(const MeshView& m, int code, double g,
     for (int k = 0; k < NC; ++k) {
         // owner: s + g*(To - Tc); neighbour: s - g*(Tc - To), the reference's face flux
         const double a = isOwner ? To[k] : Tc[k], b = isOwner ? Tc[k] : To[k];
-        s[k] = s[k] + signed_term(isOwner, g * (a - b));
+        s[k] = facc(m, s[k], isOwner, fmul(m, g, fsub(m, a, b)));
     }
 }
 
@@ -370,7 +367,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int j = 0; j < kG; ++j) {
         if (e.code[j] == FVGB_PAD) break;
-        lap_entry<NC>(m, e.code[j], Gm[j] * Ge[j], T[j], Tc, s);
+        lap_entry<NC>(m, e.code[j], fmul(m, Gm[j], Ge[j]), T[j], Tc, s);
     }
     for (int j = kG; j < e.width; ++j) {
         const int cd = __ldg(&m.g_code[e.base + j * 32]);
@@ -378,7 +375,7 @@ __global__ void __launch_bounds__(kThreads)
         const int o = __ldg(&m.g_other[e.base + j * 32]);
         const bool bnd = cd >= m.nif;
         const int f = entry_face(cd);
-        const double g = __ldg(&gamma[f]) * (bnd ? __ldg(&m.bgeo[cd - m.nif]) : __ldg(&m.geo[f]));
+        const double g = fmul(m, __ldg(&gamma[f]), bnd ? __ldg(&m.bgeo[cd - m.nif]) : __ldg(&m.geo[f]));
         double To[NC];
 #pragma unroll
         for (int k = 0; k < NC; ++k) To[k] = __ldg(&(bnd ? phi_b : phi)[o * NC + k]);
@@ -386,7 +383,7 @@ __global__ void __launch_bounds__(kThreads)
     }
     const double sc = unit ? __ldg(&m.invV[c]) : coeff / __ldg(&m.V[c]);
 #pragma unroll
-    for (int k = 0; k < NC; ++k) out[c * NC + k] = out[c * NC + k] + s[k] * sc;
+    for (int k = 0; k < NC; ++k) out[c * NC + k] = fadd(m, out[c * NC + k], fmul(m, s[k], sc));
 }
 
 // --------------------------------------------------------------------- snGrad
@@ -412,8 +409,8 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int k = 0; k < kFPT; ++k) {
         const int f = face_of(k);
-        if (f < m.nif) out[f] = d[k] * (__ldg(&phi[N[k]]) - __ldg(&phi[P[k]]));
-        else if (f < m.nif + m.nbf) out[f] = d[k] * (__ldg(&phi_b[f - m.nif]) - __ldg(&phi[P[k]]));
+        if (f < m.nif) out[f] = fmul(m, d[k], fsub(m, __ldg(&phi[N[k]]), __ldg(&phi[P[k]])));
+        else if (f < m.nif + m.nbf) out[f] = fmul(m, d[k], fsub(m, __ldg(&phi_b[f - m.nif]), __ldg(&phi[P[k]])));
     }
 }
 
@@ -438,12 +435,12 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 const double Tn = __ldg(&phi[N * NC + c]);
-                fx[f * NC + c] = F * (wf * (__ldg(&phi[P * NC + c]) - Tn) + Tn);
+                fx[f * NC + c] = fmul(m, F, fadd(m, fmul(m, wf, fsub(m, __ldg(&phi[P * NC + c]), Tn)), Tn));
             }
         } else if (f < m.nif + m.nbf) {
             const double F = __ldg(&flux[f]);
 #pragma unroll
-            for (int c = 0; c < NC; ++c) fx[f * NC + c] = F * __ldg(&phi_b[(f - m.nif) * NC + c]);
+            for (int c = 0; c < NC; ++c) fx[f * NC + c] = fmul(m, F, __ldg(&phi_b[(f - m.nif) * NC + c]));
         }
     }
 }
@@ -459,11 +456,11 @@ __global__ void __launch_bounds__(kThreads)
             const double F = __ldg(&flux[f]);
             const int cu = nonneg(F) ? __ldg(&m.own[f]) : __ldg(&m.nei[f]);
 #pragma unroll
-            for (int c = 0; c < NC; ++c) fx[f * NC + c] = F * __ldg(&phi[cu * NC + c]);
+            for (int c = 0; c < NC; ++c) fx[f * NC + c] = fmul(m, F, __ldg(&phi[cu * NC + c]));
         } else if (f < m.nif + m.nbf) {
             const double F = __ldg(&flux[f]);
 #pragma unroll
-            for (int c = 0; c < NC; ++c) fx[f * NC + c] = F * __ldg(&phi_b[(f - m.nif) * NC + c]);
+            for (int c = 0; c < NC; ++c) fx[f * NC + c] = fmul(m, F, __ldg(&phi_b[(f - m.nif) * NC + c]));
         }
     }
 }
@@ -475,16 +472,16 @@ __global__ void __launch_bounds__(kThreads)
         const int f = face_of(k);
         if (f < m.nif) {
             const double Tn = __ldg(&phi[__ldg(&m.nei[f])]);
-            const double tf = __ldg(&m.w[f]) * (__ldg(&phi[__ldg(&m.own[f])]) - Tn) + Tn;
-            fx[3 * f] = __ldg(&m.Sf[3 * f]) * tf;
-            fx[3 * f + 1] = __ldg(&m.Sf[3 * f + 1]) * tf;
-            fx[3 * f + 2] = __ldg(&m.Sf[3 * f + 2]) * tf;
+            const double tf = fadd(m, fmul(m, __ldg(&m.w[f]), fsub(m, __ldg(&phi[__ldg(&m.own[f])]), Tn)), Tn);
+            fx[3 * f] = fmul(m, __ldg(&m.Sf[3 * f]), tf);
+            fx[3 * f + 1] = fmul(m, __ldg(&m.Sf[3 * f + 1]), tf);
+            fx[3 * f + 2] = fmul(m, __ldg(&m.Sf[3 * f + 2]), tf);
         } else if (f < m.nif + m.nbf) {
             const int b = f - m.nif;
             const double tb = __ldg(&phi_b[b]);
-            fx[3 * f] = __ldg(&m.bSf[3 * b]) * tb;
-            fx[3 * f + 1] = __ldg(&m.bSf[3 * b + 1]) * tb;
-            fx[3 * f + 2] = __ldg(&m.bSf[3 * b + 2]) * tb;
+            fx[3 * f] = fmul(m, __ldg(&m.bSf[3 * b]), tb);
+            fx[3 * f + 1] = fmul(m, __ldg(&m.bSf[3 * b + 1]), tb);
+            fx[3 * f + 2] = fmul(m, __ldg(&m.bSf[3 * b + 2]), tb);
         }
     }
 }
@@ -498,15 +495,15 @@ __global__ void __launch_bounds__(kThreads)
         const int f = face_of(k);
         if (f < m.nif) {
             const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
-            const double g = __ldg(&gamma[f]) * __ldg(&m.geo[f]);
+            const double g = fmul(m, __ldg(&gamma[f]), __ldg(&m.geo[f]));
 #pragma unroll
-            for (int c = 0; c < NC; ++c) fx[f * NC + c] = g * (__ldg(&phi[N * NC + c]) - __ldg(&phi[P * NC + c]));
+            for (int c = 0; c < NC; ++c) fx[f * NC + c] = fmul(m, g, fsub(m, __ldg(&phi[N * NC + c]), __ldg(&phi[P * NC + c])));
         } else if (f < m.nif + m.nbf) {
             const int b = f - m.nif;
             const int P = __ldg(&m.bcells[b]);
-            const double g = __ldg(&gamma[f]) * __ldg(&m.bgeo[b]);
+            const double g = fmul(m, __ldg(&gamma[f]), __ldg(&m.bgeo[b]));
 #pragma unroll
-            for (int c = 0; c < NC; ++c) fx[f * NC + c] = g * (__ldg(&phi_b[b * NC + c]) - __ldg(&phi[P * NC + c]));
+            for (int c = 0; c < NC; ++c) fx[f * NC + c] = fmul(m, g, fsub(m, __ldg(&phi_b[b * NC + c]), __ldg(&phi[P * NC + c])));
         }
     }
 }
@@ -530,9 +527,9 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 const double Tn = __ldg(&phi[N * NC + c]);
-                const double tf = wf * (__ldg(&phi[P * NC + c]) - Tn) + Tn;
+                const double tf = fadd(m, fmul(m, wf, fsub(m, __ldg(&phi[P * NC + c]), Tn)), Tn);
 #pragma unroll
-                for (int d = 0; d < 3; ++d) fx[(f * NC + c) * 3 + d] = __ldg(&m.Sf[3 * f + d]) * tf;
+                for (int d = 0; d < 3; ++d) fx[(f * NC + c) * 3 + d] = fmul(m, __ldg(&m.Sf[3 * f + d]), tf);
             }
         } else if (f < m.nif + m.nbf) {
             const int b = f - m.nif;
@@ -540,7 +537,7 @@ __global__ void __launch_bounds__(kThreads)
             for (int c = 0; c < NC; ++c) {
                 const double tb = __ldg(&phi_b[b * NC + c]);
 #pragma unroll
-                for (int d = 0; d < 3; ++d) fx[(f * NC + c) * 3 + d] = __ldg(&m.bSf[3 * b + d]) * tb;
+                for (int d = 0; d < 3; ++d) fx[(f * NC + c) * 3 + d] = fmul(m, __ldg(&m.bSf[3 * b + d]), tb);
             }
         }
     }
@@ -568,21 +565,21 @@ __global__ void __launch_bounds__(kThreads)
             const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
             const double wf = __ldg(&m.w[f]);
             const double k0 = __ldg(&m.corr[3 * f]), k1 = __ldg(&m.corr[3 * f + 1]), k2 = __ldg(&m.corr[3 * f + 2]);
-            const double gm = MODE == kCorrSnGrad ? 1.0 : __ldg(&gamma[f]) * __ldg(&m.magSf[f]);
+            const double gm = MODE == kCorrSnGrad ? 1.0 : fmul(m, __ldg(&gamma[f]), __ldg(&m.magSf[f]));
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 double gf[3];
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     const double gn = __ldg(&grad[(N * NC + c) * 3 + d]);
-                    gf[d] = fma(wf, __ldg(&grad[(P * NC + c) * 3 + d]) - gn, gn);
+                    gf[d] = fma(wf, fsub(m, __ldg(&grad[(P * NC + c) * 3 + d]), gn), gn);
                 }
-                const double kg = fma(k2, gf[2], fma(k1, gf[1], k0 * gf[0]));
-                const double dT = __ldg(&phi[N * NC + c]) - __ldg(&phi[P * NC + c]);
+                const double kg = fma(k2, gf[2], fma(k1, gf[1], fmul(m, k0, gf[0])));
+                const double dT = fsub(m, __ldg(&phi[N * NC + c]), __ldg(&phi[P * NC + c]));
                 if (MODE == kCorrLaplacian)
-                    fx[f * NC + c] = fma(__ldg(&gamma[f]) * __ldg(&m.geo[f]), dT, gm * kg);
+                    fx[f * NC + c] = fma(fmul(m, __ldg(&gamma[f]), __ldg(&m.geo[f])), dT, fmul(m, gm, kg));
                 else if (MODE == kCorrOnly)
-                    fx[f * NC + c] = gm * kg;
+                    fx[f * NC + c] = fmul(m, gm, kg);
                 else
                     fx[f * NC + c] = fma(__ldg(&m.delta[f]), dT, kg);
             }
@@ -591,10 +588,10 @@ __global__ void __launch_bounds__(kThreads)
             const int P = __ldg(&m.bcells[b]);
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
-                const double dT = __ldg(&phi_b[b * NC + c]) - __ldg(&phi[P * NC + c]);
-                if (MODE == kCorrLaplacian) fx[f * NC + c] = __ldg(&gamma[f]) * __ldg(&m.bgeo[b]) * dT;
+                const double dT = fsub(m, __ldg(&phi_b[b * NC + c]), __ldg(&phi[P * NC + c]));
+                if (MODE == kCorrLaplacian) fx[f * NC + c] = fmul(m, fmul(m, __ldg(&gamma[f]), __ldg(&m.bgeo[b])), dT);
                 else if (MODE == kCorrOnly) fx[f * NC + c] = 0.0;
-                else fx[f * NC + c] = __ldg(&m.bdelta[b]) * dT;
+                else fx[f * NC + c] = fmul(m, __ldg(&m.bdelta[b]), dT);
             }
         }
     }
@@ -634,18 +631,18 @@ __global__ void __launch_bounds__(kThreads)
         if (e.code[j] == FVGB_PAD) break;
         const bool plus = e.code[j] >= 0;  // owner and boundary faces add, neighbour faces subtract
 #pragma unroll
-        for (int k = 0; k < NC; ++k) s[k] = s[k] + signed_term(plus, v[j][k]);
+        for (int k = 0; k < NC; ++k) s[k] = facc(m, s[k], plus, v[j][k]);
     }
     for (int j = kG; j < e.width; ++j) {
         const int cd = __ldg(&m.g_code[e.base + j * 32]);
         if (cd == FVGB_PAD) break;
         const int f = entry_face(cd);
 #pragma unroll
-        for (int k = 0; k < NC; ++k) s[k] = s[k] + signed_term(cd >= 0, __ldg(&fx[f * NC + k]));
+        for (int k = 0; k < NC; ++k) s[k] = facc(m, s[k], cd >= 0, __ldg(&fx[f * NC + k]));
     }
     const double sc = unit == 1 ? __ldg(&m.invV[c]) : unit == 2 ? coeff : coeff / __ldg(&m.V[c]);
 #pragma unroll
-    for (int k = 0; k < NC; ++k) out[c * NC + k] = out[c * NC + k] + s[k] * sc;
+    for (int k = 0; k < NC; ++k) out[c * NC + k] = fadd(m, out[c * NC + k], fmul(m, s[k], sc));
 }
 
 // The fused upwind advection step on a face-flux buffer: the divergence as in
@@ -666,15 +663,15 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int j = 0; j < kG; ++j) {
         if (e.code[j] == FVGB_PAD) break;
-        s = s + signed_term(e.code[j] >= 0, v[j]);
+        s = facc(m, s, e.code[j] >= 0, v[j]);
     }
     for (int j = kG; j < e.width; ++j) {
         const int cd = __ldg(&m.g_code[e.base + j * 32]);
         if (cd == FVGB_PAD) break;
-        s = s + signed_term(cd >= 0, __ldg(&fx[entry_face(cd)]));
+        s = facc(m, s, cd >= 0, __ldg(&fx[entry_face(cd)]));
     }
-    const double dv = 0.0 + s * __ldg(&m.invV[c]);
-    const double tn = __ldg(&Told[c]) - dt * dv;
+    const double dv = fadd(m, m.k_zero, fmul(m, s, __ldg(&m.invV[c])));
+    const double tn = fsub(m, __ldg(&Told[c]), fmul(m, dt, dv));
     Tnew[c] = tn;
     for (int j = e.width - 1; j >= 0; --j) {
         const int code = j < kG ? e.code[j] : __ldg(&m.g_code[e.base + j * 32]);

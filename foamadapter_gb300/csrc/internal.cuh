@@ -61,7 +61,26 @@ struct MeshView {
     const int32_t* diag_pos;
     const int32_t* own_pos;
     const int32_t* nei_pos;
+    // 1.0, -1.0, -0.0 and +0.0 as run-time values: the exact FP64 additions and
+    // products of the bit-exact kernels are issued as fused multiply-adds with
+    // one of them (fadd/fsub/fmul below), which the compiler cannot fold back
+    double k_one = 1.0, k_mone = -1.0, k_nzero = -0.0, k_zero = 0.0;
 };
+
+// Exact FP64 arithmetic issued as DFMA.  GB300 retires DFMA at ~1.9 lanes per
+// clock per SM but DADD and DMUL at ~1.6 (measured: 596 vs 502 G operations/s
+// on independent chains), and the bit-exact face loops are bound by that rate.
+// fma(a, 1, b) rounds the exact sum a + b once, fma(b, -1, a) the exact
+// difference a - b once, fma(a, b, -0) the exact product a * b once: the bits of
+// a + b, a - b and a * b, signed zeros included (x + -0 = x, -0 + -0 = -0),
+// and infinities and overflow alike.
+__device__ __forceinline__ double fadd(const MeshView& m, double a, double b) { return __fma_rn(a, m.k_one, b); }
+__device__ __forceinline__ double fsub(const MeshView& m, double a, double b) { return __fma_rn(b, m.k_mone, a); }
+__device__ __forceinline__ double fmul(const MeshView& m, double a, double b) { return __fma_rn(a, b, m.k_nzero); }
+// s + x (plus) or s - x: the owner/neighbour accumulation of a face term
+__device__ __forceinline__ double facc(const MeshView& m, double s, bool plus, double x) {
+    return __fma_rn(x, plus ? m.k_one : m.k_mone, s);
+}
 
 struct fvgb_mesh {
     MeshView v{};
