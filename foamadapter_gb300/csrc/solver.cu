@@ -3025,22 +3025,19 @@ extern "C" fvgb_status fvgb_step_destroy(fvgb_step* step) {
     return FVGB_OK;
 }
 
+namespace {
+
 // Launch-bound variants of the CG kernels: the autotuner's measurements and
-// choices for this system, optionally forcing a variant per kernel kind.
-extern "C" fvgb_status fvgb_solve_tuning(fvgb_ls* ls, const int32_t* force, int32_t* chosen, float* ms) {
-    fvgb_clear_error();
-    FVGB_CHECK_ARG(ls && chosen && ms, "fvgb_solve_tuning: null argument");
-    FVGB_CHECK_ARG(ls->ncomp == 1, "fvgb_solve_tuning: scalar systems only");
+// choices for a solver cache, optionally forcing a variant per kernel kind.
+fvgb_status tuning(SolverCache* c, const int32_t* force, int32_t* chosen, float* ms, const char* who) {
     if (force)
         for (int k = 0; k < kTuneKinds; ++k)
-            FVGB_CHECK_ARG(force[k] >= -1 && force[k] < kNumVariants, "fvgb_solve_tuning: bad variant");
-    SolverCache* c = nullptr;
-    fvgb_status st = single_cache(ls, &c);
-    if (st != FVGB_OK) return st;
+            if (!(force[k] >= -1 && force[k] < kNumVariants))
+                return fvgb_fail(FVGB_ERR_INVALID_ARG, (std::string(who) + ": bad variant").c_str());
     FVGB_CUDA_TRY(cudaDeviceSynchronize());  // no solve of this system in flight while its graphs are rebuilt
     if (force)
         for (int k = 0; k < kTuneKinds; ++k) c->forced[k] = force[k];
-    st = build_fp64(c);  // allocates and tunes once, then (re)builds the graph
+    fvgb_status st = build_fp64(c);  // allocates and tunes once, then (re)builds the graph
     if (st == FVGB_OK) st = build_mixed(c);
     if (st != FVGB_OK) return st;
     if (force) {
@@ -3054,6 +3051,24 @@ extern "C" fvgb_status fvgb_solve_tuning(fvgb_ls* ls, const int32_t* force, int3
         for (int v = 0; v < kNumVariants; ++v) ms[k * kNumVariants + v] = c->tune_ms[k][v];
     }
     return FVGB_OK;
+}
+
+}  // namespace
+
+extern "C" fvgb_status fvgb_solve_tuning(fvgb_ls* ls, const int32_t* force, int32_t* chosen, float* ms) {
+    fvgb_clear_error();
+    FVGB_CHECK_ARG(ls && chosen && ms, "fvgb_solve_tuning: null argument");
+    FVGB_CHECK_ARG(ls->ncomp == 1, "fvgb_solve_tuning: scalar systems only");
+    SolverCache* c = nullptr;
+    fvgb_status st = single_cache(ls, &c);
+    if (st != FVGB_OK) return st;
+    return tuning(c, force, chosen, ms, "fvgb_solve_tuning");
+}
+
+extern "C" fvgb_status fvgb_batch_tuning(fvgb_batch* b, const int32_t* force, int32_t* chosen, float* ms) {
+    fvgb_clear_error();
+    FVGB_CHECK_ARG(b && b->c && chosen && ms, "fvgb_batch_tuning: null argument");
+    return tuning(b->c, force, chosen, ms, "fvgb_batch_tuning");
 }
 
 // Per-kernel timing of the FP64 CG iteration (outside any graph): runs init and

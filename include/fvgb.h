@@ -375,6 +375,9 @@ fvgb_status fvgb_step_destroy(fvgb_step* step);
  * milliseconds per kind and variant (0 where not measured).  force[4] (or NULL):
  * a variant index 0..3 per kind, -1 to keep the tuned choice. */
 fvgb_status fvgb_solve_tuning(fvgb_ls* ls, const int32_t* force, int32_t* chosen, float* ms);
+/* The same for the solver of a batch (its variants are timed when the packed
+ * system has at least 2^18 rows). */
+fvgb_status fvgb_batch_tuning(fvgb_batch* batch, const int32_t* force, int32_t* chosen, float* ms);
 /* Measurement aid (no reference counterpart): runs the FP64 CG init and
  * `iters` iterations outside the graph on a private copy of x0, with CUDA
  * events around each kernel; ms_out[4] = mean milliseconds of

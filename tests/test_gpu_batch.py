@@ -92,3 +92,36 @@ def test_batch_cases_stop_independently(cuda):
     stats = batch.solve(x, rel_tol=1e-10, max_iter=12)
     assert all(s.num_iter <= 12 for s in stats)
     assert any(s.status == abi.ERR_NOT_CONVERGED for s in stats)
+
+
+def test_batch_kernel_variants_give_the_same_bits(cuda):
+    """fvgb_batch_tuning forces the launch-bound variants of a batch's solver:
+    every variant gives every case the same bits."""
+    import ctypes as C
+
+    cases = make_cases()[:3]
+    big, ranges, slices = mesh.concat([c[0] for c in cases])
+    dm = DeviceMesh(big)
+    T = neon.VolumeField(dm, np.full(big.n, 300.0), [("fixedValue", 350.0)] + [("zeroGradient", 0.0)] * 5)
+    ls = neon.LinearSystem(dm)
+    ls.assemble([neon.ddt(T.internal.clone()),
+                 neon.laplacian(neon.SurfaceField(dm, np.ones(big.nif + big.nbf)), -1.0)], 0.01, T)
+    L = abi.lib()
+    chosen, ms = (C.c_int32 * 4)(), (C.c_float * 16)()
+    out = []
+    for var in range(4):
+        b = neon.Batch(ls, ranges)
+        abi.check(L.fvgb_batch_tuning(b.handle, (C.c_int32 * 4)(var, var, var, var), chosen, ms))
+        assert list(chosen) == [(2, 4, 6, 8)[var]] * 4
+        for prec in (abi.PREC_FP64, abi.PREC_MIXED_IR):
+            x = T.internal.clone()
+            stats = b.solve(x, rel_tol=1e-9, precision=prec, inner_rel_tol=1e-3)
+            assert all(s.status == abi.OK for s in stats)
+            out.append((prec, x.cpu().numpy(), [s.num_iter for s in stats]))
+    for prec in (abi.PREC_FP64, abi.PREC_MIXED_IR):
+        runs = [o for o in out if o[0] == prec]
+        for run in runs[1:]:
+            np.testing.assert_array_equal(runs[0][1], run[1])
+            assert runs[0][2] == run[2]
+    with pytest.raises(abi.FvgbError):
+        abi.check(L.fvgb_batch_tuning(neon.Batch(ls, ranges).handle, (C.c_int32 * 4)(7, -1, -1, -1), chosen, ms))
