@@ -54,11 +54,12 @@ class SolverCfg(C.Structure):
                 ("flags", i32), ("method", i32), ("preconditioner", i32)]
 
 
-SOLVER_CG, SOLVER_BICGSTAB = 0, 1
+SOLVER_CG, SOLVER_BICGSTAB, SOLVER_BICG = 0, 1, 2
 PRECOND_JACOBI, PRECOND_MULTIGRID = 0, 1
 
 
 SOLVE_NO_TUNE = 1
+SOLVE_RHS_BASELINE = 2  # rel_tol relative to ||b|| (Ginkgo ResidualNorm, baseline rhs_norm)
 
 
 class SolverStats(C.Structure):

@@ -1185,6 +1185,8 @@ fvgb_status fvgb_amg_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* 
     if (ls->ncomp != 1) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_solve: scalar systems only");
     if (cfg->method != FVGB_SOLVER_CG)
         return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: CG only");
+    if (cfg->flags & FVGB_SOLVE_RHS_BASELINE)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: the ||b|| tolerance baseline is not implemented");
     // mixed precision: the CG, its residuals and its stopping test stay FP64;
     // the V-cycle (the preconditioner) runs in FP32
     const bool f32 = cfg->precision == FVGB_PREC_MIXED_IR;

@@ -763,7 +763,10 @@ extern "C" fvgb_status fvgb_solver_cfg_from_dict(const fvgb_dict* d, fvgb_solver
     if (!word_of(d, "type", w)) return fvgb_fail(FVGB_ERR_INVALID_ARG, "solver entry: no Ginkgo solver type");
     if (w == "solver::Cg") c.method = FVGB_SOLVER_CG;
     else if (w == "solver::Bicgstab") c.method = FVGB_SOLVER_BICGSTAB;
-    else return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("solver entry: " + w + " is not implemented (Cg, Bicgstab are)").c_str());
+    else if (w == "solver::Bicg") c.method = FVGB_SOLVER_BICG;
+    else
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED,
+                         ("solver entry: " + w + " is not implemented (Cg, Bicgstab, Bicg are)").c_str());
     const fvgb_dict::Entry* pe = entry_of(d, "preconditioner");
     const char* kPrecMsg =
         "solver entry: preconditioner::Jacobi with max_block_size 1 and solver::Multigrid (with CG) are implemented";
@@ -945,7 +948,10 @@ fvgb_status cfg_from_json(const Json& j, fvgb_solver_cfg* out) {
     if (!t || t->kind != Json::STR) return fvgb_fail(FVGB_ERR_INVALID_ARG, "Ginkgo config: no solver type");
     if (t->str == "solver::Cg") c.method = FVGB_SOLVER_CG;
     else if (t->str == "solver::Bicgstab") c.method = FVGB_SOLVER_BICGSTAB;
-    else return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("Ginkgo config: " + t->str + " is not implemented (Cg, Bicgstab are)").c_str());
+    else if (t->str == "solver::Bicg") c.method = FVGB_SOLVER_BICG;
+    else
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED,
+                         ("Ginkgo config: " + t->str + " is not implemented (Cg, Bicgstab, Bicg are)").c_str());
     const Json* p = j.get("preconditioner");
     const Json* pt = p ? p->get("type") : nullptr;
     if (!pt || pt->kind != Json::STR)
@@ -981,12 +987,17 @@ fvgb_status cfg_from_json(const Json& j, fvgb_solver_cfg* out) {
                 if (!f || f->kind != Json::NUM)
                     return fvgb_fail(FVGB_ERR_INVALID_ARG, "Ginkgo config: ResidualNorm without reduction_factor");
                 const std::string base = (b && b->kind == Json::STR) ? b->str : "rhs_norm";
-                if (base == "absolute") c.abs_tol = f->num;
-                else if (base == "initial_resnorm") c.rel_tol = f->num;
-                else
-                    return fvgb_fail(FVGB_ERR_UNSUPPORTED,
-                                     "Ginkgo config: ResidualNorm baseline rhs_norm (the default) is not implemented; "
-                                     "use absolute or initial_resnorm");
+                if (base == "absolute") {
+                    c.abs_tol = f->num;
+                } else if (base == "initial_resnorm") {
+                    c.rel_tol = f->num;
+                } else if (base == "rhs_norm") {  // Ginkgo's default: ||r|| <= f ||b||
+                    c.rel_tol = f->num;
+                    c.flags |= FVGB_SOLVE_RHS_BASELINE;
+                } else {
+                    return fvgb_fail(FVGB_ERR_INVALID_ARG, ("Ginkgo config: ResidualNorm baseline " + base +
+                                                            " is not one of rhs_norm, initial_resnorm, absolute").c_str());
+                }
             } else {
                 return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("Ginkgo config: criterion " + ct->str + " is not implemented").c_str());
             }

@@ -312,6 +312,8 @@ extern "C" fvgb_status fvgb_pcg_csr_noalloc(int32_t n, const int32_t* row_offs, 
         return fvgb_fail(FVGB_ERR_INVALID_ARG,
                          "fvgb_pcg_csr_noalloc: n exceeds the fixed work area of 262144 rows");
     FVGB_CHECK_ARG(cfg->precision == FVGB_PREC_FP64, "fvgb_pcg_csr_noalloc: FP64 precision only");
+    if (cfg->flags & FVGB_SOLVE_RHS_BASELINE)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_pcg_csr_noalloc: the ||b|| tolerance baseline is not implemented");
     FVGB_CHECK_ARG(cfg->rel_tol >= 0 && cfg->abs_tol >= 0 && cfg->max_iter >= 0,
                    "fvgb_pcg_csr_noalloc: bad tolerances or iteration cap");
     cudaStream_t s = (cudaStream_t)stream;

@@ -76,6 +76,7 @@ struct CaseState {
     unsigned int counter;  // arrivals of this case's blocks
     unsigned int signflags;
     int32_t half;          // BiCGStab: converged at the half step, x update pending
+    double bbase;          // ||b|| when the relative tolerance refers to it (-1: to the initial residual)
 };
 
 struct BatchState {
@@ -242,6 +243,14 @@ __device__ __forceinline__ float spmv_row_diff(const MeshView& m, const float* _
     return fmaf(ei, xi, s);
 }
 
+// The baseline of the relative tolerance: ||b|| (Ginkgo's ResidualNorm with its
+// default baseline, rhs_norm) when k_case_bnorm has set it, else the initial
+// residual norm.
+__device__ __forceinline__ double tol_base(const CaseState* cs, double res0) {
+    const double b = *(const volatile double*)&cs->bbase;
+    return b >= 0.0 ? b : res0;
+}
+
 __device__ __forceinline__ void case_done(BatchState* bs, CaseState* cs) {
     cs->active = 0;
     atomicSub(&bs->n_active, 1);
@@ -280,7 +289,7 @@ __global__ void __launch_bounds__(kT)
         if (threadIdx.x == 0) {
             const SolverParams& prm = L.bs->prm;
             const double res0 = sqrt(rr);
-            double tol = prm.rel_tol * res0;
+            double tol = prm.rel_tol * tol_base(cs, res0);
             if (prm.abs_tol > tol) tol = prm.abs_tol;
             cs->rz = rz;
             cs->res0 = res0;
@@ -447,6 +456,29 @@ __global__ void k_set_params(Layout L, int ncases, SolverParams prm) {
         cs->res = 0.0;
         cs->signflags = 0u;
         cs->counter = 0u;
+        cs->bbase = -1.0;
+    }
+}
+
+// ||b|| of every case, with the reduction tree of the solver's dot products
+// (FVGB_SOLVE_RHS_BASELINE); runs after k_set_params, before the solve.
+__global__ void __launch_bounds__(kT) k_case_bnorm(Layout L, const double* __restrict__ b, double* __restrict__ pa) {
+    __shared__ double sma[kT];
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const double bi = __ldg(&b[i]);
+        acc = fma(bi, bi, acc);
+    }
+    const double ba = block_tree(acc, sma);
+    if (threadIdx.x == 0) pa[blockIdx.x] = ba;
+    if (arrive_last(&cs->counter, k.nbc)) {
+        const double bb = final_tree(pa + k.blk0, k.nbc, sma);
+        if (threadIdx.x == 0) cs->bbase = sqrt(bb);
     }
 }
 
@@ -489,7 +521,7 @@ __global__ void __launch_bounds__(kT)
         if (threadIdx.x == 0) {
             const SolverParams& prm = L.bs->prm;
             const double res0 = sqrt(rr2);
-            double tol = prm.rel_tol * res0;
+            double tol = prm.rel_tol * tol_base(cs, res0);
             if (prm.abs_tol > tol) tol = prm.abs_tol;
             cs->res0 = cs->res = res0;
             cs->tol = tol;
@@ -702,6 +734,210 @@ __global__ void __launch_bounds__(kT)
         cudaGraphSetConditional(h, ld_volatile(&L.bs->n_active) > 0 ? 1u : 0u);
 }
 
+// ------------------------------------------------------------------ BiCG (FP64)
+// Jacobi-preconditioned BiCG, the method of Ginkgo's solver::Bicg that
+// FoamAdapter maps OpenFOAM's PBiCG to (fvSolution.cpp:24), for nonsymmetric
+// systems.  The shadow system is the transpose: r~ starts as r, and its
+// direction is multiplied by A^T.  Jacobi is its own transpose.
+//   init:    r = b - A x, r~ = r, z = D^-1 r, z~ = D^-1 r~, p = p~ = 0,
+//            rho = (r~, z), beta = rho / 1
+//   dir:     p = z + beta p, p~ = z~ + beta p~
+//   spmv:    q = A p, q~ = A^T p~, alpha = rho / (p~, q)
+//   update:  x += alpha p, r -= alpha q, r~ -= alpha q~, z = D^-1 r,
+//            z~ = D^-1 r~, rho' = (r~, z), |r|, beta = rho' / rho
+// A^T p~ is a gather over the matrix slots: the value of (A^T)_ij is the slot
+// of a_ji, which the face code of slot (i, j) names (own_pos / nei_pos).  The
+// fma chain of a row runs in slot (= column) order as in A p.
+
+// (A^T x)_i in slot order
+__device__ __forceinline__ double spmv_row_t(const MeshView& m, const double* __restrict__ val,
+                                             const double* __restrict__ x, int i) {
+    const int slice = i >> 5, lane = i & 31;
+    const int b0 = __ldg(&m.m_ptr[slice]);
+    const int base = b0 + lane;
+    const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+    double s = 0.0;
+    for (int k = 0; k < w; ++k) {
+        const int pos = base + k * 32;
+        const int code = __ldg(&m.m_code[pos]);
+        if (code == FVGB_PAD) continue;
+        const int tpos = code >= 0 ? __ldg(&m.nei_pos[code]) : (code == -1 ? pos : __ldg(&m.own_pos[-code - 2]));
+        s = fma(__ldg(&val[tpos]), __ldg(&x[slot_col(m, pos, i)]), s);
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bg_init(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ b,
+              double* __restrict__ dinv, double* __restrict__ r, double* __restrict__ r2, double* __restrict__ z,
+              double* __restrict__ z2, double* __restrict__ p, double* __restrict__ p2, double* __restrict__ pa,
+              double* __restrict__ pb, cudaGraphConditionalHandle h) {
+    __shared__ double sma[kT], smb[kT];
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    const double* __restrict__ x = L.bs->prm.x;
+    double arho = 0.0, arr = 0.0;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const double di = 1.0 / __ldg(&val[__ldg(&m.diag_pos[i])]);
+        dinv[i] = di;
+        const double ri = __ldg(&b[i]) - spmv_row(m, val, x, i);
+        const double zi = di * ri;
+        r[i] = ri;
+        r2[i] = ri;
+        z[i] = zi;
+        z2[i] = zi;
+        p[i] = 0.0;
+        p2[i] = 0.0;
+        arho = fma(ri, zi, arho);
+        arr = fma(ri, ri, arr);
+    }
+    const double ba = block_tree(arho, sma), bb = block_tree(arr, smb);
+    if (threadIdx.x == 0) {
+        pa[blockIdx.x] = ba;
+        pb[blockIdx.x] = bb;
+    }
+    if (arrive_last(&cs->counter, k.nbc)) {
+        const double rho = final_tree(pa + k.blk0, k.nbc, sma), rr = final_tree(pb + k.blk0, k.nbc, smb);
+        if (threadIdx.x == 0) {
+            const SolverParams& prm = L.bs->prm;
+            const double res0 = sqrt(rr);
+            double tol = prm.rel_tol * tol_base(cs, res0);
+            if (prm.abs_tol > tol) tol = prm.abs_tol;
+            cs->res0 = cs->res = res0;
+            cs->tol = tol;
+            cs->rho = rho;
+            cs->beta = rho / 1.0;
+            bool done = !(res0 > tol) || res0 == 0.0;
+            if (!isfinite(res0)) {
+                done = true;
+                cs->status = FVGB_ERR_BREAKDOWN;
+            } else if (!done && prm.max_iter <= 0) {
+                done = true;
+                cs->status = FVGB_ERR_NOT_CONVERGED;
+            } else if (!done && !(rho != 0.0 && isfinite(rho))) {
+                done = true;
+                cs->status = FVGB_ERR_BREAKDOWN;
+            }
+            if (done) case_done(L.bs, cs);
+        }
+    }
+    if (arrive_last(&L.bs->gcounter, gridDim.x) && threadIdx.x == 0)
+        cudaGraphSetConditional(h, ld_volatile(&L.bs->n_active) > 0 ? 1u : 0u);
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bg_dir(Layout L, const double* __restrict__ z, const double* __restrict__ z2, double* __restrict__ p,
+             double* __restrict__ p2) {
+    const Blk k = blk_info(L);
+    const CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->active)) return;
+    const double beta = cs->beta;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        p[i] = fma(beta, p[i], __ldg(&z[i]));
+        p2[i] = fma(beta, p2[i], __ldg(&z2[i]));
+    }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bg_spmv(Layout L, MeshView m, const double* __restrict__ val, const double* __restrict__ p,
+              const double* __restrict__ p2, double* __restrict__ q, double* __restrict__ q2,
+              double* __restrict__ pa) {
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (!ld_volatile(&cs->active)) return;
+    __shared__ double sma[kT];
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int i = blk_row(k, j);
+        if (i >= k.end) continue;
+        const double qi = spmv_row(m, val, p, i);
+        q[i] = qi;
+        q2[i] = spmv_row_t(m, val, p2, i);
+        acc = fma(__ldg(&p2[i]), qi, acc);
+    }
+    const double ba = block_tree(acc, sma);
+    if (threadIdx.x == 0) pa[blockIdx.x] = ba;
+    if (!arrive_last(&cs->counter, k.nbc)) return;
+    const double pq = final_tree(pa + k.blk0, k.nbc, sma);
+    if (threadIdx.x == 0) {
+        const double alpha = cs->rho / pq;
+        cs->alpha = alpha;
+        if (pq == 0.0 || !isfinite(alpha)) {
+            cs->status = FVGB_ERR_BREAKDOWN;
+            case_done(L.bs, cs);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bg_update(Layout L, const double* __restrict__ dinv, const double* __restrict__ p,
+                const double* __restrict__ q, const double* __restrict__ q2, double* __restrict__ r,
+                double* __restrict__ r2, double* __restrict__ z, double* __restrict__ z2, double* __restrict__ pa,
+                double* __restrict__ pb, cudaGraphConditionalHandle h) {
+    __shared__ double sma[kT], smb[kT];
+    const Blk k = blk_info(L);
+    CaseState* cs = &L.cases[k.c];
+    if (ld_volatile(&cs->active)) {
+        double* __restrict__ x = L.bs->prm.x;
+        const double alpha = cs->alpha;
+        double arho = 0.0, arr = 0.0;
+#pragma unroll
+        for (int j = 0; j < kRowsPerThread; ++j) {
+            const int i = blk_row(k, j);
+            if (i >= k.end) continue;
+            x[i] = fma(alpha, __ldg(&p[i]), x[i]);
+            const double ri = fma(-alpha, __ldg(&q[i]), r[i]);
+            const double r2i = fma(-alpha, __ldg(&q2[i]), r2[i]);
+            const double di = __ldg(&dinv[i]);
+            const double zi = di * ri;
+            r[i] = ri;
+            r2[i] = r2i;
+            z[i] = zi;
+            z2[i] = di * r2i;
+            arho = fma(r2i, zi, arho);
+            arr = fma(ri, ri, arr);
+        }
+        const double ba = block_tree(arho, sma), bb = block_tree(arr, smb);
+        if (threadIdx.x == 0) {
+            pa[blockIdx.x] = ba;
+            pb[blockIdx.x] = bb;
+        }
+        if (arrive_last(&cs->counter, k.nbc)) {
+            const double rho = final_tree(pa + k.blk0, k.nbc, sma), rr = final_tree(pb + k.blk0, k.nbc, smb);
+            if (threadIdx.x == 0) {
+                const double res = sqrt(rr);
+                cs->res = res;
+                cs->iter += 1;
+                cs->beta = rho / cs->rho;
+                cs->rho = rho;
+                bool done = false;
+                if (!isfinite(res)) {
+                    cs->status = FVGB_ERR_BREAKDOWN;
+                    done = true;
+                } else if (!(res > cs->tol)) {
+                    done = true;
+                } else if (cs->iter >= L.bs->prm.max_iter) {
+                    cs->status = FVGB_ERR_NOT_CONVERGED;
+                    done = true;
+                } else if (!(rho != 0.0 && isfinite(rho))) {
+                    cs->status = FVGB_ERR_BREAKDOWN;
+                    done = true;
+                }
+                if (done) case_done(L.bs, cs);
+            }
+        }
+    }
+    if (arrive_last(&L.bs->gcounter, gridDim.x) && threadIdx.x == 0)
+        cudaGraphSetConditional(h, ld_volatile(&L.bs->n_active) > 0 ? 1u : 0u);
+}
+
 // --------------------------------------------------- mixed precision (FP32 inner)
 // The inner CG runs in FP32 on the row-sign-normalised system  D_s A y = D_s r
 // (D_s = the sign of each row's diagonal: the solution is unchanged, and for a
@@ -846,7 +1082,7 @@ __global__ void __launch_bounds__(kT)
                 bool done = false;
                 if (FIRST) {
                     cs->res0 = res;
-                    double tol = prm.rel_tol * res;
+                    double tol = prm.rel_tol * tol_base(cs, res);
                     if (prm.abs_tol > tol) tol = prm.abs_tol;
                     cs->tol = tol;
                     const unsigned int sf = cs->signflags;
@@ -1123,7 +1359,7 @@ __global__ void __launch_bounds__(kT)
                 bool done = false;
                 if (FIRST) {
                     cs->res0 = res;
-                    double tol = prm.rel_tol * res;
+                    double tol = prm.rel_tol * tol_base(cs, res);
                     if (prm.abs_tol > tol) tol = prm.abs_tol;
                     cs->tol = tol;
                     const unsigned int sf = cs->signflags;
@@ -1614,7 +1850,7 @@ __global__ void __launch_bounds__(kPT, 1)
         const double rr = final_all(pb, nvb, sm, &cell);
         if (T == 0) {
             res0 = res = sqrt(rr);
-            tol = prm.rel_tol * res0;
+            tol = prm.rel_tol * tol_base(&L.cases[0], res0);
             if (prm.abs_tol > tol) tol = prm.abs_tol;
             bool done = !(res0 > tol) || res0 == 0.0;
             if (!isfinite(res0)) {
@@ -1974,7 +2210,7 @@ __global__ void __launch_bounds__(kPT, 1)
             if (!first) outer += 1;
             if (first) {
                 res0 = res;
-                tol = prm.rel_tol * res;
+                tol = prm.rel_tol * tol_base(&L.cases[0], res);
                 if (prm.abs_tol > tol) tol = prm.abs_tol;
                 if ((flags & 4u) || flags == 3u) {
                     status = FVGB_ERR_UNSUPPORTED;
@@ -2178,6 +2414,8 @@ struct SolverCache {
     cudaGraphExec_t g64 = nullptr, gmix = nullptr, gbi = nullptr, gmb = nullptr;
     float *mb_rr = nullptr, *mb_yv = nullptr, *mb_t = nullptr;  // mixed BiCGStab (with rh, y, pf, qf, pf2, zf)
     double *bi_rr = nullptr, *bi_v = nullptr, *bi_y = nullptr, *bi_s = nullptr, *bi_t = nullptr;  // BiCGStab
+    double *bg_r2 = nullptr, *bg_z2 = nullptr, *bg_p2 = nullptr, *bg_q2 = nullptr;                 // BiCG
+    cudaGraphExec_t gbg = nullptr;
     fvgb_solver_stats* h_stats = nullptr;  // pinned [ncases]
     GridBar* bar = nullptr;
     float *pf2 = nullptr, *zf = nullptr;   // second direction buffer and z of the persistent mixed solve
@@ -2204,6 +2442,7 @@ void fvgb_solver_cache_free(SolverCache* c) {
     if (c->gmix) cudaGraphExecDestroy(c->gmix);
     if (c->gbi) cudaGraphExecDestroy(c->gbi);
     if (c->gmb) cudaGraphExecDestroy(c->gmb);
+    if (c->gbg) cudaGraphExecDestroy(c->gbg);
     for (void* p : c->allocs) cudaFree(p);
     if (c->h_stats) cudaFreeHost(c->h_stats);
     if (c->h_active) cudaFreeHost(c->h_active);
@@ -2609,6 +2848,62 @@ fvgb_status build_bicgstab(SolverCache* c) {
     return FVGB_OK;
 }
 
+// The BiCG solve as graph nodes in `g` after `deps` (see add_fp64_nodes).
+cudaError_t add_bicg_nodes(SolverCache* c, cudaGraph_t g, const cudaGraphNode_t* deps, size_t ndeps,
+                           cudaGraphNode_t* last) {
+    const fvgb_ls* ls = c->ls;
+    MeshView m = ls->mesh->v;
+    Layout L = c->L;
+    cudaGraphConditionalHandle h;
+    cudaGraphNode_t n0, n1, b0, b1, b2;
+    cudaGraph_t body;
+    const double* val = ls->values;
+    const double* b = ls->rhs;
+    const unsigned nb = (unsigned)c->nb;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    void* a_init[] = {&L, &m, &val, &b, &c->dinv, &c->r, &c->bg_r2, &c->z, &c->bg_z2, &c->p, &c->bg_p2,
+                      &c->pa, &c->pb, &h};
+    void* a_dir[] = {&L, &c->z, &c->bg_z2, &c->p, &c->bg_p2};
+    void* a_spmv[] = {&L, &m, &val, &c->p, &c->bg_p2, &c->q, &c->bg_q2, &c->pa};
+    void* a_upd[] = {&L, &c->dinv, &c->p, &c->q, &c->bg_q2, &c->r, &c->bg_r2, &c->z, &c->bg_z2, &c->pa, &c->pb, &h};
+    void* a_fin[] = {&L};
+    if (e == cudaSuccess) e = add_kernel_deps(g, &n0, deps, ndeps, (void*)k_bg_init, nb, kT, a_init);
+    if (e == cudaSuccess) e = add_while(g, &n1, &n0, h, &body);
+    if (e == cudaSuccess) e = add_kernel(body, &b0, nullptr, (void*)k_bg_dir, nb, kT, a_dir);
+    if (e == cudaSuccess) e = add_kernel(body, &b1, &b0, (void*)k_bg_spmv, nb, kT, a_spmv);
+    if (e == cudaSuccess) e = add_kernel(body, &b2, &b1, (void*)k_bg_update, nb, kT, a_upd);
+    if (e == cudaSuccess) e = add_kernel(g, last, &n1, (void*)k_finish, grid_for(c->ncases, 128), 128, a_fin);
+    return e;
+}
+
+fvgb_status build_bicg(SolverCache* c) {
+    const size_t n = (size_t)c->n;
+    cudaError_t e = cudaSuccess;
+    if (!c->dinv) e = calloc_dev(c, &c->dinv, n);
+    if (e == cudaSuccess && !c->r) e = calloc_dev(c, &c->r, n);
+    if (e == cudaSuccess && !c->p) e = calloc_dev(c, &c->p, n);
+    if (e == cudaSuccess && !c->q) e = calloc_dev(c, &c->q, n);
+    if (e == cudaSuccess && !c->z) e = calloc_dev(c, &c->z, n);
+    if (e == cudaSuccess && !c->bg_r2) e = calloc_dev(c, &c->bg_r2, n);
+    if (e == cudaSuccess && !c->bg_z2) e = calloc_dev(c, &c->bg_z2, n);
+    if (e == cudaSuccess && !c->bg_p2) e = calloc_dev(c, &c->bg_p2, n);
+    if (e == cudaSuccess && !c->bg_q2) e = calloc_dev(c, &c->bg_q2, n);
+    if (e == cudaSuccess) e = settle_creation();
+    if (e != cudaSuccess) return cuda_fail(e, "BiCG workspace");
+    if (c->gbg) {
+        cudaGraphExecDestroy(c->gbg);
+        c->gbg = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t last;
+    e = add_bicg_nodes(c, g, nullptr, 0, &last);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->gbg, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "BiCG graph");
+    return FVGB_OK;
+}
+
 // The mixed-precision BiCGStab as graph nodes in `g` after `deps`: the
 // preparation of the FP32 system, the first refinement step, then
 // while (refining) { while (inner) { dir, spmv1, s, spmv2, update }; x += e/sig;
@@ -2681,10 +2976,14 @@ fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
     FVGB_CHECK_ARG(cfg->rel_tol >= 0 && cfg->abs_tol >= 0, "fvgb_solve: negative tolerance");
     FVGB_CHECK_ARG(cfg->max_iter >= 0 && cfg->max_iter <= 100000000, "fvgb_solve: bad max_iter");
     FVGB_CHECK_ARG(cfg->kernel_mode >= 0 && cfg->kernel_mode <= 3, "fvgb_solve: bad kernel_mode");
-    FVGB_CHECK_ARG((cfg->flags & ~FVGB_SOLVE_NO_TUNE) == 0, "fvgb_solve: unknown flags");
-    FVGB_CHECK_ARG(cfg->method == FVGB_SOLVER_CG || cfg->method == FVGB_SOLVER_BICGSTAB, "fvgb_solve: unknown method");
-    if (cfg->method == FVGB_SOLVER_BICGSTAB)
+    FVGB_CHECK_ARG((cfg->flags & ~(FVGB_SOLVE_NO_TUNE | FVGB_SOLVE_RHS_BASELINE)) == 0, "fvgb_solve: unknown flags");
+    FVGB_CHECK_ARG(cfg->method == FVGB_SOLVER_CG || cfg->method == FVGB_SOLVER_BICGSTAB ||
+                       cfg->method == FVGB_SOLVER_BICG,
+                   "fvgb_solve: unknown method");
+    if (cfg->method != FVGB_SOLVER_CG)
         FVGB_CHECK_ARG(cfg->kernel_mode != 3, "fvgb_solve: the host-driven loop is CG only");
+    if (cfg->method == FVGB_SOLVER_BICG && cfg->precision != FVGB_PREC_FP64)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_solve: BiCG is FP64 only");
     FVGB_CHECK_ARG(cfg->kernel_mode != 3 || cfg->precision == FVGB_PREC_FP64,
                    "fvgb_solve: the host-driven loop (kernel_mode 3) is FP64 only");
     if (cfg->precision == FVGB_PREC_MIXED_IR)
@@ -2771,6 +3070,10 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
         stt = build_mixed_bicgstab(c);
         if (stt != FVGB_OK) return stt;
     }
+    if (cfg->method == FVGB_SOLVER_BICG && !c->gbg) {
+        stt = build_bicg(c);
+        if (stt != FVGB_OK) return stt;
+    }
     if (cfg->method == FVGB_SOLVER_CG && cfg->precision == FVGB_PREC_FP64 && !c->g64) {
         stt = build_fp64(c, measure);
         if (stt != FVGB_OK) return stt;
@@ -2791,9 +3094,14 @@ fvgb_status launch(SolverCache* c, double* x, const fvgb_solver_cfg* cfg, fvgb_s
     prm.convert = c->converted_version != c->ls->version ? 1 : 0;
     if (cfg->precision == FVGB_PREC_MIXED_IR) c->converted_version = c->ls->version;
     k_set_params<<<grid_for(c->ncases, 128), 128, 0, s>>>(c->L, c->ncases, prm);
+    if (cfg->flags & FVGB_SOLVE_RHS_BASELINE) k_case_bnorm<<<c->nb, kT, 0, s>>>(c->L, c->ls->rhs, c->pa);
     FVGB_LAUNCH_CHECK("fvgb_solve: parameters");
     if (cfg->method == FVGB_SOLVER_BICGSTAB) {
         FVGB_CUDA_TRY(cudaGraphLaunch(mixed_ir ? c->gmb : c->gbi, s));
+        return FVGB_OK;
+    }
+    if (cfg->method == FVGB_SOLVER_BICG) {
+        FVGB_CUDA_TRY(cudaGraphLaunch(c->gbg, s));
         return FVGB_OK;
     }
     if (cfg->kernel_mode == 3) return host_loop(c, s);
@@ -2958,8 +3266,10 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
     const bool mixed = cfg->precision == FVGB_PREC_MIXED_IR;
     const bool measure = !(cfg->flags & FVGB_SOLVE_NO_TUNE);
     const bool bicg = cfg->method == FVGB_SOLVER_BICGSTAB;
-    fst = bicg ? (mixed ? build_mixed_bicgstab(c) : build_bicgstab(c))
-               : (mixed ? build_mixed(c, measure) : build_fp64(c, measure));
+    const bool bg = cfg->method == FVGB_SOLVER_BICG;
+    fst = bg ? build_bicg(c)
+             : bicg ? (mixed ? build_mixed_bicgstab(c) : build_bicgstab(c))
+                    : (mixed ? build_mixed(c, measure) : build_fp64(c, measure));
     if (fst != FVGB_OK) return fst;
     SolverParams prm{};
     prm.x = psi;
@@ -2982,6 +3292,7 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
     if (e == cudaSuccess) fst = fvgb_assemble(ls, terms, nterms, dt, bc, psi_b, (fvgb_stream)cs);
     if (e == cudaSuccess && fst == FVGB_OK) {
         k_set_params<<<grid_for(c->ncases, 128), 128, 0, cs>>>(c->L, c->ncases, prm);
+        if (cfg->flags & FVGB_SOLVE_RHS_BASELINE) k_case_bnorm<<<c->nb, kT, 0, cs>>>(c->L, ls->rhs, c->pa);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess && fst == FVGB_OK) {
@@ -2992,9 +3303,10 @@ extern "C" fvgb_status fvgb_step_create(fvgb_ls* ls, fvgb_batch* batch, const fv
         e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
         cudaGraphNode_t last;
         if (e == cudaSuccess)
-            e = bicg ? (mixed ? add_mixed_bicgstab_nodes(c, cg, deps, nd, &last)
-                              : add_bicgstab_nodes(c, cg, deps, nd, &last))
-                     : (mixed ? add_mixed_nodes(c, cg, deps, nd, &last) : add_fp64_nodes(c, cg, deps, nd, &last));
+            e = bg     ? add_bicg_nodes(c, cg, deps, nd, &last)
+                : bicg ? (mixed ? add_mixed_bicgstab_nodes(c, cg, deps, nd, &last)
+                                : add_bicgstab_nodes(c, cg, deps, nd, &last))
+                       : (mixed ? add_mixed_nodes(c, cg, deps, nd, &last) : add_fp64_nodes(c, cg, deps, nd, &last));
         if (e == cudaSuccess)
             e = cudaStreamUpdateCaptureDependencies(cs, &last, nullptr, 1, cudaStreamSetCaptureDependencies);
     }

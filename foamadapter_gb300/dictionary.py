@@ -244,7 +244,7 @@ def ginkgo_config(path) -> dict:
 def _kwargs(cfg) -> dict:
     return dict(rel_tol=cfg.rel_tol, abs_tol=cfg.abs_tol, max_iter=cfg.max_iter, precision=cfg.precision,
                 inner_rel_tol=cfg.inner_rel_tol, inner_max_iter=cfg.inner_max_iter, max_outer=cfg.max_outer,
-                method=cfg.method, preconditioner=cfg.preconditioner)
+                method=cfg.method, preconditioner=cfg.preconditioner, flags=cfg.flags)
 
 
 def scheme(fv_schemes: Dictionary, section: str, name: str) -> int:

@@ -296,11 +296,17 @@ typedef struct fvgb_solver_cfg {
                                   cooperative kernel (FP64 single case), 3 host-driven
                                   loop (FP64; blocks the caller); same results          */
     int32_t flags;             /* FVGB_SOLVE_NO_TUNE: default kernel variants, no timing
-                                  at the first solve (the timing synchronises the device) */
-    int32_t method;            /* FVGB_SOLVER_CG (Ginkgo Cg) or FVGB_SOLVER_BICGSTAB
+                                  at the first solve (the timing synchronises the device);
+                                  FVGB_SOLVE_RHS_BASELINE: rel_tol is relative to ||b||,
+                                  Ginkgo's ResidualNorm with its default baseline
+                                  rhs_norm (the reference's gko/config.bj.json), not to
+                                  the initial residual (Jacobi CG and BiCGStab) */
+    int32_t method;            /* FVGB_SOLVER_CG (Ginkgo Cg), FVGB_SOLVER_BICGSTAB
                                   (Ginkgo Bicgstab, fvSolution.cpp:25-26: nonsymmetric
                                   systems; graph path; MIXED_IR: FP32 inner BiCGStab,
-                                  restarted every refinement step)                       */
+                                  restarted every refinement step) or FVGB_SOLVER_BICG
+                                  (Ginkgo Bicg, OpenFOAM's PBiCG, fvSolution.cpp:24:
+                                  shadow residual driven by A^T; FP64, graph path)       */
     int32_t preconditioner;    /* FVGB_PRECOND_JACOBI (Ginkgo Jacobi, block size 1) or
                                   FVGB_PRECOND_MULTIGRID (Ginkgo Multigrid with PGM
                                   aggregation as tutorials/cylinder2D/system/gko/
@@ -309,8 +315,8 @@ typedef struct fvgb_solver_cfg {
                                   FVGB_PREC_MIXED_IR the V-cycle runs in FP32 inside
                                   the FP64 CG)                                          */
 } fvgb_solver_cfg;
-enum { FVGB_SOLVE_NO_TUNE = 1 };
-enum { FVGB_SOLVER_CG = 0, FVGB_SOLVER_BICGSTAB = 1 };
+enum { FVGB_SOLVE_NO_TUNE = 1, FVGB_SOLVE_RHS_BASELINE = 2 };
+enum { FVGB_SOLVER_CG = 0, FVGB_SOLVER_BICGSTAB = 1, FVGB_SOLVER_BICG = 2 };
 enum { FVGB_PRECOND_JACOBI = 0, FVGB_PRECOND_MULTIGRID = 1 };
 
 /* SolverStats {initResNorm, finalResNorm, numIter} (expression.hpp:155-158). */

@@ -609,6 +609,13 @@ double or_dot_tree(int32_t n, const double* a, const double* b) {
     return r;
 }
 
+/* The baseline of the relative tolerance: ||b|| by the GPU's reduction tree when
+ * the configuration asks for Ginkgo's default ResidualNorm baseline (rhs_norm),
+ * else the initial residual norm. */
+static double tol_base(const or_csr* A, const double* b, const or_solver_cfg* cfg, double res0) {
+    return (cfg->flags & 2) ? sqrt(or_dot_tree(A->n, b, b)) : res0;
+}
+
 /* ------------------------------------------------------------ FP64 Jacobi CG */
 static void spmv_row_fma(const or_csr* A, const double* val, const double* x, int32_t i, double* s) {
     double acc = 0.0;
@@ -647,7 +654,7 @@ static int32_t solve_fp64(const or_csr* A, const double* val, const double* b, d
     }
     double rz = final_tree(nb, pa), rr = final_tree(nb, pb);
     double res0 = sqrt(rr), res = res0;
-    double tol = cfg->rel_tol * res0;
+    double tol = cfg->rel_tol * tol_base(A, b, cfg, res0);
     if (cfg->abs_tol > tol) tol = cfg->abs_tol;
     int32_t it = 0, status = ST_OK;
     int done = !(res > tol) || res == 0.0;
@@ -855,7 +862,7 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
     for (int32_t i = 0; i < n; ++i) { y[i] = 0.0f; p[i] = z[i]; }
     rho = dot_tree_f(n, rh, z, part);
     res0 = res;
-    tol = cfg->rel_tol * res0;
+    tol = cfg->rel_tol * tol_base(A, b, cfg, res0);
     if (cfg->abs_tol > tol) tol = cfg->abs_tol;
     int done = 0;
     if (!isfinite(res)) { status = ST_BREAKDOWN; done = 1; }
@@ -979,7 +986,7 @@ static int32_t solve_bicgstab(const or_csr* A, const double* val, const double* 
     }
     double rho = dot64(n, rr, r, part);
     double res0 = sqrt(dot64(n, r, r, part)), res = res0;
-    double tol = cfg->rel_tol * res0;
+    double tol = cfg->rel_tol * tol_base(A, b, cfg, res0);
     if (cfg->abs_tol > tol) tol = cfg->abs_tol;
     double rho_prev = 1.0, alpha = 1.0, omega = 1.0;
     int32_t it = 0, status = ST_OK;
@@ -1065,7 +1072,7 @@ static int32_t solve_mixed_bicgstab(const or_csr* A, const double* val, const do
     residual_scale(sres, &sig, &isig);
     res = residual_step(A, val, b, x, dinv, sig, r, scratch, part, part2, n, nb, &sres);
     res0 = res;
-    tol = cfg->rel_tol * res0;
+    tol = cfg->rel_tol * tol_base(A, b, cfg, res0);
     if (cfg->abs_tol > tol) tol = cfg->abs_tol;
     int done = 0;
     if ((flags & 4u) || flags == 3u) { status = ST_UNSUPPORTED; done = 1; }
@@ -1153,9 +1160,102 @@ static int32_t solve_mixed_bicgstab(const or_csr* A, const double* val, const do
     return status;
 }
 
+/* ------------------------------------------------------------------ BiCG (FP64)
+ * Jacobi-preconditioned BiCG, Ginkgo's solver::Bicg (FoamAdapter maps PBiCG to
+ * it, fvSolution.cpp:24), in the operation order of the GPU kernels
+ * (solver.cu, BiCG section):
+ *   r = b - A x; r2 = r; z = D^-1 r; z2 = D^-1 r2; p = p2 = 0; rho = (r2, z); beta = rho / 1
+ *   loop: p = z + beta p; p2 = z2 + beta p2; q = A p; q2 = A^T p2;
+ *         alpha = rho / (p2, q); x += alpha p; r -= alpha q; r2 -= alpha q2;
+ *         z = D^-1 r; z2 = D^-1 r2; rho' = (r2, z); |r|; beta = rho' / rho
+ * (A^T x)_i runs over row i's columns j in order with the value a_ji. */
+static int32_t solve_bicg(const or_csr* A, const double* val, const double* b, double* x,
+                          const or_solver_cfg* cfg, or_solver_stats* st) {
+    const int32_t n = A->n, nb = nblocks_of(n);
+    double *dinv = zalloc(n), *r = zalloc(n), *r2 = zalloc(n), *z = zalloc(n), *z2 = zalloc(n);
+    double *p = zalloc(n), *p2 = zalloc(n), *q = zalloc(n), *q2 = zalloc(n), *part = zalloc(nb);
+    int32_t* tpos = (int32_t*)calloc((size_t)(A->nnz ? A->nnz : 1), sizeof(int32_t));
+    /* position of a_ji for every entry (i, j): binary search of column i in row j */
+    for (int32_t i = 0; i < n; ++i)
+        for (int32_t e = A->row_offs[i]; e < A->row_offs[i + 1]; ++e) {
+            const int32_t j = A->col[e];
+            int32_t lo = A->row_offs[j], hi = A->row_offs[j + 1] - 1, at = -1;
+            while (lo <= hi) {
+                const int32_t mid = (lo + hi) / 2;
+                if (A->col[mid] == i) { at = mid; break; }
+                if (A->col[mid] < i) lo = mid + 1; else hi = mid - 1;
+            }
+            tpos[e] = at;
+        }
+    for (int32_t i = 0; i < n; ++i) dinv[i] = 1.0 / val[A->row_offs[i] + A->diag_off[i]];
+    spmv_all(A, val, x, q);
+    for (int32_t i = 0; i < n; ++i) {
+        r[i] = b[i] - q[i];
+        r2[i] = r[i];
+        z[i] = dinv[i] * r[i];
+        z2[i] = z[i];
+    }
+    double rho = dot64(n, r2, z, part);
+    double res0 = sqrt(dot64(n, r, r, part)), res = res0;
+    double tol = cfg->rel_tol * tol_base(A, b, cfg, res0);
+    if (cfg->abs_tol > tol) tol = cfg->abs_tol;
+    double beta = rho / 1.0;
+    int32_t it = 0, status = ST_OK;
+    int done = !(res > tol) || res == 0.0;
+    if (!isfinite(res)) { done = 1; status = ST_BREAKDOWN; }
+    else if (!done && cfg->max_iter <= 0) { done = 1; status = ST_NOT_CONVERGED; }
+    else if (!done && !(rho != 0.0 && isfinite(rho))) { done = 1; status = ST_BREAKDOWN; }
+    while (!done) {
+        for (int32_t i = 0; i < n; ++i) {
+            p[i] = fma(beta, p[i], z[i]);
+            p2[i] = fma(beta, p2[i], z2[i]);
+        }
+        spmv_all(A, val, p, q);
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < n; ++i) {
+            double s = 0.0;
+            for (int32_t e = A->row_offs[i]; e < A->row_offs[i + 1]; ++e) s = fma(val[tpos[e]], p2[A->col[e]], s);
+            q2[i] = s;
+        }
+        const double pq = dot64(n, p2, q, part);
+        const double alpha = rho / pq;
+        if (pq == 0.0 || !isfinite(alpha)) { status = ST_BREAKDOWN; break; }
+        for (int32_t i = 0; i < n; ++i) {
+            x[i] = fma(alpha, p[i], x[i]);
+            r[i] = fma(-alpha, q[i], r[i]);
+            r2[i] = fma(-alpha, q2[i], r2[i]);
+            z[i] = dinv[i] * r[i];
+            z2[i] = dinv[i] * r2[i];
+        }
+        const double rho_new = dot64(n, r2, z, part);
+        res = sqrt(dot64(n, r, r, part));
+        ++it;
+        beta = rho_new / rho;
+        rho = rho_new;
+        if (!isfinite(res)) { status = ST_BREAKDOWN; break; }
+        if (!(res > tol)) break;
+        if (it >= cfg->max_iter) { status = ST_NOT_CONVERGED; break; }
+        if (!(rho != 0.0 && isfinite(rho))) { status = ST_BREAKDOWN; break; }
+    }
+    st->init_res_norm = res0;
+    st->final_res_norm = res;
+    st->num_iter = it;
+    st->num_outer = 0;
+    st->status = status;
+    free(dinv); free(r); free(r2); free(z); free(z2); free(p); free(p2); free(q); free(q2); free(part); free(tpos);
+    return status;
+}
+
 int32_t or_solve(const or_csr* A, const double* values, const double* rhs, double* x,
                  const or_solver_cfg* cfg, or_solver_stats* stats) {
     g_red_rpt = red_rows_per_thread(A->n);
+    if (cfg->method == 2) {
+        if (cfg->precision != 0) {
+            stats->status = ST_UNSUPPORTED;
+            return ST_UNSUPPORTED;
+        }
+        return solve_bicg(A, values, rhs, x, cfg, stats);
+    }
     if (cfg->method == 1) {
         if (cfg->precision == 1) return solve_mixed_bicgstab(A, values, rhs, x, cfg, stats);
         return solve_bicgstab(A, values, rhs, x, cfg, stats);

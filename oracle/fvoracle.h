@@ -49,7 +49,8 @@ typedef struct or_solver_cfg {
     int32_t max_iter, precision;
     double inner_rel_tol;
     int32_t inner_max_iter, max_outer;
-    int32_t method, pad; /* 0 CG, 1 BiCGStab (FP64 or mixed) */
+    int32_t method;      /* 0 CG, 1 BiCGStab (FP64 or mixed), 2 BiCG (FP64) */
+    int32_t flags;       /* 2: rel_tol relative to ||b|| (Ginkgo ResidualNorm, baseline rhs_norm) */
 } or_solver_cfg;
 
 typedef struct or_solver_stats {

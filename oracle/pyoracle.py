@@ -38,7 +38,7 @@ class OrTerm(C.Structure):
 class OrCfg(C.Structure):
     _fields_ = [("rel_tol", dbl), ("abs_tol", dbl), ("max_iter", i32), ("precision", i32),
                 ("inner_rel_tol", dbl), ("inner_max_iter", i32), ("max_outer", i32), ("method", i32),
-                ("pad", i32)]
+                ("flags", i32)]
 
 
 class OrStats(C.Structure):
@@ -197,10 +197,11 @@ class Oracle:
         return out
 
     def solve(self, values, rhs, x, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=0,
-              inner_rel_tol=None, inner_max_iter=1000, max_outer=50, method=0):
+              inner_rel_tol=None, inner_max_iter=1000, max_outer=50, method=0, flags=0):
+        """flags & 2: rel_tol relative to ||b|| (Ginkgo ResidualNorm, baseline rhs_norm)."""
         if inner_rel_tol is None:  # the host API's defaults: 0.1 for CG, 0.01 for BiCGStab
             inner_rel_tol = 0.01 if method == 1 else 0.1
-        cfg = OrCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer, method)
+        cfg = OrCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer, method, flags)
         st = OrStats()
         self.L.or_solve(C.byref(self.csr()), p(values), p(rhs), p(x), C.byref(cfg), C.byref(st))
         return st

@@ -158,10 +158,12 @@ def test_solver_config_rejects_what_is_not_built(ref):
     with pytest.raises(abi.FvgbError) as e:
         solver_config(m)
     assert e.value.status == abi.ERR_UNSUPPORTED
-    for text in ("solver PBiCG; preconditioner DIC;", "solver GAMG;"):
-        with pytest.raises(abi.FvgbError) as e:
-            solver_config(map_fv_solution(Dictionary.parse(text)))
-        assert e.value.status == abi.ERR_UNSUPPORTED
+    with pytest.raises(abi.FvgbError) as e:
+        solver_config(map_fv_solution(Dictionary.parse("solver GAMG;")))
+    assert e.value.status == abi.ERR_UNSUPPORTED
+    # PBiCG maps to Ginkgo's solver::Bicg, which is built
+    bicg = solver_config(map_fv_solution(Dictionary.parse("solver PBiCG; preconditioner DIC; relTol 1e-6;")))
+    assert bicg["method"] == abi.SOLVER_BICG and bicg["rel_tol"] == 1e-6
     with pytest.raises(abi.FvgbError):
         solver_config(Dictionary.parse("solver PCG;"))  # not mapped
     cfg = Dictionary.parse("configFile \"gko/config.bj.json\";")
@@ -349,10 +351,18 @@ def test_ginkgo_json_configs(ref, tmp_path):
     mg = ginkgo_config(gko / "config.mg.json")
     assert mg["method"] == abi.SOLVER_CG and mg["preconditioner"] == abi.PRECOND_MULTIGRID
     assert mg["max_iter"] == 100 and mg["abs_tol"] == 1e-5 and mg["rel_tol"] == 0.0
+    assert mg["flags"] == 0
     for name in ("config.bj.json", "p.config.bj.json"):  # ResidualNorm with Ginkgo's default baseline rhs_norm
-        with pytest.raises(abi.FvgbError) as e:
-            ginkgo_config(gko / name)
-        assert e.value.status == abi.ERR_UNSUPPORTED
+        bj = ginkgo_config(gko / name)
+        assert bj["method"] == abi.SOLVER_CG and bj["preconditioner"] == abi.PRECOND_JACOBI
+        assert bj["max_iter"] == 1000 and bj["rel_tol"] == 1e-5 and bj["abs_tol"] == 0.0
+        assert bj["flags"] == abi.SOLVE_RHS_BASELINE  # ||r|| <= 1e-5 ||b||
+    (tmp_path / "base.json").write_text(
+        '{"type": "solver::Cg", "preconditioner": {"type": "preconditioner::Jacobi", "max_block_size": 1},'
+        ' "criteria": [{"type": "ResidualNorm", "reduction_factor": 1e-9, "baseline": "something"}]}')
+    with pytest.raises(abi.FvgbError) as e:
+        ginkgo_config(tmp_path / "base.json")
+    assert e.value.status == abi.ERR_INVALID_ARG
     (tmp_path / "ok.json").write_text(
         '{"type": "solver::Bicgstab", "preconditioner": {"type": "preconditioner::Jacobi", "max_block_size": 1},'
         ' "criteria": [{"type": "Iteration", "max_iters": 77},'

@@ -419,3 +419,53 @@ def test_bicgstab_batch_equals_alone(cuda, precision):
                                                                   method=abi.SOLVER_BICGSTAB)
         assert stats[k].status == s1[0].status == abi.OK and stats[k].num_iter == s1[0].num_iter
         np.testing.assert_array_equal(x[lo:hi].cpu().numpy(), y[lo:hi].cpu().numpy())
+
+
+def test_bicg_bit_exact_on_nonsymmetric_system(cuda):
+    """BiCG (Ginkgo's solver::Bicg, the mapping of OpenFOAM's PBiCG,
+    fvSolution.cpp:24) on implicit upwind convection against the oracle's
+    restatement, bit for bit; the shadow residual runs on A^T."""
+    hm, dm, T, o, ls, v, r = convection_case()
+    x = T.internal.clone()
+    st = ls.solve(x, rel_tol=1e-10, max_iter=500, method=abi.SOLVER_BICG)
+    xo = T.host().copy()
+    so = o.solve(v, r, xo, rel_tol=1e-10, max_iter=500, method=2)
+    assert st.status == so.status == abi.OK and st.num_iter == so.num_iter > 3
+    assert (st.init_res_norm, st.final_res_norm) == (so.init_res_norm, so.final_res_norm)
+    np.testing.assert_array_equal(x.cpu().numpy(), xo)
+    assert np.linalg.norm(o.apply_operator(v, r, 1, xo)) <= 1e-10 * so.init_res_norm
+    st = ls.solve(T.internal.clone(), rel_tol=1e-14, max_iter=2, method=abi.SOLVER_BICG)
+    assert st.status == abi.ERR_NOT_CONVERGED and st.num_iter == 2
+    with pytest.raises(abi.FvgbError) as e:
+        ls.solve(T.internal.clone(), precision=abi.PREC_MIXED_IR, method=abi.SOLVER_BICG)
+    assert e.value.status == abi.ERR_UNSUPPORTED
+
+
+def test_bicg_batch_equals_alone_and_symmetric_case(cuda):
+    """Batched BiCG gives every case its bits alone; on a symmetric system BiCG
+    reaches the CG solution."""
+    parts = [mesh.box(7, 6, 5, jitter=0.1, seed=s) for s in (1, 2, 3)]
+    big, ranges, _ = mesh.concat(parts)
+    ranges = np.asarray(ranges, np.int32)
+    dm = DeviceMesh(big)
+    o = Oracle(big)
+    U = np.array([0.3, -1.0, 0.5])
+    F = o.flux_vec(np.tile(U, big.n), np.tile(U, big.nbf))
+    T = neon.VolumeField(dm, np.full(big.n, 0.5), [("fixedValue", 1.0)] * big.npatch)
+    ls = neon.LinearSystem(dm)
+    ls.assemble([neon.ddt(T.internal.clone()), neon.div(neon.SurfaceField(dm, F), "upwind"),
+                 neon.laplacian(neon.SurfaceField(dm, np.full(big.nif + big.nbf, 1e-2)), -1.0)], 0.1, T)
+    x = T.internal.clone()
+    stats = neon.Batch(ls, ranges).solve(x, rel_tol=1e-10, max_iter=500, method=abi.SOLVER_BICG)
+    for k in range(len(ranges) // 2):
+        lo, hi = int(ranges[2 * k]), int(ranges[2 * k + 1])
+        y = T.internal.clone()
+        s1 = neon.Batch(ls, np.asarray([lo, hi], np.int32)).solve(y, rel_tol=1e-10, max_iter=500,
+                                                                  method=abi.SOLVER_BICG)
+        assert stats[k].status == s1[0].status == abi.OK and stats[k].num_iter == s1[0].num_iter
+        np.testing.assert_array_equal(x[lo:hi].cpu().numpy(), y[lo:hi].cpu().numpy())
+    hm, dm2, T2, o2, ls2, v2, r2 = solve_case(12, 10, 8)
+    xb, xc = T2.internal.clone(), T2.internal.clone()
+    assert ls2.solve(xb, rel_tol=1e-12, method=abi.SOLVER_BICG).status == abi.OK
+    assert ls2.solve(xc, rel_tol=1e-12).status == abi.OK
+    np.testing.assert_allclose(xb.cpu().numpy(), xc.cpu().numpy(), rtol=1e-9, atol=0)

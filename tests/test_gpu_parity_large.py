@@ -200,3 +200,53 @@ def test_cavity_512_piso_steps_vs_oracle(cuda, precision):
     np.testing.assert_array_equal(gpu.p.host(), cpu.p)
     np.testing.assert_array_equal(gpu.U.host(), cpu.U)
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("precision,mode", [(abi.PREC_FP64, 1), (abi.PREC_FP64, 2), (abi.PREC_FP64, 3),
+                                            (abi.PREC_MIXED_IR, 1), (abi.PREC_MIXED_IR, 2)])
+def test_rhs_norm_baseline_vs_oracle(heat40k, precision, mode):
+    """Ginkgo's ResidualNorm with its default baseline (||r|| <= rel_tol ||b||,
+    the reference's gko/config.bj.json): ||b|| by the solver's reduction tree,
+    the same stop as the oracle's, bit for bit."""
+    hm, T, o, ls, v, r = heat40k
+    kw = dict(rel_tol=1e-5, max_iter=2000, inner_rel_tol=0.1, inner_max_iter=1000, max_outer=50)
+    x = T.internal.clone()
+    st = ls.solve(x, precision=precision, kernel_mode=mode, flags=abi.SOLVE_RHS_BASELINE, **kw)
+    xo = np.full(hm.n, 300.0)
+    so = o.solve(v, r, xo, precision=1 if precision == abi.PREC_MIXED_IR else 0, flags=2, **kw)
+    same(st, so, x, xo)
+    assert st.final_res_norm <= 1e-5 * float(np.linalg.norm(r))
+    # the baseline matters: relative to the initial residual the same rel_tol stops elsewhere
+    st0 = ls.solve(T.internal.clone(), precision=precision, kernel_mode=mode, **kw)
+    assert st0.num_iter != st.num_iter
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED_IR])
+def test_rhs_norm_baseline_bicgstab_vs_oracle(cuda, precision):
+    hm, T, o, ls, v, r = convection_system(34, 32, 31)
+    x = T.internal.clone()
+    st = ls.solve(x, rel_tol=1e-6, max_iter=3000, precision=precision, method=abi.SOLVER_BICGSTAB,
+                  flags=abi.SOLVE_RHS_BASELINE)
+    xo = T.host().copy()
+    so = o.solve(v, r, xo, rel_tol=1e-6, max_iter=3000, precision=1 if precision == abi.PREC_MIXED_IR else 0,
+                 method=1, flags=2)
+    same(st, so, x, xo)
+
+
+def test_rhs_norm_baseline_refused_where_not_built(heat40k):
+    hm, T, o, ls, v, r = heat40k
+    with pytest.raises(abi.FvgbError) as e:
+        ls.solve(T.internal.clone(), rel_tol=1e-5, preconditioner=abi.PRECOND_MULTIGRID,
+                 flags=abi.SOLVE_RHS_BASELINE)
+    assert e.value.status == abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("flags", [0, abi.SOLVE_RHS_BASELINE])
+def test_bicg_eight_row_tree_vs_oracle(cuda, flags):
+    hm, T, o, ls, v, r = convection_system(34, 32, 31)
+    x = T.internal.clone()
+    st = ls.solve(x, rel_tol=1e-8, max_iter=3000, method=abi.SOLVER_BICG, flags=flags)
+    xo = T.host().copy()
+    so = o.solve(v, r, xo, rel_tol=1e-8, max_iter=3000, method=2, flags=2 if flags else 0)
+    same(st, so, x, xo)
+    assert st.num_iter > 5
