@@ -38,8 +38,8 @@ CU_UNITS = {
     "serve.cu": [],
     "amg.cu": [],
 }
-CPP_UNITS = ["common.cpp", "meshgen.cpp", "foamio.cpp", "foamdict.cpp"]
-HEADERS = [INCLUDE / "fvgb.h", CSRC / "internal.cuh", CSRC / "fvgb_host_common.h"]
+CPP_UNITS = ["common.cpp", "meshgen.cpp", "foamio.cpp", "foamdict.cpp", "tunecache.cpp"]
+HEADERS = [INCLUDE / "fvgb.h", CSRC / "internal.cuh", CSRC / "fvgb_host_common.h", CSRC / "json_min.h", CSRC / "tunecache.h"]
 
 
 def _nvcc() -> str:

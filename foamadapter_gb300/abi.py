@@ -132,6 +132,10 @@ _SIGS = {
     "fvgb_solve_kernel_times": (C.c_int, [vp, vp, i32, vp, vp]),
     "fvgb_solve_tuning": (C.c_int, [vp, vp, vp, vp]),
     "fvgb_batch_tuning": (C.c_int, [vp, vp, vp, vp]),
+    "fvgb_tuning_cache_load": (C.c_int, [C.c_char_p]),
+    "fvgb_tuning_cache_save": (C.c_int, [C.c_char_p]),
+    "fvgb_tuning_cache_clear": (C.c_int, []),
+    "fvgb_tuning_cache_size": (C.c_int32, []),
     "fvgb_step_create": (C.c_int, [vp, vp, C.POINTER(Term), i32, dbl, C.POINTER(BC), vp, vp, vp,
                                    C.POINTER(SolverCfg), vp, C.POINTER(vp)]),
     "fvgb_step_launch": (C.c_int, [vp, vp]),

@@ -35,8 +35,11 @@
 #include <vector>
 
 #include "internal.cuh"
+#include "tunecache.h"
 
 #include <algorithm>
+#include <cmath>
+#include <string>
 
 namespace {
 
@@ -2427,6 +2430,7 @@ struct SolverCache {
     // blocks per SM for the FP64 kernels and the FP32 update, 6 for the FP32 SpMV
     int variant[kTuneKinds] = {3, 3, 2, 3};
     int forced[kTuneKinds] = {-1, -1, -1, -1};
+    int cached[kTuneKinds] = {-1, -1, -1, -1};  // from the tuning cache (tunecache.cpp), -1: none
     bool tuned64 = false, tunedmx = false;
     float tune_ms[kTuneKinds][kNumVariants] = {};
     int32_t* h_active = nullptr;           // pinned copy of n_active for the host-driven loop
@@ -2534,11 +2538,50 @@ float time_launch(const void* fn, unsigned grid, void** args, cudaStream_t s, cu
 // persistent kernel or are launch bound).
 constexpr int kTuneMinRows = 1 << 18;
 
-void pick(SolverCache* c, int kind) {
-    int b = 1;
+static_assert(kTuneKinds == kTuneCacheKinds && kNumVariants == kTuneCacheVariants, "tuning cache layout");
+constexpr int kDefaultVariant[kTuneKinds] = {3, 3, 2, 3};
+
+// the fastest measured variant of a kind, -1 when none was measured
+int best_measured(const SolverCache* c, int kind) {
+    int b = -1;
     for (int v = 0; v < kNumVariants; ++v)
-        if (c->tune_ms[kind][v] > 0.0f && c->tune_ms[kind][v] < c->tune_ms[kind][b]) b = v;
-    c->variant[kind] = c->forced[kind] >= 0 ? c->forced[kind] : b;
+        if (c->tune_ms[kind][v] > 0.0f && (b < 0 || c->tune_ms[kind][v] < c->tune_ms[kind][b])) b = v;
+    return b;
+}
+
+// the variant in use: forced, else measured on this system, else cached for
+// its shape, else the default
+void pick(SolverCache* c, int kind) {
+    const int b = best_measured(c, kind);
+    c->variant[kind] = c->forced[kind] >= 0 ? c->forced[kind]
+                       : b >= 0             ? b
+                       : c->cached[kind] >= 0 ? c->cached[kind]
+                                              : kDefaultVariant[kind];
+}
+
+// The shape a cached choice applies to: rows (nearest power of two), stored
+// slots per row, 16- or 32-bit column offsets, and the GPU (compute capability
+// and SM count).
+std::string tune_key(const SolverCache* c) {
+    int dev = 0, sms = 0, cmaj = 0, cmin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&cmaj, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&cmin, cudaDevAttrComputeCapabilityMinor, dev);
+    const MeshView& m = c->ls->mesh->v;
+    const int lg = c->n > 0 ? (int)std::lround(std::log2((double)c->n)) : 0;
+    const long spr = c->n > 0 ? std::lround((double)c->ls->mesh->nnz / c->n) : 0;
+    return "sm" + std::to_string(cmaj * 10 + cmin) + "x" + std::to_string(sms) + "/rows2^" + std::to_string(lg) +
+           "/slots" + std::to_string(spr) + "/off" + (m.m_off ? "16" : "32");
+}
+
+// Looks the kinds [k0, k0 + 2) up in the tuning cache; true when both are known.
+bool cache_lookup(SolverCache* c, const std::string& key, int k0) {
+    int v0 = -1, v1 = -1;
+    if (!tune_cache_get(key, k0, &v0) || !tune_cache_get(key, k0 + 1, &v1)) return false;
+    c->cached[k0] = v0;
+    c->cached[k0 + 1] = v1;
+    return true;
 }
 
 // Times the FP64 SpMV and update variants on this system: CG iterations from a
@@ -2546,7 +2589,9 @@ void pick(SolverCache* c, int kind) {
 // next solve's parameter kernel.
 fvgb_status tune_fp64(SolverCache* c, bool measure) {
     c->tuned64 = true;
-    if (measure && c->n >= kTuneMinRows) {
+    const std::string key = c->n >= kTuneMinRows ? tune_key(c) : std::string();
+    const bool hit = !key.empty() && cache_lookup(c, key, kTuneSpmv64);
+    if (measure && c->n >= kTuneMinRows && !hit) {
         FVGB_CUDA_TRY(cudaDeviceSynchronize());  // the system's assembly may still run on the caller's stream
         double* tmp = nullptr;
         cudaStream_t s = nullptr;
@@ -2582,6 +2627,7 @@ fvgb_status tune_fp64(SolverCache* c, bool measure) {
         if (s) cudaStreamDestroy(s);
         if (tmp) cudaFree(tmp);
         if (e != cudaSuccess) return cuda_fail(e, "FP64 CG autotuning");
+        for (int k = kTuneSpmv64; k <= kTuneUpdate64; ++k) tune_cache_put(key, k, best_measured(c, k), c->tune_ms[k]);
     }
     pick(c, kTuneSpmv64);
     pick(c, kTuneUpdate64);
@@ -2656,7 +2702,9 @@ fvgb_status build_fp64(SolverCache* c, bool measure = true) {
 // (after the preparation kernel, from a zero scratch vector).
 fvgb_status tune_mixed(SolverCache* c, bool measure) {
     c->tunedmx = true;
-    if (measure && c->n >= kTuneMinRows) {
+    const std::string key = c->n >= kTuneMinRows ? tune_key(c) : std::string();
+    const bool hit = !key.empty() && cache_lookup(c, key, kTuneSpmvMixed);
+    if (measure && c->n >= kTuneMinRows && !hit) {
         FVGB_CUDA_TRY(cudaDeviceSynchronize());
         double* tmp = nullptr;
         cudaStream_t s = nullptr;
@@ -2697,6 +2745,8 @@ fvgb_status tune_mixed(SolverCache* c, bool measure) {
         if (s) cudaStreamDestroy(s);
         if (tmp) cudaFree(tmp);
         if (e != cudaSuccess) return cuda_fail(e, "mixed CG autotuning");
+        for (int k = kTuneSpmvMixed; k <= kTuneUpdateMixed; ++k)
+            tune_cache_put(key, k, best_measured(c, k), c->tune_ms[k]);
     }
     pick(c, kTuneSpmvMixed);
     pick(c, kTuneUpdateMixed);

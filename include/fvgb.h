@@ -384,6 +384,18 @@ fvgb_status fvgb_solve_tuning(fvgb_ls* ls, const int32_t* force, int32_t* chosen
 /* The same for the solver of a batch (its variants are timed when the packed
  * system has at least 2^18 rows). */
 fvgb_status fvgb_batch_tuning(fvgb_batch* batch, const int32_t* force, int32_t* chosen, float* ms);
+/* The autotuner's cache (no counterpart in the reference): every measured choice
+ * is kept for the process, keyed by the system's shape (rows to the nearest power
+ * of two, stored slots per row, 16- or 32-bit column offsets, the GPU's compute
+ * capability and SM count); a later system of that shape -- also one solved with
+ * FVGB_SOLVE_NO_TUNE, as served requests are -- uses the cached choice and is not
+ * timed (ms reports 0 for it).  The cache can be written to and merged from a JSON
+ * file; the environment variable FVGB_TUNING_CACHE names a file that is read at
+ * the first lookup and rewritten after every new measurement. */
+fvgb_status fvgb_tuning_cache_load(const char* path);
+fvgb_status fvgb_tuning_cache_save(const char* path);
+fvgb_status fvgb_tuning_cache_clear(void);
+int32_t fvgb_tuning_cache_size(void);
 /* Measurement aid (no reference counterpart): runs the FP64 CG init and
  * `iters` iterations outside the graph on a private copy of x0, with CUDA
  * events around each kernel; ms_out[4] = mean milliseconds of

@@ -119,6 +119,7 @@ def test_batch_with_empty_and_single_cell_cases(cuda):
 def test_persistent_multiblock_path_above_threshold(cuda):
     """1,050,291 rows (> 2^20): the automatic mode uses the graph; forcing the
     cooperative kernel runs ~7 virtual blocks per resident block; same bits."""
+    abi.lib().fvgb_tuning_cache_clear()  # a cached choice for this shape would skip the timing checked below
     hm = mesh.box(103, 103, 99, jitter=0.05, seed=7)
     dm, T, ls, v, r = system(hm, dt=0.01)
     out = []

@@ -1,0 +1,90 @@
+"""The autotuner's cache file (tunecache.cpp): load, merge, save and clear on
+the host, and -- on a GPU -- a cached choice used for a new system of the same
+shape without timing it."""
+import ctypes as C
+import json
+
+import numpy as np
+import pytest
+
+from foamadapter_gb300 import abi
+
+
+def entry(key, variants):
+    return {"key": key, "variants": variants, "ms": [[0.1, 0.2, 0.3, 0.4]] * 4}
+
+
+def test_cache_file_round_trip(tmp_path):
+    L = abi.lib()
+    abi.check(L.fvgb_tuning_cache_clear())
+    assert L.fvgb_tuning_cache_size() == 0
+    f = tmp_path / "cache.json"
+    f.write_text(json.dumps({"version": 1, "entries": [entry("a", [0, 1, 2, 3]), entry("b", [3, -1, 2, -1])]}))
+    abi.check(L.fvgb_tuning_cache_load(str(f).encode()))
+    assert L.fvgb_tuning_cache_size() == 2
+    g = tmp_path / "out.json"
+    abi.check(L.fvgb_tuning_cache_save(str(g).encode()))
+    d = json.loads(g.read_text())
+    assert d["version"] == 1
+    assert {e["key"]: e["variants"] for e in d["entries"]} == {"a": [0, 1, 2, 3], "b": [3, -1, 2, -1]}
+    # merging keeps the other keys and replaces a key's entry
+    f.write_text(json.dumps({"version": 1, "entries": [entry("a", [3, 3, 3, 3])]}))
+    abi.check(L.fvgb_tuning_cache_load(str(f).encode()))
+    abi.check(L.fvgb_tuning_cache_save(str(g).encode()))
+    d = json.loads(g.read_text())
+    assert {e["key"]: e["variants"] for e in d["entries"]} == {"a": [3, 3, 3, 3], "b": [3, -1, 2, -1]}
+    # malformed files change nothing
+    for text in ("{", '{"version": 2, "entries": []}', '{"version": 1, "entries": [{"key": "c"}]}',
+                 json.dumps({"version": 1, "entries": [entry("c", [0, 9, 0, 0])]})):
+        f.write_text(text)
+        with pytest.raises(abi.FvgbError):
+            abi.check(L.fvgb_tuning_cache_load(str(f).encode()))
+    assert L.fvgb_tuning_cache_size() == 2
+    abi.check(L.fvgb_tuning_cache_clear())
+    assert L.fvgb_tuning_cache_size() == 0
+
+
+@pytest.mark.gpu
+def test_cached_choice_is_used_without_timing(cuda, tmp_path):
+    """A system of 2^18 rows is timed at its first solve and its choice cached;
+    after the cache is replaced by a file naming other variants, a new system of
+    the same shape uses them untimed, with the same bits."""
+    from foamadapter_gb300 import mesh, neon
+    from foamadapter_gb300.mesh import DeviceMesh
+
+    L = abi.lib()
+    abi.check(L.fvgb_tuning_cache_clear())
+    hm = mesh.box(64, 64, 64, jitter=0.1, seed=3)
+    dm = DeviceMesh(hm)
+
+    def system():
+        T = neon.VolumeField(dm, np.full(hm.n, 300.0), [("fixedValue", 400.0)] + [("zeroGradient", 0.0)] * 5)
+        ls = neon.LinearSystem(dm)
+        ls.assemble([neon.ddt(T.internal.clone()),
+                     neon.laplacian(neon.SurfaceField(dm, np.ones(hm.nif + hm.nbf)), -1.0)], 0.01, T)
+        return T, ls
+
+    chosen, ms = (C.c_int32 * 4)(), (C.c_float * 16)()
+    T, ls = system()
+    x1 = T.internal.clone()
+    assert ls.solve(x1, rel_tol=1e-8).status == abi.OK
+    abi.check(L.fvgb_solve_tuning(ls.handle, None, chosen, ms))
+    assert all(ms[v] > 0 for v in range(8))  # FP64 kinds timed
+    assert L.fvgb_tuning_cache_size() == 1
+    f = tmp_path / "cache.json"
+    abi.check(L.fvgb_tuning_cache_save(str(f).encode()))
+    d = json.loads(f.read_text())
+    key = d["entries"][0]["key"]
+    assert key.startswith("sm") and "/rows2^18/" in key
+    d["entries"][0]["variants"] = [0, 1, 0, 1]
+    f.write_text(json.dumps(d))
+    abi.check(L.fvgb_tuning_cache_clear())
+    abi.check(L.fvgb_tuning_cache_load(str(f).encode()))
+    T2, ls2 = system()
+    x2 = T2.internal.clone()
+    assert ls2.solve(x2, rel_tol=1e-8).status == abi.OK
+    abi.check(L.fvgb_solve_tuning(ls2.handle, None, chosen, ms))
+    assert list(chosen) == [2, 4, 2, 4]
+    assert all(t == 0.0 for t in ms)  # nothing timed
+    assert np.array_equal(x1.cpu().numpy(), x2.cpu().numpy())
+    abi.check(L.fvgb_tuning_cache_clear())
