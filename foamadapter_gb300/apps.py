@@ -50,6 +50,14 @@ class Advection:
         self.T.internal, self.T2 = self.T2, self.T.internal
         self.T.boundary, self.Tb2 = self.Tb2, self.T.boundary
 
+    def run(self, nsteps):
+        """nsteps steps in one call (fvgb_advect_euler_steps): the same bits as
+        nsteps calls of step()."""
+        bc = self.T.bc_struct()
+        abi.check(abi.lib().fvgb_advect_euler_steps(self.dm.handle, abi.ptr(self.flux.values),
+                                                    abi.ptr(self.T.internal), abi.ptr(self.T.boundary), self.dt,
+                                                    C.byref(bc), nsteps, abi.ptr(self.T2), abi.ptr(self.Tb2), _s()))
+
 
 class HeatTransfer:
     """ddt(T) - laplacian(kappa, T) = 0 with implicit Euler, the time loop of

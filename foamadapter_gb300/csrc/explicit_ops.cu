@@ -250,6 +250,10 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// meshes up to this size advance with the one-pass step kernel (k_advect_euler,
+// one launch per step and no face buffer); larger ones with the two-pass step
+constexpr int kStepsMaxCells = 1 << 16;
+
 // ----------------------------------------------------------------------- grad
 __device__ __forceinline__ void grad_entry(const MeshView& m, int code, double To, double wf, const double* S,
                                            double Tc, double& g0, double& g1, double& g2) {
@@ -958,6 +962,40 @@ extern "C" fvgb_status fvgb_nonorth_flux(const fvgb_mesh* m, int32_t nc, const d
     k_axpy_faces<<<grid_for(cnt, kThreads), kThreads, 0, s>>>(cnt, coeff, fx, out);
     cudaFreeAsync(fx, s);
     FVGB_LAUNCH_CHECK("fvgb_nonorth_flux");
+    return FVGB_OK;
+}
+
+extern "C" fvgb_status fvgb_advect_euler_steps(const fvgb_mesh* m, const double* flux, double* T, double* T_b,
+                                               double dt, const fvgb_bc* bc, int32_t nsteps, double* work,
+                                               double* work_b, fvgb_stream stream) {
+    FVGB_CHECK_ARG(m && bc && nsteps >= 0, "fvgb_advect_euler_steps: bad argument");
+    FVGB_CHECK_ARG(flux && T && work && ((T_b && work_b) || m->v.nbf == 0), "fvgb_advect_euler_steps: null field");
+    FVGB_CHECK_ARG(T != work && (m->v.nbf == 0 || T_b != work_b), "fvgb_advect_euler_steps: work must not alias T");
+    PatchTable pt;
+    FVGB_CHECK_ARG(make_patch_table(m, bc->patch_type, &pt), "fvgb_advect_euler_steps: bad patch types");
+    FVGB_CHECK_ARG(bc->ref || !patch_table_needs_ref(pt), "fvgb_advect_euler_steps: ref is null");
+    if (nsteps == 0) return FVGB_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (m->v.n <= kStepsMaxCells) {
+        for (int k = 0; k < nsteps; ++k) {
+            const bool even = (k & 1) == 0;
+            k_advect_euler<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(
+                m->v, pt, flux, even ? T : work, even ? T_b : work_b, dt, bc->ref, even ? work : T, even ? work_b : T_b);
+        }
+    } else {
+        for (int k = 0; k < nsteps; ++k) {
+            const bool even = (k & 1) == 0;
+            const fvgb_status st = fvgb_advect_euler_step(m, flux, even ? T : work, even ? T_b : work_b, dt, bc,
+                                                          even ? work : T, even ? work_b : T_b, stream);
+            if (st != FVGB_OK) return st;
+        }
+    }
+    FVGB_LAUNCH_CHECK("fvgb_advect_euler_steps");
+    if (nsteps & 1) {  // the last step wrote the work buffers
+        FVGB_CUDA_TRY(cudaMemcpyAsync(T, work, sizeof(double) * (size_t)m->v.n, cudaMemcpyDeviceToDevice, s));
+        if (m->v.nbf > 0)
+            FVGB_CUDA_TRY(cudaMemcpyAsync(T_b, work_b, sizeof(double) * (size_t)m->v.nbf, cudaMemcpyDeviceToDevice, s));
+    }
     return FVGB_OK;
 }
 

@@ -206,6 +206,14 @@ fvgb_status fvgb_advect_euler_step(const fvgb_mesh* mesh, const double* flux,
                                    const double* T_old, const double* T_old_b, double dt,
                                    const fvgb_bc* bc, double* T_new, double* T_new_b,
                                    fvgb_stream stream);
+/* nsteps of fvgb_advect_euler_step in place on (T, T_b), the time loop of
+ * test_advection.cpp:116-170 in one call; work/work_b (same sizes) are the other
+ * half of the ping-pong.  Meshes of at most 65536 cells take one launch of a
+ * one-pass step kernel per step (no face buffer), larger ones the two-pass step
+ * of fvgb_advect_euler_step; both give the bits of nsteps single calls. */
+fvgb_status fvgb_advect_euler_steps(const fvgb_mesh* mesh, const double* flux, double* T, double* T_b,
+                                    double dt, const fvgb_bc* bc, int32_t nsteps, double* work,
+                                    double* work_b, fvgb_stream stream);
 
 /* ----------------------------------------------- linear system and assembly */
 typedef struct fvgb_ls fvgb_ls;

@@ -170,3 +170,25 @@ def test_advection_config_bit_exact(cuda):
     np.testing.assert_array_equal(a.cpu().numpy(), T)
     np.testing.assert_array_equal(ab.cpu().numpy(), Tb)
     assert abs(T.sum() - T0.sum()) / T0.sum() < 1e-2   # nearly conservative (outflow of a small tail)
+
+
+@pytest.mark.parametrize("n,nsteps", [(64, 100), (64, 7), (300, 5), (8, 0)])
+def test_advection_many_steps_in_one_call(cuda, n, nsteps):
+    """fvgb_advect_euler_steps (the one-pass step kernel for meshes up to 65536
+    cells, the two-pass step above) gives the bits of nsteps single steps and of
+    the oracle."""
+    from foamadapter_gb300 import apps
+
+    a, b = apps.Advection(n=n), apps.Advection(n=n)
+    hm = a.hm
+    T0, Tb0 = a.T.host().copy(), a.T.boundary.cpu().numpy()[:hm.nbf].copy()
+    a.run(nsteps)
+    for _ in range(nsteps):
+        b.step()
+    np.testing.assert_array_equal(a.T.host(), b.T.host())
+    np.testing.assert_array_equal(a.T.boundary.cpu().numpy()[:hm.nbf], b.T.boundary.cpu().numpy()[:hm.nbf])
+    o = Oracle(hm)
+    T, Tb = T0, Tb0
+    for _ in range(nsteps):
+        T, Tb = o.advect_euler(a.flux.host(), T, Tb, a.dt, np.full(hm.npatch, 2, np.int32), np.zeros(hm.nbf))
+    np.testing.assert_array_equal(a.T.host(), T)
