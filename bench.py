@@ -939,15 +939,15 @@ def run_serve(args):
 def run_targets(args, hm):
     """The other targets' evidence, measured in the default run: every explicit
     operator on the same 128^3 box (HBM and FP64 fractions, floor), the 512^2
-    cavity's pressure solve FP64 vs mixed over the first PISO steps, and a
-    64-case slice of the batched workload."""
+    cavity's 200 PISO steps with the pressure solved in FP64 and in mixed
+    precision, and a 64-case slice of the batched workload."""
     import copy
 
     out = {}
     a = copy.copy(args)
     a.explicit_ops = "interp_linear,interp_upwind,div_upwind,div_linear,grad,laplacian,sngrad,advect_euler"
     a.explicit_reps = 10
-    a.cavity_steps = 3
+    a.cavity_steps = 200  # the configuration's 200 steps: early steps need more mixed inner iterations
     a.cases, a.batch_steps, a.alone_cases = 64, 10, 16
     for key, fn in (("advection_64x64_100_steps", lambda: run_advection(a)),
                     ("explicit_operators", lambda: run_explicit(a, hm=hm)),
