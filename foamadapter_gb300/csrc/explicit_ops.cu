@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(kThreads)
 // The fused upwind advection step on a face-flux buffer: the divergence as in
 // k_gather_fx (coefficient 1), then the forward-Euler update and the boundary
 // correction of k_advect_euler.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 6)
     k_advect_gather(MeshView m, PatchTable pt, const double* __restrict__ fx, const double* __restrict__ Told,
                     const double* __restrict__ Told_b, double dt, const double* __restrict__ ref,
                     double* __restrict__ Tnew, double* __restrict__ Tnew_b) {
@@ -677,10 +677,22 @@ __global__ void __launch_bounds__(kThreads)
     const double dv = fadd(m, m.k_zero, fmul(m, s, __ldg(&m.invV[c])));
     const double tn = fsub(m, __ldg(&Told[c]), fmul(m, dt, dv));
     Tnew[c] = tn;
-    for (int j = e.width - 1; j >= 0; --j) {
-        const int code = j < kG ? e.code[j] : __ldg(&m.g_code[e.base + j * 32]);
-        if (code == FVGB_PAD) continue;
-        if (code < m.nif) break;
+    // boundary faces of this cell (its last entries): the entries held in
+    // registers are tested in an unrolled loop, any beyond them reloaded
+#pragma unroll
+    for (int j = 0; j < kG; ++j) {
+        const int code = e.code[j];
+        if (code == FVGB_PAD || code < m.nif) continue;
+        const int b = code - m.nif;
+        const int t = pt.type[__ldg(&m.bpatch[b])];
+        double bv = __ldg(&Told_b[b]);
+        if (t == FVGB_BC_FIXED_VALUE) bv = __ldg(&ref[b]);
+        else if (t == FVGB_BC_FIXED_GRADIENT) bv = tn + __ldg(&ref[b]) / __ldg(&m.bdelta[b]);
+        Tnew_b[b] = bv;
+    }
+    for (int j = kG; j < e.width; ++j) {
+        const int code = __ldg(&m.g_code[e.base + j * 32]);
+        if (code == FVGB_PAD || code < m.nif) continue;
         const int b = code - m.nif;
         const int t = pt.type[__ldg(&m.bpatch[b])];
         double bv = __ldg(&Told_b[b]);
