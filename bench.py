@@ -676,18 +676,22 @@ def run_multigrid(args):
     x0 = T.internal.clone()
     out = {}
     # --profile: the V-cycles only (no conditional graphs, so ncu can capture every kernel)
-    legs = (("jacobi", abi.PRECOND_JACOBI, abi.PREC_FP64), ("multigrid", abi.PRECOND_MULTIGRID, abi.PREC_FP64),
-            ("multigrid_fp32_vcycle", abi.PRECOND_MULTIGRID, abi.PREC_MIXED_IR))
-    for name, pc, prec in () if args.profile else legs:
+    legs = (("jacobi", abi.PRECOND_JACOBI, abi.PREC_FP64, abi.SOLVER_CG),
+            ("multigrid", abi.PRECOND_MULTIGRID, abi.PREC_FP64, abi.SOLVER_CG),
+            ("multigrid_fp32_vcycle", abi.PRECOND_MULTIGRID, abi.PREC_MIXED_IR, abi.SOLVER_CG),
+            ("multigrid_solver", abi.PRECOND_JACOBI, abi.PREC_FP64, abi.SOLVER_MULTIGRID),
+            ("multigrid_solver_fp32_vcycle", abi.PRECOND_JACOBI, abi.PREC_MIXED_IR, abi.SOLVER_MULTIGRID))
+    for name, pc, prec, method in () if args.profile else legs:
         times = []
         for rep in range(4):
             x = x0.clone()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            st = ls.solve(x, rel_tol=HEAT["rel_tol"], max_iter=4000, preconditioner=pc, precision=prec)
+            st = ls.solve(x, rel_tol=HEAT["rel_tol"], max_iter=4000, preconditioner=pc, precision=prec,
+                          method=method)
             torch.cuda.synchronize()
             times.append(1e3 * (time.perf_counter() - t0))
-        out[name] = {"ms": min(times[1:]), "first_ms": times[0], "iters": st.num_iter}
+        out[name] = {"ms": min(times[1:]), "first_ms": times[0], "iters": st.num_iter, "status": st.status}
     r = torch.randn(hm.n, dtype=torch.float64, device="cuda")
     z = torch.zeros_like(r)
     reps = args.explicit_reps

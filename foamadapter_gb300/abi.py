@@ -54,7 +54,7 @@ class SolverCfg(C.Structure):
                 ("flags", i32), ("method", i32), ("preconditioner", i32)]
 
 
-SOLVER_CG, SOLVER_BICGSTAB, SOLVER_BICG = 0, 1, 2
+SOLVER_CG, SOLVER_BICGSTAB, SOLVER_BICG, SOLVER_MULTIGRID = 0, 1, 2, 3
 PRECOND_JACOBI, PRECOND_MULTIGRID = 0, 1
 
 

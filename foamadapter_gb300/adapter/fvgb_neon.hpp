@@ -396,8 +396,15 @@ struct SolverConfig {
     int innerMaxIter = 1000;
     int maxOuter = 50;
     bool bicgstab = false;  // solver "BiCGStab" (fvSolution.cpp:25-26) instead of "CG"
+    bool bicg = false;      // solver "BiCG" (PBiCG, fvSolution.cpp:24; FP64)
+    bool multigridSolver = false;  // solver "Multigrid" on its own (GAMG, fvSolution.cpp:27)
     bool multigrid = false; // preconditioner solver::Multigrid instead of Jacobi (CG; with
                             // mixedPrecision the V-cycle runs in FP32 inside the FP64 CG)
+    bool rhsBaseline = false;  // relTol relative to ||b|| (Ginkgo ResidualNorm, baseline rhs_norm)
+    int method() const {
+        return multigridSolver ? FVGB_SOLVER_MULTIGRID
+                               : bicg ? FVGB_SOLVER_BICG : bicgstab ? FVGB_SOLVER_BICGSTAB : FVGB_SOLVER_CG;
+    }
 };
 
 class LinearSystem {
@@ -439,9 +446,8 @@ public:
         fvgb_solver_cfg cfg{c.relTol, c.tolerance, c.maxIter,
                             c.mixedPrecision ? FVGB_PREC_MIXED_IR : FVGB_PREC_FP64,
                             c.innerRelTol > 0 ? c.innerRelTol : (c.bicgstab ? 0.01 : 0.1),
-                            c.innerMaxIter, c.maxOuter, 0, 0,
-                            c.bicgstab ? FVGB_SOLVER_BICGSTAB : FVGB_SOLVER_CG,
-                            c.multigrid ? FVGB_PRECOND_MULTIGRID : FVGB_PRECOND_JACOBI};
+                            c.innerMaxIter, c.maxOuter, 0, c.rhsBaseline ? FVGB_SOLVE_RHS_BASELINE : 0,
+                            c.method(), c.multigrid ? FVGB_PRECOND_MULTIGRID : FVGB_PRECOND_JACOBI};
         fvgb_solver_stats s{};
         fvgb_status r = fvgb_solve(ls_.handle(), psi_.internalVector().data(), &cfg, &s, st);
         if (r != FVGB_OK && r != FVGB_ERR_NOT_CONVERGED) check(r);  // non-convergence is not an error
@@ -689,7 +695,10 @@ inline SolverConfig solverConfigOf(const fvgb_solver_cfg& c) {
     s.innerMaxIter = c.inner_max_iter;
     s.maxOuter = c.max_outer;
     s.bicgstab = c.method == FVGB_SOLVER_BICGSTAB;
+    s.bicg = c.method == FVGB_SOLVER_BICG;
+    s.multigridSolver = c.method == FVGB_SOLVER_MULTIGRID;
     s.multigrid = c.preconditioner == FVGB_PRECOND_MULTIGRID;
+    s.rhsBaseline = (c.flags & FVGB_SOLVE_RHS_BASELINE) != 0;
     return s;
 }
 // PDESolver::solve configured by the case's fvSolution as the reference reads

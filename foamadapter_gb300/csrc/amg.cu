@@ -1,9 +1,12 @@
-// Multigrid-preconditioned CG (FP64) for a single scalar system.
+// Multigrid-preconditioned CG (FP64) for a single scalar system, and the
+// multigrid solver on its own.
 //
-// The reference selects it through a Ginkgo configuration: solver::Cg whose
-// preconditioner is solver::Multigrid with multigrid::Pgm levels
-// (tutorials/cylinder2D/system/gko/config.mg.json; GAMG in an fvSolution maps
-// to Ginkgo's multigrid, src/compatibility/fvSolution.cpp:27).  Ginkgo is not
+// The reference selects the first through a Ginkgo configuration: solver::Cg
+// whose preconditioner is solver::Multigrid with multigrid::Pgm levels
+// (tutorials/cylinder2D/system/gko/config.mg.json).  GAMG in an fvSolution
+// maps to Ginkgo's solver::Multigrid as the solver
+// (src/compatibility/fvSolution.cpp:27): cfg->method = FVGB_SOLVER_MULTIGRID
+// iterates x += V(b - A x) with the same hierarchy and V-cycle.  Ginkgo is not
 // part of the reference checkout; this is this library's own aggregation AMG
 // built on the published parallel-graph-match (PGM) idea:
 //
@@ -39,11 +42,13 @@
 // runs in one block (k_tail, which can take more levels: kTailRows).  Coarse
 // levels are sliced ELL like the system matrix.
 //
-// The solve is one CUDA graph (init, a device-side while loop over the CG
-// iteration with the V-cycle inside, bounded by max_iter).  Its stopping test
-// and statistics are those of the Jacobi-PCG (Ginkgo criteria: ||r|| below
-// max(rel_tol ||r_0||, abs_tol)).  Every reduction has a fixed order, so a
-// solve is deterministic; its iterates are not those of the Jacobi-PCG.
+// A solve is one CUDA graph (init, a device-side while loop over the CG
+// iteration with the V-cycle inside, or over the multigrid iteration, bounded
+// by max_iter).  Its stopping test and statistics are those of the Jacobi-PCG
+// (Ginkgo criteria: ||r|| below max(rel_tol ||r_0||, abs_tol), or
+// max(rel_tol ||b||, abs_tol) with FVGB_SOLVE_RHS_BASELINE).  Every reduction
+// has a fixed order, so a solve is deterministic; its iterates are not those
+// of the Jacobi-PCG.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -185,6 +190,8 @@ struct AmgState {
     double rz, alpha, beta, res0, res, tol;
     int32_t iter, status, done;
     unsigned counter;
+    int32_t want_bbase;            // FVGB_SOLVE_RHS_BASELINE: rel_tol is relative to ||b||
+    double bbase;                  // ||b|| when asked for (k_bnorm), else -1
     fvgb_solver_stats* stats_out;  // device, or null
     fvgb_solver_stats stats;
 };
@@ -247,6 +254,7 @@ struct AmgCache {
     float* ainvf = nullptr;
     TailLevelT<float>* tailf = nullptr;
     cudaGraphExec_t graph32 = nullptr;
+    cudaGraphExec_t graph_mg[2] = {nullptr, nullptr};  // the standalone multigrid solver, FP64 / FP32 V-cycle
     std::vector<void*> allocs;
     int nblk = 0;
 };
@@ -568,7 +576,9 @@ __global__ void __launch_bounds__(kT) k_to_float(int64_t count, const double* __
 
 // ------------------------------------------------------------ CG
 __global__ void k_params(AmgState* st, double* x, double rel_tol, double abs_tol, int max_iter,
-                         fvgb_solver_stats* out) {
+                         fvgb_solver_stats* out, int want_bbase) {
+    st->want_bbase = want_bbase;
+    st->bbase = -1.0;
     st->x = x;
     st->rel_tol = rel_tol;
     st->abs_tol = abs_tol;
@@ -590,6 +600,17 @@ __device__ __forceinline__ void first_sweep(int i, double ri, const double* __re
     } else {
         x0[i] = kOmega * __ldg(&dinv0[i]) * ri;
     }
+}
+
+// ||b||, the baseline of the relative tolerance when the solve asks for it
+// (Ginkgo's ResidualNorm with its default baseline, rhs_norm)
+__global__ void __launch_bounds__(kT) k_bnorm(AmgState* st, int n, const double* __restrict__ b, double* part) {
+    __shared__ double sm[kT];
+    if (!st->want_bbase) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    const double bi = i < n ? __ldg(&b[i]) : 0.0;
+    double tot;
+    if (arrive(st, part, block_sum(bi * bi, sm), sm, &tot) && threadIdx.x == 0) st->bbase = sqrt(tot);
 }
 
 // r = b - A x, ||r||; the V-cycle's first sweep
@@ -614,7 +635,7 @@ __global__ void __launch_bounds__(kT)
         st->res0 = st->res = res;
         st->iter = 0;
         st->status = FVGB_OK;
-        double tol = st->rel_tol * res;
+        double tol = st->rel_tol * (st->bbase >= 0.0 ? st->bbase : res);
         if (st->abs_tol > tol) tol = st->abs_tol;
         st->tol = tol;
         int done = !(res > tol) || res == 0.0;
@@ -729,6 +750,54 @@ __global__ void __launch_bounds__(kT)
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
     if (i < n) p[i] = fma(st->beta, p[i], __ldg(&z[i]));
+}
+
+// ------------------------------------------------------------ standalone multigrid
+// Ginkgo's solver::Multigrid (OpenFOAM's GAMG as FoamAdapter maps it): one
+// V-cycle per iteration on the current residual, x += V(b - A x), the
+// residual formed again from x, until the criteria hold.  The iteration starts
+// with k_init (r = b - A x, its norm, the tolerance, the V-cycle's first sweep).
+
+// x += z
+__global__ void __launch_bounds__(kT) k_mg_add(const AmgState* st, int n, const double* __restrict__ z) {
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    double* x = st->x;
+    if (i < n) x[i] = x[i] + __ldg(&z[i]);
+}
+
+// r = b - A x, ||r||, convergence; the V-cycle's first sweep of the next iteration
+__global__ void __launch_bounds__(kT)
+    k_mg_resid(AmgState* st, EllRows A, int n, const double* __restrict__ b, double* __restrict__ r, double* part,
+               const double* __restrict__ dinv0, double* __restrict__ x0, const float* __restrict__ d0f,
+               float* __restrict__ b0f, float* __restrict__ x0f) {
+    __shared__ double sm[kT];
+    if (done_flag(st)) return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    const double* x = st->x;
+    double ri = 0.0;
+    if (i < n) {
+        double s = 0.0;
+        A.each(i, [&](int j, double a) { s = fma(a, x[j], s); });
+        ri = __ldg(&b[i]) - s;
+        r[i] = ri;
+        first_sweep(i, ri, dinv0, x0, d0f, b0f, x0f);
+    }
+    double tot;
+    if (arrive(st, part, block_sum(ri * ri, sm), sm, &tot) && threadIdx.x == 0) {
+        const double res = sqrt(tot);
+        st->res = res;
+        st->iter += 1;
+        if (!isfinite(res)) {
+            st->status = FVGB_ERR_BREAKDOWN;
+            st->done = 1;
+        } else if (!(res > st->tol)) {
+            st->done = 1;
+        } else if (st->iter >= st->max_iter) {
+            st->status = FVGB_ERR_NOT_CONVERGED;
+            st->done = 1;
+        }
+    }
 }
 
 __global__ void k_cond(AmgState* st, cudaGraphConditionalHandle h) {
@@ -1090,7 +1159,10 @@ fvgb_status build_graph(AmgCache* c, bool f32) {
     void* a_rz[] = {&c->st, &n, &c->r, &c->z, &c->part};
     void* a_dir[] = {&c->st, &n, &c->z, &c->p};
     void* a_stats[] = {&c->st};
-    if (e == cudaSuccess) e = add_kernel(g, &node, nullptr, (void*)k_init, nb, kT, a_init);
+    void* a_bnorm[] = {&c->st, &n, &b, &c->part};
+    if (e == cudaSuccess) e = add_kernel(g, &node, nullptr, (void*)k_bnorm, nb, kT, a_bnorm);
+    prev = node;
+    if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_init, nb, kT, a_init);
     prev = node;
     if (e == cudaSuccess)
         e = f32 ? add_vcycle<float>(c, g, &prev, b0f, c->z, f0, true) : add_vcycle<double>(c, g, &prev, c->r, c->z, v0, true);
@@ -1126,6 +1198,69 @@ fvgb_status build_graph(AmgCache* c, bool f32) {
     if (e == cudaSuccess) e = cudaGraphInstantiate(&out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(e, "multigrid CG graph");
+    return FVGB_OK;
+}
+
+// The standalone multigrid solve as one graph: k_init, then a device-side
+// while loop over {V-cycle, x += z, r = b - A x}, bounded by max_iter.
+fvgb_status build_graph_mg(AmgCache* c, bool f32) {
+    cudaGraphExec_t& out = c->graph_mg[f32 ? 1 : 0];
+    if (out) {
+        cudaGraphExecDestroy(out);
+        out = nullptr;
+    }
+    const fvgb_ls* ls = c->ls;
+    EllRows A{ls->mesh->v, ls->values};
+    int n = ls->mesh->v.n;
+    const unsigned nb = (unsigned)c->nblk;
+    const double* b = ls->rhs;
+    cudaGraph_t g = nullptr;
+    FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    cudaGraphNode_t prev = nullptr, node;
+    VcycleArgs<double> v1;
+    VcycleArgs<float> f1;
+    double* x0 = f32 ? nullptr : c->lv[0].x;
+    const float* d0f = f32 ? c->lv[0].dinvf : nullptr;
+    float* b0f = f32 ? c->lv[0].bf : nullptr;
+    float* x0f = f32 ? c->lv[0].xf : nullptr;
+    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &x0, &d0f, &b0f, &x0f};
+    void* a_cond[] = {&c->st, &h};
+    void* a_add[] = {&c->st, &n, &c->z};
+    void* a_res[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &x0, &d0f, &b0f, &x0f};
+    void* a_stats[] = {&c->st};
+    void* a_bnorm[] = {&c->st, &n, &b, &c->part};
+    if (e == cudaSuccess) e = add_kernel(g, &node, nullptr, (void*)k_bnorm, nb, kT, a_bnorm);
+    prev = node;
+    if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_init, nb, kT, a_init);
+    prev = node;
+    if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_cond, 1, 1, a_cond);
+    prev = node;
+    cudaGraph_t body = nullptr;
+    if (e == cudaSuccess) {
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        e = cudaGraphAddNode(&node, g, &prev, nullptr, 1, &np);
+        if (e == cudaSuccess) body = np.conditional.phGraph_out[0];
+        prev = node;
+    }
+    cudaGraphNode_t bprev = nullptr, bnode;
+    if (e == cudaSuccess)
+        e = f32 ? add_vcycle<float>(c, body, &bprev, b0f, c->z, f1, true)
+                : add_vcycle<double>(c, body, &bprev, c->r, c->z, v1, true);
+    if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_mg_add, nb, kT, a_add);
+    bprev = bnode;
+    if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_mg_resid, nb, kT, a_res);
+    bprev = bnode;
+    if (e == cudaSuccess) e = add_kernel(body, &bnode, &bprev, (void*)k_cond, 1, 1, a_cond);
+    if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_stats, 1, 1, a_stats);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "multigrid solver graph");
     return FVGB_OK;
 }
 
@@ -1176,6 +1311,8 @@ void fvgb_amg_free(AmgCache* c) {
     if (!c) return;
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->graph32) cudaGraphExecDestroy(c->graph32);
+    for (cudaGraphExec_t g : c->graph_mg)
+        if (g) cudaGraphExecDestroy(g);
     for (void* p : c->allocs) cudaFree(p);
     delete c;
 }
@@ -1183,19 +1320,32 @@ void fvgb_amg_free(AmgCache* c) {
 fvgb_status fvgb_amg_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev,
                                  cudaStream_t s) {
     if (ls->ncomp != 1) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_solve: scalar systems only");
-    if (cfg->method != FVGB_SOLVER_CG)
-        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: CG only");
-    if (cfg->flags & FVGB_SOLVE_RHS_BASELINE)
-        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: the ||b|| tolerance baseline is not implemented");
-    // mixed precision: the CG, its residuals and its stopping test stay FP64;
-    // the V-cycle (the preconditioner) runs in FP32
+    const bool standalone = cfg->method == FVGB_SOLVER_MULTIGRID;
+    if (cfg->method != FVGB_SOLVER_CG && !standalone)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: as the preconditioner of CG only");
+    FVGB_CHECK_ARG(cfg->precision == FVGB_PREC_FP64 || cfg->precision == FVGB_PREC_MIXED_IR,
+                   "fvgb_solve: unknown precision");
+    FVGB_CHECK_ARG(cfg->rel_tol >= 0 && cfg->abs_tol >= 0, "fvgb_solve: negative tolerance");
+    FVGB_CHECK_ARG(cfg->max_iter >= 0 && cfg->max_iter <= 100000000, "fvgb_solve: bad max_iter");
+    FVGB_CHECK_ARG((cfg->flags & ~(FVGB_SOLVE_NO_TUNE | FVGB_SOLVE_RHS_BASELINE)) == 0, "fvgb_solve: unknown flags");
+    // mixed precision: the CG (or the multigrid iteration), its residuals and
+    // its stopping test stay FP64; the V-cycle runs in FP32
     const bool f32 = cfg->precision == FVGB_PREC_MIXED_IR;
     fvgb_status st = prepare(ls, s, f32);
     if (st != FVGB_OK) return st;
     AmgCache* c = ls->amg;
-    k_params<<<1, 1, 0, s>>>(c->st, x, cfg->rel_tol, cfg->abs_tol, cfg->max_iter, stats_dev);
+    if (standalone && !c->graph_mg[f32 ? 1 : 0]) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        FVGB_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return fvgb_fail(FVGB_ERR_UNSUPPORTED, "multigrid: the first solve of the multigrid solver cannot be stream-captured");
+        st = build_graph_mg(c, f32);
+        if (st != FVGB_OK) return st;
+    }
+    k_params<<<1, 1, 0, s>>>(c->st, x, cfg->rel_tol, cfg->abs_tol, cfg->max_iter, stats_dev,
+                             (cfg->flags & FVGB_SOLVE_RHS_BASELINE) ? 1 : 0);
     FVGB_LAUNCH_CHECK("multigrid params");
-    FVGB_CUDA_TRY(cudaGraphLaunch(f32 ? c->graph32 : c->graph, s));
+    FVGB_CUDA_TRY(cudaGraphLaunch(standalone ? c->graph_mg[f32 ? 1 : 0] : (f32 ? c->graph32 : c->graph), s));
     return FVGB_OK;
 }
 
@@ -1217,7 +1367,7 @@ extern "C" fvgb_status fvgb_amg_apply(fvgb_ls* ls, const double* r, double* z, f
     if (st != FVGB_OK) return st;
     AmgCache* c = ls->amg;
     // a one-off graph of the V-cycle alone, with the done flag cleared
-    k_params<<<1, 1, 0, s>>>(c->st, nullptr, 0.0, 0.0, 0, nullptr);
+    k_params<<<1, 1, 0, s>>>(c->st, nullptr, 0.0, 0.0, 0, nullptr, 0);
     cudaGraph_t g = nullptr;
     FVGB_CUDA_TRY(cudaGraphCreate(&g, 0));
     cudaGraphNode_t prev = nullptr;

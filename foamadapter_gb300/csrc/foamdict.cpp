@@ -765,15 +765,24 @@ extern "C" fvgb_status fvgb_solver_cfg_from_dict(const fvgb_dict* d, fvgb_solver
     if (w == "solver::Cg") c.method = FVGB_SOLVER_CG;
     else if (w == "solver::Bicgstab") c.method = FVGB_SOLVER_BICGSTAB;
     else if (w == "solver::Bicg") c.method = FVGB_SOLVER_BICG;
+    else if (w == "solver::Multigrid") c.method = FVGB_SOLVER_MULTIGRID;
     else
         return fvgb_fail(FVGB_ERR_UNSUPPORTED,
-                         ("solver entry: " + w + " is not implemented (Cg, Bicgstab, Bicg are)").c_str());
+                         ("solver entry: " + w + " is not implemented (Cg, Bicgstab, Bicg, Multigrid are)").c_str());
     const fvgb_dict::Entry* pe = entry_of(d, "preconditioner");
     const char* kPrecMsg =
         "solver entry: preconditioner::Jacobi with max_block_size 1 and solver::Multigrid (with CG) are implemented";
-    if (!pe || !pe->sub) return fvgb_fail(FVGB_ERR_UNSUPPORTED, kPrecMsg);
     double mbs = 0.0;
-    if (word_of(pe->sub.get(), "type", w) && w == "solver::Multigrid" && c.method == FVGB_SOLVER_CG) {
+    if (c.method == FVGB_SOLVER_MULTIGRID) {
+        // GAMG mapped (fvSolution.cpp:27): the multigrid solver; the Jacobi
+        // preconditioner entry updatePreconditioner inserts is its smoother's
+        if (pe && pe->sub &&
+            (!word_of(pe->sub.get(), "type", w) || w != "preconditioner::Jacobi" ||
+             !number_of(pe->sub.get(), "max_block_size", mbs) || mbs != 1.0))
+            return fvgb_fail(FVGB_ERR_UNSUPPORTED, "solver entry: solver::Multigrid smooths with Jacobi (block size 1) only");
+    } else if (!pe || !pe->sub) {
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, kPrecMsg);
+    } else if (word_of(pe->sub.get(), "type", w) && w == "solver::Multigrid" && c.method == FVGB_SOLVER_CG) {
         c.preconditioner = FVGB_PRECOND_MULTIGRID;
     } else if (!word_of(pe->sub.get(), "type", w) || w != "preconditioner::Jacobi" ||
                !number_of(pe->sub.get(), "max_block_size", mbs) || mbs != 1.0) {
@@ -810,6 +819,18 @@ namespace {
 using fvgb_json::Json;
 using fvgb_json::JsonParser;
 
+// a solver::Multigrid object's mg_level entries: multigrid::Pgm only
+fvgb_status pgm_levels_only(const Json& mg) {
+    const Json* lv = mg.get("mg_level");
+    if (lv && lv->kind == Json::ARR)
+        for (const Json& l : lv->arr) {
+            const Json* lt = l.get("type");
+            if (!lt || lt->kind != Json::STR || lt->str != "multigrid::Pgm")
+                return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: multigrid levels other than multigrid::Pgm");
+        }
+    return FVGB_OK;
+}
+
 fvgb_status cfg_from_json(const Json& j, fvgb_solver_cfg* out) {
     fvgb_solver_cfg c{};
     c.max_iter = 1000;
@@ -821,25 +842,25 @@ fvgb_status cfg_from_json(const Json& j, fvgb_solver_cfg* out) {
     if (t->str == "solver::Cg") c.method = FVGB_SOLVER_CG;
     else if (t->str == "solver::Bicgstab") c.method = FVGB_SOLVER_BICGSTAB;
     else if (t->str == "solver::Bicg") c.method = FVGB_SOLVER_BICG;
+    else if (t->str == "solver::Multigrid") c.method = FVGB_SOLVER_MULTIGRID;
     else
         return fvgb_fail(FVGB_ERR_UNSUPPORTED,
-                         ("Ginkgo config: " + t->str + " is not implemented (Cg, Bicgstab, Bicg are)").c_str());
+                         ("Ginkgo config: " + t->str + " is not implemented (Cg, Bicgstab, Bicg, Multigrid are)").c_str());
     const Json* p = j.get("preconditioner");
     const Json* pt = p ? p->get("type") : nullptr;
-    if (!pt || pt->kind != Json::STR)
+    if (c.method == FVGB_SOLVER_MULTIGRID) {  // the solver itself: Pgm levels, no preconditioner
+        fvgb_status ls = pgm_levels_only(j);
+        if (ls != FVGB_OK) return ls;
+        if (p) return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: solver::Multigrid takes no preconditioner");
+    } else if (!pt || pt->kind != Json::STR) {
         return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: an unpreconditioned solver is not implemented");
-    if (pt->str == "preconditioner::Jacobi") {
+    } else if (pt->str == "preconditioner::Jacobi") {
         const Json* mbs = p->get("max_block_size");
         if (!mbs || mbs->kind != Json::NUM || mbs->num != 1.0)
             return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: Jacobi with max_block_size 1 only");
     } else if (pt->str == "solver::Multigrid" && c.method == FVGB_SOLVER_CG) {
-        const Json* lv = p->get("mg_level");
-        if (lv && lv->kind == Json::ARR)
-            for (const Json& l : lv->arr) {
-                const Json* lt = l.get("type");
-                if (!lt || lt->kind != Json::STR || lt->str != "multigrid::Pgm")
-                    return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: multigrid levels other than multigrid::Pgm");
-            }
+        fvgb_status ls = pgm_levels_only(*p);
+        if (ls != FVGB_OK) return ls;
         c.preconditioner = FVGB_PRECOND_MULTIGRID;
     } else {
         return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("Ginkgo config: preconditioner " + pt->str + " is not implemented").c_str());

@@ -307,6 +307,8 @@ extern "C" fvgb_status fvgb_pcg_csr_noalloc(int32_t n, const int32_t* row_offs, 
                    "fvgb_pcg_csr_noalloc: null argument");
     if (cfg->preconditioner != FVGB_PRECOND_JACOBI)
         return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_pcg_csr_noalloc: Jacobi preconditioner only");
+    if (cfg->method != FVGB_SOLVER_CG)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "fvgb_pcg_csr_noalloc: CG only");
     FVGB_CHECK_ARG(n > 0, "fvgb_pcg_csr_noalloc: n must be positive");
     if (n > kMaxRows)
         return fvgb_fail(FVGB_ERR_INVALID_ARG,

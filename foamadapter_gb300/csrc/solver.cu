@@ -3027,6 +3027,9 @@ fvgb_status check_cfg(const fvgb_solver_cfg* cfg) {
     FVGB_CHECK_ARG(cfg->max_iter >= 0 && cfg->max_iter <= 100000000, "fvgb_solve: bad max_iter");
     FVGB_CHECK_ARG(cfg->kernel_mode >= 0 && cfg->kernel_mode <= 3, "fvgb_solve: bad kernel_mode");
     FVGB_CHECK_ARG((cfg->flags & ~(FVGB_SOLVE_NO_TUNE | FVGB_SOLVE_RHS_BASELINE)) == 0, "fvgb_solve: unknown flags");
+    if (cfg->method == FVGB_SOLVER_MULTIGRID)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED,
+                         "fvgb_solve: the multigrid solver solves single systems through fvgb_solve only");
     FVGB_CHECK_ARG(cfg->method == FVGB_SOLVER_CG || cfg->method == FVGB_SOLVER_BICGSTAB ||
                        cfg->method == FVGB_SOLVER_BICG,
                    "fvgb_solve: unknown method");
@@ -3220,14 +3223,20 @@ fvgb_status sync_stats(SolverCache* c, fvgb_solver_stats* stats, cudaStream_t s)
 
 }  // namespace
 
+namespace {
+// multigrid as CG's preconditioner or as the solver: amg.cu
+bool uses_multigrid(const fvgb_solver_cfg* cfg) {
+    return cfg->preconditioner == FVGB_PRECOND_MULTIGRID || cfg->method == FVGB_SOLVER_MULTIGRID;
+}
+}  // namespace
+
 extern "C" fvgb_status fvgb_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg,
                                         fvgb_solver_stats* stats_dev, fvgb_stream stream) {
     FVGB_CHECK_ARG(ls && x && cfg, "fvgb_solve: null argument");
     FVGB_CHECK_ARG(ls->ncomp == 1, "fvgb_solve: scalar systems only");
     FVGB_CHECK_ARG(cfg->preconditioner == FVGB_PRECOND_JACOBI || cfg->preconditioner == FVGB_PRECOND_MULTIGRID,
                    "fvgb_solve: unknown preconditioner");
-    if (cfg->preconditioner == FVGB_PRECOND_MULTIGRID)
-        return fvgb_amg_solve_async(ls, x, cfg, stats_dev, (cudaStream_t)stream);
+    if (uses_multigrid(cfg)) return fvgb_amg_solve_async(ls, x, cfg, stats_dev, (cudaStream_t)stream);
     SolverCache* c = nullptr;
     fvgb_status st = single_cache(ls, &c);
     if (st != FVGB_OK) return st;
@@ -3238,7 +3247,7 @@ extern "C" fvgb_status fvgb_solve(fvgb_ls* ls, double* x, const fvgb_solver_cfg*
                                   fvgb_stream stream) {
     fvgb_status st = fvgb_solve_async(ls, x, cfg, nullptr, stream);
     if (st != FVGB_OK) return st;
-    if (cfg->preconditioner == FVGB_PRECOND_MULTIGRID) return fvgb_amg_sync_stats(ls, stats, (cudaStream_t)stream);
+    if (uses_multigrid(cfg)) return fvgb_amg_sync_stats(ls, stats, (cudaStream_t)stream);
     return sync_stats(ls->solver, stats, (cudaStream_t)stream);
 }
 

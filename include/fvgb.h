@@ -312,9 +312,16 @@ typedef struct fvgb_solver_cfg {
     int32_t method;            /* FVGB_SOLVER_CG (Ginkgo Cg), FVGB_SOLVER_BICGSTAB
                                   (Ginkgo Bicgstab, fvSolution.cpp:25-26: nonsymmetric
                                   systems; graph path; MIXED_IR: FP32 inner BiCGStab,
-                                  restarted every refinement step) or FVGB_SOLVER_BICG
+                                  restarted every refinement step), FVGB_SOLVER_BICG
                                   (Ginkgo Bicg, OpenFOAM's PBiCG, fvSolution.cpp:24:
-                                  shadow residual driven by A^T; FP64, graph path)       */
+                                  shadow residual driven by A^T; FP64, graph path) or
+                                  FVGB_SOLVER_MULTIGRID (Ginkgo Multigrid as the solver,
+                                  OpenFOAM's GAMG, fvSolution.cpp:27: x += V(b - A x)
+                                  with the multigrid preconditioner's V-cycle until the
+                                  criteria hold; num_iter counts V-cycles; single
+                                  systems, fvgb_solve / fvgb_solve_async only;
+                                  `preconditioner` is not used; with FVGB_PREC_MIXED_IR
+                                  the V-cycle runs in FP32, the residuals in FP64)    */
     int32_t preconditioner;    /* FVGB_PRECOND_JACOBI (Ginkgo Jacobi, block size 1) or
                                   FVGB_PRECOND_MULTIGRID (Ginkgo Multigrid with PGM
                                   aggregation as tutorials/cylinder2D/system/gko/
@@ -324,7 +331,7 @@ typedef struct fvgb_solver_cfg {
                                   the FP64 CG)                                          */
 } fvgb_solver_cfg;
 enum { FVGB_SOLVE_NO_TUNE = 1, FVGB_SOLVE_RHS_BASELINE = 2 };
-enum { FVGB_SOLVER_CG = 0, FVGB_SOLVER_BICGSTAB = 1, FVGB_SOLVER_BICG = 2 };
+enum { FVGB_SOLVER_CG = 0, FVGB_SOLVER_BICGSTAB = 1, FVGB_SOLVER_BICG = 2, FVGB_SOLVER_MULTIGRID = 3 };
 enum { FVGB_PRECOND_JACOBI = 0, FVGB_PRECOND_MULTIGRID = 1 };
 
 /* SolverStats {initResNorm, finalResNorm, numIter} (expression.hpp:155-158). */

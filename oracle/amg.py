@@ -20,7 +20,10 @@ library's aggregation is checked exactly and its V-cycle to rounding:
   levels;
 * V-cycle: x = w D^-1 b, r = b - A x, restriction by aggregate sums, the
   coarser level (the coarsest solved exactly), y = x + P x_c,
-  out = y + w D^-1 (b - A y), w = 0.9.
+  out = y + w D^-1 (b - A y), w = 0.9;
+* the multigrid solver on its own (Ginkgo's solver::Multigrid, which
+  FoamAdapter maps OpenFOAM's GAMG to, src/compatibility/fvSolution.cpp:27):
+  x += V(b - A x) until ||b - A x|| <= max(rel_tol * baseline, abs_tol).
 """
 from __future__ import annotations
 
@@ -129,3 +132,34 @@ def vcycle(levels, b, l=0):
     xc = vcycle(levels, P.T @ r, l + 1)
     y = x + xc[agg]
     return y + OMEGA * dinv * (b - A @ y)
+
+
+def mg_solve(levels, b, x, rel_tol, abs_tol, max_iter, rhs_baseline=False):
+    """The multigrid solver: (x, cycles, initial and final residual norms,
+    status 0 / 3 not converged / 4 breakdown as fvgb_status), with the
+    library's stopping rules (checked after every cycle; the baseline is
+    ||r_0||, or ||b|| when rhs_baseline)."""
+    A = levels[0][0]
+    x = np.array(x, dtype=float)
+    r = b - A @ x
+    res0 = float(np.linalg.norm(r))
+    base = float(np.linalg.norm(b)) if rhs_baseline else res0
+    tol = max(rel_tol * base, abs_tol)
+    if not np.isfinite(res0):
+        return x, 0, res0, res0, 4
+    if not res0 > tol or res0 == 0.0:
+        return x, 0, res0, res0, 0
+    if max_iter <= 0:
+        return x, 0, res0, res0, 3
+    it, res = 0, res0
+    while True:
+        x = x + vcycle(levels, r)
+        r = b - A @ x
+        res = float(np.linalg.norm(r))
+        it += 1
+        if not np.isfinite(res):
+            return x, it, res0, res, 4
+        if not res > tol:
+            return x, it, res0, res, 0
+        if it >= max_iter:
+            return x, it, res0, res, 3

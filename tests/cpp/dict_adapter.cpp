@@ -74,9 +74,15 @@ int main(int argc, char** argv) {
         fvgb::Dictionary owned = p;  // an owned copy is independent
         owned.remove("criteria");
         REQUIRE(p.contains("criteria") && !owned.contains("criteria"));
+        // GAMG -> the multigrid solver; PBiCG -> BiCG
+        fvgb::SolverConfig mg = fvgb::solverConfig(fvgb::mapFvSolution(fvgb::Dictionary::parse("solver GAMG;")));
+        REQUIRE(mg.multigridSolver && mg.method() == FVGB_SOLVER_MULTIGRID && !mg.multigrid);
+        fvgb::SolverConfig bg =
+            fvgb::solverConfig(fvgb::mapFvSolution(fvgb::Dictionary::parse("solver PBiCG; preconditioner DIC;")));
+        REQUIRE(bg.bicg && bg.method() == FVGB_SOLVER_BICG);
         bool threw = false;
-        try {
-            fvgb::solverConfig(fvgb::mapFvSolution(fvgb::Dictionary::parse("solver GAMG;")));
+        try {  // DILU maps to Ginkgo's Ilu, which is not built
+            fvgb::solverConfig(fvgb::mapFvSolution(fvgb::Dictionary::parse("solver PBiCGStab; preconditioner DILU;")));
         } catch (const fvgb::Error& e) {
             threw = e.status == FVGB_ERR_UNSUPPORTED;
         }

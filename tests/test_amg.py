@@ -87,6 +87,22 @@ def test_multigrid_selected_by_dictionary():
     assert e.value.status == abi.ERR_UNSUPPORTED
 
 
+def test_multigrid_solver_restatement_converges():
+    """The oracle's multigrid solver reaches the direct solution; its cap and
+    its ||b|| baseline behave as stated."""
+    from scipy.sparse.linalg import spsolve
+
+    _, _, _, _, _, T, _, v, rhs, ro, col = heat_system(13, 11, 6)
+    levels = oamg.hierarchy(ro, col, v)
+    x, it, res0, res, status = oamg.mg_solve(levels, rhs, T, 1e-10, 0.0, 300)
+    assert status == 0 and 3 < it < 300 and res <= 1e-10 * res0
+    xs = spsolve(levels[0][0].tocsc(), rhs)
+    assert np.linalg.norm(x - xs) <= 1e-8 * np.linalg.norm(xs)
+    assert oamg.mg_solve(levels, rhs, T, 1e-14, 0.0, 2)[1:] [::3] == (2, 3)
+    xb, itb, _, resb, _ = oamg.mg_solve(levels, rhs, T, 1e-10, 0.0, 300, rhs_baseline=True)
+    assert resb <= 1e-10 * np.linalg.norm(rhs) and itb != it
+
+
 # ------------------------------------------------------------------ GPU
 def gpu_system(cuda, dims, **kw):
     import torch
@@ -264,3 +280,73 @@ def test_first_mixed_multigrid_solve_refuses_capture(cuda):
     assert b"captured" in abi.lib().fvgb_last_error()
     st = ls.solve(xm, rel_tol=1e-9, precision=abi.PREC_MIXED_IR, preconditioner=abi.PRECOND_MULTIGRID)
     assert st.status == abi.OK
+
+
+# ------------------------------------------------------ the multigrid solver
+@pytest.mark.gpu
+@pytest.mark.parametrize("rhs_baseline", [False, True])
+def test_multigrid_solver_matches_restatement(cuda, rhs_baseline):
+    """OpenFOAM's GAMG as FoamAdapter maps it (Ginkgo solver::Multigrid):
+    x += V(b - A x) until the criteria.  The cycles and the result follow the
+    numpy restatement (the V-cycle agrees to rounding, so the count may
+    differ by one only at a tolerance boundary)."""
+    s = gpu_system(cuda, (18, 14, 10))
+    ls, x0 = s["ls"], s["x0"]
+    levels = oamg.hierarchy(s["ro"], s["col"], s["v"])
+    flags = abi.SOLVE_RHS_BASELINE if rhs_baseline else 0
+    x = x0.clone()
+    st = ls.solve(x, rel_tol=1e-9, max_iter=300, method=abi.SOLVER_MULTIGRID, flags=flags)
+    xw, it, res0, res, status = oamg.mg_solve(levels, s["rhs"], x0.cpu().numpy(), 1e-9, 0.0, 300,
+                                              rhs_baseline=rhs_baseline)
+    assert st.status == status == abi.OK
+    assert abs(st.num_iter - it) <= 1 and it > 3
+    assert st.init_res_norm == pytest.approx(res0, rel=1e-12)
+    base = np.linalg.norm(s["rhs"]) if rhs_baseline else st.init_res_norm
+    assert st.final_res_norm <= 1e-9 * base
+    xg = x.cpu().numpy()
+    assert np.linalg.norm(xg - xw) <= 1e-9 * np.linalg.norm(xw)
+    # the same system with multigrid-preconditioned CG reaches the same solution
+    xc = x0.clone()
+    assert ls.solve(xc, rel_tol=1e-11, preconditioner=abi.PRECOND_MULTIGRID).status == abi.OK
+    assert np.linalg.norm(xg - xc.cpu().numpy()) <= 1e-7 * np.linalg.norm(xg)
+    # deterministic
+    x2 = x0.clone()
+    st2 = ls.solve(x2, rel_tol=1e-9, max_iter=300, method=abi.SOLVER_MULTIGRID, flags=flags)
+    assert st2.num_iter == st.num_iter and np.array_equal(x2.cpu().numpy(), xg)
+
+
+@pytest.mark.gpu
+def test_multigrid_solver_fp32_vcycle(cuda):
+    """With mixed precision the V-cycle runs in FP32; the iteration, its
+    residuals and its stopping test stay FP64 and reach the FP64 tolerance."""
+    s = gpu_system(cuda, (24, 20, 16))
+    ls, x0 = s["ls"], s["x0"]
+    x64, x32 = x0.clone(), x0.clone()
+    st64 = ls.solve(x64, rel_tol=1e-10, max_iter=400, method=abi.SOLVER_MULTIGRID)
+    st32 = ls.solve(x32, rel_tol=1e-10, max_iter=400, method=abi.SOLVER_MULTIGRID, precision=abi.PREC_MIXED_IR)
+    assert st64.status == st32.status == abi.OK
+    assert st32.final_res_norm <= 1e-10 * st32.init_res_norm
+    assert abs(st32.num_iter - st64.num_iter) <= 2
+    a, b = x64.cpu().numpy(), x32.cpu().numpy()
+    assert np.linalg.norm(a - b) <= 1e-8 * np.linalg.norm(a)
+
+
+@pytest.mark.gpu
+def test_multigrid_solver_cap_and_refusals(cuda):
+    from foamadapter_gb300 import neon
+
+    s = gpu_system(cuda, (12, 10, 8))
+    ls, x0 = s["ls"], s["x0"]
+    st = ls.solve(x0.clone(), rel_tol=1e-14, max_iter=3, method=abi.SOLVER_MULTIGRID)
+    assert st.status == abi.ERR_NOT_CONVERGED and st.num_iter == 3
+    st = ls.solve(x0.clone(), rel_tol=1e-8, max_iter=0, method=abi.SOLVER_MULTIGRID)
+    assert st.status == abi.ERR_NOT_CONVERGED and st.num_iter == 0
+    n = s["hm"].n
+    b = neon.Batch(ls, [0, n])
+    x = x0.clone()
+    with pytest.raises(abi.FvgbError) as e:
+        b.solve(x, method=abi.SOLVER_MULTIGRID)
+    assert e.value.status == abi.ERR_UNSUPPORTED
+    with pytest.raises(abi.FvgbError) as e:
+        ls.solve(x, method=abi.SOLVER_MULTIGRID, precision=7)
+    assert e.value.status == abi.ERR_INVALID_ARG

@@ -158,8 +158,13 @@ def test_solver_config_rejects_what_is_not_built(ref):
     with pytest.raises(abi.FvgbError) as e:
         solver_config(m)
     assert e.value.status == abi.ERR_UNSUPPORTED
+    # GAMG maps to Ginkgo's solver::Multigrid as the solver, which is built; the
+    # smoother entry is dropped and the DIC (Jacobi) preconditioner inserted
+    gamg = solver_config(map_fv_solution(Dictionary.parse(
+        "solver GAMG; smoother GaussSeidel; tolerance 0; relTol 1e-7; maxIter 300;")))
+    assert gamg["method"] == abi.SOLVER_MULTIGRID and gamg["rel_tol"] == 1e-7 and gamg["max_iter"] == 300
     with pytest.raises(abi.FvgbError) as e:
-        solver_config(map_fv_solution(Dictionary.parse("solver GAMG;")))
+        solver_config(map_fv_solution(Dictionary.parse("solver GAMG; preconditioner DILU;")))
     assert e.value.status == abi.ERR_UNSUPPORTED
     # PBiCG maps to Ginkgo's solver::Bicg, which is built
     bicg = solver_config(map_fv_solution(Dictionary.parse("solver PBiCG; preconditioner DIC; relTol 1e-6;")))
@@ -370,12 +375,23 @@ def test_ginkgo_json_configs(ref, tmp_path):
     c = ginkgo_config(tmp_path / "ok.json")
     assert c["method"] == abi.SOLVER_BICGSTAB and c["max_iter"] == 77 and c["rel_tol"] == 1e-9
     assert c["preconditioner"] == abi.PRECOND_JACOBI
+    # solver::Multigrid as the solver, with Pgm levels
+    (tmp_path / "mg.json").write_text(
+        '{"type": "solver::Multigrid", "mg_level": [{"type": "multigrid::Pgm"}],'
+        ' "criteria": [{"type": "Iteration", "max_iters": 60},'
+        ' {"type": "ResidualNorm", "reduction_factor": 1e-8, "baseline": "initial_resnorm"}]}')
+    c = ginkgo_config(tmp_path / "mg.json")
+    assert c["method"] == abi.SOLVER_MULTIGRID and c["max_iter"] == 60 and c["rel_tol"] == 1e-8
     for text, status in (('{"type": "solver::Cg"', abi.ERR_INVALID_ARG),
                          ('{"type": "solver::Gmres", "preconditioner": {"type": "preconditioner::Jacobi", '
                           '"max_block_size": 1}}', abi.ERR_UNSUPPORTED),
                          ('{"type": "solver::Cg", "preconditioner": {"type": "preconditioner::Jacobi", '
                           '"max_block_size": 32}}', abi.ERR_UNSUPPORTED),
-                         ('{"type": "solver::Cg"}', abi.ERR_UNSUPPORTED)):
+                         ('{"type": "solver::Cg"}', abi.ERR_UNSUPPORTED),
+                         ('{"type": "solver::Multigrid", "mg_level": [{"type": "multigrid::Uniform"}]}',
+                          abi.ERR_UNSUPPORTED),
+                         ('{"type": "solver::Multigrid", "preconditioner": {"type": "preconditioner::Jacobi", '
+                          '"max_block_size": 1}}', abi.ERR_UNSUPPORTED)):
         (tmp_path / "bad.json").write_text(text)
         with pytest.raises(abi.FvgbError) as e:
             ginkgo_config(tmp_path / "bad.json")

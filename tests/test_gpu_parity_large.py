@@ -233,12 +233,18 @@ def test_rhs_norm_baseline_bicgstab_vs_oracle(cuda, precision):
     same(st, so, x, xo)
 
 
-def test_rhs_norm_baseline_refused_where_not_built(heat40k):
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED_IR])
+def test_rhs_norm_baseline_with_multigrid(heat40k, precision):
+    """The multigrid-preconditioned CG stops at ||r|| <= rel_tol ||b|| with
+    the flag: the baseline changes where it stops, and it stops in time."""
     hm, T, o, ls, v, r = heat40k
-    with pytest.raises(abi.FvgbError) as e:
-        ls.solve(T.internal.clone(), rel_tol=1e-5, preconditioner=abi.PRECOND_MULTIGRID,
-                 flags=abi.SOLVE_RHS_BASELINE)
-    assert e.value.status == abi.ERR_UNSUPPORTED
+    bn = float(np.linalg.norm(r))
+    st = ls.solve(T.internal.clone(), rel_tol=1e-5, precision=precision, preconditioner=abi.PRECOND_MULTIGRID,
+                  flags=abi.SOLVE_RHS_BASELINE)
+    assert st.status == abi.OK and st.final_res_norm <= 1e-5 * bn
+    st0 = ls.solve(T.internal.clone(), rel_tol=1e-5, precision=precision, preconditioner=abi.PRECOND_MULTIGRID)
+    assert st0.final_res_norm <= 1e-5 * st0.init_res_norm
+    assert st0.num_iter != st.num_iter
 
 
 @pytest.mark.parametrize("flags", [0, abi.SOLVE_RHS_BASELINE])

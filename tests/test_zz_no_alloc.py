@@ -95,6 +95,12 @@ def test_noalloc_rejects_oversize_and_mixed(cuda):
     cfg.precision = abi.PREC_MIXED_IR
     status, _ = call_noalloc(4, (dummy_i, dummy_i, dummy_i), dummy_d, dummy_d, dummy_d, cfg)
     assert status == abi.ERR_INVALID_ARG
+    # CG only: another method is refused, not run as CG
+    cfg.precision = abi.PREC_FP64
+    for method in (abi.SOLVER_BICGSTAB, abi.SOLVER_BICG, abi.SOLVER_MULTIGRID):
+        cfg.method = method
+        status, _ = call_noalloc(4, (dummy_i, dummy_i, dummy_i), dummy_d, dummy_d, dummy_d, cfg)
+        assert status == abi.ERR_UNSUPPORTED
 
 
 def test_noalloc_without_iteration_cap(cuda):
