@@ -680,7 +680,8 @@ def run_multigrid(args):
             ("multigrid", abi.PRECOND_MULTIGRID, abi.PREC_FP64, abi.SOLVER_CG),
             ("multigrid_fp32_vcycle", abi.PRECOND_MULTIGRID, abi.PREC_MIXED_IR, abi.SOLVER_CG),
             ("multigrid_solver", abi.PRECOND_JACOBI, abi.PREC_FP64, abi.SOLVER_MULTIGRID),
-            ("multigrid_solver_fp32_vcycle", abi.PRECOND_JACOBI, abi.PREC_MIXED_IR, abi.SOLVER_MULTIGRID))
+            ("multigrid_solver_fp32_vcycle", abi.PRECOND_JACOBI, abi.PREC_MIXED_IR, abi.SOLVER_MULTIGRID),
+            ("ilu_cg", abi.PRECOND_ILU, abi.PREC_FP64, abi.SOLVER_CG))
     for name, pc, prec, method in () if args.profile else legs:
         times = []
         for rep in range(4):

@@ -37,6 +37,7 @@ CU_UNITS = {
     "boxmesh.cu": ["-fmad=false"],
     "serve.cu": [],
     "amg.cu": [],
+    "ilu.cu": ["-fmad=false"],
 }
 CPP_UNITS = ["common.cpp", "meshgen.cpp", "foamio.cpp", "foamdict.cpp", "tunecache.cpp"]
 HEADERS = [INCLUDE / "fvgb.h", CSRC / "internal.cuh", CSRC / "fvgb_host_common.h", CSRC / "json_min.h", CSRC / "tunecache.h"]

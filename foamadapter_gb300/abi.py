@@ -55,7 +55,7 @@ class SolverCfg(C.Structure):
 
 
 SOLVER_CG, SOLVER_BICGSTAB, SOLVER_BICG, SOLVER_MULTIGRID = 0, 1, 2, 3
-PRECOND_JACOBI, PRECOND_MULTIGRID = 0, 1
+PRECOND_JACOBI, PRECOND_MULTIGRID, PRECOND_ILU = 0, 1, 2
 
 
 SOLVE_NO_TUNE = 1

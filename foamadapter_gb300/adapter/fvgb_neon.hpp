@@ -401,6 +401,8 @@ struct SolverConfig {
     bool multigrid = false; // preconditioner solver::Multigrid instead of Jacobi (CG; with
                             // mixedPrecision the V-cycle runs in FP32 inside the FP64 CG)
     bool rhsBaseline = false;  // relTol relative to ||b|| (Ginkgo ResidualNorm, baseline rhs_norm)
+    bool ilu = false;          // preconditioner Ilu/ParIlu (DILU, fvSolution.cpp:56-63): exact ILU(0);
+                               // CG or BiCGStab, FP64
     int method() const {
         return multigridSolver ? FVGB_SOLVER_MULTIGRID
                                : bicg ? FVGB_SOLVER_BICG : bicgstab ? FVGB_SOLVER_BICGSTAB : FVGB_SOLVER_CG;
@@ -447,7 +449,8 @@ public:
                             c.mixedPrecision ? FVGB_PREC_MIXED_IR : FVGB_PREC_FP64,
                             c.innerRelTol > 0 ? c.innerRelTol : (c.bicgstab ? 0.01 : 0.1),
                             c.innerMaxIter, c.maxOuter, 0, c.rhsBaseline ? FVGB_SOLVE_RHS_BASELINE : 0,
-                            c.method(), c.multigrid ? FVGB_PRECOND_MULTIGRID : FVGB_PRECOND_JACOBI};
+                            c.method(),
+                            c.multigrid ? FVGB_PRECOND_MULTIGRID : c.ilu ? FVGB_PRECOND_ILU : FVGB_PRECOND_JACOBI};
         fvgb_solver_stats s{};
         fvgb_status r = fvgb_solve(ls_.handle(), psi_.internalVector().data(), &cfg, &s, st);
         if (r != FVGB_OK && r != FVGB_ERR_NOT_CONVERGED) check(r);  // non-convergence is not an error
@@ -699,6 +702,7 @@ inline SolverConfig solverConfigOf(const fvgb_solver_cfg& c) {
     s.multigridSolver = c.method == FVGB_SOLVER_MULTIGRID;
     s.multigrid = c.preconditioner == FVGB_PRECOND_MULTIGRID;
     s.rhsBaseline = (c.flags & FVGB_SOLVE_RHS_BASELINE) != 0;
+    s.ilu = c.preconditioner == FVGB_PRECOND_ILU;
     return s;
 }
 // PDESolver::solve configured by the case's fvSolution as the reference reads

@@ -303,6 +303,7 @@ extern "C" fvgb_status fvgb_ls_destroy(fvgb_ls* ls) {
     cudaDeviceSynchronize();
     if (ls->solver) fvgb_solver_cache_free(ls->solver);
     if (ls->amg) fvgb_amg_free(ls->amg);
+    if (ls->ilu) fvgb_ilu_free(ls->ilu);
     cudaFree(ls->values);
     cudaFree(ls->rhs);
     cudaFree(ls->bmat);

@@ -747,6 +747,22 @@ extern "C" fvgb_status fvgb_fvsolution_map(const fvgb_dict* solver_dict, fvgb_di
     return FVGB_OK;
 }
 
+// A preconditioner::Ilu entry this library implements: CG or BiCGStab,
+// reverse_apply false (or absent), and a ParIlu (or exact Ilu) factorization,
+// both of whose fixed points are the ILU(0) factors the library forms.
+static fvgb_status ilu_entry_ok(const fvgb_dict* p, int32_t method) {
+    if (method != FVGB_SOLVER_CG && method != FVGB_SOLVER_BICGSTAB)
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "solver entry: preconditioner::Ilu with Cg or Bicgstab only");
+    std::string w;
+    if (word_of(p, "reverse_apply", w) && w != "false")
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "solver entry: preconditioner::Ilu with reverse_apply true");
+    const fvgb_dict::Entry* f = entry_of(p, "factorization");
+    if (f && (!f->sub || !word_of(f->sub.get(), "type", w) ||
+              (w != "factorization::ParIlu" && w != "factorization::Ilu")))
+        return fvgb_fail(FVGB_ERR_UNSUPPORTED, "solver entry: ILU factorizations other than ParIlu / Ilu");
+    return FVGB_OK;
+}
+
 extern "C" fvgb_status fvgb_solver_cfg_from_dict(const fvgb_dict* d, fvgb_solver_cfg* cfg) {
     if (!d || !cfg) return fvgb_fail(FVGB_ERR_INVALID_ARG, "fvgb_solver_cfg_from_dict: null argument");
     fvgb_solver_cfg c{};
@@ -784,6 +800,11 @@ extern "C" fvgb_status fvgb_solver_cfg_from_dict(const fvgb_dict* d, fvgb_solver
         return fvgb_fail(FVGB_ERR_UNSUPPORTED, kPrecMsg);
     } else if (word_of(pe->sub.get(), "type", w) && w == "solver::Multigrid" && c.method == FVGB_SOLVER_CG) {
         c.preconditioner = FVGB_PRECOND_MULTIGRID;
+    } else if (word_of(pe->sub.get(), "type", w) && w == "preconditioner::Ilu") {
+        // DILU mapped (fvSolution.cpp:56-63): ILU(0) with a ParIlu factorization, L applied first
+        fvgb_status st = ilu_entry_ok(pe->sub.get(), c.method);
+        if (st != FVGB_OK) return st;
+        c.preconditioner = FVGB_PRECOND_ILU;
     } else if (!word_of(pe->sub.get(), "type", w) || w != "preconditioner::Jacobi" ||
                !number_of(pe->sub.get(), "max_block_size", mbs) || mbs != 1.0) {
         return fvgb_fail(FVGB_ERR_UNSUPPORTED, kPrecMsg);
@@ -862,6 +883,17 @@ fvgb_status cfg_from_json(const Json& j, fvgb_solver_cfg* out) {
         fvgb_status ls = pgm_levels_only(*p);
         if (ls != FVGB_OK) return ls;
         c.preconditioner = FVGB_PRECOND_MULTIGRID;
+    } else if (pt->str == "preconditioner::Ilu") {
+        if (c.method != FVGB_SOLVER_CG && c.method != FVGB_SOLVER_BICGSTAB)
+            return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: preconditioner::Ilu with Cg or Bicgstab only");
+        const Json* ra = p->get("reverse_apply");
+        if (ra && !(ra->kind == Json::BOOL && !ra->b))
+            return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: preconditioner::Ilu with reverse_apply true");
+        const Json* f = p->get("factorization");
+        const Json* ft = f ? f->get("type") : nullptr;
+        if (f && (!ft || ft->kind != Json::STR || (ft->str != "factorization::ParIlu" && ft->str != "factorization::Ilu")))
+            return fvgb_fail(FVGB_ERR_UNSUPPORTED, "Ginkgo config: ILU factorizations other than ParIlu / Ilu");
+        c.preconditioner = FVGB_PRECOND_ILU;
     } else {
         return fvgb_fail(FVGB_ERR_UNSUPPORTED, ("Ginkgo config: preconditioner " + pt->str + " is not implemented").c_str());
     }

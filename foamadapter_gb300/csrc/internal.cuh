@@ -96,6 +96,7 @@ struct fvgb_mesh {
 
 struct SolverCache;  // solver.cu
 struct AmgCache;     // amg.cu
+struct IluCache;     // ilu.cu
 
 struct fvgb_ls {
     const fvgb_mesh* mesh = nullptr;
@@ -106,6 +107,7 @@ struct fvgb_ls {
     double* brhs = nullptr;    // [nbf*ncomp]
     SolverCache* solver = nullptr;
     AmgCache* amg = nullptr;   // multigrid hierarchy (amg.cu), built at the first multigrid solve
+    IluCache* ilu = nullptr;   // ILU(0) pattern data and graphs (ilu.cu), built at the first ILU solve
     uint64_t version = 1;      // bumped whenever `values` change (assembly, SetReference)
 };
 
@@ -114,6 +116,12 @@ void fvgb_amg_free(AmgCache* c);
 fvgb_status fvgb_amg_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev,
                                  cudaStream_t s);
 fvgb_status fvgb_amg_sync_stats(fvgb_ls* ls, fvgb_solver_stats* out, cudaStream_t s);
+
+// ilu.cu: ILU(0)-preconditioned CG / BiCGStab (cfg->preconditioner == FVGB_PRECOND_ILU)
+void fvgb_ilu_free(IluCache* c);
+fvgb_status fvgb_ilu_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg, fvgb_solver_stats* stats_dev,
+                                 cudaStream_t s);
+fvgb_status fvgb_ilu_sync_stats(fvgb_ls* ls, fvgb_solver_stats* out, cudaStream_t s);
 
 // Per-call patch table passed to kernels by value.
 struct PatchTable {

@@ -3228,15 +3228,18 @@ namespace {
 bool uses_multigrid(const fvgb_solver_cfg* cfg) {
     return cfg->preconditioner == FVGB_PRECOND_MULTIGRID || cfg->method == FVGB_SOLVER_MULTIGRID;
 }
+// (the multigrid solver does not use `preconditioner`, so it takes precedence over ILU)
 }  // namespace
 
 extern "C" fvgb_status fvgb_solve_async(fvgb_ls* ls, double* x, const fvgb_solver_cfg* cfg,
                                         fvgb_solver_stats* stats_dev, fvgb_stream stream) {
     FVGB_CHECK_ARG(ls && x && cfg, "fvgb_solve: null argument");
     FVGB_CHECK_ARG(ls->ncomp == 1, "fvgb_solve: scalar systems only");
-    FVGB_CHECK_ARG(cfg->preconditioner == FVGB_PRECOND_JACOBI || cfg->preconditioner == FVGB_PRECOND_MULTIGRID,
+    FVGB_CHECK_ARG(cfg->preconditioner == FVGB_PRECOND_JACOBI || cfg->preconditioner == FVGB_PRECOND_MULTIGRID ||
+                       cfg->preconditioner == FVGB_PRECOND_ILU,
                    "fvgb_solve: unknown preconditioner");
     if (uses_multigrid(cfg)) return fvgb_amg_solve_async(ls, x, cfg, stats_dev, (cudaStream_t)stream);
+    if (cfg->preconditioner == FVGB_PRECOND_ILU) return fvgb_ilu_solve_async(ls, x, cfg, stats_dev, (cudaStream_t)stream);
     SolverCache* c = nullptr;
     fvgb_status st = single_cache(ls, &c);
     if (st != FVGB_OK) return st;
@@ -3248,6 +3251,7 @@ extern "C" fvgb_status fvgb_solve(fvgb_ls* ls, double* x, const fvgb_solver_cfg*
     fvgb_status st = fvgb_solve_async(ls, x, cfg, nullptr, stream);
     if (st != FVGB_OK) return st;
     if (uses_multigrid(cfg)) return fvgb_amg_sync_stats(ls, stats, (cudaStream_t)stream);
+    if (cfg->preconditioner == FVGB_PRECOND_ILU) return fvgb_ilu_sync_stats(ls, stats, (cudaStream_t)stream);
     return sync_stats(ls->solver, stats, (cudaStream_t)stream);
 }
 

@@ -328,11 +328,16 @@ typedef struct fvgb_solver_cfg {
                                   config.mg.json selects it; CG, single systems,
                                   fvgb_solve / fvgb_solve_async only; with
                                   FVGB_PREC_MIXED_IR the V-cycle runs in FP32 inside
-                                  the FP64 CG)                                          */
+                                  the FP64 CG) or FVGB_PRECOND_ILU (Ginkgo Ilu with a
+                                  ParIlu factorization, OpenFOAM's DILU,
+                                  fvSolution.cpp:56-63: the exact ILU(0) factors,
+                                  formed level by level in every solve, and level-
+                                  scheduled triangular solves; CG or BiCGStab, FP64,
+                                  single systems, fvgb_solve / fvgb_solve_async)       */
 } fvgb_solver_cfg;
 enum { FVGB_SOLVE_NO_TUNE = 1, FVGB_SOLVE_RHS_BASELINE = 2 };
 enum { FVGB_SOLVER_CG = 0, FVGB_SOLVER_BICGSTAB = 1, FVGB_SOLVER_BICG = 2, FVGB_SOLVER_MULTIGRID = 3 };
-enum { FVGB_PRECOND_JACOBI = 0, FVGB_PRECOND_MULTIGRID = 1 };
+enum { FVGB_PRECOND_JACOBI = 0, FVGB_PRECOND_MULTIGRID = 1, FVGB_PRECOND_ILU = 2 };
 
 /* SolverStats {initResNorm, finalResNorm, numIter} (expression.hpp:155-158). */
 typedef struct fvgb_solver_stats {

@@ -939,7 +939,8 @@ static int32_t solve_mixed(const or_csr* A, const double* val, const double* b, 
  * Jacobi-preconditioned BiCGStab (Ginkgo's solver::Bicgstab as FoamAdapter
  * selects it, fvSolution.cpp:25-26, 106-142), right preconditioning, FP64,
  * in the operation order of the GPU kernels (solver.cu BiCGStab section); every
- * dot product by the GPU's reduction tree.
+ * dot product by the GPU's reduction tree.  With an ILU(0) factor (lu), y and
+ * z below are M^-1 p and M^-1 s (ilu.cu) instead of D^-1 p and D^-1 s.
  *   r = b - A x, rr = r, p = v = 0, rho = (rr, r), rho_prev = alpha = omega = 1
  *   loop: beta = (rho/rho_prev)(alpha/omega); p = r + beta (p - omega v); y = D^-1 p
  *         v = A y; alpha = rho / (rr, v); s = r - alpha v
@@ -974,10 +975,11 @@ static void spmv_all(const or_csr* A, const double* val, const double* x, double
 }
 
 static int32_t solve_bicgstab(const or_csr* A, const double* val, const double* b, double* x,
-                              const or_solver_cfg* cfg, or_solver_stats* st) {
+                              const or_solver_cfg* cfg, or_solver_stats* st, const double* lu) {
     const int32_t n = A->n, nb = nblocks_of(n);
     double *dinv = zalloc(n), *r = zalloc(n), *rr = zalloc(n), *p = zalloc(n), *v = zalloc(n);
     double *y = zalloc(n), *s = zalloc(n), *z = zalloc(n), *t = zalloc(n), *part = zalloc(nb);
+    double* fw = lu ? zalloc(n) : NULL;  /* ILU: the forward solve's result */
     for (int32_t i = 0; i < n; ++i) dinv[i] = 1.0 / val[A->row_offs[i] + A->diag_off[i]];
     spmv_all(A, val, x, t);
     for (int32_t i = 0; i < n; ++i) {
@@ -997,15 +999,16 @@ static int32_t solve_bicgstab(const or_csr* A, const double* val, const double* 
         const double beta = (rho / rho_prev) * (alpha / omega);
         for (int32_t i = 0; i < n; ++i) {
             p[i] = fma(beta, fma(-omega, v[i], p[i]), r[i]);
-            y[i] = dinv[i] * p[i];
+            if (!lu) y[i] = dinv[i] * p[i];
         }
+        if (lu) or_ilu_apply(A, lu, p, fw, y);
         spmv_all(A, val, y, v);
         const double rv = dot64(n, rr, v, part);
         alpha = rho / rv;
         if (rv == 0.0 || !isfinite(alpha)) { status = ST_BREAKDOWN; break; }
         for (int32_t i = 0; i < n; ++i) {
             s[i] = fma(-alpha, v[i], r[i]);
-            z[i] = dinv[i] * s[i];
+            if (!lu) z[i] = dinv[i] * s[i];
         }
         const double sres = sqrt(dot64(n, s, s, part));
         if (!isfinite(sres)) { status = ST_BREAKDOWN; res = sres; break; }
@@ -1015,6 +1018,7 @@ static int32_t solve_bicgstab(const or_csr* A, const double* val, const double* 
             res = sres;
             break;
         }
+        if (lu) or_ilu_apply(A, lu, s, fw, z);
         spmv_all(A, val, z, t);
         const double ts = dot64(n, t, s, part), tt = dot64(n, t, t, part);
         omega = ts / tt;
@@ -1037,7 +1041,7 @@ static int32_t solve_bicgstab(const or_csr* A, const double* val, const double* 
     st->num_iter = it;
     st->num_outer = 0;
     st->status = status;
-    free(dinv); free(r); free(rr); free(p); free(v); free(y); free(s); free(z); free(t); free(part);
+    free(dinv); free(r); free(rr); free(p); free(v); free(y); free(s); free(z); free(t); free(part); free(fw);
     return status;
 }
 
@@ -1246,9 +1250,123 @@ static int32_t solve_bicg(const or_csr* A, const double* val, const double* b, d
     return status;
 }
 
+/* ---------------------------------------------------------------- ILU(0)
+ * DILU in an fvSolution maps to Ginkgo's preconditioner::Ilu with a
+ * factorization::ParIlu (src/compatibility/fvSolution.cpp:56-63).  ParIlu's
+ * fixed-point sweeps approach the ILU(0) factors of A's pattern; the library
+ * (ilu.cu) forms those factors exactly, row after row in the IKJ order
+ * restated here: for every entry (i,k) left of the diagonal, k ascending,
+ * l_ik = a_ik / u_kk, then a_ij -= l_ik u_kj for every j > k present in both
+ * rows i and k, j ascending (as fma(-l_ik, u_kj, a_ij)).  On a hex mesh (no
+ * three cells pairwise adjacent) only the diagonal changes: OpenFOAM's DILU.
+ * z = U^-1 L^-1 r: y_i = r_i - sum_k l_ik y_k (k ascending, fma chain), then
+ * z_i = (y_i - sum_j u_ij z_j) / u_ii (j ascending). */
+void or_ilu_factor(const or_csr* A, const double* val, double* lu) {
+    const int32_t* ro = A->row_offs;
+    memcpy(lu, val, sizeof(double) * (size_t)A->nnz);
+    for (int32_t i = 0; i < A->n; ++i) {
+        const int32_t d = ro[i] + A->diag_off[i], end = ro[i + 1];
+        for (int32_t e = ro[i]; e < d; ++e) {
+            const int32_t k = A->col[e];
+            const int32_t dk = ro[k] + A->diag_off[k];
+            const double l = lu[e] / lu[dk];
+            lu[e] = l;
+            int32_t f = e + 1, g = dk + 1;
+            while (f < end && g < ro[k + 1]) {
+                if (A->col[f] < A->col[g]) ++f;
+                else if (A->col[f] > A->col[g]) ++g;
+                else {
+                    lu[f] = fma(-l, lu[g], lu[f]);
+                    ++f;
+                    ++g;
+                }
+            }
+        }
+    }
+}
+
+void or_ilu_apply(const or_csr* A, const double* lu, const double* r, double* y, double* z) {
+    const int32_t* ro = A->row_offs;
+    for (int32_t i = 0; i < A->n; ++i) {
+        double s = r[i];
+        for (int32_t e = ro[i]; e < ro[i] + A->diag_off[i]; ++e) s = fma(-lu[e], y[A->col[e]], s);
+        y[i] = s;
+    }
+    for (int32_t i = A->n - 1; i >= 0; --i) {
+        const int32_t d = ro[i] + A->diag_off[i];
+        double s = y[i];
+        for (int32_t e = d + 1; e < ro[i + 1]; ++e) s = fma(-lu[e], z[A->col[e]], s);
+        z[i] = s / lu[d];
+    }
+}
+
+/* CG with the ILU(0) preconditioner (ilu.cu), FP64, every dot by the GPU's tree:
+ *   r = b - A x, |r|; z = M^-1 r; p = z; rz = (r, z)
+ *   loop: q = A p; alpha = rz / (p, q); x += alpha p; r -= alpha q; |r|, stop tests;
+ *         z = M^-1 r; rz' = (r, z); beta = rz' / rz; p = z + beta p */
+static int32_t solve_cg_ilu(const or_csr* A, const double* val, const double* b, double* x,
+                            const or_solver_cfg* cfg, or_solver_stats* st, const double* lu) {
+    const int32_t n = A->n, nb = nblocks_of(n);
+    double *r = zalloc(n), *p = zalloc(n), *q = zalloc(n), *z = zalloc(n), *fw = zalloc(n), *part = zalloc(nb);
+    spmv_all(A, val, x, q);
+    for (int32_t i = 0; i < n; ++i) r[i] = b[i] - q[i];
+    double res0 = sqrt(dot64(n, r, r, part)), res = res0;
+    double tol = cfg->rel_tol * tol_base(A, b, cfg, res0);
+    if (cfg->abs_tol > tol) tol = cfg->abs_tol;
+    int32_t it = 0, status = ST_OK;
+    int done = !(res > tol) || res == 0.0;
+    if (!isfinite(res)) { done = 1; status = ST_BREAKDOWN; }
+    else if (!done && cfg->max_iter <= 0) { done = 1; status = ST_NOT_CONVERGED; }
+    double rz = 0.0;
+    if (!done) {
+        or_ilu_apply(A, lu, r, fw, z);
+        memcpy(p, z, sizeof(double) * (size_t)n);
+        rz = dot64(n, r, z, part);
+    }
+    while (!done) {
+        spmv_all(A, val, p, q);
+        const double pq = dot64(n, p, q, part);
+        const double alpha = rz / pq;
+        if (pq == 0.0 || !isfinite(alpha)) { status = ST_BREAKDOWN; break; }
+        for (int32_t i = 0; i < n; ++i) {
+            x[i] = fma(alpha, p[i], x[i]);
+            r[i] = fma(-alpha, q[i], r[i]);
+        }
+        res = sqrt(dot64(n, r, r, part));
+        ++it;
+        if (!isfinite(res)) { status = ST_BREAKDOWN; break; }
+        if (!(res > tol)) break;
+        if (it >= cfg->max_iter) { status = ST_NOT_CONVERGED; break; }
+        or_ilu_apply(A, lu, r, fw, z);
+        const double rzn = dot64(n, r, z, part);
+        const double beta = rzn / rz;
+        rz = rzn;
+        for (int32_t i = 0; i < n; ++i) p[i] = fma(beta, p[i], z[i]);
+    }
+    st->init_res_norm = res0;
+    st->final_res_norm = res;
+    st->num_iter = it;
+    st->num_outer = 0;
+    st->status = status;
+    free(r); free(p); free(q); free(z); free(fw); free(part);
+    return status;
+}
+
 int32_t or_solve(const or_csr* A, const double* values, const double* rhs, double* x,
                  const or_solver_cfg* cfg, or_solver_stats* stats) {
     g_red_rpt = red_rows_per_thread(A->n);
+    if (cfg->preconditioner == 2) {
+        if (cfg->precision != 0 || (cfg->method != 0 && cfg->method != 1)) {
+            stats->status = ST_UNSUPPORTED;
+            return ST_UNSUPPORTED;
+        }
+        double* lu = zalloc((size_t)A->nnz);
+        or_ilu_factor(A, values, lu);
+        const int32_t st = cfg->method == 1 ? solve_bicgstab(A, values, rhs, x, cfg, stats, lu)
+                                            : solve_cg_ilu(A, values, rhs, x, cfg, stats, lu);
+        free(lu);
+        return st;
+    }
     if (cfg->method == 2) {
         if (cfg->precision != 0) {
             stats->status = ST_UNSUPPORTED;
@@ -1258,7 +1376,7 @@ int32_t or_solve(const or_csr* A, const double* values, const double* rhs, doubl
     }
     if (cfg->method == 1) {
         if (cfg->precision == 1) return solve_mixed_bicgstab(A, values, rhs, x, cfg, stats);
-        return solve_bicgstab(A, values, rhs, x, cfg, stats);
+        return solve_bicgstab(A, values, rhs, x, cfg, stats, NULL);
     }
     if (cfg->precision == 1) return solve_mixed(A, values, rhs, x, cfg, stats);
     return solve_fp64(A, values, rhs, x, cfg, stats);

@@ -51,6 +51,8 @@ typedef struct or_solver_cfg {
     int32_t inner_max_iter, max_outer;
     int32_t method;      /* 0 CG, 1 BiCGStab (FP64 or mixed), 2 BiCG (FP64) */
     int32_t flags;       /* 2: rel_tol relative to ||b|| (Ginkgo ResidualNorm, baseline rhs_norm) */
+    int32_t preconditioner;  /* 0 Jacobi, 2 ILU(0) (CG or BiCGStab, FP64) */
+    int32_t pad;
 } or_solver_cfg;
 
 typedef struct or_solver_stats {
@@ -112,6 +114,11 @@ void or_apply_operator(const or_csr* A, const double* values, const double* rhs,
                        const double* x, double* out);
 
 double or_dot_tree(int32_t n, const double* a, const double* b);
+/* ILU(0) factors of A's pattern in CSR order (unit lower L below the diagonal,
+ * U on and above it), and z = U^-1 L^-1 r (y: the forward result). */
+void or_ilu_factor(const or_csr* A, const double* values, double* lu);
+void or_ilu_apply(const or_csr* A, const double* lu, const double* r, double* y, double* z);
+
 int32_t or_solve(const or_csr* A, const double* values, const double* rhs, double* x,
                  const or_solver_cfg* cfg, or_solver_stats* stats);
 

@@ -38,7 +38,7 @@ class OrTerm(C.Structure):
 class OrCfg(C.Structure):
     _fields_ = [("rel_tol", dbl), ("abs_tol", dbl), ("max_iter", i32), ("precision", i32),
                 ("inner_rel_tol", dbl), ("inner_max_iter", i32), ("max_outer", i32), ("method", i32),
-                ("flags", i32)]
+                ("flags", i32), ("preconditioner", i32), ("pad", i32)]
 
 
 class OrStats(C.Structure):
@@ -197,14 +197,26 @@ class Oracle:
         return out
 
     def solve(self, values, rhs, x, rel_tol=1e-8, abs_tol=0.0, max_iter=1000, precision=0,
-              inner_rel_tol=None, inner_max_iter=1000, max_outer=50, method=0, flags=0):
-        """flags & 2: rel_tol relative to ||b|| (Ginkgo ResidualNorm, baseline rhs_norm)."""
+              inner_rel_tol=None, inner_max_iter=1000, max_outer=50, method=0, flags=0, preconditioner=0):
+        """flags & 2: rel_tol relative to ||b|| (Ginkgo ResidualNorm, baseline rhs_norm);
+        preconditioner 2: ILU(0) (CG or BiCGStab, FP64)."""
         if inner_rel_tol is None:  # the host API's defaults: 0.1 for CG, 0.01 for BiCGStab
             inner_rel_tol = 0.01 if method == 1 else 0.1
-        cfg = OrCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer, method, flags)
+        cfg = OrCfg(rel_tol, abs_tol, max_iter, precision, inner_rel_tol, inner_max_iter, max_outer, method, flags,
+                    preconditioner, 0)
         st = OrStats()
         self.L.or_solve(C.byref(self.csr()), p(values), p(rhs), p(x), C.byref(cfg), C.byref(st))
         return st
+
+    def ilu_factor(self, values):
+        lu = np.zeros(len(values))
+        self.L.or_ilu_factor(C.byref(self.csr()), p(values), p(lu))
+        return lu
+
+    def ilu_apply(self, lu, r):
+        y, z = np.zeros(self.hm.n), np.zeros(self.hm.n)
+        self.L.or_ilu_apply(C.byref(self.csr()), p(lu), p(np.ascontiguousarray(r, float)), p(y), p(z))
+        return z
 
     # -------------------------------------------------------------------- PISO
     def rau_hbya(self, values, rhs, U):

@@ -80,9 +80,13 @@ int main(int argc, char** argv) {
         fvgb::SolverConfig bg =
             fvgb::solverConfig(fvgb::mapFvSolution(fvgb::Dictionary::parse("solver PBiCG; preconditioner DIC;")));
         REQUIRE(bg.bicg && bg.method() == FVGB_SOLVER_BICG);
-        bool threw = false;
-        try {  // DILU maps to Ginkgo's Ilu, which is not built
+        // DILU -> Ginkgo's Ilu with a ParIlu factorization: the ILU(0) preconditioner
+        fvgb::SolverConfig il =
             fvgb::solverConfig(fvgb::mapFvSolution(fvgb::Dictionary::parse("solver PBiCGStab; preconditioner DILU;")));
+        REQUIRE(il.ilu && il.bicgstab && !il.multigrid);
+        bool threw = false;
+        try {  // BiCG with ILU is not built
+            fvgb::solverConfig(fvgb::mapFvSolution(fvgb::Dictionary::parse("solver PBiCG; preconditioner DILU;")));
         } catch (const fvgb::Error& e) {
             threw = e.status == FVGB_ERR_UNSUPPORTED;
         }

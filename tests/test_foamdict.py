@@ -155,8 +155,15 @@ def test_solver_config_rejects_what_is_not_built(ref):
     adv = Dictionary.read(ref / "test/setup_advection/system/fvSolution")
     m = map_fv_solution(adv.subDict("solvers").subDict("T"))  # PBiCGStab + DILU
     assert m.subDict("preconditioner").get("type") == "preconditioner::Ilu"
+    c = solver_config(m)  # DILU -> Ilu/ParIlu: the ILU(0) preconditioner around BiCGStab
+    assert c["method"] == abi.SOLVER_BICGSTAB and c["preconditioner"] == abi.PRECOND_ILU
+    assert c["abs_tol"] == 1e-14 and c["rel_tol"] == 0.0
+    with pytest.raises(abi.FvgbError) as e:  # BiCG with ILU is not built
+        solver_config(map_fv_solution(Dictionary.parse("solver PBiCG; preconditioner DILU;")))
+    assert e.value.status == abi.ERR_UNSUPPORTED
     with pytest.raises(abi.FvgbError) as e:
-        solver_config(m)
+        solver_config(Dictionary.parse('solver Ginkgo; type "solver::Cg"; preconditioner { type '
+                                       '"preconditioner::Ilu"; reverse_apply true; }'))
     assert e.value.status == abi.ERR_UNSUPPORTED
     # GAMG maps to Ginkgo's solver::Multigrid as the solver, which is built; the
     # smoother entry is dropped and the DIC (Jacobi) preconditioner inserted
@@ -382,6 +389,11 @@ def test_ginkgo_json_configs(ref, tmp_path):
         ' {"type": "ResidualNorm", "reduction_factor": 1e-8, "baseline": "initial_resnorm"}]}')
     c = ginkgo_config(tmp_path / "mg.json")
     assert c["method"] == abi.SOLVER_MULTIGRID and c["max_iter"] == 60 and c["rel_tol"] == 1e-8
+    (tmp_path / "ilu.json").write_text(
+        '{"type": "solver::Bicgstab", "preconditioner": {"type": "preconditioner::Ilu", "reverse_apply": false,'
+        ' "factorization": {"type": "factorization::ParIlu"}}}')
+    c = ginkgo_config(tmp_path / "ilu.json")
+    assert c["method"] == abi.SOLVER_BICGSTAB and c["preconditioner"] == abi.PRECOND_ILU
     for text, status in (('{"type": "solver::Cg"', abi.ERR_INVALID_ARG),
                          ('{"type": "solver::Gmres", "preconditioner": {"type": "preconditioner::Jacobi", '
                           '"max_block_size": 1}}', abi.ERR_UNSUPPORTED),
