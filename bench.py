@@ -570,10 +570,11 @@ def run_convection(args):
                  neon.laplacian(neon.SurfaceField(dm, np.full(hm.nif + hm.nbf, 1e-3)), -1.0)], dt, T)
     out, sols = {}, {}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    runs = [("fp64", abi.PREC_FP64, 0.1)] + [(f"mixed_inner_{t:g}", abi.PREC_MIXED_IR, t)
-                                             for t in (0.1, 0.03, 1e-2, 1e-3)]
-    for name, prec, inner in runs:
-        cfg = abi.SolverCfg(1e-8, 0.0, 5000, prec, inner, 1000, 50, 0, 0, abi.SOLVER_BICGSTAB)
+    runs = [("fp64", abi.PREC_FP64, 0.1, abi.PRECOND_JACOBI)] + \
+        [(f"mixed_inner_{t:g}", abi.PREC_MIXED_IR, t, abi.PRECOND_JACOBI) for t in (0.1, 0.03, 1e-2, 1e-3)] + \
+        [("fp64_ilu", abi.PREC_FP64, 0.1, abi.PRECOND_ILU)]
+    for name, prec, inner, pc in runs:
+        cfg = abi.SolverCfg(1e-8, 0.0, 5000, prec, inner, 1000, 50, 0, 0, abi.SOLVER_BICGSTAB, pc)
         times = []
         for rep in range(4):                               # the first builds the graph
             x = T_old.clone()
