@@ -53,6 +53,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -74,57 +75,116 @@ struct HostCsr {
     std::vector<double> v;
 };
 
+// ------------------------------------------------------------ host threads
+// f(begin, end, chunk) over [0, n) in contiguous chunks on up to 16 threads
+// (one when n is small).  Every use below writes only its own rows, or
+// per-chunk results that are joined in chunk order: the results are those of
+// the sequential loop.
+template <class F>
+int parallel_chunks(int n, int min_per_chunk, F f) {
+    const int hw = (int)std::thread::hardware_concurrency();
+    const int nt = std::max(1, std::min({16, hw > 0 ? hw : 1, n / std::max(1, min_per_chunk)}));
+    if (nt == 1) {
+        f(0, n, 0);
+        return 1;
+    }
+    std::vector<std::thread> th;
+    th.reserve((size_t)nt);
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back(f, (int)((int64_t)n * t / nt), (int)((int64_t)n * (t + 1) / nt), t);
+    for (std::thread& x : th) x.join();
+    return nt;
+}
+
+// Ids next, next+1, ... for the rows with flag set, in row order (a prefix
+// sum over chunks); returns how many.
+int number_flagged(int n, const std::vector<char>& flag, std::vector<int>& id, int next) {
+    std::vector<int> cnt(16, 0), base(17, 0);
+    const int nt = parallel_chunks(n, 1 << 15, [&](int b, int e, int t) {
+        int c = 0;
+        for (int i = b; i < e; ++i) c += flag[i] ? 1 : 0;
+        cnt[t] = c;
+    });
+    for (int t = 0; t < nt; ++t) base[t + 1] = base[t] + cnt[t];
+    parallel_chunks(n, 1 << 15, [&](int b, int e, int t) {
+        int k = next + base[t];
+        for (int i = b; i < e; ++i)
+            if (flag[i]) id[i] = k++;
+    });
+    return base[nt];
+}
+
 // ------------------------------------------------------------ PGM (host)
 int pgm_aggregate(int n, const int* rp, const int* ci, const double* v, std::vector<int>& agg) {
     agg.assign(n, -1);
     std::vector<int> pick(n, -1);
     std::vector<int> tmp(n, -1);  // provisional aggregate id of each row
+    std::vector<int> id(n, -1);
+    std::vector<char> flag(n, 0);
     int next = 0, left = n;
     for (int round = 0; round < kPgmRounds; ++round) {
-        for (int i = 0; i < n; ++i) {
-            pick[i] = -1;
-            if (tmp[i] >= 0) continue;
-            double best = 0.0;
-            for (int k = rp[i]; k < rp[i + 1]; ++k) {
-                const int j = ci[k];
-                if (j == i || tmp[j] >= 0) continue;
-                const double w = std::fabs(v[k]);
-                if (w > best || (w == best && w > 0.0 && (pick[i] < 0 || j < pick[i]))) {
-                    best = w;
-                    pick[i] = j;
+        parallel_chunks(n, 1 << 15, [&](int b, int e, int) {
+            for (int i = b; i < e; ++i) {
+                pick[i] = -1;
+                if (tmp[i] >= 0) continue;
+                double best = 0.0;
+                for (int k = rp[i]; k < rp[i + 1]; ++k) {
+                    const int j = ci[k];
+                    if (j == i || tmp[j] >= 0) continue;
+                    const double w = std::fabs(v[k]);
+                    if (w > best || (w == best && w > 0.0 && (pick[i] < 0 || j < pick[i]))) {
+                        best = w;
+                        pick[i] = j;
+                    }
                 }
             }
-        }
-        int formed = 0;
-        for (int i = 0; i < n; ++i) {
-            const int j = pick[i];
-            if (tmp[i] < 0 && j > i && pick[j] == i) {
-                tmp[i] = tmp[j] = next++;
-                ++formed;
-                left -= 2;
+        });
+        // mutual picks pair up (pairs are disjoint); the lower row numbers the
+        // pair, pairs numbered in the order of their lower rows
+        parallel_chunks(n, 1 << 15, [&](int b, int e, int) {
+            for (int i = b; i < e; ++i) {
+                const int j = pick[i];
+                flag[i] = (tmp[i] < 0 && j > i && pick[j] == i) ? 1 : 0;
             }
-        }
+        });
+        const int formed = number_flagged(n, flag, id, next);
+        parallel_chunks(n, 1 << 15, [&](int b, int e, int) {
+            for (int i = b; i < e; ++i)
+                if (flag[i]) tmp[i] = tmp[pick[i]] = id[i];
+        });
+        next += formed;
+        left -= 2 * formed;
         if (formed == 0 || left <= kPgmLeftRatio * n) break;
     }
     // rows left over: the strongest aggregated neighbour's aggregate, else alone
     std::vector<int> late(n, -1);
-    for (int i = 0; i < n; ++i) {
-        if (tmp[i] >= 0) continue;
-        double best = 0.0;
-        int to = -1;
-        for (int k = rp[i]; k < rp[i + 1]; ++k) {
-            const int j = ci[k];
-            if (j == i || tmp[j] < 0) continue;
-            const double w = std::fabs(v[k]);
-            if (w > best || (w == best && w > 0.0 && (to < 0 || j < to))) {
-                best = w;
-                to = j;
+    parallel_chunks(n, 1 << 15, [&](int b, int e, int) {
+        for (int i = b; i < e; ++i) {
+            if (tmp[i] >= 0) continue;
+            double best = 0.0;
+            int to = -1;
+            for (int k = rp[i]; k < rp[i + 1]; ++k) {
+                const int j = ci[k];
+                if (j == i || tmp[j] < 0) continue;
+                const double w = std::fabs(v[k]);
+                if (w > best || (w == best && w > 0.0 && (to < 0 || j < to))) {
+                    best = w;
+                    to = j;
+                }
             }
+            late[i] = to >= 0 ? tmp[to] : -1;
+            flag[i] = late[i] < 0 ? 1 : 0;
         }
-        late[i] = to >= 0 ? tmp[to] : -1;
-    }
-    for (int i = 0; i < n; ++i)
-        if (tmp[i] < 0) tmp[i] = late[i] >= 0 ? late[i] : next++;
+    });
+    parallel_chunks(n, 1 << 15, [&](int b, int e, int) {
+        for (int i = b; i < e; ++i)
+            if (tmp[i] >= 0) flag[i] = 0;
+    });
+    next += number_flagged(n, flag, id, next);  // rows alone
+    parallel_chunks(n, 1 << 15, [&](int b, int e, int) {
+        for (int i = b; i < e; ++i)
+            if (tmp[i] < 0) tmp[i] = late[i] >= 0 ? late[i] : id[i];
+    });
     // number the aggregates by their lowest row
     std::vector<int> renum(next, -1);
     int nc = 0;
@@ -147,6 +207,44 @@ void galerkin(const HostCsr& A, const std::vector<int>& agg, int nc, HostCsr& Ac
         std::vector<int> fill(mptr.begin(), mptr.end() - 1);
         for (int i = 0; i < A.n; ++i) mem[fill[agg[i]]++] = i;  // ascending within an aggregate
     }
+    // coarse rows in chunks, each chunk's rows built apart, then joined in order
+    struct Part {
+        std::vector<int> rlen, ci, glen, gsrc;
+        std::vector<double> v;
+    };
+    std::vector<Part> parts(16);
+    const int nt = parallel_chunks(nc, 4096, [&](int cb, int ce, int t) {
+        Part& P = parts[t];
+        std::vector<std::pair<int, int>> items;  // (coarse column, fine entry) in summation order
+        for (int c = cb; c < ce; ++c) {
+            items.clear();
+            for (int m = mptr[c]; m < mptr[c + 1]; ++m) {
+                const int i = mem[m];
+                for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) items.emplace_back(agg[A.ci[k]], k);
+            }
+            std::stable_sort(items.begin(), items.end(), [](const std::pair<int, int>& a, const std::pair<int, int>& b) {
+                return a.first < b.first;
+            });
+            int len = 0;
+            size_t s = 0;
+            while (s < items.size()) {
+                const int col = items[s].first;
+                double sum = 0.0;
+                size_t e = s;
+                while (e < items.size() && items[e].first == col) {
+                    sum += A.v[items[e].second];
+                    P.gsrc.push_back(items[e].second);
+                    ++e;
+                }
+                P.ci.push_back(col);
+                P.v.push_back(sum);
+                P.glen.push_back((int)(e - s));
+                ++len;
+                s = e;
+            }
+            P.rlen.push_back(len);
+        }
+    });
     Ac.n = nc;
     Ac.rp.assign(nc + 1, 0);
     Ac.ci.clear();
@@ -154,31 +252,17 @@ void galerkin(const HostCsr& A, const std::vector<int>& agg, int nc, HostCsr& Ac
     gptr.assign(1, 0);
     gsrc.clear();
     gsrc.reserve(A.ci.size());
-    std::vector<std::pair<int, int>> items;  // (coarse column, fine entry) in summation order
-    for (int c = 0; c < nc; ++c) {
-        items.clear();
-        for (int m = mptr[c]; m < mptr[c + 1]; ++m) {
-            const int i = mem[m];
-            for (int k = A.rp[i]; k < A.rp[i + 1]; ++k) items.emplace_back(agg[A.ci[k]], k);
+    int c = 0;
+    for (int t = 0; t < nt; ++t) {
+        const Part& P = parts[t];
+        for (int len : P.rlen) {
+            Ac.rp[c + 1] = Ac.rp[c] + len;
+            ++c;
         }
-        std::stable_sort(items.begin(), items.end(),
-                         [](const std::pair<int, int>& a, const std::pair<int, int>& b) { return a.first < b.first; });
-        size_t s = 0;
-        while (s < items.size()) {
-            const int col = items[s].first;
-            double sum = 0.0;
-            size_t e = s;
-            while (e < items.size() && items[e].first == col) {
-                sum += A.v[items[e].second];
-                gsrc.push_back(items[e].second);
-                ++e;
-            }
-            Ac.ci.push_back(col);
-            Ac.v.push_back(sum);
-            gptr.push_back((int)gsrc.size());
-            s = e;
-        }
-        Ac.rp[c + 1] = (int)Ac.ci.size();
+        Ac.ci.insert(Ac.ci.end(), P.ci.begin(), P.ci.end());
+        Ac.v.insert(Ac.v.end(), P.v.begin(), P.v.end());
+        for (int g : P.glen) gptr.push_back(gptr.back() + g);
+        gsrc.insert(gsrc.end(), P.gsrc.begin(), P.gsrc.end());
     }
 }
 

@@ -51,6 +51,20 @@ def test_pgm_aggregation_matches_restatement(dims):
     assert np.all(np.diff(first) > 0)
 
 
+def test_pgm_aggregation_threaded_matches_restatement():
+    """73,728 rows: the host aggregation runs on several threads (chunks of
+    at least 2^15 rows) and must give the sequential restatement's aggregates."""
+    _, _, _, _, _, _, _, v, _, ro, col = heat_system(48, 48, 32)
+    n = len(ro) - 1
+    agg = np.zeros(n, np.int32)
+    nc = C.c_int32()
+    abi.check(abi.lib().fvgb_pgm_aggregate(n, ro.ctypes.data, col.ctypes.data, v.ctypes.data, agg.ctypes.data,
+                                           C.byref(nc)))
+    want, want_nc = oamg.pgm_aggregate(n, ro, col, v)
+    assert nc.value == want_nc
+    np.testing.assert_array_equal(agg, want)
+
+
 def test_pgm_edge_cases():
     L = abi.lib()
     nc = C.c_int32()
@@ -142,6 +156,28 @@ def test_vcycle_matches_restatement(cuda):
     nnz = np.zeros(32, np.int64)
     abi.check(abi.lib().fvgb_amg_info(s["ls"].handle, C.byref(nl), rows.ctypes.data, nnz.ctypes.data, 32))
     assert nl.value == len(levels)
+    assert list(rows[:nl.value]) == [lv[0].shape[0] for lv in levels]
+    assert list(nnz[:nl.value]) == [lv[0].nnz for lv in levels]
+
+
+@pytest.mark.gpu
+def test_threaded_hierarchy_matches_restatement(cuda):
+    """A system large enough for the host setup's threads (aggregation and
+    Galerkin products in chunks): level sizes, nonzeros and the V-cycle as the
+    sequential restatement."""
+    s = gpu_system(cuda, (48, 48, 32))
+    torch = s["torch"]
+    levels = oamg.hierarchy(s["ro"], s["col"], s["v"])
+    r = np.random.default_rng(8).standard_normal(s["hm"].n)
+    rd = torch.tensor(r, dtype=torch.float64, device="cuda")
+    zd = torch.zeros_like(rd)
+    abi.check(abi.lib().fvgb_amg_apply(s["ls"].handle, abi.ptr(rd), abi.ptr(zd), None))
+    want = oamg.vcycle(levels, r)
+    assert np.linalg.norm(zd.cpu().numpy() - want) <= 1e-10 * np.linalg.norm(want)
+    nl = C.c_int32()
+    rows = np.zeros(32, np.int32)
+    nnz = np.zeros(32, np.int64)
+    abi.check(abi.lib().fvgb_amg_info(s["ls"].handle, C.byref(nl), rows.ctypes.data, nnz.ctypes.data, 32))
     assert list(rows[:nl.value]) == [lv[0].shape[0] for lv in levels]
     assert list(nnz[:nl.value]) == [lv[0].nnz for lv in levels]
 

@@ -355,6 +355,50 @@ def test_pde_solver_configured_by_fv_solution(cuda, ref):
     torch.cuda.synchronize()
 
 
+@pytest.mark.gpu
+def test_pde_solver_configured_by_dilu_entry(cuda, ref):
+    """The reference's test/setup_advection fvSolution (T: PBiCGStab, DILU,
+    tolerance 1e-14, relTol 0) on an implicit upwind convection-diffusion step:
+    BiCGStab with the ILU(0) preconditioner, the same iterations and bits as the
+    explicit configuration it maps to and as the oracle's restatement."""
+    import numpy as np
+    import torch
+
+    from foamadapter_gb300 import mesh, neon
+    from foamadapter_gb300.mesh import DeviceMesh
+    from oracle.pyoracle import Oracle
+
+    fv = Dictionary.read(ref / "test/setup_advection/system/fvSolution")
+    hm = mesh.box(16, 12, 10, jitter=0.1, seed=3)
+    dm = DeviceMesh(hm)
+    o = Oracle(hm)
+    U = np.array([1.0, 0.4, -0.2])
+    F = neon.SurfaceField(dm, o.flux_vec(np.tile(U, hm.n), np.tile(U, hm.nbf)))
+    nu = neon.SurfaceField(dm, np.full(hm.nif + hm.nbf, 1e-3))
+    bcs = [("fixedValue", 1.0)] + [("zeroGradient", 0.0)] * (hm.npatch - 1)
+    T0 = np.random.default_rng(3).random(hm.n)
+    results = []
+    for how in ("dict", "kwargs"):
+        T = neon.VolumeField(dm, T0, bcs, name="T")
+        old = T.internal.clone()
+        eqn = neon.PDESolver([neon.ddt(old), neon.div(F, "upwind"), neon.laplacian(nu, -1.0)], T, 0.05)
+        if how == "dict":
+            st = eqn.solve(fvSolution=fv)
+        else:
+            st = eqn.solve(rel_tol=0.0, abs_tol=1e-14, max_iter=1000, method=abi.SOLVER_BICGSTAB,
+                           preconditioner=abi.PRECOND_ILU)
+        assert st.status == abi.OK and st.num_iter > 1
+        results.append((st.num_iter, st.final_res_norm, T.internal.cpu().numpy().copy()))
+    assert results[0][:2] == results[1][:2]
+    assert np.array_equal(results[0][2], results[1][2])
+    v, r, _, _ = [t.cpu().numpy() for t in eqn.ls.export()]
+    xo = old.cpu().numpy().copy()
+    so = o.solve(v, r, xo, rel_tol=0.0, abs_tol=1e-14, max_iter=1000, method=1, preconditioner=2)
+    assert (so.status, so.num_iter, so.final_res_norm) == (0, results[1][0], results[1][1])
+    assert np.array_equal(xo, results[1][2])
+    torch.cuda.synchronize()
+
+
 def test_ginkgo_json_configs(ref, tmp_path):
     """The reference's own Ginkgo configurations (tutorials/cylinder2D/system/gko)."""
     from foamadapter_gb300.dictionary import ginkgo_config
