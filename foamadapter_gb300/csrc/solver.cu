@@ -190,14 +190,51 @@ __device__ __forceinline__ void slot_cols(const MeshView& m, int base, int w, in
     }
 }
 
+// s = sum of v[k] x[k], k < W, as an fma chain from +0 in k order
+template <int W>
+__device__ __forceinline__ double fma_chain(const double* v, const double* x) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < W; ++k) s = fma(v[k], x[k], s);
+    return s;
+}
+
 // Row sum of a sliced-ELL row, fma chain in slot (= column) order.  The slot
 // loads of the first 8 slots are issued before the dependent gathers.
+// The row of a W-slot slice: every slot real or padding (value 0, column =
+// row), exactly W fmas from +0.
+template <int W>
+__device__ __forceinline__ double spmv_row_w(const MeshView& m, const double* __restrict__ val,
+                                             const double* __restrict__ x, int base, int i) {
+    int col[W];
+    if (m.m_off) {
+#pragma unroll
+        for (int k = 0; k < W; ++k) col[k] = i + (int)__ldg(&m.m_off[base + k * 32]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < W; ++k) col[k] = __ldg(&m.m_col[base + k * 32]);
+    }
+    double v[W], xv[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        v[k] = __ldg(&val[base + k * 32]);
+        xv[k] = __ldg(&x[col[k]]);
+    }
+    return fma_chain<W>(v, xv);
+}
+
 __device__ __forceinline__ double spmv_row(const MeshView& m, const double* __restrict__ val,
                                            const double* __restrict__ x, int i) {
     const int slice = i >> 5, lane = i & 31;
     const int b0 = __ldg(&m.m_ptr[slice]);
     const int base = b0 + lane;
     const int w = (__ldg(&m.m_ptr[slice + 1]) - b0) >> 5;
+    // A chain predicated on k < w over 8 slots is compiled as 8 unconditional
+    // fmas (fma(0, 0, s) == s for the chain's s, which is never -0): one wasted
+    // DFMA per row of a 7-slot stencil (3-D hex meshes).  Slices of width 7
+    // take an exact 7-fma path (w is the same for the whole slice, so the
+    // branch is uniform); the bits are the same either way.
+    if (w == 7) return spmv_row_w<7>(m, val, x, base, i);
     int col[8];
     slot_cols(m, base, w, i, col);
     double v[8], xv[8];
