@@ -905,7 +905,9 @@ def run_serve(args):
         failed = [{"request": k, "status": x.status, "steps_done": x.steps_done, "cells": sample[k][1:4],
                    "steps": sample[k][4], "D": sample[k][6], "U": float(np.linalg.norm(sample[k][5]))}
                   for k, x in enumerate(r) if x.status != 0]
+        cell_steps = int(sum(x[1] * x[2] * x[3] * x[4] for x in sample))
         return {"requests": len(r), "wall_s": wall, "solves_per_s": len(r) / wall,
+                "cell_steps_per_s": cell_steps / wall,
                 "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
                 "all_ok": not failed, "failed": failed[:8], "n_failed": len(failed),
                 "peak_device_GB": info[4] / 1e9, "ticks": int(info[5]),
@@ -933,9 +935,12 @@ def run_serve(args):
            "served_fp64": served, "served_mixed": served_mixed, "sequential_plain_launches_fp64": plain,
            "sequential_best_fp64": best}
     out["solves_per_s_ratio_vs_plain"] = served["solves_per_s"] / plain["solves_per_s"]
+    # the same per unit of work (cell-steps/s): not biased by how heavy the sequential sample is
+    out["work_ratio_vs_plain"] = served["cell_steps_per_s"] / plain["cell_steps_per_s"]
     out["solves_per_s_ratio_vs_best_sequential"] = served["solves_per_s"] / best["solves_per_s"]
     if served_mixed:
         out["mixed_solves_per_s_ratio_vs_plain"] = served_mixed["solves_per_s"] / plain["solves_per_s"]
+        out["mixed_work_ratio_vs_plain"] = served_mixed["cell_steps_per_s"] / plain["cell_steps_per_s"]
     if seq_n != len(reqs):
         out["note"] = (f"the sequential runs time the first {seq_n} requests (same distribution); the ratios "
                        "compare solves/s")

@@ -279,10 +279,12 @@ extern "C" fvgb_status fvgb_ls_create(const fvgb_mesh* mesh, int32_t ncomp, fvgb
     ls->mesh = mesh;
     ls->ncomp = ncomp;
     const int64_t n = mesh->v.n, nbf = mesh->v.nbf;
-    cudaError_t e = cudaMalloc(&ls->values, sizeof(double) * (size_t)mesh->m_len);
-    if (e == cudaSuccess) e = cudaMalloc(&ls->rhs, sizeof(double) * (size_t)(n * ncomp));
-    if (e == cudaSuccess) e = cudaMalloc(&ls->bmat, sizeof(double) * (size_t)(nbf > 0 ? nbf : 1));
-    if (e == cudaSuccess) e = cudaMalloc(&ls->brhs, sizeof(double) * (size_t)(nbf > 0 ? nbf * ncomp : 1));
+    ls->pooled = devmem_pooled_now();
+    cudaError_t e = devmem_alloc((void**)&ls->values, sizeof(double) * (size_t)mesh->m_len, ls->pooled);
+    if (e == cudaSuccess) e = devmem_alloc((void**)&ls->rhs, sizeof(double) * (size_t)(n * ncomp), ls->pooled);
+    if (e == cudaSuccess) e = devmem_alloc((void**)&ls->bmat, sizeof(double) * (size_t)(nbf > 0 ? nbf : 1), ls->pooled);
+    if (e == cudaSuccess)
+        e = devmem_alloc((void**)&ls->brhs, sizeof(double) * (size_t)(nbf > 0 ? nbf * ncomp : 1), ls->pooled);
     if (e == cudaSuccess) e = cudaMemset(ls->values, 0, sizeof(double) * (size_t)mesh->m_len);
     if (e == cudaSuccess) e = cudaMemset(ls->rhs, 0, sizeof(double) * (size_t)(n * ncomp));
     if (e == cudaSuccess) e = cudaMemset(ls->bmat, 0, sizeof(double) * (size_t)(nbf > 0 ? nbf : 1));
@@ -300,14 +302,16 @@ void fvgb_solver_cache_free(SolverCache* c);  // solver.cu
 
 extern "C" fvgb_status fvgb_ls_destroy(fvgb_ls* ls) {
     if (!ls) return FVGB_OK;
-    cudaDeviceSynchronize();
+    // work in flight may still read the system: wait for it, unless its memory
+    // is pooled (then freed in order on the release stream of the thread's context)
+    if (!ls->pooled) cudaDeviceSynchronize();
     if (ls->solver) fvgb_solver_cache_free(ls->solver);
     if (ls->amg) fvgb_amg_free(ls->amg);
     if (ls->ilu) fvgb_ilu_free(ls->ilu);
-    cudaFree(ls->values);
-    cudaFree(ls->rhs);
-    cudaFree(ls->bmat);
-    cudaFree(ls->brhs);
+    devmem_free(ls->values, ls->pooled);
+    devmem_free(ls->rhs, ls->pooled);
+    devmem_free(ls->bmat, ls->pooled);
+    devmem_free(ls->brhs, ls->pooled);
     delete ls;
     return FVGB_OK;
 }

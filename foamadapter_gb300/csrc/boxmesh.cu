@@ -371,7 +371,7 @@ __global__ void k_fill_ptr(int32_t* p, int count, int width) {
 }
 
 void free_mesh_partial(fvgb_mesh* m) {
-    for (void* p : m->allocs) cudaFree(p);
+    for (void* p : m->allocs) devmem_free(p, m->pooled);
     delete m;
 }
 
@@ -435,6 +435,7 @@ extern "C" fvgb_status fvgb_mesh_create_boxes(const fvgb_box_spec* specs, int32_
         for (int32_t sl = boxes[q].cell0 / 32; sl < (boxes[q].cell0 + boxes[q].n + 31) / 32; ++sl) slice_box[sl] = q;
 
     fvgb_mesh* m = new fvgb_mesh();
+    m->pooled = devmem_pooled_now();
     m->h_patch_offs = poffs;
     m->nnz = (int32_t)(N + 2 * NIF);
     m->nslices = nslices;

@@ -82,6 +82,38 @@ __device__ __forceinline__ double facc(const MeshView& m, double s, bool plus, d
     return __fma_rn(x, plus ? m.k_one : m.k_mone, s);
 }
 
+// ---- device memory of served requests
+// Objects (meshes, linear systems, solver workspaces) created while the calling
+// thread has a memory pool set take all their device memory from that pool
+// (cudaMallocFromPoolAsync ordered on the context's allocation stream, waited
+// for at once) and release it with cudaFreeAsync on the context's release
+// stream, so releasing them never synchronises the device as cudaFree does.
+// The serving loop sets the context on its thread; everything else uses
+// cudaMalloc and cudaFree.  An object keeps the mode it was created in.
+struct DevMemCtx {
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t alloc = nullptr;    // private stream of the allocations
+    cudaStream_t release = nullptr;  // stream whose work last used what is released
+};
+inline DevMemCtx& devmem_ctx() {
+    static thread_local DevMemCtx c;
+    return c;
+}
+inline bool devmem_pooled_now() { return devmem_ctx().pool != nullptr; }
+inline cudaError_t devmem_alloc(void** p, size_t bytes, bool pooled) {
+    if (!pooled) return cudaMalloc(p, bytes);
+    const DevMemCtx& c = devmem_ctx();
+    if (!c.pool) return cudaErrorInvalidValue;  // a pooled object grows only on the thread that owns the pool
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, c.pool, c.alloc);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.alloc);
+    return e;
+}
+inline void devmem_free(void* p, bool pooled) {
+    if (!p) return;
+    if (pooled) cudaFreeAsync(p, devmem_ctx().release);
+    else cudaFree(p);
+}
+
 struct fvgb_mesh {
     MeshView v{};
     int32_t nnz = 0;
@@ -92,6 +124,7 @@ struct fvgb_mesh {
     std::vector<int32_t> h_row_offs, h_col, h_diag_off, h_own_off, h_nei_off;
     std::vector<void*> allocs;
     int64_t bytes = 0;
+    bool pooled = false;  // device memory from the serving pool (devmem_*)
 };
 
 struct SolverCache;  // solver.cu
@@ -109,6 +142,7 @@ struct fvgb_ls {
     AmgCache* amg = nullptr;   // multigrid hierarchy (amg.cu), built at the first multigrid solve
     IluCache* ilu = nullptr;   // ILU(0) pattern data and graphs (ilu.cu), built at the first ILU solve
     uint64_t version = 1;      // bumped whenever `values` change (assembly, SetReference)
+    bool pooled = false;       // device memory from the serving pool (devmem_*)
 };
 
 // amg.cu: multigrid-preconditioned CG (cfg->preconditioner == FVGB_PRECOND_MULTIGRID)
@@ -192,7 +226,7 @@ inline bool patch_table_needs_ref(const PatchTable& t) {
 template <class T>
 inline cudaError_t mesh_alloc(fvgb_mesh* m, T** p, int64_t count) {
     size_t bytes = sizeof(T) * (size_t)(count > 0 ? count : 1);
-    cudaError_t e = cudaMalloc((void**)p, bytes);
+    cudaError_t e = devmem_alloc((void**)p, bytes, m->pooled);
     if (e == cudaSuccess) {
         m->allocs.push_back(*p);
         m->bytes += (int64_t)bytes;

@@ -53,7 +53,7 @@ __global__ void k_bc_correct(MeshView m, PatchTable pt, int ncomp, const double*
 
 void free_mesh(fvgb_mesh* m) {
     if (!m) return;
-    for (void* p : m->allocs) cudaFree(p);
+    for (void* p : m->allocs) devmem_free(p, m->pooled);
     delete m;
 }
 
@@ -113,6 +113,7 @@ extern "C" fvgb_status fvgb_mesh_create(const fvgb_mesh_desc* d, fvgb_mesh** out
     }
 
     fvgb_mesh* m = new fvgb_mesh();
+    m->pooled = devmem_pooled_now();
     m->h_patch_offs.assign(d->patch_offsets, d->patch_offsets + np + 1);
     if (np == 0) m->h_patch_offs.assign(1, 0);
 
@@ -317,7 +318,9 @@ extern "C" fvgb_status fvgb_mesh_create(const fvgb_mesh_desc* d, fvgb_mesh** out
 
 extern "C" fvgb_status fvgb_mesh_destroy(fvgb_mesh* mesh) {
     if (mesh) {
-        cudaDeviceSynchronize();
+        // work in flight may still read the mesh: wait for it, unless its memory
+        // is pooled (then freed in order on the release stream of the thread's context)
+        if (!mesh->pooled) cudaDeviceSynchronize();
         free_mesh(mesh);
     }
     return FVGB_OK;

@@ -11,8 +11,11 @@
 // previous chunk finished, retires finished requests (copying the result to the
 // caller's host buffer) and admits waiting ones as budget frees up, so requests
 // of very different sizes progress at their own pace and their work overlaps
-// on the GPU.  Device memory of retired requests is released in batches (one
-// device synchronisation per batch, not per request).  Each request runs
+// on the GPU.  A request's device memory comes from the server's memory pool
+// and goes back to it, in stream order on the request's stream, as soon as its
+// result is reported: cudaFree and cudaFreeHost synchronise the whole device,
+// and under a saturated stream their flushes idled the GPU for about a second
+// every thousand requests.  Each request runs
 // exactly the computation it would run alone, so its result does not depend
 // on the mix.
 //
@@ -34,6 +37,7 @@
 
 #include "fvgb.h"
 #include "fvgb_host_common.h"
+#include "internal.cuh"
 
 namespace {
 
@@ -84,7 +88,9 @@ struct fvgb_server {
     int device = 0;
     Clock::time_point t0;
     std::vector<Slot*> retiring;            // result copy enqueued, waiting for its event
-    std::vector<Slot*> graveyard;           // retired, memory not yet released
+    std::vector<fvgb_solver_stats*> free_stats;  // pinned stats buffers of retired requests, reused
+    cudaMemPool_t pool = nullptr;           // device memory of the requests (devmem_*)
+    cudaStream_t alloc_stream = nullptr;    // the pool's allocation stream
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
@@ -104,12 +110,16 @@ int64_t estimate_bytes(const fvgb_serve_request& r) {
     return mesh + system + solver + fields + (1 << 20);
 }
 
-void release(Slot* s) {
+// Device memory of a request comes from the server's pool (set on the loop's
+// thread, devmem_*) and is released in stream order on the request's stream:
+// no device synchronisation.  Its pinned stats buffer goes back to the server's
+// free list (cudaFreeHost would synchronise the device).
+void release(fvgb_server* sv, Slot* s) {
+    devmem_ctx().release = s->stream;
     double* bufs[] = {s->T, s->Told, s->Tb, s->F, s->gamma, s->ref, s->U, s->Ub};
-    for (double* b : bufs)
-        if (b) cudaFree(b);
-    if (s->stats_dev) cudaFree(s->stats_dev);
-    if (s->stats_host) cudaFreeHost(s->stats_host);
+    for (double* b : bufs) devmem_free(b, true);
+    devmem_free(s->stats_dev, true);
+    if (s->stats_host) sv->free_stats.push_back(s->stats_host);
     if (s->done_ev) cudaEventDestroy(s->done_ev);
     s->stats_host = nullptr;
     s->done_ev = nullptr;
@@ -119,6 +129,7 @@ void release(Slot* s) {
     s->stats_dev = nullptr;
     s->ls = nullptr;
     s->mesh = nullptr;
+    devmem_ctx().release = nullptr;
 }
 
 __global__ void k_blob(double* T, int nx, int ny, int nz, int cell0) {
@@ -158,7 +169,7 @@ fvgb_status setup(fvgb_server* sv, Slot* s) {
     const size_t n = (size_t)s->n, nbf = (size_t)s->nbf, nf = (size_t)(s->nif + s->nbf);
     cudaError_t e = cudaSuccess;
     auto A = [&](double** p, size_t count) {
-        if (e == cudaSuccess) e = cudaMalloc(p, sizeof(double) * (count ? count : 1));
+        if (e == cudaSuccess) e = devmem_alloc((void**)p, sizeof(double) * (count ? count : 1), true);
     };
     A(&s->T, n);
     if (r.flags & FVGB_SERVE_REASSEMBLE) A(&s->Told, n);
@@ -168,8 +179,15 @@ fvgb_status setup(fvgb_server* sv, Slot* s) {
     A(&s->ref, nbf);
     A(&s->U, 3 * n);
     A(&s->Ub, 3 * nbf);
-    if (e == cudaSuccess) e = cudaMalloc(&s->stats_dev, sizeof(fvgb_solver_stats) * kChunk);
-    if (e == cudaSuccess) e = cudaMallocHost(&s->stats_host, sizeof(fvgb_solver_stats) * kChunk);
+    if (e == cudaSuccess) e = devmem_alloc((void**)&s->stats_dev, sizeof(fvgb_solver_stats) * kChunk, true);
+    if (e == cudaSuccess) {
+        if (!sv->free_stats.empty()) {
+            s->stats_host = sv->free_stats.back();
+            sv->free_stats.pop_back();
+        } else {
+            e = cudaMallocHost(&s->stats_host, sizeof(fvgb_solver_stats) * kChunk);
+        }
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->done_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return fvgb_fail(FVGB_ERR_OOM, "server: request allocation");
     const int nn = s->n, rn = r.nx * r.ny * r.nz;
@@ -261,31 +279,53 @@ void report(fvgb_server* sv, Slot* s) {
     res.start_s = s->start_s;
     res.finish_s = sv->now();
     res.device_bytes = s->bytes;
-    sv->graveyard.push_back(s);  // device memory released in a batch (release_graveyard)
+    // the request's work has completed (its event): its memory goes back to
+    // the pool now, and its budget with it
+    release(sv, s);
+    const int64_t bytes = s->bytes;
+    delete s;
     std::lock_guard<std::mutex> lk(sv->mu);
+    sv->used -= bytes;
     sv->done.push_back(res);
 }
 
-// Releasing device memory synchronises the device (cudaFree), which would stall
-// every request's queued work: it is done only when the loop is idle or when the
-// next waiting request needs budget that retired requests still hold, one
-// synchronisation for all of them.
-void release_graveyard(fvgb_server* sv, bool force) {
-    if (sv->graveyard.empty() || !force) return;
-    cudaDeviceSynchronize();
-    int64_t freed = 0;
-    for (Slot* s : sv->graveyard) {
-        release(s);
-        freed += s->bytes;
-        delete s;
+// The requests' device memory pool: kept across releases (no release
+// threshold), and reused only once a release has executed, never by making a
+// later allocation wait on another request's stream.
+void open_pool(fvgb_server* sv) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = sv->device;
+    if (cudaMemPoolCreate(&sv->pool, &props) != cudaSuccess) {
+        cudaGetLastError();
+        sv->pool = nullptr;
+        cudaDeviceGetDefaultMemPool(&sv->pool, sv->device);
     }
-    sv->graveyard.clear();
-    std::lock_guard<std::mutex> lk(sv->mu);
-    sv->used -= freed;
+    uint64_t keep = ~0ull;
+    int no = 0;
+    cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    cudaMemPoolSetAttribute(sv->pool, cudaMemPoolReuseAllowInternalDependencies, &no);
+    cudaStreamCreateWithFlags(&sv->alloc_stream, cudaStreamNonBlocking);
+    devmem_ctx() = DevMemCtx{sv->pool, sv->alloc_stream, nullptr};
+}
+
+void close_pool(fvgb_server* sv) {
+    cudaDeviceSynchronize();  // every release has executed
+    for (fvgb_solver_stats* p : sv->free_stats) cudaFreeHost(p);
+    sv->free_stats.clear();
+    cudaMemPool_t dflt = nullptr;
+    cudaDeviceGetDefaultMemPool(&dflt, sv->device);
+    if (sv->pool && sv->pool != dflt) cudaMemPoolDestroy(sv->pool);
+    if (sv->alloc_stream) cudaStreamDestroy(sv->alloc_stream);
+    sv->pool = nullptr;
+    sv->alloc_stream = nullptr;
+    devmem_ctx() = DevMemCtx{};
 }
 
 void run(fvgb_server* sv) {
     cudaSetDevice(sv->device);
+    open_pool(sv);
     size_t next_stream = 0;
     for (;;) {
         std::vector<Slot*> admit;
@@ -395,18 +435,9 @@ void run(fvgb_server* sv) {
         }
         sv->active.swap(keep);
         ++sv->ticks;
-        bool flush;
-        {
-            // release now if nothing runs, or if the next waiting request is held back
-            // by budget that retired requests still hold
-            std::lock_guard<std::mutex> lk(sv->mu);
-            flush = (sv->active.empty() && sv->retiring.empty()) ||
-                    (!sv->waiting.empty() && sv->used + sv->waiting.front()->bytes > sv->cfg.budget_bytes);
-        }
-        release_graveyard(sv, flush);
         if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
-    release_graveyard(sv, true);
+    close_pool(sv);
 }
 
 }  // namespace

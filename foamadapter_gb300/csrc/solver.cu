@@ -39,6 +39,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 
 namespace {
@@ -2447,6 +2448,7 @@ struct SolverCache {
     bool whole = false;  // one case covering rows [0, n): the persistent kernels' assumption
     Layout L{};
     std::vector<void*> allocs;
+    bool pooled = false;  // device memory from the serving pool (devmem_*)
     double *dinv = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *pa = nullptr, *pb = nullptr;
     double* pc = nullptr;
     float *ah = nullptr, *dinvf = nullptr, *ev = nullptr, *rh = nullptr, *y = nullptr, *pf = nullptr,
@@ -2484,8 +2486,11 @@ void fvgb_solver_cache_free(SolverCache* c) {
     if (c->gbi) cudaGraphExecDestroy(c->gbi);
     if (c->gmb) cudaGraphExecDestroy(c->gmb);
     if (c->gbg) cudaGraphExecDestroy(c->gbg);
-    for (void* p : c->allocs) cudaFree(p);
-    if (c->h_stats) cudaFreeHost(c->h_stats);
+    for (void* p : c->allocs) devmem_free(p, c->pooled);
+    if (c->h_stats) {
+        if (c->pooled) std::free(c->h_stats);  // cudaFreeHost would synchronise the device
+        else cudaFreeHost(c->h_stats);
+    }
     if (c->h_active) cudaFreeHost(c->h_active);
     delete c;
 }
@@ -2494,7 +2499,7 @@ namespace {
 
 template <class T>
 cudaError_t calloc_dev(SolverCache* c, T** p, size_t count) {
-    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+    cudaError_t e = devmem_alloc((void**)p, sizeof(T) * (count ? count : 1), c->pooled);
     if (e == cudaSuccess) {
         c->allocs.push_back(*p);
         e = cudaMemset(*p, 0, sizeof(T) * (count ? count : 1));
@@ -2505,6 +2510,7 @@ cudaError_t calloc_dev(SolverCache* c, T** p, size_t count) {
 // ranges: [2*ncases] begin/end rows of every case, validated by the caller
 fvgb_status cache_create(const fvgb_ls* ls, int ncases, const int32_t* ranges, SolverCache** out) {
     SolverCache* c = new SolverCache();
+    c->pooled = devmem_pooled_now();
     c->ls = ls;
     c->n = ls->mesh->v.n;
     c->ncases = ncases;
@@ -2544,7 +2550,14 @@ fvgb_status cache_create(const fvgb_ls* ls, int ncases, const int32_t* ranges, S
     if (e == cudaSuccess) e = calloc_dev(c, &c->pa, (size_t)c->nb);
     if (e == cudaSuccess) e = calloc_dev(c, &c->pb, (size_t)c->nb);
     if (e == cudaSuccess) e = calloc_dev(c, &c->pc, (size_t)c->nb);
-    if (e == cudaSuccess) e = cudaMallocHost(&c->h_stats, sizeof(fvgb_solver_stats) * (size_t)ncases);
+    if (e == cudaSuccess) {
+        if (c->pooled) {  // pageable: released without the device synchronisation of cudaFreeHost
+            c->h_stats = (fvgb_solver_stats*)std::malloc(sizeof(fvgb_solver_stats) * (size_t)ncases);
+            if (!c->h_stats) e = cudaErrorMemoryAllocation;
+        } else {
+            e = cudaMallocHost(&c->h_stats, sizeof(fvgb_solver_stats) * (size_t)ncases);
+        }
+    }
     if (e == cudaSuccess) e = settle_creation();
     if (e != cudaSuccess) {
         fvgb_solver_cache_free(c);
@@ -3106,7 +3119,7 @@ bool use_persistent(SolverCache* c, const fvgb_solver_cfg* cfg) {
     if (cfg->kernel_mode != 2 && c->n > (1 << 20)) return false;
     if (persistent_grid(c, cfg->precision == FVGB_PREC_MIXED_IR) <= 0) return false;
     if (!c->bar) {
-        if (cudaMalloc(&c->bar, sizeof(GridBar)) != cudaSuccess) {
+        if (devmem_alloc((void**)&c->bar, sizeof(GridBar), c->pooled) != cudaSuccess) {
             c->bar = nullptr;
             return false;
         }
