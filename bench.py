@@ -951,7 +951,8 @@ def run_targets(args, hm):
     """The other targets' evidence, measured in the default run: every explicit
     operator on the same 128^3 box (HBM and FP64 fractions, floor), the 512^2
     cavity's 200 PISO steps with the pressure solved in FP64 and in mixed
-    precision, and a 64-case slice of the batched workload."""
+    precision, a 64-case slice of the batched workload, and a 400-arrival slice
+    of the served stream (FP64; one at a time on its first 100 requests)."""
     import copy
 
     out = {}
@@ -960,10 +961,13 @@ def run_targets(args, hm):
     a.explicit_reps = 10
     a.cavity_steps = 200  # the configuration's 200 steps: early steps need more mixed inner iterations
     a.cases, a.batch_steps, a.alone_cases = 64, 10, 16
+    s = copy.copy(args)
+    s.requests, s.seq_requests, s.serve_fp64_only, s.serve_rate = 400, 100, True, 200.0
     for key, fn in (("advection_64x64_100_steps", lambda: run_advection(a)),
                     ("explicit_operators", lambda: run_explicit(a, hm=hm)),
                     ("cavity_512_pressure_solve", lambda: run_cavity(a, multigrid=False)),
-                    ("batch_64_case_slice", lambda: run_batch(a))):
+                    ("batch_64_case_slice", lambda: run_batch(a)),
+                    ("serving_400_arrivals_slice", lambda: run_serve(s))):
         try:
             out[key] = fn()
         except Exception as e:  # the headline line is printed whatever a side measurement does
