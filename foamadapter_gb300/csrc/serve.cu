@@ -21,7 +21,8 @@
 //
 // Time step (IMEX, as `imp::ddt(T) + exp::div(phi, T) - imp::laplacian(D, T)`):
 // explicit upwind convection of the previous field, implicit ddt + diffusion,
-// Jacobi-CG (FP64 or mixed precision) to a relative residual of 1e-8.
+// Jacobi-CG (FP64, or mixed precision with an inner reduction of 1e-4 per FP64
+// residual replacement) to a relative residual of 1e-8.
 // Boundaries: zero gradient; initial field: a Gaussian blob at the box centre.
 #include <cuda_runtime.h>
 
@@ -43,6 +44,7 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 constexpr int kChunk = 4;  // steps enqueued per request before the loop looks at it again
+constexpr double kServeInnerRelTol = 1e-4;  // mixed precision: inner residual reduction per FP64 replacement
 
 struct Slot {
     int64_t id = 0;
@@ -240,8 +242,13 @@ fvgb_status enqueue_step(Slot* s, int k) {
                           : fvgb_assemble_rhs(s->ls, terms, 3, s->dt, &bc, s->Tb, s->stream);
     if (st != FVGB_OK) return st;
     // the graph path by default: requests overlap on the device, which one
-    // cooperative (persistent) kernel per request would serialise
-    fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, 0.1, 1000, 50, r.kernel_mode == 0 ? 1 : r.kernel_mode,
+    // cooperative (persistent) kernel per request would serialise.  Mixed
+    // precision: a warm-started step needs about 7 CG iterations, so the FP64
+    // residual replacements set its cost; an inner reduction of 1e-4 needs two
+    // of them to reach 1e-8 where 0.1 needs eight (served stream of 2,000
+    // requests: 58.6 solves/s against 45.3, FP64 56.9)
+    fvgb_solver_cfg cfg{1e-8, 0.0, 2000, r.precision, kServeInnerRelTol, 1000, 50,
+                        r.kernel_mode == 0 ? 1 : r.kernel_mode,
                         FVGB_SOLVE_NO_TUNE};  // tuning would synchronise the device under every request
     st = fvgb_solve_async(s->ls, s->T, &cfg, s->stats_dev + k, s->stream);
     if (st != FVGB_OK) return st;

@@ -123,7 +123,7 @@ class ServedRequestCPU:
         old = self.T.copy()
         v, r, _, _ = o.assemble(1, [(DDT, 0, 1.0, old, None), (6, UPWIND, 1.0, old, self.F),
                                     (LAP, 0, -1.0, None, self.gamma)], self.dt, self.types, self.ref, self.Tb)
-        st = o.solve(v, r, self.T, rel_tol=1e-8, max_iter=2000, precision=self.precision, inner_rel_tol=0.1,
+        st = o.solve(v, r, self.T, rel_tol=1e-8, max_iter=2000, precision=self.precision, inner_rel_tol=1e-4,
                      inner_max_iter=1000, max_outer=50)
         if st.status != 0:
             raise RuntimeError(f"oracle solve status {st.status}")
