@@ -649,13 +649,25 @@ __global__ void __launch_bounds__(kThreads)
     for (int k = 0; k < NC; ++k) out[c * NC + k] = fadd(m, out[c * NC + k], fmul(m, s[k], sc));
 }
 
+// q_b = ref_b / delta_b of every fixed-gradient boundary face, whose boundary
+// value is then T_P + q_b.  Formed here by whole warps over the boundary faces:
+// in the gather only the one boundary lane of a cell warp needs it (a warp of
+// cells along x meets one x wall), and the FP64 division's instruction sequence
+// then ran at 1/32 lane use in half the warps, which kept the FP64 pipe busy.
+__global__ void __launch_bounds__(kThreads)
+    k_bc_gradq(MeshView m, PatchTable pt, const double* __restrict__ ref, double* __restrict__ q) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= m.nbf) return;
+    q[b] = pt.type[__ldg(&m.bpatch[b])] == FVGB_BC_FIXED_GRADIENT ? __ldg(&ref[b]) / __ldg(&m.bdelta[b]) : 0.0;
+}
+
 // The fused upwind advection step on a face-flux buffer: the divergence as in
 // k_gather_fx (coefficient 1), then the forward-Euler update and the boundary
-// correction of k_advect_euler.
+// correction of k_advect_euler (the fixed-gradient quotients from k_bc_gradq).
 __global__ void __launch_bounds__(kThreads, 6)
     k_advect_gather(MeshView m, PatchTable pt, const double* __restrict__ fx, const double* __restrict__ Told,
                     const double* __restrict__ Told_b, double dt, const double* __restrict__ ref,
-                    double* __restrict__ Tnew, double* __restrict__ Tnew_b) {
+                    const double* __restrict__ gq, double* __restrict__ Tnew, double* __restrict__ Tnew_b) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.n) return;
     Entries e;
@@ -687,7 +699,7 @@ __global__ void __launch_bounds__(kThreads, 6)
         const int t = pt.type[__ldg(&m.bpatch[b])];
         double bv = __ldg(&Told_b[b]);
         if (t == FVGB_BC_FIXED_VALUE) bv = __ldg(&ref[b]);
-        else if (t == FVGB_BC_FIXED_GRADIENT) bv = tn + __ldg(&ref[b]) / __ldg(&m.bdelta[b]);
+        else if (t == FVGB_BC_FIXED_GRADIENT) bv = tn + __ldg(&gq[b]);
         Tnew_b[b] = bv;
     }
     for (int j = kG; j < e.width; ++j) {
@@ -697,7 +709,7 @@ __global__ void __launch_bounds__(kThreads, 6)
         const int t = pt.type[__ldg(&m.bpatch[b])];
         double bv = __ldg(&Told_b[b]);
         if (t == FVGB_BC_FIXED_VALUE) bv = __ldg(&ref[b]);
-        else if (t == FVGB_BC_FIXED_GRADIENT) bv = tn + __ldg(&ref[b]) / __ldg(&m.bdelta[b]);
+        else if (t == FVGB_BC_FIXED_GRADIENT) bv = tn + __ldg(&gq[b]);
         Tnew_b[b] = bv;
     }
 }
@@ -1024,11 +1036,13 @@ extern "C" fvgb_status fvgb_advect_euler_step(const fvgb_mesh* m, const double* 
     FVGB_CHECK_ARG(bc->ref || !patch_table_needs_ref(pt), "fvgb_advect_euler_step: ref is null");
     cudaStream_t s = (cudaStream_t)stream;
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
-    double* fx = face_buffer((size_t)nf, s);
+    double* fx = face_buffer((size_t)(nf + m->v.nbf), s);  // face fluxes, then the boundary quotients
     if (fx) {
+        double* gq = fx + nf;
+        k_bc_gradq<<<grid_for(m->v.nbf, kThreads), kThreads, 0, s>>>(m->v, pt, bc->ref, gq);
         k_fx_div_upwind<1><<<grid_for(nf, kThreads * kFPT), kThreads, 0, s>>>(m->v, flux, T_old, T_old_b, fx);
         k_advect_gather<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, fx, T_old, T_old_b, dt, bc->ref,
-                                                                          T_new, T_new_b);
+                                                                          gq, T_new, T_new_b);
         FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
         cudaFreeAsync(fx, s);
         return FVGB_OK;
