@@ -266,3 +266,21 @@ def test_ilu_refuses_what_it_does_not_cover(cuda):
     import ctypes as C
     cfg = abi.SolverCfg(1e-8, 0.0, 100, abi.PREC_FP64, 0.1, 1000, 50, 0, 0, abi.SOLVER_CG, abi.PRECOND_ILU)
     assert abi.lib().fvgb_batch_solve(b.handle, abi.ptr(x), C.byref(cfg), None, None) == abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["setup_operator", "setup_stencil3D", "setup_unstructuredMesh"])
+def test_ilu_on_reference_meshes_vs_oracle(cuda, case):
+    """The reference's own test meshes (polyMesh fixtures): ILU(0) CG on a
+    heat system and ILU(0) BiCGStab on an upwind convection-diffusion system,
+    bit-exact against the oracle."""
+    from conftest import load_polymesh
+
+    hm, _ = load_polymesh(case)
+    for kind, method, om in (("heat", abi.SOLVER_CG, 0), ("convection", abi.SOLVER_BICGSTAB, 1)):
+        T, o, ls, v, r = gpu_system(hm, kind)
+        x = T.internal.clone()
+        st = ls.solve(x, rel_tol=1e-12, max_iter=500, method=method, preconditioner=abi.PRECOND_ILU)
+        xo = T.host().copy()
+        so = o.solve(v, r, xo, rel_tol=1e-12, max_iter=500, method=om, preconditioner=2)
+        same(st, so, x, xo)
