@@ -479,6 +479,11 @@ def run_explicit(args, hm=None, dm=None):
     L, h, s = abi.lib(), dm.handle, torch.cuda.current_stream().cuda_stream
     P = abi.ptr
     bc = T.bc_struct()
+    # the face-pass tile (faces per thread) by the autotuner, cached per mesh shape
+    tile, tile_ms = C.c_int32(), (C.c_float * 3)()
+    abi.check(L.fvgb_explicit_tune(h, s, C.byref(tile), tile_ms))
+    face_tile = {"chosen": tile.value, "ms_grad_plus_div_upwind_face_passes": dict(zip(("2", "4", "8"),
+                                                                                      [round(x, 5) for x in tile_ms]))}
     # FP64 operations of the reference's face loop (each face's value and flux formed
     # once, added to the owner and subtracted from the neighbour, then the 1/V scale)
     fp64 = {"interp_linear": 3 * nif, "interp_upwind": 0, "div_upwind": 3 * nif + 2 * nbf + 2 * n,
@@ -542,7 +547,7 @@ def run_explicit(args, hm=None, dm=None):
             "fp64_peak_ops_per_s": fp64_peak,
             "fp64_peak_source": "2 FP64 lanes per clock per SM (ncu peak_sustained) x SMs x max SM clock",
             "timing": "median of CUDA-event times of single launches, 512 MB written between launches",
-            "ops": res}
+            "face_tile": face_tile, "ops": res}
 
 
 def run_convection(args):

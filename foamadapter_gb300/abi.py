@@ -120,6 +120,8 @@ _SIGS = {
     "fvgb_nonorth_flux": (C.c_int, [vp, i32, vp, vp, vp, dbl, vp, vp]),
     "fvgb_advect_euler_step": (C.c_int, [vp, vp, vp, vp, dbl, C.POINTER(BC), vp, vp, vp]),
     "fvgb_advect_euler_steps": (C.c_int, [vp, vp, vp, vp, dbl, C.POINTER(BC), C.c_int32, vp, vp, vp]),
+    "fvgb_mesh_face_tile": (C.c_int, [vp, C.c_int32]),
+    "fvgb_explicit_tune": (C.c_int, [vp, vp, C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
     "fvgb_ls_create": (C.c_int, [vp, i32, C.POINTER(vp)]),
     "fvgb_ls_destroy": (C.c_int, [vp]),
     "fvgb_assemble": (C.c_int, [vp, C.POINTER(Term), i32, dbl, C.POINTER(BC), vp, vp]),

@@ -8,9 +8,13 @@
 // gather list, so every cell sees the same sequence of IEEE operations and the
 // result is bit-identical to the Serial face loop, with no atomics.  This file
 // is compiled with -fmad=false so no multiply-add is contracted.
+#include <algorithm>
 #include <atomic>
+#include <cmath>
+#include <string>
 
 #include "internal.cuh"
+#include "tunecache.h"
 
 namespace {
 
@@ -34,22 +38,40 @@ __device__ __forceinline__ bool nonneg(double F) {
 // (fadd, fsub, fmul): GB300 retires DFMA faster than DADD and DMUL.
 
 // ---------------------------------------------------------------- interpolation
-// Face kernels: a thread handles kFPT faces spaced a block apart (coalesced
+// Face kernels: a thread handles FPT faces spaced a block apart (coalesced
 // across the block) and issues the loads of all of them before the dependent
-// cell gathers, so each thread keeps several faces' bytes in flight.
-constexpr int kFPT = 4;
+// cell gathers, so each thread keeps several faces' bytes in flight.  FPT (the
+// face-pass tile: 2, 4 or 8) is the mesh's `face_tile`, 4 unless
+// fvgb_explicit_tune measured another; every face is computed alone, so every
+// tile gives the same bits.
+#define FVGB_FACE_TILE(tile, ...)          \
+    switch (tile) {                         \
+        case 2: {                           \
+            constexpr int FPT = 2;          \
+            __VA_ARGS__;                    \
+        } break;                            \
+        case 8: {                           \
+            constexpr int FPT = 8;          \
+            __VA_ARGS__;                    \
+        } break;                            \
+        default: {                          \
+            constexpr int FPT = 4;          \
+            __VA_ARGS__;                    \
+        } break;                            \
+    }
 
-__device__ __forceinline__ int face_of(int k) { return (blockIdx.x * kFPT + k) * blockDim.x + threadIdx.x; }
+template <int FPT>
+__device__ __forceinline__ int face_of(int k) { return (blockIdx.x * FPT + k) * blockDim.x + threadIdx.x; }
 
-template <int NC>
+template <int NC, int FPT>
 __global__ void __launch_bounds__(kThreads)
     k_interp_linear(MeshView m, const double* __restrict__ src, const double* __restrict__ src_b,
                     double* __restrict__ dst) {
-    int P[kFPT], N[kFPT];
-    double w[kFPT];
+    int P[FPT], N[FPT];
+    double w[FPT];
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         P[k] = N[k] = 0;
         w[k] = 0.0;
         if (f < m.nif) {
@@ -59,8 +81,8 @@ __global__ void __launch_bounds__(kThreads)
         }
     }
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         if (f < m.nif) {
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
@@ -75,14 +97,14 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-template <int NC>
+template <int NC, int FPT>
 __global__ void __launch_bounds__(kThreads)
     k_interp_upwind(MeshView m, const double* __restrict__ flux, const double* __restrict__ src,
                     const double* __restrict__ src_b, double* __restrict__ dst) {
-    int cidx[kFPT];
+    int cidx[FPT];
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         cidx[k] = 0;
         if (f < m.nif) {
             const double F = __ldg(&flux[f]);
@@ -91,8 +113,8 @@ __global__ void __launch_bounds__(kThreads)
         }
     }
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         if (f < m.nif) {
 #pragma unroll
             for (int c = 0; c < NC; ++c) dst[f * NC + c] = __ldg(&src[cidx[k] * NC + c]);
@@ -391,13 +413,14 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // --------------------------------------------------------------------- snGrad
+template <int FPT>
 __global__ void __launch_bounds__(kThreads)
     k_sngrad(MeshView m, const double* __restrict__ phi, const double* __restrict__ phi_b, double* __restrict__ out) {
-    int P[kFPT], N[kFPT];
-    double d[kFPT];
+    int P[FPT], N[FPT];
+    double d[FPT];
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         P[k] = N[k] = 0;
         d[k] = 0.0;
         if (f < m.nif) {
@@ -411,8 +434,8 @@ __global__ void __launch_bounds__(kThreads)
         }
     }
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         if (f < m.nif) out[f] = fmul(m, d[k], fsub(m, __ldg(&phi[N[k]]), __ldg(&phi[P[k]])));
         else if (f < m.nif + m.nbf) out[f] = fmul(m, d[k], fsub(m, __ldg(&phi_b[f - m.nif]), __ldg(&phi[P[k]])));
     }
@@ -426,13 +449,13 @@ __global__ void __launch_bounds__(kThreads)
 // those of the one-pass gather above, which evaluated every face from both of
 // its cells: same bits, about half the FP64 work per face.  fx holds NC values
 // per face, boundary faces after the internal ones (index nif + b = entry code).
-template <int NC>
+template <int NC, int FPT>
 __global__ void __launch_bounds__(kThreads)
     k_fx_div_linear(MeshView m, const double* __restrict__ flux, const double* __restrict__ phi,
                     const double* __restrict__ phi_b, double* __restrict__ fx) {
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         if (f < m.nif) {
             const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
             const double F = __ldg(&flux[f]), wf = __ldg(&m.w[f]);
@@ -449,13 +472,13 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-template <int NC>
+template <int NC, int FPT>
 __global__ void __launch_bounds__(kThreads)
     k_fx_div_upwind(MeshView m, const double* __restrict__ flux, const double* __restrict__ phi,
                     const double* __restrict__ phi_b, double* __restrict__ fx) {
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         if (f < m.nif) {
             const double F = __ldg(&flux[f]);
             const int cu = nonneg(F) ? __ldg(&m.own[f]) : __ldg(&m.nei[f]);
@@ -469,11 +492,12 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+template <int FPT>
 __global__ void __launch_bounds__(kThreads)
     k_fx_grad(MeshView m, const double* __restrict__ phi, const double* __restrict__ phi_b, double* __restrict__ fx) {
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         if (f < m.nif) {
             const double Tn = __ldg(&phi[__ldg(&m.nei[f])]);
             const double tf = fadd(m, fmul(m, __ldg(&m.w[f]), fsub(m, __ldg(&phi[__ldg(&m.own[f])]), Tn)), Tn);
@@ -490,13 +514,13 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-template <int NC>
+template <int NC, int FPT>
 __global__ void __launch_bounds__(kThreads)
     k_fx_lap(MeshView m, const double* __restrict__ gamma, const double* __restrict__ phi,
              const double* __restrict__ phi_b, double* __restrict__ fx) {
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         if (f < m.nif) {
             const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
             const double g = fmul(m, __ldg(&gamma[f]), __ldg(&m.geo[f]));
@@ -519,12 +543,12 @@ __global__ void __launch_bounds__(kThreads)
 // (non-coupled) patches carry no correction.  The gradient of each of the NC
 // components comes from k_fx_gradc + k_gather_fx<3*NC>: for NC = 1 the
 // operations of fvgb_grad exactly.
-template <int NC>
+template <int NC, int FPT>
 __global__ void __launch_bounds__(kThreads)
     k_fx_gradc(MeshView m, const double* __restrict__ phi, const double* __restrict__ phi_b, double* __restrict__ fx) {
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         if (f < m.nif) {
             const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
             const double wf = __ldg(&m.w[f]);
@@ -558,13 +582,13 @@ enum CorrMode { kCorrLaplacian = 0, kCorrOnly = 1, kCorrSnGrad = 2 };
 // FP64 operations per face and component where separate roundings took 20 (the
 // pass is bound by GB300's FP64 issue rate).  With k = 0 the flux is exactly the
 // uncorrected one: fma(a, b, 0) rounds a*b once, as the plain product does.
-template <int NC, int MODE>
+template <int NC, int MODE, int FPT>
 __global__ void __launch_bounds__(kThreads)
     k_fx_corr(MeshView m, const double* __restrict__ gamma, const double* __restrict__ phi,
               const double* __restrict__ phi_b, const double* __restrict__ grad, double* __restrict__ fx) {
 #pragma unroll
-    for (int k = 0; k < kFPT; ++k) {
-        const int f = face_of(k);
+    for (int k = 0; k < FPT; ++k) {
+        const int f = face_of<FPT>(k);
         if (f < m.nif) {
             const int P = __ldg(&m.own[f]), N = __ldg(&m.nei[f]);
             const double wf = __ldg(&m.w[f]);
@@ -747,12 +771,12 @@ fvgb_status gauss_grad_components(const fvgb_mesh* m, int nc, const double* psi,
     double* fx = face_buffer((size_t)(nf * nc * 3), s);
     if (!fx) return fvgb_fail(FVGB_ERR_OOM, "non-orthogonal correction: no face buffer");
     cudaMemsetAsync(grad, 0, sizeof(double) * (size_t)m->v.n * nc * 3, s);
-    const unsigned gf = grid_for(nf, kThreads * kFPT), g = grid_for(m->v.n, kThreads);
+    const unsigned g = grid_for(m->v.n, kThreads);
     if (nc == 1) {
-        k_fx_gradc<1><<<gf, kThreads, 0, s>>>(m->v, psi, psi_b, fx);
+        FVGB_FACE_TILE(m->face_tile, k_fx_gradc<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(m->v, psi, psi_b, fx))
         k_gather_fx<3><<<g, kThreads, 0, s>>>(m->v, fx, 1.0, 1, grad);
     } else {
-        k_fx_gradc<3><<<gf, kThreads, 0, s>>>(m->v, psi, psi_b, fx);
+        FVGB_FACE_TILE(m->face_tile, k_fx_gradc<3, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(m->v, psi, psi_b, fx))
         k_gather_fx<9><<<g, kThreads, 0, s>>>(m->v, fx, 1.0, 1, grad);
     }
     cudaFreeAsync(fx, s);
@@ -776,9 +800,12 @@ double* corrected_faces(const fvgb_mesh* m, int nc, const double* gamma, const d
     }
     double* fx = face_buffer((size_t)(nf * nc), s);
     if (fx) {
-        const unsigned gf = grid_for(nf, kThreads * kFPT);
-        if (nc == 1) k_fx_corr<1, MODE><<<gf, kThreads, 0, s>>>(m->v, gamma, psi, psi_b, grad, fx);
-        else k_fx_corr<3, MODE><<<gf, kThreads, 0, s>>>(m->v, gamma, psi, psi_b, grad, fx);
+        if (nc == 1)
+            FVGB_FACE_TILE(m->face_tile, k_fx_corr<1, MODE, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                             m->v, gamma, psi, psi_b, grad, fx))
+        else
+            FVGB_FACE_TILE(m->face_tile, k_fx_corr<3, MODE, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                             m->v, gamma, psi, psi_b, grad, fx))
     } else {
         fvgb_fail(FVGB_ERR_OOM, "non-orthogonal correction: no face buffer");
     }
@@ -812,9 +839,12 @@ extern "C" fvgb_status fvgb_interp_linear(const fvgb_mesh* m, int32_t nc, const 
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     if (nf == 0) return FVGB_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    const unsigned g = grid_for(nf, kThreads * kFPT);
-    if (nc == 1) k_interp_linear<1><<<g, kThreads, 0, s>>>(m->v, src, src_b, dst);
-    else k_interp_linear<3><<<g, kThreads, 0, s>>>(m->v, src, src_b, dst);
+    if (nc == 1)
+        FVGB_FACE_TILE(m->face_tile, k_interp_linear<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                         m->v, src, src_b, dst))
+    else
+        FVGB_FACE_TILE(m->face_tile, k_interp_linear<3, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                         m->v, src, src_b, dst))
     FVGB_LAUNCH_CHECK("fvgb_interp_linear");
     return FVGB_OK;
 }
@@ -827,9 +857,12 @@ extern "C" fvgb_status fvgb_interp_upwind(const fvgb_mesh* m, int32_t nc, const 
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     if (nf == 0) return FVGB_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    const unsigned g = grid_for(nf, kThreads * kFPT);
-    if (nc == 1) k_interp_upwind<1><<<g, kThreads, 0, s>>>(m->v, flux, src, src_b, dst);
-    else k_interp_upwind<3><<<g, kThreads, 0, s>>>(m->v, flux, src, src_b, dst);
+    if (nc == 1)
+        FVGB_FACE_TILE(m->face_tile, k_interp_upwind<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                         m->v, flux, src, src_b, dst))
+    else
+        FVGB_FACE_TILE(m->face_tile, k_interp_upwind<3, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                         m->v, flux, src, src_b, dst))
     FVGB_LAUNCH_CHECK("fvgb_interp_upwind");
     return FVGB_OK;
 }
@@ -848,15 +881,23 @@ extern "C" fvgb_status fvgb_div_explicit(const fvgb_mesh* m, int32_t scheme, int
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     double* fx = face_buffer((size_t)(nf * nc), s);
     if (fx) {
-        const unsigned gf = grid_for(nf, kThreads * kFPT);
+
         const bool up = scheme == FVGB_SCHEME_UPWIND;
         if (nc == 1) {
-            if (up) k_fx_div_upwind<1><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
-            else k_fx_div_linear<1><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
+            if (up)
+                FVGB_FACE_TILE(m->face_tile, k_fx_div_upwind<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                                 m->v, flux, phi, phi_b, fx))
+            else
+                FVGB_FACE_TILE(m->face_tile, k_fx_div_linear<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                                 m->v, flux, phi, phi_b, fx))
             k_gather_fx<1><<<g, kThreads, 0, s>>>(m->v, fx, coeff, unit, out);
         } else {
-            if (up) k_fx_div_upwind<3><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
-            else k_fx_div_linear<3><<<gf, kThreads, 0, s>>>(m->v, flux, phi, phi_b, fx);
+            if (up)
+                FVGB_FACE_TILE(m->face_tile, k_fx_div_upwind<3, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                                 m->v, flux, phi, phi_b, fx))
+            else
+                FVGB_FACE_TILE(m->face_tile, k_fx_div_linear<3, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                                 m->v, flux, phi, phi_b, fx))
             k_gather_fx<3><<<g, kThreads, 0, s>>>(m->v, fx, coeff, unit, out);
         }
         FVGB_LAUNCH_CHECK("fvgb_div_explicit");
@@ -883,7 +924,7 @@ extern "C" fvgb_status fvgb_grad(const fvgb_mesh* m, const double* phi, const do
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     double* fx = face_buffer((size_t)(3 * nf), s);
     if (fx) {
-        k_fx_grad<<<grid_for(nf, kThreads * kFPT), kThreads, 0, s>>>(m->v, phi, phi_b, fx);
+        FVGB_FACE_TILE(m->face_tile, k_fx_grad<FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(m->v, phi, phi_b, fx))
         k_gather_fx<3><<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, fx, coeff, coeff == 1.0, out);
         FVGB_LAUNCH_CHECK("fvgb_grad");
         cudaFreeAsync(fx, s);
@@ -905,12 +946,14 @@ extern "C" fvgb_status fvgb_laplacian_explicit(const fvgb_mesh* m, int32_t nc, c
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     double* fx = face_buffer((size_t)(nf * nc), s);
     if (fx) {
-        const unsigned gf = grid_for(nf, kThreads * kFPT);
+
         if (nc == 1) {
-            k_fx_lap<1><<<gf, kThreads, 0, s>>>(m->v, gamma, phi, phi_b, fx);
+            FVGB_FACE_TILE(m->face_tile, k_fx_lap<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                             m->v, gamma, phi, phi_b, fx))
             k_gather_fx<1><<<g, kThreads, 0, s>>>(m->v, fx, coeff, coeff == 1.0, out);
         } else {
-            k_fx_lap<3><<<gf, kThreads, 0, s>>>(m->v, gamma, phi, phi_b, fx);
+            FVGB_FACE_TILE(m->face_tile, k_fx_lap<3, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                             m->v, gamma, phi, phi_b, fx))
             k_gather_fx<3><<<g, kThreads, 0, s>>>(m->v, fx, coeff, coeff == 1.0, out);
         }
         FVGB_LAUNCH_CHECK("fvgb_laplacian_explicit");
@@ -929,7 +972,8 @@ extern "C" fvgb_status fvgb_sngrad(const fvgb_mesh* m, const double* phi, const 
     FVGB_CHECK_ARG(phi && out && (phi_b || m->v.nbf == 0), "fvgb_sngrad: null field");
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     if (nf == 0) return FVGB_OK;
-    k_sngrad<<<grid_for(nf, kThreads * kFPT), kThreads, 0, (cudaStream_t)stream>>>(m->v, phi, phi_b, out);
+    FVGB_FACE_TILE(m->face_tile, k_sngrad<FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, (cudaStream_t)stream>>>(
+                                     m->v, phi, phi_b, out))
     FVGB_LAUNCH_CHECK("fvgb_sngrad");
     return FVGB_OK;
 }
@@ -1040,7 +1084,8 @@ extern "C" fvgb_status fvgb_advect_euler_step(const fvgb_mesh* m, const double* 
     if (fx) {
         double* gq = fx + nf;
         k_bc_gradq<<<grid_for(m->v.nbf, kThreads), kThreads, 0, s>>>(m->v, pt, bc->ref, gq);
-        k_fx_div_upwind<1><<<grid_for(nf, kThreads * kFPT), kThreads, 0, s>>>(m->v, flux, T_old, T_old_b, fx);
+        FVGB_FACE_TILE(m->face_tile, k_fx_div_upwind<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                         m->v, flux, T_old, T_old_b, fx))
         k_advect_gather<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, fx, T_old, T_old_b, dt, bc->ref,
                                                                           gq, T_new, T_new_b);
         FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
@@ -1050,5 +1095,88 @@ extern "C" fvgb_status fvgb_advect_euler_step(const fvgb_mesh* m, const double* 
     k_advect_euler<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, flux, T_old, T_old_b, dt, bc->ref,
                                                                    T_new, T_new_b);
     FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
+    return FVGB_OK;
+}
+
+// ------------------------------------------------------- face-pass tile
+extern "C" fvgb_status fvgb_mesh_face_tile(fvgb_mesh* m, int32_t tile) {
+    FVGB_CHECK_ARG(m, "fvgb_mesh_face_tile: null mesh");
+    FVGB_CHECK_ARG(tile == 0 || tile == 2 || tile == 4 || tile == 8, "fvgb_mesh_face_tile: the tile is 2, 4 or 8");
+    m->face_tile = tile == 0 ? 4 : tile;
+    return FVGB_OK;
+}
+
+namespace {
+// The tuning cache's key of a mesh shape for the face passes
+std::string face_tune_key(const fvgb_mesh* m) {
+    int dev = 0, sms = 0, cmaj = 0, cmin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&cmaj, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&cmin, cudaDevAttrComputeCapabilityMinor, dev);
+    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+    const int lg = nf > 0 ? (int)std::lround(std::log2((double)nf)) : 0;
+    return "faces/sm" + std::to_string(cmaj * 10 + cmin) + "x" + std::to_string(sms) + "/faces2^" + std::to_string(lg);
+}
+constexpr int kTiles[3] = {2, 4, 8};
+}  // namespace
+
+// Times the face passes of grad and upwind div (the FP64-issue-bound and the
+// memory-latency-bound kind) with each tile on scratch fields of this mesh and
+// keeps the fastest; a tile cached for this mesh shape is taken untimed.
+// Synchronises `stream`.
+extern "C" fvgb_status fvgb_explicit_tune(fvgb_mesh* m, fvgb_stream stream, int32_t* tile_out, float* ms_out) {
+    FVGB_CHECK_ARG(m, "fvgb_explicit_tune: null mesh");
+    cudaStream_t s = (cudaStream_t)stream;
+    const std::string key = face_tune_key(m);
+    int cached = -1;
+    float ms[4] = {0, 0, 0, 0};
+    if (tune_cache_get(key, 0, &cached) && cached >= 0 && cached < 3) {
+        m->face_tile = kTiles[cached];
+    } else {
+        const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+        double *phi = nullptr, *phi_b = nullptr, *flux = nullptr, *fx = nullptr;
+        cudaError_t e = cudaMallocAsync(&phi, sizeof(double) * (size_t)std::max<int64_t>(1, m->v.n), s);
+        if (e == cudaSuccess) e = cudaMallocAsync(&phi_b, sizeof(double) * (size_t)std::max<int32_t>(1, m->v.nbf), s);
+        if (e == cudaSuccess) e = cudaMallocAsync(&flux, sizeof(double) * (size_t)std::max<int64_t>(1, nf), s);
+        if (e == cudaSuccess) e = cudaMallocAsync(&fx, sizeof(double) * 3 * (size_t)std::max<int64_t>(1, nf), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(phi, 0, sizeof(double) * (size_t)std::max<int64_t>(1, m->v.n), s);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(phi_b, 0, sizeof(double) * (size_t)std::max<int32_t>(1, m->v.nbf), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(flux, 0, sizeof(double) * (size_t)std::max<int64_t>(1, nf), s);
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (e == cudaSuccess) e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        int best = 1;
+        for (int t = 0; t < 3 && e == cudaSuccess; ++t) {
+            float times[3];
+            for (int r = 0; r < 4 && e == cudaSuccess; ++r) {  // the first run warms up
+                cudaEventRecord(e0, s);
+                FVGB_FACE_TILE(kTiles[t],
+                               k_fx_grad<FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(m->v, phi, phi_b, fx);
+                               k_fx_div_upwind<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                   m->v, flux, phi, phi_b, fx))
+                cudaEventRecord(e1, s);
+                e = cudaEventSynchronize(e1);
+                if (e == cudaSuccess && r > 0) e = cudaEventElapsedTime(&times[r - 1], e0, e1);
+            }
+            std::sort(times, times + 3);
+            ms[t] = times[1];
+        }
+        for (int t = 0; t < 3; ++t)
+            if (ms[t] < ms[best]) best = t;
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaFreeAsync(phi, s);
+        cudaFreeAsync(phi_b, s);
+        cudaFreeAsync(flux, s);
+        cudaFreeAsync(fx, s);
+        if (e != cudaSuccess) return cuda_fail(e, "fvgb_explicit_tune");
+        m->face_tile = kTiles[best];
+        tune_cache_put(key, 0, best, ms);
+    }
+    if (tile_out) *tile_out = m->face_tile;
+    if (ms_out)
+        for (int t = 0; t < 3; ++t) ms_out[t] = ms[t];
     return FVGB_OK;
 }

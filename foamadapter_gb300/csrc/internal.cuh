@@ -125,6 +125,7 @@ struct fvgb_mesh {
     std::vector<void*> allocs;
     int64_t bytes = 0;
     bool pooled = false;  // device memory from the serving pool (devmem_*)
+    int32_t face_tile = 4;  // faces per thread of the explicit face passes (2, 4, 8; same bits)
 };
 
 struct SolverCache;  // solver.cu

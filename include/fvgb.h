@@ -215,6 +215,17 @@ fvgb_status fvgb_advect_euler_steps(const fvgb_mesh* mesh, const double* flux, d
                                     double dt, const fvgb_bc* bc, int32_t nsteps, double* work,
                                     double* work_b, fvgb_stream stream);
 
+/* The face-pass tile of the explicit operators: how many faces one thread of a
+ * face pass handles (2, 4 or 8; 0 restores the default 4).  Every face is
+ * computed alone, so every tile gives the same bits. */
+fvgb_status fvgb_mesh_face_tile(fvgb_mesh* mesh, int32_t tile);
+/* The autotuner of that tile: times the grad and upwind-div face passes of this
+ * mesh with each tile on scratch fields, sets the fastest and records it in the
+ * tuning cache under the mesh's shape (face count, GPU), from which a later mesh
+ * of that shape takes it untimed.  *tile = the tile set; ms[3] (optional) = the
+ * times of tiles 2, 4, 8 (0 when taken from the cache).  Synchronises `stream`. */
+fvgb_status fvgb_explicit_tune(fvgb_mesh* mesh, fvgb_stream stream, int32_t* tile, float* ms);
+
 /* ----------------------------------------------- linear system and assembly */
 typedef struct fvgb_ls fvgb_ls;
 

@@ -123,5 +123,6 @@ def test_batch_kernel_variants_give_the_same_bits(cuda):
         for run in runs[1:]:
             np.testing.assert_array_equal(runs[0][1], run[1])
             assert runs[0][2] == run[2]
+    bad = neon.Batch(ls, ranges)  # kept alive for the call: its handle must not outlive the object
     with pytest.raises(abi.FvgbError):
-        abi.check(L.fvgb_batch_tuning(neon.Batch(ls, ranges).handle, (C.c_int32 * 4)(7, -1, -1, -1), chosen, ms))
+        abi.check(L.fvgb_batch_tuning(bad.handle, (C.c_int32 * 4)(7, -1, -1, -1), chosen, ms))

@@ -40,9 +40,12 @@ def host_bc(vf: neon.VolumeField):
 
 @pytest.mark.parametrize("name,hm", list(meshes()))
 @pytest.mark.parametrize("ncomp", [1, 3])
-def test_interpolation_div_laplacian(cuda, name, hm, ncomp):
+@pytest.mark.parametrize("tile", [2, 4, 8])
+def test_interpolation_div_laplacian(cuda, name, hm, ncomp, tile):
+    """Every face-pass tile (faces per thread) gives the oracle's bits."""
     rng = np.random.default_rng(hash(name) % 2**32 + ncomp)
     dm = DeviceMesh(hm)
+    abi.check(abi.lib().fvgb_mesh_face_tile(dm.handle, tile))
     o = Oracle(hm)
     nf = hm.nif + hm.nbf
     T = neon.VolumeField(dm, rng.standard_normal(hm.n * ncomp), rand_bcs(hm, rng, ncomp), ncomp)
@@ -75,9 +78,11 @@ def test_interpolation_div_laplacian(cuda, name, hm, ncomp):
 
 
 @pytest.mark.parametrize("name,hm", list(meshes()))
-def test_grad_sngrad(cuda, name, hm):
+@pytest.mark.parametrize("tile", [2, 4, 8])
+def test_grad_sngrad(cuda, name, hm, tile):
     rng = np.random.default_rng(3)
     dm = DeviceMesh(hm)
+    abi.check(abi.lib().fvgb_mesh_face_tile(dm.handle, tile))
     o = Oracle(hm)
     T = neon.VolumeField(dm, rng.standard_normal(hm.n), rand_bcs(hm, rng, 1))
     Th, Tb = T.host(), T.boundary.cpu().numpy()[:hm.nbf].copy()

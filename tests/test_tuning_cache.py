@@ -88,3 +88,30 @@ def test_cached_choice_is_used_without_timing(cuda, tmp_path):
     assert all(t == 0.0 for t in ms)  # nothing timed
     assert np.array_equal(x1.cpu().numpy(), x2.cpu().numpy())
     abi.check(L.fvgb_tuning_cache_clear())
+
+
+@pytest.mark.gpu
+def test_face_tile_tuned_and_cached(cuda):
+    """fvgb_explicit_tune times the face-pass tiles 2, 4, 8 on a mesh, sets the
+    fastest and records it; a second mesh of the same shape takes it untimed."""
+    import ctypes as C
+
+    from foamadapter_gb300 import mesh
+    from foamadapter_gb300.mesh import DeviceMesh
+
+    L = abi.lib()
+    abi.check(L.fvgb_tuning_cache_clear())
+    # the DeviceMesh objects are kept in names: a handle taken from a temporary
+    # would outlive its mesh (CPython frees the temporary at once)
+    dm = DeviceMesh(mesh.box(48, 40, 32, jitter=0.1, seed=2))
+    tile, ms = C.c_int32(), (C.c_float * 3)()
+    abi.check(L.fvgb_explicit_tune(dm.handle, None, C.byref(tile), ms))
+    assert tile.value in (2, 4, 8) and all(t > 0 for t in ms)
+    assert ms[(2, 4, 8).index(tile.value)] == min(ms)
+    dm2 = DeviceMesh(mesh.box(48, 40, 32, jitter=0.1, seed=3))
+    tile2, ms2 = C.c_int32(), (C.c_float * 3)()
+    abi.check(L.fvgb_explicit_tune(dm2.handle, None, C.byref(tile2), ms2))
+    assert tile2.value == tile.value and list(ms2) == [0.0, 0.0, 0.0]
+    with pytest.raises(abi.FvgbError):
+        abi.check(L.fvgb_mesh_face_tile(dm.handle, 3))
+    abi.check(L.fvgb_tuning_cache_clear())
