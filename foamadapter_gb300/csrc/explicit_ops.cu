@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(kThreads)
 __global__ void __launch_bounds__(kThreads)
     k_advect_euler(MeshView m, PatchTable pt, const double* __restrict__ flux,
                    const double* __restrict__ Told, const double* __restrict__ Told_b, double dt,
-                   const double* __restrict__ ref, double* __restrict__ Tnew,
+                   const double* __restrict__ ref, const double* __restrict__ gq, double* __restrict__ Tnew,
                    double* __restrict__ Tnew_b) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.n) return;
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(kThreads)
         const int t = pt.type[__ldg(&m.bpatch[b])];
         double v = __ldg(&Told_b[b]);
         if (t == FVGB_BC_FIXED_VALUE) v = __ldg(&ref[b]);
-        else if (t == FVGB_BC_FIXED_GRADIENT) v = tn + __ldg(&ref[b]) / __ldg(&m.bdelta[b]);
+        else if (t == FVGB_BC_FIXED_GRADIENT) v = tn + (gq ? __ldg(&gq[b]) : __ldg(&ref[b]) / __ldg(&m.bdelta[b]));
         Tnew_b[b] = v;
     }
 }
@@ -1033,6 +1033,34 @@ extern "C" fvgb_status fvgb_nonorth_flux(const fvgb_mesh* m, int32_t nc, const d
     return FVGB_OK;
 }
 
+// One forward-Euler upwind step: the face pass and the fused gather on a
+// face buffer (with the boundary quotients gq, formed here when null), or the
+// one-pass step kernel when no face buffer can be had.
+static fvgb_status advect_two_pass(const fvgb_mesh* m, const PatchTable& pt, const double* flux, const double* T_old,
+                            const double* T_old_b, double dt, const double* ref, const double* gq, double* T_new,
+                            double* T_new_b, cudaStream_t s) {
+    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
+    double* fx = face_buffer((size_t)(nf + (gq ? 0 : m->v.nbf)), s);  // face fluxes, then the quotients
+    if (fx) {
+        if (!gq) {
+            double* q = fx + nf;
+            k_bc_gradq<<<grid_for(m->v.nbf, kThreads), kThreads, 0, s>>>(m->v, pt, ref, q);
+            gq = q;
+        }
+        FVGB_FACE_TILE(m->face_tile, k_fx_div_upwind<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
+                                         m->v, flux, T_old, T_old_b, fx))
+        k_advect_gather<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, fx, T_old, T_old_b, dt, ref, gq,
+                                                                          T_new, T_new_b);
+        FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
+        cudaFreeAsync(fx, s);
+        return FVGB_OK;
+    }
+    k_advect_euler<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, flux, T_old, T_old_b, dt, ref, gq,
+                                                                   T_new, T_new_b);
+    FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
+    return FVGB_OK;
+}
+
 extern "C" fvgb_status fvgb_advect_euler_steps(const fvgb_mesh* m, const double* flux, double* T, double* T_b,
                                                double dt, const fvgb_bc* bc, int32_t nsteps, double* work,
                                                double* work_b, fvgb_stream stream) {
@@ -1044,20 +1072,30 @@ extern "C" fvgb_status fvgb_advect_euler_steps(const fvgb_mesh* m, const double*
     FVGB_CHECK_ARG(bc->ref || !patch_table_needs_ref(pt), "fvgb_advect_euler_steps: ref is null");
     if (nsteps == 0) return FVGB_OK;
     cudaStream_t s = (cudaStream_t)stream;
+    // the fixed-gradient boundary quotients ref/delta do not change between
+    // steps: formed once for the whole call
+    double* gq = nullptr;
+    if (m->v.nbf > 0 && cudaMallocAsync(&gq, sizeof(double) * (size_t)m->v.nbf, s) == cudaSuccess)
+        k_bc_gradq<<<grid_for(m->v.nbf, kThreads), kThreads, 0, s>>>(m->v, pt, bc->ref, gq);
+    else
+        cudaGetLastError();  // without the buffer each step forms its quotients itself
+    fvgb_status st = FVGB_OK;
     if (m->v.n <= kStepsMaxCells) {
         for (int k = 0; k < nsteps; ++k) {
             const bool even = (k & 1) == 0;
             k_advect_euler<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(
-                m->v, pt, flux, even ? T : work, even ? T_b : work_b, dt, bc->ref, even ? work : T, even ? work_b : T_b);
+                m->v, pt, flux, even ? T : work, even ? T_b : work_b, dt, bc->ref, gq, even ? work : T,
+                even ? work_b : T_b);
         }
     } else {
-        for (int k = 0; k < nsteps; ++k) {
+        for (int k = 0; k < nsteps && st == FVGB_OK; ++k) {
             const bool even = (k & 1) == 0;
-            const fvgb_status st = fvgb_advect_euler_step(m, flux, even ? T : work, even ? T_b : work_b, dt, bc,
-                                                          even ? work : T, even ? work_b : T_b, stream);
-            if (st != FVGB_OK) return st;
+            st = advect_two_pass(m, pt, flux, even ? T : work, even ? T_b : work_b, dt, bc->ref, gq,
+                                 even ? work : T, even ? work_b : T_b, s);
         }
     }
+    if (gq) cudaFreeAsync(gq, s);
+    if (st != FVGB_OK) return st;
     FVGB_LAUNCH_CHECK("fvgb_advect_euler_steps");
     if (nsteps & 1) {  // the last step wrote the work buffers
         FVGB_CUDA_TRY(cudaMemcpyAsync(T, work, sizeof(double) * (size_t)m->v.n, cudaMemcpyDeviceToDevice, s));
@@ -1079,23 +1117,13 @@ extern "C" fvgb_status fvgb_advect_euler_step(const fvgb_mesh* m, const double* 
     FVGB_CHECK_ARG(make_patch_table(m, bc->patch_type, &pt), "fvgb_advect_euler_step: bad patch types");
     FVGB_CHECK_ARG(bc->ref || !patch_table_needs_ref(pt), "fvgb_advect_euler_step: ref is null");
     cudaStream_t s = (cudaStream_t)stream;
-    const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
-    double* fx = face_buffer((size_t)(nf + m->v.nbf), s);  // face fluxes, then the boundary quotients
-    if (fx) {
-        double* gq = fx + nf;
-        k_bc_gradq<<<grid_for(m->v.nbf, kThreads), kThreads, 0, s>>>(m->v, pt, bc->ref, gq);
-        FVGB_FACE_TILE(m->face_tile, k_fx_div_upwind<1, FPT><<<grid_for(nf, kThreads * FPT), kThreads, 0, s>>>(
-                                         m->v, flux, T_old, T_old_b, fx))
-        k_advect_gather<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, fx, T_old, T_old_b, dt, bc->ref,
-                                                                          gq, T_new, T_new_b);
+    if (m->v.n <= kStepsMaxCells) {  // small meshes: one launch of the one-pass step kernel
+        k_advect_euler<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, flux, T_old, T_old_b, dt, bc->ref,
+                                                                       nullptr, T_new, T_new_b);
         FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
-        cudaFreeAsync(fx, s);
         return FVGB_OK;
     }
-    k_advect_euler<<<grid_for(m->v.n, kThreads), kThreads, 0, s>>>(m->v, pt, flux, T_old, T_old_b, dt, bc->ref,
-                                                                   T_new, T_new_b);
-    FVGB_LAUNCH_CHECK("fvgb_advect_euler_step");
-    return FVGB_OK;
+    return advect_two_pass(m, pt, flux, T_old, T_old_b, dt, bc->ref, nullptr, T_new, T_new_b, s);
 }
 
 // ------------------------------------------------------- face-pass tile
