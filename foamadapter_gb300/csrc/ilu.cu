@@ -35,7 +35,6 @@
 // final tree), so the oracle's restatements give the same bits.
 #include <algorithm>
 #include <cmath>
-#include <cstring>
 #include <vector>
 
 #include "internal.cuh"
@@ -625,37 +624,23 @@ fvgb_status symbolic(IluCache* c) {
     return FVGB_OK;
 }
 
-// Graph construction: kernel nodes in a chain; argument arrays must outlive
-// the graph's instantiation (held in `keep`).
+// Graph construction: kernel nodes in a chain.  The arguments are passed by
+// value; cudaGraphAddKernelNode copies the values the pointers point to.
 struct Chain {
     cudaGraph_t g;
     cudaGraphNode_t prev = nullptr;
     bool has_prev = false;
     cudaError_t e = cudaSuccess;
-    std::vector<std::vector<char>> keep;
 
     template <class... A>
     void add(void* fn, unsigned grid, A... args) {
         if (e != cudaSuccess) return;
-        // copy every argument into stable storage, then point the parameter array at the copies
-        size_t sizes[] = {sizeof(A)...};
-        size_t total = 0;
-        for (size_t s : sizes) total += (s + 15) & ~size_t(15);
-        keep.emplace_back(total);
-        char* base = keep.back().data();
-        std::vector<void*> ptrs;
-        size_t off = 0;
-        auto put = [&](const void* src, size_t sz) {
-            std::memcpy(base + off, src, sz);
-            ptrs.push_back(base + off);
-            off += (sz + 15) & ~size_t(15);
-        };
-        (put(&args, sizeof(A)), ...);
+        void* params[] = {(void*)&args...};
         cudaKernelNodeParams kp{};
         kp.func = fn;
         kp.gridDim = dim3(grid);
         kp.blockDim = dim3(fn == (void*)k_il_cond || fn == (void*)k_il_stats ? 1 : kT);
-        kp.kernelParams = ptrs.data();
+        kp.kernelParams = params;
         cudaGraphNode_t node;
         e = cudaGraphAddKernelNode(&node, g, has_prev ? &prev : nullptr, has_prev ? 1 : 0, &kp);
         if (e == cudaSuccess) {
