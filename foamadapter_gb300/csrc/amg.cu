@@ -276,6 +276,7 @@ struct AmgState {
     unsigned counter;
     int32_t want_bbase;            // FVGB_SOLVE_RHS_BASELINE: rel_tol is relative to ||b||
     double bbase;                  // ||b|| when asked for (k_bnorm), else -1
+    double vinv;                   // FP32 V-cycle: 1/sigma of the residual it was given (sigma_scale)
     fvgb_solver_stats* stats_out;  // device, or null
     fvgb_solver_stats stats;
 };
@@ -640,7 +641,8 @@ __global__ void __launch_bounds__(kT)
     out[i] = fmaT(T(kOmega) * __ldg(&dinv[i]), __ldg(&b[i]) - s, yi);
 }
 
-// out = y + w D^-1 (b - A y), stored as TO (level 0 hands z back as double)
+// out = y + w D^-1 (b - A y), stored as TO (level 0 hands z back as double;
+// from the FP32 V-cycle, times 1/sigma of the residual it was given)
 template <class R, class T, class TO>
 __global__ void __launch_bounds__(kT)
     k_post(const AmgState* st, R rows, int n, const T* __restrict__ dinv, const T* __restrict__ b,
@@ -650,7 +652,11 @@ __global__ void __launch_bounds__(kT)
     if (i >= n) return;
     T s = T(0);
     rows.each(i, [&](int j, T a) { s = fmaT(a, __ldg(&y[j]), s); });
-    out[i] = (TO)fmaT(T(kOmega) * __ldg(&dinv[i]), __ldg(&b[i]) - s, __ldg(&y[i]));
+    const T v = fmaT(T(kOmega) * __ldg(&dinv[i]), __ldg(&b[i]) - s, __ldg(&y[i]));
+    if constexpr (std::is_same<T, float>::value && std::is_same<TO, double>::value)
+        out[i] = (double)v * st->vinv;
+    else
+        out[i] = (TO)v;
 }
 
 __global__ void __launch_bounds__(kT) k_to_float(int64_t count, const double* __restrict__ src, float* __restrict__ dst) {
@@ -663,6 +669,7 @@ __global__ void k_params(AmgState* st, double* x, double rel_tol, double abs_tol
                          fvgb_solver_stats* out, int want_bbase) {
     st->want_bbase = want_bbase;
     st->bbase = -1.0;
+    st->vinv = 1.0;
     st->x = x;
     st->rel_tol = rel_tol;
     st->abs_tol = abs_tol;
@@ -672,18 +679,41 @@ __global__ void k_params(AmgState* st, double* x, double rel_tol, double abs_tol
     st->done = 0;
 }
 
+// The FP32 V-cycle runs on sigma r, sigma = 2^-ilogb(|r_prev|) (the previous
+// residual norm, known when the new residual is formed): the residual's entries
+// sit near 1 whatever the system's scale, so neither underflow nor overflow
+// FP32.  The V-cycle is linear and every FP32 operation commutes exactly with a
+// power-of-two scale in the normal range, so z = (double)z_sigma / sigma has
+// the bits of the unscaled V-cycle wherever that one stays in range.
+__device__ __forceinline__ double sigma_scale(double res) {
+    return (res > 0.0 && isfinite(res)) ? ldexp(1.0, -ilogb(res)) : 1.0;
+}
+
 // The V-cycle's first sweep from the new residual r_i: x0 = w D^-1 r in FP64,
-// or, for the FP32 V-cycle (b0f set), b0 = (float) r and x0 = w D^-1 b0 in FP32.
+// or, for the FP32 V-cycle (b0f set), b0 = (float)(sigma r) and x0 = w D^-1 b0
+// in FP32; neither when both are null (the FP32 first sweep of a solve runs
+// after its initial residual norm, k_first_f32).
 __device__ __forceinline__ void first_sweep(int i, double ri, const double* __restrict__ dinv0, double* __restrict__ x0,
                                             const float* __restrict__ d0f, float* __restrict__ b0f,
-                                            float* __restrict__ x0f) {
+                                            float* __restrict__ x0f, double sigma) {
     if (b0f) {
-        const float bf = (float)ri;
+        const float bf = (float)(ri * sigma);
         b0f[i] = bf;
         x0f[i] = float(kOmega) * __ldg(&d0f[i]) * bf;
-    } else {
+    } else if (x0) {
         x0[i] = kOmega * __ldg(&dinv0[i]) * ri;
     }
+}
+
+// The FP32 V-cycle's first sweep from the initial residual, once its norm is known
+__global__ void __launch_bounds__(kT)
+    k_first_f32(AmgState* st, int n, const double* __restrict__ r, const float* __restrict__ d0f,
+                float* __restrict__ b0f, float* __restrict__ x0f) {
+    if (done_flag(st)) return;
+    const double sigma = sigma_scale(st->res0);
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i < n) first_sweep(i, __ldg(&r[i]), nullptr, nullptr, d0f, b0f, x0f, sigma);
+    if (i == 0) st->vinv = 1.0 / sigma;
 }
 
 // ||b||, the baseline of the relative tolerance when the solve asks for it
@@ -711,7 +741,7 @@ __global__ void __launch_bounds__(kT)
         A.each(i, [&](int j, double a) { s = fma(a, x[j], s); });
         ri = __ldg(&b[i]) - s;
         r[i] = ri;
-        first_sweep(i, ri, dinv0, x0, d0f, b0f, x0f);
+        first_sweep(i, ri, dinv0, x0, d0f, b0f, x0f, 1.0);
     }
     double tot;
     if (arrive(st, part, block_sum(ri * ri, sm), sm, &tot) && threadIdx.x == 0) {
@@ -784,19 +814,21 @@ __global__ void __launch_bounds__(kT)
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
     const double alpha = st->alpha;
+    const double sigma = sigma_scale(st->res);  // the previous residual norm (rewritten by the last block below)
     double* x = st->x;
     double v = 0.0;
     if (i < n) {
         x[i] = fma(alpha, __ldg(&p[i]), x[i]);
         const double ri = fma(-alpha, __ldg(&q[i]), r[i]);
         r[i] = ri;
-        first_sweep(i, ri, dinv0, x0, d0f, b0f, x0f);
+        first_sweep(i, ri, dinv0, x0, d0f, b0f, x0f, sigma);
         v = ri * ri;
     }
     double tot;
     if (arrive(st, part, block_sum(v, sm), sm, &tot) && threadIdx.x == 0) {
         const double res = sqrt(tot);
         st->res = res;
+        st->vinv = 1.0 / sigma;
         st->iter += 1;
         if (!isfinite(res)) {
             st->status = FVGB_ERR_BREAKDOWN;
@@ -858,6 +890,7 @@ __global__ void __launch_bounds__(kT)
     __shared__ double sm[kT];
     if (done_flag(st)) return;
     const int i = blockIdx.x * kT + threadIdx.x;
+    const double sigma = sigma_scale(st->res);  // the previous residual norm (rewritten by the last block below)
     const double* x = st->x;
     double ri = 0.0;
     if (i < n) {
@@ -865,12 +898,13 @@ __global__ void __launch_bounds__(kT)
         A.each(i, [&](int j, double a) { s = fma(a, x[j], s); });
         ri = __ldg(&b[i]) - s;
         r[i] = ri;
-        first_sweep(i, ri, dinv0, x0, d0f, b0f, x0f);
+        first_sweep(i, ri, dinv0, x0, d0f, b0f, x0f, sigma);
     }
     double tot;
     if (arrive(st, part, block_sum(ri * ri, sm), sm, &tot) && threadIdx.x == 0) {
         const double res = sqrt(tot);
         st->res = res;
+        st->vinv = 1.0 / sigma;
         st->iter += 1;
         if (!isfinite(res)) {
             st->status = FVGB_ERR_BREAKDOWN;
@@ -1235,7 +1269,10 @@ fvgb_status build_graph(AmgCache* c, bool f32) {
     const float* d0f = f32 ? c->lv[0].dinvf : nullptr;
     float* b0f = f32 ? c->lv[0].bf : nullptr;
     float* x0f = f32 ? c->lv[0].xf : nullptr;
-    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &x0, &d0f, &b0f, &x0f};
+    // FP32: k_init forms no sweep (its norm is not known yet), k_first_f32 follows it
+    float* nof = nullptr;
+    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &x0, &d0f, f32 ? &nof : &b0f, &x0f};
+    void* a_f32[] = {&c->st, &n, &c->r, &d0f, &b0f, &x0f};
     void* a_first[] = {&c->st, &n, &c->r, &c->z, &c->p, &c->part};
     void* a_cond[] = {&c->st, &h};
     void* a_spmv[] = {&c->st, &A, &n, &c->p, &c->q, &c->part};
@@ -1248,6 +1285,10 @@ fvgb_status build_graph(AmgCache* c, bool f32) {
     prev = node;
     if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_init, nb, kT, a_init);
     prev = node;
+    if (e == cudaSuccess && f32) {
+        e = add_kernel(g, &node, &prev, (void*)k_first_f32, nb, kT, a_f32);
+        prev = node;
+    }
     if (e == cudaSuccess)
         e = f32 ? add_vcycle<float>(c, g, &prev, b0f, c->z, f0, true) : add_vcycle<double>(c, g, &prev, c->r, c->z, v0, true);
     if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_first_dir, nb, kT, a_first);
@@ -1309,7 +1350,9 @@ fvgb_status build_graph_mg(AmgCache* c, bool f32) {
     const float* d0f = f32 ? c->lv[0].dinvf : nullptr;
     float* b0f = f32 ? c->lv[0].bf : nullptr;
     float* x0f = f32 ? c->lv[0].xf : nullptr;
-    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &x0, &d0f, &b0f, &x0f};
+    float* nof = nullptr;
+    void* a_init[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &x0, &d0f, f32 ? &nof : &b0f, &x0f};
+    void* a_f32[] = {&c->st, &n, &c->r, &d0f, &b0f, &x0f};
     void* a_cond[] = {&c->st, &h};
     void* a_add[] = {&c->st, &n, &c->z};
     void* a_res[] = {&c->st, &A, &n, &b, &c->r, &c->part, &c->lv[0].dinv, &x0, &d0f, &b0f, &x0f};
@@ -1319,6 +1362,10 @@ fvgb_status build_graph_mg(AmgCache* c, bool f32) {
     prev = node;
     if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_init, nb, kT, a_init);
     prev = node;
+    if (e == cudaSuccess && f32) {
+        e = add_kernel(g, &node, &prev, (void*)k_first_f32, nb, kT, a_f32);
+        prev = node;
+    }
     if (e == cudaSuccess) e = add_kernel(g, &node, &prev, (void*)k_cond, 1, 1, a_cond);
     prev = node;
     cudaGraph_t body = nullptr;

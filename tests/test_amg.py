@@ -386,3 +386,29 @@ def test_multigrid_solver_cap_and_refusals(cuda):
     with pytest.raises(abi.FvgbError) as e:
         ls.solve(x, method=abi.SOLVER_MULTIGRID, precision=7)
     assert e.value.status == abi.ERR_INVALID_ARG
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver", ["cg", "multigrid"])
+def test_fp32_vcycle_is_scale_invariant(cuda, solver):
+    """The FP32 V-cycle runs on the residual times a power of two near 1/|r|.
+    A x = b and (2^-100 A) x = 2^-100 b then take the same iterations and give
+    bit-identical x: every FP64 and FP32 operation commutes with the scale while
+    the matrices stay in FP32's normal range.  Unscaled, the second system's
+    late residuals (below 1e-40) would underflow FP32."""
+    from foamadapter_gb300 import neon
+
+    s = gpu_system(cuda, (24, 20, 16))
+    torch = s["torch"]
+    scale = 2.0 ** -100
+    ls2 = neon.LinearSystem(s["dm"])
+    ls2.assemble([neon.ddt(s["old"], scale), neon.laplacian(s["gamma"], -scale)], 0.01, s["T"])
+    kw = dict(rel_tol=1e-10, max_iter=500, precision=abi.PREC_MIXED_IR)
+    kw.update(dict(preconditioner=abi.PRECOND_MULTIGRID) if solver == "cg" else dict(method=abi.SOLVER_MULTIGRID))
+    x1, x2 = s["x0"].clone(), s["x0"].clone()
+    st1 = s["ls"].solve(x1, **kw)
+    st2 = ls2.solve(x2, **kw)
+    assert st1.status == st2.status == abi.OK
+    assert st1.num_iter == st2.num_iter > 3
+    assert st2.init_res_norm == st1.init_res_norm * scale
+    assert torch.equal(x1, x2)
