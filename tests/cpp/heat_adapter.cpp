@@ -1,10 +1,11 @@
 // A FoamAdapter-style heat-transfer solver written against the C++ façade
 // (the shape of examples/heatTransfer/heatTransfer.cpp:60-83):
 //   while (runTime.loop()) { T.oldTime() = T; solve(ddt(T) - laplacian(kappa, T)); }
-// plus one explicit upwind advection step and the gradient of the result.
-// Writes T, the advected field and grad T as raw little-endian doubles to the
-// path given on the command line; tests/test_gpu_adapter.py compares them with
-// the CPU oracle.
+// with the solver options of a mapped fvSolution entry in turn (Jacobi, ILU(0),
+// BiCG, the ||b|| baseline, the multigrid solver), plus one explicit upwind
+// advection step and the gradient of the result.  Writes the fields as raw
+// little-endian doubles to the path given on the command line;
+// tests/test_gpu_adapter.py compares them with the CPU oracle.
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -46,16 +47,42 @@ int main(int argc, char** argv) {
         tbc[0] = fvgb::PatchBC::fixedValue({400.0});
         fvgb::VolumeField T(mesh, "T", std::vector<double>(n, 300.0), tbc);
         fvgb::DeviceArray<double> Told(n);
+        std::FILE* f = std::fopen(argv[1], "wb");
+        if (!f) return 4;
+        auto put = [&](const fvgb::DeviceArray<double>& arr) {
+            std::vector<double> h = arr.copyToHost();
+            std::fwrite(h.data(), sizeof(double), h.size(), f);
+        };
         fvgb::SolverConfig cfg;
         cfg.relTol = 1e-8;
-        for (int step = 0; step < 3; ++step) {
-            Told.copyFrom(T.internalVector());
-            fvgb::PDESolver eqn(fvgb::dsl::imp::ddt(Told) - fvgb::dsl::imp::laplacian(kappaf), T, 0.01);
-            fvgb::SolverStats st = eqn.solve(cfg);
-            std::printf("step %d: initial residual %.6e final %.6e iterations %d\n", step, st.initResNorm,
-                        st.finalResNorm, st.numIter);
-            if (st.status != FVGB_OK) return 3;
-        }
+        auto steps = [&](int count, const char* what) -> bool {
+            for (int step = 0; step < count; ++step) {
+                Told.copyFrom(T.internalVector());
+                fvgb::PDESolver eqn(fvgb::dsl::imp::ddt(Told) - fvgb::dsl::imp::laplacian(kappaf), T, 0.01);
+                fvgb::SolverStats st = eqn.solve(cfg);
+                std::printf("%s step %d: initial residual %.6e final %.6e iterations %d\n", what, step,
+                            st.initResNorm, st.finalResNorm, st.numIter);
+                if (st.status != FVGB_OK) return false;
+            }
+            return true;
+        };
+        // the solver options of a mapped fvSolution entry, one after another:
+        // PCG + DIC, PCG + DILU (ILU(0)), PBiCG, a ResidualNorm with the ||b||
+        // baseline; the field after each phase goes to the output
+        if (!steps(3, "CG+Jacobi")) return 3;
+        put(T.internalVector());
+        cfg.ilu = true;
+        if (!steps(2, "CG+ILU")) return 3;
+        put(T.internalVector());
+        cfg.ilu = false;
+        cfg.bicg = true;
+        if (!steps(1, "BiCG")) return 3;
+        put(T.internalVector());
+        cfg.bicg = false;
+        cfg.rhsBaseline = true;
+        cfg.relTol = 1e-6;
+        if (!steps(1, "CG, ||b|| baseline")) return 3;
+        put(T.internalVector());
         // explicit upwind advection of T with a uniform velocity (1, 0.5, 0.25)
         std::vector<double> U(3 * n), Ub(3 * nbf);
         for (int32_t c = 0; c < n; ++c) U[3 * c] = 1.0, U[3 * c + 1] = 0.5, U[3 * c + 2] = 0.25;
@@ -68,13 +95,14 @@ int main(int argc, char** argv) {
         fvgb::DeviceArray<double> gradT(3 * (size_t)n);
         fvgb::GaussGreenGrad(mesh).grad(T, 1.0, gradT);
         fvgb::check_cuda(cudaDeviceSynchronize(), "sync");
-
-        std::FILE* f = std::fopen(argv[1], "wb");
-        if (!f) return 4;
-        for (const auto* arr : {&T.internalVector(), &divT, &gradT}) {
-            std::vector<double> h = arr->copyToHost();
-            std::fwrite(h.data(), sizeof(double), h.size(), f);
-        }
+        put(divT);
+        put(gradT);
+        // GAMG (the multigrid solver) for one more step
+        cfg.rhsBaseline = false;
+        cfg.relTol = 1e-8;
+        cfg.multigridSolver = true;
+        if (!steps(1, "multigrid solver")) return 3;
+        put(T.internalVector());
         std::fclose(f);
         std::printf("ok %d cells\n", n);
     } catch (const fvgb::Error& e) {

@@ -1,6 +1,8 @@
 """The C++ façade (foamadapter_gb300/adapter/fvgb_neon.hpp) used the way a
-FoamAdapter solver would use NeoN: a compiled C++ heat-transfer program, its
-results compared bit for bit with the CPU oracle running the same steps."""
+FoamAdapter solver would use NeoN: a compiled C++ heat-transfer program that
+steps through the solver options of a mapped fvSolution entry (Jacobi, ILU(0),
+BiCG, the ||b|| baseline, the multigrid solver), its results compared with the
+CPU oracle running the same steps: bit for bit, the multigrid step to 1e-9."""
 import subprocess
 from pathlib import Path
 
@@ -39,7 +41,8 @@ def test_adapter_heat_transfer_matches_oracle(cuda, tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     hm = mesh.box(20, 16, 12, 1.0, 0.8, 0.6, jitter=0.1, seed=12345)
     data = np.fromfile(out, dtype=np.float64)
-    T_gpu, div_gpu, grad_gpu = np.split(data, [hm.n, 2 * hm.n])
+    n = hm.n
+    T1, T2, T3, T4, div_gpu, grad_gpu, T5 = np.split(data, [n, 2 * n, 3 * n, 4 * n, 5 * n, 8 * n])
     o = Oracle(hm)
     k = 1.0 + 0.5 * np.sin(0.37 * np.arange(hm.n))
     kf = o.interp_linear(1, k, np.ascontiguousarray(k[hm.bcells]))
@@ -49,15 +52,34 @@ def test_adapter_heat_transfer_matches_oracle(cuda, tmp_path):
     T = np.full(hm.n, 300.0)
     Tb = np.zeros(hm.nbf)
     o.bc_correct(1, types, ref, T, Tb)
-    for _ in range(3):
+    def step(**kw):
         v, rhs, _, _ = o.assemble(1, [(abi.TERM_DDT, 0, 1.0, T.copy(), None),
                                       (abi.TERM_LAPLACIAN, 0, -1.0, None, kf)], 0.01, types, ref, Tb)
-        st = o.solve(v, rhs, T, rel_tol=1e-8)
+        st = o.solve(v, rhs, T, **kw)
         assert st.status == 0
         o.bc_correct(1, types, ref, T, Tb)
-    np.testing.assert_array_equal(T_gpu, T)
+        return v, rhs
+
+    for _ in range(3):
+        step(rel_tol=1e-8)
+    np.testing.assert_array_equal(T1, T)                # CG + Jacobi
+    for _ in range(2):
+        step(rel_tol=1e-8, preconditioner=2)
+    np.testing.assert_array_equal(T2, T)                # CG + ILU(0)
+    step(rel_tol=1e-8, method=2)
+    np.testing.assert_array_equal(T3, T)                # BiCG
+    step(rel_tol=1e-6, flags=2)
+    np.testing.assert_array_equal(T4, T)                # ||r|| <= 1e-6 ||b||
     U = np.tile([1.0, 0.5, 0.25], hm.n)
     Ub = np.tile([1.0, 0.5, 0.25], hm.nbf)
     F = o.flux_vec(U, Ub)
     np.testing.assert_array_equal(div_gpu, o.div(abi.SCHEME_UPWIND, 1, F, T, Tb, 1.0, np.zeros(hm.n)))
     np.testing.assert_array_equal(grad_gpu, o.grad(T, Tb, 1.0, np.zeros(3 * hm.n)))
+    # the multigrid solver: against the numpy restatement, to its rounding
+    from oracle import amg as oamg
+    v, rhs, _, _ = o.assemble(1, [(abi.TERM_DDT, 0, 1.0, T.copy(), None),
+                                  (abi.TERM_LAPLACIAN, 0, -1.0, None, kf)], 0.01, types, ref, Tb)
+    ro, col = o.csr_arrays()[:2]
+    x, it, _, _, status = oamg.mg_solve(oamg.hierarchy(ro, col, v), rhs, T.copy(), 1e-8, 0.0, 1000)
+    assert status == 0 and it > 2
+    assert np.linalg.norm(T5 - x) <= 1e-9 * np.linalg.norm(x)
