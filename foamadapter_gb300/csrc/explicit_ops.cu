@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(kThreads)
     if (c >= m.n) return;
     double s[1];
     div_cell<1, FVGB_SCHEME_UPWIND>(m, c, flux, Told, Told_b, s);
-    const double dv = fadd(m, m.k_zero, fmul(m, s[0], __ldg(&m.invV[c])));
+    const double dv = facc0(true, fmul(m, s[0], __ldg(&m.invV[c])));  // +0 + s/V
     const double tn = fsub(m, __ldg(&Told[c]), fmul(m, dt, dv));
     Tnew[c] = tn;
     // boundary faces of this cell (they follow its internal faces in the list)
@@ -651,13 +651,16 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
         for (int k = 0; k < NC; ++k) v[j][k] = __ldg(&fx[f * NC + k]);
     }
+    // owner and boundary faces add, neighbour faces subtract; the sum starts
+    // from +0, so its first term is taken exactly on the integer pipes (a
+    // padded first entry holds 0 and gives +0)
     double s[NC];
 #pragma unroll
-    for (int k = 0; k < NC; ++k) s[k] = 0.0;
+    for (int k = 0; k < NC; ++k) s[k] = facc0(e.code[0] >= 0, v[0][k]);
 #pragma unroll
-    for (int j = 0; j < kG; ++j) {
+    for (int j = 1; j < kG; ++j) {
         if (e.code[j] == FVGB_PAD) break;
-        const bool plus = e.code[j] >= 0;  // owner and boundary faces add, neighbour faces subtract
+        const bool plus = e.code[j] >= 0;
 #pragma unroll
         for (int k = 0; k < NC; ++k) s[k] = facc(m, s[k], plus, v[j][k]);
     }
@@ -699,9 +702,9 @@ __global__ void __launch_bounds__(kThreads, 6)
     double v[kG];
 #pragma unroll
     for (int j = 0; j < kG; ++j) v[j] = e.code[j] == FVGB_PAD ? 0.0 : __ldg(&fx[entry_face(e.code[j])]);
-    double s = 0.0;
+    double s = facc0(e.code[0] >= 0, v[0]);  // the sum from +0: its first term exactly, on the integer pipes
 #pragma unroll
-    for (int j = 0; j < kG; ++j) {
+    for (int j = 1; j < kG; ++j) {
         if (e.code[j] == FVGB_PAD) break;
         s = facc(m, s, e.code[j] >= 0, v[j]);
     }
@@ -710,7 +713,7 @@ __global__ void __launch_bounds__(kThreads, 6)
         if (cd == FVGB_PAD) break;
         s = facc(m, s, cd >= 0, __ldg(&fx[entry_face(cd)]));
     }
-    const double dv = fadd(m, m.k_zero, fmul(m, s, __ldg(&m.invV[c])));
+    const double dv = facc0(true, fmul(m, s, __ldg(&m.invV[c])));  // +0 + s/V
     const double tn = fsub(m, __ldg(&Told[c]), fmul(m, dt, dv));
     Tnew[c] = tn;
     // boundary faces of this cell (its last entries): the entries held in
@@ -881,7 +884,6 @@ extern "C" fvgb_status fvgb_div_explicit(const fvgb_mesh* m, int32_t scheme, int
     const int64_t nf = (int64_t)m->v.nif + m->v.nbf;
     double* fx = face_buffer((size_t)(nf * nc), s);
     if (fx) {
-
         const bool up = scheme == FVGB_SCHEME_UPWIND;
         if (nc == 1) {
             if (up)

@@ -15,10 +15,10 @@ from oracle import amg as oamg
 from oracle.pyoracle import Oracle
 
 
-def heat_system(nx, ny, nz, seed=3, dt=0.01):
-    hm = mesh.box(nx, ny, nz, jitter=0.1, seed=seed)
+def heat_system(nx, ny, nz, seed=3, dt=0.01, lengths=(1.0, 1.0, 1.0), kspread=0.5):
+    hm = mesh.box(nx, ny, nz, *lengths, jitter=0.1, seed=seed)
     o = Oracle(hm)
-    k = np.exp(0.5 * np.random.default_rng(seed).standard_normal(hm.n))
+    k = np.exp(kspread * np.random.default_rng(seed).standard_normal(hm.n))
     kf = o.interp_linear(1, k, np.ascontiguousarray(k[hm.bcells]))
     types = np.asarray([abi.BC_FIXED_VALUE] + [abi.BC_FIXED_GRADIENT] * (hm.npatch - 1), np.int32)
     ref = np.zeros(hm.nbf)
@@ -268,6 +268,28 @@ def test_fp32_vcycle_in_fp64_cg(cuda, dims):
     x64b = s["x0"].clone()
     s64b = ls.solve(x64b, rel_tol=1e-11, max_iter=500, preconditioner=abi.PRECOND_MULTIGRID)
     assert s64b.num_iter == s64.num_iter and torch.equal(x64b, x64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,lengths,dt", [((40, 40, 8), (1.0, 1.0, 0.01), 1e3),
+                                             ((48, 48, 6), (1.0, 1.0, 0.001), 1e6)])
+def test_fp32_vcycle_on_stretched_cells(cuda, dims, lengths, dt):
+    """The CG keeps the fixed-preconditioner beta (r.z / r_old.z_old) with the
+    FP32 V-cycle. On cells of aspect ratio 100 and 1000, conductivities over
+    e^(+-4.5) and near-steady time steps, solved to 1e-12, it needs no more
+    iterations than with the FP64 V-cycle (a numpy emulation of both gives the
+    same counts, 90 and 176)."""
+    s = gpu_system(cuda, dims, dt=dt, lengths=lengths, kspread=1.5)
+    ls = s["ls"]
+    x64 = s["x0"].clone()
+    s64 = ls.solve(x64, rel_tol=1e-12, max_iter=1000, preconditioner=abi.PRECOND_MULTIGRID)
+    xm = s["x0"].clone()
+    sm = ls.solve(xm, rel_tol=1e-12, max_iter=1000, precision=abi.PREC_MIXED_IR,
+                  preconditioner=abi.PRECOND_MULTIGRID)
+    assert s64.status == sm.status == abi.OK
+    assert s64.num_iter > 40
+    assert sm.final_res_norm <= 1e-12 * sm.init_res_norm
+    assert sm.num_iter <= s64.num_iter + 3, (sm.num_iter, s64.num_iter)
 
 
 @pytest.mark.gpu

@@ -77,6 +77,47 @@ def test_interpolation_div_laplacian(cuda, name, hm, ncomp, tile):
         np.testing.assert_array_equal(out.cpu().numpy(), ref_out)
 
 
+def bits(a):
+    return np.ascontiguousarray(a).view(np.int64)
+
+
+@pytest.mark.parametrize("name,hm", list(meshes()))
+def test_zero_outputs_and_signed_zeros(cuda, name, hm):
+    """The gathers take the first term of a cell's sum from +0 on the integer
+    pipes (+-x, a zero result +0). Outputs of +0, of -0, and of zeros mixed
+    with values inside a warp, and fluxes with +-0 faces, all give the
+    oracle's bits with the sign of every zero (compared as integers)."""
+    rng = np.random.default_rng(17)
+    dm = DeviceMesh(hm)
+    o = Oracle(hm)
+    nf = hm.nif + hm.nbf
+    T = neon.VolumeField(dm, rng.standard_normal(hm.n), rand_bcs(hm, rng, 1))
+    types, ref, Tb = host_bc(T)
+    Th, Tb = T.host(), Tb[:hm.nbf].copy()
+    fl = rng.standard_normal(nf)
+    fl[::3] = 0.0
+    fl[1::5] = -0.0
+    flux = neon.SurfaceField(dm, fl)
+    mixed = rng.standard_normal(3 * hm.n)
+    mixed[::2] = 0.0
+    mixed[1::7] = -0.0
+    bases = {"+0": np.zeros(3 * hm.n), "-0": np.full(3 * hm.n, -0.0), "mixed": mixed}
+    gamma = neon.SurfaceField(dm, np.exp(rng.standard_normal(nf)))
+    for bname, b3 in bases.items():
+        b1 = b3[:hm.n].copy()
+        for scheme in ("linear", "upwind"):
+            out = neon.dev(b1)
+            neon.GaussGreenDiv(dm, scheme).div(out, flux, T, 1.0)
+            want = o.div(neon._scheme(scheme), 1, fl, Th, Tb, 1.0, b1.copy())
+            assert np.array_equal(bits(out.cpu().numpy()), bits(want)), (bname, scheme)
+        out = neon.dev(b1)
+        neon.GaussGreenLaplacian(dm).laplacian(out, gamma, T, 1.0)
+        want = o.laplacian(1, gamma.host(), Th, Tb, 1.0, b1.copy())
+        assert np.array_equal(bits(out.cpu().numpy()), bits(want)), bname
+        out = neon.GaussGreenGrad(dm).grad(T, 1.0, neon.dev(b3))
+        assert np.array_equal(bits(out.cpu().numpy()), bits(o.grad(Th, Tb, 1.0, b3.copy()))), bname
+
+
 @pytest.mark.parametrize("name,hm", list(meshes()))
 @pytest.mark.parametrize("tile", [2, 4, 8])
 def test_grad_sngrad(cuda, name, hm, tile):
