@@ -22,12 +22,13 @@
 //    backward z_i = (y_i - sum_j u_ij z_j) / u_ii, level by level, fma chains
 //    in column order.
 //
-// Each level is one kernel node of the solve's CUDA graph.  Rows of one level
-// are independent, so every row is computed by the same operations in the
-// same order as the sequential restatement (oracle/fvoracle.c or_ilu_*): the
-// bits are those of the exact sequential factorization and solves.  The
-// levels also bound the speed: a 128^3 box has 382 levels per triangle, a
-// kernel each per application.
+// Each factorization level is one kernel node of the solve's CUDA graph.  Each
+// triangular solve of an application is one launch: rows in level order,
+// each waiting (bounded) for the rows it depends on (the sweeps below).
+// Every row is computed by the same operations in the same order as the
+// sequential restatement (oracle/fvoracle.c or_ilu_*): the bits are those of
+// the exact sequential factorization and solves.  A 128^3 box has 382 levels
+// per triangle, which bound the sweeps' speed: one dependent row after another.
 //
 // CG and BiCGStab (right preconditioning) around it follow the Jacobi solvers'
 // stopping rules; every dot product uses the solver's reduction tree (256
@@ -53,6 +54,8 @@ struct IluState {
     double rho, rho_prev, omega;      // BiCGStab
     int32_t iter, status, done, half;
     unsigned counter;
+    unsigned ticket;      // the next chunk of a triangular sweep (0 between launches)
+    int32_t sweep_abort;  // a sweep's wait ran out: the solve ends with FVGB_ERR_CUDA
     fvgb_solver_stats* stats_out;
     fvgb_solver_stats stats;
 };
@@ -140,6 +143,8 @@ __global__ void k_il_params(IluState* st, double* x, double rel_tol, double abs_
     st->bbase = -1.0;
     st->stats_out = out;
     st->counter = 0;
+    st->ticket = 0;
+    st->sweep_abort = 0;
     st->done = 0;
     st->half = 0;
     st->iter = 0;
@@ -187,32 +192,153 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
-// y_i = r_i - sum_k l_ik y_k over one level of the lower triangle
-__global__ void __launch_bounds__(kT)
-    k_il_fwd(const IluState* st, Csr A, const int* __restrict__ rows, int cnt, const double* __restrict__ lu,
-             const double* __restrict__ r, double* y) {
-    if (done_flag(st)) return;
-    const int t = blockIdx.x * kT + threadIdx.x;
-    if (t >= cnt) return;
-    const int i = __ldg(&rows[t]);
-    const int b = __ldg(&A.ro[i]), d = b + __ldg(&A.dof[i]);
-    double s = __ldg(&r[i]);
-    for (int e = b; e < d; ++e) s = fma(-__ldg(&lu[e]), __ldcg(&y[__ldg(&A.col[e])]), s);
-    y[i] = s;
+// ------------------------------------------------------ triangular sweeps
+// One launch per triangle.  The rows are taken in level order, a chunk of kT
+// rows at a time, by a block ticket: a row depends only on rows of lower
+// levels, which sit earlier in that order, in chunks that blocks already
+// running took before (or in its own block), so every wait ends.  A row's
+// output holds kPending until the row is computed; the one 64-bit store of
+// the value is the signal (relaxed loads and stores at GPU scope, no flag and
+// no fence).  kPending is a signalling NaN: FP64 arithmetic writes quiet NaNs
+// at most, and every value a sweep writes is an arithmetic result.  The
+// forward sweep sets the backward sweep's output to kPending row by row, the
+// backward sweep the forward sweep's output after reading it; the solve graph
+// fills the latter once at its start.
+constexpr unsigned long long kPending = 0x7ff00000deadbeefull;
+constexpr int kSweepBlocksPerSM = 1;  // 128^3 ILU-CG: 368 ms at 1, 383 at 2, 422 at 4
+
+__device__ __forceinline__ bool pending(double v) { return (unsigned long long)__double_as_longlong(v) == kPending; }
+
+__device__ __forceinline__ double ld_relaxed(const double* p) {
+    double v;
+    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
 }
 
-// z_i = (y_i - sum_j u_ij z_j) / u_ii over one level of the upper triangle
+__device__ __forceinline__ void st_relaxed(double* p, double v) {
+    asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The wait for a pending row value: false when the sweep is aborted, because
+// this wait ran out (about a second, or 2^26 polls) or another one did.
+__device__ __noinline__ bool await_pending(const double* p, double& v, IluState* st) {
+    const unsigned long long t0 = now_ns();
+    for (unsigned k = 1; k < (1u << 26); ++k) {
+        if (k > 2) __nanosleep(k < 16 ? 32 : 256);  // rows far from the wavefront poll less
+        v = ld_relaxed(p);
+        if (!pending(v)) return true;
+        if ((k & 31) == 0) {
+            if (*(volatile const int32_t*)&st->sweep_abort) return false;
+            if (now_ns() - t0 > 1000000000ull) break;
+        }
+    }
+    atomicExch(&st->sweep_abort, 1);
+    return false;
+}
+
+// Row value of this sweep at p (see await_pending)
+__device__ __forceinline__ bool await_row(const double* p, double& v, IluState* st) {
+    v = ld_relaxed(p);
+    return !pending(v) || await_pending(p, v, st);
+}
+
+__global__ void __launch_bounds__(kT) k_il_pending(int n, double* y) {
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i < n) y[i] = __longlong_as_double((long long)kPending);
+}
+
+// s - sum over entries e in [e0, e1) of lu_e v_{col_e}, in entry order, the
+// values of this sweep.  The first kDeps entries' loads are issued together
+// and only the values still pending are waited for.  false when aborted.
+constexpr int kDeps = 4;
+__device__ __forceinline__ bool sweep_row(IluState* st, const Csr& A, const double* __restrict__ lu, int e0,
+                                          int e1, const double* v, double& s) {
+    int cj[kDeps];
+    double l[kDeps], x[kDeps];
+#pragma unroll
+    for (int k = 0; k < kDeps; ++k)
+        if (e0 + k < e1) {
+            cj[k] = __ldg(&A.col[e0 + k]);
+            l[k] = __ldg(&lu[e0 + k]);
+        }
+#pragma unroll
+    for (int k = 0; k < kDeps; ++k)
+        if (e0 + k < e1) x[k] = ld_relaxed(&v[cj[k]]);
+#pragma unroll
+    for (int k = 0; k < kDeps; ++k)
+        if (e0 + k < e1) {
+            double xk = x[k];
+            if (pending(xk) && !await_pending(&v[cj[k]], xk, st)) return false;
+            s = fma(-l[k], xk, s);
+        }
+    for (int e = e0 + kDeps; e < e1; ++e) {
+        double xe;
+        if (!await_row(&v[__ldg(&A.col[e])], xe, st)) return false;
+        s = fma(-__ldg(&lu[e]), xe, s);
+    }
+    return true;
+}
+
+// Chunk of this block (the same in all its threads), or >= nchunks when none is left.
+__device__ __forceinline__ unsigned next_chunk(IluState* st) {
+    __shared__ unsigned chunk;
+    __syncthreads();
+    if (threadIdx.x == 0) chunk = atomicAdd(&st->ticket, 1u);
+    __syncthreads();
+    return chunk;
+}
+
+// The last block resets the ticket and ends an aborted solve.
+__device__ __forceinline__ void end_sweep(IluState* st) {
+    if (arrive_last(&st->counter) && threadIdx.x == 0) {
+        st->ticket = 0;
+        if (st->sweep_abort) {
+            st->status = FVGB_ERR_CUDA;
+            st->done = 1;
+        }
+    }
+}
+
+// y_i = r_i - sum_k l_ik y_k, rows in the lower triangle's level order; the
+// backward sweep's output z set to kPending on the way
 __global__ void __launch_bounds__(kT)
-    k_il_bwd(const IluState* st, Csr A, const int* __restrict__ rows, int cnt, const double* __restrict__ lu,
-             const double* __restrict__ y, double* z) {
+    k_il_fwd(IluState* st, Csr A, const int* __restrict__ rows, unsigned nchunks, const double* __restrict__ lu,
+             const double* __restrict__ r, double* y, double* z) {
     if (done_flag(st)) return;
-    const int t = blockIdx.x * kT + threadIdx.x;
-    if (t >= cnt) return;
-    const int i = __ldg(&rows[t]);
-    const int d = __ldg(&A.ro[i]) + __ldg(&A.dof[i]), end = __ldg(&A.ro[i + 1]);
-    double s = __ldcg(&y[i]);
-    for (int e = d + 1; e < end; ++e) s = fma(-__ldg(&lu[e]), __ldcg(&z[__ldg(&A.col[e])]), s);
-    z[i] = s / __ldg(&lu[d]);
+    for (unsigned c = next_chunk(st); c < nchunks; c = next_chunk(st)) {
+        const int t = (int)c * kT + threadIdx.x;
+        if (t >= A.n) continue;
+        const int i = __ldg(&rows[t]);
+        z[i] = __longlong_as_double((long long)kPending);
+        const int b = __ldg(&A.ro[i]), d = b + __ldg(&A.dof[i]);
+        double s = __ldg(&r[i]);
+        if (sweep_row(st, A, lu, b, d, y, s)) st_relaxed(&y[i], s);
+    }
+    end_sweep(st);
+}
+
+// z_i = (y_i - sum_j u_ij z_j) / u_ii, rows in the upper triangle's level
+// order; y_i set back to kPending once read
+__global__ void __launch_bounds__(kT)
+    k_il_bwd(IluState* st, Csr A, const int* __restrict__ rows, unsigned nchunks, const double* __restrict__ lu,
+             double* y, double* z) {
+    if (done_flag(st)) return;
+    for (unsigned c = next_chunk(st); c < nchunks; c = next_chunk(st)) {
+        const int t = (int)c * kT + threadIdx.x;
+        if (t >= A.n) continue;
+        const int i = __ldg(&rows[t]);
+        const int d = __ldg(&A.ro[i]) + __ldg(&A.dof[i]), end = __ldg(&A.ro[i + 1]);
+        double s = __ldcg(&y[i]);
+        y[i] = __longlong_as_double((long long)kPending);
+        if (sweep_row(st, A, lu, d + 1, end, z, s)) st_relaxed(&z[i], s / __ldg(&lu[d]));
+    }
+    end_sweep(st);
 }
 
 // The tolerance and the first stopping test from the initial residual norm
@@ -526,6 +652,7 @@ __global__ void k_il_stats(IluState* st) {
 struct IluCache {
     const fvgb_ls* ls = nullptr;
     int n = 0, nnz = 0, R = 4, nb = 1;
+    unsigned sweep_grid = 1;  // resident blocks of a triangular sweep
     int *ro = nullptr, *col = nullptr, *dof = nullptr;
     int *op_ptr = nullptr, *op_f = nullptr, *op_g = nullptr;
     int *fwd_rows = nullptr, *bwd_rows = nullptr;
@@ -602,6 +729,17 @@ fvgb_status symbolic(IluCache* c) {
     c->nnz = nnz;
     c->R = n >= (1 << 15) ? 8 : 4;
     c->nb = std::max(1, (n + kT * c->R - 1) / (kT * c->R));
+    {
+        // the sweep's blocks stay resident (a persistent grid taking chunks);
+        // one per SM keeps the rows at the wavefront busy, and more rows in
+        // flight only add polls of rows far behind it
+        int dev = 0, sms = 1, per = 1;
+        FVGB_CUDA_TRY(cudaGetDevice(&dev));
+        FVGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        FVGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_il_fwd, kT, 0));
+        const long chunks = (n + kT - 1) / kT;
+        c->sweep_grid = (unsigned)std::max(1L, std::min(chunks, (long)sms * std::min(per, kSweepBlocksPerSM)));
+    }
     cudaError_t e = il_upload(c, &c->ro, ro);
     if (e == cudaSuccess) e = il_upload(c, &c->col, col);
     if (e == cudaSuccess) e = il_upload(c, &c->dof, dof);
@@ -652,21 +790,13 @@ struct Chain {
 
 unsigned grid_of(int count) { return count > 0 ? (unsigned)((count + kT - 1) / kT) : 1u; }
 
-// z = U^-1 L^-1 src through c->w, one node per level
+// z = U^-1 L^-1 src through c->w: a forward and a backward sweep
 void add_apply(IluCache* c, Chain& ch, const double* src, double* dst) {
     const Csr A{c->n, c->ro, c->col, c->dof};
-    const IluState* st = c->st;
+    const unsigned nchunks = (unsigned)((c->n + kT - 1) / kT);
     const double* lu = c->lu;
-    for (size_t l = 0; l + 1 < c->fwd_ptr.size(); ++l) {
-        const int cnt = c->fwd_ptr[l + 1] - c->fwd_ptr[l];
-        const int* rows = c->fwd_rows + c->fwd_ptr[l];
-        ch.add((void*)k_il_fwd, grid_of(cnt), st, A, rows, cnt, lu, src, c->w);
-    }
-    for (size_t l = 0; l + 1 < c->bwd_ptr.size(); ++l) {
-        const int cnt = c->bwd_ptr[l + 1] - c->bwd_ptr[l];
-        const int* rows = c->bwd_rows + c->bwd_ptr[l];
-        ch.add((void*)k_il_bwd, grid_of(cnt), st, A, rows, cnt, lu, (const double*)c->w, dst);
-    }
+    ch.add((void*)k_il_fwd, c->sweep_grid, c->st, A, (const int*)c->fwd_rows, nchunks, lu, src, c->w, dst);
+    ch.add((void*)k_il_bwd, c->sweep_grid, c->st, A, (const int*)c->bwd_rows, nchunks, lu, c->w, dst);
 }
 
 fvgb_status build_graph(IluCache* c, bool bicgstab) {
@@ -685,6 +815,7 @@ fvgb_status build_graph(IluCache* c, bool bicgstab) {
     cudaGraphConditionalHandle h{};
     ch.e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
     ch.add((void*)k_il_bnorm, nb, st, n, R, b, c->pa);
+    ch.add((void*)k_il_pending, ng, n, c->w);  // the forward sweeps' output, pending
     ch.add((void*)k_il_gather, grid_of(c->nnz), c->nnz, (const int*)ls->mesh->csr_pos, (const double*)ls->values,
            c->a, c->lu);
     for (size_t l = 0; l + 1 < c->fwd_ptr.size(); ++l) {

@@ -213,6 +213,24 @@ def test_ilu_bicgstab_vs_oracle(cuda, dims):
 
 
 @pytest.mark.gpu
+def test_ilu_repeated_solves_are_identical(cuda):
+    """The triangular sweeps leave their work vectors pending for the next
+    application, and each solve starts from a filled one: CG, BiCGStab, CG
+    again and BiCGStab again on one system give the same bits each time."""
+    hm = mesh.box(34, 32, 31, jitter=0.1, seed=8)
+    T, o, ls, v, r = gpu_system(hm)
+    runs = []
+    for method in (abi.SOLVER_CG, abi.SOLVER_BICGSTAB, abi.SOLVER_CG, abi.SOLVER_BICGSTAB, abi.SOLVER_CG):
+        x = T.internal.clone()
+        st = ls.solve(x, rel_tol=1e-10, max_iter=2000, method=method, preconditioner=abi.PRECOND_ILU)
+        assert st.status == abi.OK
+        runs.append((method, st.num_iter, st.final_res_norm, x.cpu().numpy()))
+    for a, b in ((0, 2), (2, 4), (1, 3)):
+        assert runs[a][:3] == runs[b][:3]
+        np.testing.assert_array_equal(runs[a][3], runs[b][3])
+
+
+@pytest.mark.gpu
 def test_ilu_with_fill_updates_vs_oracle(cuda):
     """A mesh whose matrix graph has triangles: the factorization's update
     list changes off-diagonal entries; CG and BiCGStab stay bit-exact."""
