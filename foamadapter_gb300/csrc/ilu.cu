@@ -19,8 +19,8 @@
 //    list.  On hex meshes (no three cells pairwise adjacent) only the diagonal
 //    changes: OpenFOAM's DILU;
 //  * application z = U^-1 L^-1 r: forward y_i = r_i - sum_k l_ik y_k, then
-//    backward z_i = (y_i - sum_j u_ij z_j) / u_ii, level by level, fma chains
-//    in column order.
+//    backward z_i = (y_i - sum_j u_ij z_j) / u_ii, each a single sweep over
+//    the rows in level order, fma chains in column order.
 //
 // Each factorization level is one kernel node of the solve's CUDA graph.  Each
 // triangular solve of an application is one launch: rows in level order,

@@ -342,8 +342,9 @@ typedef struct fvgb_solver_cfg {
                                   the FP64 CG) or FVGB_PRECOND_ILU (Ginkgo Ilu with a
                                   ParIlu factorization, OpenFOAM's DILU,
                                   fvSolution.cpp:56-63: the exact ILU(0) factors,
-                                  formed level by level in every solve, and level-
-                                  scheduled triangular solves; CG or BiCGStab, FP64,
+                                  formed level by level in every solve, and
+                                  triangular solves of one launch each, rows in
+                                  level order; CG or BiCGStab, FP64,
                                   single systems, fvgb_solve / fvgb_solve_async)       */
 } fvgb_solver_cfg;
 enum { FVGB_SOLVE_NO_TUNE = 1, FVGB_SOLVE_RHS_BASELINE = 2 };

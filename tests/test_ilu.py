@@ -3,7 +3,8 @@ maps it, Ginkgo preconditioner::Ilu with a factorization::ParIlu
 (src/compatibility/fvSolution.cpp:56-63).
 
 The library forms the exact ILU(0) factors (the fixed point of ParIlu's
-sweeps) level by level and applies them by level-scheduled triangular solves;
+sweeps) level by level and applies them by triangular sweeps over the rows in
+level order (one launch each, bounded waits for the rows a row depends on);
 CG and BiCGStab around them use the solver's reduction tree.  The oracle
 (oracle/fvoracle.c or_ilu_factor, or_ilu_apply, solve_cg_ilu, solve_bicgstab)
 restates the sequential factorization and solves, so the GPU must match it
