@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kT)
 // backward sweep the forward sweep's output after reading it; the solve graph
 // fills the latter once at its start.
 constexpr unsigned long long kPending = 0x7ff00000deadbeefull;
-constexpr int kSweepBlocksPerSM = 1;  // 128^3 ILU-CG: 368 ms at 1, 383 at 2, 422 at 4
+constexpr int kSweepBlocksPerSM = 1;  // 128^3 ILU-CG: 144 ms at 1, 157 at 2
 
 __device__ __forceinline__ bool pending(double v) { return (unsigned long long)__double_as_longlong(v) == kPending; }
 
@@ -253,36 +253,61 @@ __global__ void __launch_bounds__(kT) k_il_pending(int n, double* y) {
     if (i < n) y[i] = __longlong_as_double((long long)kPending);
 }
 
-// s - sum over entries e in [e0, e1) of lu_e v_{col_e}, in entry order, the
-// values of this sweep.  The first kDeps entries' loads are issued together
-// and only the values still pending are waited for.  false when aborted.
+// out = (s - sum over entries e in [e0, e1) of lu_e v_{col_e}) [/ piv], the
+// sum in entry order over values of this sweep.  The first kDeps values are
+// polled together, and a row stores its value from inside the polling loop as
+// soon as its own values are there: a lane that had left its wait would
+// otherwise hold its store at the warp's reconvergence point until the slowest
+// lane of the warp (a row one level up, or one whose values come from a
+// farther SM) arrived, and every level would wait for the slowest warp lane.
+// Entries past the first kDeps (none on hex meshes) are waited for one by
+// one.  Gives up, raising the abort flag, after about a second (or 2^26
+// polls), or when another wait of the sweep did.
 constexpr int kDeps = 4;
-__device__ __forceinline__ bool sweep_row(IluState* st, const Csr& A, const double* __restrict__ lu, int e0,
-                                          int e1, const double* v, double& s) {
+template <bool DIV>
+__device__ __forceinline__ void sweep_store(IluState* st, const Csr& A, const double* __restrict__ lu, int e0,
+                                            int e1, const double* v, double s, double piv, double* out) {
     int cj[kDeps];
     double l[kDeps], x[kDeps];
 #pragma unroll
-    for (int k = 0; k < kDeps; ++k)
+    for (int k = 0; k < kDeps; ++k) {
+        x[k] = 0.0;  // not pending
         if (e0 + k < e1) {
             cj[k] = __ldg(&A.col[e0 + k]);
             l[k] = __ldg(&lu[e0 + k]);
         }
+    }
 #pragma unroll
     for (int k = 0; k < kDeps; ++k)
         if (e0 + k < e1) x[k] = ld_relaxed(&v[cj[k]]);
+    unsigned long long t0 = 0;
+    for (unsigned it = 0; it < (1u << 26); ++it) {
+        bool ready = true;
 #pragma unroll
-    for (int k = 0; k < kDeps; ++k)
-        if (e0 + k < e1) {
-            double xk = x[k];
-            if (pending(xk) && !await_pending(&v[cj[k]], xk, st)) return false;
-            s = fma(-l[k], xk, s);
+        for (int k = 0; k < kDeps; ++k) ready = ready && !pending(x[k]);
+        if (ready) {
+#pragma unroll
+            for (int k = 0; k < kDeps; ++k)
+                if (e0 + k < e1) s = fma(-l[k], x[k], s);
+            for (int e = e0 + kDeps; e < e1; ++e) {
+                double xe;
+                if (!await_row(&v[__ldg(&A.col[e])], xe, st)) return;
+                s = fma(-__ldg(&lu[e]), xe, s);
+            }
+            st_relaxed(out, DIV ? s / piv : s);
+            return;
         }
-    for (int e = e0 + kDeps; e < e1; ++e) {
-        double xe;
-        if (!await_row(&v[__ldg(&A.col[e])], xe, st)) return false;
-        s = fma(-__ldg(&lu[e]), xe, s);
+        if (it == 0) t0 = now_ns();
+        if (it > 2) __nanosleep(it < 16 ? 32 : 256);
+#pragma unroll
+        for (int k = 0; k < kDeps; ++k)
+            if (pending(x[k])) x[k] = ld_relaxed(&v[cj[k]]);
+        if ((it & 31) == 31) {
+            if (*(volatile const int32_t*)&st->sweep_abort) return;
+            if (now_ns() - t0 > 1000000000ull) break;
+        }
     }
-    return true;
+    atomicExch(&st->sweep_abort, 1);
 }
 
 // Chunk of this block (the same in all its threads), or >= nchunks when none is left.
@@ -318,7 +343,7 @@ __global__ void __launch_bounds__(kT)
         z[i] = __longlong_as_double((long long)kPending);
         const int b = __ldg(&A.ro[i]), d = b + __ldg(&A.dof[i]);
         double s = __ldg(&r[i]);
-        if (sweep_row(st, A, lu, b, d, y, s)) st_relaxed(&y[i], s);
+        sweep_store<false>(st, A, lu, b, d, y, s, 1.0, &y[i]);
     }
     end_sweep(st);
 }
@@ -336,7 +361,7 @@ __global__ void __launch_bounds__(kT)
         const int d = __ldg(&A.ro[i]) + __ldg(&A.dof[i]), end = __ldg(&A.ro[i + 1]);
         double s = __ldcg(&y[i]);
         y[i] = __longlong_as_double((long long)kPending);
-        if (sweep_row(st, A, lu, d + 1, end, z, s)) st_relaxed(&z[i], s / __ldg(&lu[d]));
+        sweep_store<true>(st, A, lu, d + 1, end, z, s, __ldg(&lu[d]), &z[i]);
     }
     end_sweep(st);
 }
