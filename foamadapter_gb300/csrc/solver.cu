@@ -46,7 +46,6 @@ namespace {
 
 constexpr int kT = 256;
 constexpr int kRowsPerThread = 8;  // the most rows per thread of any case
-constexpr int kRowsPerBlock = kT * kRowsPerThread;
 
 // Rows per thread of a case's reduction tree: 8 (2048-row blocks, half the
 // block reductions) for cases of at least kBigCaseRows rows; 4 for smaller
