@@ -40,19 +40,77 @@ struct JsonParser {
         i += n;
         return true;
     }
+    // four hex digits at s[at..at+4)
+    bool hex4(size_t at, unsigned& u) const {
+        if (at + 4 > s.size()) return false;
+        u = 0;
+        for (size_t k = at; k < at + 4; ++k) {
+            const char c = s[k];
+            const unsigned d = c >= '0' && c <= '9' ? (unsigned)(c - '0')
+                               : c >= 'a' && c <= 'f' ? (unsigned)(c - 'a' + 10)
+                               : c >= 'A' && c <= 'F' ? (unsigned)(c - 'A' + 10)
+                                                      : 16u;
+            if (d > 15) return false;
+            u = u * 16 + d;
+        }
+        return true;
+    }
+    static void utf8(unsigned cp, std::string& out) {
+        if (cp < 0x80) {
+            out.push_back((char)cp);
+        } else if (cp < 0x800) {
+            out.push_back((char)(0xC0 | (cp >> 6)));
+            out.push_back((char)(0x80 | (cp & 0x3F)));
+        } else if (cp < 0x10000) {
+            out.push_back((char)(0xE0 | (cp >> 12)));
+            out.push_back((char)(0x80 | ((cp >> 6) & 0x3F)));
+            out.push_back((char)(0x80 | (cp & 0x3F)));
+        } else {
+            out.push_back((char)(0xF0 | (cp >> 18)));
+            out.push_back((char)(0x80 | ((cp >> 12) & 0x3F)));
+            out.push_back((char)(0x80 | ((cp >> 6) & 0x3F)));
+            out.push_back((char)(0x80 | (cp & 0x3F)));
+        }
+    }
+    // a JSON string with its escapes (\" \\ \/ \b \f \n \r \t \uXXXX, surrogate
+    // pairs joined), as UTF-8
     bool string(std::string& out) {
         if (i >= s.size() || s[i] != '"') return false;
         ++i;
         out.clear();
         while (i < s.size() && s[i] != '"') {
-            if (s[i] == '\\' && i + 1 < s.size()) {
-                ++i;
-                const char e = s[i];
-                out.push_back(e == 'n' ? '\n' : e == 't' ? '\t' : e);
-            } else {
-                out.push_back(s[i]);
+            if (s[i] != '\\') {
+                out.push_back(s[i++]);
+                continue;
             }
-            ++i;
+            if (++i >= s.size()) return false;
+            const char e = s[i++];
+            switch (e) {
+                case '"': case '\\': case '/': out.push_back(e); break;
+                case 'b': out.push_back('\b'); break;
+                case 'f': out.push_back('\f'); break;
+                case 'n': out.push_back('\n'); break;
+                case 'r': out.push_back('\r'); break;
+                case 't': out.push_back('\t'); break;
+                case 'u': {
+                    unsigned cp;
+                    if (!hex4(i, cp)) return false;
+                    i += 4;
+                    if (cp >= 0xD800 && cp < 0xDC00) {  // high surrogate: a low one must follow
+                        unsigned lo;
+                        if (i + 6 > s.size() || s[i] != '\\' || s[i + 1] != 'u' || !hex4(i + 2, lo) || lo < 0xDC00 ||
+                            lo >= 0xE000)
+                            return false;
+                        i += 6;
+                        cp = 0x10000 + ((cp - 0xD800) << 10) + (lo - 0xDC00);
+                    } else if (cp >= 0xDC00 && cp < 0xE000) {
+                        return false;
+                    }
+                    utf8(cp, out);
+                    break;
+                }
+                default: return false;
+            }
         }
         if (i >= s.size()) return false;
         ++i;

@@ -73,6 +73,11 @@ bool load_locked(const char* path, std::string* err) {
             *err = "entry without key or four variants";
             return false;
         }
+        for (char ch : k->str)
+            if ((unsigned char)ch < 0x20) {
+                *err = "key with a control character";
+                return false;
+            }
         Entry en;
         for (int q = 0; q < kTuneCacheKinds; ++q) {
             const fvgb_json::Json& x = vs->arr[q];
@@ -94,12 +99,23 @@ bool load_locked(const char* path, std::string* err) {
     return true;
 }
 
+// a key as a JSON string body: quotes and backslashes escaped (keys hold no
+// control characters: the library makes none and a load refuses them)
+std::string json_escaped(const std::string& k) {
+    std::string o;
+    for (char ch : k) {
+        if (ch == '"' || ch == '\\') o.push_back('\\');
+        o.push_back(ch);
+    }
+    return o;
+}
+
 bool save_locked(const char* path) {
     std::ostringstream o;
     o << "{\"version\": 1, \"entries\": [";
     bool first = true;
     for (const auto& kv : g_entries) {
-        o << (first ? "\n" : ",\n") << "  {\"key\": \"" << kv.first << "\", \"variants\": [";
+        o << (first ? "\n" : ",\n") << "  {\"key\": \"" << json_escaped(kv.first) << "\", \"variants\": [";
         for (int q = 0; q < kTuneCacheKinds; ++q) o << (q ? ", " : "") << kv.second.variant[q];
         o << "], \"ms\": [";
         for (int q = 0; q < kTuneCacheKinds; ++q) {

@@ -44,6 +44,29 @@ def test_cache_file_round_trip(tmp_path):
     assert L.fvgb_tuning_cache_size() == 0
 
 
+def test_cache_keys_with_quotes_round_trip(tmp_path):
+    """Keys are written as JSON strings (quotes and backslashes escaped), so a
+    saved file is valid JSON and loads back to the same keys; a key with a
+    control character is refused."""
+    L = abi.lib()
+    abi.check(L.fvgb_tuning_cache_clear())
+    f, g = tmp_path / "in.json", tmp_path / "out.json"
+    key = 'sm103 "GB300" \\ path / café \U0001f680'  # json.dumps writes \u escapes and a surrogate pair
+    f.write_text(json.dumps({"version": 1, "entries": [entry(key, [1, 2, -1, 0])]}))
+    abi.check(L.fvgb_tuning_cache_load(str(f).encode()))
+    abi.check(L.fvgb_tuning_cache_save(str(g).encode()))
+    d = json.loads(g.read_text())
+    assert [e["key"] for e in d["entries"]] == [key]
+    abi.check(L.fvgb_tuning_cache_clear())
+    abi.check(L.fvgb_tuning_cache_load(str(g).encode()))
+    abi.check(L.fvgb_tuning_cache_save(str(f).encode()))
+    assert json.loads(f.read_text()) == d
+    f.write_text(json.dumps({"version": 1, "entries": [entry("a\u0001b", [0, 0, 0, 0])]}))
+    with pytest.raises(abi.FvgbError):
+        abi.check(L.fvgb_tuning_cache_load(str(f).encode()))
+    abi.check(L.fvgb_tuning_cache_clear())
+
+
 @pytest.mark.gpu
 def test_cached_choice_is_used_without_timing(cuda, tmp_path):
     """A system of 2^18 rows is timed at its first solve and its choice cached;
